@@ -1,0 +1,927 @@
+// C ABI of libsculptgpu (include/sculpt_gpu.h): mesh upload and device mirror
+// of the PBVH, the per-call entry points that replace the reference's
+// BKE_pbvh_* / do_*_brush calls, and whole strokes (eager or CUDA graph).
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/sculpt_gpu.h"
+#include "sgpu_device.cuh"
+#include "sgpu_host.h"
+#include "sgpu_kernels.h"
+
+using namespace sgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation)
+    return fail(SGPU_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+  return fail(SGPU_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                              \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return cuda_fail(_e, what); \
+  } while (0)
+
+}  // namespace
+
+struct sgpu_mesh {
+  HostMesh host;
+  DevMesh dev{};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<void*> allocs;
+  int* d_nodes_tmp = nullptr;
+  bool has_mask = false;
+  // stroke graph cache
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned char> gkey;
+  int g_nodes = 0;
+  int g_launches = 0;
+
+  template <class T>
+  int alloc(T** out, size_t count) {
+    void* p = nullptr;
+    const size_t bytes = (count > 0 ? count : 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    allocs.push_back(p);
+    e = cudaMemsetAsync(p, 0, bytes, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    *out = static_cast<T*>(p);
+    return SGPU_OK;
+  }
+  template <class T>
+  int upload(const T** out, const std::vector<T>& v) {
+    T* p = nullptr;
+    int rc = alloc(&p, v.size());
+    if (rc) return rc;
+    if (!v.empty()) {
+      cudaError_t e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                      stream);
+      if (e != cudaSuccess) return cuda_fail(e, "upload");
+    }
+    *out = p;
+    return SGPU_OK;
+  }
+  template <class T>
+  int upload_mut(T** out, const std::vector<T>& v) {
+    const T* p = nullptr;
+    int rc = upload(&p, v);
+    *out = const_cast<T*>(p);
+    return rc;
+  }
+  void release() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+  }
+};
+
+namespace {
+
+bool g_configured = false;
+
+int ensure_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(SGPU_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
+  if (!g_configured) {
+    configure_kernels();
+    g_configured = true;
+  }
+  return SGPU_OK;
+}
+
+// Mirrors the host PBVH and work areas to the device.
+int upload_pbvh(sgpu_mesh* m) {
+  HostMesh& h = m->host;
+  DevMesh& d = m->dev;
+  const int N = h.totnode, L = static_cast<int>(h.leaf_nodes.size());
+  d.totnode = N;
+  d.nleaf = L;
+  d.nlevels = static_cast<int>(h.level_off.size()) - 1;
+  std::vector<float4> vb(2 * static_cast<size_t>(N));
+  for (int n = 0; n < N; n++) {
+    const float* b = &h.vb[6 * static_cast<size_t>(n)];
+    vb[2 * n] = make_float4(b[0], b[1], b[2], 0.0f);
+    vb[2 * n + 1] = make_float4(b[3], b[4], b[5], 0.0f);
+  }
+  int rc;
+  if ((rc = m->upload_mut(&d.vb, vb))) return rc;
+  if ((rc = m->upload_mut(&d.orig_vb, vb))) return rc;
+  if ((rc = m->upload(&d.node_child, h.children))) return rc;
+  if ((rc = m->upload(&d.node_parent, h.parent))) return rc;
+  if ((rc = m->upload(&d.node_leaf, h.node_leaf))) return rc;
+  if ((rc = m->upload(&d.leaf_node, h.leaf_nodes))) return rc;
+  std::vector<int> vert_off(L + 1, 0), uniq(L, 0), verts, prim_off(L + 1, 0), prims, lflag(L);
+  for (int k = 0; k < L; k++) {
+    const int node = h.leaf_nodes[k];
+    lflag[k] = h.flag[node];
+    prim_off[k + 1] = prim_off[k] + h.totprim[node];
+    for (int i = 0; i < h.totprim[node]; i++) prims.push_back(h.prim_indices[h.prim_off[node] + i]);
+    if (h.type == kFaces) {
+      const int tot = h.uniq[node] + h.face_verts_n[node];
+      uniq[k] = h.uniq[node];
+      vert_off[k + 1] = vert_off[k] + tot;
+      for (int i = 0; i < tot; i++) verts.push_back(h.vert_indices[h.vert_off[node] + i]);
+    }
+  }
+  if ((rc = m->upload(&d.leaf_vert_off, vert_off))) return rc;
+  if ((rc = m->upload(&d.leaf_uniq, uniq))) return rc;
+  if ((rc = m->upload(&d.leaf_verts, verts))) return rc;
+  if ((rc = m->upload(&d.leaf_prim_off, prim_off))) return rc;
+  if ((rc = m->upload(&d.leaf_prims, prims))) return rc;
+  if ((rc = m->upload_mut(&d.leaf_flag, lflag))) return rc;
+  if ((rc = m->upload(&d.level_off, h.level_off))) return rc;
+  if ((rc = m->upload(&d.level_nodes, h.level_nodes))) return rc;
+  if ((rc = m->alloc(&d.work, 1))) return rc;
+  if ((rc = m->alloc(&d.cull_list, L + 1))) return rc;
+  if ((rc = m->alloc(&d.cull_off, L + 2))) return rc;
+  if ((rc = m->alloc(&d.parts, L + 1))) return rc;
+  if ((rc = m->alloc(&d.scratch, static_cast<size_t>(h.totvert)))) return rc;
+  if ((rc = m->alloc(&d.node_upd, N))) return rc;
+  if ((rc = m->alloc(&m->d_nodes_tmp, L + 1))) return rc;
+  if (N > cull_smem_limit())
+    return fail(SGPU_ERR_UNSUPPORTED, "PBVH has %d nodes; the node search holds at most %d", N,
+                cull_smem_limit());
+  return SGPU_OK;
+}
+
+int create_common(sgpu_mesh* m) {
+  CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  CK(cudaEventCreate(&m->ev0), "cudaEventCreate");
+  CK(cudaEventCreate(&m->ev1), "cudaEventCreate");
+  return SGPU_OK;
+}
+
+int check_mesh(const sgpu_mesh* m) {
+  if (!m) return fail(SGPU_ERR_INVALID_ARG, "mesh handle is NULL");
+  return SGPU_OK;
+}
+
+int device_err(sgpu_mesh* m) {
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, &m->dev.work->err, sizeof(int), cudaMemcpyDeviceToHost, m->stream),
+     "read error word");
+  CK(cudaStreamSynchronize(m->stream), "cudaStreamSynchronize");
+  if (err) {
+    const int zero = 0;
+    cudaMemcpy(&m->dev.work->err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    return fail(err, "a kernel reported error code %d (invalid node list or bounds)", err);
+  }
+  return SGPU_OK;
+}
+
+bool make_brush(const SGPU_Brush* b, int tool, DevBrush* out) {
+  std::memset(out, 0, sizeof(*out));
+  Curve c;
+  if (!build_curve(b->curve_preset, &c)) return false;
+  out->tool = tool;
+  out->flag = b->flag;
+  out->radius = b->radius;
+  out->strength = b->strength;
+  out->normal_radius_factor = b->normal_radius_factor;
+  out->area_radius_factor = b->area_radius_factor;
+  out->plane_offset = b->plane_offset;
+  out->x_first = c.x_first;
+  out->x_last = c.x_last;
+  out->mintable = c.mintable;
+  out->range = c.range;
+  std::memcpy(out->y, c.y, sizeof(out->y));
+  return true;
+}
+
+bool tool_ok(int tool) {
+  return tool == kToolDraw || tool == kToolSmooth || tool == kToolInflate ||
+         tool == kToolClayStrips;
+}
+
+// Launches the brush of one pass over the current device node list.
+int launch_tool(sgpu_mesh* m, const DevBrush& b, PassParams pp, int* launches) {
+  const DevMesh& d = m->dev;
+  cudaStream_t s = m->stream;
+  if (b.tool == kToolDraw || b.tool == kToolClayStrips) {
+    CK(launch_area(d, b, pp, s), "area kernel");
+    CK(launch_brush(d, b, pp, s), "brush kernel");
+    *launches += 2;
+  } else if (b.tool == kToolInflate) {
+    CK(launch_brush(d, b, pp, s), "brush kernel");
+    *launches += 1;
+  } else {
+    // Smooth: 4 sub-steps per unit strength, the last one fractional.
+    float st = b.strength;
+    if (st < 0.0f) st = 0.0f;
+    if (st > 1.0f) st = 1.0f;
+    const int count = (int)(st * 4.0f);
+    const float last = 4.0f * (st - (float)count * 0.25f);
+    for (int it = 0; it <= count; it++) {
+      pp.iter_strength = (it != count) ? 1.0f : last;
+      pp.iteration = it;
+      CK(launch_smooth_iteration(d, b, pp, s), "smooth kernels");
+      *launches += 2;
+    }
+  }
+  return SGPU_OK;
+}
+
+int launch_update_normals(sgpu_mesh* m, int bounds_flag, int* launches) {
+  if (m->dev.type == kFaces) {
+    CK(launch_update_faces(m->dev, 1, bounds_flag, m->stream), "update kernel");
+    *launches += 1;
+  } else {
+    CK(launch_update_grids(m->dev, m->stream, launches), "grid update kernels");
+    if (bounds_flag) {
+      CK(launch_update_faces(m->dev, 0, bounds_flag, m->stream), "bounds kernel");
+      *launches += 1;
+    }
+  }
+  return SGPU_OK;
+}
+
+// Enqueues a whole stroke on the mesh stream.
+int enqueue_stroke(sgpu_mesh* m, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+                   const int* dab_tools, int* launches) {
+  DevBrush base;
+  if (!make_brush(brush, brush->sculpt_tool, &base))
+    return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brush->curve_preset);
+  CK(cudaMemsetAsync(&m->dev.work->displaced, 0, sizeof(unsigned long long), m->stream),
+     "reset counter");
+  for (int d = 0; d < ndabs; d++) {
+    const int tool = dab_tools ? dab_tools[d] : brush->sculpt_tool;
+    base.tool = tool;
+    const float scale = (tool == kToolClayStrips) ? 1.41421356237309504880f : 1.0f;
+    const float r = brush->radius * scale;
+    for (int pass = 0; pass < 8; pass++) {
+      if ((pass & ~brush->symmetry) != 0) continue;
+      PassParams pp{};
+      for (int k = 0; k < 3; k++) {
+        const float sgn = (pass & (1 << k)) ? -1.0f : 1.0f;
+        pp.loc[k] = sgn * dabs[d].location[k];
+        pp.delta[k] = sgn * dabs[d].grab_delta[k];
+        pp.view[k] = sgn * brush->view_normal[k];
+      }
+      pp.cull_radius_sq = r * r;
+      pp.original = brush->use_original_bb;
+      pp.iter_strength = 1.0f;
+      CK(launch_cull(m->dev, pp, m->stream), "cull kernel");
+      *launches += 1;
+      int rc = launch_tool(m, base, pp, launches);
+      if (rc) return rc;
+    }
+    int rc = launch_update_normals(m, kUpdateBB, launches);
+    if (rc) return rc;
+  }
+  CK(launch_update_faces(m->dev, 0, kUpdateOriginalBB, m->stream), "bounds kernel");
+  *launches += 1;
+  return SGPU_OK;
+}
+
+int upload_node_list(sgpu_mesh* m, const int* nodes, int totnode) {
+  if (totnode < 0 || totnode > m->dev.nleaf)
+    return fail(SGPU_ERR_INVALID_ARG, "node count %d out of range", totnode);
+  // Each leaf at most once: a repeated leaf would move its vertices twice and
+  // overrun the per-pass scratch sized to one entry per vertex.
+  std::vector<unsigned char> seen(m->dev.totnode, 0);
+  for (int k = 0; k < totnode; k++) {
+    if (nodes[k] < 0 || nodes[k] >= m->dev.totnode || m->host.node_leaf[nodes[k]] < 0)
+      return fail(SGPU_ERR_INVALID_ARG, "node %d is not a leaf of this PBVH", nodes[k]);
+    if (seen[nodes[k]]++)
+      return fail(SGPU_ERR_INVALID_ARG, "node %d appears twice in the node list", nodes[k]);
+  }
+  if (totnode > 0)
+    CK(cudaMemcpyAsync(m->d_nodes_tmp, nodes, sizeof(int) * totnode, cudaMemcpyHostToDevice,
+                       m->stream),
+       "upload node list");
+  CK(launch_set_list(m->dev, m->d_nodes_tmp, totnode, m->stream), "node list kernel");
+  CK(cudaStreamSynchronize(m->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int do_brush_tool(sgpu_mesh* m, const SGPU_Brush* brush, int tool, const float location[3],
+                  const float grab_delta[3], const int* nodes, int totnode) {
+  int rc = check_mesh(m);
+  if (rc) return rc;
+  if (!brush || !location || !grab_delta) return fail(SGPU_ERR_INVALID_ARG, "NULL argument");
+  if (!tool_ok(tool)) return fail(SGPU_ERR_INVALID_ARG, "unsupported sculpt tool %d", tool);
+  if (!(brush->radius > 0.0f)) return fail(SGPU_ERR_INVALID_ARG, "radius must be positive");
+  if (nodes && (rc = upload_node_list(m, nodes, totnode))) return rc;
+  DevBrush b;
+  if (!make_brush(brush, tool, &b))
+    return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brush->curve_preset);
+  PassParams pp{};
+  for (int k = 0; k < 3; k++) {
+    pp.loc[k] = location[k];
+    pp.delta[k] = grab_delta[k];
+    pp.view[k] = brush->view_normal[k];
+  }
+  pp.iter_strength = 1.0f;
+  int launches = 0;
+  rc = launch_tool(m, b, pp, &launches);
+  if (rc) return rc;
+  return device_err(m);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sgpu_version(void) { return "libsculptgpu 0.1 (sm_103a)"; }
+
+const char* sgpu_last_error(void) { return g_err.c_str(); }
+
+int sgpu_device_info(int* sm_count, int* cc_major, int* cc_minor) {
+  int rc = ensure_device();
+  if (rc) return rc;
+  int dev = 0;
+  CK(cudaGetDevice(&dev), "cudaGetDevice");
+  if (sm_count) CK(cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev), "attr");
+  if (cc_major) CK(cudaDeviceGetAttribute(cc_major, cudaDevAttrComputeCapabilityMajor, dev), "attr");
+  if (cc_minor) CK(cudaDeviceGetAttribute(cc_minor, cudaDevAttrComputeCapabilityMinor, dev), "attr");
+  return SGPU_OK;
+}
+
+int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPoly* polys,
+                           int totpoly, const SGPU_MLoop* loops, int totloop,
+                           const SGPU_MLoopTri* looptris, int totlooptri,
+                           const float* vert_normals, const float* mask, const float* automask,
+                           int leaf_limit, sgpu_mesh** r_mesh) {
+  if (!r_mesh) return fail(SGPU_ERR_INVALID_ARG, "r_mesh is NULL");
+  *r_mesh = nullptr;
+  if (!verts || !polys || !loops || !looptris || totvert <= 0 || totpoly <= 0 || totloop <= 0 ||
+      totlooptri <= 0)
+    return fail(SGPU_ERR_INVALID_ARG, "empty or NULL mesh arrays");
+  int rc = ensure_device();
+  if (rc) return rc;
+  sgpu_mesh* m = new (std::nothrow) sgpu_mesh();
+  if (!m) return fail(SGPU_ERR_OOM, "host allocation failed");
+  HostMesh& h = m->host;
+  h.type = kFaces;
+  h.totvert = totvert;
+  h.totpoly = totpoly;
+  h.totloop = totloop;
+  h.totlt = totlooptri;
+  h.leaf_limit = leaf_limit > 0 ? leaf_limit : 10000;
+  h.poly_loopstart.resize(totpoly);
+  h.poly_totloop.resize(totpoly);
+  h.poly_mat.resize(totpoly);
+  h.poly_flag.resize(totpoly);
+  for (int p = 0; p < totpoly; p++) {
+    h.poly_loopstart[p] = polys[p].loopstart;
+    h.poly_totloop[p] = polys[p].totloop;
+    h.poly_mat[p] = polys[p].mat_nr;
+    h.poly_flag[p] = polys[p].flag;
+  }
+  h.loop_v.resize(totloop);
+  for (int l = 0; l < totloop; l++) h.loop_v[l] = static_cast<int>(loops[l].v);
+  h.lt_v.resize(3 * static_cast<size_t>(totlooptri));
+  h.lt_poly.resize(totlooptri);
+  for (int t = 0; t < totlooptri; t++) {
+    for (int j = 0; j < 3; j++) {
+      const unsigned int l = looptris[t].tri[j];
+      if (l >= static_cast<unsigned int>(totloop)) {
+        delete m;
+        return fail(SGPU_ERR_INVALID_ARG, "looptri %d loop index out of range", t);
+      }
+      h.lt_v[3 * t + j] = h.loop_v[l];
+    }
+    h.lt_poly[t] = static_cast<int>(looptris[t].poly);
+  }
+  h.co.resize(3 * static_cast<size_t>(totvert));
+  for (int v = 0; v < totvert; v++)
+    for (int k = 0; k < 3; k++) h.co[3 * static_cast<size_t>(v) + k] = verts[v].co[k];
+  std::string err;
+  if (!build_faces(h, &err)) {
+    delete m;
+    return fail(SGPU_ERR_INVALID_ARG, "%s", err.c_str());
+  }
+  DevMesh& d = m->dev;
+  d.type = kFaces;
+  d.totvert = totvert;
+  d.totlt = totlooptri;
+  auto bail = [&](int code) {
+    m->release();
+    delete m;
+    return code;
+  };
+  if ((rc = create_common(m))) return bail(rc);
+  if ((rc = m->alloc(&d.co, totvert))) return bail(rc);
+  if ((rc = m->alloc(&d.no, totvert))) return bail(rc);
+  static_assert(sizeof(SGPU_MVert) == sizeof(float4), "MVert is 16 bytes");
+  CK(cudaMemcpyAsync(d.co, verts, sizeof(float4) * totvert, cudaMemcpyHostToDevice, m->stream),
+     "upload verts");
+  if (vert_normals) {
+    CK(cudaMemcpy2DAsync(d.no, sizeof(float4), vert_normals, 3 * sizeof(float), 3 * sizeof(float),
+                         totvert, cudaMemcpyHostToDevice, m->stream),
+       "upload normals");
+  }
+  if (mask) {
+    float* dm = nullptr;
+    if ((rc = m->alloc(&dm, totvert))) return bail(rc);
+    CK(cudaMemcpyAsync(dm, mask, sizeof(float) * totvert, cudaMemcpyHostToDevice, m->stream),
+       "upload mask");
+    d.mask = dm;
+    m->has_mask = true;
+  }
+  if (automask) {
+    float* da = nullptr;
+    if ((rc = m->alloc(&da, totvert))) return bail(rc);
+    CK(cudaMemcpyAsync(da, automask, sizeof(float) * totvert, cudaMemcpyHostToDevice, m->stream),
+       "upload automask");
+    d.automask = da;
+  }
+  std::vector<int4> lt(totlooptri);
+  for (int t = 0; t < totlooptri; t++)
+    lt[t] = make_int4(h.lt_v[3 * t], h.lt_v[3 * t + 1], h.lt_v[3 * t + 2], h.lt_poly[t]);
+  std::vector<int2> pl(totpoly);
+  for (int p = 0; p < totpoly; p++) pl[p] = make_int2(h.poly_loopstart[p], h.poly_totloop[p]);
+  if ((rc = m->upload(&d.lt, lt))) return bail(rc);
+  if ((rc = m->upload(&d.poly, pl))) return bail(rc);
+  if ((rc = m->upload(&d.loop_v, h.loop_v))) return bail(rc);
+  if ((rc = m->upload(&d.vt_off, h.vt_off))) return bail(rc);
+  if ((rc = m->upload(&d.vt_idx, h.vt_idx))) return bail(rc);
+  if ((rc = m->upload(&d.nb_off, h.nb_off))) return bail(rc);
+  if ((rc = m->upload(&d.nb_idx, h.nb_idx))) return bail(rc);
+  if ((rc = m->upload(&d.lt_leaf, h.lt_leaf))) return bail(rc);
+  if ((rc = m->alloc(&d.vtag, totvert))) return bail(rc);
+  if ((rc = upload_pbvh(m))) return bail(rc);
+  if (!vert_normals) {
+    // Every vertex tagged and every leaf flagged, then one normal update.
+    CK(cudaMemsetAsync(d.vtag, 1, totvert, m->stream), "tag all");
+    std::vector<int> lflag(d.nleaf);
+    for (int k = 0; k < d.nleaf; k++) lflag[k] = h.flag[h.leaf_nodes[k]] | kUpdateNormals;
+    CK(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf, cudaMemcpyHostToDevice,
+                       m->stream),
+       "flag all");
+    CK(launch_update_faces(d, 1, 0, m->stream), "normal kernel");
+  }
+  CK(cudaStreamSynchronize(m->stream), "cudaStreamSynchronize");
+  h.co.clear();
+  h.co.shrink_to_fit();
+  *r_mesh = m;
+  return SGPU_OK;
+}
+
+int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
+                           const float* grids_no, const float* grids_mask, int num_faces,
+                           const int* face_start, const int* face_ngrids, const int* face_verts,
+                           const int* face_edges, int num_base_verts, int num_base_edges,
+                           const int* edge_verts, int leaf_limit, sgpu_mesh** r_mesh) {
+  if (!r_mesh) return fail(SGPU_ERR_INVALID_ARG, "r_mesh is NULL");
+  *r_mesh = nullptr;
+  if (num_grids <= 0 || grid_size < 2 || !grids_co || num_faces <= 0 || !face_start ||
+      !face_ngrids || !face_verts || !face_edges || !edge_verts || num_base_verts <= 0 ||
+      num_base_edges <= 0)
+    return fail(SGPU_ERR_INVALID_ARG, "empty or NULL grid arrays");
+  const long long elems = static_cast<long long>(num_grids) * grid_size * grid_size;
+  if (elems > 0x7fffffffLL) return fail(SGPU_ERR_UNSUPPORTED, "more than 2^31 grid elements");
+  int rc = ensure_device();
+  if (rc) return rc;
+  sgpu_mesh* m = new (std::nothrow) sgpu_mesh();
+  if (!m) return fail(SGPU_ERR_OOM, "host allocation failed");
+  HostMesh& h = m->host;
+  h.type = kGrids;
+  h.num_grids = num_grids;
+  h.grid_size = grid_size;
+  h.grid_area = grid_size * grid_size;
+  h.totvert = static_cast<int>(elems);
+  h.num_faces = num_faces;
+  h.num_base_verts = num_base_verts;
+  h.num_base_edges = num_base_edges;
+  h.face_start.assign(face_start, face_start + num_faces);
+  h.face_ngrids.assign(face_ngrids, face_ngrids + num_faces);
+  int corners = 0;
+  for (int f = 0; f < num_faces; f++) corners += face_ngrids[f] > 0 ? face_ngrids[f] : 0;
+  h.face_verts.assign(face_verts, face_verts + corners);
+  h.face_edges.assign(face_edges, face_edges + corners);
+  h.edge_elems.assign(edge_verts, edge_verts + 2 * static_cast<size_t>(num_base_edges));
+  for (int e = 0; e < 2 * num_base_edges; e++)
+    if (edge_verts[e] < 0 || edge_verts[e] >= num_base_verts) {
+      delete m;
+      return fail(SGPU_ERR_INVALID_ARG, "edge vertex out of range");
+    }
+  h.leaf_limit = leaf_limit > 0 ? leaf_limit
+                                : (10000 / h.grid_area > 1 ? 10000 / h.grid_area : 1);
+  h.co.assign(grids_co, grids_co + 3 * static_cast<size_t>(elems));
+  std::string err;
+  if (!build_grids(h, &err)) {
+    delete m;
+    return fail(SGPU_ERR_INVALID_ARG, "%s", err.c_str());
+  }
+  DevMesh& d = m->dev;
+  d.type = kGrids;
+  d.totvert = static_cast<int>(elems);
+  d.grid_size = grid_size;
+  d.grid_area = h.grid_area;
+  d.num_faces = num_faces;
+  d.num_base_verts = num_base_verts;
+  d.num_base_edges = num_base_edges;
+  auto bail = [&](int code) {
+    m->release();
+    delete m;
+    return code;
+  };
+  if ((rc = create_common(m))) return bail(rc);
+  if ((rc = m->alloc(&d.co, elems))) return bail(rc);
+  if ((rc = m->alloc(&d.no, elems))) return bail(rc);
+  CK(cudaMemcpy2DAsync(d.co, sizeof(float4), grids_co, 3 * sizeof(float), 3 * sizeof(float), elems,
+                       cudaMemcpyHostToDevice, m->stream),
+     "upload grid positions");
+  if (grids_no)
+    CK(cudaMemcpy2DAsync(d.no, sizeof(float4), grids_no, 3 * sizeof(float), 3 * sizeof(float),
+                         elems, cudaMemcpyHostToDevice, m->stream),
+       "upload grid normals");
+  if (grids_mask) {
+    float* dm = nullptr;
+    if ((rc = m->alloc(&dm, elems))) return bail(rc);
+    CK(cudaMemcpyAsync(dm, grids_mask, sizeof(float) * elems, cudaMemcpyHostToDevice, m->stream),
+       "upload grid mask");
+    d.mask = dm;
+    m->has_mask = true;
+  }
+  if ((rc = m->upload(&d.grid_face, h.grid_face))) return bail(rc);
+  if ((rc = m->upload(&d.face_start, h.face_start))) return bail(rc);
+  if ((rc = m->upload(&d.face_ngrids, h.face_ngrids))) return bail(rc);
+  if ((rc = m->upload(&d.face_verts, h.face_verts))) return bail(rc);
+  if ((rc = m->upload(&d.face_edges, h.face_edges))) return bail(rc);
+  if ((rc = m->upload(&d.edge_off, h.edge_off))) return bail(rc);
+  if ((rc = m->upload(&d.edge_elems, h.edge_elems))) return bail(rc);
+  if ((rc = m->upload(&d.bvert_off, h.bvert_off))) return bail(rc);
+  if ((rc = m->upload(&d.bvert_elems, h.bvert_elems))) return bail(rc);
+  if ((rc = m->alloc(&d.face_list, num_faces))) return bail(rc);
+  if ((rc = m->alloc(&d.edge_list, num_base_edges))) return bail(rc);
+  if ((rc = m->alloc(&d.bvert_list, num_base_verts))) return bail(rc);
+  if ((rc = m->alloc(&d.face_mark, num_faces))) return bail(rc);
+  if ((rc = m->alloc(&d.edge_mark, num_base_edges))) return bail(rc);
+  if ((rc = m->alloc(&d.bvert_mark, num_base_verts))) return bail(rc);
+  if ((rc = m->alloc(&d.grid_counts, 4))) return bail(rc);
+  if ((rc = upload_pbvh(m))) return bail(rc);
+  if (!grids_no) {
+    std::vector<int> lflag(d.nleaf);
+    for (int k = 0; k < d.nleaf; k++) lflag[k] = h.flag[h.leaf_nodes[k]] | kUpdateNormals;
+    CK(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf, cudaMemcpyHostToDevice,
+                       m->stream),
+       "flag all");
+    int launches = 0;
+    CK(launch_update_grids(d, m->stream, &launches), "grid normal kernels");
+  }
+  CK(cudaStreamSynchronize(m->stream), "cudaStreamSynchronize");
+  h.co.clear();
+  h.co.shrink_to_fit();
+  *r_mesh = m;
+  return SGPU_OK;
+}
+
+int sgpu_mesh_destroy(sgpu_mesh* mesh) {
+  if (!mesh) return fail(SGPU_ERR_INVALID_ARG, "mesh handle is NULL");
+  mesh->release();
+  delete mesh;
+  return SGPU_OK;
+}
+
+int sgpu_mesh_info(const sgpu_mesh* mesh, SGPU_MeshInfo* r_info) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!r_info) return fail(SGPU_ERR_INVALID_ARG, "r_info is NULL");
+  const HostMesh& h = mesh->host;
+  r_info->type = h.type;
+  r_info->totvert = h.totvert;
+  r_info->totnode = h.totnode;
+  r_info->totleaf = static_cast<int>(h.leaf_nodes.size());
+  r_info->leaf_limit = h.leaf_limit;
+  r_info->totprim = static_cast<int>(h.prim_indices.size());
+  r_info->leaf_vert_entries = static_cast<int>(h.vert_indices.size());
+  r_info->grid_size = h.grid_size;
+  return SGPU_OK;
+}
+
+int sgpu_mesh_sync(sgpu_mesh* mesh) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+void* sgpu_mesh_stream(sgpu_mesh* mesh) { return mesh ? static_cast<void*>(mesh->stream) : nullptr; }
+
+int sgpu_search_sphere(sgpu_mesh* mesh, const float center[3], float radius_sq, int original,
+                       int* r_nodes, int* r_tot) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!center) return fail(SGPU_ERR_INVALID_ARG, "center is NULL");
+  PassParams pp{};
+  for (int k = 0; k < 3; k++) pp.loc[k] = center[k];
+  pp.cull_radius_sq = radius_sq;
+  pp.original = original;
+  CK(launch_cull(mesh->dev, pp, mesh->stream), "cull kernel");
+  if (r_nodes || r_tot) {
+    int cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, &mesh->dev.work->cull_count, sizeof(int), cudaMemcpyDeviceToHost,
+                       mesh->stream),
+       "read count");
+    CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+    if (r_nodes && cnt > 0) {
+      std::vector<int> ids(cnt);
+      CK(cudaMemcpy(ids.data(), mesh->dev.cull_list, sizeof(int) * cnt, cudaMemcpyDeviceToHost),
+         "read list");
+      for (int k = 0; k < cnt; k++) r_nodes[k] = mesh->host.leaf_nodes[ids[k]];
+    }
+    if (r_tot) *r_tot = cnt;
+  }
+  return SGPU_OK;
+}
+
+int sgpu_do_draw_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                       const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolDraw, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_smooth_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                         const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolSmooth, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_inflate_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                          const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolInflate, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_clay_strips_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                              const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolClayStrips, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                  const float grab_delta[3], const int* nodes, int totnode) {
+  if (!brush) return fail(SGPU_ERR_INVALID_ARG, "brush is NULL");
+  return do_brush_tool(mesh, brush, brush->sculpt_tool, location, grab_delta, nodes, totnode);
+}
+
+int sgpu_pbvh_update_normals(sgpu_mesh* mesh) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  int launches = 0;
+  if ((rc = launch_update_normals(mesh, 0, &launches))) return rc;
+  return device_err(mesh);
+}
+
+int sgpu_pbvh_update_bounds(sgpu_mesh* mesh, int flag) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  CK(launch_update_faces(mesh->dev, 0, flag, mesh->stream), "bounds kernel");
+  return device_err(mesh);
+}
+
+int sgpu_pbvh_node_mark_update(sgpu_mesh* mesh, int node) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (node < 0 || node >= mesh->dev.totnode || mesh->host.node_leaf[node] < 0)
+    return fail(SGPU_ERR_INVALID_ARG, "node %d is not a leaf", node);
+  CK(launch_mark_node(mesh->dev, node, mesh->stream), "mark kernel");
+  return SGPU_OK;
+}
+
+int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+                const int* dab_tools, int mode, SGPU_StrokeStats* stats) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!brush || (!dabs && ndabs > 0) || ndabs < 0)
+    return fail(SGPU_ERR_INVALID_ARG, "NULL brush or dabs");
+  if (!(brush->radius > 0.0f)) return fail(SGPU_ERR_INVALID_ARG, "radius must be positive");
+  for (int d = 0; d < ndabs; d++) {
+    const int tool = dab_tools ? dab_tools[d] : brush->sculpt_tool;
+    if (!tool_ok(tool)) return fail(SGPU_ERR_INVALID_ARG, "unsupported sculpt tool %d", tool);
+  }
+  if (brush->symmetry < 0 || brush->symmetry > 7)
+    return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
+  int launches = 0;
+  CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
+  if (mode == SGPU_STROKE_GRAPH) {
+    // Key: everything the captured launches depend on.
+    std::vector<unsigned char> key(sizeof(SGPU_Brush) + sizeof(SGPU_Dab) * ndabs +
+                                   sizeof(int) * (dab_tools ? ndabs : 0) + sizeof(int));
+    unsigned char* p = key.data();
+    std::memcpy(p, brush, sizeof(SGPU_Brush));
+    p += sizeof(SGPU_Brush);
+    if (ndabs) std::memcpy(p, dabs, sizeof(SGPU_Dab) * ndabs);
+    p += sizeof(SGPU_Dab) * ndabs;
+    if (dab_tools) std::memcpy(p, dab_tools, sizeof(int) * ndabs);
+    p += sizeof(int) * (dab_tools ? ndabs : 0);
+    const int nd = ndabs;
+    std::memcpy(p, &nd, sizeof(int));
+    if (!mesh->gexec || key != mesh->gkey) {
+      if (mesh->gexec) cudaGraphExecDestroy(mesh->gexec);
+      mesh->gexec = nullptr;
+      cudaGraph_t graph = nullptr;
+      CK(cudaStreamBeginCapture(mesh->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      rc = enqueue_stroke(mesh, brush, dabs, ndabs, dab_tools, &launches);
+      cudaError_t ce = cudaStreamEndCapture(mesh->stream, &graph);
+      if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (ce != cudaSuccess) return cuda_fail(ce, "end capture");
+      size_t nn = 0;
+      cudaGraphGetNodes(graph, nullptr, &nn);
+      ce = cudaGraphInstantiate(&mesh->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) return cuda_fail(ce, "graph instantiate");
+      mesh->gkey = key;
+      mesh->g_nodes = static_cast<int>(nn);
+      mesh->g_launches = launches;
+      CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
+    }
+    launches = mesh->g_launches;
+    CK(cudaGraphLaunch(mesh->gexec, mesh->stream), "graph launch");
+  } else {
+    rc = enqueue_stroke(mesh, brush, dabs, ndabs, dab_tools, &launches);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(mesh->ev1, mesh->stream), "event");
+  unsigned long long displaced = 0;
+  CK(cudaMemcpyAsync(&displaced, &mesh->dev.work->displaced, sizeof(displaced),
+                     cudaMemcpyDeviceToHost, mesh->stream),
+     "read counter");
+  if ((rc = device_err(mesh))) return rc;
+  if (stats) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, mesh->ev0, mesh->ev1), "elapsed");
+    stats->verts_displaced = static_cast<int64_t>(displaced);
+    stats->gpu_ms = ms;
+    stats->kernel_launches = launches;
+    stats->graph_nodes = mode == SGPU_STROKE_GRAPH ? mesh->g_nodes : 0;
+  }
+  return SGPU_OK;
+}
+
+int sgpu_get_verts(sgpu_mesh* mesh, SGPU_MVert* out) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (mesh->dev.type != kFaces) return fail(SGPU_ERR_INVALID_ARG, "not a FACES mesh");
+  CK(cudaMemcpyAsync(out, mesh->dev.co, sizeof(float4) * mesh->dev.totvert, cudaMemcpyDeviceToHost,
+                     mesh->stream),
+     "download verts");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_set_verts(sgpu_mesh* mesh, const SGPU_MVert* verts) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (mesh->dev.type != kFaces) return fail(SGPU_ERR_INVALID_ARG, "not a FACES mesh");
+  CK(cudaMemcpyAsync(mesh->dev.co, verts, sizeof(float4) * mesh->dev.totvert,
+                     cudaMemcpyHostToDevice, mesh->stream),
+     "upload verts");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_get_positions(sgpu_mesh* mesh, float* out_xyz) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), mesh->dev.co, sizeof(float4), 3 * sizeof(float),
+                       mesh->dev.totvert, cudaMemcpyDeviceToHost, mesh->stream),
+     "download positions");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_set_positions(sgpu_mesh* mesh, const float* xyz) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  CK(cudaMemcpy2DAsync(mesh->dev.co, sizeof(float4), xyz, 3 * sizeof(float), 3 * sizeof(float),
+                       mesh->dev.totvert, cudaMemcpyHostToDevice, mesh->stream),
+     "upload positions");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_get_normals(sgpu_mesh* mesh, float* out_xyz) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), mesh->dev.no, sizeof(float4), 3 * sizeof(float),
+                       mesh->dev.totvert, cudaMemcpyDeviceToHost, mesh->stream),
+     "download normals");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_get_mask(sgpu_mesh* mesh, float* out) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->dev.mask) return fail(SGPU_ERR_INVALID_ARG, "mesh has no mask");
+  CK(cudaMemcpyAsync(out, mesh->dev.mask, sizeof(float) * mesh->dev.totvert,
+                     cudaMemcpyDeviceToHost, mesh->stream),
+     "download mask");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_get_node_bbs(sgpu_mesh* mesh, float* vb, float* orig_vb) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  const int N = mesh->dev.totnode;
+  std::vector<float4> a(2 * static_cast<size_t>(N)), b(2 * static_cast<size_t>(N));
+  CK(cudaMemcpyAsync(a.data(), mesh->dev.vb, sizeof(float4) * 2 * N, cudaMemcpyDeviceToHost,
+                     mesh->stream),
+     "download vb");
+  CK(cudaMemcpyAsync(b.data(), mesh->dev.orig_vb, sizeof(float4) * 2 * N, cudaMemcpyDeviceToHost,
+                     mesh->stream),
+     "download orig_vb");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  for (int n = 0; n < N; n++) {
+    const float4 a0 = a[2 * n], a1 = a[2 * n + 1], b0 = b[2 * n], b1 = b[2 * n + 1];
+    if (vb) {
+      float* o = vb + 6 * static_cast<size_t>(n);
+      o[0] = a0.x, o[1] = a0.y, o[2] = a0.z, o[3] = a1.x, o[4] = a1.y, o[5] = a1.z;
+    }
+    if (orig_vb) {
+      float* o = orig_vb + 6 * static_cast<size_t>(n);
+      o[0] = b0.x, o[1] = b0.y, o[2] = b0.z, o[3] = b1.x, o[4] = b1.y, o[5] = b1.z;
+    }
+  }
+  return SGPU_OK;
+}
+
+int sgpu_get_nodes(sgpu_mesh* mesh, int* children_offset, int* flag, int* prim_off, int* totprim,
+                   int* uniq_verts, int* face_verts, int* vert_off) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  const HostMesh& h = mesh->host;
+  const int N = h.totnode, L = mesh->dev.nleaf;
+  std::vector<int> lflag(L);
+  CK(cudaMemcpyAsync(lflag.data(), mesh->dev.leaf_flag, sizeof(int) * L, cudaMemcpyDeviceToHost,
+                     mesh->stream),
+     "download flags");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  for (int n = 0; n < N; n++) {
+    const bool leaf = (h.flag[n] & kLeaf) != 0;
+    if (children_offset) children_offset[n] = leaf ? -1 : h.children[n];
+    if (flag) flag[n] = leaf ? lflag[h.node_leaf[n]] : h.flag[n];
+    if (prim_off) prim_off[n] = leaf ? h.prim_off[n] : -1;
+    if (totprim) totprim[n] = leaf ? h.totprim[n] : 0;
+    if (uniq_verts) uniq_verts[n] = leaf ? h.uniq[n] : 0;
+    if (face_verts) face_verts[n] = leaf ? h.face_verts_n[n] : 0;
+    if (vert_off) vert_off[n] = leaf ? h.vert_off[n] : -1;
+  }
+  return SGPU_OK;
+}
+
+int sgpu_get_prim_indices(sgpu_mesh* mesh, int* out) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  std::memcpy(out, mesh->host.prim_indices.data(), sizeof(int) * mesh->host.prim_indices.size());
+  return SGPU_OK;
+}
+
+int sgpu_get_vert_indices(sgpu_mesh* mesh, int* out) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  std::memcpy(out, mesh->host.vert_indices.data(), sizeof(int) * mesh->host.vert_indices.size());
+  return SGPU_OK;
+}
+
+int sgpu_curve_table(int preset, float* table_xy, float* params) {
+  Curve c;
+  if (!build_curve(preset, &c)) return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", preset);
+  if (table_xy)
+    for (int a = 0; a <= kCurveTable; a++) {
+      table_xy[2 * a] = c.table_x[a];
+      table_xy[2 * a + 1] = c.y[a];
+    }
+  if (params) {
+    params[0] = c.mintable;
+    params[1] = c.maxtable;
+    params[2] = c.range;
+    params[3] = c.ext_in[0];
+    params[4] = c.ext_in[1];
+    params[5] = c.ext_out[0];
+    params[6] = c.ext_out[1];
+  }
+  return SGPU_OK;
+}
+
+}  // extern "C"

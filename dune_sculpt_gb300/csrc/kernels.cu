@@ -1,0 +1,760 @@
+// Per-call CUDA kernels of libsculptgpu: node culling, area normal/centre
+// reduction, the four brushes, the FACES normal update and the bounding-box
+// refit with its bottom-up flush.  Each kernel is one phase of the reference's
+// per-dab call sequence; they read their work sizes (culled leaf count, vertex
+// prefix) from device memory, so a whole stroke can be captured in one CUDA
+// graph without host round trips.
+#include <cuda_runtime.h>
+
+#include "sgpu_device.cuh"
+#include "sgpu_kernels.h"
+
+namespace sgpu {
+
+constexpr int kCullThreads = 1024;
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------------------
+// Block-wide exclusive scan of ints (blockDim.x a multiple of 32, <= 1024).
+__device__ int block_exclusive_scan(int v, int* total, int* smem32) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem32[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < nwarps ? smem32[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    smem32[lane] = w;  // inclusive prefix of warp totals
+  }
+  __syncthreads();
+  const int warp_base = warp > 0 ? smem32[warp - 1] : 0;
+  *total = smem32[nwarps - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+// Sphere callback of the spec (closest point of the box; strict "<").
+__device__ __forceinline__ bool sphere_hits(float4 mn, float4 mx, const float* c, float rsq) {
+  float t[3];
+  const float bmin[3] = {mn.x, mn.y, mn.z};
+  const float bmax[3] = {mx.x, mx.y, mx.z};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    float nearest;
+    if (bmin[i] > c[i]) {
+      nearest = bmin[i];
+    } else if (bmax[i] < c[i]) {
+      nearest = bmax[i];
+    } else {
+      nearest = c[i];
+    }
+    t[i] = c[i] - nearest;
+  }
+  return (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]) < rsq;
+}
+
+// BKE_pbvh_search_gather with the sphere callback (pbvh.c:2622-2767).  A leaf
+// is gathered when it and every ancestor pass the callback (the DFS prunes a
+// failing internal node's subtree).  Leaves are numbered by their left-first
+// DFS rank, so emitting passing leaves in rank order reproduces the
+// reference's output order.  One CTA; per-node results in shared memory.
+__global__ void __launch_bounds__(kCullThreads) k_cull(DevMesh m, PassParams pp) {
+  extern __shared__ unsigned char pass[];
+  __shared__ int smem32[32];
+  __shared__ int run_cnt, run_verts;
+  const float4* bb = pp.original ? m.orig_vb : m.vb;
+  for (int n = threadIdx.x; n < m.totnode; n += blockDim.x)
+    pass[n] = sphere_hits(bb[2 * n], bb[2 * n + 1], pp.loc, pp.cull_radius_sq) ? 1 : 0;
+  if (threadIdx.x == 0) {
+    run_cnt = 0;
+    run_verts = 0;
+  }
+  __syncthreads();
+  for (int base = 0; base < m.nleaf; base += blockDim.x) {
+    const int id = base + threadIdx.x;
+    int ok = 0, nv = 0;
+    if (id < m.nleaf) {
+      int node = m.leaf_node[id];
+      ok = pass[node];
+      int p = m.node_parent[node];
+      while (ok && p >= 0) {
+        ok = pass[p];
+        p = m.node_parent[p];
+      }
+      nv = ok ? leaf_nverts(m, id) : 0;
+    }
+    int tot_ok, tot_nv;
+    const int pos = block_exclusive_scan(ok, &tot_ok, smem32);
+    const int voff = block_exclusive_scan(nv, &tot_nv, smem32);
+    if (ok) {
+      m.cull_list[run_cnt + pos] = id;
+      m.cull_off[run_cnt + pos] = run_verts + voff;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      run_cnt += tot_ok;
+      run_verts += tot_nv;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    m.work->cull_count = run_cnt;
+    m.cull_off[run_cnt] = run_verts;
+  }
+}
+
+// Host-provided node list: node indices -> leaf ids and vertex prefix.
+__global__ void __launch_bounds__(kCullThreads) k_set_list(DevMesh m, const int* nodes,
+                                                           int totnode) {
+  __shared__ int smem32[32];
+  __shared__ int run_verts;
+  if (threadIdx.x == 0) run_verts = 0;
+  __syncthreads();
+  for (int base = 0; base < totnode; base += blockDim.x) {
+    const int k = base + threadIdx.x;
+    int nv = 0, id = -1;
+    if (k < totnode) {
+      const int node = nodes[k];
+      if (node < 0 || node >= m.totnode || m.node_leaf[node] < 0) {
+        set_err(m, SGPU_ERR_INVALID_ARG);
+      } else {
+        id = m.node_leaf[node];
+        nv = leaf_nverts(m, id);
+      }
+    }
+    int tot_nv;
+    const int voff = block_exclusive_scan(nv, &tot_nv, smem32);
+    if (k < totnode) {
+      m.cull_list[k] = id < 0 ? 0 : id;
+      m.cull_off[k] = run_verts + voff;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) run_verts += tot_nv;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    m.work->cull_count = totnode;
+    m.cull_off[totnode] = run_verts;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Area normal / centre (spec): per culled leaf, lane t (of 256) sums elements
+// t, t+256, ... with compensated sums; lanes merge pairwise (t, t+s) for
+// s = 128 .. 1; leaf partials then merge pairwise over the culled-list index
+// (i, i+s), s = 1, 2, 4, ...  The last CTA to finish performs that final tree.
+
+struct Lane {
+  CSum v[6];
+  int n_no, n_co;
+};
+
+__device__ __forceinline__ void lane_merge(Lane& a, const Lane& b) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) a.v[k] = cs_merge(a.v[k], b.v[k]);
+  a.n_no += b.n_no;
+  a.n_co += b.n_co;
+}
+
+__device__ __forceinline__ Lane lane_shfl_down(const Lane& a, int s) {
+  Lane r;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    r.v[k].s = __shfl_down_sync(0xffffffffu, a.v[k].s, s);
+    r.v[k].e = __shfl_down_sync(0xffffffffu, a.v[k].e, s);
+  }
+  r.n_no = __shfl_down_sync(0xffffffffu, a.n_no, s);
+  r.n_co = __shfl_down_sync(0xffffffffu, a.n_co, s);
+  return r;
+}
+
+__device__ __forceinline__ void part_store(AreaPart* p, const Lane& l) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    __stcg(&p->s[k], l.v[k].s);
+    __stcg(&p->e[k], l.v[k].e);
+  }
+  __stcg(&p->n_no, l.n_no);
+  __stcg(&p->n_co, l.n_co);
+}
+__device__ __forceinline__ Lane part_load(const AreaPart* p) {
+  Lane l;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    l.v[k].s = __ldcg(&p->s[k]);
+    l.v[k].e = __ldcg(&p->e[k]);
+  }
+  l.n_no = __ldcg(&p->n_no);
+  l.n_co = __ldcg(&p->n_co);
+  return l;
+}
+
+__global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassParams pp) {
+  __shared__ Lane sl[kThreads];
+  __shared__ bool am_last;
+  const int cnt = m.work->cull_count;
+  const float rn = b.radius * b.normal_radius_factor;
+  const float ra = b.radius * b.area_radius_factor;
+  const float rn2 = rn * rn, ra2 = ra * ra;
+  const int t = threadIdx.x;
+  for (int k = blockIdx.x; k < cnt; k += gridDim.x) {
+    const int leaf = m.cull_list[k];
+    const int nv = leaf_nverts(m, leaf);
+    Lane l;
+#pragma unroll
+    for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
+    l.n_no = l.n_co = 0;
+    for (int i = t; i < nv; i += kThreads) {
+      const int v = leaf_vert(m, leaf, i);
+      const float4 co = m.co[v];
+      const float d2 = dist_sq(co, pp.loc);
+      if (d2 <= rn2) {
+        const float4 no = m.no[v];
+        cs_add(l.v[0], no.x);
+        cs_add(l.v[1], no.y);
+        cs_add(l.v[2], no.z);
+        l.n_no++;
+      }
+      if (d2 <= ra2) {
+        cs_add(l.v[3], co.x);
+        cs_add(l.v[4], co.y);
+        cs_add(l.v[5], co.z);
+        l.n_co++;
+      }
+    }
+    sl[t] = l;
+    __syncthreads();
+    for (int s = kThreads / 2; s >= 32; s >>= 1) {
+      if (t < s) {
+        Lane a = sl[t];
+        lane_merge(a, sl[t + s]);
+        sl[t] = a;
+      }
+      __syncthreads();
+    }
+    if (t < 32) {
+      Lane a = sl[t];
+      for (int s = 16; s >= 1; s >>= 1) {
+        const Lane o = lane_shfl_down(a, s);
+        lane_merge(a, o);
+      }
+      if (t == 0) part_store(&m.parts[k], a);
+    }
+    __syncthreads();
+  }
+  __threadfence();
+  __syncthreads();
+  if (t == 0) {
+    const unsigned int ticket = atomicAdd(&m.work->ticket_area, 1u);
+    am_last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  for (int s = 1; s < cnt; s <<= 1) {
+    for (int i = t * 2 * s; i + s < cnt; i += kThreads * 2 * s) {
+      Lane a = part_load(&m.parts[i]);
+      lane_merge(a, part_load(&m.parts[i + s]));
+      part_store(&m.parts[i], a);
+    }
+    __threadfence_block();
+    __syncthreads();
+  }
+  if (t == 0) {
+    Lane tot;
+    if (cnt > 0) {
+      tot = part_load(&m.parts[0]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 6; q++) tot.v[q].s = tot.v[q].e = 0.0f;
+      tot.n_no = tot.n_co = 0;
+    }
+    float nx = tot.v[0].s + tot.v[0].e;
+    float ny = tot.v[1].s + tot.v[1].e;
+    float nz = tot.v[2].s + tot.v[2].e;
+    normalize3(nx, ny, nz);
+    float cx, cy, cz;
+    if (tot.n_co > 0) {
+      const float inv = 1.0f / (float)tot.n_co;
+      cx = (tot.v[3].s + tot.v[3].e) * inv;
+      cy = (tot.v[4].s + tot.v[4].e) * inv;
+      cz = (tot.v[5].s + tot.v[5].e) * inv;
+    } else {
+      cx = pp.loc[0];
+      cy = pp.loc[1];
+      cz = pp.loc[2];
+    }
+    Work* w = m.work;
+    w->area_no[0] = nx;
+    w->area_no[1] = ny;
+    w->area_no[2] = nz;
+    w->area_co[0] = cx;
+    w->area_co[1] = cy;
+    w->area_co[2] = cz;
+    w->area_n_co = tot.n_co;
+    w->ticket_area = 0u;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Brushes.  Work item i in [0, cull_off[cnt]) is vertex (i - cull_off[k]) of
+// culled leaf k, found by binary search over cull_off.
+
+__device__ __forceinline__ int find_slot(const int* off, int cnt, int i) {
+  int lo = 0, hi = cnt;  // off[lo] <= i < off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&off[mid]) <= i) {
+      lo = mid;
+    } else {
+      hi = mid;
+    }
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void count_displaced(const DevMesh& m, bool moved) {
+  const unsigned int bal = __ballot_sync(0xffffffffu, moved);
+  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&m.work->displaced, (unsigned long long)__popc(bal));
+}
+
+__device__ __forceinline__ void mark_culled(const DevMesh& m, int cnt) {
+  if (blockIdx.x == 0)
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) atomicOr(&m.leaf_flag[m.cull_list[k]], kMarkUpdate);
+}
+
+__device__ __forceinline__ void load_curve(const DevBrush& b, float* y) {
+  for (int i = threadIdx.x; i <= kCurveTable; i += blockDim.x) y[i] = b.y[i];
+  __syncthreads();
+}
+
+__device__ __forceinline__ void cross3(float* r, const float* a, const float* b) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Draw, inflate and clay strips (one pass each; positions written in place,
+// each vertex by exactly one thread since leaves expose unique vertices).
+__global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassParams pp) {
+  __shared__ float ys[kCurveTable + 1];
+  load_curve(b, ys);
+  const int cnt = m.work->cull_count;
+  const int total = m.cull_off[cnt];
+  const float radius = b.radius;
+  const float radius_sq = radius * radius;
+  float area_no[3] = {0.0f, 0.0f, 0.0f}, area_co[3] = {0.0f, 0.0f, 0.0f};
+  if (b.tool == kToolDraw || b.tool == kToolClayStrips) {
+    for (int k = 0; k < 3; k++) {
+      area_no[k] = __ldcg(&m.work->area_no[k]);
+      area_co[k] = __ldcg(&m.work->area_co[k]);
+    }
+  }
+  // Clay strips frame: z = area normal, x = z cross grab delta, y = z cross x.
+  float xa[3], ya[3], pd = 0.0f, inv_r = 0.0f, inv_rz = 0.0f;
+  if (b.tool == kToolClayStrips) {
+    cross3(xa, area_no, pp.delta);
+    if (normalize3(xa[0], xa[1], xa[2]) == 0.0f) return;
+    cross3(ya, area_no, xa);
+    if (normalize3(ya[0], ya[1], ya[2]) == 0.0f) return;
+    const float rsign = b.strength < 0.0f ? -radius : radius;
+    const float displace = rsign * (0.18f + b.plane_offset);
+    float p[3];
+    for (int k = 0; k < 3; k++) p[k] = area_co[k] + area_no[k] * displace;
+    pd = -(area_no[0] * p[0] + area_no[1] * p[1] + area_no[2] * p[2]);
+    inv_r = 1.0f / radius;
+    inv_rz = 1.0f / (radius * 1.25f);
+  }
+  mark_culled(m, cnt);
+  const float dd = radius * b.strength;
+  const float off[3] = {area_no[0] * dd, area_no[1] * dd, area_no[2] * dd};
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < total; base += stride) {
+    const int i = base + threadIdx.x;
+    bool moved = false;
+    if (i < total) {
+      const int k = find_slot(m.cull_off, cnt, i);
+      const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
+      float4 co = m.co[v];
+      bool hit = false;
+      if (b.tool == kToolDraw) {
+        const float d2 = dist_sq(co, pp.loc);
+        if (d2 <= radius_sq) {
+          const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+          co.x = co.x + off[0] * sf;
+          co.y = co.y + off[1] * sf;
+          co.z = co.z + off[2] * sf;
+          hit = true;
+          moved = sf != 0.0f;
+        }
+      } else if (b.tool == kToolInflate) {
+        const float d2 = dist_sq(co, pp.loc);
+        if (d2 <= radius_sq) {
+          const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+          const float fade = b.strength * sf;
+          const float kk = fade * radius;
+          const float4 no = m.no[v];
+          co.x = co.x + no.x * kk;
+          co.y = co.y + no.y * kk;
+          co.z = co.z + no.z * kk;
+          hit = true;
+          moved = sf != 0.0f;
+        }
+      } else {  // clay strips
+        const float r0 = co.x - pp.loc[0], r1 = co.y - pp.loc[1], r2 = co.z - pp.loc[2];
+        const float lx = fabsf((r0 * xa[0] + r1 * xa[1] + r2 * xa[2]) * inv_r);
+        const float ly = fabsf((r0 * ya[0] + r1 * ya[1] + r2 * ya[2]) * inv_r);
+        const float lz = fabsf((r0 * area_no[0] + r1 * area_no[1] + r2 * area_no[2]) * inv_rz);
+        if (lx <= 1.0f && ly <= 1.0f && lz <= 1.0f) {
+          const float dloc = (lx > ly) ? lx : ly;
+          const float sf = strength_factor(m, b, ys, pp, v, radius * dloc, radius);
+          const float fade = b.strength * sf;
+          const float side = (co.x * area_no[0] + co.y * area_no[1] + co.z * area_no[2]) + pd;
+          const float ns = -side;
+          const float v0 = (co.x + area_no[0] * ns) - co.x;
+          const float v1 = (co.y + area_no[1] * ns) - co.y;
+          const float v2 = (co.z + area_no[2] * ns) - co.z;
+          co.x = co.x + v0 * fade;
+          co.y = co.y + v1 * fade;
+          co.z = co.z + v2 * fade;
+          hit = true;
+          moved = sf != 0.0f;
+        }
+      }
+      if (hit) {
+        m.co[v] = co;
+        if (m.type == kFaces) m.vtag[v] = 1;
+      }
+    }
+    count_displaced(m, moved);
+  }
+}
+
+// Smooth, one Jacobi sweep in two launches: compute new positions from the
+// sweep-start state into scratch (w = 1 marks a hit), then write them back.
+__device__ __forceinline__ float3 neighbor_average(const DevMesh& m, int v, float4 c0) {
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+  int n = 0;
+  if (m.type == kFaces) {
+    const int e = m.nb_off[v + 1];
+    for (int q = m.nb_off[v]; q < e; q++) {
+      const float4 c = m.co[m.nb_idx[q]];
+      sx += c.x;
+      sy += c.y;
+      sz += c.z;
+      n++;
+    }
+  } else {
+    const int gs = m.grid_size, area = m.grid_area;
+    const int g = v / area, r = v % area, x = r % gs, y = r / gs;
+    const int nx[4] = {x - 1, x + 1, x, x};
+    const int ny[4] = {y, y, y - 1, y + 1};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (nx[k] >= 0 && nx[k] < gs && ny[k] >= 0 && ny[k] < gs) {
+        const float4 c = m.co[g * area + ny[k] * gs + nx[k]];
+        sx += c.x;
+        sy += c.y;
+        sz += c.z;
+        n++;
+      }
+    }
+  }
+  if (n == 0) return make_float3(c0.x, c0.y, c0.z);
+  const float inv = 1.0f / (float)n;
+  return make_float3(sx * inv, sy * inv, sz * inv);
+}
+
+__global__ void __launch_bounds__(kThreads) k_smooth_compute(DevMesh m, DevBrush b,
+                                                             PassParams pp) {
+  __shared__ float ys[kCurveTable + 1];
+  load_curve(b, ys);
+  const int cnt = m.work->cull_count;
+  const int total = m.cull_off[cnt];
+  const float radius = b.radius;
+  const float radius_sq = radius * radius;
+  if (pp.iteration == 0) mark_culled(m, cnt);
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < total; base += stride) {
+    const int i = base + threadIdx.x;
+    bool moved = false;
+    if (i < total) {
+      const int k = find_slot(m.cull_off, cnt, i);
+      const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
+      const float4 co = m.co[v];
+      const float d2 = dist_sq(co, pp.loc);
+      float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (d2 <= radius_sq) {
+        const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+        const float fade = pp.iter_strength * sf;
+        const float3 avg = neighbor_average(m, v, co);
+        out.x = co.x + (avg.x - co.x) * fade;
+        out.y = co.y + (avg.y - co.y) * fade;
+        out.z = co.z + (avg.z - co.z) * fade;
+        out.w = 1.0f;
+        moved = (pp.iteration == 0) && sf != 0.0f;
+      }
+      m.scratch[i] = out;
+    }
+    count_displaced(m, moved);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_smooth_apply(DevMesh m) {
+  const int cnt = m.work->cull_count;
+  const int total = m.cull_off[cnt];
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const float4 s = m.scratch[i];
+    if (s.w == 0.0f) continue;
+    const int k = find_slot(m.cull_off, cnt, i);
+    const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
+    float4 co = m.co[v];
+    co.x = s.x;
+    co.y = s.y;
+    co.z = s.z;
+    m.co[v] = co;
+    if (m.type == kFaces) m.vtag[v] = 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FACES normal update (gather form of pbvh.c:2912-3036) fused with the leaf
+// bounding-box refit (update_node_vb over PBVH_ITER_ALL, pbvh.c:2026-2046;
+// pbvh_update_BB_redraw, pbvh.c:3124-3160).  The last CTA clears the
+// UpdateNormals flags and runs the bottom-up flush (pbvh_flush_bb,
+// pbvh.c:3287-3317) level by level.
+
+__device__ __forceinline__ float fmin_ref(float a, float b) { return (a < b) ? a : b; }
+__device__ __forceinline__ float fmax_ref(float a, float b) { return (a > b) ? a : b; }
+
+__device__ void leaf_refit(const DevMesh& m, int leaf, float* red /* 6*kThreads/32 */) {
+  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+  float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  const int nv = leaf_nverts_all(m, leaf);
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    int v;
+    if (m.type == kFaces) {
+      v = m.leaf_verts[m.leaf_vert_off[leaf] + i];
+    } else {
+      v = leaf_vert(m, leaf, i);
+    }
+    const float4 c = m.co[v];
+    mn[0] = fmin_ref(mn[0], c.x);
+    mn[1] = fmin_ref(mn[1], c.y);
+    mn[2] = fmin_ref(mn[2], c.z);
+    mx[0] = fmax_ref(mx[0], c.x);
+    mx[1] = fmax_ref(mx[1], c.y);
+    mx[2] = fmax_ref(mx[2], c.z);
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      mn[k] = fmin_ref(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+      mx[k] = fmax_ref(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+    }
+  }
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    for (int k = 0; k < 3; k++) {
+      red[warp * 6 + k] = mn[k];
+      red[warp * 6 + 3 + k] = mx[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; w++)
+      for (int k = 0; k < 3; k++) {
+        mn[k] = fmin_ref(mn[k], red[w * 6 + k]);
+        mx[k] = fmax_ref(mx[k], red[w * 6 + 3 + k]);
+      }
+    const int node = m.leaf_node[leaf];
+    m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+    m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+  }
+  __syncthreads();
+}
+
+__device__ void faces_leaf_normals(const DevMesh& m, int leaf) {
+  const int off = m.leaf_vert_off[leaf];
+  const int nu = m.leaf_uniq[leaf];
+  for (int i = threadIdx.x; i < nu; i += blockDim.x) {
+    const int v = m.leaf_verts[off + i];
+    if (!m.vtag[v]) continue;
+    CSum ax = {0.0f, 0.0f}, ay = {0.0f, 0.0f}, az = {0.0f, 0.0f};
+    const int e = m.vt_off[v + 1];
+    for (int q = m.vt_off[v]; q < e; q++) {
+      const int t = m.vt_idx[q];
+      if (!(m.leaf_flag[m.lt_leaf[t]] & kUpdateNormals)) continue;
+      const float3 fn = poly_normal(m, m.lt[t].w);
+      cs_add(ax, fn.x);
+      cs_add(ay, fn.y);
+      cs_add(az, fn.z);
+    }
+    float nx = ax.s + ax.e, ny = ay.s + ay.e, nz = az.s + az.e;
+    normalize3(nx, ny, nz);
+    m.no[v] = make_float4(nx, ny, nz, 0.0f);
+    m.vtag[v] = 0;
+  }
+}
+
+// Bottom-up flush of updated boxes, run by one CTA.
+__device__ void flush_bounds(const DevMesh& m, int flag) {
+  const int bits = flag & (kUpdateBB | kUpdateOriginalBB);
+  for (int leaf = threadIdx.x; leaf < m.nleaf; leaf += blockDim.x) {
+    const int node = m.leaf_node[leaf];
+    const int f = m.leaf_flag[leaf];
+    m.node_upd[node] = (unsigned char)(f & bits);
+    if (f & bits) m.leaf_flag[leaf] = f & ~bits;
+  }
+  __syncthreads();
+  for (int l = 0; l < m.nlevels; l++) {
+    const int b0 = m.level_off[l], b1 = m.level_off[l + 1];
+    for (int j = b0 + threadIdx.x; j < b1; j += blockDim.x) {
+      const int node = m.level_nodes[j];
+      const int c = m.node_child[node];
+      const int u = m.node_upd[c] | m.node_upd[c + 1];
+      m.node_upd[node] = (unsigned char)u;
+      if (u & kUpdateBB) {
+        const float4 a0 = m.vb[2 * c], a1 = m.vb[2 * c + 1];
+        const float4 c0 = m.vb[2 * (c + 1)], c1 = m.vb[2 * (c + 1) + 1];
+        float4 mn, mx;
+        mn.x = fmin_ref(fmin_ref(FLT_MAX, a0.x), c0.x);
+        mn.y = fmin_ref(fmin_ref(FLT_MAX, a0.y), c0.y);
+        mn.z = fmin_ref(fmin_ref(FLT_MAX, a0.z), c0.z);
+        mx.x = fmax_ref(fmax_ref(-FLT_MAX, a1.x), c1.x);
+        mx.y = fmax_ref(fmax_ref(-FLT_MAX, a1.y), c1.y);
+        mx.z = fmax_ref(fmax_ref(-FLT_MAX, a1.z), c1.z);
+        mn.w = mx.w = 0.0f;
+        m.vb[2 * node] = mn;
+        m.vb[2 * node + 1] = mx;
+      }
+      if (u & kUpdateOriginalBB) {
+        m.orig_vb[2 * node] = m.vb[2 * node];
+        m.orig_vb[2 * node + 1] = m.vb[2 * node + 1];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_update_faces(DevMesh m, int do_normals,
+                                                           int bounds_flag) {
+  __shared__ float red[6 * (kThreads / 32)];
+  __shared__ bool am_last;
+  for (int leaf = blockIdx.x; leaf < m.nleaf; leaf += gridDim.x) {
+    const int f = m.leaf_flag[leaf];
+    if (do_normals && m.type == kFaces && (f & kUpdateNormals)) faces_leaf_normals(m, leaf);
+    if ((bounds_flag & kUpdateBB) && (f & kUpdateBB)) leaf_refit(m, leaf, red);
+    if (threadIdx.x == 0) {
+      const int node = m.leaf_node[leaf];
+      if ((bounds_flag & kUpdateOriginalBB) && (f & kUpdateOriginalBB)) {
+        m.orig_vb[2 * node] = m.vb[2 * node];
+        m.orig_vb[2 * node + 1] = m.vb[2 * node + 1];
+      }
+      if ((bounds_flag & kUpdateRedraw) && (f & kUpdateRedraw))
+        atomicAnd(&m.leaf_flag[leaf], ~kUpdateRedraw);
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int ticket = atomicAdd(&m.work->ticket_update, 1u);
+    am_last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  if (do_normals && m.type == kFaces) {
+    for (int leaf = threadIdx.x; leaf < m.nleaf; leaf += blockDim.x)
+      m.leaf_flag[leaf] &= ~kUpdateNormals;
+    __syncthreads();
+  }
+  if (bounds_flag & (kUpdateBB | kUpdateOriginalBB)) flush_bounds(m, bounds_flag);
+  if (threadIdx.x == 0) m.work->ticket_update = 0u;
+}
+
+__global__ void k_mark_node(DevMesh m, int node) {
+  if (node >= 0 && node < m.totnode && m.node_leaf[node] >= 0)
+    atomicOr(&m.leaf_flag[m.node_leaf[node]], kMarkUpdate);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+static int g_grid = 0;
+
+static int work_grid() {
+  if (g_grid == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    g_grid = sms > 0 ? 2 * sms : 264;
+  }
+  return g_grid;
+}
+
+cudaError_t launch_cull(const DevMesh& m, const PassParams& pp, cudaStream_t s) {
+  const size_t smem = (static_cast<size_t>(m.totnode) + 15) & ~static_cast<size_t>(15);
+  k_cull<<<1, kCullThreads, smem, s>>>(m, pp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_list(const DevMesh& m, const int* dev_nodes, int totnode,
+                            cudaStream_t s) {
+  k_set_list<<<1, kCullThreads, 0, s>>>(m, dev_nodes, totnode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_area(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                        cudaStream_t s) {
+  int g = m.nleaf < work_grid() ? m.nleaf : work_grid();
+  if (g < 1) g = 1;
+  k_area<<<g, kThreads, 0, s>>>(m, b, pp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_brush(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                         cudaStream_t s) {
+  k_brush<<<work_grid(), kThreads, 0, s>>>(m, b, pp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth_iteration(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                                    cudaStream_t s) {
+  k_smooth_compute<<<work_grid(), kThreads, 0, s>>>(m, b, pp);
+  k_smooth_apply<<<work_grid(), kThreads, 0, s>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update_faces(const DevMesh& m, int do_normals, int bounds_flag,
+                                cudaStream_t s) {
+  int g = m.nleaf < work_grid() ? m.nleaf : work_grid();
+  if (g < 1) g = 1;
+  k_update_faces<<<g, kThreads, 0, s>>>(m, do_normals, bounds_flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s) {
+  k_mark_node<<<1, 1, 0, s>>>(m, node);
+  return cudaGetLastError();
+}
+
+int cull_smem_limit() { return 200 * 1024; }
+
+void configure_kernels() {
+  cudaFuncSetAttribute(k_cull, cudaFuncAttributeMaxDynamicSharedMemorySize, cull_smem_limit());
+}
+
+}  // namespace sgpu

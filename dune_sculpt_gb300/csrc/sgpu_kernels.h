@@ -1,0 +1,29 @@
+// Kernel launchers of libsculptgpu (defined in kernels.cu / kernels_grids.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sgpu_device.cuh"
+
+namespace sgpu {
+
+cudaError_t launch_cull(const DevMesh& m, const PassParams& pp, cudaStream_t s);
+cudaError_t launch_set_list(const DevMesh& m, const int* dev_nodes, int totnode, cudaStream_t s);
+cudaError_t launch_area(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                        cudaStream_t s);
+cudaError_t launch_brush(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                         cudaStream_t s);
+// One smooth iteration = two launches (compute, apply).
+cudaError_t launch_smooth_iteration(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                                    cudaStream_t s);
+// FACES normals (do_normals) and/or bounds refit + flush (bounds_flag); bounds
+// also serve GRIDS meshes.
+cudaError_t launch_update_faces(const DevMesh& m, int do_normals, int bounds_flag,
+                                cudaStream_t s);
+// GRIDS normal update with seam stitching.  Returns the number of launches.
+cudaError_t launch_update_grids(const DevMesh& m, cudaStream_t s, int* launches);
+cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s);
+int cull_smem_limit();
+void configure_kernels();
+
+}  // namespace sgpu

@@ -1,0 +1,330 @@
+"""Python binding of libsculptgpu (the C ABI declared in include/sculpt_gpu.h).
+
+``PBVH`` mirrors the reference's PBVH call surface for the sculpt dab path
+(source/dune/kernel/intern/pbvh.c): ``build_mesh`` / ``build_grids``
+(BKE_pbvh_build_mesh / _grids), ``search_gather_sphere``
+(BKE_pbvh_search_gather with the sculpt sphere callback), ``do_draw_brush`` and
+the other ``do_*_brush`` entry points, ``update_normals``
+(BKE_pbvh_update_normals), ``update_bounds`` (BKE_pbvh_update_bounds) and
+``node_mark_update``.  Errors raise ``SculptGPUError`` with the library's status
+code, as the C entry points return it.  There is no CPU fallback: without the
+compiled library or a GPU every call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import synth
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libsculptgpu.so")
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_BOUNDS, ERR_UNSUPPORTED = range(7)
+PBVH_Leaf, PBVH_UpdateNormals, PBVH_UpdateBB, PBVH_UpdateOriginalBB = 1, 2, 4, 8
+PBVH_UpdateDrawBuffers, PBVH_UpdateRedraw = 16, 32
+STROKE_EAGER, STROKE_GRAPH = 0, 1
+
+
+class SculptGPUError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"libsculptgpu error {code}: {msg}")
+        self.code = code
+
+
+class SGPU_Brush(C.Structure):
+    _fields_ = [("sculpt_tool", C.c_int), ("flag", C.c_int), ("symmetry", C.c_int),
+                ("curve_preset", C.c_int), ("radius", C.c_float), ("strength", C.c_float),
+                ("normal_radius_factor", C.c_float), ("area_radius_factor", C.c_float),
+                ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
+                ("use_original_bb", C.c_int)]
+
+
+class SGPU_MeshInfo(C.Structure):
+    _fields_ = [("type", C.c_int), ("totvert", C.c_int), ("totnode", C.c_int),
+                ("totleaf", C.c_int), ("leaf_limit", C.c_int), ("totprim", C.c_int),
+                ("leaf_vert_entries", C.c_int), ("grid_size", C.c_int)]
+
+
+class SGPU_StrokeStats(C.Structure):
+    _fields_ = [("verts_displaced", C.c_int64), ("gpu_ms", C.c_float),
+                ("kernel_launches", C.c_int), ("graph_nodes", C.c_int)]
+
+
+# Every exported symbol, as declared in include/sculpt_gpu.h.
+EXPORTS = (
+    "sgpu_version", "sgpu_last_error", "sgpu_device_info", "sgpu_mesh_create_faces",
+    "sgpu_mesh_create_grids", "sgpu_mesh_destroy", "sgpu_mesh_info", "sgpu_mesh_sync",
+    "sgpu_mesh_stream", "sgpu_search_sphere", "sgpu_do_draw_brush", "sgpu_do_smooth_brush",
+    "sgpu_do_inflate_brush", "sgpu_do_clay_strips_brush", "sgpu_do_brush",
+    "sgpu_pbvh_update_normals", "sgpu_pbvh_update_bounds", "sgpu_pbvh_node_mark_update",
+    "sgpu_stroke", "sgpu_get_verts", "sgpu_set_verts", "sgpu_get_positions",
+    "sgpu_set_positions", "sgpu_get_normals", "sgpu_get_mask", "sgpu_get_node_bbs",
+    "sgpu_get_nodes", "sgpu_get_prim_indices", "sgpu_get_vert_indices", "sgpu_curve_table",
+)
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads libsculptgpu; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libsculptgpu is not built ({p} missing); run __graft_entry__.build()")
+    L = C.CDLL(p)
+    vp, i, f = C.c_void_p, C.c_int, C.c_float
+    L.sgpu_version.restype = C.c_char_p
+    L.sgpu_last_error.restype = C.c_char_p
+    L.sgpu_device_info.argtypes = [vp, vp, vp]
+    L.sgpu_mesh_create_faces.argtypes = [vp, i, vp, i, vp, i, vp, i, vp, vp, vp, i, vp]
+    L.sgpu_mesh_create_grids.argtypes = [i, i, vp, vp, vp, i, vp, vp, vp, vp, i, i, vp, i, vp]
+    L.sgpu_mesh_destroy.argtypes = [vp]
+    L.sgpu_mesh_info.argtypes = [vp, C.POINTER(SGPU_MeshInfo)]
+    L.sgpu_mesh_sync.argtypes = [vp]
+    L.sgpu_mesh_stream.argtypes = [vp]
+    L.sgpu_mesh_stream.restype = vp
+    L.sgpu_search_sphere.argtypes = [vp, vp, f, i, vp, vp]
+    for name in ("sgpu_do_draw_brush", "sgpu_do_smooth_brush", "sgpu_do_inflate_brush",
+                 "sgpu_do_clay_strips_brush", "sgpu_do_brush"):
+        getattr(L, name).argtypes = [vp, C.POINTER(SGPU_Brush), vp, vp, vp, i]
+    L.sgpu_pbvh_update_normals.argtypes = [vp]
+    L.sgpu_pbvh_update_bounds.argtypes = [vp, i]
+    L.sgpu_pbvh_node_mark_update.argtypes = [vp, i]
+    L.sgpu_stroke.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, i,
+                              C.POINTER(SGPU_StrokeStats)]
+    for name in ("sgpu_get_verts", "sgpu_set_verts", "sgpu_get_positions", "sgpu_set_positions",
+                 "sgpu_get_normals", "sgpu_get_mask", "sgpu_get_prim_indices",
+                 "sgpu_get_vert_indices"):
+        getattr(L, name).argtypes = [vp, vp]
+    L.sgpu_get_node_bbs.argtypes = [vp, vp, vp]
+    L.sgpu_get_nodes.argtypes = [vp] + [vp] * 7
+    L.sgpu_curve_table.argtypes = [i, vp, vp]
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _check(rc: int):
+    if rc != OK:
+        raise SculptGPUError(rc, load().sgpu_last_error().decode())
+
+
+def make_brush(st) -> SGPU_Brush:
+    b = SGPU_Brush()
+    b.sculpt_tool = st.tool
+    b.flag = st.flag
+    b.symmetry = st.symmetry
+    b.curve_preset = st.curve_preset
+    b.radius = st.radius
+    b.strength = st.strength
+    b.normal_radius_factor = st.normal_radius_factor
+    b.area_radius_factor = st.area_radius_factor
+    b.plane_offset = st.plane_offset
+    for k in range(3):
+        b.view_normal[k] = st.view_normal[k]
+    b.use_original_bb = st.use_original_bb
+    return b
+
+
+def device_info() -> tuple[int, int, int]:
+    L = load()
+    sms, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    _check(L.sgpu_device_info(C.byref(sms), C.byref(ma), C.byref(mi)))
+    return sms.value, ma.value, mi.value
+
+
+def curve_table(preset: int):
+    t = np.zeros((257, 2), dtype=np.float32)
+    p = np.zeros(7, dtype=np.float32)
+    _check(load().sgpu_curve_table(preset, _p(t), _p(p)))
+    return t, p
+
+
+class PBVH:
+    """Device mirror of one PBVH and its mesh (one handle of libsculptgpu)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        self._info = SGPU_MeshInfo()
+        _check(load().sgpu_mesh_info(self._h, C.byref(self._info)))
+
+    # -- construction (BKE_pbvh_build_mesh / BKE_pbvh_build_grids)
+    @classmethod
+    def build_mesh(cls, mesh: "synth.FacesMesh", leaf_limit: int = 0, vert_normals=None,
+                   automask=None) -> "PBVH":
+        L = load()
+        h = C.c_void_p()
+        mask = None if mesh.mask is None else np.ascontiguousarray(mesh.mask, dtype=np.float32)
+        no = None if vert_normals is None else np.ascontiguousarray(vert_normals, np.float32)
+        am = None if automask is None else np.ascontiguousarray(automask, dtype=np.float32)
+        _check(L.sgpu_mesh_create_faces(
+            _p(mesh.verts), mesh.verts.shape[0], _p(mesh.polys), mesh.polys.shape[0],
+            _p(mesh.loops), mesh.loops.shape[0], _p(mesh.looptris), mesh.looptris.shape[0],
+            _p(no), _p(mask), _p(am), leaf_limit, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def build_grids(cls, g: "synth.GridsMesh", leaf_limit: int = 0, normals=None) -> "PBVH":
+        L = load()
+        h = C.c_void_p()
+        co = np.ascontiguousarray(g.co, dtype=np.float32)
+        no = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32)
+        mask = None if g.mask is None else np.ascontiguousarray(g.mask, dtype=np.float32)
+        arrs = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (g.face_start, g.face_ngrids, g.face_verts, g.face_edges, g.edge_verts)]
+        _check(L.sgpu_mesh_create_grids(
+            g.num_grids, g.grid_size, _p(co), _p(no), _p(mask), g.num_faces, _p(arrs[0]),
+            _p(arrs[1]), _p(arrs[2]), _p(arrs[3]), g.num_base_verts, arrs[4].shape[0],
+            _p(arrs[4]), leaf_limit, C.byref(h)))
+        return cls(h)
+
+    def free(self):
+        if self._h:
+            _check(load().sgpu_mesh_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def info(self) -> SGPU_MeshInfo:
+        return self._info
+
+    @property
+    def num_nodes(self) -> int:
+        return self._info.totnode
+
+    @property
+    def num_leaves(self) -> int:
+        return self._info.totleaf
+
+    @property
+    def num_verts(self) -> int:
+        return self._info.totvert
+
+    # -- the reference's per-call entry points
+    def search_gather_sphere(self, center, radius_sq: float, original: int = 0) -> np.ndarray:
+        out = np.zeros(self.num_leaves + 1, dtype=np.int32)
+        tot = C.c_int()
+        c = np.asarray(center, dtype=np.float32)
+        _check(load().sgpu_search_sphere(self._h, _p(c), radius_sq, original, _p(out),
+                                         C.byref(tot)))
+        return out[:tot.value]
+
+    def search_sphere_device(self, center, radius_sq: float, original: int = 0):
+        c = np.asarray(center, dtype=np.float32)
+        _check(load().sgpu_search_sphere(self._h, _p(c), radius_sq, original, None, None))
+
+    def _brush(self, fn: str, st, location, grab_delta, nodes=None):
+        b = make_brush(st)
+        loc = np.asarray(location, dtype=np.float32)
+        gd = np.asarray(grab_delta, dtype=np.float32)
+        nd = None if nodes is None else np.ascontiguousarray(nodes, dtype=np.int32)
+        _check(getattr(load(), fn)(self._h, C.byref(b), _p(loc), _p(gd), _p(nd),
+                                   0 if nd is None else nd.shape[0]))
+
+    def do_draw_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_draw_brush", st, location, grab_delta, nodes)
+
+    def do_smooth_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_smooth_brush", st, location, grab_delta, nodes)
+
+    def do_inflate_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_inflate_brush", st, location, grab_delta, nodes)
+
+    def do_clay_strips_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_clay_strips_brush", st, location, grab_delta, nodes)
+
+    def do_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_brush", st, location, grab_delta, nodes)
+
+    def update_normals(self):
+        _check(load().sgpu_pbvh_update_normals(self._h))
+
+    def update_bounds(self, flag: int):
+        _check(load().sgpu_pbvh_update_bounds(self._h, flag))
+
+    def node_mark_update(self, node: int):
+        _check(load().sgpu_pbvh_node_mark_update(self._h, node))
+
+    # -- whole strokes
+    def stroke(self, st, mode: int = STROKE_GRAPH, dabs=None, dab_tools=None) -> SGPU_StrokeStats:
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        stats = SGPU_StrokeStats()
+        _check(load().sgpu_stroke(self._h, C.byref(b), _p(d), d.shape[0], _p(tools), mode,
+                                  C.byref(stats)))
+        return stats
+
+    def sync(self):
+        _check(load().sgpu_mesh_sync(self._h))
+
+    # -- data access
+    def positions(self) -> np.ndarray:
+        out = np.zeros((self.num_verts, 3), dtype=np.float32)
+        _check(load().sgpu_get_positions(self._h, _p(out)))
+        return out
+
+    def set_positions(self, co: np.ndarray):
+        co = np.ascontiguousarray(co, dtype=np.float32)
+        _check(load().sgpu_set_positions(self._h, _p(co)))
+
+    def verts(self) -> np.ndarray:
+        out = np.zeros(self.num_verts, dtype=synth.MVERT_DT)
+        _check(load().sgpu_get_verts(self._h, _p(out)))
+        return out
+
+    def set_verts(self, verts: np.ndarray):
+        v = np.ascontiguousarray(verts)
+        _check(load().sgpu_set_verts(self._h, _p(v)))
+
+    def normals(self) -> np.ndarray:
+        out = np.zeros((self.num_verts, 3), dtype=np.float32)
+        _check(load().sgpu_get_normals(self._h, _p(out)))
+        return out
+
+    def mask(self) -> np.ndarray:
+        out = np.zeros(self.num_verts, dtype=np.float32)
+        _check(load().sgpu_get_mask(self._h, _p(out)))
+        return out
+
+    def bbs(self):
+        vb = np.zeros((self.num_nodes, 6), dtype=np.float32)
+        ovb = np.zeros((self.num_nodes, 6), dtype=np.float32)
+        _check(load().sgpu_get_node_bbs(self._h, _p(vb), _p(ovb)))
+        return vb, ovb
+
+    def nodes(self) -> dict:
+        n = self.num_nodes
+        keys = ("children_offset", "flag", "prim_off", "totprim", "uniq", "face_verts",
+                "vert_off")
+        arrs = {k: np.zeros(n, dtype=np.int32) for k in keys}
+        _check(load().sgpu_get_nodes(self._h, *[_p(arrs[k]) for k in keys]))
+        return arrs
+
+    def prim_indices(self) -> np.ndarray:
+        out = np.zeros(max(self._info.totprim, 1), dtype=np.int32)
+        _check(load().sgpu_get_prim_indices(self._h, _p(out)))
+        return out[:self._info.totprim]
+
+    def vert_indices(self) -> np.ndarray:
+        n = self._info.leaf_vert_entries
+        out = np.zeros(max(n, 1), dtype=np.int32)
+        _check(load().sgpu_get_vert_indices(self._h, _p(out)))
+        return out[:n]

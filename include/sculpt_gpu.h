@@ -1,0 +1,235 @@
+/*
+ * libsculptgpu — GB300 (sm_103a) implementation of the sculpt-brush dab path of
+ * Kielan/dune_sculpt behind a plain C ABI.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (SGPU_OK or an SGPU_ERR_* code); nothing aborts.  Device memory belongs to a
+ * mesh handle; host arrays passed in are read and copied.  A handle owns one
+ * CUDA stream and is not thread-safe; distinct handles may be used from
+ * distinct threads.  There is no CPU fallback: without a usable GB300 every
+ * compute entry point returns SGPU_ERR_CUDA.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   BKE_pbvh_new / BKE_pbvh_build_mesh / BKE_pbvh_build_grids / BKE_pbvh_free
+ *       source/dune/kernel/intern/pbvh.c:2563, :2452, :2516, :2570
+ *   BKE_pbvh_search_gather (sphere callback)     pbvh.c:2736-2767
+ *   do_draw/smooth/inflate/clay_strips_brush     absent in the reference (its
+ *       sculpt.c is missing); signature shape do_X_brush(sd, ob, nodes, totnode)
+ *       is fixed here, with the brush math of the project's brush specification
+ *   BKE_pbvh_update_normals                      pbvh.c:4559-4587
+ *   BKE_pbvh_update_bounds                       pbvh.c:3319-3339
+ *   BKE_pbvh_node_mark_update                    pbvh.c:3641-3645
+ *   BKE_pbvh_node_get_BB / _get_original_BB      pbvh.c:3830-3840
+ *   KERNEL_curvemapping_evaluateF (brush falloff) colortools.c:942-980
+ */
+#ifndef SCULPT_GPU_H
+#define SCULPT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SGPU_OK 0
+#define SGPU_ERR_INVALID_ARG 1
+#define SGPU_ERR_OOM 2
+#define SGPU_ERR_CUDA 3
+#define SGPU_ERR_TIMEOUT 4
+#define SGPU_ERR_BOUNDS 5
+#define SGPU_ERR_UNSUPPORTED 6
+
+/* ---- element layouts (source/dune/types/types_meshdata.h) ---- */
+typedef struct SGPU_MVert { /* MVert, types_meshdata.h:13-17 */
+  float co[3];
+  char flag, bweight;
+  char _pad[2];
+} SGPU_MVert;
+
+typedef struct SGPU_MPoly { /* MPoly, types_meshdata.h:50-56 */
+  int loopstart;
+  int totloop;
+  short mat_nr;
+  char flag, _pad;
+} SGPU_MPoly;
+
+typedef struct SGPU_MLoop { /* MLoop, types_meshdata.h:69-74 */
+  unsigned int v;
+  unsigned int e;
+} SGPU_MLoop;
+
+typedef struct SGPU_MLoopTri { /* MLoopTri, types_meshdata.h:178-181 */
+  unsigned int tri[3];
+  unsigned int poly;
+} SGPU_MLoopTri;
+
+/* ---- PBVHNodeFlags (values the reference's pbvh.c relies on) ---- */
+#define SGPU_PBVH_Leaf 1
+#define SGPU_PBVH_UpdateNormals 2
+#define SGPU_PBVH_UpdateBB 4
+#define SGPU_PBVH_UpdateOriginalBB 8
+#define SGPU_PBVH_UpdateDrawBuffers 16
+#define SGPU_PBVH_UpdateRedraw 32
+
+/* ---- brush (subset of Brush, types_brush.h:138-362) ---- */
+#define SGPU_TOOL_DRAW 1         /* SCULPT_TOOL_DRW */
+#define SGPU_TOOL_SMOOTH 2       /* SCULPT_TOOL_SMOOTH */
+#define SGPU_TOOL_INFLATE 4      /* SCULPT_TOOL_INFLATE */
+#define SGPU_TOOL_CLAY_STRIPS 18 /* SCULPT_TOOL_CLAY_STRIPS */
+#define SGPU_BRUSH_FRONTFACE (1 << 27)
+#define SGPU_SYMM_X 1 /* PAINT_SYMM_X, types_scene.h:2174 */
+#define SGPU_SYMM_Y 2
+#define SGPU_SYMM_Z 4
+#define SGPU_CURVE_PRESET_LINE 0
+#define SGPU_CURVE_PRESET_SHARP 1
+#define SGPU_CURVE_PRESET_SMOOTH 2
+#define SGPU_CURVE_PRESET_MAX 3
+#define SGPU_CURVE_PRESET_ROUND 5
+#define SGPU_CURVE_PRESET_ROOT 6
+
+typedef struct SGPU_Brush {
+  int sculpt_tool;            /* SGPU_TOOL_* */
+  int flag;                   /* SGPU_BRUSH_FRONTFACE or 0 */
+  int symmetry;               /* SGPU_SYMM_* bits */
+  int curve_preset;           /* falloff curve, SGPU_CURVE_PRESET_* */
+  float radius;               /* object-space radius */
+  float strength;             /* bstrength */
+  float normal_radius_factor; /* default 0.5 (types_brush_defaults.h:25) */
+  float area_radius_factor;   /* default 0.5 (types_brush_defaults.h:27) */
+  float plane_offset;         /* clay strips plane offset */
+  float view_normal[3];       /* front-face reference direction */
+  int use_original_bb;        /* cull against orig_vb instead of vb */
+} SGPU_Brush;
+
+/* One dab of a stroke: location and grab delta (stroke direction). */
+typedef struct SGPU_Dab {
+  float location[3];
+  float grab_delta[3];
+} SGPU_Dab;
+
+typedef struct SGPU_MeshInfo {
+  int type; /* 0 PBVH_FACES, 1 PBVH_GRIDS */
+  int totvert; /* vertices, or grid elements */
+  int totnode;
+  int totleaf;
+  int leaf_limit;
+  int totprim;
+  int leaf_vert_entries; /* FACES: total vert_indices entries over leaves */
+  int grid_size;
+} SGPU_MeshInfo;
+
+typedef struct SGPU_StrokeStats {
+  int64_t verts_displaced; /* sum over dabs and symmetry passes of verts moved */
+  float gpu_ms;            /* CUDA-event time of the stroke on the mesh stream */
+  int kernel_launches;     /* kernels launched by the library for the stroke */
+  int graph_nodes;         /* nodes of the captured graph (graph mode) */
+} SGPU_StrokeStats;
+
+typedef struct sgpu_mesh sgpu_mesh;
+
+/* ---- library ---- */
+const char *sgpu_version(void);
+const char *sgpu_last_error(void);
+int sgpu_device_info(int *sm_count, int *cc_major, int *cc_minor);
+
+/* ---- mesh lifetime ----
+ * BKE_pbvh_new + BKE_pbvh_build_mesh (pbvh.c:2452-2514).  vert_normals (3 floats
+ * per vertex) may be NULL: the normals are then computed by the normal update
+ * over every vertex.  mask (CD_PAINT_MASK, one float per vertex) and automask
+ * (one factor per vertex) may be NULL.  leaf_limit <= 0 selects the reference's
+ * LEAF_LIMIT (10000 primitives, pbvh.c:1950). */
+int sgpu_mesh_create_faces(const SGPU_MVert *verts, int totvert, const SGPU_MPoly *polys,
+                           int totpoly, const SGPU_MLoop *loops, int totloop,
+                           const SGPU_MLoopTri *looptris, int totlooptri,
+                           const float *vert_normals, const float *mask, const float *automask,
+                           int leaf_limit, sgpu_mesh **r_mesh);
+
+/* BKE_pbvh_build_grids (pbvh.c:2516-2561) over grids in the CCG layout of
+ * subdiv_ccg.c:40-89 (co, mask, no per element; given here as separate arrays
+ * of num_grids*grid_size^2 elements).  The base topology gives the seam
+ * adjacency (subdiv_ccg.c:397-549): per face its first grid and corner count,
+ * per corner its base vertex and the base edge to the next corner, per base
+ * edge its two vertices.  grids_no may be NULL (computed). */
+int sgpu_mesh_create_grids(int num_grids, int grid_size, const float *grids_co,
+                           const float *grids_no, const float *grids_mask, int num_faces,
+                           const int *face_start, const int *face_ngrids, const int *face_verts,
+                           const int *face_edges, int num_base_verts, int num_base_edges,
+                           const int *edge_verts, int leaf_limit, sgpu_mesh **r_mesh);
+
+int sgpu_mesh_destroy(sgpu_mesh *mesh); /* BKE_pbvh_free, pbvh.c:2570 */
+int sgpu_mesh_info(const sgpu_mesh *mesh, SGPU_MeshInfo *r_info);
+int sgpu_mesh_sync(sgpu_mesh *mesh);
+void *sgpu_mesh_stream(sgpu_mesh *mesh); /* the handle's cudaStream_t */
+
+/* ---- per-call entry points (one reference call each) ---- */
+
+/* BKE_pbvh_search_gather with the sphere callback: leaves whose box (vb, or
+ * orig_vb when original != 0) is closer than sqrt(radius_sq) to center, in the
+ * reference's left-first DFS order.  The list stays on the device as the
+ * mesh's current node list.  r_nodes (host, capacity >= totleaf) and r_tot may
+ * be NULL; when given they receive node indices and count (synchronises). */
+int sgpu_search_sphere(sgpu_mesh *mesh, const float center[3], float radius_sq, int original,
+                       int *r_nodes, int *r_tot);
+
+/* do_<tool>_brush(sd, ob, nodes, totnode) for one symmetry pass: location and
+ * grab_delta are already mirrored for the pass, as the reference's stroke
+ * cache does.  nodes == NULL uses the device list of the last search; otherwise
+ * the host list (node indices) is uploaded.  Marks the nodes for update
+ * (BKE_pbvh_node_mark_update) and tags the moved vertices (vert_bitmap). */
+int sgpu_do_draw_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                       const float grab_delta[3], const int *nodes, int totnode);
+int sgpu_do_smooth_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                         const float grab_delta[3], const int *nodes, int totnode);
+int sgpu_do_inflate_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                          const float grab_delta[3], const int *nodes, int totnode);
+int sgpu_do_clay_strips_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                              const float grab_delta[3], const int *nodes, int totnode);
+/* Dispatch on brush->sculpt_tool. */
+int sgpu_do_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                  const float grab_delta[3], const int *nodes, int totnode);
+
+/* BKE_pbvh_update_normals (FACES: tagged vertices of flagged leaves; GRIDS:
+ * inner grid normals of the affected faces plus seam stitching). */
+int sgpu_pbvh_update_normals(sgpu_mesh *mesh);
+/* BKE_pbvh_update_bounds(pbvh, flag) with SGPU_PBVH_Update* bits. */
+int sgpu_pbvh_update_bounds(sgpu_mesh *mesh, int flag);
+/* BKE_pbvh_node_mark_update on one node index. */
+int sgpu_pbvh_node_mark_update(sgpu_mesh *mesh, int node);
+
+/* ---- whole strokes ----
+ * Per dab: for every enabled symmetry pass the sphere search and the brush,
+ * then the normal update and update_bounds(UpdateBB); update_bounds(
+ * UpdateOriginalBB) once at the end.  dab_tools (nullable) overrides the tool
+ * per dab (mixed strokes).  mode: 0 = launched call by call, 1 = the stroke
+ * captured once as a CUDA graph and replayed.  stats may be NULL. */
+#define SGPU_STROKE_EAGER 0
+#define SGPU_STROKE_GRAPH 1
+int sgpu_stroke(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, int ndabs,
+                const int *dab_tools, int mode, SGPU_StrokeStats *stats);
+
+/* ---- data access (synchronous) ---- */
+int sgpu_get_verts(sgpu_mesh *mesh, SGPU_MVert *out);          /* FACES */
+int sgpu_set_verts(sgpu_mesh *mesh, const SGPU_MVert *verts);  /* FACES */
+int sgpu_get_positions(sgpu_mesh *mesh, float *out_xyz);       /* 3 floats per vertex/element */
+int sgpu_set_positions(sgpu_mesh *mesh, const float *xyz);
+int sgpu_get_normals(sgpu_mesh *mesh, float *out_xyz);
+int sgpu_get_mask(sgpu_mesh *mesh, float *out);
+/* Node bounding boxes, 6 floats each (min xyz, max xyz), reference node order. */
+int sgpu_get_node_bbs(sgpu_mesh *mesh, float *vb, float *orig_vb);
+/* Node table in reference order: children_offset (-1 for leaves), flag,
+ * prim_off/totprim (leaves), uniq_verts, face_verts, vert_off (FACES leaves). */
+int sgpu_get_nodes(sgpu_mesh *mesh, int *children_offset, int *flag, int *prim_off, int *totprim,
+                   int *uniq_verts, int *face_verts, int *vert_off);
+int sgpu_get_prim_indices(sgpu_mesh *mesh, int *out);
+int sgpu_get_vert_indices(sgpu_mesh *mesh, int *out);
+
+/* Brush falloff table (curvemap_make_table, colortools.c:597-771) for a preset:
+ * 257 (x, y) pairs and {mintable, maxtable, range, ext_in[2], ext_out[2]}. */
+int sgpu_curve_table(int preset, float *table_xy, float *params);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCULPT_GPU_H */

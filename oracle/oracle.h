@@ -1,0 +1,110 @@
+/*
+ * CPU oracle for the sculpt-brush dab path — TEST INFRASTRUCTURE ONLY.
+ *
+ * This library is the checker: a plain-C restatement of the reference's PBVH
+ * build, node search, vertex-normal update, bounding-box refit and falloff-curve
+ * tables (Kielan/dune_sculpt, source/dune/kernel/intern/pbvh.c, colortools.c,
+ * mesh_evaluate.c, subdiv_ccg.c; lib/intern/math_*), plus the brush math the
+ * reference lacks (its sculpt.c is absent), written from the project's brush
+ * specification.  Every arithmetic step runs twice: once in FP32 (the parity
+ * target of the GPU path, bit-for-bit) and once in FP64 (the error reference).
+ *
+ * Only tests, the smoke check and the benchmark's CPU-baseline leg may load it.
+ * The GPU product never links or calls it.
+ *
+ * Parity pinning: the reference ships no tests, fixtures or golden vectors for
+ * this path and cannot be compiled (its public headers are missing), so parity
+ * of this restatement against the reference itself is unpinned; it is pinned
+ * against known-answer tests written from the reference's own definitions.
+ */
+#ifndef ORACLE_H
+#define ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct OrMesh OrMesh;
+
+/* Field order matches SGPU_Brush in include/sculpt_gpu.h. */
+typedef struct OrBrush {
+  int sculpt_tool; /* 1 draw, 2 smooth, 4 inflate, 18 clay strips (eBrushSculptTool) */
+  int flag;        /* eBrushFlags subset: BRUSH_FRONTFACE (1 << 27) */
+  int symmetry;    /* PAINT_SYMM_X | _Y | _Z */
+  int curve_preset;
+  float radius;
+  float strength;
+  float normal_radius_factor;
+  float area_radius_factor;
+  float plane_offset;
+  float view_normal[3];
+  int use_original_bb;
+} OrBrush;
+
+/* ---- mesh (PBVH_FACES) ---- */
+OrMesh *or_mesh_create_faces(const void *mverts, int totvert, const void *mpolys, int totpoly,
+                             const void *mloops, int totloop, const void *looptris, int totlt,
+                             const float *mask, const float *automask, int leaf_limit);
+void or_mesh_free(OrMesh *m);
+
+/* ---- mesh (PBVH_GRIDS) ----
+ * grids_co/no: num_grids*grid_size^2*3 floats, mask: num_grids*grid_size^2 (nullable).
+ * face_start/face_ngrids: per base face, first grid and corner count.
+ * face_verts/face_edges: per face corner, base vertex / base edge (edge i joins corner i, i+1).
+ * edge_verts: per base edge, its two base vertices. */
+OrMesh *or_mesh_create_grids(int num_grids, int grid_size, const float *grids_co,
+                             const float *grids_no, const float *grids_mask, int num_faces,
+                             const int *face_start, const int *face_ngrids, const int *face_verts,
+                             const int *face_edges, int num_base_verts, int num_base_edges,
+                             const int *edge_verts, int leaf_limit);
+
+int or_num_nodes(const OrMesh *m);
+int or_num_leaves(const OrMesh *m);
+int or_num_verts(const OrMesh *m);
+void or_get_nodes(const OrMesh *m, int *children_offset, int *flag, int *prim_off, int *totprim,
+                  int *uniq, int *face_verts, int *vert_off);
+void or_get_prim_indices(const OrMesh *m, int *out);
+int or_num_leaf_vert_entries(const OrMesh *m);
+void or_get_vert_indices(const OrMesh *m, int *out);
+void or_get_bbs(const OrMesh *m, float *vb, float *orig_vb);
+void or_get_bbs64(const OrMesh *m, double *vb, double *orig_vb);
+void or_get_co(const OrMesh *m, float *out);
+void or_get_no(const OrMesh *m, float *out);
+void or_get_mask(const OrMesh *m, float *out);
+void or_get_co64(const OrMesh *m, double *out);
+void or_get_no64(const OrMesh *m, double *out);
+void or_set_co(OrMesh *m, const float *co);
+
+/* Left-first DFS node search with the sphere callback; returns the count. */
+int or_search_sphere(OrMesh *m, const float center[3], float radius_sq, int original,
+                     int *out_nodes);
+
+/* Initial normals: every vertex tagged, every leaf flagged, one normal update. */
+void or_recalc_all_normals(OrMesh *m);
+
+/* Single steps, FP32 state (tests of the fine-grained entry points). */
+int or_brush_pass(OrMesh *m, const OrBrush *b, const float location[3],
+                  const float grab_delta[3], const int *nodes, int totnode, float *area_out);
+void or_update_normals(OrMesh *m);
+void or_update_bounds(OrMesh *m, int flag);
+void or_node_mark_update(OrMesh *m, int node);
+
+/* Whole stroke: per dab, symmetry passes (search + brush), normals, bounds(UpdateBB);
+ * bounds(UpdateOriginalBB) at the end.  which: 1 = FP32, 2 = FP64, 3 = both.
+ * Returns vertices displaced (FP32 run if it ran).  dabs: ndabs * 6 floats;
+ * dab_tools (nullable) overrides the tool per dab. */
+int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
+                  const int *dab_tools, int which, int nthreads, int64_t *per_dab_counts);
+
+/* Falloff curve of a brush preset (colortools.c): table 257*(x,y), params
+ * {mintable, maxtable, range, ext_in[2], ext_out[2]}. */
+void or_curve_table(int preset, float *table_xy, float *params);
+float or_curve_strength(int preset, float dist, float radius);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,111 @@
+/*
+ * CPU oracle, part 2: the numeric core instantiated in FP32 and FP64, and the
+ * exported entry points.  TEST INFRASTRUCTURE ONLY (see oracle.h).
+ */
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "oracle_internal.h"
+
+void or_curve_build(int preset, OrCurve *cu);
+
+#define REAL float
+#define SFX(n) n##_f
+#define STATE OrStateF
+#define RSQRT sqrtf
+#define RFABS fabsf
+#include "oracle_core.inc"
+#undef REAL
+#undef SFX
+#undef STATE
+#undef RSQRT
+#undef RFABS
+
+#define REAL double
+#define SFX(n) n##_d
+#define STATE OrStateD
+#define RSQRT sqrt
+#define RFABS fabs
+#include "oracle_core.inc"
+#undef REAL
+#undef SFX
+#undef STATE
+#undef RSQRT
+#undef RFABS
+
+int or_search_sphere(OrMesh *m, const float center[3], float radius_sq, int original,
+                     int *out_nodes)
+{
+  return search_f(m, &m->sf, 0, center, radius_sq, original, 0, out_nodes);
+}
+
+void or_recalc_all_normals(OrMesh *m)
+{
+  recalc_all_normals_f(m, &m->sf);
+  recalc_all_normals_d(m, &m->sd);
+}
+
+int or_brush_pass(OrMesh *m, const OrBrush *b, const float location[3],
+                  const float grab_delta[3], const int *nodes, int totnode, float *area_out)
+{
+  OrCurve cu;
+  or_curve_build(b->curve_preset, &cu);
+  return (int)brush_pass_f(m, &m->sf, &cu, b, location, grab_delta, b->view_normal, nodes,
+                           totnode, area_out);
+}
+
+void or_update_normals(OrMesh *m) { update_normals_f(m, &m->sf); }
+
+void or_update_bounds(OrMesh *m, int flag) { update_bounds_f(m, &m->sf, flag); }
+
+void or_node_mark_update(OrMesh *m, int node)
+{
+  if (node >= 0 && node < m->totnode) {
+    mark_nodes_f(m, &node, 1);
+  }
+}
+
+int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
+                  const int *dab_tools, int which, int nthreads, int64_t *per_dab_counts)
+{
+#ifdef _OPENMP
+  if (nthreads > 0) {
+    omp_set_num_threads(nthreads);
+  }
+#else
+  (void)nthreads;
+#endif
+  int64_t total = 0;
+  if (which & 1) {
+    total = stroke_f(m, &m->sf, b, dabs, ndabs, dab_tools, per_dab_counts);
+  }
+  if (which & 2) {
+    const int64_t t64 =
+        stroke_d(m, &m->sd, b, dabs, ndabs, dab_tools, (which & 1) ? NULL : per_dab_counts);
+    if (!(which & 1)) {
+      total = t64;
+    }
+  }
+  return total;
+}
+
+float or_curve_strength(int preset, float dist, float radius)
+{
+  OrCurve cu;
+  or_curve_build(preset, &cu);
+  return curve_strength_f(&cu, dist, radius);
+}
+
+int or_max_threads(void)
+{
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

@@ -1,0 +1,261 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: loaded by tests/, the smoke check and the CPU
+baseline leg of bench.py, never by the GPU product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+class OrBrush(C.Structure):
+    _fields_ = [("sculpt_tool", C.c_int), ("flag", C.c_int), ("symmetry", C.c_int),
+                ("curve_preset", C.c_int), ("radius", C.c_float), ("strength", C.c_float),
+                ("normal_radius_factor", C.c_float), ("area_radius_factor", C.c_float),
+                ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
+                ("use_original_bb", C.c_int)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = C.CDLL(_LIB_PATH)
+        vp, i, f = C.c_void_p, C.c_int, C.c_float
+        L.or_mesh_create_faces.restype = vp
+        L.or_mesh_create_faces.argtypes = [vp, i, vp, i, vp, i, vp, i, vp, vp, i]
+        L.or_mesh_create_grids.restype = vp
+        L.or_mesh_create_grids.argtypes = [i, i, vp, vp, vp, i, vp, vp, vp, vp, i, i, vp, i]
+        L.or_mesh_free.argtypes = [vp]
+        for name in ("or_num_nodes", "or_num_leaves", "or_num_verts", "or_num_leaf_vert_entries"):
+            getattr(L, name).restype = i
+            getattr(L, name).argtypes = [vp]
+        L.or_get_nodes.argtypes = [vp] + [vp] * 7
+        for name in ("or_get_prim_indices", "or_get_vert_indices", "or_get_co", "or_get_no",
+                     "or_get_mask", "or_get_co64", "or_get_no64", "or_set_co"):
+            getattr(L, name).argtypes = [vp, vp]
+        L.or_get_bbs.argtypes = [vp, vp, vp]
+        L.or_get_bbs64.argtypes = [vp, vp, vp]
+        L.or_search_sphere.restype = i
+        L.or_search_sphere.argtypes = [vp, vp, f, i, vp]
+        L.or_recalc_all_normals.argtypes = [vp]
+        L.or_brush_pass.restype = i
+        L.or_brush_pass.argtypes = [vp, C.POINTER(OrBrush), vp, vp, vp, i, vp]
+        L.or_update_normals.argtypes = [vp]
+        L.or_update_bounds.argtypes = [vp, i]
+        L.or_node_mark_update.argtypes = [vp, i]
+        L.or_stroke.restype = C.c_int64
+        L.or_stroke.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
+        L.or_curve_table.argtypes = [i, vp, vp]
+        L.or_curve_strength.restype = f
+        L.or_curve_strength.argtypes = [i, f, f]
+        L.or_max_threads.restype = i
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def make_brush(st) -> OrBrush:
+    b = OrBrush()
+    b.sculpt_tool = st.tool
+    b.flag = st.flag
+    b.symmetry = st.symmetry
+    b.curve_preset = st.curve_preset
+    b.radius = st.radius
+    b.strength = st.strength
+    b.normal_radius_factor = st.normal_radius_factor
+    b.area_radius_factor = st.area_radius_factor
+    b.plane_offset = st.plane_offset
+    for k in range(3):
+        b.view_normal[k] = st.view_normal[k]
+    b.use_original_bb = st.use_original_bb
+    return b
+
+
+class OracleMesh:
+    """The oracle's mirror of one PBVH (FP32 and FP64 states)."""
+
+    def __init__(self, handle, keep):
+        self.h = handle
+        self._keep = keep
+
+    @classmethod
+    def faces(cls, m, leaf_limit: int, automask=None):
+        L = lib()
+        mask = None if m.mask is None else np.ascontiguousarray(m.mask, dtype=np.float32)
+        am = None if automask is None else np.ascontiguousarray(automask, dtype=np.float32)
+        h = L.or_mesh_create_faces(_p(m.verts), m.verts.shape[0], _p(m.polys), m.polys.shape[0],
+                                   _p(m.loops), m.loops.shape[0], _p(m.looptris),
+                                   m.looptris.shape[0], _p(mask), _p(am), leaf_limit)
+        return cls(h, (m, mask, am))
+
+    @classmethod
+    def grids(cls, g, leaf_limit: int = 0, normals=None):
+        L = lib()
+        co = np.ascontiguousarray(g.co, dtype=np.float32)
+        no = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32)
+        mask = None if g.mask is None else np.ascontiguousarray(g.mask, dtype=np.float32)
+        fs = np.ascontiguousarray(g.face_start, dtype=np.int32)
+        fn = np.ascontiguousarray(g.face_ngrids, dtype=np.int32)
+        fv = np.ascontiguousarray(g.face_verts, dtype=np.int32)
+        fe = np.ascontiguousarray(g.face_edges, dtype=np.int32)
+        ev = np.ascontiguousarray(g.edge_verts, dtype=np.int32)
+        h = L.or_mesh_create_grids(g.num_grids, g.grid_size, _p(co), _p(no), _p(mask),
+                                   g.num_faces, _p(fs), _p(fn), _p(fv), _p(fe),
+                                   g.num_base_verts, ev.shape[0], _p(ev), leaf_limit)
+        return cls(h, (co, no, mask, fs, fn, fv, fe, ev))
+
+    def close(self):
+        if self.h:
+            lib().or_mesh_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_nodes(self) -> int:
+        return lib().or_num_nodes(self.h)
+
+    @property
+    def num_leaves(self) -> int:
+        return lib().or_num_leaves(self.h)
+
+    @property
+    def num_verts(self) -> int:
+        return lib().or_num_verts(self.h)
+
+    def nodes(self) -> dict:
+        n = self.num_nodes
+        arrs = {k: np.zeros(n, dtype=np.int32) for k in
+                ("children_offset", "flag", "prim_off", "totprim", "uniq", "face_verts",
+                 "vert_off")}
+        lib().or_get_nodes(self.h, *[_p(arrs[k]) for k in
+                                     ("children_offset", "flag", "prim_off", "totprim", "uniq",
+                                      "face_verts", "vert_off")])
+        return arrs
+
+    def prim_indices(self) -> np.ndarray:
+        nd = self.nodes()
+        tot = int(nd["totprim"].sum())
+        out = np.zeros(max(tot, 1), dtype=np.int32)
+        lib().or_get_prim_indices(self.h, _p(out))
+        return out[:tot]
+
+    def vert_indices(self) -> np.ndarray:
+        n = lib().or_num_leaf_vert_entries(self.h)
+        out = np.zeros(max(n, 1), dtype=np.int32)
+        lib().or_get_vert_indices(self.h, _p(out))
+        return out[:n]
+
+    def bbs(self):
+        n = self.num_nodes
+        vb = np.zeros((n, 6), dtype=np.float32)
+        ovb = np.zeros((n, 6), dtype=np.float32)
+        lib().or_get_bbs(self.h, _p(vb), _p(ovb))
+        return vb, ovb
+
+    def bbs64(self):
+        n = self.num_nodes
+        vb = np.zeros((n, 6), dtype=np.float64)
+        ovb = np.zeros((n, 6), dtype=np.float64)
+        lib().or_get_bbs64(self.h, _p(vb), _p(ovb))
+        return vb, ovb
+
+    def co(self) -> np.ndarray:
+        out = np.zeros((self.num_verts, 3), dtype=np.float32)
+        lib().or_get_co(self.h, _p(out))
+        return out
+
+    def no(self) -> np.ndarray:
+        out = np.zeros((self.num_verts, 3), dtype=np.float32)
+        lib().or_get_no(self.h, _p(out))
+        return out
+
+    def mask(self) -> np.ndarray:
+        out = np.zeros(self.num_verts, dtype=np.float32)
+        lib().or_get_mask(self.h, _p(out))
+        return out
+
+    def co64(self) -> np.ndarray:
+        out = np.zeros((self.num_verts, 3), dtype=np.float64)
+        lib().or_get_co64(self.h, _p(out))
+        return out
+
+    def no64(self) -> np.ndarray:
+        out = np.zeros((self.num_verts, 3), dtype=np.float64)
+        lib().or_get_no64(self.h, _p(out))
+        return out
+
+    def set_co(self, co: np.ndarray):
+        co = np.ascontiguousarray(co, dtype=np.float32)
+        lib().or_set_co(self.h, _p(co))
+
+    def search_sphere(self, center, radius_sq: float, original: int = 0) -> np.ndarray:
+        out = np.zeros(self.num_nodes + 1, dtype=np.int32)
+        c = np.asarray(center, dtype=np.float32)
+        n = lib().or_search_sphere(self.h, _p(c), radius_sq, original, _p(out))
+        return out[:n]
+
+    def recalc_all_normals(self):
+        lib().or_recalc_all_normals(self.h)
+
+    def brush_pass(self, st, location, grab_delta, nodes) -> tuple[int, np.ndarray]:
+        b = make_brush(st)
+        loc = np.asarray(location, dtype=np.float32)
+        gd = np.asarray(grab_delta, dtype=np.float32)
+        nd = np.ascontiguousarray(nodes, dtype=np.int32)
+        area = np.zeros(6, dtype=np.float32)
+        n = lib().or_brush_pass(self.h, C.byref(b), _p(loc), _p(gd), _p(nd), nd.shape[0],
+                                _p(area))
+        return n, area
+
+    def update_normals(self):
+        lib().or_update_normals(self.h)
+
+    def update_bounds(self, flag: int):
+        lib().or_update_bounds(self.h, flag)
+
+    def stroke(self, st, which: int = 3, nthreads: int = 0, dabs=None, dab_tools=None):
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        per = np.zeros(d.shape[0], dtype=np.int64)
+        tot = lib().or_stroke(self.h, C.byref(b), _p(d), d.shape[0], _p(tools), which, nthreads,
+                              _p(per))
+        return int(tot), per
+
+
+def curve_table(preset: int):
+    t = np.zeros((257, 2), dtype=np.float32)
+    p = np.zeros(7, dtype=np.float32)
+    lib().or_curve_table(preset, _p(t), _p(p))
+    return t, p
+
+
+def curve_strength(preset: int, dist: float, radius: float) -> float:
+    return float(lib().or_curve_strength(preset, dist, radius))
+
+
+def max_threads() -> int:
+    return int(lib().or_max_threads())

@@ -1,0 +1,201 @@
+"""GPU parity: libsculptgpu against the CPU oracle on the same seeded inputs.
+
+Node tables, node lists, indices and bounding boxes must match bit for bit;
+positions and normals must match the FP32 restatement bit for bit (the GPU
+kernels evaluate every formula in the same order with separately rounded
+operations), and stay within 1e-6 norm-wise relative error of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from dune_sculpt_gb300 import synth
+from dune_sculpt_gb300.sculpt import (PBVH, PBVH_UpdateBB, PBVH_UpdateOriginalBB, STROKE_EAGER,
+                                      STROKE_GRAPH, SculptGPUError)
+
+from helpers import bits_equal, first_diff, rel_err, small_grid, small_icosphere, small_uvsphere
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-6  # positions vs the FP64 oracle, norm-wise relative
+
+
+def _cases():
+    return {
+        "grid": (small_grid(48), 300),
+        "icosphere": (small_icosphere(4), 200),
+        "uvsphere": (small_uvsphere(64), 300),
+    }
+
+
+@pytest.fixture(params=["grid", "icosphere", "uvsphere"])
+def case(request):
+    m, ll = _cases()[request.param]
+    return request.param, m, ll
+
+
+def _pair(gpu, oracle, m, ll):
+    g = PBVH.build_mesh(m, ll)
+    o = oracle.OracleMesh.faces(m, ll)
+    o.recalc_all_normals()
+    return g, o
+
+
+def _assert_state_equal(g, o, what=""):
+    assert bits_equal(g.positions(), o.co()), what + " positions: " + first_diff(g.positions(), o.co())
+    assert bits_equal(g.normals(), o.no()), what + " normals: " + first_diff(g.normals(), o.no())
+    gvb, govb = g.bbs()
+    ovb, oovb = o.bbs()
+    assert bits_equal(gvb, ovb), what + " vb: " + first_diff(gvb, ovb)
+    assert bits_equal(govb, oovb), what + " orig_vb: " + first_diff(govb, oovb)
+
+
+def test_build_matches_oracle(gpu, oracle, case):
+    name, m, ll = case
+    g, o = _pair(gpu, oracle, m, ll)
+    gn, on = g.nodes(), o.nodes()
+    for k in ("children_offset", "prim_off", "totprim", "uniq", "face_verts", "vert_off"):
+        assert np.array_equal(gn[k], on[k]), (name, k)
+    assert np.array_equal(gn["flag"] & 1, on["flag"] & 1)
+    assert np.array_equal(g.prim_indices(), o.prim_indices())
+    assert np.array_equal(g.vert_indices(), o.vert_indices())
+    _assert_state_equal(g, o, name)
+
+
+def test_search_matches_oracle(gpu, oracle, case):
+    name, m, ll = case
+    g, o = _pair(gpu, oracle, m, ll)
+    rng = np.random.default_rng(11)
+    co = o.co()
+    for trial in range(60):
+        if trial % 3 == 0:
+            c = co[rng.integers(0, co.shape[0])]
+        else:
+            c = rng.uniform(-1.2, 1.2, size=3).astype(np.float32)
+        r = np.float32(rng.choice([0.0, 1e-4, 0.03, 0.1, 0.4, 5.0]))
+        rsq = float(np.float32(r * r))
+        for original in (0, 1):
+            got = g.search_gather_sphere(c, rsq, original)
+            want = o.search_sphere(c, rsq, original)
+            assert np.array_equal(got, want), (name, trial, c, r)
+    # far away: empty list
+    assert g.search_gather_sphere([50, 50, 50], 0.01).size == 0
+
+
+TOOLS = [synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS]
+
+
+@pytest.mark.parametrize("tool", TOOLS)
+def test_single_pass_per_tool(gpu, oracle, case, tool):
+    """One reference-style call sequence: search, do_<tool>_brush, update
+    normals, update bounds."""
+    name, m, ll = case
+    g, o = _pair(gpu, oracle, m, ll)
+    co = o.co()
+    rng = np.random.default_rng(tool)
+    radius = 0.12
+    st = synth.Stroke(tool, radius, 0.6, synth.CURVE_SMOOTH, 0, None)
+    for step in range(4):
+        c = co[rng.integers(0, co.shape[0])]
+        delta = rng.normal(size=3).astype(np.float32)
+        scale = np.float32(1.41421356237309504880) if tool == synth.TOOL_CLAY_STRIPS else np.float32(1)
+        rr = np.float32(np.float32(radius) * scale)
+        rsq = float(np.float32(rr * rr))
+        nodes = o.search_sphere(c, rsq)
+        g.search_sphere_device(c, rsq)
+        o.brush_pass(st, c, delta, nodes)
+        g.do_brush(st, c, delta)  # device node list of the last search
+        assert bits_equal(g.positions(), o.co()), (name, step, first_diff(g.positions(), o.co()))
+        g.update_normals()
+        o.update_normals()
+        g.update_bounds(PBVH_UpdateBB)
+        o.update_bounds(PBVH_UpdateBB)
+        _assert_state_equal(g, o, f"{name} step {step}")
+        assert np.array_equal(g.nodes()["flag"] & 15, o.nodes()["flag"] & 15)
+    g.update_bounds(PBVH_UpdateOriginalBB)
+    o.update_bounds(PBVH_UpdateOriginalBB)
+    _assert_state_equal(g, o, name + " final")
+
+
+def test_host_node_list_and_errors(gpu, oracle):
+    m, ll = small_icosphere(4), 200
+    g, o = _pair(gpu, oracle, m, ll)
+    st = synth.Stroke(synth.TOOL_INFLATE, 0.2, 0.5, synth.CURVE_SHARP, 0, None)
+    c = o.co()[17]
+    nodes = o.search_sphere(c, 0.09)
+    o.brush_pass(st, c, [1, 0, 0], nodes)
+    g.do_inflate_brush(st, c, [1, 0, 0], nodes=nodes)
+    assert bits_equal(g.positions(), o.co())
+    # an empty list moves nothing
+    before = g.positions()
+    g.do_inflate_brush(st, c, [1, 0, 0], nodes=np.zeros(0, dtype=np.int32))
+    assert bits_equal(g.positions(), before)
+    # an internal node is rejected with an error code
+    internal = int(np.nonzero(g.nodes()["children_offset"] >= 0)[0][0])
+    with pytest.raises(SculptGPUError) as e:
+        g.do_inflate_brush(st, c, [1, 0, 0], nodes=np.array([internal], dtype=np.int32))
+    assert e.value.code == 1
+    with pytest.raises(SculptGPUError):
+        g.node_mark_update(10 ** 6)
+
+
+@pytest.mark.parametrize("tool", TOOLS)
+@pytest.mark.parametrize("mode", [STROKE_EAGER, STROKE_GRAPH])
+def test_stroke_parity(gpu, oracle, case, tool, mode):
+    name, m, ll = case
+    g, o = _pair(gpu, oracle, m, ll)
+    if name == "grid":
+        dabs = synth.line_dabs(5, 24)
+    else:
+        dabs = synth.arc_dabs(5, 24, 0.03)
+    st = synth.Stroke(tool, 0.1, 0.7, synth.CURVE_SMOOTH if tool != synth.TOOL_CLAY_STRIPS
+                      else synth.CURVE_SHARP, synth.SYMM_X, dabs)
+    stats = g.stroke(st, mode=mode)
+    tot, _ = o.stroke(st, which=3)
+    assert stats.verts_displaced == tot
+    _assert_state_equal(g, o, f"{name} tool {tool} mode {mode}")
+    assert rel_err(g.positions(), o.co64()) < FP64_TOL
+    assert stats.kernel_launches > 0
+    if mode == STROKE_GRAPH:
+        # replaying the cached graph reproduces the eager result of a second stroke
+        stats2 = g.stroke(st, mode=mode)
+        tot2, _ = o.stroke(st, which=1)
+        assert stats2.verts_displaced == tot2
+        _assert_state_equal(g, o, f"{name} replay")
+
+
+def test_full_mask_moves_nothing(gpu, oracle):
+    m = small_icosphere(4, masked=False)
+    m.mask = np.ones(m.totvert, dtype=np.float32)
+    g = PBVH.build_mesh(m, 200)
+    before = g.positions()
+    for tool in TOOLS:
+        st = synth.Stroke(tool, 0.2, 0.9, synth.CURVE_SMOOTH, synth.SYMM_X,
+                          synth.arc_dabs(7, 6, 0.05))
+        stats = g.stroke(st, mode=STROKE_EAGER)
+        assert stats.verts_displaced == 0
+    assert bits_equal(g.positions(), before)
+
+
+def test_frontface_and_automask(gpu, oracle):
+    m = small_icosphere(4)
+    am = synth._f32(synth.hash_u01(3, 3, np.arange(m.totvert)))
+    g = PBVH.build_mesh(m, 200, automask=am)
+    o = oracle.OracleMesh.faces(m, 200, automask=am)
+    o.recalc_all_normals()
+    st = synth.Stroke(synth.TOOL_DRAW, 0.15, 0.8, synth.CURVE_SMOOTH, synth.SYMM_X,
+                      synth.arc_dabs(9, 16, 0.04), flag=1 << 27, view_normal=(0.3, 0.5, 0.81))
+    stats = g.stroke(st, mode=STROKE_GRAPH)
+    tot, _ = o.stroke(st, which=1)
+    assert stats.verts_displaced == tot
+    _assert_state_equal(g, o, "frontface")
+
+
+def test_use_original_bb(gpu, oracle):
+    m = small_uvsphere(48)
+    g, o = _pair(gpu, oracle, m, 200)
+    st = synth.Stroke(synth.TOOL_INFLATE, 0.1, 0.9, synth.CURVE_SMOOTH, 0,
+                      synth.arc_dabs(13, 20, 0.02), use_original_bb=1)
+    stats = g.stroke(st, mode=STROKE_EAGER)
+    tot, _ = o.stroke(st, which=1)
+    assert stats.verts_displaced == tot
+    _assert_state_equal(g, o, "orig bb")
