@@ -58,6 +58,32 @@ struct sgpu_mesh {
   std::vector<unsigned char> gkey;
   int g_nodes = 0;
   int g_launches = 0;
+  // profiling: event pool and (kind, start, end) marks of the current stroke
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  struct Mark {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> prof_marks;
+  // snapshot (per-stroke restore) and L2 flush buffers
+  float4* snap_co = nullptr;
+  float4* snap_no = nullptr;
+  float* snap_mask = nullptr;
+  float4* snap_vb = nullptr;
+  float4* snap_orig_vb = nullptr;
+  int* snap_flag = nullptr;
+  void* flush_buf = nullptr;
+
+  cudaEvent_t prof_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
 
   template <class T>
   int alloc(T** out, size_t count) {
@@ -99,6 +125,8 @@ struct sgpu_mesh {
     allocs.clear();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+    ev_pool.clear();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -115,6 +143,7 @@ int ensure_device() {
     return fail(SGPU_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
   if (!g_configured) {
     configure_kernels();
+    configure_grid_kernels();
     g_configured = true;
   }
   return SGPU_OK;
@@ -224,17 +253,47 @@ bool tool_ok(int tool) {
          tool == kToolClayStrips;
 }
 
+// Launch bookkeeping: counts launches and, while profiling, brackets each one
+// with CUDA events on the mesh stream.
+struct Launcher {
+  sgpu_mesh* m;
+  int launches = 0;
+  template <class F>
+  int run(int kind, const char* what, F&& f) {
+    cudaEvent_t a = nullptr;
+    if (m->profiling) {
+      a = m->prof_event();
+      if (!a) return fail(SGPU_ERR_CUDA, "cudaEventCreate failed");
+      cudaEventRecord(a, m->stream);
+    }
+    const cudaError_t e = f();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (m->profiling) {
+      cudaEvent_t b = m->prof_event();
+      if (!b) return fail(SGPU_ERR_CUDA, "cudaEventCreate failed");
+      cudaEventRecord(b, m->stream);
+      m->prof_marks.push_back({kind, a, b});
+    }
+    launches++;
+    return SGPU_OK;
+  }
+};
+
+#define LAUNCH(L, kind, what, expr)                                \
+  do {                                                             \
+    const int _rc = (L).run((kind), (what), [&] { return (expr); }); \
+    if (_rc) return _rc;                                           \
+  } while (0)
+
 // Launches the brush of one pass over the current device node list.
-int launch_tool(sgpu_mesh* m, const DevBrush& b, PassParams pp, int* launches) {
-  const DevMesh& d = m->dev;
-  cudaStream_t s = m->stream;
+int launch_tool(Launcher& L, const DevBrush& b, PassParams pp) {
+  const DevMesh& d = L.m->dev;
+  cudaStream_t s = L.m->stream;
   if (b.tool == kToolDraw || b.tool == kToolClayStrips) {
-    CK(launch_area(d, b, pp, s), "area kernel");
-    CK(launch_brush(d, b, pp, s), "brush kernel");
-    *launches += 2;
+    LAUNCH(L, kKArea, "area kernel", launch_area(d, b, pp, s));
+    LAUNCH(L, kKBrush, "brush kernel", launch_brush(d, b, pp, s));
   } else if (b.tool == kToolInflate) {
-    CK(launch_brush(d, b, pp, s), "brush kernel");
-    *launches += 1;
+    LAUNCH(L, kKBrush, "brush kernel", launch_brush(d, b, pp, s));
   } else {
     // Smooth: 4 sub-steps per unit strength, the last one fractional.
     float st = b.strength;
@@ -245,30 +304,31 @@ int launch_tool(sgpu_mesh* m, const DevBrush& b, PassParams pp, int* launches) {
     for (int it = 0; it <= count; it++) {
       pp.iter_strength = (it != count) ? 1.0f : last;
       pp.iteration = it;
-      CK(launch_smooth_iteration(d, b, pp, s), "smooth kernels");
-      *launches += 2;
+      LAUNCH(L, kKSmoothCompute, "smooth kernel", launch_smooth_compute(d, b, pp, s));
+      LAUNCH(L, kKSmoothApply, "smooth kernel", launch_smooth_apply(d, s));
     }
   }
   return SGPU_OK;
 }
 
-int launch_update_normals(sgpu_mesh* m, int bounds_flag, int* launches) {
-  if (m->dev.type == kFaces) {
-    CK(launch_update_faces(m->dev, 1, bounds_flag, m->stream), "update kernel");
-    *launches += 1;
+int launch_update_normals(Launcher& L, int bounds_flag) {
+  const DevMesh& d = L.m->dev;
+  cudaStream_t s = L.m->stream;
+  if (d.type == kFaces) {
+    LAUNCH(L, kKUpdate, "update kernel", launch_update_faces(d, 1, bounds_flag, s));
   } else {
-    CK(launch_update_grids(m->dev, m->stream, launches), "grid update kernels");
-    if (bounds_flag) {
-      CK(launch_update_faces(m->dev, 0, bounds_flag, m->stream), "bounds kernel");
-      *launches += 1;
-    }
+    LAUNCH(L, kKGridGather, "grid gather kernel", launch_grid_gather(d, s));
+    LAUNCH(L, kKGridFaces, "grid face kernel", launch_grid_faces(d, s));
+    LAUNCH(L, kKGridSeams, "grid seam kernel", launch_grid_seams(d, s));
+    if (bounds_flag) LAUNCH(L, kKUpdate, "bounds kernel", launch_update_faces(d, 0, bounds_flag, s));
   }
   return SGPU_OK;
 }
 
 // Enqueues a whole stroke on the mesh stream.
-int enqueue_stroke(sgpu_mesh* m, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
-                   const int* dab_tools, int* launches) {
+int enqueue_stroke(Launcher& L, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+                   const int* dab_tools) {
+  sgpu_mesh* m = L.m;
   DevBrush base;
   if (!make_brush(brush, brush->sculpt_tool, &base))
     return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brush->curve_preset);
@@ -291,18 +351,20 @@ int enqueue_stroke(sgpu_mesh* m, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
       pp.cull_radius_sq = r * r;
       pp.original = brush->use_original_bb;
       pp.iter_strength = 1.0f;
-      CK(launch_cull(m->dev, pp, m->stream), "cull kernel");
-      *launches += 1;
-      int rc = launch_tool(m, base, pp, launches);
+      LAUNCH(L, kKCull, "cull kernel", launch_cull(m->dev, pp, m->stream));
+      const int rc = launch_tool(L, base, pp);
       if (rc) return rc;
     }
-    int rc = launch_update_normals(m, kUpdateBB, launches);
+    const int rc = launch_update_normals(L, kUpdateBB);
     if (rc) return rc;
   }
-  CK(launch_update_faces(m->dev, 0, kUpdateOriginalBB, m->stream), "bounds kernel");
-  *launches += 1;
+  LAUNCH(L, kKUpdate, "bounds kernel", launch_update_faces(m->dev, 0, kUpdateOriginalBB, m->stream));
   return SGPU_OK;
 }
+
+int run_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+               const int* dab_tools, int mode, int* launches_out);
+int finish_stroke(sgpu_mesh* mesh, int mode, int launches, SGPU_StrokeStats* stats);
 
 int upload_node_list(sgpu_mesh* m, const int* nodes, int totnode) {
   if (totnode < 0 || totnode > m->dev.nleaf)
@@ -343,8 +405,8 @@ int do_brush_tool(sgpu_mesh* m, const SGPU_Brush* brush, int tool, const float l
     pp.view[k] = brush->view_normal[k];
   }
   pp.iter_strength = 1.0f;
-  int launches = 0;
-  rc = launch_tool(m, b, pp, &launches);
+  Launcher L{m};
+  rc = launch_tool(L, b, pp);
   if (rc) return rc;
   return device_err(m);
 }
@@ -502,6 +564,9 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
     return fail(SGPU_ERR_INVALID_ARG, "empty or NULL grid arrays");
   const long long elems = static_cast<long long>(num_grids) * grid_size * grid_size;
   if (elems > 0x7fffffffLL) return fail(SGPU_ERR_UNSUPPORTED, "more than 2^31 grid elements");
+  if (grid_size > grid_size_limit())
+    return fail(SGPU_ERR_UNSUPPORTED, "grid_size %d above the supported %d", grid_size,
+                grid_size_limit());
   int rc = ensure_device();
   if (rc) return rc;
   sgpu_mesh* m = new (std::nothrow) sgpu_mesh();
@@ -589,8 +654,8 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
     CK(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf, cudaMemcpyHostToDevice,
                        m->stream),
        "flag all");
-    int launches = 0;
-    CK(launch_update_grids(d, m->stream, &launches), "grid normal kernels");
+    Launcher L{m};
+    if ((rc = launch_update_normals(L, 0))) return bail(rc);
   }
   CK(cudaStreamSynchronize(m->stream), "cudaStreamSynchronize");
   h.co.clear();
@@ -683,8 +748,8 @@ int sgpu_do_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location
 int sgpu_pbvh_update_normals(sgpu_mesh* mesh) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
-  int launches = 0;
-  if ((rc = launch_update_normals(mesh, 0, &launches))) return rc;
+  Launcher L{mesh};
+  if ((rc = launch_update_normals(L, 0))) return rc;
   return device_err(mesh);
 }
 
@@ -717,8 +782,208 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   if (brush->symmetry < 0 || brush->symmetry > 7)
     return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
-  int launches = 0;
   CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
+  int launches = 0;
+  if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, mode, &launches))) return rc;
+  CK(cudaEventRecord(mesh->ev1, mesh->stream), "event");
+  return finish_stroke(mesh, mode, launches, stats);
+}
+
+}  // extern "C"
+
+namespace {
+
+int validate_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+                    const int* dab_tools) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!brush || (!dabs && ndabs > 0) || ndabs < 0)
+    return fail(SGPU_ERR_INVALID_ARG, "NULL brush or dabs");
+  if (!(brush->radius > 0.0f)) return fail(SGPU_ERR_INVALID_ARG, "radius must be positive");
+  for (int d = 0; d < ndabs; d++) {
+    const int tool = dab_tools ? dab_tools[d] : brush->sculpt_tool;
+    if (!tool_ok(tool)) return fail(SGPU_ERR_INVALID_ARG, "unsupported sculpt tool %d", tool);
+  }
+  if (brush->symmetry < 0 || brush->symmetry > 7)
+    return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
+  return SGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+                     const int* dab_tools, const SGPU_MVert* verts_in,
+                     const float* vert_normals_in, SGPU_MVert* verts_out,
+                     SGPU_StrokeStats* stats) {
+  int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
+  if (rc) return rc;
+  if (mesh->dev.type != kFaces) return fail(SGPU_ERR_INVALID_ARG, "not a FACES mesh");
+  if (!verts_in || !verts_out) return fail(SGPU_ERR_INVALID_ARG, "NULL host buffers");
+  DevMesh& d = mesh->dev;
+  CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
+  CK(cudaMemcpyAsync(d.co, verts_in, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
+                     mesh->stream),
+     "upload verts");
+  if (vert_normals_in)
+    CK(cudaMemcpy2DAsync(d.no, sizeof(float4), vert_normals_in, 3 * sizeof(float),
+                         3 * sizeof(float), d.totvert, cudaMemcpyHostToDevice, mesh->stream),
+       "upload normals");
+  // New positions: every leaf box is refit and flushed before the stroke.
+  CK(launch_mark_all(d, kUpdateBB | kUpdateOriginalBB, mesh->stream), "mark kernel");
+  CK(launch_update_faces(d, 0, kUpdateBB | kUpdateOriginalBB, mesh->stream), "bounds kernel");
+  int launches = 2;
+  if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, SGPU_STROKE_GRAPH, &launches)))
+    return rc;
+  CK(cudaMemcpyAsync(verts_out, d.co, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
+                     mesh->stream),
+     "download verts");
+  CK(cudaEventRecord(mesh->ev1, mesh->stream), "event");
+  return finish_stroke(mesh, SGPU_STROKE_GRAPH, launches, stats);
+}
+
+int sgpu_stroke_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
+                        int ndabs, const int* dab_tools, SGPU_KernelProfile* out,
+                        SGPU_StrokeStats* stats) {
+  int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
+  if (rc) return rc;
+  if (!out) return fail(SGPU_ERR_INVALID_ARG, "NULL profile table");
+  static const char* names[SGPU_KERNEL_KINDS] = {
+      "k_cull", "k_set_list", "k_area", "k_brush", "k_smooth_compute",
+      "k_smooth_apply", "k_update_faces", "k_grid_gather", "k_grid_faces", "k_grid_seams"};
+  unsigned long long* counters = nullptr;
+  CK(cudaMalloc(&counters, sizeof(unsigned long long) * kKindCount), "cudaMalloc");
+  CK(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * kKindCount, mesh->stream),
+     "memset");
+  mesh->dev.prof = counters;
+  mesh->profiling = true;
+  mesh->ev_used = 0;
+  mesh->prof_marks.clear();
+  CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
+  int launches = 0;
+  rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, SGPU_STROKE_EAGER, &launches);
+  mesh->profiling = false;
+  mesh->dev.prof = nullptr;
+  if (rc) {
+    cudaFree(counters);
+    return rc;
+  }
+  cudaEventRecord(mesh->ev1, mesh->stream);
+  unsigned long long host_counters[kKindCount];
+  cudaMemcpyAsync(host_counters, counters, sizeof(host_counters), cudaMemcpyDeviceToHost,
+                  mesh->stream);
+  rc = finish_stroke(mesh, SGPU_STROKE_EAGER, launches, stats);
+  cudaFree(counters);
+  if (rc) return rc;
+  for (int k = 0; k < SGPU_KERNEL_KINDS; k++) {
+    std::memset(&out[k], 0, sizeof(out[k]));
+    std::snprintf(out[k].name, sizeof(out[k].name), "%s", names[k]);
+    out[k].alg_bytes = static_cast<double>(host_counters[k]);
+  }
+  for (const auto& mk : mesh->prof_marks) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, mk.a, mk.b), "elapsed");
+    out[mk.kind].launches++;
+    out[mk.kind].total_ms += ms;
+  }
+  mesh->prof_marks.clear();
+  return SGPU_OK;
+}
+
+int sgpu_mesh_snapshot(sgpu_mesh* mesh) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  DevMesh& d = mesh->dev;
+  const size_t V = static_cast<size_t>(d.totvert), N2 = 2 * static_cast<size_t>(d.totnode);
+  if (!mesh->snap_co) {
+    if ((rc = mesh->alloc(&mesh->snap_co, V))) return rc;
+    if ((rc = mesh->alloc(&mesh->snap_no, V))) return rc;
+    if (d.mask && (rc = mesh->alloc(&mesh->snap_mask, V))) return rc;
+    if ((rc = mesh->alloc(&mesh->snap_vb, N2))) return rc;
+    if ((rc = mesh->alloc(&mesh->snap_orig_vb, N2))) return rc;
+    if ((rc = mesh->alloc(&mesh->snap_flag, static_cast<size_t>(d.nleaf)))) return rc;
+  }
+  cudaStream_t s = mesh->stream;
+  CK(cudaMemcpyAsync(mesh->snap_co, d.co, sizeof(float4) * V, cudaMemcpyDeviceToDevice, s), "snap");
+  CK(cudaMemcpyAsync(mesh->snap_no, d.no, sizeof(float4) * V, cudaMemcpyDeviceToDevice, s), "snap");
+  if (d.mask)
+    CK(cudaMemcpyAsync(mesh->snap_mask, d.mask, sizeof(float) * V, cudaMemcpyDeviceToDevice, s),
+       "snap");
+  CK(cudaMemcpyAsync(mesh->snap_vb, d.vb, sizeof(float4) * N2, cudaMemcpyDeviceToDevice, s), "snap");
+  CK(cudaMemcpyAsync(mesh->snap_orig_vb, d.orig_vb, sizeof(float4) * N2, cudaMemcpyDeviceToDevice,
+                     s),
+     "snap");
+  CK(cudaMemcpyAsync(mesh->snap_flag, d.leaf_flag, sizeof(int) * d.nleaf, cudaMemcpyDeviceToDevice,
+                     s),
+     "snap");
+  CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_mesh_restore(sgpu_mesh* mesh) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->snap_co) return fail(SGPU_ERR_INVALID_ARG, "no snapshot taken");
+  DevMesh& d = mesh->dev;
+  const size_t V = static_cast<size_t>(d.totvert), N2 = 2 * static_cast<size_t>(d.totnode);
+  cudaStream_t s = mesh->stream;
+  CK(cudaMemcpyAsync(d.co, mesh->snap_co, sizeof(float4) * V, cudaMemcpyDeviceToDevice, s), "restore");
+  CK(cudaMemcpyAsync(d.no, mesh->snap_no, sizeof(float4) * V, cudaMemcpyDeviceToDevice, s), "restore");
+  if (d.mask)
+    CK(cudaMemcpyAsync(d.mask, mesh->snap_mask, sizeof(float) * V, cudaMemcpyDeviceToDevice, s),
+       "restore");
+  CK(cudaMemcpyAsync(d.vb, mesh->snap_vb, sizeof(float4) * N2, cudaMemcpyDeviceToDevice, s),
+     "restore");
+  CK(cudaMemcpyAsync(d.orig_vb, mesh->snap_orig_vb, sizeof(float4) * N2, cudaMemcpyDeviceToDevice,
+                     s),
+     "restore");
+  CK(cudaMemcpyAsync(d.leaf_flag, mesh->snap_flag, sizeof(int) * d.nleaf, cudaMemcpyDeviceToDevice,
+                     s),
+     "restore");
+  CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_mesh_flush_l2(sgpu_mesh* mesh) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  const size_t bytes = 256ull << 20;
+  if (!mesh->flush_buf) {
+    void* p = nullptr;
+    if ((rc = mesh->alloc(reinterpret_cast<char**>(&p), bytes))) return rc;
+    mesh->flush_buf = p;
+  }
+  CK(launch_l2_flush(mesh->flush_buf, bytes, mesh->stream), "flush kernel");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+void* sgpu_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+    fail(SGPU_ERR_OOM, "cudaMallocHost(%zu) failed", bytes);
+    return nullptr;
+  }
+  return p;
+}
+
+int sgpu_host_free(void* ptr) {
+  if (!ptr) return SGPU_OK;
+  CK(cudaFreeHost(ptr), "cudaFreeHost");
+  return SGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Enqueues the stroke eagerly or through the per-mesh cached CUDA graph.
+int run_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+               const int* dab_tools, int mode, int* launches_out) {
+  int rc;
+  Launcher L{mesh};
+  int& launches = *launches_out;
   if (mode == SGPU_STROKE_GRAPH) {
     // Key: everything the captured launches depend on.
     std::vector<unsigned char> key(sizeof(SGPU_Brush) + sizeof(SGPU_Dab) * ndabs +
@@ -737,7 +1002,7 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
       mesh->gexec = nullptr;
       cudaGraph_t graph = nullptr;
       CK(cudaStreamBeginCapture(mesh->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-      rc = enqueue_stroke(mesh, brush, dabs, ndabs, dab_tools, &launches);
+      rc = enqueue_stroke(L, brush, dabs, ndabs, dab_tools);
       cudaError_t ce = cudaStreamEndCapture(mesh->stream, &graph);
       if (rc) {
         if (graph) cudaGraphDestroy(graph);
@@ -751,16 +1016,21 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
       if (ce != cudaSuccess) return cuda_fail(ce, "graph instantiate");
       mesh->gkey = key;
       mesh->g_nodes = static_cast<int>(nn);
-      mesh->g_launches = launches;
-      CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
+      mesh->g_launches = L.launches;
     }
-    launches = mesh->g_launches;
+    launches += mesh->g_launches;
     CK(cudaGraphLaunch(mesh->gexec, mesh->stream), "graph launch");
   } else {
-    rc = enqueue_stroke(mesh, brush, dabs, ndabs, dab_tools, &launches);
+    rc = enqueue_stroke(L, brush, dabs, ndabs, dab_tools);
     if (rc) return rc;
+    launches += L.launches;
   }
-  CK(cudaEventRecord(mesh->ev1, mesh->stream), "event");
+  return SGPU_OK;
+}
+
+// Reads the stroke's counters and error word; fills stats (events ev0..ev1).
+int finish_stroke(sgpu_mesh* mesh, int mode, int launches, SGPU_StrokeStats* stats) {
+  int rc;
   unsigned long long displaced = 0;
   CK(cudaMemcpyAsync(&displaced, &mesh->dev.work->displaced, sizeof(displaced),
                      cudaMemcpyDeviceToHost, mesh->stream),
@@ -776,6 +1046,10 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   return SGPU_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int sgpu_get_verts(sgpu_mesh* mesh, SGPU_MVert* out) {
   int rc = check_mesh(mesh);

@@ -111,6 +111,8 @@ __global__ void __launch_bounds__(kCullThreads) k_cull(DevMesh m, PassParams pp)
     m.work->cull_count = run_cnt;
     m.cull_off[run_cnt] = run_verts;
   }
+  // 24 B per node box tested, 8 B per leaf emitted (id + vertex offset).
+  prof_add(m, kKCull, threadIdx.x == 0 ? 24ull * m.totnode + 8ull * run_cnt : 0ull);
 }
 
 // Host-provided node list: node indices -> leaf ids and vertex prefix.
@@ -207,6 +209,7 @@ __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassPa
   const float ra = b.radius * b.area_radius_factor;
   const float rn2 = rn * rn, ra2 = ra * ra;
   const int t = threadIdx.x;
+  unsigned long long ab = 0;  // algorithmic bytes (profiling)
   for (int k = blockIdx.x; k < cnt; k += gridDim.x) {
     const int leaf = m.cull_list[k];
     const int nv = leaf_nverts(m, leaf);
@@ -218,6 +221,7 @@ __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassPa
       const int v = leaf_vert(m, leaf, i);
       const float4 co = m.co[v];
       const float d2 = dist_sq(co, pp.loc);
+      ab += (m.type == kFaces ? 4u : 0u) + 24u;  // index, co, no
       if (d2 <= rn2) {
         const float4 no = m.no[v];
         cs_add(l.v[0], no.x);
@@ -252,6 +256,7 @@ __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassPa
     }
     __syncthreads();
   }
+  prof_add(m, kKArea, ab);
   __threadfence();
   __syncthreads();
   if (t == 0) {
@@ -378,6 +383,7 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
   mark_culled(m, cnt);
   const float dd = radius * b.strength;
   const float off[3] = {area_no[0] * dd, area_no[1] * dd, area_no[2] * dd};
+  unsigned long long ab = 0;  // algorithmic bytes (profiling)
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < total; base += stride) {
     const int i = base + threadIdx.x;
@@ -435,9 +441,13 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
         m.co[v] = co;
         if (m.type == kFaces) m.vtag[v] = 1;
       }
+      // index, co, mask, automask, normal (inflate / front-face); co write on a hit
+      ab += (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) + (m.automask ? 4u : 0u) +
+            ((b.tool == kToolInflate || (b.flag & kBrushFrontFace)) ? 12u : 0u) + (hit ? 12u : 0u);
     }
     count_displaced(m, moved);
   }
+  prof_add(m, kKBrush, ab);
 }
 
 // Smooth, one Jacobi sweep in two launches: compute new positions from the
@@ -484,6 +494,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth_compute(DevMesh m, DevBrush
   const float radius = b.radius;
   const float radius_sq = radius * radius;
   if (pp.iteration == 0) mark_culled(m, cnt);
+  unsigned long long ab = 0;  // algorithmic bytes (profiling)
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < total; base += stride) {
     const int i = base + threadIdx.x;
@@ -503,19 +514,25 @@ __global__ void __launch_bounds__(kThreads) k_smooth_compute(DevMesh m, DevBrush
         out.z = co.z + (avg.z - co.z) * fade;
         out.w = 1.0f;
         moved = (pp.iteration == 0) && sf != 0.0f;
+        const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
+        ab += (m.type == kFaces ? 8u : 0u) + 16ull * valence;  // ring range, ring ids + co
       }
       m.scratch[i] = out;
+      ab += (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) + 16u;  // idx, co, mask, out
     }
     count_displaced(m, moved);
   }
+  prof_add(m, kKSmoothCompute, ab);
 }
 
 __global__ void __launch_bounds__(kThreads) k_smooth_apply(DevMesh m) {
   const int cnt = m.work->cull_count;
   const int total = m.cull_off[cnt];
   const int stride = gridDim.x * blockDim.x;
+  unsigned long long ab = 0;  // algorithmic bytes (profiling)
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
     const float4 s = m.scratch[i];
+    ab += 16u;
     if (s.w == 0.0f) continue;
     const int k = find_slot(m.cull_off, cnt, i);
     const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
@@ -525,7 +542,9 @@ __global__ void __launch_bounds__(kThreads) k_smooth_apply(DevMesh m) {
     co.z = s.z;
     m.co[v] = co;
     if (m.type == kFaces) m.vtag[v] = 1;
+    ab += (m.type == kFaces ? 4u : 0u) + 12u;
   }
+  prof_add(m, kKSmoothApply, ab);
 }
 
 // ---------------------------------------------------------------------------
@@ -538,10 +557,15 @@ __global__ void __launch_bounds__(kThreads) k_smooth_apply(DevMesh m) {
 __device__ __forceinline__ float fmin_ref(float a, float b) { return (a < b) ? a : b; }
 __device__ __forceinline__ float fmax_ref(float a, float b) { return (a > b) ? a : b; }
 
-__device__ void leaf_refit(const DevMesh& m, int leaf, float* red /* 6*kThreads/32 */) {
+__device__ void leaf_refit(const DevMesh& m, int leaf, float* red /* 6*kThreads/32 */,
+                           unsigned long long& ab) {
   float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
   float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
   const int nv = leaf_nverts_all(m, leaf);
+  // co of every leaf vertex (+ its index for FACES); the node box written once
+  if (threadIdx.x < nv)
+    ab += (m.type == kFaces ? 16ull : 12ull) * ((nv - threadIdx.x + blockDim.x - 1) / blockDim.x);
+  if (threadIdx.x == 0) ab += 24u;
   for (int i = threadIdx.x; i < nv; i += blockDim.x) {
     int v;
     if (m.type == kFaces) {
@@ -586,7 +610,7 @@ __device__ void leaf_refit(const DevMesh& m, int leaf, float* red /* 6*kThreads/
   __syncthreads();
 }
 
-__device__ void faces_leaf_normals(const DevMesh& m, int leaf) {
+__device__ void faces_leaf_normals(const DevMesh& m, int leaf, unsigned long long& ab) {
   const int off = m.leaf_vert_off[leaf];
   const int nu = m.leaf_uniq[leaf];
   for (int i = threadIdx.x; i < nu; i += blockDim.x) {
@@ -594,9 +618,11 @@ __device__ void faces_leaf_normals(const DevMesh& m, int leaf) {
     if (!m.vtag[v]) continue;
     CSum ax = {0.0f, 0.0f}, ay = {0.0f, 0.0f}, az = {0.0f, 0.0f};
     const int e = m.vt_off[v + 1];
+    ab += 24u;  // the vertex's co read and normal written
     for (int q = m.vt_off[v]; q < e; q++) {
       const int t = m.vt_idx[q];
       if (!(m.leaf_flag[m.lt_leaf[t]] & kUpdateNormals)) continue;
+      ab += 16u;  // looptri record (3 vertex ids + polygon id)
       const float3 fn = poly_normal(m, m.lt[t].w);
       cs_add(ax, fn.x);
       cs_add(ay, fn.y);
@@ -653,10 +679,11 @@ __global__ void __launch_bounds__(kThreads) k_update_faces(DevMesh m, int do_nor
                                                            int bounds_flag) {
   __shared__ float red[6 * (kThreads / 32)];
   __shared__ bool am_last;
+  unsigned long long ab = 0;  // algorithmic bytes (profiling)
   for (int leaf = blockIdx.x; leaf < m.nleaf; leaf += gridDim.x) {
     const int f = m.leaf_flag[leaf];
-    if (do_normals && m.type == kFaces && (f & kUpdateNormals)) faces_leaf_normals(m, leaf);
-    if ((bounds_flag & kUpdateBB) && (f & kUpdateBB)) leaf_refit(m, leaf, red);
+    if (do_normals && m.type == kFaces && (f & kUpdateNormals)) faces_leaf_normals(m, leaf, ab);
+    if ((bounds_flag & kUpdateBB) && (f & kUpdateBB)) leaf_refit(m, leaf, red, ab);
     if (threadIdx.x == 0) {
       const int node = m.leaf_node[leaf];
       if ((bounds_flag & kUpdateOriginalBB) && (f & kUpdateOriginalBB)) {
@@ -667,6 +694,7 @@ __global__ void __launch_bounds__(kThreads) k_update_faces(DevMesh m, int do_nor
         atomicAnd(&m.leaf_flag[leaf], ~kUpdateRedraw);
     }
   }
+  prof_add(m, kKUpdate, ab);
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -683,6 +711,17 @@ __global__ void __launch_bounds__(kThreads) k_update_faces(DevMesh m, int do_nor
   }
   if (bounds_flag & (kUpdateBB | kUpdateOriginalBB)) flush_bounds(m, bounds_flag);
   if (threadIdx.x == 0) m.work->ticket_update = 0u;
+}
+
+__global__ void k_mark_all(DevMesh m, int bits) {
+  for (int leaf = blockIdx.x * blockDim.x + threadIdx.x; leaf < m.nleaf;
+       leaf += gridDim.x * blockDim.x)
+    atomicOr(&m.leaf_flag[leaf], bits);
+}
+
+cudaError_t launch_mark_all(const DevMesh& m, int bits, cudaStream_t s) {
+  k_mark_all<<<(m.nleaf + kThreads - 1) / kThreads, kThreads, 0, s>>>(m, bits);
+  return cudaGetLastError();
 }
 
 __global__ void k_mark_node(DevMesh m, int node) {
@@ -731,10 +770,25 @@ cudaError_t launch_brush(const DevMesh& m, const DevBrush& b, const PassParams& 
   return cudaGetLastError();
 }
 
-cudaError_t launch_smooth_iteration(const DevMesh& m, const DevBrush& b, const PassParams& pp,
-                                    cudaStream_t s) {
+cudaError_t launch_smooth_compute(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                                  cudaStream_t s) {
   k_smooth_compute<<<work_grid(), kThreads, 0, s>>>(m, b, pp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth_apply(const DevMesh& m, cudaStream_t s) {
   k_smooth_apply<<<work_grid(), kThreads, 0, s>>>(m);
+  return cudaGetLastError();
+}
+
+__global__ void k_l2_flush(uint4* buf, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    buf[i] = make_uint4((unsigned)i, 0u, 0u, 0u);
+}
+
+cudaError_t launch_l2_flush(void* buf, size_t bytes, cudaStream_t s) {
+  k_l2_flush<<<work_grid() * 4, kThreads, 0, s>>>(static_cast<uint4*>(buf), bytes / 16);
   return cudaGetLastError();
 }
 

@@ -74,9 +74,13 @@ __global__ void __launch_bounds__(kGThreads) k_grid_faces(DevMesh m) {
   extern __shared__ float fn[];  // 3 * (gs-1)^2
   const int nf = m.grid_counts[0];
   const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area;
+  unsigned long long ab = 0;  // algorithmic bytes (profiling)
   for (int k = blockIdx.x; k < nf; k += gridDim.x) {
     const int f = m.face_list[k];
     const int start = m.face_start[f], n = m.face_ngrids[f];
+    // co read + normal written per element; each seam pair and the centre
+    // read and write co, no and mask of their elements
+    if (threadIdx.x == 0) ab += 24ull * area * n + 112ull * g1 * n + 56ull * n;
     for (int c = 0; c < n; c++) {
       const int base = (start + c) * area;
       // subdiv_ccg_recalc_inner_face_normals: quad {(x,y+1),(x+1,y+1),(x+1,y),(x,y)}
@@ -156,6 +160,7 @@ __global__ void __launch_bounds__(kGThreads) k_grid_faces(DevMesh m) {
     }
     __syncthreads();
   }
+  prof_add(m, kKGridFaces, ab);
 }
 
 // Edges: one thread per (edge, boundary index 1 .. 2gs-2); corners: one thread
@@ -166,6 +171,7 @@ __global__ void __launch_bounds__(kGThreads) k_grid_seams(DevMesh m) {
   const int g2 = 2 * m.grid_size, inner = g2 - 2;
   const long long edge_items = (long long)ne * inner;
   const long long total = edge_items + nv;
+  unsigned long long ab = 0;  // algorithmic bytes (profiling)
   for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
        it += (long long)gridDim.x * blockDim.x) {
     if (it < edge_items) {
@@ -174,6 +180,7 @@ __global__ void __launch_bounds__(kGThreads) k_grid_seams(DevMesh m) {
       const int f0 = m.edge_off[e], f1 = m.edge_off[e + 1];
       const int nfe = f1 - f0;
       if (nfe == 1) continue;
+      ab += 56ull * nfe;  // co, no, mask read and written per adjacent face
       float cx = 0.0f, cy = 0.0f, cz = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f, mk = 0.0f;
       for (int f = f0; f < f1; f++) {
         const int el = m.edge_elems[(long long)f * g2 + i];
@@ -198,6 +205,7 @@ __global__ void __launch_bounds__(kGThreads) k_grid_seams(DevMesh m) {
       const int f0 = m.bvert_off[v], f1 = m.bvert_off[v + 1];
       const int nfv = f1 - f0;
       if (nfv == 1) continue;
+      ab += 56ull * nfv;
       float cx = 0.0f, cy = 0.0f, cz = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f, mk = 0.0f;
       for (int f = f0; f < f1; f++) {
         const int el = m.bvert_elems[f];
@@ -219,6 +227,7 @@ __global__ void __launch_bounds__(kGThreads) k_grid_seams(DevMesh m) {
       }
     }
   }
+  prof_add(m, kKGridSeams, ab);
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -247,15 +256,30 @@ static int grids_grid() {
   return g;
 }
 
-cudaError_t launch_update_grids(const DevMesh& m, cudaStream_t s, int* launches) {
+int grid_size_limit() { return 65; }
+
+void configure_grid_kernels() {
+  const int g1 = grid_size_limit() - 1;
+  cudaFuncSetAttribute(k_grid_faces, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(sizeof(float) * 3 * g1 * g1));
+}
+
+cudaError_t launch_grid_gather(const DevMesh& m, cudaStream_t s) {
   const int g = grids_grid();
   int gl = m.nleaf < g ? m.nleaf : g;
   if (gl < 1) gl = 1;
   k_grid_gather<<<gl, kGThreads, 0, s>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grid_faces(const DevMesh& m, cudaStream_t s) {
   const size_t smem = sizeof(float) * 3 * (m.grid_size - 1) * (m.grid_size - 1);
-  k_grid_faces<<<g, kGThreads, smem, s>>>(m);
-  k_grid_seams<<<g, kGThreads, 0, s>>>(m);
-  if (launches) *launches += 3;
+  k_grid_faces<<<grids_grid(), kGThreads, smem, s>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grid_seams(const DevMesh& m, cudaStream_t s) {
+  k_grid_seams<<<grids_grid(), kGThreads, 0, s>>>(m);
   return cudaGetLastError();
 }
 

@@ -102,7 +102,33 @@ struct DevMesh {
   AreaPart* parts;  // nleaf
   float4* scratch;  // smooth Jacobi values, totvert
   unsigned char* node_upd;  // totnode
+  // Profiling: algorithmic bytes per kernel kind (nullptr outside profiling).
+  unsigned long long* prof;
 };
+
+// Kernel kinds for profiling (index into DevMesh::prof and the profile table).
+enum KernelKind {
+  kKCull = 0,
+  kKSetList,
+  kKArea,
+  kKBrush,
+  kKSmoothCompute,
+  kKSmoothApply,
+  kKUpdate,
+  kKGridGather,
+  kKGridFaces,
+  kKGridSeams,
+  kKindCount
+};
+
+// Adds per-thread algorithmic bytes to the kernel's counter (warp-aggregated).
+// Called by every thread of the block from converged code.
+__device__ __forceinline__ void prof_add(const DevMesh& m, int kind, unsigned long long bytes) {
+  if (!m.prof) return;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+  if ((threadIdx.x & 31) == 0 && bytes) atomicAdd(&m.prof[kind], bytes);
+}
 
 // Brush constants of one stroke (kernel parameter).
 struct DevBrush {

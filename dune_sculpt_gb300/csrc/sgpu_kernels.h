@@ -13,17 +13,25 @@ cudaError_t launch_area(const DevMesh& m, const DevBrush& b, const PassParams& p
                         cudaStream_t s);
 cudaError_t launch_brush(const DevMesh& m, const DevBrush& b, const PassParams& pp,
                          cudaStream_t s);
-// One smooth iteration = two launches (compute, apply).
-cudaError_t launch_smooth_iteration(const DevMesh& m, const DevBrush& b, const PassParams& pp,
-                                    cudaStream_t s);
+// One smooth iteration = two launches (compute into scratch, apply).
+cudaError_t launch_smooth_compute(const DevMesh& m, const DevBrush& b, const PassParams& pp,
+                                  cudaStream_t s);
+cudaError_t launch_smooth_apply(const DevMesh& m, cudaStream_t s);
 // FACES normals (do_normals) and/or bounds refit + flush (bounds_flag); bounds
 // also serve GRIDS meshes.
 cudaError_t launch_update_faces(const DevMesh& m, int do_normals, int bounds_flag,
                                 cudaStream_t s);
-// GRIDS normal update with seam stitching.  Returns the number of launches.
-cudaError_t launch_update_grids(const DevMesh& m, cudaStream_t s, int* launches);
+// GRIDS normal update with seam stitching: gather, per-face, seams.
+cudaError_t launch_grid_gather(const DevMesh& m, cudaStream_t s);
+cudaError_t launch_grid_faces(const DevMesh& m, cudaStream_t s);
+cudaError_t launch_grid_seams(const DevMesh& m, cudaStream_t s);
+// Writes a buffer larger than L2.
+cudaError_t launch_l2_flush(void* buf, size_t bytes, cudaStream_t s);
 cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s);
+cudaError_t launch_mark_all(const DevMesh& m, int bits, cudaStream_t s);
 int cull_smem_limit();
+int grid_size_limit();
 void configure_kernels();
+void configure_grid_kernels();
 
 }  // namespace sgpu

@@ -53,6 +53,14 @@ class SGPU_StrokeStats(C.Structure):
                 ("kernel_launches", C.c_int), ("graph_nodes", C.c_int)]
 
 
+KERNEL_KINDS = 10
+
+
+class SGPU_KernelProfile(C.Structure):
+    _fields_ = [("name", C.c_char * 24), ("launches", C.c_int), ("total_ms", C.c_float),
+                ("alg_bytes", C.c_double)]
+
+
 # Every exported symbol, as declared in include/sculpt_gpu.h.
 EXPORTS = (
     "sgpu_version", "sgpu_last_error", "sgpu_device_info", "sgpu_mesh_create_faces",
@@ -63,6 +71,8 @@ EXPORTS = (
     "sgpu_stroke", "sgpu_get_verts", "sgpu_set_verts", "sgpu_get_positions",
     "sgpu_set_positions", "sgpu_get_normals", "sgpu_get_mask", "sgpu_get_node_bbs",
     "sgpu_get_nodes", "sgpu_get_prim_indices", "sgpu_get_vert_indices", "sgpu_curve_table",
+    "sgpu_stroke_host", "sgpu_mesh_snapshot", "sgpu_mesh_restore", "sgpu_stroke_profile",
+    "sgpu_mesh_flush_l2", "sgpu_host_alloc", "sgpu_host_free",
 )
 
 _lib = None
@@ -104,8 +114,43 @@ def load(path: str | None = None):
     L.sgpu_get_node_bbs.argtypes = [vp, vp, vp]
     L.sgpu_get_nodes.argtypes = [vp] + [vp] * 7
     L.sgpu_curve_table.argtypes = [i, vp, vp]
+    L.sgpu_stroke_host.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp, vp,
+                                   C.POINTER(SGPU_StrokeStats)]
+    L.sgpu_stroke_profile.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp,
+                                      C.POINTER(SGPU_KernelProfile),
+                                      C.POINTER(SGPU_StrokeStats)]
+    for name in ("sgpu_mesh_snapshot", "sgpu_mesh_restore", "sgpu_mesh_flush_l2"):
+        getattr(L, name).argtypes = [vp]
+    L.sgpu_host_alloc.restype = vp
+    L.sgpu_host_alloc.argtypes = [C.c_size_t]
+    L.sgpu_host_free.argtypes = [vp]
     _lib = L
     return L
+
+
+class PinnedArray:
+    """A numpy array in page-locked host memory from sgpu_host_alloc."""
+
+    def __init__(self, shape, dtype):
+        dt = np.dtype(dtype)
+        n = int(np.prod(shape)) * dt.itemsize
+        self._ptr = load().sgpu_host_alloc(max(n, 16))
+        if not self._ptr:
+            raise SculptGPUError(ERR_OOM, load().sgpu_last_error().decode())
+        buf = (C.c_char * n).from_address(self._ptr)
+        self.array = np.frombuffer(buf, dtype=dt).reshape(shape)
+
+    def free(self):
+        if self._ptr:
+            self.array = None
+            load().sgpu_host_free(self._ptr)
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def _p(a):
@@ -271,6 +316,44 @@ class PBVH:
         _check(load().sgpu_stroke(self._h, C.byref(b), _p(d), d.shape[0], _p(tools), mode,
                                   C.byref(stats)))
         return stats
+
+    def stroke_host(self, st, verts_in, verts_out, normals_in=None, dabs=None,
+                    dab_tools=None) -> SGPU_StrokeStats:
+        """Host-buffer stroke: upload, refit, stroke, download (one C-ABI call)."""
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        stats = SGPU_StrokeStats()
+        _check(load().sgpu_stroke_host(self._h, C.byref(b), _p(d), d.shape[0], _p(tools),
+                                       _p(verts_in), _p(normals_in), _p(verts_out),
+                                       C.byref(stats)))
+        return stats
+
+    def stroke_profile(self, st, dabs=None, dab_tools=None):
+        """Eager stroke with per-launch CUDA events and algorithmic-byte counters.
+        Returns ({kernel: {launches, total_ms, alg_bytes}}, stats)."""
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        prof = (SGPU_KernelProfile * KERNEL_KINDS)()
+        stats = SGPU_StrokeStats()
+        _check(load().sgpu_stroke_profile(self._h, C.byref(b), _p(d), d.shape[0], _p(tools),
+                                          prof, C.byref(stats)))
+        out = {}
+        for p in prof:
+            if p.launches:
+                out[p.name.decode()] = {"launches": p.launches, "total_ms": p.total_ms,
+                                        "alg_bytes": p.alg_bytes}
+        return out, stats
+
+    def snapshot(self):
+        _check(load().sgpu_mesh_snapshot(self._h))
+
+    def restore(self):
+        _check(load().sgpu_mesh_restore(self._h))
+
+    def flush_l2(self):
+        _check(load().sgpu_mesh_flush_l2(self._h))
 
     def sync(self):
         _check(load().sgpu_mesh_sync(self._h))

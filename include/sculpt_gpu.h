@@ -25,6 +25,7 @@
 #ifndef SCULPT_GPU_H
 #define SCULPT_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -207,6 +208,40 @@ int sgpu_pbvh_node_mark_update(sgpu_mesh *mesh, int node);
 #define SGPU_STROKE_GRAPH 1
 int sgpu_stroke(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, int ndabs,
                 const int *dab_tools, int mode, SGPU_StrokeStats *stats);
+
+/* The stroke with host buffers, as a host application calls it: verts_in (and
+ * vert_normals_in, nullable) are copied to the device, every leaf box is
+ * refit, the stroke runs, and the positions are copied back to verts_out.
+ * stats->gpu_ms covers the copies and the kernels.  FACES meshes. */
+int sgpu_stroke_host(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, int ndabs,
+                     const int *dab_tools, const SGPU_MVert *verts_in,
+                     const float *vert_normals_in, SGPU_MVert *verts_out,
+                     SGPU_StrokeStats *stats);
+
+/* ---- per-stroke restore (undo) ----
+ * snapshot copies positions, normals, mask, node boxes and node flags into
+ * device memory owned by the handle; restore copies them back. */
+int sgpu_mesh_snapshot(sgpu_mesh *mesh);
+int sgpu_mesh_restore(sgpu_mesh *mesh);
+
+/* ---- measurement ---- */
+#define SGPU_KERNEL_KINDS 10
+typedef struct SGPU_KernelProfile {
+  char name[24];   /* kernel kind */
+  int launches;    /* launches of this kind in the stroke */
+  float total_ms;  /* sum of per-launch CUDA-event durations */
+  double alg_bytes; /* algorithmic bytes moved by those launches */
+} SGPU_KernelProfile;
+/* Runs the stroke call by call with CUDA events around every launch and the
+ * kernels' algorithmic-byte counters on; out has SGPU_KERNEL_KINDS entries. */
+int sgpu_stroke_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
+                        int ndabs, const int *dab_tools, SGPU_KernelProfile *out,
+                        SGPU_StrokeStats *stats);
+/* Writes a device buffer larger than L2 (256 MiB) on the mesh stream. */
+int sgpu_mesh_flush_l2(sgpu_mesh *mesh);
+/* Page-locked host memory for the host-buffer path. */
+void *sgpu_host_alloc(size_t bytes);
+int sgpu_host_free(void *ptr);
 
 /* ---- data access (synchronous) ---- */
 int sgpu_get_verts(sgpu_mesh *mesh, SGPU_MVert *out);          /* FACES */
