@@ -8,18 +8,27 @@ stroke: per dab and symmetry pass the node search and the brush, then the
 normal update and bounding-box refit, as the reference's stroke does.
 
   value  : device-resident throughput — Sum(vertices displaced) / Sum(stroke
-           time), stroke time from CUDA events on the mesh stream, the stroke
-           replayed from its captured CUDA graph; positions, normals and node
-           boxes restored from a device snapshot and L2 flushed (256 MiB write)
+           time), stroke time from CUDA events on the mesh stream; the stroke
+           runs as one launch of the persistent stroke kernel (cluster size
+           picked by the autotuner); positions, normals and node boxes are
+           restored from a device snapshot and L2 flushed (256 MiB write)
            before every step, both outside the timed region.
   e2e    : the same through sgpu_stroke_host with page-locked host buffers:
            H2D of positions and normals, full box refit, stroke, D2H of
            positions, all inside the event-timed region.
-  roofline: the dominant kernel of an event-profiled eager run: algorithmic
-           bytes per launch / mean launch time, against the measured HBM copy
+  roofline: k_team_stroke (the only kernel of a step): algorithmic bytes per
+           launch (the kernel's own counters, an instrumented run) / mean
+           step time of the timed run, against the measured HBM copy
            bandwidth.
+  plain_graph / plain_eager: the same stroke through the per-call kernels
+           (one kernel per reference call), replayed as a CUDA graph / eager.
+  batch  : the 64-mesh uneven batch, one persistent launch versus 64
+           sequential plain strokes.
   cpu_baseline: the FP32 CPU restatement (oracle, OpenMP over PBVH nodes) on
            the host cores, same stroke.
+
+--quick runs three persistent strokes of the workload and exits (the
+command profiled with ncu).
 
 --impl reference times the CPU restatement of the reference path (the
 reference itself does not build: its headers and brush code are missing).
@@ -55,7 +64,28 @@ def parse_args():
     ap.add_argument("--cpu-sample-dabs", type=int, default=0,
                     help="dabs of the stroke in the CPU sample (0 = whole stroke)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-mesh batch comparison")
+    ap.add_argument("--quick", action="store_true",
+                    help="three persistent strokes of the workload, no report (for ncu)")
+    ap.add_argument("--cluster", type=int, default=16, help="cluster size for --quick")
     return ap.parse_args()
+
+
+def run_quick(args):
+    from dune_sculpt_gb300 import build as libbuild
+
+    libbuild.build()
+    from dune_sculpt_gb300.sculpt import PBVH, STROKE_TEAM
+
+    m, st, leaf_limit, _ = workload()
+    g = PBVH.build_mesh(m, leaf_limit)
+    g.snapshot()
+    g.set_team(args.cluster)
+    for _ in range(3):
+        g.restore()
+        s = g.stroke(st, mode=STROKE_TEAM)
+    print(f"quick: {s.verts_displaced} vertices displaced, {s.gpu_ms:.3f} ms")
+    return 0
 
 
 def dist_env():
@@ -168,20 +198,23 @@ def run_reference(args):
     pyoracle.build()
     sample = args.cpu_sample_dabs or 32
     dabs = st.dabs[:sample]
-    o = pyoracle.OracleMesh.faces(m, leaf_limit)
-    o.recalc_all_normals()
     threads = pyoracle.max_threads()
-    co0 = o.co()
+
+    def fresh():
+        o = pyoracle.OracleMesh.faces(m, leaf_limit)
+        o.recalc_all_normals()
+        return o
+
     for _ in range(args.warmup):
-        o.set_co(co0)
-        o.stroke(st, which=1, nthreads=threads, dabs=dabs)
+        fresh().stroke(st, which=1, nthreads=threads, dabs=dabs)
     total_v, total_s = 0, 0.0
     for _ in range(args.steps):
-        o.set_co(co0)
+        o = fresh()  # every step starts from the same mesh state (untimed)
         t0 = time.perf_counter()
         tot, _ = o.stroke(st, which=1, nthreads=threads, dabs=dabs)
         total_s += time.perf_counter() - t0
         total_v += tot
+        o.close()
     value = total_v / total_s
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -208,44 +241,51 @@ def run_gpu(args):
     from dune_sculpt_gb300 import build as libbuild
 
     libbuild.build()
-    from dune_sculpt_gb300 import sculpt
-    from dune_sculpt_gb300.sculpt import PBVH, STROKE_EAGER, STROKE_GRAPH, PinnedArray
+    from dune_sculpt_gb300 import synth
+    from dune_sculpt_gb300.sculpt import (BATCH_SEQUENTIAL, BATCH_TEAM, PBVH, STROKE_EAGER,
+                                          STROKE_GRAPH, STROKE_TEAM, PinnedArray, batch_stroke)
 
     m, st, leaf_limit, cfg = workload()
     g = PBVH.build_mesh(m, leaf_limit)
     g.snapshot()
+    cluster, tune_ms = g.autotune_team(st)  # restores the snapshot
 
     def barrier():
         if world > 1:
             dist.barrier()
 
-    # warm-up (graph capture happens on the first call)
     for _ in range(args.warmup):
         g.restore()
-        g.stroke(st, mode=STROKE_GRAPH)
+        g.stroke(st, mode=STROKE_TEAM)
     barrier()
     clocks = ClockSampler(local) if rank == 0 else None
     total_ms, total_v, launches = 0.0, 0, 0
     for _ in range(args.steps):
         g.restore()
         g.flush_l2()
-        s = g.stroke(st, mode=STROKE_GRAPH)
+        s = g.stroke(st, mode=STROKE_TEAM)
         total_ms += s.gpu_ms
         total_v += s.verts_displaced
         launches += s.kernel_launches
     g.sync()
     barrier()
     clk = clocks.stop() if clocks else None
-    graph_nodes = s.graph_nodes
 
-    # plain (call-by-call) launches of the same stroke, for comparison
-    eager_ms, eager_v = 0.0, 0
-    for _ in range(2):
-        g.restore()
-        g.flush_l2()
-        se = g.stroke(st, mode=STROKE_EAGER)
-        eager_ms += se.gpu_ms
-        eager_v += se.verts_displaced
+    # the same stroke through the per-call kernels: captured graph, and eager
+    def plain(mode, n=2):
+        ms, v = 0.0, 0
+        for _ in range(n):
+            g.restore()
+            g.flush_l2()
+            se = g.stroke(st, mode=mode)
+            ms += se.gpu_ms
+            v += se.verts_displaced
+        return {"value": v / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / n}
+
+    g.restore()
+    g.stroke(st, mode=STROKE_GRAPH)  # graph capture outside the timing
+    plain_graph = plain(STROKE_GRAPH)
+    plain_eager = plain(STROKE_EAGER)
 
     # e2e through the host-buffer entry point with page-locked buffers
     V = m.totvert
@@ -256,21 +296,24 @@ def run_gpu(args):
     nin.array[:] = g.normals()
     vout = PinnedArray((V,), m.verts.dtype)
     g.restore()
-    g.stroke_host(st, vin.array, vout.array, nin.array)  # warm (graph capture)
+    g.stroke_host(st, vin.array, vout.array, nin.array, mode=STROKE_TEAM)
     e2e_ms, e2e_v = 0.0, 0
     for _ in range(args.steps):
         g.restore()
         g.flush_l2()
-        s2 = g.stroke_host(st, vin.array, vout.array, nin.array)
+        s2 = g.stroke_host(st, vin.array, vout.array, nin.array, mode=STROKE_TEAM)
         e2e_ms += s2.gpu_ms
         e2e_v += s2.verts_displaced
 
-    # kernel profile (event-bracketed eager run with algorithmic-byte counters)
+    # phase profile of the persistent kernel (instrumented run, not timed)
     g.restore()
     g.flush_l2()
-    prof, _ = g.stroke_profile(st)
+    phases, prof_ms, _ = g.stroke_team_profile(st)
+    alg_bytes = sum(p["bytes"] for p in phases.values())
 
-    # max over ranks
+    batch = None if args.no_batch else run_batch(args, synth, PBVH, batch_stroke, BATCH_TEAM,
+                                                  BATCH_SEQUENTIAL)
+
     if world > 1:
         import torch
 
@@ -284,38 +327,38 @@ def run_gpu(args):
         return 0
 
     peak, peak_kind = measured_peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1]["total_ms"])
-    dname, d = dom
-    achieved = d["alg_bytes"] / (d["total_ms"] / 1e3) / 1e9 if d["total_ms"] > 0 else 0.0
+    step_ms = total_ms / args.steps
+    achieved = alg_bytes / (step_ms / 1e3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(cfg["workload"], {}).get(dname)
+            traffic = json.load(f).get(cfg["workload"], {}).get("k_team_stroke")
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(m, st, leaf_limit, args.cpu_sample_dabs)
     value = total_v / (total_ms / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded icosphere, Gaussian radial noise, smooth-noise mask)",
-        "config": dict(cfg, parallelism=f"replicas{world}", mode="CUDA graph per stroke"),
+        "config": dict(cfg, parallelism=f"replicas{world}",
+                       mode=f"persistent stroke kernel, cluster of {cluster} CTAs (autotuned)"),
         "e2e": {"value": e2e_v / (e2e_ms / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": int(V * 16 + V * 12), "d2h_bytes_per_step": int(V * 16)},
         "gpu_launches": launches,
-        "graph_nodes_per_step": graph_nodes,
-        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "alg_bytes_per_launch": d["alg_bytes"] / d["launches"],
-                     "mean_launch_us": 1e3 * d["total_ms"] / d["launches"],
+        "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS hbm_gbs)",
+                     "alg_bytes_per_launch": alg_bytes, "mean_launch_ms": step_ms,
                      "traffic": traffic},
-        "kernels": {k: {"launches": v["launches"], "total_ms": round(v["total_ms"], 4),
-                        "GBps": (v["alg_bytes"] / (v["total_ms"] / 1e3) / 1e9)
-                        if v["total_ms"] > 0 else None} for k, v in prof.items()},
-        "plain_eager": {"value": eager_v / (eager_ms / 1e3), "unit": UNIT,
-                        "ms_per_step": eager_ms / 2},
+        "team_phases_ms": {k: round(v["ms"], 4) for k, v in phases.items()},
+        "team_phases_bytes": {k: v["bytes"] for k, v in phases.items()},
+        "autotune_ms": tune_ms,
+        "plain_graph": plain_graph,
+        "plain_eager": plain_eager,
+        "batch": batch,
         "cpu_baseline": ({k: v for k, v in cpu.items() if k != "seconds"} if cpu else None),
         "clocks": clk,
     }
@@ -323,10 +366,55 @@ def run_gpu(args):
     return 0
 
 
+def run_batch(args, synth, PBVH, batch_stroke, BATCH_TEAM, BATCH_SEQUENTIAL):
+    """The 64-mesh uneven batch: one persistent launch versus 64 sequential
+    plain strokes (each a CUDA graph of per-call kernels)."""
+    batch = synth.cfg4_batch()
+    gs = [PBVH.build_mesh(mm, ll) for (mm, _, ll) in batch]
+    strokes = [s for (_, s, _) in batch]
+    for p in gs:
+        p.snapshot()
+    nverts = sum(mm.totvert for (mm, _, _) in batch)
+    best = None
+    for cl in (4, 8, 16):
+        for p in gs:
+            p.restore()
+        batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=cl)
+        ms_l = []
+        for _ in range(3):
+            for p in gs:
+                p.restore()
+            gs[0].flush_l2()
+            stats, ms = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=cl)
+            ms_l.append(ms)
+        disp = sum(s.verts_displaced for s in stats)
+        ms = statistics.median(ms_l)
+        if best is None or ms < best["ms_per_step"]:
+            best = {"cluster": cl, "ms_per_step": ms, "value": disp / (ms / 1e3)}
+    for p in gs:
+        p.restore()
+    batch_stroke(gs, strokes, mode=BATCH_SEQUENTIAL)  # graph captures
+    for p in gs:
+        p.restore()
+    t0 = time.perf_counter()
+    stats, seq_ms = batch_stroke(gs, strokes, mode=BATCH_SEQUENTIAL)
+    wall = (time.perf_counter() - t0) * 1e3
+    disp = sum(s.verts_displaced for s in stats)
+    return {"workload": "64 meshes (grid/uv-sphere alternating, log-uniform 1e4-5e5 verts, "
+                        f"{nverts} verts total), 32-dab draw/inflate strokes",
+            "persistent": {"value": best["value"], "unit": UNIT, "ms_per_step": best["ms_per_step"],
+                           "cluster": best["cluster"]},
+            "sequential_plain": {"value": disp / (seq_ms / 1e3), "unit": UNIT,
+                                 "ms_per_step": seq_ms, "wall_ms": wall},
+            "speedup": best["value"] / (disp / (seq_ms / 1e3))}
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.quick:
+        return run_quick(args)
     return run_gpu(args)
 
 

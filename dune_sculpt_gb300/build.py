@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
-CU_SOURCES = ["kernels.cu", "kernels_grids.cu", "api.cu"]
+CU_SOURCES = ["kernels.cu", "kernels_grids.cu", "kernels_team.cu", "api.cu"]
 CXX_SOURCES = ["host_pbvh.cpp"]
 
 
@@ -81,7 +81,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError("libsculptgpu compilation failed")
     objs = [os.path.join(BUILD, s + ".o") for s in CU_SOURCES + CXX_SOURCES]
     tmp = LIB + ".tmp"
-    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xlinker", "--no-undefined"]
     if run(link) != 0:
         raise RuntimeError("libsculptgpu link failed")
     os.replace(tmp, LIB)

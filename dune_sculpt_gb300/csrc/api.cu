@@ -14,6 +14,10 @@
 #include "sgpu_device.cuh"
 #include "sgpu_host.h"
 #include "sgpu_kernels.h"
+#include "sgpu_team.h"
+
+#include <algorithm>
+#include <chrono>
 
 using namespace sgpu;
 
@@ -50,6 +54,7 @@ struct sgpu_mesh {
   DevMesh dev{};
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_h0 = nullptr, ev_h1 = nullptr;  // host-buffer path
   std::vector<void*> allocs;
   int* d_nodes_tmp = nullptr;
   bool has_mask = false;
@@ -75,6 +80,14 @@ struct sgpu_mesh {
   float4* snap_orig_vb = nullptr;
   int* snap_flag = nullptr;
   void* flush_buf = nullptr;
+  // persistent stroke kernel: cluster size and device staging of the job
+  int team_cluster = 8;
+  DevMesh* t_meshes = nullptr;
+  TeamJob* t_jobs = nullptr;
+  float* t_dabs = nullptr;
+  int* t_tools = nullptr;
+  int* t_counter = nullptr;
+  size_t t_dab_cap = 0, t_tool_cap = 0;
 
   cudaEvent_t prof_event() {
     if (ev_used == ev_pool.size()) {
@@ -125,6 +138,8 @@ struct sgpu_mesh {
     allocs.clear();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (ev_h0) cudaEventDestroy(ev_h0);
+    if (ev_h1) cudaEventDestroy(ev_h1);
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     ev_pool.clear();
     if (stream) cudaStreamDestroy(stream);
@@ -191,6 +206,12 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->upload_mut(&d.leaf_flag, lflag))) return rc;
   if ((rc = m->upload(&d.level_off, h.level_off))) return rc;
   if ((rc = m->upload(&d.level_nodes, h.level_nodes))) return rc;
+  if ((rc = m->upload(&d.node_leaf_lo, h.leaf_lo))) return rc;
+  if ((rc = m->upload(&d.node_leaf_hi, h.leaf_hi))) return rc;
+  if ((rc = m->alloc(&d.hit_list[0], static_cast<size_t>(h.totvert)))) return rc;
+  if ((rc = m->alloc(&d.hit_list[1], static_cast<size_t>(h.totvert)))) return rc;
+  if ((rc = m->alloc(&d.tag_list, static_cast<size_t>(h.totvert)))) return rc;
+  if ((rc = m->alloc(&d.touch_list, L + 1))) return rc;
   if ((rc = m->alloc(&d.work, 1))) return rc;
   if ((rc = m->alloc(&d.cull_list, L + 1))) return rc;
   if ((rc = m->alloc(&d.cull_off, L + 2))) return rc;
@@ -365,6 +386,14 @@ int enqueue_stroke(Launcher& L, const SGPU_Brush* brush, const SGPU_Dab* dabs, i
 int run_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
                const int* dab_tools, int mode, int* launches_out);
 int finish_stroke(sgpu_mesh* mesh, int mode, int launches, SGPU_StrokeStats* stats);
+int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_Dab* dabs,
+               const int* offs, const int* tools, int cluster, cudaStream_t s,
+               SGPU_StrokeStats* stats, float* total_ms);
+// Profiling counters handed to the next persistent launch (nullptr otherwise).
+thread_local unsigned long long* g_team_prof_bytes = nullptr;
+thread_local unsigned long long* g_team_phase_ns = nullptr;
+int validate_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+                    const int* dab_tools);
 
 int upload_node_list(sgpu_mesh* m, const int* nodes, int totnode) {
   if (totnode < 0 || totnode > m->dev.nleaf)
@@ -536,7 +565,7 @@ int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPol
   if ((rc = upload_pbvh(m))) return bail(rc);
   if (!vert_normals) {
     // Every vertex tagged and every leaf flagged, then one normal update.
-    CK(cudaMemsetAsync(d.vtag, 1, totvert, m->stream), "tag all");
+    CK(cudaMemsetAsync(d.vtag, 1, sizeof(unsigned int) * totvert, m->stream), "tag all");
     std::vector<int> lflag(d.nleaf);
     for (int k = 0; k < d.nleaf; k++) lflag[k] = h.flag[h.leaf_nodes[k]] | kUpdateNormals;
     CK(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf, cudaMemcpyHostToDevice,
@@ -782,11 +811,146 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   if (brush->symmetry < 0 || brush->symmetry > 7)
     return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
+  if (mode == SGPU_STROKE_TEAM) {
+    const int offs[2] = {0, ndabs};
+    sgpu_mesh* one[1] = {mesh};
+    float total_ms = 0.0f;
+    rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh->team_cluster, mesh->stream,
+                    stats, &total_ms);
+    return rc;
+  }
   CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
   int launches = 0;
   if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, mode, &launches))) return rc;
   CK(cudaEventRecord(mesh->ev1, mesh->stream), "event");
   return finish_stroke(mesh, mode, launches, stats);
+}
+
+int sgpu_stroke_team_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
+                             int ndabs, const int* dab_tools, SGPU_TeamProfile* out,
+                             SGPU_StrokeStats* stats) {
+  int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
+  if (rc) return rc;
+  if (!out) return fail(SGPU_ERR_INVALID_ARG, "NULL profile");
+  unsigned long long* counters = nullptr;
+  CK(cudaMalloc(&counters, sizeof(unsigned long long) * 2 * kTeamPhases), "cudaMalloc");
+  CK(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2 * kTeamPhases, mesh->stream),
+     "memset");
+  g_team_prof_bytes = counters;
+  g_team_phase_ns = counters + kTeamPhases;
+  const int offs[2] = {0, ndabs};
+  sgpu_mesh* one[1] = {mesh};
+  float total = 0.0f;
+  SGPU_StrokeStats st;
+  rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh->team_cluster, mesh->stream, &st,
+                  &total);
+  g_team_prof_bytes = nullptr;
+  g_team_phase_ns = nullptr;
+  unsigned long long host[2 * kTeamPhases] = {};
+  if (!rc) cudaMemcpy(host, counters, sizeof(host), cudaMemcpyDeviceToHost);
+  cudaFree(counters);
+  if (rc) return rc;
+  std::memset(out, 0, sizeof(*out));
+  out->total_ms = total;
+  for (int k = 0; k < kTeamPhases && k < SGPU_TEAM_PHASES; k++) {
+    out->phase_bytes[k] = static_cast<double>(host[k]);
+    out->phase_ms[k] = static_cast<double>(host[kTeamPhases + k]) * 1e-6;
+  }
+  if (stats) *stats = st;
+  return SGPU_OK;
+}
+
+int sgpu_mesh_set_team(sgpu_mesh* mesh, int cluster_size) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (cluster_size != 1 && cluster_size != 2 && cluster_size != 4 && cluster_size != 8 &&
+      cluster_size != 16)
+    return fail(SGPU_ERR_INVALID_ARG, "cluster size must be 1, 2, 4, 8 or 16");
+  mesh->team_cluster = cluster_size;
+  return SGPU_OK;
+}
+
+int sgpu_mesh_get_team(const sgpu_mesh* mesh, int* cluster_size) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (cluster_size) *cluster_size = mesh->team_cluster;
+  return SGPU_OK;
+}
+
+int sgpu_autotune_team(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
+                       int ndabs, const int* dab_tools, int* r_cluster, float* r_ms) {
+  int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
+  if (rc) return rc;
+  if ((rc = sgpu_mesh_snapshot(mesh))) return rc;
+  const int sizes[5] = {1, 2, 4, 8, 16};
+  int best = mesh->team_cluster;
+  float best_ms = -1.0f;
+  for (int k = 0; k < 5; k++) {
+    float ms = -1.0f;
+    if (team_max_active_clusters(sizes[k], mesh->dev.totnode, mesh->dev.nleaf) > 0) {
+      const int offs[2] = {0, ndabs};
+      sgpu_mesh* one[1] = {mesh};
+      // two trials, keep the second (the first pays one-time setup)
+      for (int trial = 0; trial < 2; trial++) {
+        if ((rc = sgpu_mesh_restore(mesh))) return rc;
+        SGPU_StrokeStats st;
+        float total = 0.0f;
+        if ((rc = team_batch(one, 1, brush, dabs, offs, dab_tools, sizes[k], mesh->stream, &st,
+                             &total)))
+          return rc;
+        ms = total;
+      }
+      if (best_ms < 0.0f || ms < best_ms) {
+        best_ms = ms;
+        best = sizes[k];
+      }
+    }
+    if (r_ms) r_ms[k] = ms;
+  }
+  if ((rc = sgpu_mesh_restore(mesh))) return rc;
+  mesh->team_cluster = best;
+  if (r_cluster) *r_cluster = best;
+  return SGPU_OK;
+}
+
+int sgpu_batch_stroke(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes,
+                      const SGPU_Dab* dabs, const int* dab_offsets, const int* dab_tools,
+                      int mode, int cluster_size, SGPU_StrokeStats* stats, float* r_total_ms) {
+  if (!meshes || nmesh <= 0 || !brushes || !dab_offsets)
+    return fail(SGPU_ERR_INVALID_ARG, "NULL or empty batch");
+  for (int i = 0; i < nmesh; i++) {
+    const int nd = dab_offsets[i + 1] - dab_offsets[i];
+    int rc = validate_stroke(meshes[i], &brushes[i], dabs + dab_offsets[i], nd,
+                             dab_tools ? dab_tools + dab_offsets[i] : nullptr);
+    if (rc) return rc;
+  }
+  for (int i = 0; i < nmesh; i++) CK(cudaStreamSynchronize(meshes[i]->stream), "sync");
+  if (mode == SGPU_BATCH_TEAM) {
+    const int cl = cluster_size > 0 ? cluster_size : meshes[0]->team_cluster;
+    float total = 0.0f;
+    int rc = team_batch(meshes, nmesh, brushes, dabs, dab_offsets, dab_tools, cl,
+                        meshes[0]->stream, stats, &total);
+    if (r_total_ms) *r_total_ms = total;
+    return rc;
+  }
+  if (mode != SGPU_BATCH_SEQUENTIAL) return fail(SGPU_ERR_INVALID_ARG, "unknown batch mode");
+  // one plain graph-mode stroke per mesh, one after another on the first
+  // mesh's timeline (each waits for the previous one to finish)
+  cudaEvent_t t0 = meshes[0]->ev0, t1 = nullptr;
+  CK(cudaEventRecord(t0, meshes[0]->stream), "event");
+  float sum = 0.0f;
+  for (int i = 0; i < nmesh; i++) {
+    const int nd = dab_offsets[i + 1] - dab_offsets[i];
+    SGPU_StrokeStats st;
+    int rc = sgpu_stroke(meshes[i], &brushes[i], dabs + dab_offsets[i], nd,
+                         dab_tools ? dab_tools + dab_offsets[i] : nullptr, SGPU_STROKE_GRAPH, &st);
+    if (rc) return rc;
+    if (stats) stats[i] = st;
+    sum += st.gpu_ms;
+  }
+  (void)t1;
+  if (r_total_ms) *r_total_ms = sum;
+  return SGPU_OK;
 }
 
 }  // extern "C"
@@ -815,14 +979,20 @@ extern "C" {
 
 int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
                      const int* dab_tools, const SGPU_MVert* verts_in,
-                     const float* vert_normals_in, SGPU_MVert* verts_out,
+                     const float* vert_normals_in, SGPU_MVert* verts_out, int mode,
                      SGPU_StrokeStats* stats) {
   int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
   if (rc) return rc;
   if (mesh->dev.type != kFaces) return fail(SGPU_ERR_INVALID_ARG, "not a FACES mesh");
   if (!verts_in || !verts_out) return fail(SGPU_ERR_INVALID_ARG, "NULL host buffers");
+  if (mode != SGPU_STROKE_EAGER && mode != SGPU_STROKE_GRAPH && mode != SGPU_STROKE_TEAM)
+    return fail(SGPU_ERR_INVALID_ARG, "unknown stroke mode %d", mode);
+  if (!mesh->ev_h0) {
+    CK(cudaEventCreate(&mesh->ev_h0), "cudaEventCreate");
+    CK(cudaEventCreate(&mesh->ev_h1), "cudaEventCreate");
+  }
   DevMesh& d = mesh->dev;
-  CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
+  CK(cudaEventRecord(mesh->ev_h0, mesh->stream), "event");
   CK(cudaMemcpyAsync(d.co, verts_in, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
                      mesh->stream),
      "upload verts");
@@ -834,13 +1004,39 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
   CK(launch_mark_all(d, kUpdateBB | kUpdateOriginalBB, mesh->stream), "mark kernel");
   CK(launch_update_faces(d, 0, kUpdateBB | kUpdateOriginalBB, mesh->stream), "bounds kernel");
   int launches = 2;
-  if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, SGPU_STROKE_GRAPH, &launches)))
-    return rc;
+  SGPU_StrokeStats inner;
+  std::memset(&inner, 0, sizeof(inner));
+  if (mode == SGPU_STROKE_TEAM) {
+    const int offs[2] = {0, ndabs};
+    sgpu_mesh* one[1] = {mesh};
+    float total = 0.0f;
+    if ((rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh->team_cluster, mesh->stream,
+                         &inner, &total)))
+      return rc;
+    launches += 1;
+  } else {
+    if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, mode, &launches))) return rc;
+  }
   CK(cudaMemcpyAsync(verts_out, d.co, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
                      mesh->stream),
      "download verts");
-  CK(cudaEventRecord(mesh->ev1, mesh->stream), "event");
-  return finish_stroke(mesh, SGPU_STROKE_GRAPH, launches, stats);
+  CK(cudaEventRecord(mesh->ev_h1, mesh->stream), "event");
+  unsigned long long displaced = 0;
+  if (mode != SGPU_STROKE_TEAM)
+    CK(cudaMemcpyAsync(&displaced, &d.work->displaced, sizeof(displaced), cudaMemcpyDeviceToHost,
+                       mesh->stream),
+       "read counter");
+  if ((rc = device_err(mesh))) return rc;
+  if (stats) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, mesh->ev_h0, mesh->ev_h1), "elapsed");
+    stats->verts_displaced =
+        mode == SGPU_STROKE_TEAM ? inner.verts_displaced : static_cast<int64_t>(displaced);
+    stats->gpu_ms = ms;
+    stats->kernel_launches = launches;
+    stats->graph_nodes = mode == SGPU_STROKE_GRAPH ? mesh->g_nodes : 0;
+  }
+  return SGPU_OK;
 }
 
 int sgpu_stroke_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
@@ -1199,3 +1395,144 @@ int sgpu_curve_table(int preset, float* table_xy, float* params) {
 }
 
 }  // extern "C"
+
+namespace {
+
+template <class T>
+int ensure_dev(T** p, size_t* cap, size_t n) {
+  if (*p && n <= *cap) return SGPU_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  const size_t want = n > 0 ? n : 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), want * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  *cap = want;
+  return SGPU_OK;
+}
+
+// One persistent launch over the meshes: jobs (whole strokes) are ordered by
+// estimated work, longest first, and taken by cluster teams from a counter.
+int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_Dab* dabs,
+               const int* offs, const int* tools, int cluster, cudaStream_t s,
+               SGPU_StrokeStats* stats, float* total_ms) {
+  sgpu_mesh* m0 = meshes[0];
+  int max_nodes = 0, max_leaves = 0;
+  for (int i = 0; i < n; i++) {
+    if (meshes[i]->dev.type != kFaces)
+      return fail(SGPU_ERR_UNSUPPORTED, "the persistent stroke kernel takes FACES meshes");
+    max_nodes = std::max(max_nodes, meshes[i]->dev.totnode);
+    max_leaves = std::max(max_leaves, meshes[i]->dev.nleaf);
+  }
+  if (max_leaves > 64 * 256 || team_smem_bytes(max_nodes, max_leaves) > 160 * 1024)
+    return fail(SGPU_ERR_UNSUPPORTED, "PBVH too large for the persistent stroke kernel");
+  const int nteams_max = team_max_active_clusters(cluster, max_nodes, max_leaves);
+  if (nteams_max <= 0)
+    return fail(SGPU_ERR_UNSUPPORTED, "cluster size %d cannot be launched", cluster);
+  static size_t mesh_cap = 0, job_cap = 0;  // capacities of m0's staging (per process)
+  (void)mesh_cap;
+  (void)job_cap;
+  size_t cap_m = m0->t_meshes ? static_cast<size_t>(n) : 0, cap_j = cap_m;
+  int rc;
+  // staging buffers live on the first mesh; re-create when too small
+  static thread_local std::vector<DevMesh> h_meshes;
+  static thread_local std::vector<TeamJob> h_jobs;
+  h_meshes.assign(n, DevMesh{});
+  h_jobs.assign(n, TeamJob{});
+  const size_t ndab = static_cast<size_t>(offs[n]);
+  {
+    size_t c = m0->t_meshes ? m0->t_dab_cap : 0;
+    (void)c;
+  }
+  if ((rc = ensure_dev(&m0->t_dabs, &m0->t_dab_cap, ndab * 6))) return rc;
+  if (tools && (rc = ensure_dev(&m0->t_tools, &m0->t_tool_cap, ndab))) return rc;
+  {
+    // mesh/job tables: sized to n each call (small)
+    if (m0->t_meshes) cudaFree(m0->t_meshes);
+    if (m0->t_jobs) cudaFree(m0->t_jobs);
+    m0->t_meshes = nullptr;
+    m0->t_jobs = nullptr;
+    size_t c1 = 0, c2 = 0;
+    if ((rc = ensure_dev(&m0->t_meshes, &c1, static_cast<size_t>(n)))) return rc;
+    if ((rc = ensure_dev(&m0->t_jobs, &c2, static_cast<size_t>(n)))) return rc;
+    if (!m0->t_counter) {
+      size_t c3 = 0;
+      if ((rc = ensure_dev(&m0->t_counter, &c3, 1))) return rc;
+    }
+  }
+  (void)cap_m;
+  (void)cap_j;
+  std::vector<int> order(n);
+  std::vector<double> est(n);
+  for (int i = 0; i < n; i++) {
+    order[i] = i;
+    const double r = brushes[i].radius;
+    const int nd = offs[i + 1] - offs[i];
+    const int passes = 1 << __builtin_popcount(brushes[i].symmetry & 7);
+    est[i] = static_cast<double>(nd) * passes *
+             (static_cast<double>(meshes[i]->dev.totvert) * r * r + 64.0 * meshes[i]->dev.nleaf);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return est[a] > est[b]; });
+  for (int j = 0; j < n; j++) {
+    const int i = order[j];
+    h_meshes[j] = meshes[i]->dev;
+    h_meshes[j].prof = nullptr;
+    TeamJob& job = h_jobs[j];
+    job.mesh = j;
+    job.ndabs = offs[i + 1] - offs[i];
+    job.symmetry = brushes[i].symmetry & 7;
+    job.use_orig = brushes[i].use_original_bb;
+    for (int k = 0; k < 3; k++) job.view[k] = brushes[i].view_normal[k];
+    job.dabs = m0->t_dabs + static_cast<size_t>(offs[i]) * 6;
+    job.tools = tools ? m0->t_tools + offs[i] : nullptr;
+    if (!make_brush(&brushes[i], brushes[i].sculpt_tool, &job.brush))
+      return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brushes[i].curve_preset);
+  }
+  CK(cudaEventRecord(m0->ev0, s), "event");
+  if (ndab)
+    CK(cudaMemcpyAsync(m0->t_dabs, dabs, sizeof(SGPU_Dab) * ndab, cudaMemcpyHostToDevice, s),
+       "upload dabs");
+  if (tools && ndab)
+    CK(cudaMemcpyAsync(m0->t_tools, tools, sizeof(int) * ndab, cudaMemcpyHostToDevice, s),
+       "upload tools");
+  CK(cudaMemcpyAsync(m0->t_meshes, h_meshes.data(), sizeof(DevMesh) * n, cudaMemcpyHostToDevice, s),
+     "upload mesh table");
+  CK(cudaMemcpyAsync(m0->t_jobs, h_jobs.data(), sizeof(TeamJob) * n, cudaMemcpyHostToDevice, s),
+     "upload jobs");
+  CK(cudaMemsetAsync(m0->t_counter, 0, sizeof(int), s), "reset job counter");
+  for (int i = 0; i < n; i++)
+    CK(cudaMemsetAsync(&meshes[i]->dev.work->displaced, 0, sizeof(unsigned long long), s),
+       "reset counter");
+  TeamArgs a;
+  a.meshes = m0->t_meshes;
+  a.jobs = m0->t_jobs;
+  a.njobs = n;
+  a.next_job = m0->t_counter;
+  a.max_nodes = max_nodes;
+  a.max_leaves = max_leaves;
+  a.prof_bytes = g_team_prof_bytes;
+  a.phase_ns = g_team_phase_ns;
+  const int nteams = std::min(n, nteams_max);
+  CK(launch_team_stroke(a, cluster, nteams, s), "persistent stroke kernel");
+  CK(cudaEventRecord(m0->ev1, s), "event");
+  std::vector<unsigned long long> disp(n, 0);
+  for (int i = 0; i < n; i++)
+    CK(cudaMemcpyAsync(&disp[i], &meshes[i]->dev.work->displaced, sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, s),
+       "read counter");
+  CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, m0->ev0, m0->ev1), "elapsed");
+  for (int i = 0; i < n; i++) {
+    if ((rc = device_err(meshes[i]))) return rc;
+    if (stats) {
+      stats[i].verts_displaced = static_cast<int64_t>(disp[i]);
+      stats[i].gpu_ms = ms;
+      stats[i].kernel_launches = (i == 0) ? 1 : 0;
+      stats[i].graph_nodes = 0;
+    }
+  }
+  if (total_ms) *total_ms = ms;
+  return SGPU_OK;
+}
+
+}  // namespace

@@ -267,6 +267,19 @@ void derive_tables(HostMesh& m) {
       if (!(m.flag[i] & kLeaf) && depth[i] == d) m.level_nodes.push_back(i);
     m.level_off.push_back(static_cast<int>(m.level_nodes.size()));
   }
+  // Leaves of a subtree are consecutive in left-first DFS order.
+  m.leaf_lo.assign(n, 0);
+  m.leaf_hi.assign(n, 0);
+  for (int i = 0; i < n; i++)
+    if (m.flag[i] & kLeaf) {
+      m.leaf_lo[i] = m.node_leaf[i];
+      m.leaf_hi[i] = m.node_leaf[i] + 1;
+    }
+  for (int node : m.level_nodes) {  // deepest first: children are done
+    const int c = m.children[node];
+    m.leaf_lo[node] = m.leaf_lo[c];
+    m.leaf_hi[node] = m.leaf_hi[c + 1];
+  }
 }
 
 void build_vertex_looptri(HostMesh& m) {

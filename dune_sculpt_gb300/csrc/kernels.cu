@@ -156,51 +156,6 @@ __global__ void __launch_bounds__(kCullThreads) k_set_list(DevMesh m, const int*
 // s = 128 .. 1; leaf partials then merge pairwise over the culled-list index
 // (i, i+s), s = 1, 2, 4, ...  The last CTA to finish performs that final tree.
 
-struct Lane {
-  CSum v[6];
-  int n_no, n_co;
-};
-
-__device__ __forceinline__ void lane_merge(Lane& a, const Lane& b) {
-#pragma unroll
-  for (int k = 0; k < 6; k++) a.v[k] = cs_merge(a.v[k], b.v[k]);
-  a.n_no += b.n_no;
-  a.n_co += b.n_co;
-}
-
-__device__ __forceinline__ Lane lane_shfl_down(const Lane& a, int s) {
-  Lane r;
-#pragma unroll
-  for (int k = 0; k < 6; k++) {
-    r.v[k].s = __shfl_down_sync(0xffffffffu, a.v[k].s, s);
-    r.v[k].e = __shfl_down_sync(0xffffffffu, a.v[k].e, s);
-  }
-  r.n_no = __shfl_down_sync(0xffffffffu, a.n_no, s);
-  r.n_co = __shfl_down_sync(0xffffffffu, a.n_co, s);
-  return r;
-}
-
-__device__ __forceinline__ void part_store(AreaPart* p, const Lane& l) {
-#pragma unroll
-  for (int k = 0; k < 6; k++) {
-    __stcg(&p->s[k], l.v[k].s);
-    __stcg(&p->e[k], l.v[k].e);
-  }
-  __stcg(&p->n_no, l.n_no);
-  __stcg(&p->n_co, l.n_co);
-}
-__device__ __forceinline__ Lane part_load(const AreaPart* p) {
-  Lane l;
-#pragma unroll
-  for (int k = 0; k < 6; k++) {
-    l.v[k].s = __ldcg(&p->s[k]);
-    l.v[k].e = __ldcg(&p->e[k]);
-  }
-  l.n_no = __ldcg(&p->n_no);
-  l.n_co = __ldcg(&p->n_co);
-  return l;
-}
-
 __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassParams pp) {
   __shared__ Lane sl[kThreads];
   __shared__ bool am_last;
@@ -343,12 +298,6 @@ __device__ __forceinline__ void load_curve(const DevBrush& b, float* y) {
   __syncthreads();
 }
 
-__device__ __forceinline__ void cross3(float* r, const float* a, const float* b) {
-  r[0] = a[1] * b[2] - a[2] * b[1];
-  r[1] = a[2] * b[0] - a[0] * b[2];
-  r[2] = a[0] * b[1] - a[1] * b[0];
-}
-
 // Draw, inflate and clay strips (one pass each; positions written in place,
 // each vertex by exactly one thread since leaves expose unique vertices).
 __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassParams pp) {
@@ -356,8 +305,6 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
   load_curve(b, ys);
   const int cnt = m.work->cull_count;
   const int total = m.cull_off[cnt];
-  const float radius = b.radius;
-  const float radius_sq = radius * radius;
   float area_no[3] = {0.0f, 0.0f, 0.0f}, area_co[3] = {0.0f, 0.0f, 0.0f};
   if (b.tool == kToolDraw || b.tool == kToolClayStrips) {
     for (int k = 0; k < 3; k++) {
@@ -365,24 +312,9 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
       area_co[k] = __ldcg(&m.work->area_co[k]);
     }
   }
-  // Clay strips frame: z = area normal, x = z cross grab delta, y = z cross x.
-  float xa[3], ya[3], pd = 0.0f, inv_r = 0.0f, inv_rz = 0.0f;
-  if (b.tool == kToolClayStrips) {
-    cross3(xa, area_no, pp.delta);
-    if (normalize3(xa[0], xa[1], xa[2]) == 0.0f) return;
-    cross3(ya, area_no, xa);
-    if (normalize3(ya[0], ya[1], ya[2]) == 0.0f) return;
-    const float rsign = b.strength < 0.0f ? -radius : radius;
-    const float displace = rsign * (0.18f + b.plane_offset);
-    float p[3];
-    for (int k = 0; k < 3; k++) p[k] = area_co[k] + area_no[k] * displace;
-    pd = -(area_no[0] * p[0] + area_no[1] * p[1] + area_no[2] * p[2]);
-    inv_r = 1.0f / radius;
-    inv_rz = 1.0f / (radius * 1.25f);
-  }
+  BrushFrame f;
+  if (!make_frame(b, pp, area_no, area_co, f)) return;
   mark_culled(m, cnt);
-  const float dd = radius * b.strength;
-  const float off[3] = {area_no[0] * dd, area_no[1] * dd, area_no[2] * dd};
   unsigned long long ab = 0;  // algorithmic bytes (profiling)
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < total; base += stride) {
@@ -392,51 +324,7 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
       const int k = find_slot(m.cull_off, cnt, i);
       const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
       float4 co = m.co[v];
-      bool hit = false;
-      if (b.tool == kToolDraw) {
-        const float d2 = dist_sq(co, pp.loc);
-        if (d2 <= radius_sq) {
-          const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
-          co.x = co.x + off[0] * sf;
-          co.y = co.y + off[1] * sf;
-          co.z = co.z + off[2] * sf;
-          hit = true;
-          moved = sf != 0.0f;
-        }
-      } else if (b.tool == kToolInflate) {
-        const float d2 = dist_sq(co, pp.loc);
-        if (d2 <= radius_sq) {
-          const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
-          const float fade = b.strength * sf;
-          const float kk = fade * radius;
-          const float4 no = m.no[v];
-          co.x = co.x + no.x * kk;
-          co.y = co.y + no.y * kk;
-          co.z = co.z + no.z * kk;
-          hit = true;
-          moved = sf != 0.0f;
-        }
-      } else {  // clay strips
-        const float r0 = co.x - pp.loc[0], r1 = co.y - pp.loc[1], r2 = co.z - pp.loc[2];
-        const float lx = fabsf((r0 * xa[0] + r1 * xa[1] + r2 * xa[2]) * inv_r);
-        const float ly = fabsf((r0 * ya[0] + r1 * ya[1] + r2 * ya[2]) * inv_r);
-        const float lz = fabsf((r0 * area_no[0] + r1 * area_no[1] + r2 * area_no[2]) * inv_rz);
-        if (lx <= 1.0f && ly <= 1.0f && lz <= 1.0f) {
-          const float dloc = (lx > ly) ? lx : ly;
-          const float sf = strength_factor(m, b, ys, pp, v, radius * dloc, radius);
-          const float fade = b.strength * sf;
-          const float side = (co.x * area_no[0] + co.y * area_no[1] + co.z * area_no[2]) + pd;
-          const float ns = -side;
-          const float v0 = (co.x + area_no[0] * ns) - co.x;
-          const float v1 = (co.y + area_no[1] * ns) - co.y;
-          const float v2 = (co.z + area_no[2] * ns) - co.z;
-          co.x = co.x + v0 * fade;
-          co.y = co.y + v1 * fade;
-          co.z = co.z + v2 * fade;
-          hit = true;
-          moved = sf != 0.0f;
-        }
-      }
+      const bool hit = brush_vertex(m, b, ys, pp, f, v, co, moved);
       if (hit) {
         m.co[v] = co;
         if (m.type == kFaces) m.vtag[v] = 1;
@@ -452,47 +340,12 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
 
 // Smooth, one Jacobi sweep in two launches: compute new positions from the
 // sweep-start state into scratch (w = 1 marks a hit), then write them back.
-__device__ __forceinline__ float3 neighbor_average(const DevMesh& m, int v, float4 c0) {
-  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-  int n = 0;
-  if (m.type == kFaces) {
-    const int e = m.nb_off[v + 1];
-    for (int q = m.nb_off[v]; q < e; q++) {
-      const float4 c = m.co[m.nb_idx[q]];
-      sx += c.x;
-      sy += c.y;
-      sz += c.z;
-      n++;
-    }
-  } else {
-    const int gs = m.grid_size, area = m.grid_area;
-    const int g = v / area, r = v % area, x = r % gs, y = r / gs;
-    const int nx[4] = {x - 1, x + 1, x, x};
-    const int ny[4] = {y, y, y - 1, y + 1};
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      if (nx[k] >= 0 && nx[k] < gs && ny[k] >= 0 && ny[k] < gs) {
-        const float4 c = m.co[g * area + ny[k] * gs + nx[k]];
-        sx += c.x;
-        sy += c.y;
-        sz += c.z;
-        n++;
-      }
-    }
-  }
-  if (n == 0) return make_float3(c0.x, c0.y, c0.z);
-  const float inv = 1.0f / (float)n;
-  return make_float3(sx * inv, sy * inv, sz * inv);
-}
-
 __global__ void __launch_bounds__(kThreads) k_smooth_compute(DevMesh m, DevBrush b,
                                                              PassParams pp) {
   __shared__ float ys[kCurveTable + 1];
   load_curve(b, ys);
   const int cnt = m.work->cull_count;
   const int total = m.cull_off[cnt];
-  const float radius = b.radius;
-  const float radius_sq = radius * radius;
   if (pp.iteration == 0) mark_culled(m, cnt);
   unsigned long long ab = 0;  // algorithmic bytes (profiling)
   const int stride = gridDim.x * blockDim.x;
@@ -503,19 +356,15 @@ __global__ void __launch_bounds__(kThreads) k_smooth_compute(DevMesh m, DevBrush
       const int k = find_slot(m.cull_off, cnt, i);
       const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
       const float4 co = m.co[v];
-      const float d2 = dist_sq(co, pp.loc);
       float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (d2 <= radius_sq) {
-        const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
-        const float fade = pp.iter_strength * sf;
-        const float3 avg = neighbor_average(m, v, co);
-        out.x = co.x + (avg.x - co.x) * fade;
-        out.y = co.y + (avg.y - co.y) * fade;
-        out.z = co.z + (avg.z - co.z) * fade;
+      bool mv = false;
+      if (smooth_vertex(m, b, ys, pp, v, co, out, mv)) {
         out.w = 1.0f;
-        moved = (pp.iteration == 0) && sf != 0.0f;
+        moved = (pp.iteration == 0) && mv;
         const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
         ab += (m.type == kFaces ? 8u : 0u) + 16ull * valence;  // ring range, ring ids + co
+      } else {
+        out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
       m.scratch[i] = out;
       ab += (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) + 16u;  // idx, co, mask, out
@@ -554,8 +403,6 @@ __global__ void __launch_bounds__(kThreads) k_smooth_apply(DevMesh m) {
 // UpdateNormals flags and runs the bottom-up flush (pbvh_flush_bb,
 // pbvh.c:3287-3317) level by level.
 
-__device__ __forceinline__ float fmin_ref(float a, float b) { return (a < b) ? a : b; }
-__device__ __forceinline__ float fmax_ref(float a, float b) { return (a > b) ? a : b; }
 
 __device__ void leaf_refit(const DevMesh& m, int leaf, float* red /* 6*kThreads/32 */,
                            unsigned long long& ab) {
@@ -616,21 +463,11 @@ __device__ void faces_leaf_normals(const DevMesh& m, int leaf, unsigned long lon
   for (int i = threadIdx.x; i < nu; i += blockDim.x) {
     const int v = m.leaf_verts[off + i];
     if (!m.vtag[v]) continue;
-    CSum ax = {0.0f, 0.0f}, ay = {0.0f, 0.0f}, az = {0.0f, 0.0f};
-    const int e = m.vt_off[v + 1];
-    ab += 24u;  // the vertex's co read and normal written
-    for (int q = m.vt_off[v]; q < e; q++) {
-      const int t = m.vt_idx[q];
-      if (!(m.leaf_flag[m.lt_leaf[t]] & kUpdateNormals)) continue;
-      ab += 16u;  // looptri record (3 vertex ids + polygon id)
-      const float3 fn = poly_normal(m, m.lt[t].w);
-      cs_add(ax, fn.x);
-      cs_add(ay, fn.y);
-      cs_add(az, fn.z);
-    }
-    float nx = ax.s + ax.e, ny = ay.s + ay.e, nz = az.s + az.e;
-    normalize3(nx, ny, nz);
-    m.no[v] = make_float4(nx, ny, nz, 0.0f);
+    float4 n;
+    const int used = vertex_normal(m, v, n);
+    // the vertex's co read and normal written; one looptri record per face used
+    ab += 24u + 16u * used;
+    m.no[v] = n;
     m.vtag[v] = 0;
   }
 }

@@ -1,0 +1,720 @@
+// Persistent stroke kernel of libsculptgpu.
+//
+// One launch runs whole strokes.  Each thread-block cluster ("team", C CTAs of
+// 256 threads, C chosen by the autotuner) takes a mesh's stroke from a work
+// queue (an atomic job counter) and runs every dab of it: per symmetry pass the
+// node search, the area normal/centre, the brush (smooth as Jacobi sweeps over
+// a compacted list of vertices inside the sphere), then the normal update and
+// the bounding-box refit with its flush; UpdateOriginalBB at the end of the
+// stroke.  Phases are separated by cluster barriers (barrier.cluster
+// arrive.release / wait.acquire), so no phase waits for a kernel boundary.
+// Meshes are independent: teams never wait for one another, and a team that
+// starts late simply finds fewer jobs.
+//
+// The arithmetic is the same device code as the per-call kernels
+// (sgpu_device.cuh), so results are bit-identical to them and to the FP32
+// restatement of the reference.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "sgpu_device.cuh"
+#include "sgpu_kernels.h"
+#include "sgpu_team.h"
+
+namespace cg = cooperative_groups;
+
+namespace sgpu {
+
+constexpr int kTeamThreads = 256;
+
+struct TeamShared {
+  DevMesh m;
+  TeamJob job;
+  int jobid;
+  int cnt, total;
+  int scan[32];
+  int run[2];
+  float area[6];
+  int nmark;
+};
+
+// Block-wide exclusive scan (kTeamThreads threads).
+__device__ int team_block_scan(int v, int* total, int* smem32) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nwarps = kTeamThreads / 32;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem32[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < nwarps ? smem32[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    smem32[lane] = w;
+  }
+  __syncthreads();
+  const int warp_base = warp > 0 ? smem32[warp - 1] : 0;
+  *total = smem32[nwarps - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+__device__ __forceinline__ bool box_hits(float4 mn, float4 mx, const float* c, float rsq) {
+  const float bmin[3] = {mn.x, mn.y, mn.z};
+  const float bmax[3] = {mx.x, mx.y, mx.z};
+  float t[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    float nearest;
+    if (bmin[i] > c[i]) {
+      nearest = bmin[i];
+    } else if (bmax[i] < c[i]) {
+      nearest = bmax[i];
+    } else {
+      nearest = c[i];
+    }
+    t[i] = c[i] - nearest;
+  }
+  return (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]) < rsq;
+}
+
+__device__ __forceinline__ int smem_find_slot(const int* off, int cnt, int i) {
+  int lo = 0, hi = cnt;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= i) {
+      lo = mid;
+    } else {
+      hi = mid;
+    }
+  }
+  return lo;
+}
+
+// Appends v to list (counter cnt) with one atomic per coalesced group.
+__device__ __forceinline__ void append(int* list, int* cnt, int v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(cnt, static_cast<int>(g.size()));
+  base = g.shfl(base, 0);
+  list[base + g.thread_rank()] = v;
+}
+
+__device__ __forceinline__ void tag_vertex(const DevMesh& m, int v, int* tag_cnt) {
+  if (atomicExch(&m.vtag[v], 1u) == 0u) append(m.tag_list, tag_cnt, v);
+}
+
+// Node search of one pass into this CTA's shared memory (every CTA of the team
+// computes the same list).  Same test and order as k_cull.
+__device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_par,
+                          unsigned char* s_pass, int* s_cl, int* s_coff, TeamShared& sh) {
+  const float4* bb = pp.original ? m.orig_vb : m.vb;
+  for (int n = threadIdx.x; n < m.totnode; n += kTeamThreads)
+    s_pass[n] = box_hits(__ldcg(&bb[2 * n]), __ldcg(&bb[2 * n + 1]), pp.loc, pp.cull_radius_sq);
+  if (threadIdx.x == 0) sh.run[0] = sh.run[1] = 0;
+  __syncthreads();
+  for (int base = 0; base < m.nleaf; base += kTeamThreads) {
+    const int id = base + threadIdx.x;
+    int ok = 0, nv = 0;
+    if (id < m.nleaf) {
+      const int node = m.leaf_node[id];
+      ok = s_pass[node];
+      int p = s_par[node];
+      while (ok && p >= 0) {
+        ok = s_pass[p];
+        p = s_par[p];
+      }
+      nv = ok ? leaf_nverts(m, id) : 0;
+    }
+    int tot_ok, tot_nv;
+    const int pos = team_block_scan(ok, &tot_ok, sh.scan);
+    const int voff = team_block_scan(nv, &tot_nv, sh.scan);
+    if (ok) {
+      s_cl[sh.run[0] + pos] = id;
+      s_coff[sh.run[0] + pos] = sh.run[1] + voff;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      sh.run[0] += tot_ok;
+      sh.run[1] += tot_nv;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    sh.cnt = sh.run[0];
+    sh.total = sh.run[1];
+    s_coff[sh.run[0]] = sh.run[1];
+  }
+  __syncthreads();
+}
+
+// Leaf box refit by the whole CTA (update_node_vb over PBVH_ITER_ALL).
+__device__ void team_leaf_refit(const DevMesh& m, int leaf, float* red) {
+  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+  float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  const int nv = leaf_nverts_all(m, leaf);
+  for (int i = threadIdx.x; i < nv; i += kTeamThreads) {
+    const int v = m.type == kFaces ? m.leaf_verts[m.leaf_vert_off[leaf] + i] : leaf_vert(m, leaf, i);
+    const float4 c = __ldcg(&m.co[v]);
+    mn[0] = fmin_ref(mn[0], c.x);
+    mn[1] = fmin_ref(mn[1], c.y);
+    mn[2] = fmin_ref(mn[2], c.z);
+    mx[0] = fmax_ref(mx[0], c.x);
+    mx[1] = fmax_ref(mx[1], c.y);
+    mx[2] = fmax_ref(mx[2], c.z);
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      mn[k] = fmin_ref(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+      mx[k] = fmax_ref(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+    }
+  }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 3; k++) {
+      red[warp * 6 + k] = mn[k];
+      red[warp * 6 + 3 + k] = mx[k];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kTeamThreads / 32; w++)
+      for (int k = 0; k < 3; k++) {
+        mn[k] = fmin_ref(mn[k], red[w * 6 + k]);
+        mx[k] = fmax_ref(mx[k], red[w * 6 + 3 + k]);
+      }
+    const int node = m.leaf_node[leaf];
+    m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+    m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+  }
+  __syncthreads();
+}
+
+// Compensated area partial of one culled leaf by the CTA (256 lanes), the same
+// structure as k_area.
+__device__ void team_area_leaf(const DevMesh& m, const PassParams& pp, float rn2, float ra2,
+                               int leaf, Lane* sl, AreaPart* out) {
+  const int t = threadIdx.x;
+  const int nv = leaf_nverts(m, leaf);
+  Lane l;
+#pragma unroll
+  for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
+  l.n_no = l.n_co = 0;
+  for (int i = t; i < nv; i += kTeamThreads) {
+    const int v = leaf_vert(m, leaf, i);
+    const float4 co = __ldcg(&m.co[v]);
+    const float d2 = dist_sq(co, pp.loc);
+    if (d2 <= rn2) {
+      const float4 no = __ldcg(&m.no[v]);
+      cs_add(l.v[0], no.x);
+      cs_add(l.v[1], no.y);
+      cs_add(l.v[2], no.z);
+      l.n_no++;
+    }
+    if (d2 <= ra2) {
+      cs_add(l.v[3], co.x);
+      cs_add(l.v[4], co.y);
+      cs_add(l.v[5], co.z);
+      l.n_co++;
+    }
+  }
+  sl[t] = l;
+  __syncthreads();
+  for (int s = kTeamThreads / 2; s >= 32; s >>= 1) {
+    if (t < s) {
+      Lane a = sl[t];
+      lane_merge(a, sl[t + s]);
+      sl[t] = a;
+    }
+    __syncthreads();
+  }
+  if (t < 32) {
+    Lane a = sl[t];
+    for (int s = 16; s >= 1; s >>= 1) {
+      const Lane o = lane_shfl_down(a, s);
+      lane_merge(a, o);
+    }
+    if (t == 0) part_store(out, a);
+  }
+  __syncthreads();
+}
+
+// Final pairwise tree over the leaf partials (i, i+s), s = 1, 2, 4, ... by one
+// CTA in shared memory; writes area normal and centre into sh.area.
+constexpr int kTeamMaxChunks = 64;  // culled leaves per pass <= 64 * 256
+
+__device__ void team_area_final(const DevMesh& m, const PassParams& pp, int cnt, Lane* sl,
+                                Lane* chunks, TeamShared& sh) {
+  // Partials are staged in shared memory in chunks of kTeamThreads (a power of
+  // two, so each chunk is a complete subtree of the pairwise tree); the chunk
+  // totals then merge with the same pairwise rule, which completes the tree.
+  const int nchunks = (cnt + kTeamThreads - 1) / kTeamThreads;
+  for (int c = 0; c < nchunks; c++) {
+    const int c0 = c * kTeamThreads;
+    const int n = min(kTeamThreads, cnt - c0);
+    if (threadIdx.x < n) sl[threadIdx.x] = part_load(&m.parts[c0 + threadIdx.x]);
+    __syncthreads();
+    for (int s = 1; s < n; s <<= 1) {
+      const int i = threadIdx.x * 2 * s;
+      if (i + s < n) {
+        Lane a = sl[i];
+        lane_merge(a, sl[i + s]);
+        sl[i] = a;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) chunks[c] = sl[0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 1; s < nchunks; s <<= 1)
+      for (int i = 0; i + s < nchunks; i += 2 * s) lane_merge(chunks[i], chunks[i + s]);
+    Lane acc;
+    if (nchunks > 0) {
+      acc = chunks[0];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 6; q++) acc.v[q].s = acc.v[q].e = 0.0f;
+      acc.n_no = acc.n_co = 0;
+    }
+    float nx = acc.v[0].s + acc.v[0].e, ny = acc.v[1].s + acc.v[1].e, nz = acc.v[2].s + acc.v[2].e;
+    normalize3(nx, ny, nz);
+    sh.area[0] = nx;
+    sh.area[1] = ny;
+    sh.area[2] = nz;
+    if (acc.n_co > 0) {
+      const float inv = 1.0f / (float)acc.n_co;
+      sh.area[3] = (acc.v[3].s + acc.v[3].e) * inv;
+      sh.area[4] = (acc.v[4].s + acc.v[4].e) * inv;
+      sh.area[5] = (acc.v[5].s + acc.v[5].e) * inv;
+    } else {
+      sh.area[3] = pp.loc[0];
+      sh.area[4] = pp.loc[1];
+      sh.area[5] = pp.loc[2];
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void team_sync(const cg::cluster_group& cluster, unsigned C) {
+  if (C > 1) {
+    cluster.sync();
+  } else {
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Profiling helpers: algorithmic bytes (warp-aggregated, converged code) and
+// per-phase time measured by the team's first thread.
+__device__ __forceinline__ void team_bytes(const TeamArgs& a, int phase, unsigned long long b) {
+  if (!a.prof_bytes) return;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&a.prof_bytes[phase], b);
+}
+
+struct PhaseClock {
+  unsigned long long last;
+  __device__ __forceinline__ void mark(const TeamArgs& a, unsigned rank, int phase) {
+    if (!a.phase_ns || rank != 0 || threadIdx.x != 0) return;
+    const unsigned long long now = global_ns();
+    atomicAdd(&a.phase_ns[phase], now - last);
+    last = now;
+  }
+};
+
+__global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned C = cluster.num_blocks();
+  const unsigned rank = cluster.block_rank();
+  const int gt = rank * kTeamThreads + threadIdx.x;
+  const int GT = C * kTeamThreads;
+  __shared__ TeamShared sh;
+  __shared__ Lane s_lanes[kTeamThreads];
+  __shared__ Lane s_chunks[kTeamMaxChunks];
+  __shared__ float s_red[6 * (kTeamThreads / 32)];
+  extern __shared__ __align__(16) unsigned char dyn[];
+  int* s_par = reinterpret_cast<int*>(dyn);
+  int* s_cl = s_par + a.max_nodes;
+  int* s_coff = s_cl + a.max_leaves + 1;
+  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_coff + a.max_leaves + 2);
+  PhaseClock clk;
+  clk.last = a.phase_ns ? global_ns() : 0ull;
+
+  for (;;) {
+    if (rank == 0 && threadIdx.x == 0) sh.jobid = atomicAdd(a.next_job, 1);
+    team_sync(cluster, C);
+    const int jid = (C > 1) ? *cluster.map_shared_rank(&sh.jobid, 0) : sh.jobid;
+    team_sync(cluster, C);
+    if (jid >= a.njobs) return;
+    {
+      const int* src = reinterpret_cast<const int*>(&a.jobs[jid]);
+      int* dst = reinterpret_cast<int*>(&sh.job);
+      for (int i = threadIdx.x; i < static_cast<int>(sizeof(TeamJob) / 4); i += kTeamThreads)
+        dst[i] = src[i];
+    }
+    __syncthreads();
+    {
+      const int* src = reinterpret_cast<const int*>(&a.meshes[sh.job.mesh]);
+      int* dst = reinterpret_cast<int*>(&sh.m);
+      for (int i = threadIdx.x; i < static_cast<int>(sizeof(DevMesh) / 4); i += kTeamThreads)
+        dst[i] = src[i];
+    }
+    __syncthreads();
+    const DevMesh& m = sh.m;
+    DevBrush& b = sh.job.brush;
+    Work* w = m.work;
+    for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_par[i] = m.node_parent[i];
+    if (rank == 0 && threadIdx.x == 0) {
+      for (int k = 0; k < 3; k++) w->hit_count[k] = 0;
+      w->tag_count[0] = w->tag_count[1] = 0;
+      w->touch_count[0] = w->touch_count[1] = 0;
+    }
+    team_sync(cluster, C);
+    // Leaves flagged and vertices tagged before the stroke (by per-call entry
+    // points) join the first dab's update, as they would in the per-call path.
+    if (rank == 0)
+      for (int leaf = threadIdx.x; leaf < m.nleaf; leaf += kTeamThreads) {
+        const int f = __ldcg(&m.leaf_flag[leaf]);
+        if (!(f & (kUpdateNormals | kUpdateBB))) continue;
+        append(m.touch_list, &w->touch_count[0], leaf);
+        if ((f & kUpdateNormals) && m.type == kFaces) {
+          const int off = m.leaf_vert_off[leaf];
+          for (int i = 0; i < m.leaf_uniq[leaf]; i++) {
+            const int v = m.leaf_verts[off + i];
+            if (__ldcg(&m.vtag[v])) m.tag_list[atomicAdd(&w->tag_count[0], 1)] = v;
+          }
+        }
+      }
+    team_sync(cluster, C);
+    clk.mark(a, rank, kPhJob);
+    const int default_tool = b.tool;
+    int q = 0;  // smooth sweep counter (hit-list rotation)
+    for (int d = 0; d < sh.job.ndabs; d++) {
+      const int par = d & 1;
+      if (rank == 0 && threadIdx.x == 0) {
+        w->tag_count[par ^ 1] = 0;
+        w->touch_count[par ^ 1] = 0;
+      }
+      const int tool = sh.job.tools ? sh.job.tools[d] : default_tool;
+      __syncthreads();
+      if (threadIdx.x == 0) b.tool = tool;
+      __syncthreads();
+      const float scale = (tool == kToolClayStrips) ? 1.41421356237309504880f : 1.0f;
+      const float r = b.radius * scale;
+      int* tag_cnt = &w->tag_count[par];
+      int* touch_cnt = &w->touch_count[par];
+      for (int pass = 0; pass < 8; pass++) {
+        if ((pass & ~sh.job.symmetry) != 0) continue;
+        PassParams pp;
+        for (int k = 0; k < 3; k++) {
+          const float sgn = (pass & (1 << k)) ? -1.0f : 1.0f;
+          pp.loc[k] = sgn * sh.job.dabs[6 * d + k];
+          pp.delta[k] = sgn * sh.job.dabs[6 * d + 3 + k];
+          pp.view[k] = sgn * sh.job.view[k];
+        }
+        pp.cull_radius_sq = r * r;
+        pp.original = sh.job.use_orig;
+        pp.iter_strength = 1.0f;
+        pp.iteration = 0;
+        team_cull(m, pp, s_par, s_pass, s_cl, s_coff, sh);
+        const int cnt = sh.cnt, total = sh.total;
+        // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
+        team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
+        clk.mark(a, rank, kPhCull);
+        float area_no[3] = {0.0f, 0.0f, 0.0f}, area_co[3] = {0.0f, 0.0f, 0.0f};
+        if (tool == kToolDraw || tool == kToolClayStrips) {
+          const float rn = b.radius * b.normal_radius_factor;
+          const float ra = b.radius * b.area_radius_factor;
+          unsigned long long ab = 0;
+          for (int k = rank; k < cnt; k += C) {
+            team_area_leaf(m, pp, rn * rn, ra * ra, s_cl[k], s_lanes, &m.parts[k]);
+            const int nv = leaf_nverts(m, s_cl[k]);
+            if (threadIdx.x < nv)
+              ab += ((m.type == kFaces ? 4ull : 0ull) + 24ull) *
+                    ((nv - threadIdx.x + kTeamThreads - 1) / kTeamThreads);
+          }
+          team_bytes(a, kPhArea, ab);
+          team_sync(cluster, C);
+          team_area_final(m, pp, cnt, s_lanes, s_chunks, sh);
+          for (int k = 0; k < 3; k++) {
+            area_no[k] = sh.area[k];
+            area_co[k] = sh.area[3 + k];
+          }
+          clk.mark(a, rank, kPhArea);
+        }
+        BrushFrame f;
+        if (!make_frame(b, pp, area_no, area_co, f)) continue;
+        if (rank == 0)
+          for (int k = threadIdx.x; k < cnt; k += kTeamThreads) {
+            const int leaf = s_cl[k];
+            const int old = atomicOr(&m.leaf_flag[leaf], kMarkUpdate);
+            if (!(old & kUpdateNormals)) append(m.touch_list, touch_cnt, leaf);
+          }
+        if (tool != kToolSmooth) {
+          unsigned long long ab = 0;
+          const unsigned vbytes = (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) +
+                                  (m.automask ? 4u : 0u) +
+                                  ((tool == kToolInflate || (b.flag & kBrushFrontFace)) ? 12u : 0u);
+          for (int base = rank * kTeamThreads; base < total; base += GT) {
+            const int i = base + threadIdx.x;
+            bool moved = false;
+            if (i < total) {
+              const int k = smem_find_slot(s_coff, cnt, i);
+              const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+              float4 co = __ldcg(&m.co[v]);
+              ab += vbytes;
+              if (brush_vertex(m, b, b.y, pp, f, v, co, moved)) {
+                m.co[v] = co;
+                ab += 12u;
+                if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+              }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, moved);
+            if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
+          }
+          team_bytes(a, kPhBrush, ab);
+          team_sync(cluster, C);
+          clk.mark(a, rank, kPhBrush);
+        } else {
+          float st = b.strength;
+          if (st < 0.0f) st = 0.0f;
+          if (st > 1.0f) st = 1.0f;
+          const int count = (int)(st * 4.0f);
+          const float last = 4.0f * (st - (float)count * 0.25f);
+          for (int it = 0; it <= count; it++, q++) {
+            pp.iter_strength = (it != count) ? 1.0f : last;
+            pp.iteration = it;
+            int* out_list = m.hit_list[q & 1];
+            const int* in_list = m.hit_list[(q + 1) & 1];
+            int* out_cnt = &w->hit_count[q % 3];
+            const int ncand = (it == 0) ? total : __ldcg(&w->hit_count[(q + 2) % 3]);
+            // sweep: candidates are the culled vertices, then the previous hits
+            // (a vertex outside the sphere does not move, so it stays outside)
+            unsigned long long ab = 0;
+            for (int base = rank * kTeamThreads; base < ncand; base += GT) {
+              const int i = base + threadIdx.x;
+              bool moved = false;
+              if (i < ncand) {
+                int v;
+                if (it == 0) {
+                  const int k = smem_find_slot(s_coff, cnt, i);
+                  v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+                } else {
+                  v = __ldcg(&in_list[i]);
+                }
+                const float4 co = __ldcg(&m.co[v]);
+                ab += 4u + 12u + (m.mask ? 4u : 0u);  // vertex id, co, mask
+                float4 out;
+                bool mv = false;
+                if (smooth_vertex(m, b, b.y, pp, v, co, out, mv)) {
+                  cg::coalesced_group g = cg::coalesced_threads();
+                  int slot = 0;
+                  if (g.thread_rank() == 0) slot = atomicAdd(out_cnt, static_cast<int>(g.size()));
+                  slot = g.shfl(slot, 0) + g.thread_rank();
+                  out_list[slot] = v;
+                  m.scratch[slot] = out;
+                  moved = (it == 0) && mv;
+                  const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
+                  // ring range and ring (id + co) reads; hit id and value written
+                  ab += (m.type == kFaces ? 8ull : 0ull) + 16ull * valence + 20ull;
+                }
+              }
+              const unsigned bal = __ballot_sync(0xffffffffu, moved);
+              if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
+            }
+            team_bytes(a, kPhBrush, ab);
+            team_sync(cluster, C);
+            clk.mark(a, rank, kPhBrush);
+            const int nhit = __ldcg(out_cnt);
+            if (rank == 0 && threadIdx.x == 0) w->hit_count[(q + 1) % 3] = 0;
+            ab = 0;
+            for (int j = gt; j < nhit; j += GT) {
+              const int v = __ldcg(&out_list[j]);
+              m.co[v] = __ldcg(&m.scratch[j]);
+              if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+              ab += 4u + 16u + 12u;  // hit id, value, co write
+            }
+            team_bytes(a, kPhApply, ab);
+            team_sync(cluster, C);
+            clk.mark(a, rank, kPhApply);
+          }
+        }
+      }
+      // normal update for the tagged vertices, refit of the touched leaves
+      const int ntag = __ldcg(tag_cnt);
+      const int ntouch = __ldcg(touch_cnt);
+      unsigned long long ab = 0;
+      if (m.type == kFaces) {
+        for (int j = gt; j < ntag; j += GT) {
+          const int v = __ldcg(&m.tag_list[j]);
+          float4 n;
+          const int used = vertex_normal(m, v, n);
+          m.no[v] = n;
+          m.vtag[v] = 0u;
+          ab += 24ull + 16ull * used;
+        }
+      }
+      for (int k = rank; k < ntouch; k += C) {
+        const int leaf = __ldcg(&m.touch_list[k]);
+        team_leaf_refit(m, leaf, s_red);
+        const int nv = leaf_nverts_all(m, leaf);
+        if (threadIdx.x < nv)
+          ab += (m.type == kFaces ? 16ull : 12ull) * ((nv - threadIdx.x + kTeamThreads - 1) / kTeamThreads);
+        if (threadIdx.x == 0) ab += 24u;
+      }
+      team_bytes(a, kPhUpdate, ab);
+      team_sync(cluster, C);
+      clk.mark(a, rank, kPhUpdate);
+      // flush: every ancestor of a touched leaf is the union of the boxes of
+      // the leaves below it (a leaf-id range in left-first DFS order)
+      for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_pass[i] = 0;
+      __syncthreads();
+      for (int k = threadIdx.x; k < ntouch; k += kTeamThreads) {
+        int p = s_par[m.leaf_node[__ldcg(&m.touch_list[k])]];
+        while (p >= 0 && !s_pass[p]) {
+          s_pass[p] = 1;
+          p = s_par[p];
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) sh.run[0] = 0;
+      __syncthreads();
+      for (int base = 0; base < m.totnode; base += kTeamThreads) {
+        const int n = base + threadIdx.x;
+        const int mk = (n < m.totnode) ? s_pass[n] : 0;
+        int tot;
+        const int pos = team_block_scan(mk, &tot, sh.scan);
+        if (mk) s_cl[sh.run[0] + pos] = n;
+        __syncthreads();
+        if (threadIdx.x == 0) sh.run[0] += tot;
+        __syncthreads();
+      }
+      const int nmark = sh.run[0];
+      const int lane = threadIdx.x & 31;
+      for (int idx = gt >> 5; idx < nmark; idx += GT >> 5) {
+        const int node = s_cl[idx];
+        float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+        float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int l = m.node_leaf_lo[node] + lane; l < m.node_leaf_hi[node]; l += 32) {
+          const int ln = m.leaf_node[l];
+          const float4 a0 = __ldcg(&m.vb[2 * ln]), a1 = __ldcg(&m.vb[2 * ln + 1]);
+          mn[0] = fmin_ref(mn[0], a0.x);
+          mn[1] = fmin_ref(mn[1], a0.y);
+          mn[2] = fmin_ref(mn[2], a0.z);
+          mx[0] = fmax_ref(mx[0], a1.x);
+          mx[1] = fmax_ref(mx[1], a1.y);
+          mx[2] = fmax_ref(mx[2], a1.z);
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            mn[k] = fmin_ref(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = fmax_ref(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+          }
+        if (lane == 0) {
+          m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+          m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+        }
+      }
+      for (int k = gt; k < ntouch; k += GT)
+        atomicAnd(&m.leaf_flag[__ldcg(&m.touch_list[k])], ~(kUpdateNormals | kUpdateBB));
+      // two child boxes read and one box written per updated ancestor
+      team_bytes(a, kPhFlush, gt < nmark ? 72ull * ((nmark - gt + GT - 1) / GT) : 0ull);
+      team_sync(cluster, C);
+      clk.mark(a, rank, kPhFlush);
+    }
+    // end of stroke: BKE_pbvh_update_bounds(UpdateOriginalBB)
+    for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_pass[i] = 0;
+    __syncthreads();
+    for (int leaf = threadIdx.x; leaf < m.nleaf; leaf += kTeamThreads) {
+      if (!(__ldcg(&m.leaf_flag[leaf]) & kUpdateOriginalBB)) continue;
+      int n = m.leaf_node[leaf];
+      s_pass[n] = 1;
+      n = s_par[n];
+      while (n >= 0 && !s_pass[n]) {
+        s_pass[n] = 1;
+        n = s_par[n];
+      }
+    }
+    __syncthreads();
+    for (int n = gt; n < m.totnode; n += GT)
+      if (s_pass[n]) {
+        m.orig_vb[2 * n] = __ldcg(&m.vb[2 * n]);
+        m.orig_vb[2 * n + 1] = __ldcg(&m.vb[2 * n + 1]);
+      }
+    team_sync(cluster, C);
+    for (int leaf = gt; leaf < m.nleaf; leaf += GT) atomicAnd(&m.leaf_flag[leaf], ~kUpdateOriginalBB);
+    team_sync(cluster, C);
+    clk.mark(a, rank, kPhJob);
+  }
+}
+
+size_t team_smem_bytes(int max_nodes, int max_leaves) {
+  return sizeof(int) * (static_cast<size_t>(max_nodes) + 2 * static_cast<size_t>(max_leaves) + 3) +
+         static_cast<size_t>(max_nodes) + 16;
+}
+
+int team_max_cluster() { return 16; }
+
+cudaError_t configure_team_kernel(size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_team_stroke, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_team_stroke, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(smem));
+}
+
+cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaStream_t s) {
+  const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves);
+  cudaError_t e = configure_team_kernel(smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(cluster * nteams));
+  cfg.blockDim = dim3(kTeamThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_team_stroke, a);
+}
+
+int team_max_active_clusters(int cluster, int max_nodes, int max_leaves) {
+  const size_t smem = team_smem_bytes(max_nodes, max_leaves);
+  if (configure_team_kernel(smem) != cudaSuccess) return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(cluster));
+  cfg.blockDim = dim3(kTeamThreads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_team_stroke, &cfg) != cudaSuccess) return 0;
+  return n;
+}
+
+}  // namespace sgpu

@@ -29,6 +29,11 @@ struct Work {
   float area_co[3];
   int area_n_co;
   unsigned int grid_epoch;  // last finished GRIDS update (work-list stamps)
+  // persistent stroke kernel: smooth hit-list counts (3-way rotation), tagged
+  // vertices and touched leaves per dab (2-way by dab parity)
+  int hit_count[3];
+  int tag_count[2];
+  int touch_count[2];
 };
 
 // Compensated partial of the area reduction: (s, e) pairs for normal xyz and
@@ -61,7 +66,7 @@ struct DevMesh {
   const int* nb_off;
   const int* nb_idx;
   const int* lt_leaf;  // looptri -> leaf id
-  unsigned char* vtag;
+  unsigned int* vtag;  // vert_bitmap, one word per vertex
   // PBVH
   float4* vb;  // 2 per node: (min xyz, 0), (max xyz, 0)
   float4* orig_vb;
@@ -77,6 +82,12 @@ struct DevMesh {
   int* leaf_flag;            // PBVHNodeFlags per leaf
   const int* level_off;      // internal nodes by depth, deepest first
   const int* level_nodes;
+  const int* node_leaf_lo;   // first leaf id under the node
+  const int* node_leaf_hi;   // one past the last leaf id under the node
+  // persistent stroke kernel work lists
+  int* hit_list[2];  // smooth: vertices inside the sphere, ping-pong per iteration
+  int* tag_list;     // vertices tagged in the current dab
+  int* touch_list;   // leaves marked in the current dab
   // GRIDS topology
   int num_faces, num_base_verts, num_base_edges;
   const int* grid_face;
@@ -326,6 +337,228 @@ __device__ __forceinline__ float dist_sq(float4 co, const float* c) {
 
 __device__ __forceinline__ void set_err(const DevMesh& m, int code) {
   atomicCAS(&m.work->err, 0, code);
+}
+
+// ---------------------------------------------------------------------------
+// Per-vertex brush math shared by the per-call kernels and the persistent
+// stroke kernel (one definition, so both paths round identically).
+
+__device__ __forceinline__ void cross3(float* r, const float* a, const float* b) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Pass constants derived from the area normal/centre (draw, clay strips).
+struct BrushFrame {
+  float area_no[3];
+  float off[3];  // draw: area_no * radius * strength
+  float xa[3], ya[3];  // clay strips: in-plane axes
+  float pd, inv_r, inv_rz;  // clay strips: plane offset, inverse extents
+};
+
+// Returns false when the clay-strips frame is degenerate (the pass then does
+// nothing, marks nothing).
+__device__ __forceinline__ bool make_frame(const DevBrush& b, const PassParams& pp,
+                                           const float* area_no, const float* area_co,
+                                           BrushFrame& f) {
+  const float radius = b.radius;
+  for (int k = 0; k < 3; k++) f.area_no[k] = area_no[k];
+  const float dd = radius * b.strength;
+  for (int k = 0; k < 3; k++) f.off[k] = area_no[k] * dd;
+  f.pd = f.inv_r = f.inv_rz = 0.0f;
+  if (b.tool == kToolClayStrips) {
+    cross3(f.xa, area_no, pp.delta);
+    if (normalize3(f.xa[0], f.xa[1], f.xa[2]) == 0.0f) return false;
+    cross3(f.ya, area_no, f.xa);
+    if (normalize3(f.ya[0], f.ya[1], f.ya[2]) == 0.0f) return false;
+    const float rsign = b.strength < 0.0f ? -radius : radius;
+    const float displace = rsign * (0.18f + b.plane_offset);
+    float p[3];
+    for (int k = 0; k < 3; k++) p[k] = area_co[k] + area_no[k] * displace;
+    f.pd = -(area_no[0] * p[0] + area_no[1] * p[1] + area_no[2] * p[2]);
+    f.inv_r = 1.0f / radius;
+    f.inv_rz = 1.0f / (radius * 1.25f);
+  }
+  return true;
+}
+
+// Draw / inflate / clay strips on one vertex.  Returns true when the vertex is
+// inside the brush test (then co holds the new position); moved reports a
+// non-zero strength factor.
+__device__ __forceinline__ bool brush_vertex(const DevMesh& m, const DevBrush& b, const float* ys,
+                                             const PassParams& pp, const BrushFrame& f, int v,
+                                             float4& co, bool& moved) {
+  const float radius = b.radius;
+  if (b.tool == kToolDraw) {
+    const float d2 = dist_sq(co, pp.loc);
+    if (!(d2 <= radius * radius)) return false;
+    const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+    co.x = co.x + f.off[0] * sf;
+    co.y = co.y + f.off[1] * sf;
+    co.z = co.z + f.off[2] * sf;
+    moved = sf != 0.0f;
+    return true;
+  }
+  if (b.tool == kToolInflate) {
+    const float d2 = dist_sq(co, pp.loc);
+    if (!(d2 <= radius * radius)) return false;
+    const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+    const float fade = b.strength * sf;
+    const float kk = fade * radius;
+    const float4 no = m.no[v];
+    co.x = co.x + no.x * kk;
+    co.y = co.y + no.y * kk;
+    co.z = co.z + no.z * kk;
+    moved = sf != 0.0f;
+    return true;
+  }
+  // clay strips
+  const float* an = f.area_no;
+  const float r0 = co.x - pp.loc[0], r1 = co.y - pp.loc[1], r2 = co.z - pp.loc[2];
+  const float lx = fabsf((r0 * f.xa[0] + r1 * f.xa[1] + r2 * f.xa[2]) * f.inv_r);
+  const float ly = fabsf((r0 * f.ya[0] + r1 * f.ya[1] + r2 * f.ya[2]) * f.inv_r);
+  const float lz = fabsf((r0 * an[0] + r1 * an[1] + r2 * an[2]) * f.inv_rz);
+  if (!(lx <= 1.0f && ly <= 1.0f && lz <= 1.0f)) return false;
+  const float dloc = (lx > ly) ? lx : ly;
+  const float sf = strength_factor(m, b, ys, pp, v, radius * dloc, radius);
+  const float fade = b.strength * sf;
+  const float side = (co.x * an[0] + co.y * an[1] + co.z * an[2]) + f.pd;
+  const float ns = -side;
+  const float v0 = (co.x + an[0] * ns) - co.x;
+  const float v1 = (co.y + an[1] * ns) - co.y;
+  const float v2 = (co.z + an[2] * ns) - co.z;
+  co.x = co.x + v0 * fade;
+  co.y = co.y + v1 * fade;
+  co.z = co.z + v2 * fade;
+  moved = sf != 0.0f;
+  return true;
+}
+
+// Smooth neighbour average: FACES one-ring (CSR order) or the in-grid
+// 4-neighbourhood (x-1, x+1, y-1, y+1) for GRIDS.
+__device__ __forceinline__ float3 neighbor_average(const DevMesh& m, int v, float4 c0) {
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+  int n = 0;
+  if (m.type == kFaces) {
+    const int e = m.nb_off[v + 1];
+    for (int q = m.nb_off[v]; q < e; q++) {
+      const float4 c = m.co[m.nb_idx[q]];
+      sx += c.x;
+      sy += c.y;
+      sz += c.z;
+      n++;
+    }
+  } else {
+    const int gs = m.grid_size, area = m.grid_area;
+    const int g = v / area, r = v % area, x = r % gs, y = r / gs;
+    const int nx[4] = {x - 1, x + 1, x, x};
+    const int ny[4] = {y, y, y - 1, y + 1};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (nx[k] >= 0 && nx[k] < gs && ny[k] >= 0 && ny[k] < gs) {
+        const float4 c = m.co[g * area + ny[k] * gs + nx[k]];
+        sx += c.x;
+        sy += c.y;
+        sz += c.z;
+        n++;
+      }
+    }
+  }
+  if (n == 0) return make_float3(c0.x, c0.y, c0.z);
+  const float inv = 1.0f / (float)n;
+  return make_float3(sx * inv, sy * inv, sz * inv);
+}
+
+// One Jacobi smooth step on one vertex from the sweep-start state.  Returns
+// true when inside the sphere (out then holds the new position).
+__device__ __forceinline__ bool smooth_vertex(const DevMesh& m, const DevBrush& b, const float* ys,
+                                              const PassParams& pp, int v, float4 co, float4& out,
+                                              bool& moved) {
+  const float radius = b.radius;
+  const float d2 = dist_sq(co, pp.loc);
+  if (!(d2 <= radius * radius)) return false;
+  const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+  const float fade = pp.iter_strength * sf;
+  const float3 avg = neighbor_average(m, v, co);
+  out.x = co.x + (avg.x - co.x) * fade;
+  out.y = co.y + (avg.y - co.y) * fade;
+  out.z = co.z + (avg.z - co.z) * fade;
+  out.w = co.w;
+  moved = sf != 0.0f;
+  return true;
+}
+
+// FACES vertex normal (gather form of pbvh.c:2933-3009): compensated sum of
+// the poly normals of the vertex's looptris lying in UpdateNormals leaves,
+// ascending looptri order, then normalize_v3.  Returns the looptris used.
+__device__ __forceinline__ int vertex_normal(const DevMesh& m, int v, float4& out) {
+  CSum ax = {0.0f, 0.0f}, ay = {0.0f, 0.0f}, az = {0.0f, 0.0f};
+  const int e = m.vt_off[v + 1];
+  int used = 0;
+  for (int q = m.vt_off[v]; q < e; q++) {
+    const int t = m.vt_idx[q];
+    if (!(__ldcg(&m.leaf_flag[m.lt_leaf[t]]) & kUpdateNormals)) continue;
+    const float3 fn = poly_normal(m, m.lt[t].w);
+    cs_add(ax, fn.x);
+    cs_add(ay, fn.y);
+    cs_add(az, fn.z);
+    used++;
+  }
+  float nx = ax.s + ax.e, ny = ay.s + ay.e, nz = az.s + az.e;
+  normalize3(nx, ny, nz);
+  out = make_float4(nx, ny, nz, 0.0f);
+  return used;
+}
+
+__device__ __forceinline__ float fmin_ref(float a, float b) { return (a < b) ? a : b; }
+__device__ __forceinline__ float fmax_ref(float a, float b) { return (a > b) ? a : b; }
+
+// Area normal/centre lanes: compensated (s, e) sums of normal xyz and centre
+// xyz plus the two counts; merged pairwise in the order the spec fixes.
+struct Lane {
+  CSum v[6];
+  int n_no, n_co;
+};
+
+__device__ __forceinline__ void lane_merge(Lane& a, const Lane& b) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) a.v[k] = cs_merge(a.v[k], b.v[k]);
+  a.n_no += b.n_no;
+  a.n_co += b.n_co;
+}
+
+__device__ __forceinline__ Lane lane_shfl_down(const Lane& a, int s) {
+  Lane r;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    r.v[k].s = __shfl_down_sync(0xffffffffu, a.v[k].s, s);
+    r.v[k].e = __shfl_down_sync(0xffffffffu, a.v[k].e, s);
+  }
+  r.n_no = __shfl_down_sync(0xffffffffu, a.n_no, s);
+  r.n_co = __shfl_down_sync(0xffffffffu, a.n_co, s);
+  return r;
+}
+
+__device__ __forceinline__ void part_store(AreaPart* p, const Lane& l) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    __stcg(&p->s[k], l.v[k].s);
+    __stcg(&p->e[k], l.v[k].e);
+  }
+  __stcg(&p->n_no, l.n_no);
+  __stcg(&p->n_co, l.n_co);
+}
+__device__ __forceinline__ Lane part_load(const AreaPart* p) {
+  Lane l;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    l.v[k].s = __ldcg(&p->s[k]);
+    l.v[k].e = __ldcg(&p->e[k]);
+  }
+  l.n_no = __ldcg(&p->n_no);
+  l.n_co = __ldcg(&p->n_co);
+  return l;
 }
 
 }  // namespace sgpu

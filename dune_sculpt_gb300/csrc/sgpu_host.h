@@ -74,6 +74,7 @@ struct HostMesh {
   std::vector<int> leaf_nodes;  // leaf id (left-first DFS rank) -> node
   std::vector<int> node_leaf;   // node -> leaf id or -1
   std::vector<int> level_off, level_nodes;  // internal nodes by depth, deepest first
+  std::vector<int> leaf_lo, leaf_hi;        // per node: leaf-id range of its subtree
   std::vector<int> lt_leaf;                 // looptri -> leaf id
 };
 

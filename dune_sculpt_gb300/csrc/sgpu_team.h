@@ -1,0 +1,51 @@
+// Persistent stroke kernel interface (kernels_team.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sgpu_device.cuh"
+
+namespace sgpu {
+
+// One mesh's whole stroke.
+struct TeamJob {
+  int mesh;      // index into TeamArgs::meshes
+  int ndabs;
+  int symmetry;  // PAINT_SYMM_* bits
+  int use_orig;  // cull against orig_vb
+  float view[3];
+  float pad;
+  const float* dabs;  // ndabs * 6 floats (location, grab delta), device memory
+  const int* tools;   // per-dab tool or nullptr, device memory
+  DevBrush brush;     // brush.tool: the default tool
+};
+
+struct TeamArgs {
+  const DevMesh* meshes;
+  const TeamJob* jobs;
+  int njobs;
+  int* next_job;  // job counter, zero at launch
+  int max_nodes, max_leaves;  // shared-memory sizing over the meshes
+  // profiling (nullable): algorithmic bytes and nanoseconds per phase
+  unsigned long long* prof_bytes;  // kTeamPhases entries
+  unsigned long long* phase_ns;    // kTeamPhases entries
+};
+
+// Phases of a dab in the persistent kernel (profiling).
+enum TeamPhase {
+  kPhCull = 0,
+  kPhArea,
+  kPhBrush,
+  kPhApply,
+  kPhUpdate,
+  kPhFlush,
+  kPhJob,
+  kTeamPhases
+};
+
+size_t team_smem_bytes(int max_nodes, int max_leaves);
+int team_max_cluster();
+int team_max_active_clusters(int cluster, int max_nodes, int max_leaves);
+cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaStream_t s);
+
+}  // namespace sgpu

@@ -25,7 +25,9 @@ LIB_PATH = os.path.join(_HERE, "lib", "libsculptgpu.so")
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_BOUNDS, ERR_UNSUPPORTED = range(7)
 PBVH_Leaf, PBVH_UpdateNormals, PBVH_UpdateBB, PBVH_UpdateOriginalBB = 1, 2, 4, 8
 PBVH_UpdateDrawBuffers, PBVH_UpdateRedraw = 16, 32
-STROKE_EAGER, STROKE_GRAPH = 0, 1
+STROKE_EAGER, STROKE_GRAPH, STROKE_TEAM = 0, 1, 2
+BATCH_SEQUENTIAL, BATCH_TEAM = 0, 1
+TEAM_SIZES = (1, 2, 4, 8, 16)
 
 
 class SculptGPUError(RuntimeError):
@@ -61,6 +63,14 @@ class SGPU_KernelProfile(C.Structure):
                 ("alg_bytes", C.c_double)]
 
 
+TEAM_PHASES = ("search", "area", "brush", "smooth_apply", "normals_refit", "flush", "job")
+
+
+class SGPU_TeamProfile(C.Structure):
+    _fields_ = [("total_ms", C.c_float), ("phase_ms", C.c_double * 7),
+                ("phase_bytes", C.c_double * 7)]
+
+
 # Every exported symbol, as declared in include/sculpt_gpu.h.
 EXPORTS = (
     "sgpu_version", "sgpu_last_error", "sgpu_device_info", "sgpu_mesh_create_faces",
@@ -72,7 +82,8 @@ EXPORTS = (
     "sgpu_set_positions", "sgpu_get_normals", "sgpu_get_mask", "sgpu_get_node_bbs",
     "sgpu_get_nodes", "sgpu_get_prim_indices", "sgpu_get_vert_indices", "sgpu_curve_table",
     "sgpu_stroke_host", "sgpu_mesh_snapshot", "sgpu_mesh_restore", "sgpu_stroke_profile",
-    "sgpu_mesh_flush_l2", "sgpu_host_alloc", "sgpu_host_free",
+    "sgpu_mesh_flush_l2", "sgpu_host_alloc", "sgpu_host_free", "sgpu_mesh_set_team",
+    "sgpu_mesh_get_team", "sgpu_autotune_team", "sgpu_batch_stroke", "sgpu_stroke_team_profile",
 )
 
 _lib = None
@@ -114,8 +125,11 @@ def load(path: str | None = None):
     L.sgpu_get_node_bbs.argtypes = [vp, vp, vp]
     L.sgpu_get_nodes.argtypes = [vp] + [vp] * 7
     L.sgpu_curve_table.argtypes = [i, vp, vp]
-    L.sgpu_stroke_host.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp, vp,
+    L.sgpu_stroke_host.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp, vp, i,
                                    C.POINTER(SGPU_StrokeStats)]
+    L.sgpu_stroke_team_profile.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp,
+                                           C.POINTER(SGPU_TeamProfile),
+                                           C.POINTER(SGPU_StrokeStats)]
     L.sgpu_stroke_profile.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp,
                                       C.POINTER(SGPU_KernelProfile),
                                       C.POINTER(SGPU_StrokeStats)]
@@ -124,8 +138,29 @@ def load(path: str | None = None):
     L.sgpu_host_alloc.restype = vp
     L.sgpu_host_alloc.argtypes = [C.c_size_t]
     L.sgpu_host_free.argtypes = [vp]
+    L.sgpu_mesh_set_team.argtypes = [vp, i]
+    L.sgpu_mesh_get_team.argtypes = [vp, vp]
+    L.sgpu_autotune_team.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp]
+    L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
     _lib = L
     return L
+
+
+def batch_stroke(pbvhs, strokes, mode: int = BATCH_TEAM, cluster: int = 0, dab_tools=None):
+    """Strokes many independent meshes; returns (per-mesh stats list, total_ms)."""
+    L = load()
+    n = len(pbvhs)
+    handles = (C.c_void_p * n)(*[p.handle for p in pbvhs])
+    brushes = (SGPU_Brush * n)(*[make_brush(s) for s in strokes])
+    dabs = np.ascontiguousarray(np.concatenate([s.dabs for s in strokes]), dtype=np.float32)
+    offs = np.zeros(n + 1, dtype=np.int32)
+    offs[1:] = np.cumsum([s.dabs.shape[0] for s in strokes])
+    tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+    stats = (SGPU_StrokeStats * n)()
+    total = C.c_float()
+    _check(L.sgpu_batch_stroke(handles, n, brushes, _p(dabs), _p(offs), _p(tools), mode,
+                               cluster, stats, C.byref(total)))
+    return list(stats), total.value
 
 
 class PinnedArray:
@@ -318,16 +353,30 @@ class PBVH:
         return stats
 
     def stroke_host(self, st, verts_in, verts_out, normals_in=None, dabs=None,
-                    dab_tools=None) -> SGPU_StrokeStats:
+                    dab_tools=None, mode: int = STROKE_TEAM) -> SGPU_StrokeStats:
         """Host-buffer stroke: upload, refit, stroke, download (one C-ABI call)."""
         b = make_brush(st)
         d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
         tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
         stats = SGPU_StrokeStats()
         _check(load().sgpu_stroke_host(self._h, C.byref(b), _p(d), d.shape[0], _p(tools),
-                                       _p(verts_in), _p(normals_in), _p(verts_out),
+                                       _p(verts_in), _p(normals_in), _p(verts_out), mode,
                                        C.byref(stats)))
         return stats
+
+    def stroke_team_profile(self, st, dabs=None, dab_tools=None):
+        """Persistent stroke with phase timers and algorithmic-byte counters.
+        Returns ({phase: {ms, bytes}}, total_ms, stats)."""
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        prof = SGPU_TeamProfile()
+        stats = SGPU_StrokeStats()
+        _check(load().sgpu_stroke_team_profile(self._h, C.byref(b), _p(d), d.shape[0],
+                                               _p(tools), C.byref(prof), C.byref(stats)))
+        out = {name: {"ms": prof.phase_ms[k], "bytes": prof.phase_bytes[k]}
+               for k, name in enumerate(TEAM_PHASES)}
+        return out, prof.total_ms, stats
 
     def stroke_profile(self, st, dabs=None, dab_tools=None):
         """Eager stroke with per-launch CUDA events and algorithmic-byte counters.
@@ -345,6 +394,26 @@ class PBVH:
                 out[p.name.decode()] = {"launches": p.launches, "total_ms": p.total_ms,
                                         "alg_bytes": p.alg_bytes}
         return out, stats
+
+    def set_team(self, cluster: int):
+        _check(load().sgpu_mesh_set_team(self._h, cluster))
+
+    def team(self) -> int:
+        c = C.c_int()
+        _check(load().sgpu_mesh_get_team(self._h, C.byref(c)))
+        return c.value
+
+    def autotune_team(self, st, dabs=None, dab_tools=None):
+        """Times the persistent stroke for each cluster size; keeps the fastest.
+        Returns (best cluster size, {size: ms})."""
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        best = C.c_int()
+        ms = np.zeros(5, dtype=np.float32)
+        _check(load().sgpu_autotune_team(self._h, C.byref(b), _p(d), d.shape[0], _p(tools),
+                                         C.byref(best), _p(ms)))
+        return best.value, {s: float(t) for s, t in zip(TEAM_SIZES, ms)}
 
     def snapshot(self):
         _check(load().sgpu_mesh_snapshot(self._h))

@@ -206,16 +206,57 @@ int sgpu_pbvh_node_mark_update(sgpu_mesh *mesh, int node);
  * captured once as a CUDA graph and replayed.  stats may be NULL. */
 #define SGPU_STROKE_EAGER 0
 #define SGPU_STROKE_GRAPH 1
+#define SGPU_STROKE_TEAM 2 /* one persistent launch of the whole stroke (cluster team) */
 int sgpu_stroke(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, int ndabs,
                 const int *dab_tools, int mode, SGPU_StrokeStats *stats);
 
+/* Cluster size (CTAs of 256 threads working on one mesh) of the persistent
+ * stroke kernel for this mesh: 1, 2, 4, 8 or 16.  Default 8. */
+int sgpu_mesh_set_team(sgpu_mesh *mesh, int cluster_size);
+int sgpu_mesh_get_team(const sgpu_mesh *mesh, int *cluster_size);
+/* Autotuner: times the stroke in SGPU_STROKE_TEAM mode for every cluster size,
+ * restoring the mesh state between trials, and keeps the fastest for the mesh.
+ * r_ms (nullable) receives 5 timings (sizes 1, 2, 4, 8, 16; -1 if unsupported). */
+int sgpu_autotune_team(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
+                       int ndabs, const int *dab_tools, int *r_cluster, float *r_ms);
+
+/* Profile of one SGPU_STROKE_TEAM stroke: the persistent kernel's time split
+ * by phase (time of the team's first thread from phase start to the barrier
+ * that ends it) and the algorithmic bytes each phase moved.  Phases: 0 node
+ * search, 1 area normal/centre, 2 brush sweep, 3 smooth apply, 4 normals and
+ * leaf refit, 5 ancestor flush, 6 job set-up and end-of-stroke bounds. */
+#define SGPU_TEAM_PHASES 7
+typedef struct SGPU_TeamProfile {
+  float total_ms; /* CUDA-event time of the launch */
+  double phase_ms[SGPU_TEAM_PHASES];
+  double phase_bytes[SGPU_TEAM_PHASES];
+} SGPU_TeamProfile;
+int sgpu_stroke_team_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
+                             int ndabs, const int *dab_tools, SGPU_TeamProfile *out,
+                             SGPU_StrokeStats *stats);
+
+/* ---- batches of independent meshes ----
+ * Mesh i strokes with brushes[i] over dabs[dab_offsets[i] .. dab_offsets[i+1]);
+ * dab_tools (nullable) is indexed like dabs.
+ *   SGPU_BATCH_SEQUENTIAL: one graph-mode stroke per mesh, one after another.
+ *   SGPU_BATCH_TEAM: one persistent launch; cluster teams take meshes from a
+ *     work queue, longest estimated stroke first.
+ * cluster_size 0 uses the first mesh's setting.  stats (nullable) gets one
+ * entry per mesh; r_total_ms the CUDA-event time of the whole batch. */
+#define SGPU_BATCH_SEQUENTIAL 0
+#define SGPU_BATCH_TEAM 1
+int sgpu_batch_stroke(sgpu_mesh **meshes, int nmesh, const SGPU_Brush *brushes,
+                      const SGPU_Dab *dabs, const int *dab_offsets, const int *dab_tools,
+                      int mode, int cluster_size, SGPU_StrokeStats *stats, float *r_total_ms);
+
 /* The stroke with host buffers, as a host application calls it: verts_in (and
  * vert_normals_in, nullable) are copied to the device, every leaf box is
- * refit, the stroke runs, and the positions are copied back to verts_out.
- * stats->gpu_ms covers the copies and the kernels.  FACES meshes. */
+ * refit, the stroke runs (mode as in sgpu_stroke), and the positions are
+ * copied back to verts_out.  stats->gpu_ms covers the copies and the kernels.
+ * FACES meshes. */
 int sgpu_stroke_host(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, int ndabs,
                      const int *dab_tools, const SGPU_MVert *verts_in,
-                     const float *vert_normals_in, SGPU_MVert *verts_out,
+                     const float *vert_normals_in, SGPU_MVert *verts_out, int mode,
                      SGPU_StrokeStats *stats);
 
 /* ---- per-stroke restore (undo) ----

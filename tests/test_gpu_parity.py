@@ -199,3 +199,90 @@ def test_use_original_bb(gpu, oracle):
     tot, _ = o.stroke(st, which=1)
     assert stats.verts_displaced == tot
     _assert_state_equal(g, o, "orig bb")
+
+
+# ---------------------------------------------------------------------------
+# Persistent stroke kernel (one launch per stroke or per batch)
+
+from dune_sculpt_gb300.sculpt import (BATCH_SEQUENTIAL, BATCH_TEAM, STROKE_TEAM,  # noqa: E402
+                                      batch_stroke)
+
+
+@pytest.mark.parametrize("tool", TOOLS)
+@pytest.mark.parametrize("cluster", [1, 4, 16])
+def test_team_stroke_parity(gpu, oracle, case, tool, cluster):
+    name, m, ll = case
+    g, o = _pair(gpu, oracle, m, ll)
+    g.set_team(cluster)
+    dabs = synth.line_dabs(5, 24) if name == "grid" else synth.arc_dabs(5, 24, 0.03)
+    st = synth.Stroke(tool, 0.1, 0.7, synth.CURVE_SMOOTH if tool != synth.TOOL_CLAY_STRIPS
+                      else synth.CURVE_SHARP, synth.SYMM_X, dabs)
+    stats = g.stroke(st, mode=STROKE_TEAM)
+    tot, _ = o.stroke(st, which=1)
+    assert stats.verts_displaced == tot
+    _assert_state_equal(g, o, f"{name} team{cluster} tool {tool}")
+    assert np.array_equal(g.nodes()["flag"] & 15, o.nodes()["flag"] & 15)
+
+
+def test_team_after_pending_per_call_brush(gpu, oracle):
+    """A per-call brush left without its update joins the next stroke's first
+    dab update in both paths."""
+    m = small_icosphere(4)
+    ga, o = _pair(gpu, oracle, m, 200)
+    gb = PBVH.build_mesh(m, 200)
+    st1 = synth.Stroke(synth.TOOL_INFLATE, 0.2, 0.5, synth.CURVE_SMOOTH, 0, None)
+    c = o.co()[33]
+    rsq = float(np.float32(np.float32(0.2) * np.float32(0.2)))
+    for g in (ga, gb):
+        g.search_sphere_device(c, rsq)
+        g.do_inflate_brush(st1, c, [0, 0, 1])
+    st2 = synth.Stroke(synth.TOOL_SMOOTH, 0.12, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X,
+                       synth.arc_dabs(8, 10, 0.03))
+    ga.stroke(st2, mode=STROKE_GRAPH)
+    gb.set_team(4)
+    gb.stroke(st2, mode=STROKE_TEAM)
+    _assert_state_equal_gpu(ga, gb)
+
+
+def _assert_state_equal_gpu(a, b):
+    assert bits_equal(a.positions(), b.positions()), first_diff(a.positions(), b.positions())
+    assert bits_equal(a.normals(), b.normals()), first_diff(a.normals(), b.normals())
+    for x, y in zip(a.bbs(), b.bbs()):
+        assert bits_equal(x, y), first_diff(x, y)
+
+
+@pytest.mark.parametrize("mode", [BATCH_SEQUENTIAL, BATCH_TEAM])
+def test_batch_matches_oracle(gpu, oracle, mode):
+    batch = synth.cfg4_batch(nmesh=6, vmin=2000, vmax=20000, ndabs=10)
+    gs, os_, strokes = [], [], []
+    for k, (m, st, ll) in enumerate(batch):
+        ll = 300
+        gs.append(PBVH.build_mesh(m, ll))
+        o = oracle.OracleMesh.faces(m, ll)
+        o.recalc_all_normals()
+        os_.append(o)
+        if k % 3 == 1:
+            st.symmetry = synth.SYMM_X
+        strokes.append(st)
+    stats, total_ms = batch_stroke(gs, strokes, mode=mode, cluster=4)
+    assert total_ms > 0
+    for g, o, st, s in zip(gs, os_, strokes, stats):
+        tot, _ = o.stroke(st, which=1)
+        assert s.verts_displaced == tot
+        _assert_state_equal(g, o, "batch")
+
+
+def test_autotune_restores_state(gpu, oracle):
+    m = small_uvsphere(48)
+    g, o = _pair(gpu, oracle, m, 200)
+    st = synth.Stroke(synth.TOOL_DRAW, 0.1, 0.5, synth.CURVE_SMOOTH, synth.SYMM_X,
+                      synth.arc_dabs(21, 12, 0.03))
+    best, times = g.autotune_team(st)
+    assert best in (1, 2, 4, 8, 16)
+    assert times[best] > 0
+    assert g.team() == best
+    _assert_state_equal(g, o, "after autotune")
+    stats = g.stroke(st, mode=STROKE_TEAM)
+    tot, _ = o.stroke(st, which=1)
+    assert stats.verts_displaced == tot
+    _assert_state_equal(g, o, "autotuned stroke")
