@@ -10,6 +10,12 @@ from helpers import bits_equal, first_diff, rel_err
 
 pytestmark = pytest.mark.gpu
 
+# FP32 vs FP64 positions, norm-wise relative.  The GPU equals the FP32
+# restatement bit for bit; the FP32 arithmetic itself (seam averages, grid
+# normals feeding draw/inflate) drifts up to ~1.1e-6 from FP64 over these
+# strokes, so the bound here is 2e-6 (FACES strokes stay under 1e-6).
+FP64_TOL_GRIDS = 2e-6
+
 TOOLS = [synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS]
 
 
@@ -79,7 +85,7 @@ def test_grids_stroke_parity(gpu, oracle, tool, mode):
     tot, _ = o.stroke(st, which=3)
     assert s.verts_displaced == tot and tot > 0
     _assert_equal(gp, o, f"tool {tool}")
-    assert rel_err(gp.positions(), o.co64()) < 1e-6
+    assert rel_err(gp.positions(), o.co64()) < FP64_TOL_GRIDS
     _seam_consistent(g, gp.positions())
 
 
@@ -96,4 +102,4 @@ def test_grids_mixed_stroke(gpu, oracle):
     tot, _ = o.stroke(st, which=3, dab_tools=tools)
     assert s.verts_displaced == tot
     _assert_equal(gp, o, "mixed")
-    assert rel_err(gp.positions(), o.co64()) < 1e-6
+    assert rel_err(gp.positions(), o.co64()) < FP64_TOL_GRIDS
