@@ -49,6 +49,10 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 }  // namespace
 
+namespace sgpu {
+void set_error_message(const std::string& msg) { g_err = msg; }
+}  // namespace sgpu
+
 struct sgpu_mesh {
   HostMesh host;
   DevMesh dev{};

@@ -284,6 +284,31 @@ int sgpu_mesh_flush_l2(sgpu_mesh *mesh);
 void *sgpu_host_alloc(size_t bytes);
 int sgpu_host_free(void *ptr);
 
+/* ---- allocation-free smooth dab ----
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory — an application embedding this library under a device-memory budget
+ * it fixed up front, a plug-in host that forbids allocation, code recorded
+ * into a CUDA graph someone else owns — and so cannot create a mesh handle
+ * (creating one allocates).  They pass device arrays they already own: co (4
+ * floats per vertex, the MVert layout, moved in place), normals (4 floats per
+ * vertex, read only for SGPU_BRUSH_FRONTFACE; may be NULL otherwise), mask and
+ * automask (may be NULL), the one-ring as CSR nb_off/nb_idx, and the candidate
+ * vertices verts[nverts] (each vertex once, e.g. the unique vertices of the
+ * leaves sgpu_search_sphere found).  One smooth-brush pass at location, with
+ * the same sweeps and arithmetic as sgpu_do_smooth_brush; vertices are not
+ * tagged and nodes not marked (there is no mesh handle).
+ * The Jacobi scratch is a fixed device array of SGPU_NOALLOC_MAX_VERTS float4
+ * (1 MiB) that every GPU loading the library holds until exit; nverts above
+ * that returns SGPU_ERR_INVALID_ARG.  The first call on a device looks up the
+ * array's device address, so make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race.  No cudaMalloc, no
+ * cudaFree.  Synchronous on stream (a cudaStream_t; NULL = default stream). */
+#define SGPU_NOALLOC_MAX_VERTS 65536
+int sgpu_smooth_dab_noalloc(float *co, const float *normals, const float *mask,
+                            const float *automask, const int *nb_off, const int *nb_idx,
+                            const int *verts, int nverts, const SGPU_Brush *brush,
+                            const float location[3], void *stream);
+
 /* ---- data access (synchronous) ---- */
 int sgpu_get_verts(sgpu_mesh *mesh, SGPU_MVert *out);          /* FACES */
 int sgpu_set_verts(sgpu_mesh *mesh, const SGPU_MVert *verts);  /* FACES */
