@@ -91,7 +91,7 @@ struct sgpu_mesh {
   float* t_dabs = nullptr;
   int* t_tools = nullptr;
   int* t_counter = nullptr;
-  size_t t_dab_cap = 0, t_tool_cap = 0;
+  size_t t_dab_cap = 0, t_tool_cap = 0, t_mesh_cap = 0, t_job_cap = 0, t_counter_cap = 0;
 
   cudaEvent_t prof_event() {
     if (ev_used == ev_pool.size()) {
@@ -140,6 +140,15 @@ struct sgpu_mesh {
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
+    for (void* p : {static_cast<void*>(t_meshes), static_cast<void*>(t_jobs),
+                    static_cast<void*>(t_dabs), static_cast<void*>(t_tools),
+                    static_cast<void*>(t_counter)})
+      if (p) cudaFree(p);
+    t_meshes = nullptr;
+    t_jobs = nullptr;
+    t_dabs = nullptr;
+    t_tools = nullptr;
+    t_counter = nullptr;
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev_h0) cudaEventDestroy(ev_h0);
@@ -891,7 +900,8 @@ int sgpu_autotune_team(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab*
   float best_ms = -1.0f;
   for (int k = 0; k < 5; k++) {
     float ms = -1.0f;
-    if (team_max_active_clusters(sizes[k], mesh->dev.totnode, mesh->dev.nleaf) > 0) {
+    const int g1 = mesh->dev.type == kGrids ? mesh->dev.grid_size - 1 : 0;
+    if (team_max_active_clusters(sizes[k], mesh->dev.totnode, mesh->dev.nleaf, 3 * g1 * g1) > 0) {
       const int offs[2] = {0, ndabs};
       sgpu_mesh* one[1] = {mesh};
       // two trials, keep the second (the first pays one-time setup)
@@ -1420,22 +1430,20 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
                const int* offs, const int* tools, int cluster, cudaStream_t s,
                SGPU_StrokeStats* stats, float* total_ms) {
   sgpu_mesh* m0 = meshes[0];
-  int max_nodes = 0, max_leaves = 0;
+  int max_nodes = 0, max_leaves = 0, max_fn = 0;
   for (int i = 0; i < n; i++) {
-    if (meshes[i]->dev.type != kFaces)
-      return fail(SGPU_ERR_UNSUPPORTED, "the persistent stroke kernel takes FACES meshes");
     max_nodes = std::max(max_nodes, meshes[i]->dev.totnode);
     max_leaves = std::max(max_leaves, meshes[i]->dev.nleaf);
+    if (meshes[i]->dev.type == kGrids) {
+      const int g1 = meshes[i]->dev.grid_size - 1;
+      max_fn = std::max(max_fn, 3 * g1 * g1);
+    }
   }
-  if (max_leaves > 64 * 256 || team_smem_bytes(max_nodes, max_leaves) > 160 * 1024)
+  if (max_leaves > 64 * 256 || team_smem_bytes(max_nodes, max_leaves, max_fn) > 160 * 1024)
     return fail(SGPU_ERR_UNSUPPORTED, "PBVH too large for the persistent stroke kernel");
-  const int nteams_max = team_max_active_clusters(cluster, max_nodes, max_leaves);
+  const int nteams_max = team_max_active_clusters(cluster, max_nodes, max_leaves, max_fn);
   if (nteams_max <= 0)
     return fail(SGPU_ERR_UNSUPPORTED, "cluster size %d cannot be launched", cluster);
-  static size_t mesh_cap = 0, job_cap = 0;  // capacities of m0's staging (per process)
-  (void)mesh_cap;
-  (void)job_cap;
-  size_t cap_m = m0->t_meshes ? static_cast<size_t>(n) : 0, cap_j = cap_m;
   int rc;
   // staging buffers live on the first mesh; re-create when too small
   static thread_local std::vector<DevMesh> h_meshes;
@@ -1443,28 +1451,11 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   h_meshes.assign(n, DevMesh{});
   h_jobs.assign(n, TeamJob{});
   const size_t ndab = static_cast<size_t>(offs[n]);
-  {
-    size_t c = m0->t_meshes ? m0->t_dab_cap : 0;
-    (void)c;
-  }
   if ((rc = ensure_dev(&m0->t_dabs, &m0->t_dab_cap, ndab * 6))) return rc;
   if (tools && (rc = ensure_dev(&m0->t_tools, &m0->t_tool_cap, ndab))) return rc;
-  {
-    // mesh/job tables: sized to n each call (small)
-    if (m0->t_meshes) cudaFree(m0->t_meshes);
-    if (m0->t_jobs) cudaFree(m0->t_jobs);
-    m0->t_meshes = nullptr;
-    m0->t_jobs = nullptr;
-    size_t c1 = 0, c2 = 0;
-    if ((rc = ensure_dev(&m0->t_meshes, &c1, static_cast<size_t>(n)))) return rc;
-    if ((rc = ensure_dev(&m0->t_jobs, &c2, static_cast<size_t>(n)))) return rc;
-    if (!m0->t_counter) {
-      size_t c3 = 0;
-      if ((rc = ensure_dev(&m0->t_counter, &c3, 1))) return rc;
-    }
-  }
-  (void)cap_m;
-  (void)cap_j;
+  if ((rc = ensure_dev(&m0->t_meshes, &m0->t_mesh_cap, static_cast<size_t>(n)))) return rc;
+  if ((rc = ensure_dev(&m0->t_jobs, &m0->t_job_cap, static_cast<size_t>(n)))) return rc;
+  if ((rc = ensure_dev(&m0->t_counter, &m0->t_counter_cap, 1))) return rc;
   std::vector<int> order(n);
   std::vector<double> est(n);
   for (int i = 0; i < n; i++) {
@@ -1513,6 +1504,7 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.next_job = m0->t_counter;
   a.max_nodes = max_nodes;
   a.max_leaves = max_leaves;
+  a.max_grid_fn = max_fn;
   a.prof_bytes = g_team_prof_bytes;
   a.phase_ns = g_team_phase_ns;
   const int nteams = std::min(n, nteams_max);

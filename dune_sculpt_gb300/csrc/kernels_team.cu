@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "sgpu_device.cuh"
+#include "sgpu_grids.cuh"
 #include "sgpu_kernels.h"
 #include "sgpu_team.h"
 
@@ -26,6 +27,12 @@ namespace cg = cooperative_groups;
 namespace sgpu {
 
 constexpr int kTeamThreads = 256;
+
+__host__ __device__ inline size_t team_fn_offset(int max_nodes, int max_leaves) {
+  const size_t b = sizeof(int) * (static_cast<size_t>(max_nodes) + 2 * static_cast<size_t>(max_leaves) + 3) +
+                   static_cast<size_t>(max_nodes);
+  return (b + 15) & ~static_cast<size_t>(15);
+}
 
 struct TeamShared {
   DevMesh m;
@@ -352,6 +359,7 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
   int* s_cl = s_par + a.max_nodes;
   int* s_coff = s_cl + a.max_leaves + 1;
   unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_coff + a.max_leaves + 2);
+  float* s_fn = reinterpret_cast<float*>(dyn + team_fn_offset(a.max_nodes, a.max_leaves));
   PhaseClock clk;
   clk.last = a.phase_ns ? global_ns() : 0ull;
 
@@ -379,10 +387,14 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
     DevBrush& b = sh.job.brush;
     Work* w = m.work;
     for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_par[i] = m.node_parent[i];
+    // GRIDS work-list stamps: dab d uses epoch grid_epoch0 + d + 1
+    const unsigned int grid_epoch0 = __ldcg(&w->grid_epoch);
+    team_sync(cluster, C);
     if (rank == 0 && threadIdx.x == 0) {
       for (int k = 0; k < 3; k++) w->hit_count[k] = 0;
       w->tag_count[0] = w->tag_count[1] = 0;
       w->touch_count[0] = w->touch_count[1] = 0;
+      if (m.type == kGrids) m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = 0;
     }
     team_sync(cluster, C);
     // Leaves flagged and vertices tagged before the stroke (by per-call entry
@@ -568,6 +580,33 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
           m.vtag[v] = 0u;
           ab += 24ull + 16ull * used;
         }
+      } else {
+        // GRIDS: faces of the touched leaves, their inner normals and seams,
+        // then the base edges and corners (positions move at the seams, so
+        // the refit below follows).
+        const unsigned int epoch = grid_epoch0 + static_cast<unsigned int>(d) + 1u;
+        for (int k = rank; k < ntouch; k += C) {
+          const int leaf = __ldcg(&m.touch_list[k]);
+          const int p0 = m.leaf_prim_off[leaf], p1 = m.leaf_prim_off[leaf + 1];
+          for (int j = p0 + threadIdx.x; j < p1; j += kTeamThreads) grid_claim_face(m, m.leaf_prims[j], epoch);
+        }
+        team_sync(cluster, C);
+        const int nf = __ldcg(&m.grid_counts[0]);
+        const int g1 = m.grid_size - 1;
+        for (int k = rank; k < nf; k += C) {
+          const int f = __ldcg(&m.face_list[k]);
+          grid_face_update(m, f, s_fn);
+          if (threadIdx.x == 0) {
+            const int n = m.face_ngrids[f];
+            ab += 24ull * m.grid_area * n + 112ull * g1 * n + 56ull * n;
+          }
+        }
+        team_sync(cluster, C);
+        const int ne = __ldcg(&m.grid_counts[1]), nv = __ldcg(&m.grid_counts[2]);
+        const long long items = (long long)ne * (2 * m.grid_size - 2) + nv;
+        for (long long it = gt; it < items; it += GT) grid_seam_item(m, it, ne);
+        team_sync(cluster, C);
+        if (rank == 0 && threadIdx.x == 0) m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = 0;
       }
       for (int k = rank; k < ntouch; k += C) {
         const int leaf = __ldcg(&m.touch_list[k]);
@@ -660,14 +699,17 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
       }
     team_sync(cluster, C);
     for (int leaf = gt; leaf < m.nleaf; leaf += GT) atomicAnd(&m.leaf_flag[leaf], ~kUpdateOriginalBB);
+    if (rank == 0 && threadIdx.x == 0 && m.type == kGrids)
+      w->grid_epoch = grid_epoch0 + static_cast<unsigned int>(sh.job.ndabs);
     team_sync(cluster, C);
     clk.mark(a, rank, kPhJob);
   }
 }
 
-size_t team_smem_bytes(int max_nodes, int max_leaves) {
-  return sizeof(int) * (static_cast<size_t>(max_nodes) + 2 * static_cast<size_t>(max_leaves) + 3) +
-         static_cast<size_t>(max_nodes) + 16;
+// Dynamic shared memory: parents, culled list and offsets, node marks, then
+// the grid face-normal scratch (16-byte aligned, team_fn_offset).
+size_t team_smem_bytes(int max_nodes, int max_leaves, int max_grid_fn) {
+  return team_fn_offset(max_nodes, max_leaves) + sizeof(float) * static_cast<size_t>(max_grid_fn) + 16;
 }
 
 int team_max_cluster() { return 16; }
@@ -680,7 +722,7 @@ cudaError_t configure_team_kernel(size_t smem) {
 }
 
 cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaStream_t s) {
-  const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves);
+  const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves, a.max_grid_fn);
   cudaError_t e = configure_team_kernel(smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
@@ -698,8 +740,8 @@ cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaS
   return cudaLaunchKernelEx(&cfg, k_team_stroke, a);
 }
 
-int team_max_active_clusters(int cluster, int max_nodes, int max_leaves) {
-  const size_t smem = team_smem_bytes(max_nodes, max_leaves);
+int team_max_active_clusters(int cluster, int max_nodes, int max_leaves, int max_grid_fn) {
+  const size_t smem = team_smem_bytes(max_nodes, max_leaves, max_grid_fn);
   if (configure_team_kernel(smem) != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(static_cast<unsigned>(cluster));

@@ -397,7 +397,7 @@ __device__ __forceinline__ bool brush_vertex(const DevMesh& m, const DevBrush& b
     co.x = co.x + f.off[0] * sf;
     co.y = co.y + f.off[1] * sf;
     co.z = co.z + f.off[2] * sf;
-    moved = sf != 0.0f;
+    moved = (b.strength * sf) != 0.0f;
     return true;
   }
   if (b.tool == kToolInflate) {
@@ -410,7 +410,7 @@ __device__ __forceinline__ bool brush_vertex(const DevMesh& m, const DevBrush& b
     co.x = co.x + no.x * kk;
     co.y = co.y + no.y * kk;
     co.z = co.z + no.z * kk;
-    moved = sf != 0.0f;
+    moved = fade != 0.0f;
     return true;
   }
   // clay strips
@@ -431,7 +431,7 @@ __device__ __forceinline__ bool brush_vertex(const DevMesh& m, const DevBrush& b
   co.x = co.x + v0 * fade;
   co.y = co.y + v1 * fade;
   co.z = co.z + v2 * fade;
-  moved = sf != 0.0f;
+  moved = fade != 0.0f;
   return true;
 }
 
@@ -485,7 +485,7 @@ __device__ __forceinline__ bool smooth_vertex(const DevMesh& m, const DevBrush& 
   out.y = co.y + (avg.y - co.y) * fade;
   out.z = co.z + (avg.z - co.z) * fade;
   out.w = co.w;
-  moved = sf != 0.0f;
+  moved = fade != 0.0f;
   return true;
 }
 

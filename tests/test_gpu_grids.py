@@ -103,3 +103,28 @@ def test_grids_mixed_stroke(gpu, oracle):
     assert s.verts_displaced == tot
     _assert_equal(gp, o, "mixed")
     assert rel_err(gp.positions(), o.co64()) < FP64_TOL_GRIDS
+
+
+@pytest.mark.parametrize("cluster", [1, 8])
+def test_grids_team_stroke(gpu, oracle, cluster):
+    """The persistent stroke kernel on multires grids, mixed tools, X mirror."""
+    from dune_sculpt_gb300.sculpt import STROKE_TEAM
+
+    g = small_torus(5)
+    gp, o = _pair(oracle, g, leaf_limit=8)
+    gp.set_team(cluster)
+    dabs = synth.torus_dabs(43, 24, 0.12)
+    tools = np.array([(synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE,
+                       synth.TOOL_CLAY_STRIPS)[d % 4] for d in range(dabs.shape[0])],
+                     dtype=np.int32)
+    st = synth.Stroke(synth.TOOL_DRAW, 0.12, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
+    s = gp.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
+    tot, _ = o.stroke(st, which=1, dab_tools=tools)
+    assert s.verts_displaced == tot and tot > 0
+    _assert_equal(gp, o, f"team{cluster}")
+    _seam_consistent(g, gp.positions())
+    # a second stroke continues from the first (epochs, flags, counters)
+    s = gp.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
+    tot, _ = o.stroke(st, which=1, dab_tools=tools)
+    assert s.verts_displaced == tot
+    _assert_equal(gp, o, f"team{cluster} second")
