@@ -86,6 +86,7 @@ struct sgpu_mesh {
   void* flush_buf = nullptr;
   // persistent stroke kernel: cluster size and device staging of the job
   int team_cluster = 8;
+  int nchunks = 0;  // refit chunks over all leaves
   DevMesh* t_meshes = nullptr;
   TeamJob* t_jobs = nullptr;
   float* t_dabs = nullptr;
@@ -221,6 +222,22 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->upload(&d.level_nodes, h.level_nodes))) return rc;
   if ((rc = m->upload(&d.node_leaf_lo, h.leaf_lo))) return rc;
   if ((rc = m->upload(&d.node_leaf_hi, h.leaf_hi))) return rc;
+  if ((rc = m->upload(&d.node_depth, h.depth))) return rc;
+  d.max_depth = h.max_depth;
+  if (h.max_depth >= 256)
+    return fail(SGPU_ERR_UNSUPPORTED, "PBVH depth %d above 255", h.max_depth);
+  {
+    std::vector<int> choff(L + 1, 0);
+    for (int k = 0; k < L; k++) {
+      const int node = h.leaf_nodes[k];
+      const int nall = h.type == kFaces ? h.uniq[node] + h.face_verts_n[node]
+                                        : h.totprim[node] * h.grid_area;
+      choff[k + 1] = choff[k] + (nall + kChunk - 1) / kChunk;
+    }
+    if ((rc = m->upload(&d.leaf_chunk_off, choff))) return rc;
+    if ((rc = m->alloc(&d.chunk_box, 2 * static_cast<size_t>(choff[L]) + 2))) return rc;
+    m->nchunks = choff[L];
+  }
   if ((rc = m->alloc(&d.hit_list[0], static_cast<size_t>(h.totvert)))) return rc;
   if ((rc = m->alloc(&d.hit_list[1], static_cast<size_t>(h.totvert)))) return rc;
   if ((rc = m->alloc(&d.tag_list, static_cast<size_t>(h.totvert)))) return rc;
@@ -235,6 +252,7 @@ int upload_pbvh(sgpu_mesh* m) {
   if (N > cull_smem_limit())
     return fail(SGPU_ERR_UNSUPPORTED, "PBVH has %d nodes; the node search holds at most %d", N,
                 cull_smem_limit());
+  CK(launch_chunk_boxes_all(d, m->nchunks, m->stream), "chunk box kernel");
   return SGPU_OK;
 }
 
@@ -1151,6 +1169,7 @@ int sgpu_mesh_restore(sgpu_mesh* mesh) {
   CK(cudaMemcpyAsync(d.leaf_flag, mesh->snap_flag, sizeof(int) * d.nleaf, cudaMemcpyDeviceToDevice,
                      s),
      "restore");
+  CK(launch_chunk_boxes_all(d, mesh->nchunks, s), "chunk box kernel");
   CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   return SGPU_OK;
 }
@@ -1279,6 +1298,7 @@ int sgpu_set_verts(sgpu_mesh* mesh, const SGPU_MVert* verts) {
   CK(cudaMemcpyAsync(mesh->dev.co, verts, sizeof(float4) * mesh->dev.totvert,
                      cudaMemcpyHostToDevice, mesh->stream),
      "upload verts");
+  CK(launch_chunk_boxes_all(mesh->dev, mesh->nchunks, mesh->stream), "chunk box kernel");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
 }
@@ -1299,6 +1319,7 @@ int sgpu_set_positions(sgpu_mesh* mesh, const float* xyz) {
   CK(cudaMemcpy2DAsync(mesh->dev.co, sizeof(float4), xyz, 3 * sizeof(float), 3 * sizeof(float),
                        mesh->dev.totvert, cudaMemcpyHostToDevice, mesh->stream),
      "upload positions");
+  CK(launch_chunk_boxes_all(mesh->dev, mesh->nchunks, mesh->stream), "chunk box kernel");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
 }

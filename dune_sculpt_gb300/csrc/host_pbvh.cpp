@@ -267,6 +267,8 @@ void derive_tables(HostMesh& m) {
       if (!(m.flag[i] & kLeaf) && depth[i] == d) m.level_nodes.push_back(i);
     m.level_off.push_back(static_cast<int>(m.level_nodes.size()));
   }
+  m.depth = depth;
+  m.max_depth = maxd;
   // Leaves of a subtree are consecutive in left-first DFS order.
   m.leaf_lo.assign(n, 0);
   m.leaf_hi.assign(n, 0);

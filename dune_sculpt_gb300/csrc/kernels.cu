@@ -408,53 +408,45 @@ __device__ void leaf_refit(const DevMesh& m, int leaf, float* red /* 6*kThreads/
                            unsigned long long& ab) {
   float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
   float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  (void)red;
   const int nv = leaf_nverts_all(m, leaf);
   // co of every leaf vertex (+ its index for FACES); the node box written once
   if (threadIdx.x < nv)
     ab += (m.type == kFaces ? 16ull : 12ull) * ((nv - threadIdx.x + blockDim.x - 1) / blockDim.x);
   if (threadIdx.x == 0) ab += 24u;
-  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-    int v;
-    if (m.type == kFaces) {
-      v = m.leaf_verts[m.leaf_vert_off[leaf] + i];
-    } else {
-      v = leaf_vert(m, leaf, i);
-    }
-    const float4 c = m.co[v];
-    mn[0] = fmin_ref(mn[0], c.x);
-    mn[1] = fmin_ref(mn[1], c.y);
-    mn[2] = fmin_ref(mn[2], c.z);
-    mx[0] = fmax_ref(mx[0], c.x);
-    mx[1] = fmax_ref(mx[1], c.y);
-    mx[2] = fmax_ref(mx[2], c.z);
-  }
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      mn[k] = fmin_ref(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-      mx[k] = fmax_ref(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
-    }
-  }
-  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    for (int k = 0; k < 3; k++) {
-      red[warp * 6 + k] = mn[k];
-      red[warp * 6 + 3 + k] = mx[k];
-    }
-  }
+  // chunk boxes (one warp per chunk of kChunk entries), then their union
+  const int nch = m.leaf_chunk_off[leaf + 1] - m.leaf_chunk_off[leaf];
+  for (int c = threadIdx.x >> 5; c < nch; c += blockDim.x >> 5) chunk_refit_warp(m, leaf, c, mn, mx);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < nw; w++)
-      for (int k = 0; k < 3; k++) {
-        mn[k] = fmin_ref(mn[k], red[w * 6 + k]);
-        mx[k] = fmax_ref(mx[k], red[w * 6 + 3 + k]);
+  if (threadIdx.x < 32) leaf_box_from_chunks(m, leaf);
+  __syncthreads();
+}
+
+// Chunk boxes of every leaf (mesh creation, positions replaced): one warp per
+// chunk, grid-stride over all chunks.
+__global__ void __launch_bounds__(kThreads) k_chunk_boxes_all(DevMesh m, int nchunks) {
+  float mn[3], mx[3];
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); id < nchunks; id += warps) {
+    int lo = 0, hi = m.nleaf;  // leaf_chunk_off[lo] <= id < leaf_chunk_off[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (m.leaf_chunk_off[mid] <= id) {
+        lo = mid;
+      } else {
+        hi = mid;
       }
-    const int node = m.leaf_node[leaf];
-    m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
-    m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+    }
+    chunk_refit_warp(m, lo, id - m.leaf_chunk_off[lo], mn, mx);
   }
-  __syncthreads();
+}
+
+cudaError_t launch_chunk_boxes_all(const DevMesh& m, int nchunks, cudaStream_t s) {
+  int g = (nchunks + (kThreads / 32) - 1) / (kThreads / 32);
+  if (g > 4096) g = 4096;
+  if (g < 1) g = 1;
+  k_chunk_boxes_all<<<g, kThreads, 0, s>>>(m, nchunks);
+  return cudaGetLastError();
 }
 
 __device__ void faces_leaf_normals(const DevMesh& m, int leaf, unsigned long long& ab) {

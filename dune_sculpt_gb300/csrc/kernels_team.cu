@@ -29,8 +29,9 @@ namespace sgpu {
 constexpr int kTeamThreads = 256;
 
 __host__ __device__ inline size_t team_fn_offset(int max_nodes, int max_leaves) {
+  // parents, culled list, offsets (int); node positions (ushort); node marks
   const size_t b = sizeof(int) * (static_cast<size_t>(max_nodes) + 2 * static_cast<size_t>(max_leaves) + 3) +
-                   static_cast<size_t>(max_nodes);
+                   sizeof(unsigned short) * static_cast<size_t>(max_nodes) + static_cast<size_t>(max_nodes);
   return (b + 15) & ~static_cast<size_t>(15);
 }
 
@@ -40,7 +41,7 @@ struct TeamShared {
   int jobid;
   int cnt, total;
   int scan[32];
-  int run[2];
+  unsigned long long scan64[32];
   float area[6];
   int nmark;
 };
@@ -118,90 +119,178 @@ __device__ __forceinline__ void tag_vertex(const DevMesh& m, int v, int* tag_cnt
   if (atomicExch(&m.vtag[v], 1u) == 0u) append(m.tag_list, tag_cnt, v);
 }
 
+// Block-wide exclusive scan of 64-bit values (kTeamThreads threads).
+__device__ unsigned long long team_block_scan64(unsigned long long v, unsigned long long* total,
+                                                unsigned long long* smem32) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nwarps = kTeamThreads / 32;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem32[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < nwarps ? smem32[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    smem32[lane] = w;
+  }
+  __syncthreads();
+  const unsigned long long warp_base = warp > 0 ? smem32[warp - 1] : 0ull;
+  *total = smem32[nwarps - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+__device__ __forceinline__ bool leaf_passes(const DevMesh& m, const int* s_par,
+                                            const unsigned char* s_pass, int id) {
+  const int node = m.leaf_node[id];
+  bool ok = s_pass[node];
+  int p = s_par[node];
+  while (ok && p >= 0) {
+    ok = s_pass[p];
+    p = s_par[p];
+  }
+  return ok;
+}
+
 // Node search of one pass into this CTA's shared memory (every CTA of the team
-// computes the same list).  Same test and order as k_cull.
+// computes the same list).  Same test and order as k_cull: every node box is
+// tested, then each thread owns a run of consecutive leaves, and one block
+// scan of (count, vertex count) places each run's passing leaves.
 __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_par,
                           unsigned char* s_pass, int* s_cl, int* s_coff, TeamShared& sh) {
   const float4* bb = pp.original ? m.orig_vb : m.vb;
   for (int n = threadIdx.x; n < m.totnode; n += kTeamThreads)
     s_pass[n] = box_hits(__ldcg(&bb[2 * n]), __ldcg(&bb[2 * n + 1]), pp.loc, pp.cull_radius_sq);
-  if (threadIdx.x == 0) sh.run[0] = sh.run[1] = 0;
   __syncthreads();
-  for (int base = 0; base < m.nleaf; base += kTeamThreads) {
-    const int id = base + threadIdx.x;
-    int ok = 0, nv = 0;
-    if (id < m.nleaf) {
-      const int node = m.leaf_node[id];
-      ok = s_pass[node];
-      int p = s_par[node];
-      while (ok && p >= 0) {
-        ok = s_pass[p];
-        p = s_par[p];
-      }
-      nv = ok ? leaf_nverts(m, id) : 0;
+  const int L = m.nleaf;
+  const int seg = (L + kTeamThreads - 1) / kTeamThreads;
+  const int l0 = min(L, threadIdx.x * seg), l1 = min(L, l0 + seg);
+  unsigned long long okmask = 0ull;
+  unsigned long long cnt = 0ull, nvs = 0ull;
+  for (int id = l0; id < l1; id++) {
+    if (leaf_passes(m, s_par, s_pass, id)) {
+      cnt++;
+      nvs += static_cast<unsigned long long>(leaf_nverts(m, id));
+      if (id - l0 < 64) okmask |= 1ull << (id - l0);
     }
-    int tot_ok, tot_nv;
-    const int pos = team_block_scan(ok, &tot_ok, sh.scan);
-    const int voff = team_block_scan(nv, &tot_nv, sh.scan);
-    if (ok) {
-      s_cl[sh.run[0] + pos] = id;
-      s_coff[sh.run[0] + pos] = sh.run[1] + voff;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      sh.run[0] += tot_ok;
-      sh.run[1] += tot_nv;
-    }
-    __syncthreads();
+  }
+  // (vertex count << 24) | leaf count: leaves < 2^24, vertices < 2^31
+  unsigned long long total;
+  const unsigned long long excl = team_block_scan64((nvs << 24) | cnt, &total, sh.scan64);
+  int pos = static_cast<int>(excl & 0xFFFFFFull);
+  int voff = static_cast<int>(excl >> 24);
+  for (int id = l0; id < l1; id++) {
+    const bool ok = (id - l0 < 64) ? ((okmask >> (id - l0)) & 1ull) != 0ull
+                                   : leaf_passes(m, s_par, s_pass, id);
+    if (!ok) continue;
+    s_cl[pos] = id;
+    s_coff[pos] = voff;
+    pos++;
+    voff += leaf_nverts(m, id);
   }
   if (threadIdx.x == 0) {
-    sh.cnt = sh.run[0];
-    sh.total = sh.run[1];
-    s_coff[sh.run[0]] = sh.run[1];
+    sh.cnt = static_cast<int>(total & 0xFFFFFFull);
+    sh.total = static_cast<int>(total >> 24);
+    s_coff[sh.cnt] = sh.total;
   }
   __syncthreads();
 }
 
-// Leaf box refit by the whole CTA (update_node_vb over PBVH_ITER_ALL).
-__device__ void team_leaf_refit(const DevMesh& m, int leaf, float* red) {
-  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
-  float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-  const int nv = leaf_nverts_all(m, leaf);
-  for (int i = threadIdx.x; i < nv; i += kTeamThreads) {
-    const int v = m.type == kFaces ? m.leaf_verts[m.leaf_vert_off[leaf] + i] : leaf_vert(m, leaf, i);
-    const float4 c = __ldcg(&m.co[v]);
-    mn[0] = fmin_ref(mn[0], c.x);
-    mn[1] = fmin_ref(mn[1], c.y);
-    mn[2] = fmin_ref(mn[2], c.z);
-    mx[0] = fmax_ref(mx[0], c.x);
-    mx[1] = fmax_ref(mx[1], c.y);
-    mx[2] = fmax_ref(mx[2], c.z);
-  }
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      mn[k] = fmin_ref(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-      mx[k] = fmax_ref(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
-    }
-  }
+constexpr int kFlushTab = 256;  // ancestor boxes cached in shared memory
+constexpr unsigned short kNoPos = 0xFFFFu, kClaimed = 0xFFFEu;
+
+// Bottom-up flush by one CTA: touched leaf boxes from their chunk boxes, then
+// every ancestor of a touched leaf recomputed from its two children
+// (update_node_vb, pbvh.c:2026-2046), deepest level first, as pbvh_flush_bb
+// (pbvh.c:3287-3317) orders it.  Clears the touched leaves' UpdateNormals and
+// UpdateBB.  s_idx holds kNoPos for every node on entry and on exit; an
+// ancestor is first claimed with kClaimed, then given its sorted position.
+__device__ void team_flush(const DevMesh& m, int ntouch, const int* s_par, unsigned short* s_idx,
+                           int* s_list, int* s_sorted, float4* s_tab, int* s_start, int* s_cur,
+                           TeamShared& sh, unsigned long long& ab) {
   const int warp = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0)
-    for (int k = 0; k < 3; k++) {
-      red[warp * 6 + k] = mn[k];
-      red[warp * 6 + 3 + k] = mx[k];
+  for (int k = warp; k < ntouch; k += kTeamThreads / 32) {
+    const int leaf = __ldcg(&m.touch_list[k]);
+    leaf_box_from_chunks(m, leaf);
+    // chunk boxes read, leaf box written
+    if ((threadIdx.x & 31) == 0) ab += 32ull * (m.leaf_chunk_off[leaf + 1] - m.leaf_chunk_off[leaf] + 1);
+  }
+  if (threadIdx.x == 0) sh.nmark = 0;
+  for (int i = threadIdx.x; i <= m.max_depth; i += kTeamThreads) s_start[i] = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < ntouch; k += kTeamThreads) {
+    int p = s_par[m.leaf_node[__ldcg(&m.touch_list[k])]];
+    while (p >= 0 && atomicCAS(&s_idx[p], kNoPos, kClaimed) == kNoPos) {
+      s_list[atomicAdd(&sh.nmark, 1)] = p;
+      p = s_par[p];
     }
+  }
+  __syncthreads();
+  const int nm = sh.nmark;
+  for (int j = threadIdx.x; j < nm; j += kTeamThreads) atomicAdd(&s_start[m.node_depth[s_list[j]]], 1);
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < kTeamThreads / 32; w++)
-      for (int k = 0; k < 3; k++) {
-        mn[k] = fmin_ref(mn[k], red[w * 6 + k]);
-        mx[k] = fmax_ref(mx[k], red[w * 6 + 3 + k]);
-      }
-    const int node = m.leaf_node[leaf];
-    m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
-    m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+    int run = 0;
+    for (int dd = m.max_depth; dd >= 0; dd--) {
+      const int c = s_start[dd];
+      s_start[dd] = run;
+      s_cur[dd] = run;
+      run += c;
+    }
   }
+  __syncthreads();
+  for (int j = threadIdx.x; j < nm; j += kTeamThreads) {
+    const int node = s_list[j];
+    const int pos = atomicAdd(&s_cur[m.node_depth[node]], 1);
+    s_sorted[pos] = node;
+    s_idx[node] = static_cast<unsigned short>(pos);
+  }
+  __syncthreads();
+  for (int dd = m.max_depth; dd >= 0; dd--) {
+    const int b0 = s_start[dd], b1 = s_cur[dd];
+    for (int pos = b0 + threadIdx.x; pos < b1; pos += kTeamThreads) {
+      const int node = s_sorted[pos];
+      const int c = m.node_child[node];
+      float4 box[2][2];
+      for (int h = 0; h < 2; h++) {
+        const int ci = s_idx[c + h];  // children are one level deeper: done
+        if (ci < kFlushTab) {
+          box[h][0] = s_tab[2 * ci];
+          box[h][1] = s_tab[2 * ci + 1];
+        } else {
+          box[h][0] = __ldcg(&m.vb[2 * (c + h)]);
+          box[h][1] = __ldcg(&m.vb[2 * (c + h) + 1]);
+        }
+      }
+      float4 mn, mx;
+      mn.x = fmin_ref(fmin_ref(FLT_MAX, box[0][0].x), box[1][0].x);
+      mn.y = fmin_ref(fmin_ref(FLT_MAX, box[0][0].y), box[1][0].y);
+      mn.z = fmin_ref(fmin_ref(FLT_MAX, box[0][0].z), box[1][0].z);
+      mx.x = fmax_ref(fmax_ref(-FLT_MAX, box[0][1].x), box[1][1].x);
+      mx.y = fmax_ref(fmax_ref(-FLT_MAX, box[0][1].y), box[1][1].y);
+      mx.z = fmax_ref(fmax_ref(-FLT_MAX, box[0][1].z), box[1][1].z);
+      mn.w = mx.w = 0.0f;
+      m.vb[2 * node] = mn;
+      m.vb[2 * node + 1] = mx;
+      if (pos < kFlushTab) {
+        s_tab[2 * pos] = mn;
+        s_tab[2 * pos + 1] = mx;
+      }
+      ab += 72u;  // two child boxes read, one box written
+    }
+    __syncthreads();
+  }
+  for (int pos = threadIdx.x; pos < nm; pos += kTeamThreads) s_idx[s_sorted[pos]] = kNoPos;
+  for (int k = threadIdx.x; k < ntouch; k += kTeamThreads)
+    atomicAnd(&m.leaf_flag[__ldcg(&m.touch_list[k])], ~(kUpdateNormals | kUpdateBB));
   __syncthreads();
 }
 
@@ -344,7 +433,7 @@ struct PhaseClock {
   }
 };
 
-__global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
+__global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned C = cluster.num_blocks();
   const unsigned rank = cluster.block_rank();
@@ -353,12 +442,14 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
   __shared__ TeamShared sh;
   __shared__ Lane s_lanes[kTeamThreads];
   __shared__ Lane s_chunks[kTeamMaxChunks];
-  __shared__ float s_red[6 * (kTeamThreads / 32)];
+  __shared__ float4 s_tab[2 * kFlushTab];
+  __shared__ int s_start[256], s_cur[256];
   extern __shared__ __align__(16) unsigned char dyn[];
   int* s_par = reinterpret_cast<int*>(dyn);
   int* s_cl = s_par + a.max_nodes;
   int* s_coff = s_cl + a.max_leaves + 1;
-  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_coff + a.max_leaves + 2);
+  unsigned short* s_idx = reinterpret_cast<unsigned short*>(s_coff + a.max_leaves + 2);
+  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_idx + a.max_nodes);
   float* s_fn = reinterpret_cast<float*>(dyn + team_fn_offset(a.max_nodes, a.max_leaves));
   PhaseClock clk;
   clk.last = a.phase_ns ? global_ns() : 0ull;
@@ -386,7 +477,10 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
     const DevMesh& m = sh.m;
     DevBrush& b = sh.job.brush;
     Work* w = m.work;
-    for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_par[i] = m.node_parent[i];
+    for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) {
+      s_par[i] = m.node_parent[i];
+      s_idx[i] = kNoPos;
+    }
     // GRIDS work-list stamps: dab d uses epoch grid_epoch0 + d + 1
     const unsigned int grid_epoch0 = __ldcg(&w->grid_epoch);
     team_sync(cluster, C);
@@ -608,73 +702,42 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
         team_sync(cluster, C);
         if (rank == 0 && threadIdx.x == 0) m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = 0;
       }
-      for (int k = rank; k < ntouch; k += C) {
-        const int leaf = __ldcg(&m.touch_list[k]);
-        team_leaf_refit(m, leaf, s_red);
-        const int nv = leaf_nverts_all(m, leaf);
-        if (threadIdx.x < nv)
-          ab += (m.type == kFaces ? 16ull : 12ull) * ((nv - threadIdx.x + kTeamThreads - 1) / kTeamThreads);
-        if (threadIdx.x == 0) ab += 24u;
+      // refit: the chunk boxes of the touched leaves, one warp per chunk
+      // across the team (chunk offsets of the touched leaves in s_coff)
+      {
+        const int seg = (ntouch + kTeamThreads - 1) / kTeamThreads;
+        const int t0 = min(ntouch, static_cast<int>(threadIdx.x) * seg), t1 = min(ntouch, t0 + seg);
+        int nc = 0;
+        for (int k = t0; k < t1; k++) {
+          const int leaf = __ldcg(&m.touch_list[k]);
+          s_cl[k] = leaf;
+          nc += m.leaf_chunk_off[leaf + 1] - m.leaf_chunk_off[leaf];
+        }
+        int nchunk;
+        int off = team_block_scan(nc, &nchunk, sh.scan);
+        for (int k = t0; k < t1; k++) {
+          s_coff[k] = off;
+          off += m.leaf_chunk_off[s_cl[k] + 1] - m.leaf_chunk_off[s_cl[k]];
+        }
+        __syncthreads();
+        const int wpc = kTeamThreads / 32;
+        const unsigned idb = (m.type == kFaces ? 4u : 0u) + 12u;  // vertex id, position
+        for (int j = rank * wpc + (threadIdx.x >> 5); j < nchunk; j += C * wpc) {
+          const int k = smem_find_slot(s_coff, ntouch, j);
+          const int leaf = s_cl[k], c = j - s_coff[k];
+          float mn[3], mx[3];
+          chunk_refit_warp(m, leaf, c, mn, mx);
+          if ((threadIdx.x & 31) == 0)
+            ab += 32ull + idb * static_cast<unsigned long long>(min(kChunk, leaf_nverts_all(m, leaf) - c * kChunk));
+        }
       }
       team_bytes(a, kPhUpdate, ab);
       team_sync(cluster, C);
       clk.mark(a, rank, kPhUpdate);
-      // flush: every ancestor of a touched leaf is the union of the boxes of
-      // the leaves below it (a leaf-id range in left-first DFS order)
-      for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_pass[i] = 0;
-      __syncthreads();
-      for (int k = threadIdx.x; k < ntouch; k += kTeamThreads) {
-        int p = s_par[m.leaf_node[__ldcg(&m.touch_list[k])]];
-        while (p >= 0 && !s_pass[p]) {
-          s_pass[p] = 1;
-          p = s_par[p];
-        }
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) sh.run[0] = 0;
-      __syncthreads();
-      for (int base = 0; base < m.totnode; base += kTeamThreads) {
-        const int n = base + threadIdx.x;
-        const int mk = (n < m.totnode) ? s_pass[n] : 0;
-        int tot;
-        const int pos = team_block_scan(mk, &tot, sh.scan);
-        if (mk) s_cl[sh.run[0] + pos] = n;
-        __syncthreads();
-        if (threadIdx.x == 0) sh.run[0] += tot;
-        __syncthreads();
-      }
-      const int nmark = sh.run[0];
-      const int lane = threadIdx.x & 31;
-      for (int idx = gt >> 5; idx < nmark; idx += GT >> 5) {
-        const int node = s_cl[idx];
-        float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
-        float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-        for (int l = m.node_leaf_lo[node] + lane; l < m.node_leaf_hi[node]; l += 32) {
-          const int ln = m.leaf_node[l];
-          const float4 a0 = __ldcg(&m.vb[2 * ln]), a1 = __ldcg(&m.vb[2 * ln + 1]);
-          mn[0] = fmin_ref(mn[0], a0.x);
-          mn[1] = fmin_ref(mn[1], a0.y);
-          mn[2] = fmin_ref(mn[2], a0.z);
-          mx[0] = fmax_ref(mx[0], a1.x);
-          mx[1] = fmax_ref(mx[1], a1.y);
-          mx[2] = fmax_ref(mx[2], a1.z);
-        }
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1)
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            mn[k] = fmin_ref(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-            mx[k] = fmax_ref(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
-          }
-        if (lane == 0) {
-          m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
-          m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
-        }
-      }
-      for (int k = gt; k < ntouch; k += GT)
-        atomicAnd(&m.leaf_flag[__ldcg(&m.touch_list[k])], ~(kUpdateNormals | kUpdateBB));
-      // two child boxes read and one box written per updated ancestor
-      team_bytes(a, kPhFlush, gt < nmark ? 72ull * ((nmark - gt + GT - 1) / GT) : 0ull);
+      // flush by CTA 0: touched leaf boxes, then their ancestors bottom-up
+      unsigned long long fb = 0;
+      if (rank == 0) team_flush(m, ntouch, s_par, s_idx, s_cl, s_coff, s_tab, s_start, s_cur, sh, fb);
+      team_bytes(a, kPhFlush, fb);
       team_sync(cluster, C);
       clk.mark(a, rank, kPhFlush);
     }
@@ -706,8 +769,9 @@ __global__ void __launch_bounds__(kTeamThreads) k_team_stroke(TeamArgs a) {
   }
 }
 
-// Dynamic shared memory: parents, culled list and offsets, node marks, then
-// the grid face-normal scratch (16-byte aligned, team_fn_offset).
+// Dynamic shared memory: parents, culled list and offsets, flush positions,
+// node marks, then the grid face-normal scratch (16-byte aligned,
+// team_fn_offset).
 size_t team_smem_bytes(int max_nodes, int max_leaves, int max_grid_fn) {
   return team_fn_offset(max_nodes, max_leaves) + sizeof(float) * static_cast<size_t>(max_grid_fn) + 16;
 }

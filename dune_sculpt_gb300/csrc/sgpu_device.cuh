@@ -84,6 +84,13 @@ struct DevMesh {
   const int* level_nodes;
   const int* node_leaf_lo;   // first leaf id under the node
   const int* node_leaf_hi;   // one past the last leaf id under the node
+  const int* node_depth;     // root = 0
+  int max_depth;
+  // Refit chunks: each leaf's full vertex list (PBVH_ITER_ALL order) in runs
+  // of kChunk entries; chunk_box holds each run's box (2 float4), refreshed by
+  // every refit, so a leaf box is the union of its chunk boxes.
+  const int* leaf_chunk_off;  // nleaf+1
+  float4* chunk_box;
   // persistent stroke kernel work lists
   int* hit_list[2];  // smooth: vertices inside the sphere, ping-pong per iteration
   int* tag_list;     // vertices tagged in the current dab
@@ -328,6 +335,74 @@ __device__ __forceinline__ int leaf_vert(const DevMesh& m, int leaf, int i) {
 __device__ __forceinline__ int leaf_nverts_all(const DevMesh& m, int leaf) {
   if (m.type == kFaces) return m.leaf_vert_off[leaf + 1] - m.leaf_vert_off[leaf];
   return (m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf]) * m.grid_area;
+}
+__device__ __forceinline__ int leaf_vert_all(const DevMesh& m, int leaf, int i) {
+  if (m.type == kFaces) return m.leaf_verts[m.leaf_vert_off[leaf] + i];
+  return leaf_vert(m, leaf, i);
+}
+
+constexpr int kChunk = 64;
+
+// Box of refit chunk c of a leaf by one warp (two entries per lane, loads
+// issued together), stored in chunk_box; every lane returns the box.
+__device__ __forceinline__ void chunk_refit_warp(const DevMesh& m, int leaf, int c, float* mn,
+                                                 float* mx) {
+  const int lane = threadIdx.x & 31;
+  const int nv = leaf_nverts_all(m, leaf);
+  const int i0 = c * kChunk + lane, i1 = i0 + 32;
+  const int e = min(nv, (c + 1) * kChunk);
+  const int v0 = i0 < e ? leaf_vert_all(m, leaf, i0) : -1;
+  const int v1 = i1 < e ? leaf_vert_all(m, leaf, i1) : -1;
+  const float4 p0 = v0 >= 0 ? __ldcg(&m.co[v0]) : make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
+  const float4 p1 = v1 >= 0 ? __ldcg(&m.co[v1]) : p0;
+  float a[3] = {p0.x, p0.y, p0.z}, b[3] = {p1.x, p1.y, p1.z};
+  for (int k = 0; k < 3; k++) {
+    mn[k] = v0 >= 0 ? ((a[k] < b[k]) ? a[k] : b[k]) : FLT_MAX;
+    mx[k] = v0 >= 0 ? ((a[k] > b[k]) ? a[k] : b[k]) : -FLT_MAX;
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float omn = __shfl_xor_sync(0xffffffffu, mn[k], o);
+      const float omx = __shfl_xor_sync(0xffffffffu, mx[k], o);
+      mn[k] = (mn[k] < omn) ? mn[k] : omn;
+      mx[k] = (mx[k] > omx) ? mx[k] : omx;
+    }
+  if (lane == 0) {
+    const int id = m.leaf_chunk_off[leaf] + c;
+    m.chunk_box[2 * id] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+    m.chunk_box[2 * id + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+  }
+}
+
+// Leaf box as the union of its chunk boxes, by one warp; lane 0 writes vb.
+__device__ __forceinline__ void leaf_box_from_chunks(const DevMesh& m, int leaf) {
+  const int lane = threadIdx.x & 31;
+  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int id = m.leaf_chunk_off[leaf] + lane; id < m.leaf_chunk_off[leaf + 1]; id += 32) {
+    const float4 a = __ldcg(&m.chunk_box[2 * id]), b = __ldcg(&m.chunk_box[2 * id + 1]);
+    mn[0] = (mn[0] < a.x) ? mn[0] : a.x;
+    mn[1] = (mn[1] < a.y) ? mn[1] : a.y;
+    mn[2] = (mn[2] < a.z) ? mn[2] : a.z;
+    mx[0] = (mx[0] > b.x) ? mx[0] : b.x;
+    mx[1] = (mx[1] > b.y) ? mx[1] : b.y;
+    mx[2] = (mx[2] > b.z) ? mx[2] : b.z;
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float omn = __shfl_xor_sync(0xffffffffu, mn[k], o);
+      const float omx = __shfl_xor_sync(0xffffffffu, mx[k], o);
+      mn[k] = (mn[k] < omn) ? mn[k] : omn;
+      mx[k] = (mx[k] > omx) ? mx[k] : omx;
+    }
+  if (lane == 0) {
+    const int node = m.leaf_node[leaf];
+    m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+    m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+  }
 }
 
 __device__ __forceinline__ float dist_sq(float4 co, const float* c) {

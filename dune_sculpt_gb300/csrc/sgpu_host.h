@@ -75,6 +75,8 @@ struct HostMesh {
   std::vector<int> node_leaf;   // node -> leaf id or -1
   std::vector<int> level_off, level_nodes;  // internal nodes by depth, deepest first
   std::vector<int> leaf_lo, leaf_hi;        // per node: leaf-id range of its subtree
+  std::vector<int> depth;                   // per node, root = 0
+  int max_depth = 0;
   std::vector<int> lt_leaf;                 // looptri -> leaf id
 };
 

@@ -29,6 +29,8 @@ cudaError_t launch_grid_seams(const DevMesh& m, cudaStream_t s);
 cudaError_t launch_l2_flush(void* buf, size_t bytes, cudaStream_t s);
 cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s);
 cudaError_t launch_mark_all(const DevMesh& m, int bits, cudaStream_t s);
+// Refit-chunk boxes of every leaf from the current positions.
+cudaError_t launch_chunk_boxes_all(const DevMesh& m, int nchunks, cudaStream_t s);
 int cull_smem_limit();
 int grid_size_limit();
 void configure_kernels();
