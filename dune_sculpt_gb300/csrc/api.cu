@@ -247,6 +247,10 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->alloc(&d.cull_off, L + 2))) return rc;
   if ((rc = m->alloc(&d.parts, L + 1))) return rc;
   if ((rc = m->alloc(&d.scratch, static_cast<size_t>(h.totvert)))) return rc;
+  if ((rc = m->alloc(&d.scratch2, static_cast<size_t>(h.totvert)))) return rc;
+  if ((rc = m->alloc(&d.slot_map, static_cast<size_t>(h.totvert)))) return rc;
+  CK(cudaMemsetAsync(d.slot_map, 0xFF, sizeof(int) * static_cast<size_t>(h.totvert), m->stream),
+     "slot map init");
   if ((rc = m->alloc(&d.node_upd, N))) return rc;
   if ((rc = m->alloc(&m->d_nodes_tmp, L + 1))) return rc;
   if (N > cull_smem_limit())
@@ -370,7 +374,8 @@ int launch_update_normals(Launcher& L, int bounds_flag) {
     LAUNCH(L, kKUpdate, "update kernel", launch_update_faces(d, 1, bounds_flag, s));
   } else {
     LAUNCH(L, kKGridGather, "grid gather kernel", launch_grid_gather(d, s));
-    LAUNCH(L, kKGridFaces, "grid face kernel", launch_grid_faces(d, s));
+    LAUNCH(L, kKGridFaces, "grid inner-normal kernel", launch_grid_inner(d, s));
+    LAUNCH(L, kKGridFaces, "grid face-seam kernel", launch_grid_face_seams(d, s));
     LAUNCH(L, kKGridSeams, "grid seam kernel", launch_grid_seams(d, s));
     if (bounds_flag) LAUNCH(L, kKUpdate, "bounds kernel", launch_update_faces(d, 0, bounds_flag, s));
   }
@@ -579,19 +584,31 @@ int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPol
        "upload automask");
     d.automask = da;
   }
-  std::vector<int4> lt(totlooptri);
-  for (int t = 0; t < totlooptri; t++)
-    lt[t] = make_int4(h.lt_v[3 * t], h.lt_v[3 * t + 1], h.lt_v[3 * t + 2], h.lt_poly[t]);
   std::vector<int2> pl(totpoly);
-  for (int p = 0; p < totpoly; p++) pl[p] = make_int2(h.poly_loopstart[p], h.poly_totloop[p]);
-  if ((rc = m->upload(&d.lt, lt))) return bail(rc);
+  std::vector<int4> pv(totpoly);
+  for (int p = 0; p < totpoly; p++) {
+    const int ls = h.poly_loopstart[p], tl = h.poly_totloop[p];
+    pl[p] = make_int2(ls, tl);
+    if (tl == 3) {
+      pv[p] = make_int4(h.loop_v[ls], h.loop_v[ls + 1], h.loop_v[ls + 2], -1);
+    } else if (tl == 4) {
+      pv[p] = make_int4(h.loop_v[ls], h.loop_v[ls + 1], h.loop_v[ls + 2], h.loop_v[ls + 3]);
+    } else {
+      pv[p] = make_int4(-1, -1, -1, -1);
+    }
+  }
+  std::vector<int2> vt_meta(h.vt_idx.size());
+  for (size_t q = 0; q < h.vt_idx.size(); q++) {
+    const int t = h.vt_idx[q];
+    vt_meta[q] = make_int2(h.lt_poly[t], h.lt_leaf[t]);
+  }
   if ((rc = m->upload(&d.poly, pl))) return bail(rc);
+  if ((rc = m->upload(&d.poly_v4, pv))) return bail(rc);
   if ((rc = m->upload(&d.loop_v, h.loop_v))) return bail(rc);
   if ((rc = m->upload(&d.vt_off, h.vt_off))) return bail(rc);
-  if ((rc = m->upload(&d.vt_idx, h.vt_idx))) return bail(rc);
+  if ((rc = m->upload(&d.vt_meta, vt_meta))) return bail(rc);
   if ((rc = m->upload(&d.nb_off, h.nb_off))) return bail(rc);
   if ((rc = m->upload(&d.nb_idx, h.nb_idx))) return bail(rc);
-  if ((rc = m->upload(&d.lt_leaf, h.lt_leaf))) return bail(rc);
   if ((rc = m->alloc(&d.vtag, totvert))) return bail(rc);
   if ((rc = upload_pbvh(m))) return bail(rc);
   if (!vert_normals) {
@@ -701,6 +718,7 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
   if ((rc = m->upload(&d.bvert_off, h.bvert_off))) return bail(rc);
   if ((rc = m->upload(&d.bvert_elems, h.bvert_elems))) return bail(rc);
   if ((rc = m->alloc(&d.face_list, num_faces))) return bail(rc);
+  if ((rc = m->alloc(&d.cgrid_list, num_grids))) return bail(rc);
   if ((rc = m->alloc(&d.edge_list, num_base_edges))) return bail(rc);
   if ((rc = m->alloc(&d.bvert_list, num_base_verts))) return bail(rc);
   if ((rc = m->alloc(&d.face_mark, num_faces))) return bail(rc);
@@ -918,8 +936,7 @@ int sgpu_autotune_team(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab*
   float best_ms = -1.0f;
   for (int k = 0; k < 5; k++) {
     float ms = -1.0f;
-    const int g1 = mesh->dev.type == kGrids ? mesh->dev.grid_size - 1 : 0;
-    if (team_max_active_clusters(sizes[k], mesh->dev.totnode, mesh->dev.nleaf, 3 * g1 * g1) > 0) {
+    if (team_max_active_clusters(sizes[k], mesh->dev.totnode, mesh->dev.nleaf) > 0) {
       const int offs[2] = {0, ndabs};
       sgpu_mesh* one[1] = {mesh};
       // two trials, keep the second (the first pays one-time setup)
@@ -1451,18 +1468,14 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
                const int* offs, const int* tools, int cluster, cudaStream_t s,
                SGPU_StrokeStats* stats, float* total_ms) {
   sgpu_mesh* m0 = meshes[0];
-  int max_nodes = 0, max_leaves = 0, max_fn = 0;
+  int max_nodes = 0, max_leaves = 0;
   for (int i = 0; i < n; i++) {
     max_nodes = std::max(max_nodes, meshes[i]->dev.totnode);
     max_leaves = std::max(max_leaves, meshes[i]->dev.nleaf);
-    if (meshes[i]->dev.type == kGrids) {
-      const int g1 = meshes[i]->dev.grid_size - 1;
-      max_fn = std::max(max_fn, 3 * g1 * g1);
-    }
   }
-  if (max_leaves > 64 * 256 || team_smem_bytes(max_nodes, max_leaves, max_fn) > 160 * 1024)
+  if (max_leaves > 64 * 256 || team_smem_bytes(max_nodes, max_leaves) > 160 * 1024)
     return fail(SGPU_ERR_UNSUPPORTED, "PBVH too large for the persistent stroke kernel");
-  const int nteams_max = team_max_active_clusters(cluster, max_nodes, max_leaves, max_fn);
+  const int nteams_max = team_max_active_clusters(cluster, max_nodes, max_leaves);
   if (nteams_max <= 0)
     return fail(SGPU_ERR_UNSUPPORTED, "cluster size %d cannot be launched", cluster);
   int rc;
@@ -1525,7 +1538,6 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.next_job = m0->t_counter;
   a.max_nodes = max_nodes;
   a.max_leaves = max_leaves;
-  a.max_grid_fn = max_fn;
   a.prof_bytes = g_team_prof_bytes;
   a.phase_ns = g_team_phase_ns;
   const int nteams = std::min(n, nteams_max);

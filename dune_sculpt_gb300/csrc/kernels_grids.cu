@@ -4,8 +4,8 @@
 // (subdiv_ccg.c:847-874).
 //   k_grid_gather:  faces of flagged leaves (deduplicated), their base edges
 //                   and base vertices; clears UpdateNormals.
-//   k_grid_faces:   per face, inner grid normals and the face-internal
-//                   seam/centre averaging.
+//   k_grid_inner:   inner normals of every element of the claimed grids.
+//   k_grid_face_seams: face-internal seam pairs and face centres.
 //   k_grid_seams:   averaging across base edges and base-vertex corners; both
 //                   touch disjoint elements.
 // Work lists are built with atomics, so their order varies, but every list
@@ -31,20 +31,28 @@ __global__ void __launch_bounds__(kGThreads) k_grid_gather(DevMesh m) {
   }
 }
 
-// One CTA per affected face (grid-stride).  Shared memory: (gs-1)^2 quad
-// normals of the grid being processed.
-__global__ void __launch_bounds__(kGThreads) k_grid_faces(DevMesh m) {
-  extern __shared__ float fn[];  // 3 * (gs-1)^2
-  const int nf = m.grid_counts[0];
-  const int g1 = m.grid_size - 1, area = m.grid_area;
-  unsigned long long ab = 0;  // algorithmic bytes (profiling)
-  for (int k = blockIdx.x; k < nf; k += gridDim.x) {
-    const int f = m.face_list[k];
-    const int n = m.face_ngrids[f];
-    // co read + normal written per element; each seam pair and the centre
-    // read and write co, no and mask of their elements
-    if (threadIdx.x == 0) ab += 24ull * area * n + 112ull * g1 * n + 56ull * n;
-    grid_face_update(m, f, fn);
+// One thread per element of the claimed grids (grid-stride).
+__global__ void __launch_bounds__(kGThreads) k_grid_inner(DevMesh m) {
+  const long long items = (long long)m.grid_counts[3] * m.grid_area;
+  unsigned long long ab = 0;  // algorithmic bytes (profiling): co read, normal written
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+       it += (long long)gridDim.x * blockDim.x) {
+    grid_inner_item(m, it);
+    ab += 24u;
+  }
+  prof_add(m, kKGridFaces, ab);
+}
+
+// One thread per face-internal seam pair or face centre (grid-stride).
+__global__ void __launch_bounds__(kGThreads) k_grid_face_seams(DevMesh m) {
+  const int ng = m.grid_counts[3], nf = m.grid_counts[0];
+  const long long pairs = (long long)ng * (m.grid_size - 1);
+  const long long items = pairs + nf;
+  unsigned long long ab = 0;  // co, no and mask read and written per element
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+       it += (long long)gridDim.x * blockDim.x) {
+    grid_face_seam_item(m, it, ng);
+    ab += it < pairs ? 112ull : 56ull * m.face_ngrids[m.face_list[it - pairs]];
   }
   prof_add(m, kKGridFaces, ab);
 }
@@ -84,6 +92,7 @@ __global__ void __launch_bounds__(kGThreads) k_grid_seams(DevMesh m) {
     m.grid_counts[0] = 0;
     m.grid_counts[1] = 0;
     m.grid_counts[2] = 0;
+    m.grid_counts[3] = 0;
     m.work->grid_epoch = m.work->grid_epoch + 1u;
     m.work->ticket_update = 0u;
   }
@@ -102,11 +111,7 @@ static int grids_grid() {
 
 int grid_size_limit() { return 65; }
 
-void configure_grid_kernels() {
-  const int g1 = grid_size_limit() - 1;
-  cudaFuncSetAttribute(k_grid_faces, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       static_cast<int>(sizeof(float) * 3 * g1 * g1));
-}
+void configure_grid_kernels() {}
 
 cudaError_t launch_grid_gather(const DevMesh& m, cudaStream_t s) {
   const int g = grids_grid();
@@ -116,9 +121,13 @@ cudaError_t launch_grid_gather(const DevMesh& m, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_grid_faces(const DevMesh& m, cudaStream_t s) {
-  const size_t smem = sizeof(float) * 3 * (m.grid_size - 1) * (m.grid_size - 1);
-  k_grid_faces<<<grids_grid(), kGThreads, smem, s>>>(m);
+cudaError_t launch_grid_inner(const DevMesh& m, cudaStream_t s) {
+  k_grid_inner<<<grids_grid(), kGThreads, 0, s>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grid_face_seams(const DevMesh& m, cudaStream_t s) {
+  k_grid_face_seams<<<grids_grid(), kGThreads, 0, s>>>(m);
   return cudaGetLastError();
 }
 

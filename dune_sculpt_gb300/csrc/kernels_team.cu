@@ -28,13 +28,6 @@ namespace sgpu {
 
 constexpr int kTeamThreads = 256;
 
-__host__ __device__ inline size_t team_fn_offset(int max_nodes, int max_leaves) {
-  // parents, culled list, offsets (int); node positions (ushort); node marks
-  const size_t b = sizeof(int) * (static_cast<size_t>(max_nodes) + 2 * static_cast<size_t>(max_leaves) + 3) +
-                   sizeof(unsigned short) * static_cast<size_t>(max_nodes) + static_cast<size_t>(max_nodes);
-  return (b + 15) & ~static_cast<size_t>(15);
-}
-
 struct TeamShared {
   DevMesh m;
   TeamJob job;
@@ -167,8 +160,23 @@ __device__ __forceinline__ bool leaf_passes(const DevMesh& m, const int* s_par,
 __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_par,
                           unsigned char* s_pass, int* s_cl, int* s_coff, TeamShared& sh) {
   const float4* bb = pp.original ? m.orig_vb : m.vb;
-  for (int n = threadIdx.x; n < m.totnode; n += kTeamThreads)
-    s_pass[n] = box_hits(__ldcg(&bb[2 * n]), __ldcg(&bb[2 * n + 1]), pp.loc, pp.cull_radius_sq);
+  constexpr int kBoxBatch = 2;  // node boxes loaded together
+  for (int n0 = threadIdx.x; n0 < m.totnode; n0 += kBoxBatch * kTeamThreads) {
+    float4 lo[kBoxBatch], hi[kBoxBatch];
+#pragma unroll
+    for (int j = 0; j < kBoxBatch; j++) {
+      const int n = n0 + j * kTeamThreads;
+      if (n < m.totnode) {
+        lo[j] = __ldcg(&bb[2 * n]);
+        hi[j] = __ldcg(&bb[2 * n + 1]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kBoxBatch; j++) {
+      const int n = n0 + j * kTeamThreads;
+      if (n < m.totnode) s_pass[n] = box_hits(lo[j], hi[j], pp.loc, pp.cull_radius_sq);
+    }
+  }
   __syncthreads();
   const int L = m.nleaf;
   const int seg = (L + kTeamThreads - 1) / kTeamThreads;
@@ -204,8 +212,17 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_p
   __syncthreads();
 }
 
-constexpr int kFlushTab = 256;  // ancestor boxes cached in shared memory
+constexpr int kFlushTab = 128;  // ancestors whose boxes stay in shared memory
 constexpr unsigned short kNoPos = 0xFFFFu, kClaimed = 0xFFFEu;
+
+// Shared memory of the flush: for the first kFlushTab ancestors in sorted
+// order, their new box, their first child and the boxes of those of their two
+// children that are not ancestors themselves (prefetched in one sweep).
+struct FlushSmem {
+  float4 own[2 * kFlushTab];
+  float4 kid[4 * kFlushTab];
+  int child[kFlushTab];
+};
 
 // Bottom-up flush by one CTA: touched leaf boxes from their chunk boxes, then
 // every ancestor of a touched leaf recomputed from its two children
@@ -214,7 +231,7 @@ constexpr unsigned short kNoPos = 0xFFFFu, kClaimed = 0xFFFEu;
 // UpdateBB.  s_idx holds kNoPos for every node on entry and on exit; an
 // ancestor is first claimed with kClaimed, then given its sorted position.
 __device__ void team_flush(const DevMesh& m, int ntouch, const int* s_par, unsigned short* s_idx,
-                           int* s_list, int* s_sorted, float4* s_tab, int* s_start, int* s_cur,
+                           int* s_list, int* s_sorted, FlushSmem& fs, int* s_start, int* s_cur,
                            TeamShared& sh, unsigned long long& ab) {
   const int warp = threadIdx.x >> 5;
   for (int k = warp; k < ntouch; k += kTeamThreads / 32) {
@@ -254,17 +271,32 @@ __device__ void team_flush(const DevMesh& m, int ntouch, const int* s_par, unsig
     s_idx[node] = static_cast<unsigned short>(pos);
   }
   __syncthreads();
+  const int npre = min(nm, kFlushTab);
+  for (int i = threadIdx.x; i < 2 * npre; i += kTeamThreads) {
+    const int pos = i >> 1, h = i & 1;
+    const int c = m.node_child[s_sorted[pos]];
+    if (h == 0) fs.child[pos] = c;
+    if (s_idx[c + h] == kNoPos) {
+      fs.kid[2 * i] = __ldcg(&m.vb[2 * (c + h)]);
+      fs.kid[2 * i + 1] = __ldcg(&m.vb[2 * (c + h) + 1]);
+    }
+  }
+  __syncthreads();
   for (int dd = m.max_depth; dd >= 0; dd--) {
     const int b0 = s_start[dd], b1 = s_cur[dd];
     for (int pos = b0 + threadIdx.x; pos < b1; pos += kTeamThreads) {
       const int node = s_sorted[pos];
-      const int c = m.node_child[node];
+      const bool cached = pos < kFlushTab;
+      const int c = cached ? fs.child[pos] : m.node_child[node];
       float4 box[2][2];
       for (int h = 0; h < 2; h++) {
         const int ci = s_idx[c + h];  // children are one level deeper: done
         if (ci < kFlushTab) {
-          box[h][0] = s_tab[2 * ci];
-          box[h][1] = s_tab[2 * ci + 1];
+          box[h][0] = fs.own[2 * ci];
+          box[h][1] = fs.own[2 * ci + 1];
+        } else if (ci == kNoPos && cached) {
+          box[h][0] = fs.kid[4 * pos + 2 * h];
+          box[h][1] = fs.kid[4 * pos + 2 * h + 1];
         } else {
           box[h][0] = __ldcg(&m.vb[2 * (c + h)]);
           box[h][1] = __ldcg(&m.vb[2 * (c + h) + 1]);
@@ -280,9 +312,9 @@ __device__ void team_flush(const DevMesh& m, int ntouch, const int* s_par, unsig
       mn.w = mx.w = 0.0f;
       m.vb[2 * node] = mn;
       m.vb[2 * node + 1] = mx;
-      if (pos < kFlushTab) {
-        s_tab[2 * pos] = mn;
-        s_tab[2 * pos + 1] = mx;
+      if (cached) {
+        fs.own[2 * pos] = mn;
+        fs.own[2 * pos + 1] = mx;
       }
       ab += 72u;  // two child boxes read, one box written
     }
@@ -304,22 +336,40 @@ __device__ void team_area_leaf(const DevMesh& m, const PassParams& pp, float rn2
 #pragma unroll
   for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
   l.n_no = l.n_co = 0;
-  for (int i = t; i < nv; i += kTeamThreads) {
-    const int v = leaf_vert(m, leaf, i);
-    const float4 co = __ldcg(&m.co[v]);
-    const float d2 = dist_sq(co, pp.loc);
-    if (d2 <= rn2) {
-      const float4 no = __ldcg(&m.no[v]);
-      cs_add(l.v[0], no.x);
-      cs_add(l.v[1], no.y);
-      cs_add(l.v[2], no.z);
-      l.n_no++;
+  // lane t takes elements t, t + 256, ... in order; loads of kAreaBatch of
+  // them are issued together
+  constexpr int kAreaBatch = 2;
+  for (int i0 = t; i0 < nv; i0 += kAreaBatch * kTeamThreads) {
+    int vv[kAreaBatch];
+#pragma unroll
+    for (int j = 0; j < kAreaBatch; j++) {
+      const int i = i0 + j * kTeamThreads;
+      vv[j] = i < nv ? leaf_vert(m, leaf, i) : -1;
     }
-    if (d2 <= ra2) {
-      cs_add(l.v[3], co.x);
-      cs_add(l.v[4], co.y);
-      cs_add(l.v[5], co.z);
-      l.n_co++;
+    float4 co[kAreaBatch], no[kAreaBatch];
+#pragma unroll
+    for (int j = 0; j < kAreaBatch; j++) {
+      if (vv[j] >= 0) {
+        co[j] = __ldcg(&m.co[vv[j]]);
+        no[j] = __ldcg(&m.no[vv[j]]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kAreaBatch; j++) {
+      if (vv[j] < 0) break;
+      const float d2 = dist_sq(co[j], pp.loc);
+      if (d2 <= rn2) {
+        cs_add(l.v[0], no[j].x);
+        cs_add(l.v[1], no[j].y);
+        cs_add(l.v[2], no[j].z);
+        l.n_no++;
+      }
+      if (d2 <= ra2) {
+        cs_add(l.v[3], co[j].x);
+        cs_add(l.v[4], co[j].y);
+        cs_add(l.v[5], co[j].z);
+        l.n_co++;
+      }
     }
   }
   sl[t] = l;
@@ -437,20 +487,30 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned C = cluster.num_blocks();
   const unsigned rank = cluster.block_rank();
-  const int gt = rank * kTeamThreads + threadIdx.x;
+  // Item lists are dealt to the team in warp-sized blocks, round-robin over
+  // the CTAs (block b goes to CTA b % C), so that a short list still spreads
+  // its scattered loads over every SM of the cluster.
+  const int lane = threadIdx.x & 31;
+  const int gt = 32 * ((threadIdx.x >> 5) * static_cast<int>(C) + static_cast<int>(rank)) + lane;
   const int GT = C * kTeamThreads;
   __shared__ TeamShared sh;
-  __shared__ Lane s_lanes[kTeamThreads];
+  // area lanes and flush tables are never live at the same time
+  union Scratch {
+    Lane lanes[kTeamThreads];
+    FlushSmem flush;
+  };
+  static_assert(sizeof(FlushSmem) <= sizeof(Lane) * kTeamThreads, "flush tables exceed the lanes");
+  __shared__ Scratch s_scr;
+  Lane* s_lanes = s_scr.lanes;
   __shared__ Lane s_chunks[kTeamMaxChunks];
-  __shared__ float4 s_tab[2 * kFlushTab];
   __shared__ int s_start[256], s_cur[256];
   extern __shared__ __align__(16) unsigned char dyn[];
-  int* s_par = reinterpret_cast<int*>(dyn);
+  float4* s_nbc = reinterpret_cast<float4*>(dyn);  // smooth neighbour tables
+  int* s_par = reinterpret_cast<int*>(s_nbc + kNbCache * kTeamThreads);
   int* s_cl = s_par + a.max_nodes;
   int* s_coff = s_cl + a.max_leaves + 1;
   unsigned short* s_idx = reinterpret_cast<unsigned short*>(s_coff + a.max_leaves + 2);
   unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_idx + a.max_nodes);
-  float* s_fn = reinterpret_cast<float*>(dyn + team_fn_offset(a.max_nodes, a.max_leaves));
   PhaseClock clk;
   clk.last = a.phase_ns ? global_ns() : 0ull;
 
@@ -488,7 +548,7 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
       for (int k = 0; k < 3; k++) w->hit_count[k] = 0;
       w->tag_count[0] = w->tag_count[1] = 0;
       w->touch_count[0] = w->touch_count[1] = 0;
-      if (m.type == kGrids) m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = 0;
+      if (m.type == kGrids) m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = m.grid_counts[3] = 0;
     }
     team_sync(cluster, C);
     // Leaves flagged and vertices tagged before the stroke (by per-call entry
@@ -576,8 +636,8 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
           const unsigned vbytes = (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) +
                                   (m.automask ? 4u : 0u) +
                                   ((tool == kToolInflate || (b.flag & kBrushFrontFace)) ? 12u : 0u);
-          for (int base = rank * kTeamThreads; base < total; base += GT) {
-            const int i = base + threadIdx.x;
+          for (int base = gt - lane; base < total; base += GT) {
+            const int i = base + lane;
             bool moved = false;
             if (i < total) {
               const int k = smem_find_slot(s_coff, cnt, i);
@@ -602,63 +662,100 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
           if (st > 1.0f) st = 1.0f;
           const int count = (int)(st * 4.0f);
           const float last = 4.0f * (st - (float)count * 0.25f);
-          for (int it = 0; it <= count; it++, q++) {
-            pp.iter_strength = (it != count) ? 1.0f : last;
-            pp.iteration = it;
-            int* out_list = m.hit_list[q & 1];
-            const int* in_list = m.hit_list[(q + 1) & 1];
-            int* out_cnt = &w->hit_count[q % 3];
-            const int ncand = (it == 0) ? total : __ldcg(&w->hit_count[(q + 2) % 3]);
-            // sweep: candidates are the culled vertices, then the previous hits
-            // (a vertex outside the sphere does not move, so it stays outside)
-            unsigned long long ab = 0;
-            for (int base = rank * kTeamThreads; base < ncand; base += GT) {
-              const int i = base + threadIdx.x;
-              bool moved = false;
-              if (i < ncand) {
-                int v;
-                if (it == 0) {
-                  const int k = smem_find_slot(s_coff, cnt, i);
-                  v = leaf_vert(m, s_cl[k], i - s_coff[k]);
-                } else {
-                  v = __ldcg(&in_list[i]);
-                }
-                const float4 co = __ldcg(&m.co[v]);
-                ab += 4u + 12u + (m.mask ? 4u : 0u);  // vertex id, co, mask
-                float4 out;
-                bool mv = false;
-                if (smooth_vertex(m, b, b.y, pp, v, co, out, mv)) {
-                  cg::coalesced_group g = cg::coalesced_threads();
-                  int slot = 0;
-                  if (g.thread_rank() == 0) slot = atomicAdd(out_cnt, static_cast<int>(g.size()));
-                  slot = g.shfl(slot, 0) + g.thread_rank();
-                  out_list[slot] = v;
-                  m.scratch[slot] = out;
-                  moved = (it == 0) && mv;
-                  const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
-                  // ring range and ring (id + co) reads; hit id and value written
-                  ab += (m.type == kFaces ? 8ull : 0ull) + 16ull * valence + 20ull;
-                }
+          // Jacobi sweeps over slots (smooth_slot): the first sweep gives each
+          // culled vertex inside the sphere a slot and its first value; the
+          // later ones run over the slots only; one apply writes the last
+          // values back.  Slot counters rotate over three words so the reset
+          // of the next pass's counter never meets a running pass.
+          int* slot_v = m.hit_list[0];
+          int* nslot_cnt = &w->hit_count[q % 3];
+          if (rank == 0 && threadIdx.x == 0) w->hit_count[(q + 1) % 3] = 0;
+          q++;
+          pp.iter_strength = (count != 0) ? 1.0f : last;
+          pp.iteration = 0;
+          unsigned long long ab = 0;
+          for (int base = gt - lane; base < total; base += GT) {
+            const int i = base + lane;
+            bool moved = false;
+            if (i < total) {
+              const int k = smem_find_slot(s_coff, cnt, i);
+              const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+              const float4 co = __ldcg(&m.co[v]);
+              ab += 4u + 12u + (m.mask ? 4u : 0u);  // vertex id, co, mask
+              float4 out;
+              bool mv = false;
+              if (smooth_vertex(m, b, b.y, pp, v, co, out, mv)) {
+                cg::coalesced_group g = cg::coalesced_threads();
+                int slot = 0;
+                if (g.thread_rank() == 0) slot = atomicAdd(nslot_cnt, static_cast<int>(g.size()));
+                slot = g.shfl(slot, 0) + g.thread_rank();
+                slot_v[slot] = v;
+                m.scratch[slot] = out;
+                m.slot_map[v] = slot;
+                moved = mv;
+                const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
+                // ring range and ring (id + co) reads; slot id, value and map written
+                ab += (m.type == kFaces ? 8ull : 0ull) + 16ull * valence + 24ull;
               }
-              const unsigned bal = __ballot_sync(0xffffffffu, moved);
-              if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
             }
-            team_bytes(a, kPhBrush, ab);
-            team_sync(cluster, C);
-            clk.mark(a, rank, kPhBrush);
-            const int nhit = __ldcg(out_cnt);
-            if (rank == 0 && threadIdx.x == 0) w->hit_count[(q + 1) % 3] = 0;
-            ab = 0;
-            for (int j = gt; j < nhit; j += GT) {
-              const int v = __ldcg(&out_list[j]);
-              m.co[v] = __ldcg(&m.scratch[j]);
-              if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
-              ab += 4u + 16u + 12u;  // hit id, value, co write
-            }
-            team_bytes(a, kPhApply, ab);
-            team_sync(cluster, C);
-            clk.mark(a, rank, kPhApply);
+            const unsigned bal = __ballot_sync(0xffffffffu, moved);
+            if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
           }
+          team_bytes(a, kPhBrush, ab);
+          team_sync(cluster, C);
+          clk.mark(a, rank, kPhBrush);
+          const int ns = __ldcg(nslot_cnt);
+          float4* const val[2] = {m.scratch, m.scratch2};
+          if (count > 0) {
+            // the thread's first slot keeps its vertex, value and neighbour
+            // table on chip across the sweeps; further slots reload them
+            const int s0 = gt;
+            int v0 = -1, n0 = -1;
+            float4 own = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (s0 < ns) {
+              v0 = __ldcg(&slot_v[s0]);
+              own = __ldcg(&val[0][s0]);
+              n0 = smooth_table(m, v0, s_nbc + threadIdx.x, kTeamThreads);
+            }
+            for (int it = 1; it <= count; it++) {
+              pp.iter_strength = (it != count) ? 1.0f : last;
+              pp.iteration = it;
+              const float4* src = val[(it - 1) & 1];
+              float4* dst = val[it & 1];
+              ab = 0;
+              for (int sidx = s0; sidx < ns; sidx += GT) {
+                float4 out;
+                int nring;
+                if (sidx == s0 && n0 >= 0) {
+                  out = smooth_slot_cached(m, b, pp, v0, own, n0, s_nbc + threadIdx.x, kTeamThreads, src);
+                  own = out;
+                  nring = n0;
+                } else {
+                  const int v = __ldcg(&slot_v[sidx]);
+                  out = smooth_slot(m, b, pp, v, __ldcg(&src[sidx]), src);
+                  nring = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
+                }
+                dst[sidx] = out;
+                // slot id, value and mask read, ring values read, value written
+                ab += 4ull + 16ull + (m.mask ? 4ull : 0ull) + 16ull * nring + 16ull;
+              }
+              team_bytes(a, kPhBrush, ab);
+              team_sync(cluster, C);
+              clk.mark(a, rank, kPhBrush);
+            }
+          }
+          const float4* fin = val[count & 1];
+          ab = 0;
+          for (int sidx = gt; sidx < ns; sidx += GT) {
+            const int v = __ldcg(&slot_v[sidx]);
+            m.co[v] = __ldcg(&fin[sidx]);
+            m.slot_map[v] = -1;
+            if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+            ab += 4u + 16u + 12u + 4u;  // slot id, value, co write, map reset
+          }
+          team_bytes(a, kPhApply, ab);
+          team_sync(cluster, C);
+          clk.mark(a, rank, kPhApply);
         }
       }
       // normal update for the tagged vertices, refit of the touched leaves
@@ -675,9 +772,9 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
           ab += 24ull + 16ull * used;
         }
       } else {
-        // GRIDS: faces of the touched leaves, their inner normals and seams,
-        // then the base edges and corners (positions move at the seams, so
-        // the refit below follows).
+        // GRIDS: faces of the touched leaves, the inner normals of their
+        // grids, the face seams and centres, then the base edges and corners
+        // (positions move at the seams, so the refit below follows).
         const unsigned int epoch = grid_epoch0 + static_cast<unsigned int>(d) + 1u;
         for (int k = rank; k < ntouch; k += C) {
           const int leaf = __ldcg(&m.touch_list[k]);
@@ -685,22 +782,26 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
           for (int j = p0 + threadIdx.x; j < p1; j += kTeamThreads) grid_claim_face(m, m.leaf_prims[j], epoch);
         }
         team_sync(cluster, C);
-        const int nf = __ldcg(&m.grid_counts[0]);
-        const int g1 = m.grid_size - 1;
-        for (int k = rank; k < nf; k += C) {
-          const int f = __ldcg(&m.face_list[k]);
-          grid_face_update(m, f, s_fn);
-          if (threadIdx.x == 0) {
-            const int n = m.face_ngrids[f];
-            ab += 24ull * m.grid_area * n + 112ull * g1 * n + 56ull * n;
-          }
+        const int nf = __ldcg(&m.grid_counts[0]), ng = __ldcg(&m.grid_counts[3]);
+        const long long inner = (long long)ng * m.grid_area;
+        for (long long it = gt; it < inner; it += GT) {
+          grid_inner_item(m, it);
+          ab += 24u;  // co read, normal written
+        }
+        team_sync(cluster, C);
+        const long long pairs = (long long)ng * (m.grid_size - 1);
+        for (long long it = gt; it < pairs + nf; it += GT) {
+          grid_face_seam_item(m, it, ng);
+          // co, no and mask read and written per element
+          ab += it < pairs ? 112ull : 56ull * m.face_ngrids[__ldcg(&m.face_list[it - pairs])];
         }
         team_sync(cluster, C);
         const int ne = __ldcg(&m.grid_counts[1]), nv = __ldcg(&m.grid_counts[2]);
         const long long items = (long long)ne * (2 * m.grid_size - 2) + nv;
         for (long long it = gt; it < items; it += GT) grid_seam_item(m, it, ne);
         team_sync(cluster, C);
-        if (rank == 0 && threadIdx.x == 0) m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = 0;
+        if (rank == 0 && threadIdx.x == 0)
+          m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = m.grid_counts[3] = 0;
       }
       // refit: the chunk boxes of the touched leaves, one warp per chunk
       // across the team (chunk offsets of the touched leaves in s_coff)
@@ -722,7 +823,7 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
         __syncthreads();
         const int wpc = kTeamThreads / 32;
         const unsigned idb = (m.type == kFaces ? 4u : 0u) + 12u;  // vertex id, position
-        for (int j = rank * wpc + (threadIdx.x >> 5); j < nchunk; j += C * wpc) {
+        for (int j = (threadIdx.x >> 5) * static_cast<int>(C) + static_cast<int>(rank); j < nchunk; j += C * wpc) {
           const int k = smem_find_slot(s_coff, ntouch, j);
           const int leaf = s_cl[k], c = j - s_coff[k];
           float mn[3], mx[3];
@@ -736,7 +837,7 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
       clk.mark(a, rank, kPhUpdate);
       // flush by CTA 0: touched leaf boxes, then their ancestors bottom-up
       unsigned long long fb = 0;
-      if (rank == 0) team_flush(m, ntouch, s_par, s_idx, s_cl, s_coff, s_tab, s_start, s_cur, sh, fb);
+      if (rank == 0) team_flush(m, ntouch, s_par, s_idx, s_cl, s_coff, s_scr.flush, s_start, s_cur, sh, fb);
       team_bytes(a, kPhFlush, fb);
       team_sync(cluster, C);
       clk.mark(a, rank, kPhFlush);
@@ -769,11 +870,13 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
   }
 }
 
-// Dynamic shared memory: parents, culled list and offsets, flush positions,
-// node marks, then the grid face-normal scratch (16-byte aligned,
-// team_fn_offset).
-size_t team_smem_bytes(int max_nodes, int max_leaves, int max_grid_fn) {
-  return team_fn_offset(max_nodes, max_leaves) + sizeof(float) * static_cast<size_t>(max_grid_fn) + 16;
+// Dynamic shared memory: smooth neighbour tables (float4), parents, culled
+// list and offsets (int), flush positions (ushort), node marks (byte).
+size_t team_smem_bytes(int max_nodes, int max_leaves) {
+  const size_t b = sizeof(float4) * kNbCache * kTeamThreads +
+                   sizeof(int) * (static_cast<size_t>(max_nodes) + 2 * static_cast<size_t>(max_leaves) + 3) +
+                   sizeof(unsigned short) * static_cast<size_t>(max_nodes) + static_cast<size_t>(max_nodes);
+  return (b + 15) & ~static_cast<size_t>(15);
 }
 
 int team_max_cluster() { return 16; }
@@ -786,7 +889,7 @@ cudaError_t configure_team_kernel(size_t smem) {
 }
 
 cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaStream_t s) {
-  const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves, a.max_grid_fn);
+  const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves);
   cudaError_t e = configure_team_kernel(smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
@@ -804,8 +907,8 @@ cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaS
   return cudaLaunchKernelEx(&cfg, k_team_stroke, a);
 }
 
-int team_max_active_clusters(int cluster, int max_nodes, int max_leaves, int max_grid_fn) {
-  const size_t smem = team_smem_bytes(max_nodes, max_leaves, max_grid_fn);
+int team_max_active_clusters(int cluster, int max_nodes, int max_leaves) {
+  const size_t smem = team_smem_bytes(max_nodes, max_leaves);
   if (configure_team_kernel(smem) != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(static_cast<unsigned>(cluster));

@@ -58,14 +58,13 @@ struct DevMesh {
   float* mask;      // nullable
   const float* automask;  // nullable
   // FACES topology
-  const int4* lt;    // looptri: v0, v1, v2, poly
-  const int2* poly;  // loopstart, totloop
+  const int2* poly;     // loopstart, totloop
+  const int4* poly_v4;  // corner vertices of a triangle (w = -1) or quad; x = -1 otherwise
   const int* loop_v;
   const int* vt_off;
-  const int* vt_idx;
+  const int2* vt_meta;  // per vertex, its looptris in ascending order: (poly, leaf id)
   const int* nb_off;
   const int* nb_idx;
-  const int* lt_leaf;  // looptri -> leaf id
   unsigned int* vtag;  // vert_bitmap, one word per vertex
   // PBVH
   float4* vb;  // 2 per node: (min xyz, 0), (max xyz, 0)
@@ -107,18 +106,21 @@ struct DevMesh {
   const int* bvert_off;
   const int* bvert_elems;
   int* face_list;
+  int* cgrid_list;  // grids of the claimed faces
   int* edge_list;
   int* bvert_list;
   unsigned int* face_mark;
   unsigned int* edge_mark;
   unsigned int* bvert_mark;
-  int* grid_counts;  // [0] faces, [1] edges, [2] base verts
+  int* grid_counts;  // [0] faces, [1] edges, [2] base verts, [3] grids
   // work
   Work* work;
   int* cull_list;  // nleaf
   int* cull_off;   // nleaf+1: prefix of brush-visible vertex counts over cull_list
   AreaPart* parts;  // nleaf
-  float4* scratch;  // smooth Jacobi values, totvert
+  float4* scratch;   // smooth Jacobi values, totvert
+  float4* scratch2;  // second value buffer of the slot sweeps, totvert
+  int* slot_map;     // vertex -> smooth slot of the current pass, or -1
   unsigned char* node_upd;  // totnode
   // Profiling: algorithmic bytes per kernel kind (nullptr outside profiling).
   unsigned long long* prof;
@@ -511,31 +513,47 @@ __device__ __forceinline__ bool brush_vertex(const DevMesh& m, const DevBrush& b
 }
 
 // Smooth neighbour average: FACES one-ring (CSR order) or the in-grid
-// 4-neighbourhood (x-1, x+1, y-1, y+1) for GRIDS.
-__device__ __forceinline__ float3 neighbor_average(const DevMesh& m, int v, float4 c0) {
+// 4-neighbourhood (x-1, x+1, y-1, y+1) for GRIDS.  fetch(u) gives the
+// position of neighbour u; the sum runs in ring order whatever the source.
+template <int kNbBatch, class Fetch>
+__device__ __forceinline__ float3 ring_average(const DevMesh& m, int v, float4 c0, Fetch fetch) {
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
   int n = 0;
   if (m.type == kFaces) {
+    // ring positions loaded kNbBatch at a time, summed in ring order
     const int e = m.nb_off[v + 1];
-    for (int q = m.nb_off[v]; q < e; q++) {
-      const float4 c = m.co[m.nb_idx[q]];
-      sx += c.x;
-      sy += c.y;
-      sz += c.z;
-      n++;
+    for (int base = m.nb_off[v]; base < e; base += kNbBatch) {
+      int id[kNbBatch];
+#pragma unroll
+      for (int j = 0; j < kNbBatch; j++) id[j] = (base + j < e) ? m.nb_idx[base + j] : -1;
+      float3 c[kNbBatch];
+#pragma unroll
+      for (int j = 0; j < kNbBatch; j++) c[j] = id[j] >= 0 ? fetch(id[j]) : make_float3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+      for (int j = 0; j < kNbBatch; j++) {
+        if (id[j] < 0) break;
+        sx += c[j].x;
+        sy += c[j].y;
+        sz += c[j].z;
+        n++;
+      }
     }
   } else {
     const int gs = m.grid_size, area = m.grid_area;
     const int g = v / area, r = v % area, x = r % gs, y = r / gs;
     const int nx[4] = {x - 1, x + 1, x, x};
     const int ny[4] = {y, y, y - 1, y + 1};
+    float3 c[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      c[k] = (nx[k] >= 0 && nx[k] < gs && ny[k] >= 0 && ny[k] < gs) ? fetch(g * area + ny[k] * gs + nx[k])
+                                                                   : make_float3(0.0f, 0.0f, 0.0f);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       if (nx[k] >= 0 && nx[k] < gs && ny[k] >= 0 && ny[k] < gs) {
-        const float4 c = m.co[g * area + ny[k] * gs + nx[k]];
-        sx += c.x;
-        sy += c.y;
-        sz += c.z;
+        sx += c[k].x;
+        sy += c[k].y;
+        sz += c[k].z;
         n++;
       }
     }
@@ -543,6 +561,119 @@ __device__ __forceinline__ float3 neighbor_average(const DevMesh& m, int v, floa
   if (n == 0) return make_float3(c0.x, c0.y, c0.z);
   const float inv = 1.0f / (float)n;
   return make_float3(sx * inv, sy * inv, sz * inv);
+}
+
+__device__ __forceinline__ float3 neighbor_average(const DevMesh& m, int v, float4 c0) {
+  return ring_average<8>(m, v, c0, [&](int u) { return xyz(m.co[u]); });
+}
+
+// Jacobi update of one position: co + (avg - co) * fade, w kept.
+__device__ __forceinline__ float4 smooth_step(float4 co, float3 avg, float fade) {
+  float4 out;
+  out.x = co.x + (avg.x - co.x) * fade;
+  out.y = co.y + (avg.y - co.y) * fade;
+  out.z = co.z + (avg.z - co.z) * fade;
+  out.w = co.w;
+  return out;
+}
+
+// Smooth sweeps after the first, over slots.  The first sweep gives every
+// vertex inside the sphere a slot (slot_map[v] = slot) and stores its new
+// position in the slot; sweep k reads the slot values of sweep k-1 for
+// neighbours with a slot and the unchanged positions of the others (a vertex
+// outside the sphere does not move, so it never enters later).  co is the
+// vertex's own value after sweep k-1; a vertex now outside keeps it.
+__device__ __forceinline__ float4 smooth_slot(const DevMesh& m, const DevBrush& b,
+                                              const PassParams& pp, int v, float4 co,
+                                              const float4* src) {
+  const float radius = b.radius;
+  const float d2 = dist_sq(co, pp.loc);
+  if (!(d2 <= radius * radius)) return co;
+  const float sf = strength_factor(m, b, b.y, pp, v, sqrtf(d2), radius);
+  const float fade = pp.iter_strength * sf;
+  const float3 avg = ring_average<4>(m, v, co, [&](int u) {
+    const int sl = __ldcg(&m.slot_map[u]);
+    return xyz(sl >= 0 ? __ldcg(&src[sl]) : m.co[u]);
+  });
+  return smooth_step(co, avg, fade);
+}
+
+// Neighbour table of one slot vertex for the later sweeps, kept by its thread
+// in shared memory (tab[j * stride]): xyz = the fixed position of a neighbour
+// without a slot, w = its slot (as int bits) or -1.  Returns the ring size,
+// or -1 when it exceeds kNbCache (the vertex then takes smooth_slot).
+constexpr int kNbCache = 8;
+__device__ __forceinline__ int smooth_table(const DevMesh& m, int v, float4* tab, int stride) {
+  int id[kNbCache];
+  int n = 0;
+  if (m.type == kFaces) {
+    const int q0 = m.nb_off[v], q1 = m.nb_off[v + 1];
+    if (q1 - q0 > kNbCache) return -1;
+    n = q1 - q0;
+#pragma unroll
+    for (int j = 0; j < kNbCache; j++) id[j] = j < n ? m.nb_idx[q0 + j] : -1;
+  } else {
+    const int gs = m.grid_size, area = m.grid_area;
+    const int g = v / area, r = v % area, x = r % gs, y = r / gs;
+    const int nx[4] = {x - 1, x + 1, x, x};
+    const int ny[4] = {y, y, y - 1, y + 1};
+#pragma unroll
+    for (int j = 0; j < kNbCache; j++) id[j] = -1;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (nx[k] >= 0 && nx[k] < gs && ny[k] >= 0 && ny[k] < gs) id[n++] = g * area + ny[k] * gs + nx[k];
+  }
+  int sl[kNbCache];
+#pragma unroll
+  for (int j = 0; j < kNbCache; j++) sl[j] = id[j] >= 0 ? __ldcg(&m.slot_map[id[j]]) : -1;
+#pragma unroll
+  for (int j = 0; j < kNbCache; j++) {
+    if (j >= n) break;
+    const float3 p = sl[j] < 0 ? xyz(m.co[id[j]]) : make_float3(0.0f, 0.0f, 0.0f);
+    tab[j * stride] = make_float4(p.x, p.y, p.z, __int_as_float(sl[j]));
+  }
+  return n;
+}
+
+// smooth_slot with the neighbour table of smooth_table (n entries).
+__device__ __forceinline__ float4 smooth_slot_cached(const DevMesh& m, const DevBrush& b,
+                                                     const PassParams& pp, int v, float4 co,
+                                                     int n, const float4* tab, int stride,
+                                                     const float4* src) {
+  const float radius = b.radius;
+  const float d2 = dist_sq(co, pp.loc);
+  if (!(d2 <= radius * radius)) return co;
+  const float sf = strength_factor(m, b, b.y, pp, v, sqrtf(d2), radius);
+  const float fade = pp.iter_strength * sf;
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+#pragma unroll
+  for (int h = 0; h < kNbCache; h += 4) {
+    float3 c[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (h + j < n) {
+        const float4 e = tab[(h + j) * stride];
+        const int sl = __float_as_int(e.w);
+        c[j] = sl >= 0 ? xyz(__ldcg(&src[sl])) : make_float3(e.x, e.y, e.z);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (h + j < n) {
+        sx += c[j].x;
+        sy += c[j].y;
+        sz += c[j].z;
+      }
+    }
+  }
+  float3 avg;
+  if (n == 0) {
+    avg = make_float3(co.x, co.y, co.z);
+  } else {
+    const float inv = 1.0f / (float)n;
+    avg = make_float3(sx * inv, sy * inv, sz * inv);
+  }
+  return smooth_step(co, avg, fade);
 }
 
 // One Jacobi smooth step on one vertex from the sweep-start state.  Returns
@@ -555,11 +686,7 @@ __device__ __forceinline__ bool smooth_vertex(const DevMesh& m, const DevBrush& 
   if (!(d2 <= radius * radius)) return false;
   const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
   const float fade = pp.iter_strength * sf;
-  const float3 avg = neighbor_average(m, v, co);
-  out.x = co.x + (avg.x - co.x) * fade;
-  out.y = co.y + (avg.y - co.y) * fade;
-  out.z = co.z + (avg.z - co.z) * fade;
-  out.w = co.w;
+  out = smooth_step(co, neighbor_average(m, v, co), fade);
   moved = fade != 0.0f;
   return true;
 }
@@ -568,17 +695,48 @@ __device__ __forceinline__ bool smooth_vertex(const DevMesh& m, const DevBrush& 
 // the poly normals of the vertex's looptris lying in UpdateNormals leaves,
 // ascending looptri order, then normalize_v3.  Returns the looptris used.
 __device__ __forceinline__ int vertex_normal(const DevMesh& m, int v, float4& out) {
+  // Entries are taken kNrmBatch at a time: their (poly, leaf) pairs, then the
+  // leaf flags and corner indices, then the corner positions are each loaded
+  // together; the compensated sums then run in entry order.
+  constexpr int kNrmBatch = 4;
   CSum ax = {0.0f, 0.0f}, ay = {0.0f, 0.0f}, az = {0.0f, 0.0f};
   const int e = m.vt_off[v + 1];
   int used = 0;
-  for (int q = m.vt_off[v]; q < e; q++) {
-    const int t = m.vt_idx[q];
-    if (!(__ldcg(&m.leaf_flag[m.lt_leaf[t]]) & kUpdateNormals)) continue;
-    const float3 fn = poly_normal(m, m.lt[t].w);
-    cs_add(ax, fn.x);
-    cs_add(ay, fn.y);
-    cs_add(az, fn.z);
-    used++;
+  for (int base = m.vt_off[v]; base < e; base += kNrmBatch) {
+    int2 meta[kNrmBatch];
+#pragma unroll
+    for (int j = 0; j < kNrmBatch; j++) meta[j] = (base + j < e) ? m.vt_meta[base + j] : make_int2(-1, -1);
+    bool on[kNrmBatch];
+    int4 pv[kNrmBatch];
+#pragma unroll
+    for (int j = 0; j < kNrmBatch; j++) {
+      on[j] = meta[j].x >= 0 && (__ldcg(&m.leaf_flag[meta[j].y]) & kUpdateNormals);
+      pv[j] = meta[j].x >= 0 ? m.poly_v4[meta[j].x] : make_int4(-1, -1, -1, -1);
+    }
+    float3 c[kNrmBatch][4];
+#pragma unroll
+    for (int j = 0; j < kNrmBatch; j++) {
+      const bool ld = on[j] && pv[j].x >= 0;
+      const int idx[4] = {pv[j].x, pv[j].y, pv[j].z, pv[j].w};
+#pragma unroll
+      for (int k = 0; k < 4; k++) c[j][k] = (ld && idx[k] >= 0) ? xyz(m.co[idx[k]]) : make_float3(0.0f, 0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int j = 0; j < kNrmBatch; j++) {
+      if (!on[j]) continue;
+      float3 fn;
+      if (pv[j].x < 0) {
+        fn = poly_normal(m, meta[j].x);
+      } else if (pv[j].w < 0) {
+        fn = normal_tri(c[j][0], c[j][1], c[j][2]);
+      } else {
+        fn = normal_quad(c[j][0], c[j][1], c[j][2], c[j][3]);
+      }
+      cs_add(ax, fn.x);
+      cs_add(ay, fn.y);
+      cs_add(az, fn.z);
+      used++;
+    }
   }
   float nx = ax.s + ax.e, ny = ay.s + ay.e, nz = az.s + az.e;
   normalize3(nx, ny, nz);

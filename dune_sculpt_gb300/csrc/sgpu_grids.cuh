@@ -1,12 +1,17 @@
 // PBVH_GRIDS normal update and seam stitching, per work item; shared by the
 // per-call kernels (kernels_grids.cu) and the persistent stroke kernel.
-//   grid_claim_face:   a face of a flagged leaf joins the update (once per epoch)
-//                      with its base edges and base vertices.
-//   grid_face_update:  one face by one CTA — inner quad normals and per-element
-//                      averages of its grids (subdiv_ccg.c:670-740), then the
-//                      face-internal seams and the shared centre (:951-984).
-//   grid_seam_item:    one boundary element index of a base edge (:1010-1048)
-//                      or one base-vertex corner (:1081-1104).
+//   grid_claim_face:     a face of a flagged leaf joins the update (once per
+//                        epoch) with its grids, base edges and base vertices.
+//   grid_element_normal: one element of a claimed grid — the mean of the
+//                        normals of the quads around it (subdiv_ccg.c:670-740).
+//   grid_face_seam_item: one face-internal seam pair or one face centre
+//                        (:951-984), after every inner normal is done.
+//   grid_seam_item:      one boundary element index of a base edge
+//                        (:1010-1048) or one base-vertex corner (:1081-1104).
+// The three element passes only depend on one another in that order: inner
+// normals read positions of their own grid, seams and centres touch disjoint
+// elements, and the base edges and corners come last, as the reference runs
+// them after every face.
 #pragma once
 
 #include "sgpu_device.cuh"
@@ -22,6 +27,8 @@ __device__ __forceinline__ void grid_claim_face(const DevMesh& m, int grid, unsi
   if (!grid_claim(m.face_mark, f, epoch)) return;
   m.face_list[atomicAdd(&m.grid_counts[0], 1)] = f;
   const int s = m.face_start[f], n = m.face_ngrids[f];
+  const int gb = atomicAdd(&m.grid_counts[3], n);
+  for (int c = 0; c < n; c++) m.cgrid_list[gb + c] = s + c;
   for (int c = 0; c < n; c++) {
     const int e = m.face_edges[s + c];
     const int v = m.face_verts[s + c];
@@ -79,66 +86,81 @@ __device__ __forceinline__ void grid_average_set(const DevMesh& m, int n, ElemAt
   }
 }
 
-// One face, the whole CTA; fn: shared memory for 3*(gs-1)^2 floats.
-__device__ inline void grid_face_update(const DevMesh& m, int f, float* fn) {
+// Normal of element (x, y) of the grid starting at element base: the mean of
+// the normals of the quads around it, added in the order of
+// subdiv_ccg.c:707-737.  Quad (qx, qy) has corners (qx, qy+1), (qx+1, qy+1),
+// (qx+1, qy), (qx, qy); its normal is the same normal_quad value whichever
+// element evaluates it.
+__device__ __forceinline__ float4 grid_element_normal(const DevMesh& m, int base, int x, int y) {
+  const int gs = m.grid_size, g1 = gs - 1;
+  float3 p[3][3];  // p[dy + 1][dx + 1] = position of (x + dx, y + dy)
+#pragma unroll
+  for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+      const int xx = x + dx, yy = y + dy;
+      p[dy + 1][dx + 1] = (xx >= 0 && xx < gs && yy >= 0 && yy < gs)
+                              ? xyz(__ldcg(&m.co[base + yy * gs + xx]))
+                              : make_float3(0.0f, 0.0f, 0.0f);
+    }
+  // quad with lower corner (x + ox, y + oy), ox, oy in {-1, 0}
+  auto quad = [&](int ox, int oy) {
+    return normal_quad(p[oy + 2][ox + 1], p[oy + 2][ox + 2], p[oy + 1][ox + 2], p[oy + 1][ox + 1]);
+  };
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  int counter = 0;
+  if (x < g1 && y < g1) {
+    const float3 q = quad(0, 0);
+    ax += q.x, ay += q.y, az += q.z;
+    counter++;
+  }
+  if (x >= 1) {
+    if (y < g1) {
+      const float3 q = quad(-1, 0);
+      ax += q.x, ay += q.y, az += q.z;
+      counter++;
+    }
+    if (y >= 1) {
+      const float3 q = quad(-1, -1);
+      ax += q.x, ay += q.y, az += q.z;
+      counter++;
+    }
+  }
+  if (y >= 1 && x < g1) {
+    const float3 q = quad(0, -1);
+    ax += q.x, ay += q.y, az += q.z;
+    counter++;
+  }
+  const float inv = 1.0f / (float)counter;
+  return make_float4(ax * inv, ay * inv, az * inv, 0.0f);
+}
+
+// Inner-normal item it < ng * area: element it % area of claimed grid it / area.
+__device__ __forceinline__ void grid_inner_item(const DevMesh& m, long long it) {
+  const int area = m.grid_area, gs = m.grid_size;
+  const int g = __ldcg(&m.cgrid_list[it / area]);
+  const int e = static_cast<int>(it % area);
+  m.no[g * area + e] = grid_element_normal(m, g * area, e % gs, e / gs);
+}
+
+// Face-seam item: it < ng * (gs-1) pairs element (i, 0) of the previous grid
+// of the face with (0, i) of the claimed grid, i = 1 + it % (gs-1); the rest
+// are face centres, element (0, 0) of every grid of the face.
+__device__ __forceinline__ void grid_face_seam_item(const DevMesh& m, long long it, int ng) {
   const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area;
-  const int start = m.face_start[f], n = m.face_ngrids[f];
-  for (int c = 0; c < n; c++) {
-    const int base = (start + c) * area;
-    for (int q = threadIdx.x; q < g1 * g1; q += blockDim.x) {
-      const int x = q % g1, y = q / g1;
-      const float3 nq = normal_quad(xyz(__ldcg(&m.co[base + (y + 1) * gs + x])),
-                                    xyz(__ldcg(&m.co[base + (y + 1) * gs + x + 1])),
-                                    xyz(__ldcg(&m.co[base + y * gs + x + 1])),
-                                    xyz(__ldcg(&m.co[base + y * gs + x])));
-      fn[3 * q] = nq.x;
-      fn[3 * q + 1] = nq.y;
-      fn[3 * q + 2] = nq.z;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < area; e += blockDim.x) {
-      const int x = e % gs, y = e / gs;
-      float ax = 0.0f, ay = 0.0f, az = 0.0f;
-      int counter = 0;
-      int q;
-      if (x < g1 && y < g1) {
-        q = y * g1 + x;
-        ax += fn[3 * q], ay += fn[3 * q + 1], az += fn[3 * q + 2];
-        counter++;
-      }
-      if (x >= 1) {
-        if (y < g1) {
-          q = y * g1 + (x - 1);
-          ax += fn[3 * q], ay += fn[3 * q + 1], az += fn[3 * q + 2];
-          counter++;
-        }
-        if (y >= 1) {
-          q = (y - 1) * g1 + (x - 1);
-          ax += fn[3 * q], ay += fn[3 * q + 1], az += fn[3 * q + 2];
-          counter++;
-        }
-      }
-      if (y >= 1 && x < g1) {
-        q = (y - 1) * g1 + x;
-        ax += fn[3 * q], ay += fn[3 * q + 1], az += fn[3 * q + 2];
-        counter++;
-      }
-      const float inv = 1.0f / (float)counter;
-      m.no[base + e] = make_float4(ax * inv, ay * inv, az * inv, 0.0f);
-    }
-    __syncthreads();
-  }
-  // seams between consecutive grids: prev grid (i, 0) with grid (0, i), i >= 1
-  for (int w = threadIdx.x; w < n * g1; w += blockDim.x) {
-    const int c = w / g1, i = 1 + w % g1;
-    const int g = start + c;
-    const int prev = start + (c + n - 1) % n;
+  const long long pairs = (long long)ng * g1;
+  if (it < pairs) {
+    const int g = __ldcg(&m.cgrid_list[it / g1]);
+    const int i = 1 + static_cast<int>(it % g1);
+    const int f = m.grid_face[g];
+    const int s = m.face_start[f], n = m.face_ngrids[f];
+    const int prev = s + (g - s + n - 1) % n;
     grid_avg_pair(m, prev * area + i, g * area + i * gs);
+  } else {
+    const int f = __ldcg(&m.face_list[it - pairs]);
+    const int s = m.face_start[f], n = m.face_ngrids[f];
+    grid_average_set(m, n, [&](int c) { return (s + c) * area; });
   }
-  __syncthreads();
-  if (threadIdx.x == 0)
-    grid_average_set(m, n, [&](int c) { return (start + c) * area; });
-  __syncthreads();
 }
 
 // One seam item: it < ne*(2gs-2) is (edge, boundary index 1..2gs-2), the rest

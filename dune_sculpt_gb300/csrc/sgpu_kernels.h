@@ -21,9 +21,11 @@ cudaError_t launch_smooth_apply(const DevMesh& m, cudaStream_t s);
 // also serve GRIDS meshes.
 cudaError_t launch_update_faces(const DevMesh& m, int do_normals, int bounds_flag,
                                 cudaStream_t s);
-// GRIDS normal update with seam stitching: gather, per-face, seams.
+// GRIDS normal update with seam stitching: gather, inner normals, face
+// seams and centres, base edges and corners.
 cudaError_t launch_grid_gather(const DevMesh& m, cudaStream_t s);
-cudaError_t launch_grid_faces(const DevMesh& m, cudaStream_t s);
+cudaError_t launch_grid_inner(const DevMesh& m, cudaStream_t s);
+cudaError_t launch_grid_face_seams(const DevMesh& m, cudaStream_t s);
 cudaError_t launch_grid_seams(const DevMesh& m, cudaStream_t s);
 // Writes a buffer larger than L2.
 cudaError_t launch_l2_flush(void* buf, size_t bytes, cudaStream_t s);

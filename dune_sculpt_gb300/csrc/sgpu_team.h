@@ -26,7 +26,6 @@ struct TeamArgs {
   int njobs;
   int* next_job;  // job counter, zero at launch
   int max_nodes, max_leaves;  // shared-memory sizing over the meshes
-  int max_grid_fn;            // floats of the grid face-normal scratch (GRIDS meshes)
   // profiling (nullable): algorithmic bytes and nanoseconds per phase
   unsigned long long* prof_bytes;  // kTeamPhases entries
   unsigned long long* phase_ns;    // kTeamPhases entries
@@ -44,9 +43,9 @@ enum TeamPhase {
   kTeamPhases
 };
 
-size_t team_smem_bytes(int max_nodes, int max_leaves, int max_grid_fn);
+size_t team_smem_bytes(int max_nodes, int max_leaves);
 int team_max_cluster();
-int team_max_active_clusters(int cluster, int max_nodes, int max_leaves, int max_grid_fn);
+int team_max_active_clusters(int cluster, int max_nodes, int max_leaves);
 cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaStream_t s);
 
 }  // namespace sgpu
