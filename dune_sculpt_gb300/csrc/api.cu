@@ -62,6 +62,11 @@ struct sgpu_mesh {
   std::vector<void*> allocs;
   int* d_nodes_tmp = nullptr;
   bool has_mask = false;
+  // FACES device vertex order (see sgpu_mesh_create_faces): caller index ->
+  // device index and back; empty / null for GRIDS (element order kept).
+  std::vector<int> o2n;
+  const int* d_o2n = nullptr;
+  const int* d_n2o = nullptr;
   // stroke graph cache
   cudaGraphExec_t gexec = nullptr;
   std::vector<unsigned char> gkey;
@@ -126,6 +131,15 @@ struct sgpu_mesh {
       if (e != cudaSuccess) return cuda_fail(e, "upload");
     }
     *out = p;
+    return SGPU_OK;
+  }
+  template <class T>
+  int upload_to(T* dst, const std::vector<T>& v) {
+    cudaError_t e = cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                    stream);
+    if (e != cudaSuccess) return cuda_fail(e, "upload");
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
     return SGPU_OK;
   }
   template <class T>
@@ -199,7 +213,9 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->upload(&d.node_parent, h.parent))) return rc;
   if ((rc = m->upload(&d.node_leaf, h.node_leaf))) return rc;
   if ((rc = m->upload(&d.leaf_node, h.leaf_nodes))) return rc;
-  std::vector<int> vert_off(L + 1, 0), uniq(L, 0), verts, prim_off(L + 1, 0), prims, lflag(L);
+  std::vector<int> vert_off(L + 1, 0), uniq(L, 0), ubase(L, 0), verts, prim_off(L + 1, 0), prims,
+      lflag(L);
+  int unext = 0;
   for (int k = 0; k < L; k++) {
     const int node = h.leaf_nodes[k];
     lflag[k] = h.flag[node];
@@ -208,12 +224,21 @@ int upload_pbvh(sgpu_mesh* m) {
     if (h.type == kFaces) {
       const int tot = h.uniq[node] + h.face_verts_n[node];
       uniq[k] = h.uniq[node];
+      ubase[k] = unext;
       vert_off[k + 1] = vert_off[k] + tot;
-      for (int i = 0; i < tot; i++) verts.push_back(h.vert_indices[h.vert_off[node] + i]);
+      for (int i = 0; i < tot; i++) {
+        const int v = m->o2n[h.vert_indices[h.vert_off[node] + i]];
+        // the unique vertices of the leaf are consecutive in device order
+        if (i < h.uniq[node] && v != unext + i)
+          return fail(SGPU_ERR_INVALID_ARG, "leaf %d owns vertex %d twice", k, v);
+        verts.push_back(v);
+      }
+      unext += h.uniq[node];
     }
   }
   if ((rc = m->upload(&d.leaf_vert_off, vert_off))) return rc;
   if ((rc = m->upload(&d.leaf_uniq, uniq))) return rc;
+  if ((rc = m->upload(&d.leaf_ubase, ubase))) return rc;
   if ((rc = m->upload(&d.leaf_verts, verts))) return rc;
   if ((rc = m->upload(&d.leaf_prim_off, prim_off))) return rc;
   if ((rc = m->upload(&d.leaf_prims, prims))) return rc;
@@ -238,7 +263,10 @@ int upload_pbvh(sgpu_mesh* m) {
     if ((rc = m->alloc(&d.chunk_box, 2 * static_cast<size_t>(choff[L]) + 2))) return rc;
     m->nchunks = choff[L];
   }
-  if ((rc = m->alloc(&d.hit_list[0], static_cast<size_t>(h.totvert)))) return rc;
+  // smooth slot arrays: the persistent kernel's per-CTA slot ranges may end
+  // up to 32 entries per CTA (at most 16 CTAs) past the vertex count
+  const size_t nslot = static_cast<size_t>(h.totvert) + 32 * 16;
+  if ((rc = m->alloc(&d.hit_list[0], nslot))) return rc;
   if ((rc = m->alloc(&d.hit_list[1], static_cast<size_t>(h.totvert)))) return rc;
   if ((rc = m->alloc(&d.tag_list, static_cast<size_t>(h.totvert)))) return rc;
   if ((rc = m->alloc(&d.touch_list, L + 1))) return rc;
@@ -246,11 +274,13 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->alloc(&d.cull_list, L + 1))) return rc;
   if ((rc = m->alloc(&d.cull_off, L + 2))) return rc;
   if ((rc = m->alloc(&d.parts, L + 1))) return rc;
-  if ((rc = m->alloc(&d.scratch, static_cast<size_t>(h.totvert)))) return rc;
-  if ((rc = m->alloc(&d.scratch2, static_cast<size_t>(h.totvert)))) return rc;
-  if ((rc = m->alloc(&d.slot_map, static_cast<size_t>(h.totvert)))) return rc;
-  CK(cudaMemsetAsync(d.slot_map, 0xFF, sizeof(int) * static_cast<size_t>(h.totvert), m->stream),
-     "slot map init");
+  if ((rc = m->alloc(&d.scratch, nslot))) return rc;
+  if ((rc = m->alloc(&d.scratch2, nslot))) return rc;
+  for (int k = 0; k < 2; k++) {
+    if ((rc = m->alloc(&d.slot_map[k], static_cast<size_t>(h.totvert)))) return rc;
+    CK(cudaMemsetAsync(d.slot_map[k], 0xFF, sizeof(int) * static_cast<size_t>(h.totvert), m->stream),
+       "slot map init");
+  }
   if ((rc = m->alloc(&d.node_upd, N))) return rc;
   if ((rc = m->alloc(&m->d_nodes_tmp, L + 1))) return rc;
   if (N > cull_smem_limit())
@@ -559,56 +589,108 @@ int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPol
     return code;
   };
   if ((rc = create_common(m))) return bail(rc);
+  // Device vertex order: the unique vertices of each leaf, leaf by leaf in
+  // left-first order and in the order of the leaf's vertex list, then the
+  // vertices no leaf owns.  A leaf's brush-visible vertices are then one
+  // contiguous range, and one-ring and face neighbours mostly share cache
+  // lines.  Every order the results depend on (leaf vertex lists, one-rings,
+  // vertex looptri lists) is kept as an explicit list, so the relabelling
+  // does not change any result; entry points taking or returning per-vertex
+  // arrays convert at the boundary.
+  std::vector<int> n2o(totvert);
+  {
+    std::vector<int>& o2n = m->o2n;
+    o2n.assign(totvert, -1);
+    int c = 0;
+    for (int node : h.leaf_nodes)
+      for (int i = 0; i < h.uniq[node]; i++) {
+        const int v = h.vert_indices[h.vert_off[node] + i];
+        if (o2n[v] < 0) {
+          o2n[v] = c;
+          n2o[c++] = v;
+        }
+      }
+    for (int v = 0; v < totvert; v++)
+      if (o2n[v] < 0) {
+        o2n[v] = c;
+        n2o[c++] = v;
+      }
+    if ((rc = m->upload(&m->d_o2n, o2n))) return bail(rc);
+    if ((rc = m->upload(&m->d_n2o, n2o))) return bail(rc);
+  }
+  const std::vector<int>& o2n = m->o2n;
   if ((rc = m->alloc(&d.co, totvert))) return bail(rc);
   if ((rc = m->alloc(&d.no, totvert))) return bail(rc);
   static_assert(sizeof(SGPU_MVert) == sizeof(float4), "MVert is 16 bytes");
-  CK(cudaMemcpyAsync(d.co, verts, sizeof(float4) * totvert, cudaMemcpyHostToDevice, m->stream),
-     "upload verts");
-  if (vert_normals) {
-    CK(cudaMemcpy2DAsync(d.no, sizeof(float4), vert_normals, 3 * sizeof(float), 3 * sizeof(float),
-                         totvert, cudaMemcpyHostToDevice, m->stream),
-       "upload normals");
+  {
+    std::vector<float4> co4(totvert);
+    for (int n = 0; n < totvert; n++) std::memcpy(&co4[n], &verts[n2o[n]], sizeof(float4));
+    CK(cudaMemcpyAsync(d.co, co4.data(), sizeof(float4) * totvert, cudaMemcpyHostToDevice,
+                       m->stream),
+       "upload verts");
+    if (vert_normals) {
+      for (int n = 0; n < totvert; n++) {
+        const float* q = vert_normals + 3 * static_cast<size_t>(n2o[n]);
+        co4[n] = make_float4(q[0], q[1], q[2], 0.0f);
+      }
+      CK(cudaMemcpyAsync(d.no, co4.data(), sizeof(float4) * totvert, cudaMemcpyHostToDevice,
+                         m->stream),
+         "upload normals");
+    }
+    CK(cudaStreamSynchronize(m->stream), "cudaStreamSynchronize");
   }
+  std::vector<float> tmp1(totvert);
   if (mask) {
     float* dm = nullptr;
     if ((rc = m->alloc(&dm, totvert))) return bail(rc);
-    CK(cudaMemcpyAsync(dm, mask, sizeof(float) * totvert, cudaMemcpyHostToDevice, m->stream),
-       "upload mask");
+    for (int n = 0; n < totvert; n++) tmp1[n] = mask[n2o[n]];
+    if ((rc = m->upload_to(dm, tmp1))) return bail(rc);
     d.mask = dm;
     m->has_mask = true;
   }
   if (automask) {
     float* da = nullptr;
     if ((rc = m->alloc(&da, totvert))) return bail(rc);
-    CK(cudaMemcpyAsync(da, automask, sizeof(float) * totvert, cudaMemcpyHostToDevice, m->stream),
-       "upload automask");
+    for (int n = 0; n < totvert; n++) tmp1[n] = automask[n2o[n]];
+    if ((rc = m->upload_to(da, tmp1))) return bail(rc);
     d.automask = da;
   }
+  std::vector<int> loop_n(totloop);
+  for (int l = 0; l < totloop; l++) loop_n[l] = o2n[h.loop_v[l]];
   std::vector<int2> pl(totpoly);
   std::vector<int4> pv(totpoly);
   for (int p = 0; p < totpoly; p++) {
     const int ls = h.poly_loopstart[p], tl = h.poly_totloop[p];
     pl[p] = make_int2(ls, tl);
     if (tl == 3) {
-      pv[p] = make_int4(h.loop_v[ls], h.loop_v[ls + 1], h.loop_v[ls + 2], -1);
+      pv[p] = make_int4(loop_n[ls], loop_n[ls + 1], loop_n[ls + 2], -1);
     } else if (tl == 4) {
-      pv[p] = make_int4(h.loop_v[ls], h.loop_v[ls + 1], h.loop_v[ls + 2], h.loop_v[ls + 3]);
+      pv[p] = make_int4(loop_n[ls], loop_n[ls + 1], loop_n[ls + 2], loop_n[ls + 3]);
     } else {
       pv[p] = make_int4(-1, -1, -1, -1);
     }
   }
+  // per-vertex lists in device order: rows moved, one-ring ids relabelled
+  std::vector<int> vt_off(totvert + 1, 0), nb_off(totvert + 1, 0);
   std::vector<int2> vt_meta(h.vt_idx.size());
-  for (size_t q = 0; q < h.vt_idx.size(); q++) {
-    const int t = h.vt_idx[q];
-    vt_meta[q] = make_int2(h.lt_poly[t], h.lt_leaf[t]);
+  std::vector<int> nb_idx(h.nb_idx.size());
+  for (int n = 0; n < totvert; n++) {
+    const int v = n2o[n];
+    vt_off[n + 1] = vt_off[n] + (h.vt_off[v + 1] - h.vt_off[v]);
+    for (int q = h.vt_off[v], o = vt_off[n]; q < h.vt_off[v + 1]; q++, o++) {
+      const int t = h.vt_idx[q];
+      vt_meta[o] = make_int2(h.lt_poly[t], h.lt_leaf[t]);
+    }
+    nb_off[n + 1] = nb_off[n] + (h.nb_off[v + 1] - h.nb_off[v]);
+    for (int q = h.nb_off[v], o = nb_off[n]; q < h.nb_off[v + 1]; q++, o++) nb_idx[o] = o2n[h.nb_idx[q]];
   }
   if ((rc = m->upload(&d.poly, pl))) return bail(rc);
   if ((rc = m->upload(&d.poly_v4, pv))) return bail(rc);
-  if ((rc = m->upload(&d.loop_v, h.loop_v))) return bail(rc);
-  if ((rc = m->upload(&d.vt_off, h.vt_off))) return bail(rc);
+  if ((rc = m->upload(&d.loop_v, loop_n))) return bail(rc);
+  if ((rc = m->upload(&d.vt_off, vt_off))) return bail(rc);
   if ((rc = m->upload(&d.vt_meta, vt_meta))) return bail(rc);
-  if ((rc = m->upload(&d.nb_off, h.nb_off))) return bail(rc);
-  if ((rc = m->upload(&d.nb_idx, h.nb_idx))) return bail(rc);
+  if ((rc = m->upload(&d.nb_off, nb_off))) return bail(rc);
+  if ((rc = m->upload(&d.nb_idx, nb_idx))) return bail(rc);
   if ((rc = m->alloc(&d.vtag, totvert))) return bail(rc);
   if ((rc = upload_pbvh(m))) return bail(rc);
   if (!vert_normals) {
@@ -1042,17 +1124,21 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
   }
   DevMesh& d = mesh->dev;
   CK(cudaEventRecord(mesh->ev_h0, mesh->stream), "event");
-  CK(cudaMemcpyAsync(d.co, verts_in, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
+  // host buffers in the caller's vertex order, converted on the device
+  CK(cudaMemcpyAsync(d.scratch, verts_in, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
                      mesh->stream),
      "upload verts");
-  if (vert_normals_in)
-    CK(cudaMemcpy2DAsync(d.no, sizeof(float4), vert_normals_in, 3 * sizeof(float),
+  CK(launch_gather_f4(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
+  if (vert_normals_in) {
+    CK(cudaMemcpy2DAsync(d.scratch2, sizeof(float4), vert_normals_in, 3 * sizeof(float),
                          3 * sizeof(float), d.totvert, cudaMemcpyHostToDevice, mesh->stream),
        "upload normals");
+    CK(launch_gather_xyz(d.no, d.scratch2, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
+  }
   // New positions: every leaf box is refit and flushed before the stroke.
   CK(launch_mark_all(d, kUpdateBB | kUpdateOriginalBB, mesh->stream), "mark kernel");
   CK(launch_update_faces(d, 0, kUpdateBB | kUpdateOriginalBB, mesh->stream), "bounds kernel");
-  int launches = 2;
+  int launches = 3 + (vert_normals_in ? 1 : 0);  // gathers, mark, bounds
   SGPU_StrokeStats inner;
   std::memset(&inner, 0, sizeof(inner));
   if (mode == SGPU_STROKE_TEAM) {
@@ -1066,7 +1152,9 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
   } else {
     if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, mode, &launches))) return rc;
   }
-  CK(cudaMemcpyAsync(verts_out, d.co, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
+  CK(launch_gather_f4(d.scratch, d.co, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
+  launches += 1;
+  CK(cudaMemcpyAsync(verts_out, d.scratch, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
                      mesh->stream),
      "download verts");
   CK(cudaEventRecord(mesh->ev_h1, mesh->stream), "event");
@@ -1301,7 +1389,9 @@ int sgpu_get_verts(sgpu_mesh* mesh, SGPU_MVert* out) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   if (mesh->dev.type != kFaces) return fail(SGPU_ERR_INVALID_ARG, "not a FACES mesh");
-  CK(cudaMemcpyAsync(out, mesh->dev.co, sizeof(float4) * mesh->dev.totvert, cudaMemcpyDeviceToHost,
+  const DevMesh& d = mesh->dev;
+  CK(launch_gather_f4(d.scratch, d.co, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
+  CK(cudaMemcpyAsync(out, d.scratch, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
                      mesh->stream),
      "download verts");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
@@ -1312,9 +1402,11 @@ int sgpu_set_verts(sgpu_mesh* mesh, const SGPU_MVert* verts) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   if (mesh->dev.type != kFaces) return fail(SGPU_ERR_INVALID_ARG, "not a FACES mesh");
-  CK(cudaMemcpyAsync(mesh->dev.co, verts, sizeof(float4) * mesh->dev.totvert,
-                     cudaMemcpyHostToDevice, mesh->stream),
+  const DevMesh& d = mesh->dev;
+  CK(cudaMemcpyAsync(d.scratch, verts, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
+                     mesh->stream),
      "upload verts");
+  CK(launch_gather_f4(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
   CK(launch_chunk_boxes_all(mesh->dev, mesh->nchunks, mesh->stream), "chunk box kernel");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1323,8 +1415,14 @@ int sgpu_set_verts(sgpu_mesh* mesh, const SGPU_MVert* verts) {
 int sgpu_get_positions(sgpu_mesh* mesh, float* out_xyz) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
-  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), mesh->dev.co, sizeof(float4), 3 * sizeof(float),
-                       mesh->dev.totvert, cudaMemcpyDeviceToHost, mesh->stream),
+  const DevMesh& d = mesh->dev;
+  const float4* src = d.co;
+  if (mesh->d_o2n) {
+    CK(launch_gather_f4(d.scratch, d.co, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
+    src = d.scratch;
+  }
+  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), src, sizeof(float4), 3 * sizeof(float),
+                       d.totvert, cudaMemcpyDeviceToHost, mesh->stream),
      "download positions");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1333,9 +1431,13 @@ int sgpu_get_positions(sgpu_mesh* mesh, float* out_xyz) {
 int sgpu_set_positions(sgpu_mesh* mesh, const float* xyz) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
-  CK(cudaMemcpy2DAsync(mesh->dev.co, sizeof(float4), xyz, 3 * sizeof(float), 3 * sizeof(float),
-                       mesh->dev.totvert, cudaMemcpyHostToDevice, mesh->stream),
+  const DevMesh& d = mesh->dev;
+  float4* dst = mesh->d_n2o ? d.scratch : d.co;
+  CK(cudaMemcpy2DAsync(dst, sizeof(float4), xyz, 3 * sizeof(float), 3 * sizeof(float), d.totvert,
+                       cudaMemcpyHostToDevice, mesh->stream),
      "upload positions");
+  if (mesh->d_n2o)
+    CK(launch_gather_xyz(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
   CK(launch_chunk_boxes_all(mesh->dev, mesh->nchunks, mesh->stream), "chunk box kernel");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1344,8 +1446,14 @@ int sgpu_set_positions(sgpu_mesh* mesh, const float* xyz) {
 int sgpu_get_normals(sgpu_mesh* mesh, float* out_xyz) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
-  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), mesh->dev.no, sizeof(float4), 3 * sizeof(float),
-                       mesh->dev.totvert, cudaMemcpyDeviceToHost, mesh->stream),
+  const DevMesh& d = mesh->dev;
+  const float4* src = d.no;
+  if (mesh->d_o2n) {
+    CK(launch_gather_f4(d.scratch, d.no, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
+    src = d.scratch;
+  }
+  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), src, sizeof(float4), 3 * sizeof(float),
+                       d.totvert, cudaMemcpyDeviceToHost, mesh->stream),
      "download normals");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1355,8 +1463,14 @@ int sgpu_get_mask(sgpu_mesh* mesh, float* out) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   if (!mesh->dev.mask) return fail(SGPU_ERR_INVALID_ARG, "mesh has no mask");
-  CK(cudaMemcpyAsync(out, mesh->dev.mask, sizeof(float) * mesh->dev.totvert,
-                     cudaMemcpyDeviceToHost, mesh->stream),
+  const DevMesh& d = mesh->dev;
+  const float* src = d.mask;
+  if (mesh->d_o2n) {
+    float* tmp = reinterpret_cast<float*>(d.scratch);
+    CK(launch_gather_f1(tmp, d.mask, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
+    src = tmp;
+  }
+  CK(cudaMemcpyAsync(out, src, sizeof(float) * d.totvert, cudaMemcpyDeviceToHost, mesh->stream),
      "download mask");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1540,8 +1654,7 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.max_leaves = max_leaves;
   a.prof_bytes = g_team_prof_bytes;
   a.phase_ns = g_team_phase_ns;
-  const int nteams = std::min(n, nteams_max);
-  CK(launch_team_stroke(a, cluster, nteams, s), "persistent stroke kernel");
+  CK(launch_team_stroke(a, cluster, s), "persistent stroke kernel");
   CK(cudaEventRecord(m0->ev1, s), "event");
   std::vector<unsigned long long> disp(n, 0);
   for (int i = 0; i < n; i++)

@@ -634,6 +634,41 @@ cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Conversions between a caller's vertex order and the device order:
+// out[i] = in[idx[i]] (whole float4, one float, or xyz with out.w kept).
+__global__ void k_gather_f4(float4* out, const float4* in, const int* idx, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = in[idx[i]];
+}
+__global__ void k_gather_f1(float* out, const float* in, const int* idx, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = in[idx[i]];
+}
+__global__ void k_gather_xyz(float4* out, const float4* in, const int* idx, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 a = in[idx[i]];
+    const float w = out[i].w;
+    out[i] = make_float4(a.x, a.y, a.z, w);
+  }
+}
+
+static int gather_grid(int n) {
+  const int g = (n + kThreads - 1) / kThreads;
+  const int cap = 4 * work_grid();
+  return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
+cudaError_t launch_gather_f4(float4* out, const float4* in, const int* idx, int n, cudaStream_t s) {
+  k_gather_f4<<<gather_grid(n), kThreads, 0, s>>>(out, in, idx, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_gather_f1(float* out, const float* in, const int* idx, int n, cudaStream_t s) {
+  k_gather_f1<<<gather_grid(n), kThreads, 0, s>>>(out, in, idx, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_gather_xyz(float4* out, const float4* in, const int* idx, int n, cudaStream_t s) {
+  k_gather_xyz<<<gather_grid(n), kThreads, 0, s>>>(out, in, idx, n);
+  return cudaGetLastError();
+}
+
 int cull_smem_limit() { return 200 * 1024; }
 
 void configure_kernels() {

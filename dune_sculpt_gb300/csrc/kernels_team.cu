@@ -14,6 +14,7 @@
 // The arithmetic is the same device code as the per-call kernels
 // (sgpu_device.cuh), so results are bit-identical to them and to the FP32
 // restatement of the reference.
+#include <algorithm>
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -35,6 +36,9 @@ struct TeamShared {
   int cnt, total;
   int scan[32];
   unsigned long long scan64[32];
+  int nh;                  // smooth hits of this CTA in the current pass
+  int hv[kTeamThreads];    // their vertices and positions (first kTeamThreads)
+  float4 hco[kTeamThreads];
   float area[6];
   int nmark;
 };
@@ -483,7 +487,10 @@ struct PhaseClock {
   }
 };
 
-__global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
+// Two builds of the kernel: one CTA per SM with the full register file (the
+// fastest single strokes), or two CTAs per SM (twice the teams for batches).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamArgs a) {
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned C = cluster.num_blocks();
   const unsigned rank = cluster.block_rank();
@@ -662,100 +669,139 @@ __global__ void __launch_bounds__(kTeamThreads, 2) k_team_stroke(TeamArgs a) {
           if (st > 1.0f) st = 1.0f;
           const int count = (int)(st * 4.0f);
           const float last = 4.0f * (st - (float)count * 0.25f);
-          // Jacobi sweeps over slots (smooth_slot): the first sweep gives each
-          // culled vertex inside the sphere a slot and its first value; the
-          // later ones run over the slots only; one apply writes the last
-          // values back.  Slot counters rotate over three words so the reset
-          // of the next pass's counter never meets a running pass.
-          int* slot_v = m.hit_list[0];
-          int* nslot_cnt = &w->hit_count[q % 3];
-          if (rank == 0 && threadIdx.x == 0) w->hit_count[(q + 1) % 3] = 0;
+          // Jacobi sweeps over slots.  CTA r gives its hits the slots
+          // [r * R, r * R + nh) (R bounds its share of the candidates), so no
+          // slot counter is shared.  The thread that runs a hit's first sweep
+          // keeps it for the later ones; its first hit keeps vertex, value and
+          // ring table on chip.  The last sweep writes the positions.  The two
+          // slot maps alternate by pass, so a pass clears its entries while
+          // the next one fills the other map.
+          int* const smap = m.slot_map[q & 1];
           q++;
+          int* const slot_v = m.hit_list[0];
+          float4* const val[2] = {m.scratch, m.scratch2};
+          const int R = 32 * ((total + 32 * static_cast<int>(C) - 1) / (32 * static_cast<int>(C)));
+          const int sbase = static_cast<int>(rank) * R;
+          if (threadIdx.x == 0) sh.nh = 0;
+          __syncthreads();
+          // first sweep, stage 1: distance test of this CTA's candidates
           pp.iter_strength = (count != 0) ? 1.0f : last;
           pp.iteration = 0;
+          const float rr = b.radius * b.radius;
           unsigned long long ab = 0;
-          for (int base = gt - lane; base < total; base += GT) {
-            const int i = base + lane;
-            bool moved = false;
-            if (i < total) {
-              const int k = smem_find_slot(s_coff, cnt, i);
-              const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
-              const float4 co = __ldcg(&m.co[v]);
-              ab += 4u + 12u + (m.mask ? 4u : 0u);  // vertex id, co, mask
-              float4 out;
-              bool mv = false;
-              if (smooth_vertex(m, b, b.y, pp, v, co, out, mv)) {
-                cg::coalesced_group g = cg::coalesced_threads();
-                int slot = 0;
-                if (g.thread_rank() == 0) slot = atomicAdd(nslot_cnt, static_cast<int>(g.size()));
-                slot = g.shfl(slot, 0) + g.thread_rank();
-                slot_v[slot] = v;
-                m.scratch[slot] = out;
-                m.slot_map[v] = slot;
-                moved = mv;
-                const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
-                // ring range and ring (id + co) reads; slot id, value and map written
-                ab += (m.type == kFaces ? 8ull : 0ull) + 16ull * valence + 24ull;
+          constexpr int kCand = 4;
+          for (int base = gt - lane; base < total; base += kCand * GT) {
+            int vv[kCand];
+            float4 cc[kCand];
+#pragma unroll
+            for (int j = 0; j < kCand; j++) {
+              const int i = base + j * GT + lane;
+              vv[j] = -1;
+              if (i < total) {
+                const int k = smem_find_slot(s_coff, cnt, i);
+                vv[j] = leaf_vert(m, s_cl[k], i - s_coff[k]);
               }
             }
+#pragma unroll
+            for (int j = 0; j < kCand; j++)
+              if (vv[j] >= 0) cc[j] = __ldcg(&m.co[vv[j]]);
+#pragma unroll
+            for (int j = 0; j < kCand; j++) {
+              if (vv[j] < 0) continue;
+              ab += 16u;  // vertex id, co
+              if (!(dist_sq(cc[j], pp.loc) <= rr)) continue;
+              cg::coalesced_group g = cg::coalesced_threads();
+              int h = 0;
+              if (g.thread_rank() == 0) h = atomicAdd(&sh.nh, static_cast<int>(g.size()));
+              h = g.shfl(h, 0) + g.thread_rank();
+              slot_v[sbase + h] = vv[j];
+              if (h < kTeamThreads) {
+                sh.hv[h] = vv[j];
+                sh.hco[h] = cc[j];
+              }
+            }
+          }
+          __syncthreads();
+          const int nh = sh.nh;
+          // stage 2: the first sweep of the hits
+          int v0 = -1, n0 = -1;
+          float4 own = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          for (int hb = threadIdx.x - lane; hb < nh; hb += kTeamThreads) {
+            const int h = hb + lane;
+            bool moved = false;
+            if (h < nh) {
+              const int v = h < kTeamThreads ? sh.hv[h] : __ldcg(&slot_v[sbase + h]);
+              const float4 co = h < kTeamThreads ? sh.hco[h] : __ldcg(&m.co[v]);
+              float4 out;
+              int nr = -1;
+              if (h == static_cast<int>(threadIdx.x)) {
+                out = smooth_first(m, b, pp, v, co, s_nbc + threadIdx.x, kTeamThreads, &nr, moved);
+                v0 = v;
+                n0 = nr;
+                own = out;
+              } else {
+                smooth_vertex(m, b, b.y, pp, v, co, out, moved);
+              }
+              val[0][sbase + h] = out;
+              smap[v] = sbase + h;
+              if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+              const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
+              // mask, ring range and ring (id + co) reads; value, map and slot written
+              ab += (m.mask ? 4ull : 0ull) + (m.type == kFaces ? 8ull : 0ull) + 16ull * valence + 24ull;
+            }
             const unsigned bal = __ballot_sync(0xffffffffu, moved);
-            if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
+            if (lane == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
           }
           team_bytes(a, kPhBrush, ab);
           team_sync(cluster, C);
           clk.mark(a, rank, kPhBrush);
-          const int ns = __ldcg(nslot_cnt);
-          float4* const val[2] = {m.scratch, m.scratch2};
-          if (count > 0) {
-            // the thread's first slot keeps its vertex, value and neighbour
-            // table on chip across the sweeps; further slots reload them
-            const int s0 = gt;
-            int v0 = -1, n0 = -1;
-            float4 own = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (s0 < ns) {
-              v0 = __ldcg(&slot_v[s0]);
-              own = __ldcg(&val[0][s0]);
-              n0 = smooth_table(m, v0, s_nbc + threadIdx.x, kTeamThreads);
+          if (count == 0) {
+            for (int h = threadIdx.x; h < nh; h += kTeamThreads) {
+              const int v = h == static_cast<int>(threadIdx.x) ? v0 : __ldcg(&slot_v[sbase + h]);
+              m.co[v] = h == static_cast<int>(threadIdx.x) ? own : __ldcg(&val[0][sbase + h]);
             }
-            for (int it = 1; it <= count; it++) {
-              pp.iter_strength = (it != count) ? 1.0f : last;
-              pp.iteration = it;
-              const float4* src = val[(it - 1) & 1];
-              float4* dst = val[it & 1];
-              ab = 0;
-              for (int sidx = s0; sidx < ns; sidx += GT) {
-                float4 out;
-                int nring;
-                if (sidx == s0 && n0 >= 0) {
-                  out = smooth_slot_cached(m, b, pp, v0, own, n0, s_nbc + threadIdx.x, kTeamThreads, src);
-                  own = out;
-                  nring = n0;
-                } else {
-                  const int v = __ldcg(&slot_v[sidx]);
-                  out = smooth_slot(m, b, pp, v, __ldcg(&src[sidx]), src);
-                  nring = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
-                }
-                dst[sidx] = out;
-                // slot id, value and mask read, ring values read, value written
-                ab += 4ull + 16ull + (m.mask ? 4ull : 0ull) + 16ull * nring + 16ull;
+          }
+          for (int it = 1; it <= count; it++) {
+            pp.iter_strength = (it != count) ? 1.0f : last;
+            pp.iteration = it;
+            const float4* src = val[(it - 1) & 1];
+            float4* dst = val[it & 1];
+            ab = 0;
+            for (int h = threadIdx.x; h < nh; h += kTeamThreads) {
+              float4 out;
+              int v, nring;
+              if (h == static_cast<int>(threadIdx.x) && n0 >= 0) {
+                if (it == 1) smooth_resolve(s_nbc + threadIdx.x, kTeamThreads, n0, smap);
+                out = smooth_slot_cached(m, b, pp, v0, own, n0, s_nbc + threadIdx.x, kTeamThreads, src);
+                v = v0;
+                nring = n0;
+              } else {
+                const bool first = h == static_cast<int>(threadIdx.x);
+                v = first ? v0 : __ldcg(&slot_v[sbase + h]);
+                out = smooth_slot(m, b, pp, v, first ? own : __ldcg(&src[sbase + h]), src, smap);
+                nring = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
               }
-              team_bytes(a, kPhBrush, ab);
-              team_sync(cluster, C);
-              clk.mark(a, rank, kPhBrush);
+              if (h == static_cast<int>(threadIdx.x)) own = out;
+              if (it == count) {
+                m.co[v] = out;
+              } else {
+                dst[sbase + h] = out;
+              }
+              // value and mask read, ring values read, value written
+              ab += 16ull + (m.mask ? 4ull : 0ull) + 16ull * nring + 16ull;
             }
+            team_bytes(a, kPhBrush, ab);
+            team_sync(cluster, C);
+            clk.mark(a, rank, kPhBrush);
           }
-          const float4* fin = val[count & 1];
-          ab = 0;
-          for (int sidx = gt; sidx < ns; sidx += GT) {
-            const int v = __ldcg(&slot_v[sidx]);
-            m.co[v] = __ldcg(&fin[sidx]);
-            m.slot_map[v] = -1;
-            if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
-            ab += 4u + 16u + 12u + 4u;  // slot id, value, co write, map reset
+          if (count == 0) {
+            team_sync(cluster, C);
+            clk.mark(a, rank, kPhApply);
           }
-          team_bytes(a, kPhApply, ab);
-          team_sync(cluster, C);
-          clk.mark(a, rank, kPhApply);
+          // clear this pass's map entries; the map is next filled two smooth
+          // passes later, after at least one more team barrier
+          for (int h = threadIdx.x; h < nh; h += kTeamThreads)
+            smap[h == static_cast<int>(threadIdx.x) ? v0 : __ldcg(&slot_v[sbase + h])] = -1;
         }
       }
       // normal update for the tagged vertices, refit of the touched leaves
@@ -881,49 +927,56 @@ size_t team_smem_bytes(int max_nodes, int max_leaves) {
 
 int team_max_cluster() { return 16; }
 
+template <int kMinBlocks>
 cudaError_t configure_team_kernel(size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_team_stroke, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaError_t e = cudaFuncSetAttribute(k_team_stroke<kMinBlocks>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_team_stroke, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_team_stroke<kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(smem));
 }
 
-cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaStream_t s) {
-  const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves);
-  cudaError_t e = configure_team_kernel(smem);
-  if (e != cudaSuccess) return e;
+static cudaLaunchConfig_t team_config(int cluster, int nteams, size_t smem, cudaStream_t s,
+                                      cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(static_cast<unsigned>(cluster * nteams));
   cfg.blockDim = dim3(kTeamThreads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_team_stroke, a);
+  return cfg;
+}
+
+template <int kMinBlocks>
+static int active_clusters(int cluster, size_t smem) {
+  if (configure_team_kernel<kMinBlocks>(smem) != cudaSuccess) return 0;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = team_config(cluster, 1, smem, nullptr, attr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_team_stroke<kMinBlocks>, &cfg) != cudaSuccess) return 0;
+  return n;
 }
 
 int team_max_active_clusters(int cluster, int max_nodes, int max_leaves) {
   const size_t smem = team_smem_bytes(max_nodes, max_leaves);
-  if (configure_team_kernel(smem) != cudaSuccess) return 0;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(static_cast<unsigned>(cluster));
-  cfg.blockDim = dim3(kTeamThreads);
-  cfg.dynamicSmemBytes = smem;
+  return std::max(active_clusters<1>(cluster, smem), active_clusters<2>(cluster, smem));
+}
+
+cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s) {
+  const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves);
+  // the one-CTA-per-SM build when it holds a team for every job
+  const int n1 = active_clusters<1>(cluster, smem);
+  const int n2 = n1 >= a.njobs ? 0 : active_clusters<2>(cluster, smem);
+  const bool wide = n2 > n1;
+  const int nteams = std::max(1, std::min(a.njobs, wide ? n2 : n1));
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_team_stroke, &cfg) != cudaSuccess) return 0;
-  return n;
+  cudaLaunchConfig_t cfg = team_config(cluster, nteams, smem, s, attr);
+  if (wide) return cudaLaunchKernelEx(&cfg, k_team_stroke<2>, a);
+  return cudaLaunchKernelEx(&cfg, k_team_stroke<1>, a);
 }
 
 }  // namespace sgpu

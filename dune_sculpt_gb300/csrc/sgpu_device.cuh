@@ -75,6 +75,7 @@ struct DevMesh {
   const int* leaf_node;    // leaf id (left-first DFS rank) -> node
   const int* leaf_vert_off;  // FACES: nleaf+1 offsets into leaf_verts
   const int* leaf_uniq;      // FACES: unique vertex count per leaf
+  const int* leaf_ubase;     // FACES: device index of the leaf's first unique vertex
   const int* leaf_verts;     // FACES: vert_indices per leaf, leaf-id order
   const int* leaf_prim_off;  // nleaf+1
   const int* leaf_prims;     // prim indices, leaf-id order
@@ -120,7 +121,7 @@ struct DevMesh {
   AreaPart* parts;  // nleaf
   float4* scratch;   // smooth Jacobi values, totvert
   float4* scratch2;  // second value buffer of the slot sweeps, totvert
-  int* slot_map;     // vertex -> smooth slot of the current pass, or -1
+  int* slot_map[2];  // vertex -> smooth slot of a pass, or -1; passes alternate
   unsigned char* node_upd;  // totnode
   // Profiling: algorithmic bytes per kernel kind (nullptr outside profiling).
   unsigned long long* prof;
@@ -329,7 +330,8 @@ __device__ __forceinline__ int leaf_nverts(const DevMesh& m, int leaf) {
   return (m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf]) * m.grid_area;
 }
 __device__ __forceinline__ int leaf_vert(const DevMesh& m, int leaf, int i) {
-  if (m.type == kFaces) return m.leaf_verts[m.leaf_vert_off[leaf] + i];
+  // FACES: the unique vertices of a leaf are one range in device order
+  if (m.type == kFaces) return m.leaf_ubase[leaf] + i;
   const int g = m.leaf_prims[m.leaf_prim_off[leaf] + i / m.grid_area];
   return g * m.grid_area + i % m.grid_area;
 }
@@ -339,7 +341,7 @@ __device__ __forceinline__ int leaf_nverts_all(const DevMesh& m, int leaf) {
   return (m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf]) * m.grid_area;
 }
 __device__ __forceinline__ int leaf_vert_all(const DevMesh& m, int leaf, int i) {
-  if (m.type == kFaces) return m.leaf_verts[m.leaf_vert_off[leaf] + i];
+  if (m.type == kFaces) return i < m.leaf_uniq[leaf] ? m.leaf_ubase[leaf] + i : m.leaf_verts[m.leaf_vert_off[leaf] + i];
   return leaf_vert(m, leaf, i);
 }
 
@@ -577,34 +579,31 @@ __device__ __forceinline__ float4 smooth_step(float4 co, float3 avg, float fade)
   return out;
 }
 
-// Smooth sweeps after the first, over slots.  The first sweep gives every
-// vertex inside the sphere a slot (slot_map[v] = slot) and stores its new
-// position in the slot; sweep k reads the slot values of sweep k-1 for
-// neighbours with a slot and the unchanged positions of the others (a vertex
-// outside the sphere does not move, so it never enters later).  co is the
-// vertex's own value after sweep k-1; a vertex now outside keeps it.
+// Smooth sweeps over slots.  The first sweep of a pass gives every vertex
+// inside the sphere a slot (smap[v] = slot) and stores its new position in
+// the slot; sweep k reads the slot values of sweep k-1 for neighbours with a
+// slot and the unchanged positions of the others (a vertex outside the
+// sphere does not move, so it never enters later).  co is the vertex's own
+// value after sweep k-1; a vertex now outside keeps it.
 __device__ __forceinline__ float4 smooth_slot(const DevMesh& m, const DevBrush& b,
                                               const PassParams& pp, int v, float4 co,
-                                              const float4* src) {
+                                              const float4* src, const int* smap) {
   const float radius = b.radius;
   const float d2 = dist_sq(co, pp.loc);
   if (!(d2 <= radius * radius)) return co;
   const float sf = strength_factor(m, b, b.y, pp, v, sqrtf(d2), radius);
   const float fade = pp.iter_strength * sf;
   const float3 avg = ring_average<4>(m, v, co, [&](int u) {
-    const int sl = __ldcg(&m.slot_map[u]);
+    const int sl = __ldcg(&smap[u]);
     return xyz(sl >= 0 ? __ldcg(&src[sl]) : m.co[u]);
   });
   return smooth_step(co, avg, fade);
 }
 
-// Neighbour table of one slot vertex for the later sweeps, kept by its thread
-// in shared memory (tab[j * stride]): xyz = the fixed position of a neighbour
-// without a slot, w = its slot (as int bits) or -1.  Returns the ring size,
-// or -1 when it exceeds kNbCache (the vertex then takes smooth_slot).
+// Ring of v in smooth order (FACES one-ring, GRIDS x-1, x+1, y-1, y+1 inside
+// the grid) into id[]; returns its size, or -1 above kNbCache.
 constexpr int kNbCache = 8;
-__device__ __forceinline__ int smooth_table(const DevMesh& m, int v, float4* tab, int stride) {
-  int id[kNbCache];
+__device__ __forceinline__ int ring_ids(const DevMesh& m, int v, int* id) {
   int n = 0;
   if (m.type == kFaces) {
     const int q0 = m.nb_off[v], q1 = m.nb_off[v + 1];
@@ -623,19 +622,66 @@ __device__ __forceinline__ int smooth_table(const DevMesh& m, int v, float4* tab
     for (int k = 0; k < 4; k++)
       if (nx[k] >= 0 && nx[k] < gs && ny[k] >= 0 && ny[k] < gs) id[n++] = g * area + ny[k] * gs + nx[k];
   }
-  int sl[kNbCache];
-#pragma unroll
-  for (int j = 0; j < kNbCache; j++) sl[j] = id[j] >= 0 ? __ldcg(&m.slot_map[id[j]]) : -1;
-#pragma unroll
-  for (int j = 0; j < kNbCache; j++) {
-    if (j >= n) break;
-    const float3 p = sl[j] < 0 ? xyz(m.co[id[j]]) : make_float3(0.0f, 0.0f, 0.0f);
-    tab[j * stride] = make_float4(p.x, p.y, p.z, __int_as_float(sl[j]));
-  }
   return n;
 }
 
-// smooth_slot with the neighbour table of smooth_table (n entries).
+// First sweep of a vertex known to be inside the sphere: the same value as
+// smooth_vertex, with its ring recorded in tab (tab[j * stride]: xyz = the
+// neighbour's position, w = its id as int bits) for the later sweeps.
+// *nring = ring size, or -1 when the ring exceeds kNbCache (tab unused).
+__device__ __forceinline__ float4 smooth_first(const DevMesh& m, const DevBrush& b,
+                                               const PassParams& pp, int v, float4 co,
+                                               float4* tab, int stride, int* nring,
+                                               bool& moved) {
+  const float radius = b.radius;
+  const float d2 = dist_sq(co, pp.loc);
+  const float sf = strength_factor(m, b, b.y, pp, v, sqrtf(d2), radius);
+  const float fade = pp.iter_strength * sf;
+  moved = fade != 0.0f;
+  int id[kNbCache];
+  const int n = ring_ids(m, v, id);
+  *nring = n;
+  if (n < 0) return smooth_step(co, neighbor_average(m, v, co), fade);
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+#pragma unroll
+  for (int h = 0; h < kNbCache; h += 4) {
+    float3 c[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (h + j < n) c[j] = xyz(m.co[id[h + j]]);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (h + j < n) {
+        sx += c[j].x;
+        sy += c[j].y;
+        sz += c[j].z;
+        tab[(h + j) * stride] = make_float4(c[j].x, c[j].y, c[j].z, __int_as_float(id[h + j]));
+      }
+    }
+  }
+  float3 avg;
+  if (n == 0) {
+    avg = make_float3(co.x, co.y, co.z);
+  } else {
+    const float inv = 1.0f / (float)n;
+    avg = make_float3(sx * inv, sy * inv, sz * inv);
+  }
+  return smooth_step(co, avg, fade);
+}
+
+// Replaces the neighbour ids of a ring table by their slots (or -1), once
+// the first sweep has given out every slot of the pass.
+__device__ __forceinline__ void smooth_resolve(float4* tab, int stride, int n, const int* smap) {
+  int sl[kNbCache];
+#pragma unroll
+  for (int j = 0; j < kNbCache; j++) sl[j] = j < n ? __ldcg(&smap[__float_as_int(tab[j * stride].w)]) : -1;
+#pragma unroll
+  for (int j = 0; j < kNbCache; j++)
+    if (j < n) tab[j * stride].w = __int_as_float(sl[j]);
+}
+
+// smooth_slot with a resolved ring table (n entries: w = slot or -1, xyz =
+// the fixed position of a neighbour without a slot).
 __device__ __forceinline__ float4 smooth_slot_cached(const DevMesh& m, const DevBrush& b,
                                                      const PassParams& pp, int v, float4 co,
                                                      int n, const float4* tab, int stride,

@@ -33,6 +33,10 @@ cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s);
 cudaError_t launch_mark_all(const DevMesh& m, int bits, cudaStream_t s);
 // Refit-chunk boxes of every leaf from the current positions.
 cudaError_t launch_chunk_boxes_all(const DevMesh& m, int nchunks, cudaStream_t s);
+// out[i] = in[idx[i]]: float4, float, or xyz keeping out.w.
+cudaError_t launch_gather_f4(float4* out, const float4* in, const int* idx, int n, cudaStream_t s);
+cudaError_t launch_gather_f1(float* out, const float* in, const int* idx, int n, cudaStream_t s);
+cudaError_t launch_gather_xyz(float4* out, const float4* in, const int* idx, int n, cudaStream_t s);
 int cull_smem_limit();
 int grid_size_limit();
 void configure_kernels();

@@ -46,6 +46,7 @@ enum TeamPhase {
 size_t team_smem_bytes(int max_nodes, int max_leaves);
 int team_max_cluster();
 int team_max_active_clusters(int cluster, int max_nodes, int max_leaves);
-cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, int nteams, cudaStream_t s);
+// Launches min(njobs, resident teams) teams of the build that holds the most.
+cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s);
 
 }  // namespace sgpu
