@@ -231,9 +231,9 @@ struct FlushSmem {
 // Bottom-up flush by one CTA: touched leaf boxes from their chunk boxes, then
 // every ancestor of a touched leaf recomputed from its two children
 // (update_node_vb, pbvh.c:2026-2046), deepest level first, as pbvh_flush_bb
-// (pbvh.c:3287-3317) orders it.  Clears the touched leaves' UpdateNormals and
-// UpdateBB.  s_idx holds kNoPos for every node on entry and on exit; an
-// ancestor is first claimed with kClaimed, then given its sorted position.
+// (pbvh.c:3287-3317) orders it.  s_idx holds kNoPos for every node on entry
+// and on exit; an ancestor is first claimed with kClaimed, then given its
+// sorted position.  The caller clears the touched leaves' update flags.
 __device__ void team_flush(const DevMesh& m, int ntouch, const int* s_par, unsigned short* s_idx,
                            int* s_list, int* s_sorted, FlushSmem& fs, int* s_start, int* s_cur,
                            TeamShared& sh, unsigned long long& ab) {
@@ -325,8 +325,6 @@ __device__ void team_flush(const DevMesh& m, int ntouch, const int* s_par, unsig
     __syncthreads();
   }
   for (int pos = threadIdx.x; pos < nm; pos += kTeamThreads) s_idx[s_sorted[pos]] = kNoPos;
-  for (int k = threadIdx.x; k < ntouch; k += kTeamThreads)
-    atomicAnd(&m.leaf_flag[__ldcg(&m.touch_list[k])], ~(kUpdateNormals | kUpdateBB));
   __syncthreads();
 }
 
@@ -804,20 +802,15 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
             smap[h == static_cast<int>(threadIdx.x) ? v0 : __ldcg(&slot_v[sbase + h])] = -1;
         }
       }
-      // normal update for the tagged vertices, refit of the touched leaves
+      // End of the dab.  FACES: refit of the touched leaves, then the flush
+      // (CTA 0) alongside the normal update of the tagged vertices (the other
+      // CTAs): normals read positions and leaf flags, the flush reads chunk
+      // boxes and writes node boxes.  GRIDS: the normal update moves seam
+      // positions, so it runs first, then refit and flush.
       const int ntag = __ldcg(tag_cnt);
       const int ntouch = __ldcg(touch_cnt);
       unsigned long long ab = 0;
-      if (m.type == kFaces) {
-        for (int j = gt; j < ntag; j += GT) {
-          const int v = __ldcg(&m.tag_list[j]);
-          float4 n;
-          const int used = vertex_normal(m, v, n);
-          m.no[v] = n;
-          m.vtag[v] = 0u;
-          ab += 24ull + 16ull * used;
-        }
-      } else {
+      if (m.type == kGrids) {
         // GRIDS: faces of the touched leaves, the inner normals of their
         // grids, the face seams and centres, then the base edges and corners
         // (positions move at the seams, so the refit below follows).
@@ -885,8 +878,27 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       unsigned long long fb = 0;
       if (rank == 0) team_flush(m, ntouch, s_par, s_idx, s_cl, s_coff, s_scr.flush, s_start, s_cur, sh, fb);
       team_bytes(a, kPhFlush, fb);
+      if (m.type == kFaces && (rank != 0 || C == 1)) {
+        // normals over CTAs 1..C-1 (all of the team when it is one CTA)
+        const int nc = C > 1 ? static_cast<int>(C) - 1 : 1;
+        const int cr = C > 1 ? static_cast<int>(rank) - 1 : 0;
+        ab = 0;
+        for (int j = 32 * ((threadIdx.x >> 5) * nc + cr) + lane; j < ntag; j += nc * kTeamThreads) {
+          const int v = __ldcg(&m.tag_list[j]);
+          float4 n;
+          const int used = vertex_normal(m, v, n);
+          m.no[v] = n;
+          m.vtag[v] = 0u;
+          ab += 24ull + 16ull * used;
+        }
+        team_bytes(a, kPhUpdate, ab);
+      }
       team_sync(cluster, C);
       clk.mark(a, rank, kPhFlush);
+      // the touched leaves' update flags clear once both have read them
+      if (rank == 0)
+        for (int k = threadIdx.x; k < ntouch; k += kTeamThreads)
+          atomicAnd(&m.leaf_flag[__ldcg(&m.touch_list[k])], ~(kUpdateNormals | kUpdateBB));
     }
     // end of stroke: BKE_pbvh_update_bounds(UpdateOriginalBB)
     for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_pass[i] = 0;
