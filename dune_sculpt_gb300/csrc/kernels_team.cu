@@ -216,115 +216,176 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_p
   __syncthreads();
 }
 
-constexpr int kFlushTab = 128;  // ancestors whose boxes stay in shared memory
-constexpr unsigned short kNoPos = 0xFFFFu, kClaimed = 0xFFFEu;
+constexpr int kFlushTab = 128;  // ancestors whose boxes stay on chip
+constexpr unsigned short kNoPos = 0xFFFFu;
 
-// Shared memory of the flush: for the first kFlushTab ancestors in sorted
-// order, their new box, their first child and the boxes of those of their two
-// children that are not ancestors themselves (prefetched in one sweep).
+// Flush tables (CTA 0): new boxes of the first kFlushTab listed ancestors,
+// and the new boxes of their children that are touched leaves.
 struct FlushSmem {
   float4 own[2 * kFlushTab];
   float4 kid[4 * kFlushTab];
-  int child[kFlushTab];
 };
 
-// Bottom-up flush by one CTA: touched leaf boxes from their chunk boxes, then
-// every ancestor of a touched leaf recomputed from its two children
-// (update_node_vb, pbvh.c:2026-2046), deepest level first, as pbvh_flush_bb
-// (pbvh.c:3287-3317) orders it.  s_idx holds kNoPos for every node on entry
-// and on exit; an ancestor is first claimed with kClaimed, then given its
-// sorted position.  The caller clears the touched leaves' update flags.
-__device__ void team_flush(const DevMesh& m, int ntouch, const int* s_par, unsigned short* s_idx,
-                           int* s_list, int* s_sorted, FlushSmem& fs, int* s_start, int* s_cur,
-                           TeamShared& sh, unsigned long long& ab) {
-  const int warp = threadIdx.x >> 5;
-  for (int k = warp; k < ntouch; k += kTeamThreads / 32) {
-    const int leaf = __ldcg(&m.touch_list[k]);
-    leaf_box_from_chunks(m, leaf);
-    // chunk boxes read, leaf box written
-    if ((threadIdx.x & 31) == 0) ab += 32ull * (m.leaf_chunk_off[leaf + 1] - m.leaf_chunk_off[leaf] + 1);
-  }
+// One listed ancestor per thread (fast path): its node, depth, and per child
+// the source of the child's box: 0 = unchanged (a/b registers), 1 = touched
+// leaf (fs.kid), 2 = listed ancestor at list position p0/p1 (fs.own).
+struct FlushState {
+  int node, dep;
+  int k0, k1, p0, p1;
+  float4 a0, a1, b0, b1;
+};
+
+__device__ __forceinline__ bool bit_set(const unsigned int* bits, int i) {
+  return (bits[i >> 5] >> (i & 31)) & 1u;
+}
+
+// Flush, first half (CTA 0 while the other CTAs refit): every ancestor of a
+// touched leaf is listed once (claimed in a bitmap over the nodes, which also
+// marks the touched leaf nodes) and s_idx[node] = its list position; with at
+// most kFlushTab ancestors, each thread takes one and loads the boxes of its
+// children that the update leaves unchanged.  touched: the touched leaves.
+__device__ void team_flush_mark(const DevMesh& m, int ntouch, const int* touched, const int* s_par,
+                                unsigned int* bits, int* s_list, unsigned short* s_idx,
+                                TeamShared& sh, FlushState& f) {
+  for (int i = threadIdx.x; i < (m.totnode + 31) / 32; i += kTeamThreads) bits[i] = 0u;
   if (threadIdx.x == 0) sh.nmark = 0;
-  for (int i = threadIdx.x; i <= m.max_depth; i += kTeamThreads) s_start[i] = 0;
   __syncthreads();
   for (int k = threadIdx.x; k < ntouch; k += kTeamThreads) {
-    int p = s_par[m.leaf_node[__ldcg(&m.touch_list[k])]];
-    while (p >= 0 && atomicCAS(&s_idx[p], kNoPos, kClaimed) == kNoPos) {
+    const int leaf_node = m.leaf_node[touched[k]];
+    atomicOr(&bits[leaf_node >> 5], 1u << (leaf_node & 31));
+    int p = s_par[leaf_node];
+    while (p >= 0) {
+      const unsigned int bit = 1u << (p & 31);
+      if (atomicOr(&bits[p >> 5], bit) & bit) break;  // claimed: so are its ancestors
       s_list[atomicAdd(&sh.nmark, 1)] = p;
       p = s_par[p];
     }
   }
   __syncthreads();
   const int nm = sh.nmark;
-  for (int j = threadIdx.x; j < nm; j += kTeamThreads) atomicAdd(&s_start[m.node_depth[s_list[j]]], 1);
+  for (int t = threadIdx.x; t < nm; t += kTeamThreads) s_idx[s_list[t]] = static_cast<unsigned short>(t);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
+  f.node = -1;
+  f.dep = -1;
+  if (nm <= kFlushTab && static_cast<int>(threadIdx.x) < nm) {
+    f.node = s_list[threadIdx.x];
+    f.dep = m.node_depth[f.node];
+    const int c = m.node_child[f.node];
+    f.p0 = s_idx[c];
+    f.p1 = s_idx[c + 1];
+    f.k0 = f.p0 != kNoPos ? 2 : (bit_set(bits, c) ? 1 : 0);
+    f.k1 = f.p1 != kNoPos ? 2 : (bit_set(bits, c + 1) ? 1 : 0);
+    if (f.k0 == 0) {
+      f.a0 = __ldcg(&m.vb[2 * c]);
+      f.a1 = __ldcg(&m.vb[2 * c + 1]);
+    }
+    if (f.k1 == 0) {
+      f.b0 = __ldcg(&m.vb[2 * c + 2]);
+      f.b1 = __ldcg(&m.vb[2 * c + 3]);
+    }
+  }
+}
+
+__device__ __forceinline__ void box_union(const float4& a0, const float4& a1, const float4& b0,
+                                          const float4& b1, float4& mn, float4& mx) {
+  mn.x = fmin_ref(fmin_ref(FLT_MAX, a0.x), b0.x);
+  mn.y = fmin_ref(fmin_ref(FLT_MAX, a0.y), b0.y);
+  mn.z = fmin_ref(fmin_ref(FLT_MAX, a0.z), b0.z);
+  mx.x = fmax_ref(fmax_ref(-FLT_MAX, a1.x), b1.x);
+  mx.y = fmax_ref(fmax_ref(-FLT_MAX, a1.y), b1.y);
+  mx.z = fmax_ref(fmax_ref(-FLT_MAX, a1.z), b1.z);
+  mn.w = mx.w = 0.0f;
+}
+
+// Flush, second half (CTA 0, after the refit): the touched leaf boxes from
+// their chunk boxes (one warp per leaf; also handed to the parent's thread in
+// fs.kid), then each listed ancestor becomes the union of its two children
+// (update_node_vb, pbvh.c:2026-2046), deepest level first as pbvh_flush_bb
+// (pbvh.c:3287-3317) orders it.  Resets s_idx to kNoPos.
+__device__ void team_flush_levels(const DevMesh& m, int ntouch, const int* touched,
+                                  const int* s_par, const int* s_list, unsigned short* s_idx,
+                                  FlushSmem& fs, TeamShared& sh, FlushState& f,
+                                  unsigned long long& ab) {
+  const int nm = sh.nmark;
+  const int lane = threadIdx.x & 31;
+  for (int k = threadIdx.x >> 5; k < ntouch; k += kTeamThreads / 32) {
+    const int leaf = touched[k];
+    float4 mn, mx;
+    leaf_box_from_chunks(m, leaf, mn, mx);
+    if (lane == 0) {
+      const int node = m.leaf_node[leaf];
+      const int p = s_par[node];
+      const int pos = p >= 0 ? s_idx[p] : kNoPos;
+      if (pos < kFlushTab) {
+        const int h = node - m.node_child[p];
+        fs.kid[2 * (2 * pos + h)] = mn;
+        fs.kid[2 * (2 * pos + h) + 1] = mx;
+      }
+      ab += 32ull * (m.leaf_chunk_off[leaf + 1] - m.leaf_chunk_off[leaf] + 1);
+    }
+  }
+  __syncthreads();
+  if (nm <= kFlushTab) {
+    const int t = threadIdx.x;
+    if (f.node >= 0) ab += 72u;  // two child boxes read, one box written
     for (int dd = m.max_depth; dd >= 0; dd--) {
-      const int c = s_start[dd];
-      s_start[dd] = run;
-      s_cur[dd] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-  for (int j = threadIdx.x; j < nm; j += kTeamThreads) {
-    const int node = s_list[j];
-    const int pos = atomicAdd(&s_cur[m.node_depth[node]], 1);
-    s_sorted[pos] = node;
-    s_idx[node] = static_cast<unsigned short>(pos);
-  }
-  __syncthreads();
-  const int npre = min(nm, kFlushTab);
-  for (int i = threadIdx.x; i < 2 * npre; i += kTeamThreads) {
-    const int pos = i >> 1, h = i & 1;
-    const int c = m.node_child[s_sorted[pos]];
-    if (h == 0) fs.child[pos] = c;
-    if (s_idx[c + h] == kNoPos) {
-      fs.kid[2 * i] = __ldcg(&m.vb[2 * (c + h)]);
-      fs.kid[2 * i + 1] = __ldcg(&m.vb[2 * (c + h) + 1]);
-    }
-  }
-  __syncthreads();
-  for (int dd = m.max_depth; dd >= 0; dd--) {
-    const int b0 = s_start[dd], b1 = s_cur[dd];
-    for (int pos = b0 + threadIdx.x; pos < b1; pos += kTeamThreads) {
-      const int node = s_sorted[pos];
-      const bool cached = pos < kFlushTab;
-      const int c = cached ? fs.child[pos] : m.node_child[node];
-      float4 box[2][2];
-      for (int h = 0; h < 2; h++) {
-        const int ci = s_idx[c + h];  // children are one level deeper: done
-        if (ci < kFlushTab) {
-          box[h][0] = fs.own[2 * ci];
-          box[h][1] = fs.own[2 * ci + 1];
-        } else if (ci == kNoPos && cached) {
-          box[h][0] = fs.kid[4 * pos + 2 * h];
-          box[h][1] = fs.kid[4 * pos + 2 * h + 1];
-        } else {
-          box[h][0] = __ldcg(&m.vb[2 * (c + h)]);
-          box[h][1] = __ldcg(&m.vb[2 * (c + h) + 1]);
+      if (f.dep == dd) {
+        if (f.k0 == 2) {
+          f.a0 = fs.own[2 * f.p0];
+          f.a1 = fs.own[2 * f.p0 + 1];
+        } else if (f.k0 == 1) {
+          f.a0 = fs.kid[4 * t];
+          f.a1 = fs.kid[4 * t + 1];
         }
+        if (f.k1 == 2) {
+          f.b0 = fs.own[2 * f.p1];
+          f.b1 = fs.own[2 * f.p1 + 1];
+        } else if (f.k1 == 1) {
+          f.b0 = fs.kid[4 * t + 2];
+          f.b1 = fs.kid[4 * t + 3];
+        }
+        float4 mn, mx;
+        box_union(f.a0, f.a1, f.b0, f.b1, mn, mx);
+        fs.own[2 * t] = mn;
+        fs.own[2 * t + 1] = mx;
+        m.vb[2 * f.node] = mn;
+        m.vb[2 * f.node + 1] = mx;
       }
-      float4 mn, mx;
-      mn.x = fmin_ref(fmin_ref(FLT_MAX, box[0][0].x), box[1][0].x);
-      mn.y = fmin_ref(fmin_ref(FLT_MAX, box[0][0].y), box[1][0].y);
-      mn.z = fmin_ref(fmin_ref(FLT_MAX, box[0][0].z), box[1][0].z);
-      mx.x = fmax_ref(fmax_ref(-FLT_MAX, box[0][1].x), box[1][1].x);
-      mx.y = fmax_ref(fmax_ref(-FLT_MAX, box[0][1].y), box[1][1].y);
-      mx.z = fmax_ref(fmax_ref(-FLT_MAX, box[0][1].z), box[1][1].z);
-      mn.w = mx.w = 0.0f;
-      m.vb[2 * node] = mn;
-      m.vb[2 * node + 1] = mx;
-      if (cached) {
-        fs.own[2 * pos] = mn;
-        fs.own[2 * pos + 1] = mx;
-      }
-      ab += 72u;  // two child boxes read, one box written
+      __syncthreads();
     }
-    __syncthreads();
+  } else {
+    // many ancestors: per level, every thread scans the list; child boxes
+    // come from fs.own (first kFlushTab list positions) or global memory
+    for (int dd = m.max_depth; dd >= 0; dd--) {
+      for (int t = threadIdx.x; t < nm; t += kTeamThreads) {
+        const int node = s_list[t];
+        if (m.node_depth[node] != dd) continue;
+        const int c = m.node_child[node];
+        float4 box[2][2];
+        for (int h = 0; h < 2; h++) {
+          const int pc = s_idx[c + h];
+          if (pc < kFlushTab) {
+            box[h][0] = fs.own[2 * pc];
+            box[h][1] = fs.own[2 * pc + 1];
+          } else {
+            box[h][0] = __ldcg(&m.vb[2 * (c + h)]);
+            box[h][1] = __ldcg(&m.vb[2 * (c + h) + 1]);
+          }
+        }
+        float4 mn, mx;
+        box_union(box[0][0], box[0][1], box[1][0], box[1][1], mn, mx);
+        if (t < kFlushTab) {
+          fs.own[2 * t] = mn;
+          fs.own[2 * t + 1] = mx;
+        }
+        m.vb[2 * node] = mn;
+        m.vb[2 * node + 1] = mx;
+        ab += 72u;
+      }
+      __syncthreads();
+    }
   }
-  for (int pos = threadIdx.x; pos < nm; pos += kTeamThreads) s_idx[s_sorted[pos]] = kNoPos;
+  for (int t = threadIdx.x; t < nm; t += kTeamThreads) s_idx[s_list[t]] = kNoPos;
   __syncthreads();
 }
 
@@ -508,14 +569,15 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
   __shared__ Scratch s_scr;
   Lane* s_lanes = s_scr.lanes;
   __shared__ Lane s_chunks[kTeamMaxChunks];
-  __shared__ int s_start[256], s_cur[256];
   extern __shared__ __align__(16) unsigned char dyn[];
   float4* s_nbc = reinterpret_cast<float4*>(dyn);  // smooth neighbour tables
   int* s_par = reinterpret_cast<int*>(s_nbc + kNbCache * kTeamThreads);
   int* s_cl = s_par + a.max_nodes;
   int* s_coff = s_cl + a.max_leaves + 1;
   unsigned short* s_idx = reinterpret_cast<unsigned short*>(s_coff + a.max_leaves + 2);
-  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_idx + a.max_nodes);
+  // node marks; also the flush's claim bitmap (32-bit words): the ushort
+  // array before it has an even length, so this starts 4-byte aligned
+  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_idx + ((a.max_nodes + 1) & ~1));
   PhaseClock clk;
   clk.last = a.phase_ns ? global_ns() : 0ull;
 
@@ -810,6 +872,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       const int ntag = __ldcg(tag_cnt);
       const int ntouch = __ldcg(touch_cnt);
       unsigned long long ab = 0;
+      FlushState fst;
       if (m.type == kGrids) {
         // GRIDS: faces of the touched leaves, the inner normals of their
         // grids, the face seams and centres, then the base edges and corners
@@ -860,23 +923,30 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           off += m.leaf_chunk_off[s_cl[k] + 1] - m.leaf_chunk_off[s_cl[k]];
         }
         __syncthreads();
+        // chunks dealt over CTAs 1..C-1 while CTA 0 lists the ancestors to flush
         const int wpc = kTeamThreads / 32;
+        const int rc = C > 1 ? static_cast<int>(C) - 1 : 1;
+        const int rr = C > 1 ? static_cast<int>(rank) - 1 : 0;
         const unsigned idb = (m.type == kFaces ? 4u : 0u) + 12u;  // vertex id, position
-        for (int j = (threadIdx.x >> 5) * static_cast<int>(C) + static_cast<int>(rank); j < nchunk; j += C * wpc) {
-          const int k = smem_find_slot(s_coff, ntouch, j);
-          const int leaf = s_cl[k], c = j - s_coff[k];
-          float mn[3], mx[3];
-          chunk_refit_warp(m, leaf, c, mn, mx);
-          if ((threadIdx.x & 31) == 0)
-            ab += 32ull + idb * static_cast<unsigned long long>(min(kChunk, leaf_nverts_all(m, leaf) - c * kChunk));
+        if (rank != 0 || C == 1) {
+          for (int j = (threadIdx.x >> 5) * rc + rr; j < nchunk; j += rc * wpc) {
+            const int k = smem_find_slot(s_coff, ntouch, j);
+            const int leaf = s_cl[k], c = j - s_coff[k];
+            float mn[3], mx[3];
+            chunk_refit_warp(m, leaf, c, mn, mx);
+            if (lane == 0)
+              ab += 32ull + idb * static_cast<unsigned long long>(min(kChunk, leaf_nverts_all(m, leaf) - c * kChunk));
+          }
         }
+        if (rank == 0)
+          team_flush_mark(m, ntouch, s_cl, s_par, reinterpret_cast<unsigned int*>(s_pass), s_coff, s_idx, sh, fst);
       }
       team_bytes(a, kPhUpdate, ab);
       team_sync(cluster, C);
       clk.mark(a, rank, kPhUpdate);
-      // flush by CTA 0: touched leaf boxes, then their ancestors bottom-up
+      // flush by CTA 0: the listed ancestors bottom-up
       unsigned long long fb = 0;
-      if (rank == 0) team_flush(m, ntouch, s_par, s_idx, s_cl, s_coff, s_scr.flush, s_start, s_cur, sh, fb);
+      if (rank == 0) team_flush_levels(m, ntouch, s_cl, s_par, s_coff, s_idx, s_scr.flush, sh, fst, fb);
       team_bytes(a, kPhFlush, fb);
       if (m.type == kFaces && (rank != 0 || C == 1)) {
         // normals over CTAs 1..C-1 (all of the team when it is one CTA)
@@ -929,11 +999,14 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
 }
 
 // Dynamic shared memory: smooth neighbour tables (float4), parents, culled
-// list and offsets (int), flush positions (ushort), node marks (byte).
+// list and offsets (int), flush positions (ushort, even count), node marks
+// (byte; at least the claim bitmap's 32-bit words).
 size_t team_smem_bytes(int max_nodes, int max_leaves) {
+  const size_t n = static_cast<size_t>(max_nodes);
+  const size_t marks = std::max(n, 4 * ((n + 31) / 32));
   const size_t b = sizeof(float4) * kNbCache * kTeamThreads +
-                   sizeof(int) * (static_cast<size_t>(max_nodes) + 2 * static_cast<size_t>(max_leaves) + 3) +
-                   sizeof(unsigned short) * static_cast<size_t>(max_nodes) + static_cast<size_t>(max_nodes);
+                   sizeof(int) * (n + 2 * static_cast<size_t>(max_leaves) + 3) +
+                   sizeof(unsigned short) * ((n + 1) & ~static_cast<size_t>(1)) + marks;
   return (b + 15) & ~static_cast<size_t>(15);
 }
 

@@ -380,8 +380,10 @@ __device__ __forceinline__ void chunk_refit_warp(const DevMesh& m, int leaf, int
   }
 }
 
-// Leaf box as the union of its chunk boxes, by one warp; lane 0 writes vb.
-__device__ __forceinline__ void leaf_box_from_chunks(const DevMesh& m, int leaf) {
+// Leaf box as the union of its chunk boxes, by one warp; lane 0 writes vb,
+// every lane returns the box in omn / omx.
+__device__ __forceinline__ void leaf_box_from_chunks(const DevMesh& m, int leaf, float4& omn,
+                                                     float4& omx) {
   const int lane = threadIdx.x & 31;
   float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
   for (int id = m.leaf_chunk_off[leaf] + lane; id < m.leaf_chunk_off[leaf + 1]; id += 32) {
@@ -402,11 +404,18 @@ __device__ __forceinline__ void leaf_box_from_chunks(const DevMesh& m, int leaf)
       mn[k] = (mn[k] < omn) ? mn[k] : omn;
       mx[k] = (mx[k] > omx) ? mx[k] : omx;
     }
+  omn = make_float4(mn[0], mn[1], mn[2], 0.0f);
+  omx = make_float4(mx[0], mx[1], mx[2], 0.0f);
   if (lane == 0) {
     const int node = m.leaf_node[leaf];
-    m.vb[2 * node] = make_float4(mn[0], mn[1], mn[2], 0.0f);
-    m.vb[2 * node + 1] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+    m.vb[2 * node] = omn;
+    m.vb[2 * node + 1] = omx;
   }
+}
+
+__device__ __forceinline__ void leaf_box_from_chunks(const DevMesh& m, int leaf) {
+  float4 mn, mx;
+  leaf_box_from_chunks(m, leaf, mn, mx);
 }
 
 __device__ __forceinline__ float dist_sq(float4 co, const float* c) {
