@@ -219,11 +219,16 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_p
 constexpr int kFlushTab = 128;  // ancestors whose boxes stay on chip
 constexpr unsigned short kNoPos = 0xFFFFu;
 
+constexpr int kFlushTouch = 128;  // touched leaves whose flush data is staged
+
 // Flush tables (CTA 0): new boxes of the first kFlushTab listed ancestors,
-// and the new boxes of their children that are touched leaves.
+// the new boxes of their children that are touched leaves, and per touched
+// leaf (first kFlushTouch) its slot in kid (or -1) and its chunk range.
 struct FlushSmem {
   float4 own[2 * kFlushTab];
   float4 kid[4 * kFlushTab];
+  int kslot[kFlushTouch];
+  int2 kco[kFlushTouch];
 };
 
 // One listed ancestor per thread (fast path): its node, depth, and per child
@@ -246,7 +251,7 @@ __device__ __forceinline__ bool bit_set(const unsigned int* bits, int i) {
 // children that the update leaves unchanged.  touched: the touched leaves.
 __device__ void team_flush_mark(const DevMesh& m, int ntouch, const int* touched, const int* s_par,
                                 unsigned int* bits, int* s_list, unsigned short* s_idx,
-                                TeamShared& sh, FlushState& f) {
+                                FlushSmem& fs, TeamShared& sh, FlushState& f) {
   for (int i = threadIdx.x; i < (m.totnode + 31) / 32; i += kTeamThreads) bits[i] = 0u;
   if (threadIdx.x == 0) sh.nmark = 0;
   __syncthreads();
@@ -265,6 +270,14 @@ __device__ void team_flush_mark(const DevMesh& m, int ntouch, const int* touched
   const int nm = sh.nmark;
   for (int t = threadIdx.x; t < nm; t += kTeamThreads) s_idx[s_list[t]] = static_cast<unsigned short>(t);
   __syncthreads();
+  for (int k = threadIdx.x; k < min(ntouch, kFlushTouch); k += kTeamThreads) {
+    const int leaf = touched[k];
+    const int node = m.leaf_node[leaf];
+    const int p = s_par[node];
+    const int pos = p >= 0 ? s_idx[p] : kNoPos;
+    fs.kslot[k] = pos < kFlushTab ? 2 * pos + (node - m.node_child[p]) : -1;
+    fs.kco[k] = make_int2(m.leaf_chunk_off[leaf], m.leaf_chunk_off[leaf + 1]);
+  }
   f.node = -1;
   f.dep = -1;
   if (nm <= kFlushTab && static_cast<int>(threadIdx.x) < nm) {
@@ -309,23 +322,90 @@ __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int* touch
   const int nm = sh.nmark;
   const int lane = threadIdx.x & 31;
   for (int k = threadIdx.x >> 5; k < ntouch; k += kTeamThreads / 32) {
-    const int leaf = touched[k];
-    float4 mn, mx;
-    leaf_box_from_chunks(m, leaf, mn, mx);
-    if (lane == 0) {
+    int2 co;
+    int slot;
+    if (k < kFlushTouch) {
+      co = fs.kco[k];
+      slot = fs.kslot[k];
+    } else {
+      const int leaf = touched[k];
+      co = make_int2(m.leaf_chunk_off[leaf], m.leaf_chunk_off[leaf + 1]);
       const int node = m.leaf_node[leaf];
       const int p = s_par[node];
       const int pos = p >= 0 ? s_idx[p] : kNoPos;
-      if (pos < kFlushTab) {
-        const int h = node - m.node_child[p];
-        fs.kid[2 * (2 * pos + h)] = mn;
-        fs.kid[2 * (2 * pos + h) + 1] = mx;
+      slot = pos < kFlushTab ? 2 * pos + (node - m.node_child[p]) : -1;
+    }
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int id = co.x + lane; id < co.y; id += 32) {
+      const float4 c0 = __ldcg(&m.chunk_box[2 * id]), c1 = __ldcg(&m.chunk_box[2 * id + 1]);
+      mn[0] = fmin_ref(mn[0], c0.x);
+      mn[1] = fmin_ref(mn[1], c0.y);
+      mn[2] = fmin_ref(mn[2], c0.z);
+      mx[0] = fmax_ref(mx[0], c1.x);
+      mx[1] = fmax_ref(mx[1], c1.y);
+      mx[2] = fmax_ref(mx[2], c1.z);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        mn[q] = fmin_ref(mn[q], __shfl_xor_sync(0xffffffffu, mn[q], o));
+        mx[q] = fmax_ref(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], o));
       }
-      ab += 32ull * (m.leaf_chunk_off[leaf + 1] - m.leaf_chunk_off[leaf] + 1);
+    if (lane == 0) {
+      const float4 bmn = make_float4(mn[0], mn[1], mn[2], 0.0f);
+      const float4 bmx = make_float4(mx[0], mx[1], mx[2], 0.0f);
+      const int node = m.leaf_node[touched[k]];
+      m.vb[2 * node] = bmn;
+      m.vb[2 * node + 1] = bmx;
+      if (slot >= 0) {
+        fs.kid[2 * slot] = bmn;
+        fs.kid[2 * slot + 1] = bmx;
+      }
+      ab += 32ull * (co.y - co.x + 1);  // chunk boxes read, leaf box written
     }
   }
   __syncthreads();
-  if (nm <= kFlushTab) {
+  if (nm <= 32) {
+    // one warp: each lane keeps one ancestor's box in registers and hands it
+    // to its parent's lane by shuffle
+    if (threadIdx.x < 32) {
+      const int t = lane;
+      float own[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+      if (f.node >= 0) ab += 72u;
+      for (int dd = m.max_depth; dd >= 0; dd--) {
+        float c0[6], c1[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+          c0[q] = __shfl_sync(0xffffffffu, own[q], f.p0 & 31);
+          c1[q] = __shfl_sync(0xffffffffu, own[q], f.p1 & 31);
+        }
+        if (f.dep == dd) {
+          if (f.k0 == 2) {
+            f.a0 = make_float4(c0[0], c0[1], c0[2], 0.0f);
+            f.a1 = make_float4(c0[3], c0[4], c0[5], 0.0f);
+          } else if (f.k0 == 1) {
+            f.a0 = fs.kid[4 * t];
+            f.a1 = fs.kid[4 * t + 1];
+          }
+          if (f.k1 == 2) {
+            f.b0 = make_float4(c1[0], c1[1], c1[2], 0.0f);
+            f.b1 = make_float4(c1[3], c1[4], c1[5], 0.0f);
+          } else if (f.k1 == 1) {
+            f.b0 = fs.kid[4 * t + 2];
+            f.b1 = fs.kid[4 * t + 3];
+          }
+          float4 mn, mx;
+          box_union(f.a0, f.a1, f.b0, f.b1, mn, mx);
+          own[0] = mn.x, own[1] = mn.y, own[2] = mn.z;
+          own[3] = mx.x, own[4] = mx.y, own[5] = mx.z;
+          m.vb[2 * f.node] = mn;
+          m.vb[2 * f.node + 1] = mx;
+        }
+      }
+    }
+    __syncthreads();
+  } else if (nm <= kFlushTab) {
     const int t = threadIdx.x;
     if (f.node >= 0) ab += 72u;  // two child boxes read, one box written
     for (int dd = m.max_depth; dd >= 0; dd--) {
@@ -939,7 +1019,8 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           }
         }
         if (rank == 0)
-          team_flush_mark(m, ntouch, s_cl, s_par, reinterpret_cast<unsigned int*>(s_pass), s_coff, s_idx, sh, fst);
+          team_flush_mark(m, ntouch, s_cl, s_par, reinterpret_cast<unsigned int*>(s_pass), s_coff, s_idx,
+                          s_scr.flush, sh, fst);
       }
       team_bytes(a, kPhUpdate, ab);
       team_sync(cluster, C);
