@@ -98,6 +98,9 @@ struct sgpu_mesh {
   int* t_tools = nullptr;
   int* t_counter = nullptr;
   size_t t_dab_cap = 0, t_tool_cap = 0, t_mesh_cap = 0, t_job_cap = 0, t_counter_cap = 0;
+  // page-locked displaced counters of the last persistent launch
+  unsigned long long* h_disp = nullptr;
+  size_t h_disp_cap = 0;
 
   cudaEvent_t prof_event() {
     if (ev_used == ev_pool.size()) {
@@ -164,6 +167,9 @@ struct sgpu_mesh {
     t_dabs = nullptr;
     t_tools = nullptr;
     t_counter = nullptr;
+    if (h_disp) cudaFreeHost(h_disp);
+    h_disp = nullptr;
+    h_disp_cap = 0;
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev_h0) cudaEventDestroy(ev_h0);
@@ -452,9 +458,11 @@ int enqueue_stroke(Launcher& L, const SGPU_Brush* brush, const SGPU_Dab* dabs, i
 int run_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
                const int* dab_tools, int mode, int* launches_out);
 int finish_stroke(sgpu_mesh* mesh, int mode, int launches, SGPU_StrokeStats* stats);
+// wait = false: enqueue only (launch, then the displaced counters into the
+// first mesh's h_disp); the caller synchronizes and reads them.
 int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_Dab* dabs,
                const int* offs, const int* tools, int cluster, cudaStream_t s,
-               SGPU_StrokeStats* stats, float* total_ms);
+               SGPU_StrokeStats* stats, float* total_ms, bool wait = true);
 // Profiling counters handed to the next persistent launch (nullptr otherwise).
 thread_local unsigned long long* g_team_prof_bytes = nullptr;
 thread_local unsigned long long* g_team_phase_ns = nullptr;
@@ -1130,10 +1138,11 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
      "upload verts");
   CK(launch_gather_f4(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
   if (vert_normals_in) {
-    CK(cudaMemcpy2DAsync(d.scratch2, sizeof(float4), vert_normals_in, 3 * sizeof(float),
-                         3 * sizeof(float), d.totvert, cudaMemcpyHostToDevice, mesh->stream),
+    float* flat = reinterpret_cast<float*>(d.scratch2);
+    CK(cudaMemcpyAsync(flat, vert_normals_in, 3 * sizeof(float) * d.totvert, cudaMemcpyHostToDevice,
+                       mesh->stream),
        "upload normals");
-    CK(launch_gather_xyz(d.no, d.scratch2, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
+    CK(launch_xyz_to_f4(d.no, flat, mesh->d_n2o, d.totvert, true, mesh->stream), "gather kernel");
   }
   // New positions: every leaf box is refit and flushed before the stroke.
   CK(launch_mark_all(d, kUpdateBB | kUpdateOriginalBB, mesh->stream), "mark kernel");
@@ -1146,7 +1155,7 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
     sgpu_mesh* one[1] = {mesh};
     float total = 0.0f;
     if ((rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh->team_cluster, mesh->stream,
-                         &inner, &total)))
+                         &inner, &total, false)))
       return rc;
     launches += 1;
   } else {
@@ -1163,12 +1172,13 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
     CK(cudaMemcpyAsync(&displaced, &d.work->displaced, sizeof(displaced), cudaMemcpyDeviceToHost,
                        mesh->stream),
        "read counter");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  if (mode == SGPU_STROKE_TEAM) displaced = mesh->h_disp[0];
   if ((rc = device_err(mesh))) return rc;
   if (stats) {
     float ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, mesh->ev_h0, mesh->ev_h1), "elapsed");
-    stats->verts_displaced =
-        mode == SGPU_STROKE_TEAM ? inner.verts_displaced : static_cast<int64_t>(displaced);
+    stats->verts_displaced = static_cast<int64_t>(displaced);
     stats->gpu_ms = ms;
     stats->kernel_launches = launches;
     stats->graph_nodes = mode == SGPU_STROKE_GRAPH ? mesh->g_nodes : 0;
@@ -1416,13 +1426,10 @@ int sgpu_get_positions(sgpu_mesh* mesh, float* out_xyz) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   const DevMesh& d = mesh->dev;
-  const float4* src = d.co;
-  if (mesh->d_o2n) {
-    CK(launch_gather_f4(d.scratch, d.co, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
-    src = d.scratch;
-  }
-  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), src, sizeof(float4), 3 * sizeof(float),
-                       d.totvert, cudaMemcpyDeviceToHost, mesh->stream),
+  float* flat = reinterpret_cast<float*>(d.scratch);
+  CK(launch_f4_to_xyz(flat, d.co, mesh->d_o2n, d.totvert, mesh->stream), "pack kernel");
+  CK(cudaMemcpyAsync(out_xyz, flat, 3 * sizeof(float) * d.totvert, cudaMemcpyDeviceToHost,
+                     mesh->stream),
      "download positions");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1432,12 +1439,10 @@ int sgpu_set_positions(sgpu_mesh* mesh, const float* xyz) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   const DevMesh& d = mesh->dev;
-  float4* dst = mesh->d_n2o ? d.scratch : d.co;
-  CK(cudaMemcpy2DAsync(dst, sizeof(float4), xyz, 3 * sizeof(float), 3 * sizeof(float), d.totvert,
-                       cudaMemcpyHostToDevice, mesh->stream),
+  float* flat = reinterpret_cast<float*>(d.scratch);
+  CK(cudaMemcpyAsync(flat, xyz, 3 * sizeof(float) * d.totvert, cudaMemcpyHostToDevice, mesh->stream),
      "upload positions");
-  if (mesh->d_n2o)
-    CK(launch_gather_xyz(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
+  CK(launch_xyz_to_f4(d.co, flat, mesh->d_n2o, d.totvert, true, mesh->stream), "unpack kernel");
   CK(launch_chunk_boxes_all(mesh->dev, mesh->nchunks, mesh->stream), "chunk box kernel");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1447,13 +1452,10 @@ int sgpu_get_normals(sgpu_mesh* mesh, float* out_xyz) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   const DevMesh& d = mesh->dev;
-  const float4* src = d.no;
-  if (mesh->d_o2n) {
-    CK(launch_gather_f4(d.scratch, d.no, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
-    src = d.scratch;
-  }
-  CK(cudaMemcpy2DAsync(out_xyz, 3 * sizeof(float), src, sizeof(float4), 3 * sizeof(float),
-                       d.totvert, cudaMemcpyDeviceToHost, mesh->stream),
+  float* flat = reinterpret_cast<float*>(d.scratch);
+  CK(launch_f4_to_xyz(flat, d.no, mesh->d_o2n, d.totvert, mesh->stream), "pack kernel");
+  CK(cudaMemcpyAsync(out_xyz, flat, 3 * sizeof(float) * d.totvert, cudaMemcpyDeviceToHost,
+                     mesh->stream),
      "download normals");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
@@ -1580,7 +1582,7 @@ int ensure_dev(T** p, size_t* cap, size_t n) {
 // estimated work, longest first, and taken by cluster teams from a counter.
 int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_Dab* dabs,
                const int* offs, const int* tools, int cluster, cudaStream_t s,
-               SGPU_StrokeStats* stats, float* total_ms) {
+               SGPU_StrokeStats* stats, float* total_ms, bool wait) {
   sgpu_mesh* m0 = meshes[0];
   int max_nodes = 0, max_leaves = 0;
   for (int i = 0; i < n; i++) {
@@ -1656,11 +1658,21 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.phase_ns = g_team_phase_ns;
   CK(launch_team_stroke(a, cluster, s), "persistent stroke kernel");
   CK(cudaEventRecord(m0->ev1, s), "event");
-  std::vector<unsigned long long> disp(n, 0);
+  if (m0->h_disp_cap < static_cast<size_t>(n)) {
+    if (m0->h_disp) cudaFreeHost(m0->h_disp);
+    m0->h_disp = nullptr;
+    m0->h_disp_cap = 0;
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&m0->h_disp), sizeof(unsigned long long) * n,
+                     cudaHostAllocDefault),
+       "cudaHostAlloc");
+    m0->h_disp_cap = static_cast<size_t>(n);
+  }
+  unsigned long long* disp = m0->h_disp;
   for (int i = 0; i < n; i++)
     CK(cudaMemcpyAsync(&disp[i], &meshes[i]->dev.work->displaced, sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, s),
        "read counter");
+  if (!wait) return SGPU_OK;
   CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   float ms = 0.0f;
   CK(cudaEventElapsedTime(&ms, m0->ev0, m0->ev1), "elapsed");

@@ -635,18 +635,29 @@ cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s) {
 }
 
 // Conversions between a caller's vertex order and the device order:
-// out[i] = in[idx[i]] (whole float4, one float, or xyz with out.w kept).
+// out[i] = in[idx[i]] (whole float4 or one float).
 __global__ void k_gather_f4(float4* out, const float4* in, const int* idx, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = in[idx[i]];
 }
 __global__ void k_gather_f1(float* out, const float* in, const int* idx, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = in[idx[i]];
 }
-__global__ void k_gather_xyz(float4* out, const float4* in, const int* idx, int n) {
+
+// Packed xyz (3 floats per vertex, the caller's layout) to and from the
+// float4 device arrays, through an optional order map (idx, nullable).
+__global__ void k_xyz_to_f4(float4* out, const float* in3, const int* idx, int n, int keep_w) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 a = in[idx[i]];
-    const float w = out[i].w;
-    out[i] = make_float4(a.x, a.y, a.z, w);
+    const size_t j = 3 * static_cast<size_t>(idx ? idx[i] : i);
+    out[i] = make_float4(in3[j], in3[j + 1], in3[j + 2], keep_w ? out[i].w : 0.0f);
+  }
+}
+__global__ void k_f4_to_xyz(float* out3, const float4* in, const int* idx, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 a = in[idx ? idx[i] : i];
+    const size_t j = 3 * static_cast<size_t>(i);
+    out3[j] = a.x;
+    out3[j + 1] = a.y;
+    out3[j + 2] = a.z;
   }
 }
 
@@ -664,8 +675,13 @@ cudaError_t launch_gather_f1(float* out, const float* in, const int* idx, int n,
   k_gather_f1<<<gather_grid(n), kThreads, 0, s>>>(out, in, idx, n);
   return cudaGetLastError();
 }
-cudaError_t launch_gather_xyz(float4* out, const float4* in, const int* idx, int n, cudaStream_t s) {
-  k_gather_xyz<<<gather_grid(n), kThreads, 0, s>>>(out, in, idx, n);
+cudaError_t launch_xyz_to_f4(float4* out, const float* in3, const int* idx, int n, bool keep_w,
+                             cudaStream_t s) {
+  k_xyz_to_f4<<<gather_grid(n), kThreads, 0, s>>>(out, in3, idx, n, keep_w ? 1 : 0);
+  return cudaGetLastError();
+}
+cudaError_t launch_f4_to_xyz(float* out3, const float4* in, const int* idx, int n, cudaStream_t s) {
+  k_f4_to_xyz<<<gather_grid(n), kThreads, 0, s>>>(out3, in, idx, n);
   return cudaGetLastError();
 }
 

@@ -15,6 +15,9 @@
 // (sgpu_device.cuh), so results are bit-identical to them and to the FP32
 // restatement of the reference.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -1117,13 +1120,32 @@ static cudaLaunchConfig_t team_config(int cluster, int nteams, size_t smem, cuda
   return cfg;
 }
 
+// Resident clusters of one build for (cluster size, shared memory), cached
+// per device so that a launch makes no occupancy query.
 template <int kMinBlocks>
 static int active_clusters(int cluster, size_t smem) {
-  if (configure_team_kernel<kMinBlocks>(smem) != cudaSuccess) return 0;
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, size_t>, int> cache;
+  static std::map<int, size_t> configured;  // per device: largest smem set so far
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(dev, cluster, smem);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    if (configured[dev] < smem) {
+      if (configure_team_kernel<kMinBlocks>(smem) != cudaSuccess) return 0;
+      configured[dev] = smem;
+    }
+    return it->second;
+  }
+  if (configure_team_kernel<kMinBlocks>(std::max(smem, configured[dev])) != cudaSuccess) return 0;
+  configured[dev] = std::max(smem, configured[dev]);
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = team_config(cluster, 1, smem, nullptr, attr);
   int n = 0;
   if (cudaOccupancyMaxActiveClusters(&n, k_team_stroke<kMinBlocks>, &cfg) != cudaSuccess) return 0;
+  cache[key] = n;
   return n;
 }
 

@@ -33,10 +33,14 @@ cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s);
 cudaError_t launch_mark_all(const DevMesh& m, int bits, cudaStream_t s);
 // Refit-chunk boxes of every leaf from the current positions.
 cudaError_t launch_chunk_boxes_all(const DevMesh& m, int nchunks, cudaStream_t s);
-// out[i] = in[idx[i]]: float4, float, or xyz keeping out.w.
+// out[i] = in[idx[i]]: float4 or float.
 cudaError_t launch_gather_f4(float4* out, const float4* in, const int* idx, int n, cudaStream_t s);
 cudaError_t launch_gather_f1(float* out, const float* in, const int* idx, int n, cudaStream_t s);
-cudaError_t launch_gather_xyz(float4* out, const float4* in, const int* idx, int n, cudaStream_t s);
+// Packed xyz <-> float4: out[i] = in3[idx[i]] (idx nullable: identity);
+// out3[i] = in[idx[i]].xyz.
+cudaError_t launch_xyz_to_f4(float4* out, const float* in3, const int* idx, int n, bool keep_w,
+                             cudaStream_t s);
+cudaError_t launch_f4_to_xyz(float* out3, const float4* in, const int* idx, int n, cudaStream_t s);
 int cull_smem_limit();
 int grid_size_limit();
 void configure_kernels();
