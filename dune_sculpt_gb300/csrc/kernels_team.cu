@@ -148,68 +148,84 @@ __device__ unsigned long long team_block_scan64(unsigned long long v, unsigned l
   return warp_base + x - v;
 }
 
-__device__ __forceinline__ bool leaf_passes(const DevMesh& m, const int* s_par,
-                                            const unsigned char* s_pass, int id) {
-  const int node = m.leaf_node[id];
-  bool ok = s_pass[node];
-  int p = s_par[node];
-  while (ok && p >= 0) {
-    ok = s_pass[p];
-    p = s_par[p];
-  }
-  return ok;
-}
+// Per-job tables of the node search in shared memory.
+struct CullTabs {
+  const unsigned short* lnode;  // leaf -> node
+  const int* lnv;               // leaf -> brush-visible vertex count
+};
 
 // Node search of one pass into this CTA's shared memory (every CTA of the team
-// computes the same list).  Same test and order as k_cull: every node box is
-// tested, then each thread owns a run of consecutive leaves, and one block
-// scan of (count, vertex count) places each run's passing leaves.
+// computes the same list).  Same result and order as k_cull: a leaf is listed
+// when its box and the boxes of all its ancestors pass.  Every node box is
+// tested (kBox loads in flight per thread); a failing internal node covers
+// the leaf-id range of its subtree (left-first DFS ranks), recorded as +1/-1
+// in a difference array; a running sum over the leaves then says which
+// leaves lie under a failing ancestor.  Each thread owns a run of consecutive
+// leaves (at most 64: the team kernel takes at most 64 * 256 leaves); block
+// scans give the coverage entering the run and the list positions.  s_coff
+// doubles as the difference array.
+template <int kBox>
 __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_par,
-                          unsigned char* s_pass, int* s_cl, int* s_coff, TeamShared& sh) {
+                          unsigned char* s_pass, int* s_cl, int* s_coff, const CullTabs& ct,
+                          TeamShared& sh) {
   const float4* bb = pp.original ? m.orig_vb : m.vb;
-  constexpr int kBoxBatch = 2;  // node boxes loaded together
-  for (int n0 = threadIdx.x; n0 < m.totnode; n0 += kBoxBatch * kTeamThreads) {
-    float4 lo[kBoxBatch], hi[kBoxBatch];
+  const int L = m.nleaf;
+  for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
+  __syncthreads();
+  for (int n0 = threadIdx.x; n0 < m.totnode; n0 += kBox * kTeamThreads) {
+    float4 lo[kBox], hi[kBox];
+    int llo[kBox], lhi[kBox];
 #pragma unroll
-    for (int j = 0; j < kBoxBatch; j++) {
+    for (int j = 0; j < kBox; j++) {
       const int n = n0 + j * kTeamThreads;
       if (n < m.totnode) {
         lo[j] = __ldcg(&bb[2 * n]);
         hi[j] = __ldcg(&bb[2 * n + 1]);
+        llo[j] = m.node_leaf_lo[n];
+        lhi[j] = m.node_leaf_hi[n];
       }
     }
 #pragma unroll
-    for (int j = 0; j < kBoxBatch; j++) {
+    for (int j = 0; j < kBox; j++) {
       const int n = n0 + j * kTeamThreads;
-      if (n < m.totnode) s_pass[n] = box_hits(lo[j], hi[j], pp.loc, pp.cull_radius_sq);
+      if (n >= m.totnode) continue;
+      const bool hit = box_hits(lo[j], hi[j], pp.loc, pp.cull_radius_sq);
+      s_pass[n] = hit;
+      if (!hit && lhi[j] - llo[j] > 1) {  // internal node (leaves own a range of one)
+        atomicAdd(&s_coff[llo[j]], 1);
+        atomicAdd(&s_coff[lhi[j]], -1);
+      }
     }
   }
   __syncthreads();
-  const int L = m.nleaf;
   const int seg = (L + kTeamThreads - 1) / kTeamThreads;
-  const int l0 = min(L, threadIdx.x * seg), l1 = min(L, l0 + seg);
+  const int l0 = min(L, static_cast<int>(threadIdx.x) * seg), l1 = min(L, l0 + seg);
+  int dsum = 0;
+  for (int id = l0; id < l1; id++) dsum += s_coff[id];
+  int dtot;
+  int cov = team_block_scan(dsum, &dtot, sh.scan);
   unsigned long long okmask = 0ull;
   unsigned long long cnt = 0ull, nvs = 0ull;
   for (int id = l0; id < l1; id++) {
-    if (leaf_passes(m, s_par, s_pass, id)) {
+    cov += s_coff[id];
+    if (cov == 0 && s_pass[ct.lnode[id]]) {
       cnt++;
-      nvs += static_cast<unsigned long long>(leaf_nverts(m, id));
-      if (id - l0 < 64) okmask |= 1ull << (id - l0);
+      nvs += static_cast<unsigned long long>(ct.lnv[id]);
+      okmask |= 1ull << (id - l0);
     }
   }
   // (vertex count << 24) | leaf count: leaves < 2^24, vertices < 2^31
   unsigned long long total;
   const unsigned long long excl = team_block_scan64((nvs << 24) | cnt, &total, sh.scan64);
+  // the scan's barriers separate the reads of s_coff above from the writes below
   int pos = static_cast<int>(excl & 0xFFFFFFull);
   int voff = static_cast<int>(excl >> 24);
   for (int id = l0; id < l1; id++) {
-    const bool ok = (id - l0 < 64) ? ((okmask >> (id - l0)) & 1ull) != 0ull
-                                   : leaf_passes(m, s_par, s_pass, id);
-    if (!ok) continue;
+    if (!((okmask >> (id - l0)) & 1ull)) continue;
     s_cl[pos] = id;
     s_coff[pos] = voff;
     pos++;
-    voff += leaf_nverts(m, id);
+    voff += ct.lnv[id];
   }
   if (threadIdx.x == 0) {
     sh.cnt = static_cast<int>(total & 0xFFFFFFull);
@@ -657,10 +673,13 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
   int* s_par = reinterpret_cast<int*>(s_nbc + kNbCache * kTeamThreads);
   int* s_cl = s_par + a.max_nodes;
   int* s_coff = s_cl + a.max_leaves + 1;
-  unsigned short* s_idx = reinterpret_cast<unsigned short*>(s_coff + a.max_leaves + 2);
+  int* s_lnv = s_coff + a.max_leaves + 2;
+  unsigned short* s_idx = reinterpret_cast<unsigned short*>(s_lnv + a.max_leaves);
+  unsigned short* s_lnode = s_idx + ((a.max_nodes + 1) & ~1);
   // node marks; also the flush's claim bitmap (32-bit words): the ushort
-  // array before it has an even length, so this starts 4-byte aligned
-  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_idx + ((a.max_nodes + 1) & ~1));
+  // arrays before it have even lengths, so this starts 4-byte aligned
+  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_lnode + ((a.max_leaves + 1) & ~1));
+  const CullTabs ct{s_lnode, s_lnv};
   PhaseClock clk;
   clk.last = a.phase_ns ? global_ns() : 0ull;
 
@@ -690,6 +709,10 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
     for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) {
       s_par[i] = m.node_parent[i];
       s_idx[i] = kNoPos;
+    }
+    for (int k = threadIdx.x; k < m.nleaf; k += kTeamThreads) {
+      s_lnode[k] = static_cast<unsigned short>(m.leaf_node[k]);
+      s_lnv[k] = leaf_nverts(m, k);
     }
     // GRIDS work-list stamps: dab d uses epoch grid_epoch0 + d + 1
     const unsigned int grid_epoch0 = __ldcg(&w->grid_epoch);
@@ -747,7 +770,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         pp.original = sh.job.use_orig;
         pp.iter_strength = 1.0f;
         pp.iteration = 0;
-        team_cull(m, pp, s_par, s_pass, s_cl, s_coff, sh);
+        team_cull<kMinBlocks == 1 ? 8 : 2>(m, pp, s_par, s_pass, s_cl, s_coff, ct, sh);
         const int cnt = sh.cnt, total = sh.total;
         // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
         team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
@@ -1082,15 +1105,16 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
   }
 }
 
-// Dynamic shared memory: smooth neighbour tables (float4), parents, culled
-// list and offsets (int), flush positions (ushort, even count), node marks
-// (byte; at least the claim bitmap's 32-bit words).
+// Dynamic shared memory: smooth neighbour tables (float4); parents, culled
+// list and offsets, leaf vertex counts (int); flush positions, leaf nodes
+// (ushort, even counts); node marks (byte; at least the claim bitmap's
+// 32-bit words).
 size_t team_smem_bytes(int max_nodes, int max_leaves) {
-  const size_t n = static_cast<size_t>(max_nodes);
+  const size_t n = static_cast<size_t>(max_nodes), l = static_cast<size_t>(max_leaves);
+  const size_t even_n = (n + 1) & ~static_cast<size_t>(1), even_l = (l + 1) & ~static_cast<size_t>(1);
   const size_t marks = std::max(n, 4 * ((n + 31) / 32));
-  const size_t b = sizeof(float4) * kNbCache * kTeamThreads +
-                   sizeof(int) * (n + 2 * static_cast<size_t>(max_leaves) + 3) +
-                   sizeof(unsigned short) * ((n + 1) & ~static_cast<size_t>(1)) + marks;
+  const size_t b = sizeof(float4) * kNbCache * kTeamThreads + sizeof(int) * (n + 3 * l + 3) +
+                   sizeof(unsigned short) * (even_n + even_l) + marks;
   return (b + 15) & ~static_cast<size_t>(15);
 }
 
