@@ -13,9 +13,16 @@
  * The GPU product never links or calls it.
  *
  * Parity pinning: the reference ships no tests, fixtures or golden vectors for
- * this path and cannot be compiled (its public headers are missing), so parity
- * of this restatement against the reference itself is unpinned; it is pinned
- * against known-answer tests written from the reference's own definitions.
+ * this path and does not build as shipped (its public headers are missing).
+ * oracle/refpin compiles the reference's own pbvh.c, poly-normal, vector-math
+ * and colortools.c code from the reference tree behind stand-in headers, and
+ * tests/test_refpin.py checks this restatement against it: PBVH build, node
+ * search and bounding boxes bit for bit, vertex normals within 1e-6 (the
+ * reference's float atomics add in task order), falloff tables and curve
+ * evaluation bit for bit.  The brush math has no reference code (sculpt.c is
+ * missing) and the multires normal/seam code needs OpenSubdiv: those parts
+ * stay pinned only by known-answer tests written from the reference's
+ * definitions.
  */
 #ifndef ORACLE_H
 #define ORACLE_H
@@ -90,6 +97,8 @@ int or_brush_pass(OrMesh *m, const OrBrush *b, const float location[3],
 void or_update_normals(OrMesh *m);
 void or_update_bounds(OrMesh *m, int flag);
 void or_node_mark_update(OrMesh *m, int node);
+void or_vert_mark_update(OrMesh *m, int vertex);
+void or_get_vert_tags(const OrMesh *m, unsigned char *out);
 
 /* Whole stroke: per dab, symmetry passes (search + brush), normals, bounds(UpdateBB);
  * bounds(UpdateOriginalBB) at the end.  which: 1 = FP32, 2 = FP64, 3 = both.

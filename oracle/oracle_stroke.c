@@ -70,6 +70,20 @@ void or_node_mark_update(OrMesh *m, int node)
   }
 }
 
+/* BKE_pbvh_vert_mark_update (pbvh.c:3729): tag one vertex for the normal update. */
+void or_vert_mark_update(OrMesh *m, int vertex)
+{
+  if (vertex >= 0 && vertex < m->totvert) {
+    m->vtag[vertex] = 1;
+  }
+}
+
+/* The vert_bitmap tags (one byte per vertex, 0 or 1). */
+void or_get_vert_tags(const OrMesh *m, unsigned char *out)
+{
+  memcpy(out, m->vtag, (size_t)m->totvert);
+}
+
 int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
                   const int *dab_tools, int which, int nthreads, int64_t *per_dab_counts)
 {

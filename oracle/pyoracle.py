@@ -58,6 +58,8 @@ def lib():
         L.or_update_normals.argtypes = [vp]
         L.or_update_bounds.argtypes = [vp, i]
         L.or_node_mark_update.argtypes = [vp, i]
+        L.or_vert_mark_update.argtypes = [vp, i]
+        L.or_get_vert_tags.argtypes = [vp, vp]
         L.or_stroke.restype = C.c_int64
         L.or_stroke.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
         L.or_curve_table.argtypes = [i, vp, vp]
@@ -232,6 +234,17 @@ class OracleMesh:
 
     def update_normals(self):
         lib().or_update_normals(self.h)
+
+    def node_mark_update(self, node: int):
+        lib().or_node_mark_update(self.h, int(node))
+
+    def vert_mark_update(self, vertex: int):
+        lib().or_vert_mark_update(self.h, int(vertex))
+
+    def vert_tags(self) -> np.ndarray:
+        out = np.zeros(self.num_verts, dtype=np.uint8)
+        lib().or_get_vert_tags(self.h, _p(out))
+        return out
 
     def update_bounds(self, flag: int):
         lib().or_update_bounds(self.h, flag)

@@ -1,0 +1,202 @@
+"""ctypes binding of the reference-pinning harness (oracle/_ref/librefpin.so).
+
+TEST INFRASTRUCTURE ONLY.  The library is the reference's own pbvh.c (and the
+poly-normal / vector-math code it calls) compiled from the reference tree by
+oracle/refpin/Makefile; tests use it to check the oracle's restatement of the
+PBVH build, node search, normal update and bounding-box refit against the
+reference itself.  It can only be built where the reference tree is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_DIR = os.path.join(_HERE, "refpin")
+_LIB_PATH = os.path.join(_HERE, "_ref", "librefpin.so")
+REFERENCE_ROOT = os.environ.get("DUNE_SCULPT_REFERENCE", "/root/reference")
+_lib = None
+
+
+def available() -> bool:
+    """True when the library exists or the reference tree is here to build it."""
+    return os.path.exists(_LIB_PATH) or os.path.isdir(os.path.join(REFERENCE_ROOT, "source"))
+
+
+def build() -> str:
+    if os.path.isdir(os.path.join(REFERENCE_ROOT, "source")):
+        subprocess.run(["make", "-s", "-C", _DIR, f"REF={REFERENCE_ROOT}"], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        vp, i, f = C.c_void_p, C.c_int, C.c_float
+        L.rp_build_faces.restype = vp
+        L.rp_build_faces.argtypes = [vp, i, vp, i, vp, i, vp, i, vp, vp]
+        L.rp_build_grids.restype = vp
+        L.rp_build_grids.argtypes = [i, i, vp, vp, vp]
+        L.rp_free.argtypes = [vp]
+        L.rp_set_leaf_limit.argtypes = [i]
+        for name in ("rp_num_nodes", "rp_leaf_limit"):
+            getattr(L, name).restype = i
+            getattr(L, name).argtypes = [vp]
+        L.rp_get_nodes.argtypes = [vp] + [vp] * 6
+        L.rp_get_prim_indices.argtypes = [vp, vp]
+        L.rp_get_node_vert_indices.argtypes = [vp, i, vp]
+        L.rp_get_node_face_vert_indices.argtypes = [vp, i, vp]
+        L.rp_get_bbs.argtypes = [vp, vp, vp]
+        L.rp_search_sphere.restype = i
+        L.rp_search_sphere.argtypes = [vp, vp, f, i, vp]
+        L.rp_set_co.argtypes = [vp, vp]
+        L.rp_set_grid_co.argtypes = [vp, vp]
+        L.rp_get_no.argtypes = [vp, vp]
+        L.rp_node_mark_update.argtypes = [vp, i]
+        L.rp_vert_mark_update.argtypes = [vp, i]
+        L.rp_update_normals.argtypes = [vp]
+        L.rp_update_bounds.argtypes = [vp, i]
+        L.rp_node_flag.restype = i
+        L.rp_node_flag.argtypes = [vp, i]
+        L.rp_curve_table.argtypes = [i, vp, vp]
+        L.rp_curve_evaluate.argtypes = [i, vp, i, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def curve_table(preset: int):
+    """The brush falloff table built by the reference's colortools.c."""
+    t = np.zeros((257, 2), dtype=np.float32)
+    p = np.zeros(7, dtype=np.float32)
+    lib().rp_curve_table(preset, _p(t), _p(p))
+    return t, p
+
+
+def curve_evaluate(preset: int, values) -> np.ndarray:
+    """KERNEL_curvemapping_evaluateF of the brush curve (colortools.c:964-980)."""
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    out = np.zeros_like(v)
+    lib().rp_curve_evaluate(preset, _p(v), v.shape[0], _p(out))
+    return out
+
+
+class RefPBVH:
+    """One PBVH built and updated by the reference's own compiled code."""
+
+    def __init__(self, handle, keep, totvert: int):
+        self.h = handle
+        self._keep = keep
+        self.totvert = totvert
+
+    @classmethod
+    def faces(cls, m, vert_normals: np.ndarray, leaf_limit: int = 10000):
+        """BKE_pbvh_build_mesh; leaf_limit replaces pbvh.c's LEAF_LIMIT (10000)."""
+        lib().rp_set_leaf_limit(leaf_limit)
+        no = np.ascontiguousarray(vert_normals, dtype=np.float32)
+        mask = None if m.mask is None else np.ascontiguousarray(m.mask, dtype=np.float32)
+        h = lib().rp_build_faces(_p(m.verts), m.verts.shape[0], _p(m.polys), m.polys.shape[0],
+                                 _p(m.loops), m.loops.shape[0], _p(m.looptris),
+                                 m.looptris.shape[0], _p(no), _p(mask))
+        return cls(h, (m, no, mask), m.verts.shape[0])
+
+    @classmethod
+    def grids(cls, num_grids: int, grid_size: int, co, no, mask=None, leaf_limit: int = 10000):
+        """BKE_pbvh_build_grids: leaves of max(leaf_limit / grid_size^2, 1) grids."""
+        lib().rp_set_leaf_limit(leaf_limit)
+        co = np.ascontiguousarray(co, dtype=np.float32)
+        no = np.ascontiguousarray(no, dtype=np.float32)
+        mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        h = lib().rp_build_grids(num_grids, grid_size, _p(co), _p(no), _p(mask))
+        return cls(h, (co, no, mask), co.shape[0])
+
+    def close(self):
+        if self.h:
+            lib().rp_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_nodes(self) -> int:
+        return lib().rp_num_nodes(self.h)
+
+    @property
+    def leaf_limit(self) -> int:
+        return lib().rp_leaf_limit(self.h)
+
+    def nodes(self) -> dict:
+        n = self.num_nodes
+        keys = ("children_offset", "flag", "prim_off", "totprim", "uniq", "face_verts")
+        arrs = {k: np.zeros(n, dtype=np.int32) for k in keys}
+        lib().rp_get_nodes(self.h, *[_p(arrs[k]) for k in keys])
+        return arrs
+
+    def prim_indices(self) -> np.ndarray:
+        tot = int(self.nodes()["totprim"].sum())
+        out = np.zeros(max(tot, 1), dtype=np.int32)
+        lib().rp_get_prim_indices(self.h, _p(out))
+        return out[:tot]
+
+    def node_vert_indices(self, node: int) -> np.ndarray:
+        nd = self.nodes()
+        n = int(nd["uniq"][node] + nd["face_verts"][node])
+        out = np.zeros(max(n, 1), dtype=np.int32)
+        lib().rp_get_node_vert_indices(self.h, node, _p(out))
+        return out[:n]
+
+    def node_face_vert_indices(self, node: int) -> np.ndarray:
+        n = int(self.nodes()["totprim"][node])
+        out = np.zeros((max(n, 1), 3), dtype=np.int32)
+        lib().rp_get_node_face_vert_indices(self.h, node, _p(out))
+        return out[:n]
+
+    def bbs(self):
+        n = self.num_nodes
+        vb = np.zeros((n, 6), dtype=np.float32)
+        ovb = np.zeros((n, 6), dtype=np.float32)
+        lib().rp_get_bbs(self.h, _p(vb), _p(ovb))
+        return vb, ovb
+
+    def search_sphere(self, center, radius_sq: float, original: int = 0) -> np.ndarray:
+        out = np.zeros(self.num_nodes + 1, dtype=np.int32)
+        c = np.asarray(center, dtype=np.float32)
+        n = lib().rp_search_sphere(self.h, _p(c), radius_sq, original, _p(out))
+        return out[:n]
+
+    def set_co(self, co: np.ndarray):
+        co = np.ascontiguousarray(co, dtype=np.float32)
+        lib().rp_set_co(self.h, _p(co))
+
+    def set_grid_co(self, co: np.ndarray):
+        co = np.ascontiguousarray(co, dtype=np.float32)
+        lib().rp_set_grid_co(self.h, _p(co))
+
+    def no(self) -> np.ndarray:
+        out = np.zeros((self.totvert, 3), dtype=np.float32)
+        lib().rp_get_no(self.h, _p(out))
+        return out
+
+    def node_mark_update(self, node: int):
+        lib().rp_node_mark_update(self.h, int(node))
+
+    def vert_mark_update(self, vertex: int):
+        lib().rp_vert_mark_update(self.h, int(vertex))
+
+    def update_normals(self):
+        lib().rp_update_normals(self.h)
+
+    def update_bounds(self, flag: int):
+        lib().rp_update_bounds(self.h, flag)

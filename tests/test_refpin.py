@@ -1,0 +1,327 @@
+"""The oracle against the reference's own compiled PBVH code (CPU).
+
+oracle/refpin compiles the reference's pbvh.c (complete copy, pbvh.c:1913-4986),
+BKE_mesh_calc_poly_normal (mesh_evaluate.c:39-86), normal_tri_v3 /
+normal_quad_v3 (math_geom.cc:31-68) and its inline vector math from the
+reference tree, behind stand-ins for the headers the reference does not ship.
+These tests check, on the same inputs, that the oracle's restatement gives
+
+* the same PBVH (BKE_pbvh_build_mesh / _build_grids): node table, prim order,
+  per-leaf vertex lists with the unique/shared split, node boxes — bit for bit;
+* the same node lists from BKE_pbvh_search_gather with the sphere callback,
+  over vb and orig_vb — exactly;
+* the same boxes after BKE_pbvh_update_bounds (UpdateBB, UpdateOriginalBB) —
+  bit for bit;
+* the same vertex normals after BKE_pbvh_update_normals within 1e-6 absolute
+  (unit vectors): the reference adds face normals with float atomics in task
+  order, the oracle in ascending looptri order with compensated sums, so the
+  last bit may differ.
+
+The replay tests drive whole oracle strokes (draw, smooth, inflate, clay
+strips; X symmetry) and, after every dab, hand the oracle's positions, vertex
+tags and culled nodes to the reference's update code.
+
+They need the reference tree (to build oracle/_ref/librefpin.so) and skip
+without it.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import pyrefpin
+from dune_sculpt_gb300 import synth
+from helpers import bits_equal, first_diff, small_icosphere, small_uvsphere
+
+pytestmark = pytest.mark.skipif(not pyrefpin.available(),
+                                reason="reference tree absent: the pinning library cannot be built")
+
+LEAF = 1          # PBVH_Leaf
+UPD_BB = 4        # PBVH_UpdateBB
+UPD_ORIG_BB = 8   # PBVH_UpdateOriginalBB
+NORMAL_ATOL = 1e-6
+
+
+def ngon_mesh(nq: int = 120) -> synth.FacesMesh:
+    """A grid whose quads are merged in pairs into hexagons (n-gon polys,
+    fan looptris), with a few triangles and quads left over at the row ends,
+    and a smooth height field so the Newell normals are not all +Z."""
+    n = nq + 1
+    j, i = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    x = i.reshape(-1) / nq
+    y = j.reshape(-1) / nq
+    z = 0.05 * np.sin(6.0 * x) * np.cos(5.0 * y)
+    co = synth._f32(np.stack([x, y, z], 1))
+    polys = []
+    for qj in range(nq):
+        qi = 0
+        while qi < nq:
+            v00 = qj * n + qi
+            if qi + 1 < nq and (qi + qj) % 5 != 4:
+                polys.append([v00, v00 + 1, v00 + 2, v00 + 2 + n, v00 + 1 + n, v00 + n])
+                qi += 2
+            else:
+                polys.append([v00, v00 + 1, v00 + 1 + n])
+                polys.append([v00, v00 + 1 + n, v00 + n])
+                qi += 1
+    P = len(polys)
+    sizes = np.array([len(p) for p in polys], dtype=np.int32)
+    verts = np.zeros(n * n, dtype=synth.MVERT_DT)
+    verts["co"] = co
+    mp = np.zeros(P, dtype=synth.MPOLY_DT)
+    mp["totloop"] = sizes
+    mp["loopstart"] = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int32)
+    mp["flag"] = 1
+    loops = np.zeros(int(sizes.sum()), dtype=synth.MLOOP_DT)
+    loops["v"] = np.concatenate(polys).astype(np.uint32)
+    tris = []
+    for p, ls in enumerate(mp["loopstart"]):
+        for k in range(1, sizes[p] - 1):
+            tris.append((ls, ls + k, ls + k + 1, p))
+    lt = np.zeros(len(tris), dtype=synth.MLOOPTRI_DT)
+    t = np.array(tris, dtype=np.uint32)
+    lt["tri"] = t[:, :3]
+    lt["poly"] = t[:, 3]
+    return synth.FacesMesh(verts=verts, polys=mp, loops=loops, looptris=lt, kind="ngon")
+
+
+def material_grid(nq: int = 96) -> synth.FacesMesh:
+    """A flat grid whose polys carry four materials in stripes and a flat/smooth
+    checker, so leaves are split by material (partition_indices_material)."""
+    m = synth.grid_mesh(nq)
+    p = np.arange(m.polys.shape[0])
+    m.polys["mat_nr"] = ((p % nq) * 4 // nq).astype(np.int16)
+    m.polys["flag"] = np.where((p // (nq * 8)) % 2 == 0, 1, 0).astype(m.polys["flag"].dtype)
+    return m
+
+
+MESHES = {
+    "grid": lambda: synth.grid_mesh(160),
+    "icosphere": lambda: small_icosphere(6),
+    "uvsphere": lambda: small_uvsphere(180),
+    "ngon": lambda: ngon_mesh(120),
+    "materials": lambda: material_grid(96),
+}
+
+
+def _pair(oracle, name, leaf_limit):
+    m = MESHES[name]()
+    o = oracle.OracleMesh.faces(m, leaf_limit)
+    o.recalc_all_normals()
+    r = pyrefpin.RefPBVH.faces(m, o.no(), leaf_limit)
+    return m, o, r
+
+
+def _assert_same_tree(o, r):
+    on, rn = o.nodes(), r.nodes()
+    assert o.num_nodes == r.num_nodes
+    for k in ("children_offset", "prim_off", "totprim", "uniq", "face_verts"):
+        assert np.array_equal(on[k], rn[k]), k
+    assert np.array_equal(on["flag"] & LEAF, rn["flag"] & LEAF)
+    assert np.array_equal(o.prim_indices(), r.prim_indices())
+    ov = o.vert_indices()
+    for n in np.nonzero(on["flag"] & LEAF)[0]:
+        cnt = on["uniq"][n] + on["face_verts"][n]
+        a = ov[on["vert_off"][n]:on["vert_off"][n] + cnt]
+        assert np.array_equal(a, r.node_vert_indices(int(n))), f"leaf {n}"
+    ovb, oovb = o.bbs()
+    rvb, rovb = r.bbs()
+    assert bits_equal(ovb, rvb), first_diff(ovb, rvb)
+    assert bits_equal(oovb, rovb), first_diff(oovb, rovb)
+
+
+@pytest.mark.parametrize("leaf_limit", [10000, 5000, 700])
+@pytest.mark.parametrize("name", list(MESHES))
+def test_build_matches_reference(oracle, name, leaf_limit):
+    _, o, r = _pair(oracle, name, leaf_limit)
+    assert r.leaf_limit == leaf_limit
+    _assert_same_tree(o, r)
+    assert int((o.nodes()["flag"] & LEAF).sum()) > 1
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+def test_search_matches_reference(oracle, name):
+    m, o, r = _pair(oracle, name, 5000)
+    co = m.verts["co"]
+    lo, hi = co.min(0), co.max(0)
+    rng = np.random.default_rng(7)
+    hits = 0
+    for _ in range(150):
+        c = rng.uniform(lo - 0.1, hi + 0.1).astype(np.float32)
+        rsq = np.float32(rng.uniform(0.0, 0.5 * float((hi - lo).max()))) ** 2
+        for orig in (0, 1):
+            a = o.search_sphere(c, rsq, orig)
+            b = r.search_sphere(c, rsq, orig)
+            assert np.array_equal(a, b), (c, rsq, orig, a, b)
+            hits += a.size
+    assert hits > 0
+    # empty and all-covering spheres, a zero radius on a vertex
+    assert r.search_sphere(hi + 10.0, np.float32(1.0)).size == 0
+    assert o.search_sphere(hi + 10.0, np.float32(1.0)).size == 0
+    big = np.float32(1e6)
+    assert np.array_equal(o.search_sphere(lo, big), r.search_sphere(lo, big))
+    assert np.array_equal(o.search_sphere(co[0], np.float32(0.0)),
+                          r.search_sphere(co[0], np.float32(0.0)))
+
+
+def _edit(o, r, co, center, rad, amp):
+    """Displace the vertices inside a sphere smoothly, tag them, mark the
+    culled nodes, in both; then the reference's and the oracle's updates."""
+    rsq = np.float32(rad) * np.float32(rad)
+    d2 = ((co - center) ** 2).sum(1)
+    inside = np.nonzero(d2 < rsq)[0]
+    fall = (np.float32(1) - d2[inside] / rsq).astype(np.float32)
+    co = co.copy()
+    co[inside] += (np.float32(amp) * fall)[:, None] * np.array([0.3, -0.2, 1.0], np.float32)
+    nodes = o.search_sphere(center, rsq, 0)
+    assert np.array_equal(nodes, r.search_sphere(center, rsq, 0))
+    o.set_co(co)
+    r.set_co(co)
+    for n in nodes:
+        o.node_mark_update(int(n))
+        r.node_mark_update(int(n))
+    for v in inside:
+        o.vert_mark_update(int(v))
+        r.vert_mark_update(int(v))
+    return co, inside
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+def test_update_normals_and_bounds_match_reference(oracle, name):
+    m, o, r = _pair(oracle, name, 5000)
+    co = o.co()
+    lo, hi = co.min(0), co.max(0)
+    rng = np.random.default_rng(11)
+    for step in range(4):
+        center = rng.uniform(lo, hi).astype(np.float32)
+        rad = 0.15 * float((hi - lo).max())
+        co, inside = _edit(o, r, co, center, rad, 0.02)
+        o.update_normals()
+        r.update_normals()
+        no_o, no_r = o.no(), r.no()
+        err = float(np.abs(no_o - no_r).max())
+        assert err <= NORMAL_ATOL, (step, err)
+        o.update_bounds(UPD_BB)
+        r.update_bounds(UPD_BB)
+        ovb, oovb = o.bbs()
+        rvb, rovb = r.bbs()
+        assert bits_equal(ovb, rvb), first_diff(ovb, rvb)
+        assert bits_equal(oovb, rovb), first_diff(oovb, rovb)
+        assert np.array_equal(o.nodes()["flag"] & 0xF, r.nodes()["flag"] & 0xF)
+    o.update_bounds(UPD_ORIG_BB)
+    r.update_bounds(UPD_ORIG_BB)
+    ovb, oovb = o.bbs()
+    rvb, rovb = r.bbs()
+    assert bits_equal(oovb, rovb), first_diff(oovb, rovb)
+    assert bits_equal(ovb, rvb)
+
+
+REPLAY = [
+    ("grid", synth.TOOL_DRAW, 0.05, 0.5, synth.CURVE_SMOOTH, 0),
+    ("icosphere", synth.TOOL_SMOOTH, 0.12, 0.7, synth.CURVE_SMOOTH, synth.SYMM_X),
+    ("uvsphere", synth.TOOL_CLAY_STRIPS, 0.1, 0.8, synth.CURVE_SHARP, synth.SYMM_X),
+    ("icosphere", synth.TOOL_INFLATE, 0.1, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X),
+    ("ngon", synth.TOOL_DRAW, 0.06, 0.9, synth.CURVE_SHARP, synth.SYMM_X),
+]
+
+
+@pytest.mark.parametrize("case", REPLAY, ids=[f"{c[0]}-tool{c[1]}" for c in REPLAY])
+def test_stroke_replay_in_reference(oracle, case):
+    """Every PBVH step of an oracle stroke re-run by the reference's code."""
+    name, tool, radius, strength, curve, symm = case
+    m, o, r = _pair(oracle, name, 5000)
+    if m.kind == "grid" or m.kind == "ngon":
+        dabs = synth.line_dabs(synth.SEED_BASE, 12)
+    else:
+        dabs = synth.arc_dabs(synth.SEED_BASE + 1, 12, 0.5 * radius)
+    st = synth.Stroke(tool, radius, strength, curve, symm, dabs)
+    scale = np.float32(1.41421356237309504880) if tool == synth.TOOL_CLAY_STRIPS else np.float32(1)
+    rr = np.float32(radius) * scale
+    rsq = rr * rr
+    moved = 0
+    for d in range(dabs.shape[0]):
+        for p in range(8):
+            if p & ~symm:
+                continue
+            sgn = np.array([-1 if p & (1 << k) else 1 for k in range(3)], np.float32)
+            loc = dabs[d, :3] * sgn
+            delta = dabs[d, 3:] * sgn
+            nodes = o.search_sphere(loc, rsq, 0)
+            assert np.array_equal(nodes, r.search_sphere(loc, rsq, 0)), (d, p)
+            n, _ = o.brush_pass(st, loc, delta, nodes)
+            moved += n
+            for nd in nodes:
+                r.node_mark_update(int(nd))
+        r.set_co(o.co())
+        for v in np.nonzero(o.vert_tags())[0]:
+            r.vert_mark_update(int(v))
+        o.update_normals()
+        r.update_normals()
+        err = float(np.abs(o.no() - r.no()).max())
+        assert err <= NORMAL_ATOL, (d, err)
+        o.update_bounds(UPD_BB)
+        r.update_bounds(UPD_BB)
+        ovb, _ = o.bbs()
+        rvb, _ = r.bbs()
+        assert bits_equal(ovb, rvb), (d, first_diff(ovb, rvb))
+    o.update_bounds(UPD_ORIG_BB)
+    r.update_bounds(UPD_ORIG_BB)
+    _, oovb = o.bbs()
+    _, rovb = r.bbs()
+    assert bits_equal(oovb, rovb)
+    assert moved > 0
+
+
+def test_grids_build_search_bounds_match_reference(oracle):
+    """BKE_pbvh_build_grids (leaf = max(limit / 17^2, 1) grids), search and the
+    grid-element refit, against the oracle on a multires torus."""
+    g = synth.torus_grids(40, 12, 5)
+    o = oracle.OracleMesh.grids(g, 0)
+    o.recalc_all_normals()
+    no = o.no()
+    r = pyrefpin.RefPBVH.grids(g.num_grids, g.grid_size, g.co, no, g.mask)
+    assert r.leaf_limit == max(10000 // (g.grid_size ** 2), 1)
+    on, rn = o.nodes(), r.nodes()
+    assert o.num_nodes == r.num_nodes
+    for k in ("children_offset", "prim_off", "totprim"):
+        assert np.array_equal(on[k], rn[k]), k
+    assert np.array_equal(o.prim_indices(), r.prim_indices())
+    ovb, oovb = o.bbs()
+    rvb, rovb = r.bbs()
+    assert bits_equal(ovb, rvb) and bits_equal(oovb, rovb)
+    rng = np.random.default_rng(3)
+    for _ in range(100):
+        c = rng.uniform(-1.4, 1.4, 3).astype(np.float32)
+        rsq = np.float32(rng.uniform(0.0, 0.5)) ** 2
+        assert np.array_equal(o.search_sphere(c, rsq), r.search_sphere(c, rsq))
+    co = g.co.copy()
+    center = co[co.shape[0] // 3]
+    d2 = ((co - center) ** 2).sum(1)
+    inside = d2 < np.float32(0.04)
+    co[inside] *= np.float32(1.03)
+    nodes = o.search_sphere(center, np.float32(0.04))
+    o.set_co(co)
+    r.set_grid_co(co)
+    for n in nodes:
+        o.node_mark_update(int(n))
+        r.node_mark_update(int(n))
+    o.update_bounds(UPD_BB)
+    r.update_bounds(UPD_BB)
+    ovb, _ = o.bbs()
+    rvb, _ = r.bbs()
+    assert bits_equal(ovb, rvb), first_diff(ovb, rvb)
+
+
+@pytest.mark.parametrize("preset", [0, 1, 2, 3, 5, 6])
+def test_curve_table_matches_reference(oracle, preset):
+    """Falloff table (KERNEL_curvemap_reset + KERNEL_curvemapping_changed ->
+    curvemap_make_table, colortools.c:249-416, 597-771, 846-922) and its
+    evaluation (KERNEL_curvemapping_evaluateF, :942-980), bit for bit."""
+    t_o, p_o = oracle.curve_table(preset)
+    t_r, p_r = pyrefpin.curve_table(preset)
+    assert bits_equal(t_o, t_r), first_diff(t_o, t_r)
+    assert bits_equal(p_o, p_r), first_diff(p_o, p_r)
+    v = np.linspace(0.0, 1.0, 4097, dtype=np.float32)[:-1]
+    got = np.array([oracle.curve_strength(preset, float(x), 1.0) for x in v], dtype=np.float32)
+    ref = pyrefpin.curve_evaluate(preset, v)
+    assert bits_equal(got, ref), first_diff(got, ref)
