@@ -14,15 +14,14 @@
  *
  * Parity pinning: the reference ships no tests, fixtures or golden vectors for
  * this path and does not build as shipped (its public headers are missing).
- * oracle/refpin compiles the reference's own pbvh.c, poly-normal, vector-math
- * and colortools.c code from the reference tree behind stand-in headers, and
- * tests/test_refpin.py checks this restatement against it: PBVH build, node
- * search and bounding boxes bit for bit, vertex normals within 1e-6 (the
- * reference's float atomics add in task order), falloff tables and curve
- * evaluation bit for bit.  The brush math has no reference code (sculpt.c is
- * missing) and the multires normal/seam code needs OpenSubdiv: those parts
- * stay pinned only by known-answer tests written from the reference's
- * definitions.
+ * oracle/refpin compiles the reference's own pbvh.c, subdiv_ccg.c,
+ * poly-normal, vector-math and colortools.c code from the reference tree
+ * behind stand-in headers, and tests/test_refpin.py checks this restatement
+ * against it: PBVH build, node search, bounding boxes, multires normals with
+ * seam stitching, falloff tables and curve evaluation bit for bit; FACES vertex
+ * normals within 1e-6 (the reference's float atomics add in task order).  The
+ * brush math has no reference code (sculpt.c is missing): it is pinned only by
+ * known-answer tests written from the reference's definitions.
  */
 #ifndef ORACLE_H
 #define ORACLE_H

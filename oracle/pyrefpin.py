@@ -63,6 +63,24 @@ def lib():
         L.rp_update_bounds.argtypes = [vp, i]
         L.rp_node_flag.restype = i
         L.rp_node_flag.argtypes = [vp, i]
+        L.rg_create.restype = vp
+        L.rg_create.argtypes = [i, vp, vp, vp, vp, i, i, vp, i, vp, vp, vp, i]
+        L.rg_free.argtypes = [vp]
+        for name in ("rg_num_grids", "rg_num_nodes"):
+            getattr(L, name).restype = i
+            getattr(L, name).argtypes = [vp]
+        L.rg_get_bbs.argtypes = [vp, vp, vp]
+        L.rg_get.argtypes = [vp, vp, vp, vp]
+        L.rg_set.argtypes = [vp, vp, vp]
+        L.rg_node_mark_update.argtypes = [vp, i]
+        L.rg_update_normals.argtypes = [vp]
+        L.rg_update_bounds.argtypes = [vp, i]
+        L.rg_edge_num_faces.restype = i
+        L.rg_edge_num_faces.argtypes = [vp, i]
+        L.rg_edge_coords.argtypes = [vp, i, i, vp]
+        L.rg_vertex_num_faces.restype = i
+        L.rg_vertex_num_faces.argtypes = [vp, i]
+        L.rg_vertex_coords.argtypes = [vp, i, vp]
         L.rp_curve_table.argtypes = [i, vp, vp]
         L.rp_curve_evaluate.argtypes = [i, vp, i, vp]
         _lib = L
@@ -200,3 +218,79 @@ class RefPBVH:
 
     def update_bounds(self, flag: int):
         lib().rp_update_bounds(self.h, flag)
+
+
+class RefGrids:
+    """Multires grids driven by the reference's own subdiv_ccg.c and pbvh.c:
+    adjacency, PBVH, normal update with seam stitching, bounds refit."""
+
+    def __init__(self, g, no, leaf_limit: int = 10000):
+        arr = lambda a: np.ascontiguousarray(a, dtype=np.int32)  # noqa: E731
+        self._keep = [arr(g.face_start), arr(g.face_ngrids), arr(g.face_verts),
+                      arr(g.face_edges), arr(g.edge_verts),
+                      np.ascontiguousarray(g.co, dtype=np.float32),
+                      np.ascontiguousarray(no, dtype=np.float32),
+                      None if g.mask is None else np.ascontiguousarray(g.mask, dtype=np.float32)]
+        fs, fn, fv, fe, ev, co, nrm, mask = self._keep
+        self.grid_size = g.grid_size
+        self.nelem = co.shape[0]
+        self.has_mask = mask is not None
+        self.h = lib().rg_create(fs.shape[0], _p(fs), _p(fn), _p(fv), _p(fe), g.num_base_verts,
+                                 ev.shape[0], _p(ev), g.grid_size, _p(co), _p(nrm), _p(mask),
+                                 leaf_limit)
+
+    def close(self):
+        if self.h:
+            lib().rg_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_nodes(self) -> int:
+        return lib().rg_num_nodes(self.h)
+
+    def bbs(self):
+        n = self.num_nodes
+        vb = np.zeros((n, 6), dtype=np.float32)
+        ovb = np.zeros((n, 6), dtype=np.float32)
+        lib().rg_get_bbs(self.h, _p(vb), _p(ovb))
+        return vb, ovb
+
+    def get(self):
+        co = np.zeros((self.nelem, 3), dtype=np.float32)
+        no = np.zeros((self.nelem, 3), dtype=np.float32)
+        mask = np.zeros(self.nelem, dtype=np.float32)
+        lib().rg_get(self.h, _p(co), _p(no), _p(mask))
+        return co, no, (mask if self.has_mask else None)
+
+    def set(self, co, mask=None):
+        co = np.ascontiguousarray(co, dtype=np.float32)
+        mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        lib().rg_set(self.h, _p(co), _p(mask))
+
+    def node_mark_update(self, node: int):
+        lib().rg_node_mark_update(self.h, int(node))
+
+    def update_normals(self):
+        lib().rg_update_normals(self.h)
+
+    def update_bounds(self, flag: int):
+        lib().rg_update_bounds(self.h, flag)
+
+    def edge_coords(self, edge: int) -> np.ndarray:
+        nf = lib().rg_edge_num_faces(self.h, edge)
+        out = np.zeros((nf, 2 * self.grid_size, 3), dtype=np.int32)
+        for f in range(nf):
+            lib().rg_edge_coords(self.h, edge, f, _p(out[f]))
+        return out
+
+    def vertex_coords(self, vertex: int) -> np.ndarray:
+        nf = lib().rg_vertex_num_faces(self.h, vertex)
+        out = np.zeros((max(nf, 1), 3), dtype=np.int32)
+        lib().rg_vertex_coords(self.h, vertex, _p(out))
+        return out[:nf]

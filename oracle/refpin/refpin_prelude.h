@@ -262,13 +262,17 @@ void *BLI_gsetIterator_getKey(GSetIterator *it);
 typedef struct TaskParallelTLS {
   void *userdata_chunk;
 } TaskParallelTLS;
+typedef void (*TaskParallelReduceFunc)(const void *__restrict userdata,
+                                       void *__restrict chunk_join,
+                                       void *__restrict chunk);
+typedef void (*TaskParallelFreeFunc)(const void *__restrict userdata, void *__restrict chunk);
 typedef struct TaskParallelSettings {
   bool use_threading;
   int min_iter_per_thread;
   void *userdata_chunk;
   size_t userdata_chunk_size;
-  void *func_reduce;
-  void *func_free;
+  TaskParallelReduceFunc func_reduce;
+  TaskParallelFreeFunc func_free;
 } TaskParallelSettings;
 typedef void (*TaskParallelRangeFunc)(void *__restrict userdata,
                                       const int iter,
@@ -362,7 +366,150 @@ typedef struct DMFlagMat {
   char flag;
 } DMFlagMat;
 
-typedef struct SubdivCCG SubdivCCG;
+/* ---- multires grids (subdiv_ccg.c; KERNEL_subdiv_ccg.h, KERNEL_subdiv.h and
+ * OpenSubdiv's topology-refiner C API are not in the reference): the types
+ * with the fields subdiv_ccg.c reads and writes.  The topology refiner is a
+ * table of query functions; the harness answers them from the base mesh's
+ * face / edge / vertex arrays (refpin_subdiv.c). ---- */
+typedef struct OpenSubdiv_TopologyRefiner OpenSubdiv_TopologyRefiner;
+struct OpenSubdiv_TopologyRefiner {
+  int (*getNumVertices)(const OpenSubdiv_TopologyRefiner *r);
+  int (*getNumEdges)(const OpenSubdiv_TopologyRefiner *r);
+  int (*getNumFaces)(const OpenSubdiv_TopologyRefiner *r);
+  int (*getNumFaceVertices)(const OpenSubdiv_TopologyRefiner *r, int face);
+  void (*getFaceVertices)(const OpenSubdiv_TopologyRefiner *r, int face, int *out);
+  int (*getNumFaceEdges)(const OpenSubdiv_TopologyRefiner *r, int face);
+  void (*getFaceEdges)(const OpenSubdiv_TopologyRefiner *r, int face, int *out);
+  void (*getEdgeVertices)(const OpenSubdiv_TopologyRefiner *r, int edge, int out[2]);
+  int (*getNumVertexEdges)(const OpenSubdiv_TopologyRefiner *r, int vertex);
+  void (*getVertexEdges)(const OpenSubdiv_TopologyRefiner *r, int vertex, int *out);
+  void *user_data;
+};
+typedef struct SubdivStats {
+  double dummy;
+} SubdivStats;
+enum { SUBDIV_STATS_SUBDIV_TO_CCG = 0 };
+typedef struct Subdiv {
+  OpenSubdiv_TopologyRefiner *topology_refiner;
+  void *displacement_evaluator;
+  SubdivStats stats;
+} Subdiv;
+typedef struct SubdivCCGCoord {
+  int grid_index;
+  short x, y;
+} SubdivCCGCoord;
+typedef struct SubdivCCGFace {
+  int num_grids;
+  int start_grid_index;
+} SubdivCCGFace;
+typedef struct SubdivCCGAdjacentEdge {
+  int num_adjacent_faces;
+  SubdivCCGCoord **boundary_coords;
+} SubdivCCGAdjacentEdge;
+typedef struct SubdivCCGAdjacentVertex {
+  int num_adjacent_faces;
+  SubdivCCGCoord *corner_coords;
+} SubdivCCGAdjacentVertex;
+typedef struct SubdivCCGNeighbors {
+  SubdivCCGCoord *coords;
+  int size;
+  int num_duplicates;
+  SubdivCCGCoord coords_fixed[256];
+} SubdivCCGNeighbors;
+typedef enum SubdivCCGAdjacencyType {
+  SUBDIV_CCG_ADJACENT_NONE,
+  SUBDIV_CCG_ADJACENT_VERTEX,
+  SUBDIV_CCG_ADJACENT_EDGE,
+} SubdivCCGAdjacencyType;
+typedef struct SubdivToCCGSettings {
+  int resolution;
+  bool need_normal;
+  bool need_mask;
+} SubdivToCCGSettings;
+typedef struct SubdivCCGMaskEvaluator SubdivCCGMaskEvaluator;
+struct SubdivCCGMaskEvaluator {
+  float (*eval_mask)(SubdivCCGMaskEvaluator *ev, int ptex_face_index, float u, float v);
+  void (*free)(SubdivCCGMaskEvaluator *ev);
+  void *user_data;
+};
+typedef struct SubdivCCGMaterialFlagsEvaluator SubdivCCGMaterialFlagsEvaluator;
+struct SubdivCCGMaterialFlagsEvaluator {
+  DMFlagMat (*eval_material_flags)(SubdivCCGMaterialFlagsEvaluator *ev, int coarse_face_index);
+  void (*free)(SubdivCCGMaterialFlagsEvaluator *ev);
+  void *user_data;
+};
+typedef struct SubdivCCG {
+  Subdiv *subdiv;
+  int level;
+  int grid_size;
+  int grid_element_size;
+  bool has_normal, has_mask;
+  int normal_offset, mask_offset;
+  int num_grids;
+  CCGElem **grids;
+  unsigned char *grids_storage;
+  DMFlagMat *grid_flag_mats;
+  BLI_bitmap **grid_hidden;
+  int num_faces;
+  SubdivCCGFace *faces;
+  SubdivCCGFace **grid_faces;
+  int num_adjacent_edges;
+  SubdivCCGAdjacentEdge *adjacent_edges;
+  int num_adjacent_vertices;
+  SubdivCCGAdjacentVertex *adjacent_vertices;
+  void *edges, *vertices;
+  struct {
+    int *start_face_grid_index;
+  } cache_;
+} SubdivCCG;
+#define LIB_INLINE static inline
+#define LIB_BITMAP_NEW BLI_BITMAP_NEW
+#define LIB_task_parallel_range BLI_task_parallel_range
+#define LIB_gset_ptr_new BLI_gset_ptr_new
+#define LIB_gset_add BLI_gset_add
+#define LIB_gset_free BLI_gset_free
+void LIB_parallel_range_settings_defaults(TaskParallelSettings *settings);
+static inline int KERNEL_subdiv_grid_size_from_level(const int level)
+{
+  return (1 << (level - 1)) + 1;
+}
+static inline int bitscan_forward_i(int a)
+{
+  return __builtin_ctz((unsigned int)a);
+}
+void KERNEL_subdiv_ccg_key_top_level(CCGKey *key, const SubdivCCG *subdiv_ccg);
+void KERNEL_subdiv_ccg_recalc_normals(SubdivCCG *subdiv_ccg);
+void KERNEL_subdiv_ccg_average_grids(SubdivCCG *subdiv_ccg);
+void KERNEL_subdiv_ccg_destroy(SubdivCCG *subdiv_ccg);
+#define LIB_assert(a) ((void)0)
+#define UNUSED_VARS_NDEBUG(...) ((void)0)
+enum { SUBDIV_EVALUATOR_TYPE_CPU = 0 };
+/* Grid evaluation through OpenSubdiv (not in the reference, not pinned). */
+int *KERNEL_subdiv_face_ptex_offset_get(Subdiv *subdiv);
+#define BKE_subdiv_face_ptex_offset_get KERNEL_subdiv_face_ptex_offset_get
+void KERNEL_subdiv_rotate_grid_to_quad(int corner, float grid_u, float grid_v, float *r_quad_u,
+                                       float *r_quad_v);
+void KERNEL_subdiv_eval_limit_point(Subdiv *subdiv, int ptex_face_index, float u, float v,
+                                    float r_P[3]);
+void KERNEL_subdiv_eval_limit_point_and_normal(Subdiv *subdiv, int ptex_face_index, float u,
+                                               float v, float r_P[3], float r_N[3]);
+void KERNEL_subdiv_eval_final_point(Subdiv *subdiv, int ptex_face_index, float u, float v,
+                                    float r_P[3]);
+bool KERNEL_subdiv_eval_begin_from_mesh(Subdiv *subdiv, const Mesh *mesh,
+                                        const float (*coarse_vertex_cos)[3], int evaluator_type,
+                                        void *evaluator_cache);
+void KERNEL_subdiv_stats_begin(SubdivStats *stats, int value);
+void KERNEL_subdiv_stats_end(SubdivStats *stats, int value);
+void KERNEL_subdiv_free(Subdiv *subdiv);
+bool KERNEL_subdiv_ccg_mask_init_from_paint(SubdivCCGMaskEvaluator *mask_evaluator,
+                                            const Mesh *mesh);
+void KERNEL_subdiv_ccg_material_flags_init_from_mesh(
+    SubdivCCGMaterialFlagsEvaluator *material_flags_evaluator, const Mesh *mesh);
+Mesh *KERNEL_mesh_new_nomain_from_template(const Mesh *me_src, int verts_len, int edges_len,
+                                           int tessface_len, int loops_len, int polys_len);
+int poly_find_loop_from_vert(const MPoly *poly, const MLoop *loopstart, unsigned int vert);
+void KERNEL_subdiv_ccg_update_normals(SubdivCCG *subdiv_ccg, struct CCGFace **effected_faces,
+                                      int num_effected_faces);
 void BKE_subdiv_ccg_update_normals(SubdivCCG *subdiv_ccg, struct CCGFace **effected_faces,
                                    int num_effected_faces);
 int BKE_subdiv_ccg_grid_to_face_index(const SubdivCCG *subdiv_ccg, const int grid_index);

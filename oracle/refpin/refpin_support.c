@@ -242,17 +242,32 @@ void *BLI_gsetIterator_getKey(GSetIterator *it)
   return BLI_ghashIterator_getKey(it);
 }
 
-/* ---- task range: the callback over [start, stop) in order ---- */
+/* ---- task range: the callback over [start, stop) in order, one thread; the
+ * per-thread chunk is a copy of settings->userdata_chunk, freed at the end ---- */
 void BLI_task_parallel_range(const int start,
                              const int stop,
                              void *userdata,
                              TaskParallelRangeFunc func,
                              const TaskParallelSettings *settings)
 {
-  (void)settings;
   TaskParallelTLS tls = {NULL};
+  void *chunk = NULL;
+  if (settings && settings->userdata_chunk && settings->userdata_chunk_size) {
+    chunk = malloc(settings->userdata_chunk_size);
+    memcpy(chunk, settings->userdata_chunk, settings->userdata_chunk_size);
+    tls.userdata_chunk = chunk;
+  }
   for (int i = start; i < stop; i++) {
     func(userdata, i, &tls);
+  }
+  if (chunk) {
+    if (settings->func_reduce) {
+      settings->func_reduce(userdata, settings->userdata_chunk, chunk);
+    }
+    if (settings->func_free) {
+      settings->func_free(userdata, chunk);
+    }
+    free(chunk);
   }
 }
 
@@ -386,16 +401,6 @@ int BM_elem_flag_test(const void *ele, int hflag)
 void BM_mesh_elem_index_ensure(BMesh *bm, int htype)
 {
   refpin_unreachable("dyntopo");
-}
-void BKE_subdiv_ccg_update_normals(SubdivCCG *subdiv_ccg, struct CCGFace **effected_faces,
-                                   int num_effected_faces)
-{
-  refpin_unreachable("multires normal update (subdiv_ccg.c)");
-}
-int BKE_subdiv_ccg_grid_to_face_index(const SubdivCCG *subdiv_ccg, const int grid_index)
-{
-  refpin_unreachable("subdiv_ccg");
-  return 0;
 }
 void GPU_pbvh_buffers_free(GPU_PBVH_Buffers *buffers)
 {

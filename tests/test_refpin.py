@@ -1,9 +1,10 @@
 """The oracle against the reference's own compiled PBVH code (CPU).
 
 oracle/refpin compiles the reference's pbvh.c (complete copy, pbvh.c:1913-4986),
-BKE_mesh_calc_poly_normal (mesh_evaluate.c:39-86), normal_tri_v3 /
-normal_quad_v3 (math_geom.cc:31-68) and its inline vector math from the
-reference tree, behind stand-ins for the headers the reference does not ship.
+subdiv_ccg.c, BKE_mesh_calc_poly_normal (mesh_evaluate.c:39-86), normal_tri_v3 /
+normal_quad_v3 (math_geom.cc:31-68), its inline vector math and the falloff
+curve code of colortools.c from the reference tree, behind stand-ins for the
+headers the reference does not ship.
 These tests check, on the same inputs, that the oracle's restatement gives
 
 * the same PBVH (BKE_pbvh_build_mesh / _build_grids): node table, prim order,
@@ -16,6 +17,11 @@ These tests check, on the same inputs, that the oracle's restatement gives
   (unit vectors): the reference adds face normals with float atomics in task
   order, the oracle in ascending looptri order with compensated sums, so the
   last bit may differ.
+
+* the same multires normals, seam-stitched positions and masks after
+  KERNEL_subdiv_ccg_update_normals (the reference builds its own edge / corner
+  adjacency) — bit for bit;
+* the same falloff tables and curve values — bit for bit.
 
 The replay tests drive whole oracle strokes (draw, smooth, inflate, clay
 strips; X symmetry) and, after every dab, hand the oracle's positions, vertex
@@ -325,3 +331,69 @@ def test_curve_table_matches_reference(oracle, preset):
     got = np.array([oracle.curve_strength(preset, float(x), 1.0) for x in v], dtype=np.float32)
     ref = pyrefpin.curve_evaluate(preset, v)
     assert bits_equal(got, ref), first_diff(got, ref)
+
+
+def _grid_pair(oracle, nu=24, nv=8):
+    g = synth.torus_grids(nu, nv, 5)
+    o = oracle.OracleMesh.grids(g, 0)
+    r = pyrefpin.RefGrids(g, np.zeros_like(g.co))
+    assert o.num_nodes == r.num_nodes
+    return g, o, r
+
+
+def _assert_same_grids(o, r, what):
+    co_r, no_r, m_r = r.get()
+    assert bits_equal(o.co(), co_r), (what, "co", first_diff(o.co(), co_r))
+    assert bits_equal(o.no(), no_r), (what, "no", first_diff(o.no(), no_r))
+    assert bits_equal(o.mask(), m_r), (what, "mask", first_diff(o.mask(), m_r))
+
+
+def test_grids_normals_and_stitching_match_reference(oracle):
+    """Every grid normal recomputed with all seams stitched (subdiv_ccg.c
+    normal update: inner quad normals, face-internal seams and centres, base
+    edges and corners — positions, normals and masks averaged), bit for bit;
+    the reference builds its own edge/corner adjacency from the base topology
+    (subdiv_ccg.c:397-540)."""
+    g, o, r = _grid_pair(oracle)
+    o.recalc_all_normals()
+    for n in np.nonzero(o.nodes()["flag"] & LEAF)[0]:
+        r.node_mark_update(int(n))
+    r.update_normals()
+    _assert_same_grids(o, r, "full update")
+
+
+def test_grids_stroke_replay_in_reference(oracle):
+    """A mixed draw / smooth / inflate oracle stroke on multires grids with X
+    symmetry; after every dab the reference's normal update (with seam
+    stitching) and refit run on the oracle's brushed grids and give the same
+    positions, normals, masks and boxes bit for bit."""
+    g, o, r = _grid_pair(oracle)
+    o.recalc_all_normals()
+    for n in np.nonzero(o.nodes()["flag"] & LEAF)[0]:
+        r.node_mark_update(int(n))
+    r.update_normals()
+    dabs = synth.torus_dabs(synth.SEED_BASE + 4, 18, 0.12)
+    tools = (synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE)
+    moved = 0
+    for d in range(dabs.shape[0]):
+        st = synth.Stroke(tools[d % 3], 0.12, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
+        rsq = np.float32(0.12) * np.float32(0.12)
+        for p in (0, 1):
+            sgn = np.array([-1 if p & 1 else 1, 1, 1], np.float32)
+            loc = dabs[d, :3] * sgn
+            delta = dabs[d, 3:] * sgn
+            nodes = o.search_sphere(loc, rsq, 0)
+            n, _ = o.brush_pass(st, loc, delta, nodes)
+            moved += n
+            for nd in nodes:
+                r.node_mark_update(int(nd))
+        r.set(o.co(), o.mask())
+        o.update_normals()
+        r.update_normals()
+        _assert_same_grids(o, r, f"dab {d}")
+        o.update_bounds(UPD_BB)
+        r.update_bounds(UPD_BB)
+        ovb, _ = o.bbs()
+        rvb, _ = r.bbs()
+        assert bits_equal(ovb, rvb), (d, first_diff(ovb, rvb))
+    assert moved > 0
