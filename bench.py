@@ -28,7 +28,8 @@ normal update and bounding-box refit, as the reference's stroke does.
            the host cores, same stroke.
 
 --quick runs three persistent strokes of the workload and exits (the
-command profiled with ncu).
+command profiled with ncu).  --phases prints the persistent kernel's per-dab
+phase profile on all five workloads.
 
 --impl reference times the CPU restatement of the reference path (the
 reference itself does not build: its headers and brush code are missing).
@@ -68,6 +69,9 @@ def parse_args():
     ap.add_argument("--quick", action="store_true",
                     help="three persistent strokes of the workload, no report (for ncu)")
     ap.add_argument("--cluster", type=int, default=16, help="cluster size for --quick")
+    ap.add_argument("--phases", action="store_true",
+                    help="per-phase profile of the persistent stroke on all five workloads "
+                         "(one JSON line each), no report")
     return ap.parse_args()
 
 
@@ -85,6 +89,51 @@ def run_quick(args):
         g.restore()
         s = g.stroke(st, mode=STROKE_TEAM)
     print(f"quick: {s.verts_displaced} vertices displaced, {s.gpu_ms:.3f} ms")
+    return 0
+
+
+def run_phases(args):
+    """Per-dab phase times of the persistent stroke kernel on the five workloads:
+    the autotuned cluster, the best of three L2-flushed strokes, then one
+    instrumented stroke (phase timers of the team's first thread)."""
+    from dune_sculpt_gb300 import build as libbuild
+
+    libbuild.build()
+    from dune_sculpt_gb300 import synth
+    from dune_sculpt_gb300.sculpt import PBVH, STROKE_TEAM
+
+    def one(name, g, st, tools=None):
+        g.snapshot()
+        best, _ = g.autotune_team(st, dab_tools=tools)
+        times = []
+        for _ in range(3):
+            g.restore()
+            g.flush_l2()
+            times.append(g.stroke(st, mode=STROKE_TEAM, dab_tools=tools).gpu_ms)
+        g.restore()
+        g.flush_l2()
+        ph, _, stats = g.stroke_team_profile(st, dab_tools=tools)
+        nd = st.dabs.shape[0]
+        print(json.dumps({
+            "workload": name, "cluster": best, "ms_per_stroke": round(min(times), 3),
+            "us_per_dab": round(1000 * min(times) / nd, 2),
+            "verts_displaced": stats.verts_displaced,
+            "phase_us_per_dab": {k: round(1000 * v["ms"] / nd, 2) for k, v in ph.items()},
+            "phase_alg_MB_per_stroke": {k: round(v["bytes"] / 1e6, 2) for k, v in ph.items()}}),
+            flush=True)
+        g.free()
+
+    m, st, ll = synth.cfg1_grid_draw()
+    one("grid513_draw", PBVH.build_mesh(m, ll), st)
+    m, st, ll = synth.cfg2_icosphere_smooth()
+    one("icosphere8_smooth_masked_xmirror", PBVH.build_mesh(m, ll), st)
+    m, st, ll = synth.cfg3_sphere_clay()
+    one("uvsphere2048_clay_strips_xmirror", PBVH.build_mesh(m, ll), st)
+    g, dabs = synth.cfg5_multires()
+    tools = np.array([(synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE)[d % 3]
+                      for d in range(dabs.shape[0])], dtype=np.int32)
+    st = synth.Stroke(synth.TOOL_DRAW, 0.04, 0.6, synth.CURVE_SMOOTH, 0, dabs)
+    one("multires_torus_50000x17x17_mixed", PBVH.build_grids(g), st, tools)
     return 0
 
 
@@ -415,6 +464,8 @@ def main():
         return run_reference(args)
     if args.quick:
         return run_quick(args)
+    if args.phases:
+        return run_phases(args)
     return run_gpu(args)
 
 

@@ -956,9 +956,9 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
               // value and mask read, ring values read, value written
               ab += 16ull + (m.mask ? 4ull : 0ull) + 16ull * nring + 16ull;
             }
-            team_bytes(a, kPhBrush, ab);
+            team_bytes(a, kPhApply, ab);
             team_sync(cluster, C);
-            clk.mark(a, rank, kPhBrush);
+            clk.mark(a, rank, kPhApply);
           }
           if (count == 0) {
             team_sync(cluster, C);

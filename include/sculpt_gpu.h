@@ -223,8 +223,9 @@ int sgpu_autotune_team(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab 
 /* Profile of one SGPU_STROKE_TEAM stroke: the persistent kernel's time split
  * by phase (time of the team's first thread from phase start to the barrier
  * that ends it) and the algorithmic bytes each phase moved.  Phases: 0 node
- * search, 1 area normal/centre, 2 brush sweep, 3 smooth apply, 4 normals and
- * leaf refit, 5 ancestor flush, 6 job set-up and end-of-stroke bounds. */
+ * search, 1 area normal/centre, 2 brush sweep (smooth: candidate test and
+ * first sweep), 3 smooth sweeps after the first, 4 normals and leaf refit,
+ * 5 ancestor flush, 6 job set-up and end-of-stroke bounds. */
 #define SGPU_TEAM_PHASES 7
 typedef struct SGPU_TeamProfile {
   float total_ms; /* CUDA-event time of the launch */
