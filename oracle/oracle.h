@@ -106,6 +106,14 @@ void or_get_vert_tags(const OrMesh *m, unsigned char *out);
 int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
                   const int *dab_tools, int which, int nthreads, int64_t *per_dab_counts);
 
+/* BKE_pbvh_raycast (PBVH_FACES) with the sculpt ray-cast callback of the brush
+ * specification.  depth: in = ray length, out = nearest hit depth.  Returns 1
+ * on a hit (active vertex, its face and the hit triangle's normal set).
+ * r_nleaves (nullable): leaves whose box the ray meets. */
+int or_raycast(OrMesh *m, const float ray_start[3], const float ray_normal[3], int original,
+               float *depth, int *active_vertex, int *active_face, float face_normal[3],
+               int *r_nleaves);
+
 /* Falloff curve of a brush preset (colortools.c): table 257*(x,y), params
  * {mintable, maxtable, range, ext_in[2], ext_out[2]}. */
 void or_curve_table(int preset, float *table_xy, float *params);

@@ -62,6 +62,8 @@ def lib():
         L.or_get_vert_tags.argtypes = [vp, vp]
         L.or_stroke.restype = C.c_int64
         L.or_stroke.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
+        L.or_raycast.restype = i
+        L.or_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp, vp]
         L.or_curve_table.argtypes = [i, vp, vp]
         L.or_curve_strength.restype = f
         L.or_curve_strength.argtypes = [i, f, f]
@@ -248,6 +250,21 @@ class OracleMesh:
 
     def update_bounds(self, flag: int):
         lib().or_update_bounds(self.h, flag)
+
+    def raycast(self, ray_start, ray_normal, depth: float = 3.4028234663852886e38,
+                original: int = 0):
+        """BKE_pbvh_raycast with the spec'd callback: (hit, depth, active vertex,
+        active face, face normal, leaves the ray's line meets)."""
+        o = np.asarray(ray_start, dtype=np.float32)
+        d = np.asarray(ray_normal, dtype=np.float32)
+        dep = np.array([depth], dtype=np.float32)
+        av = np.array([-1], dtype=np.int32)
+        af = np.array([-1], dtype=np.int32)
+        fn = np.zeros(3, dtype=np.float32)
+        nl = np.zeros(1, dtype=np.int32)
+        hit = lib().or_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(af), _p(fn),
+                               _p(nl))
+        return bool(hit), dep[0], int(av[0]), int(af[0]), fn, int(nl[0])
 
     def stroke(self, st, which: int = 3, nthreads: int = 0, dabs=None, dab_tools=None):
         b = make_brush(st)

@@ -81,6 +81,8 @@ def lib():
         L.rg_vertex_num_faces.restype = i
         L.rg_vertex_num_faces.argtypes = [vp, i]
         L.rg_vertex_coords.argtypes = [vp, i, vp]
+        L.rp_raycast.restype = i
+        L.rp_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
         L.rp_curve_table.argtypes = [i, vp, vp]
         L.rp_curve_evaluate.argtypes = [i, vp, i, vp]
         _lib = L
@@ -218,6 +220,19 @@ class RefPBVH:
 
     def update_bounds(self, flag: int):
         lib().rp_update_bounds(self.h, flag)
+
+    def raycast(self, ray_start, ray_normal, depth: float = 3.4028234663852886e38,
+                original: int = 0):
+        """BKE_pbvh_raycast with the spec'd callback: (hit, depth, active vertex,
+        active face, face normal)."""
+        o = np.asarray(ray_start, dtype=np.float32)
+        d = np.asarray(ray_normal, dtype=np.float32)
+        dep = np.array([depth], dtype=np.float32)
+        av = np.array([-1], dtype=np.int32)
+        af = np.array([-1], dtype=np.int32)
+        fn = np.zeros(3, dtype=np.float32)
+        hit = lib().rp_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(af), _p(fn))
+        return bool(hit), dep[0], int(av[0]), int(af[0]), fn
 
 
 class RefGrids:

@@ -329,3 +329,50 @@ void rp_curve_evaluate(int preset, const float *values, int n, float *out)
   }
   KERNEL_curvemapping_free_data(&cumap);
 }
+
+/* ---- ray cast (pbvh.c:3897-3929, 4042-4108, 4204-4262) ---- */
+typedef struct RaycastCb {
+  PBVH *pbvh;
+  const float *start, *normal;
+  IsectRayPrecalc isect;
+  float depth;
+  int active_vertex, active_face;
+  float face_normal[3];
+  bool hit;
+} RaycastCb;
+
+/* The sculpt ray-cast callback of the brush specification (the reference's
+ * sculpt.c, which would hold it, is absent): a node is ray cast when its entry
+ * distance is below the running minimum; a hit lowers the minimum to the hit
+ * depth. */
+static void raycast_cb(PBVHNode *node, void *data_v, float *tmin)
+{
+  RaycastCb *d = data_v;
+  if (BKE_pbvh_node_get_tmin(node) < *tmin) {
+    if (BKE_pbvh_node_raycast(d->pbvh, node, NULL, false, d->start, d->normal, &d->isect,
+                              &d->depth, &d->active_vertex, &d->active_face, d->face_normal)) {
+      d->hit = true;
+      *tmin = d->depth;
+    }
+  }
+}
+
+/* BKE_pbvh_raycast with that callback; depth in = ray length, out = hit depth. */
+int rp_raycast(RefPin *r, const float start[3], const float normal[3], int original, float *depth,
+               int *active_vertex, int *active_face, float face_normal[3])
+{
+  RaycastCb d;
+  memset(&d, 0, sizeof(d));
+  d.pbvh = r->pbvh;
+  d.start = start;
+  d.normal = normal;
+  d.depth = *depth;
+  d.active_vertex = d.active_face = -1;
+  isect_ray_tri_watertight_v3_precalc(&d.isect, normal);
+  BKE_pbvh_raycast(r->pbvh, raycast_cb, &d, start, normal, original != 0);
+  *depth = d.depth;
+  *active_vertex = d.active_vertex;
+  *active_face = d.active_face;
+  memcpy(face_normal, d.face_normal, sizeof(float[3]));
+  return d.hit ? 1 : 0;
+}

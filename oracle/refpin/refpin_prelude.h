@@ -106,6 +106,8 @@ static inline bool refpin_elem_(int v, const int *list, size_t n)
 /* Forward use inside math_vector_inline.c (the missing BLI_math_vector.h
  * declares it in the reference's build). */
 MINLINE bool is_zero_v3(const float v[3]);
+MINLINE int float_as_int(float f);
+MINLINE float int_as_float(int i);
 /* math_inline_ref.h is generated by the Makefile: math_base_inline.c lines
  * 21-605 (min_ff, max_ff, max_ii, ...; the file's next function,
  * compare_threshold_relative, names an undeclared variable and does not
@@ -633,6 +635,14 @@ void BKE_pbvh_get_grid_updates(PBVH *pbvh, bool clear, void ***r_gridfaces, int 
 void BKE_pbvh_parallel_range_settings(TaskParallelSettings *settings, bool use_threading,
                                       int totnode);
 PBVHType BKE_pbvh_type(const PBVH *pbvh);
+float BKE_pbvh_node_get_tmin(PBVHNode *node);
+bool BKE_pbvh_node_raycast(PBVH *pbvh, PBVHNode *node, float (*origco)[3], bool use_origco,
+                           const float ray_start[3], const float ray_normal[3],
+                           struct IsectRayPrecalc *isect_precalc, float *depth,
+                           int *active_vertex_index, int *active_face_grid_index,
+                           float *face_normal);
+void BKE_pbvh_raycast(PBVH *pbvh, BKE_pbvh_HitOccludedCallback cb, void *data,
+                      const float ray_start[3], const float ray_normal[3], bool original);
 GSet *BKE_pbvh_bmesh_node_unique_verts(PBVHNode *node);
 GSet *BKE_pbvh_bmesh_node_other_verts(PBVHNode *node);
 void BKE_pbvh_node_fully_masked_set(PBVHNode *node, int fully_masked);

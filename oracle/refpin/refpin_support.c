@@ -450,32 +450,8 @@ void GPU_pbvh_buffers_update_flush(GPU_PBVH_Buffers *buffers)
   refpin_unreachable("draw buffers");
 }
 
-/* Ray queries (raycast / nearest-to-ray) are not pinned: isect_ray_tri_watertight_v3
- * in lib/intern/math_geom.cc is C++ (functional casts) and dist_squared_ray_to_seg_v3
- * (:574-580) has an empty body in the reference. */
-void isect_ray_tri_watertight_v3_precalc(IsectRayPrecalc *isect_precalc,
-                                         const float ray_direction[3])
-{
-  refpin_unreachable("raycast");
-}
-bool isect_ray_tri_watertight_v3(const float ray_origin[3], const IsectRayPrecalc *isect_precalc,
-                                 const float v0[3], const float v1[3], const float v2[3],
-                                 float *r_dist, float r_uv[2])
-{
-  refpin_unreachable("raycast");
-  return false;
-}
-void isect_ray_aabb_v3_precalc(IsectRayAABBPrecalc *data, const float ray_origin[3],
-                               const float ray_direction[3])
-{
-  refpin_unreachable("raycast");
-}
-bool isect_ray_aabb_v3(const IsectRayAABBPrecalc *data, const float bb_min[3],
-                       const float bb_max[3], float *tmin)
-{
-  refpin_unreachable("raycast");
-  return false;
-}
+/* Nearest-to-ray queries are not pinned: dist_squared_ray_to_seg_v3
+ * (math_geom.cc:574-580) has an empty body in the reference. */
 void dist_squared_ray_to_aabb_v3_precalc(DistRayAABBPrecalc *neasrest_precalc,
                                          const float ray_origin[3], const float ray_direction[3])
 {

@@ -397,3 +397,57 @@ def test_grids_stroke_replay_in_reference(oracle):
         rvb, _ = r.bbs()
         assert bits_equal(ovb, rvb), (d, first_diff(ovb, rvb))
     assert moved > 0
+
+
+def _rays(rng, n, center, radius):
+    """Rays from a sphere around the mesh towards points near its middle; every
+    seventh one axis-aligned (exercises the 1/0 slabs of the box test)."""
+    out = []
+    for k in range(n):
+        s = rng.normal(size=3)
+        s = (center + s / np.linalg.norm(s) * radius).astype(np.float32)
+        if k % 7 == 0:
+            ax = k % 3
+            d = np.zeros(3, np.float32)
+            d[ax] = -1.0 if s[ax] > center[ax] else 1.0
+        else:
+            t = center + rng.normal(size=3) * 0.3 * radius / 3.0
+            d = (t - s) / np.linalg.norm(t - s)
+        out.append((s, d.astype(np.float32)))
+    return out
+
+
+def _same_hit(a, b):
+    return (a[0] == b[0] and np.float32(a[1]).view(np.uint32) == np.float32(b[1]).view(np.uint32)
+            and a[2] == b[2] and a[3] == b[3] and bits_equal(a[4], b[4]))
+
+
+@pytest.mark.parametrize("name", ["grid", "icosphere", "uvsphere", "ngon"])
+def test_raycast_matches_reference(oracle, name):
+    """BKE_pbvh_raycast (pbvh.c:3916) + BKE_pbvh_node_raycast with the spec'd
+    sculpt callback: hit flag, depth, active vertex, active face and face normal
+    bit for bit, over vb and orig_vb, with finite and unbounded ray lengths,
+    before and after brushing."""
+    m, o, r = _pair(oracle, name, 5000)
+    co = o.co()
+    center = (co.min(0) + co.max(0)) / 2
+    radius = float(np.linalg.norm(co.max(0) - co.min(0)))
+    rng = np.random.default_rng(17)
+    hits = 0
+    for k, (s, d) in enumerate(_rays(rng, 300, center, radius)):
+        depth = np.float32(3.4028235e38) if k % 3 else np.float32(radius * 0.8)
+        a = o.raycast(s, d, depth, original=k % 2)
+        b = r.raycast(s, d, depth, original=k % 2)
+        assert _same_hit(a[:5], b), (k, a, b)
+        hits += a[0]
+    assert hits > 50
+    # after an edit (boxes refit, orig_vb kept) the same holds
+    co2, _ = _edit(o, r, co, center.astype(np.float32), 0.3 * radius, 0.05 * radius)
+    o.update_normals()
+    r.update_normals()
+    o.update_bounds(UPD_BB)
+    r.update_bounds(UPD_BB)
+    for k, (s, d) in enumerate(_rays(rng, 100, center, radius)):
+        a = o.raycast(s, d, original=k % 2)
+        b = r.raycast(s, d, original=k % 2)
+        assert _same_hit(a[:5], b), (k, a, b)
