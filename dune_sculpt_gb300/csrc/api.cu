@@ -14,6 +14,7 @@
 #include "sgpu_device.cuh"
 #include "sgpu_host.h"
 #include "sgpu_kernels.h"
+#include "sgpu_ray.h"
 #include "sgpu_team.h"
 
 #include <algorithm>
@@ -101,6 +102,13 @@ struct sgpu_mesh {
   // page-locked displaced counters of the last persistent launch
   unsigned long long* h_disp = nullptr;
   size_t h_disp_cap = 0;
+  // ray-cast batch buffers (grown to the largest batch; see sgpu_raycast)
+  RayBatch ray{};
+  float* ray_in = nullptr;   // 7 per ray: start, direction, length
+  float* ray_out = nullptr;  // 4 per ray: depth, face normal
+  int* ray_iout = nullptr;   // 3 per ray: hit, active vertex, active face
+  size_t ray_cap = 0;
+  bool ray_configured = false;
 
   cudaEvent_t prof_event() {
     if (ev_used == ev_pool.size()) {
@@ -170,6 +178,16 @@ struct sgpu_mesh {
     if (h_disp) cudaFreeHost(h_disp);
     h_disp = nullptr;
     h_disp_cap = 0;
+    for (void* p : {static_cast<void*>(ray_in), static_cast<void*>(ray_out),
+                    static_cast<void*>(ray_iout), static_cast<void*>(ray.count),
+                    static_cast<void*>(ray.slot_leaf), static_cast<void*>(ray.slot_tmin),
+                    static_cast<void*>(ray.slot_order), static_cast<void*>(ray.slot_key),
+                    static_cast<void*>(ray.items), static_cast<void*>(ray.nitems)})
+      if (p) cudaFree(p);
+    ray = RayBatch{};
+    ray_in = ray_out = nullptr;
+    ray_iout = nullptr;
+    ray_cap = 0;
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev_h0) cudaEventDestroy(ev_h0);
@@ -691,6 +709,13 @@ int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPol
     }
     nb_off[n + 1] = nb_off[n] + (h.nb_off[v + 1] - h.nb_off[v]);
     for (int q = h.nb_off[v], o = nb_off[n]; q < h.nb_off[v + 1]; q++, o++) nb_idx[o] = o2n[h.nb_idx[q]];
+  }
+  {
+    std::vector<int4> lt4(totlooptri);
+    for (int t = 0; t < totlooptri; t++)
+      lt4[t] = make_int4(o2n[h.lt_v[3 * t]], o2n[h.lt_v[3 * t + 1]], o2n[h.lt_v[3 * t + 2]],
+                         h.lt_poly[t]);
+    if ((rc = m->upload(&d.lt_v4, lt4))) return bail(rc);
   }
   if ((rc = m->upload(&d.poly, pl))) return bail(rc);
   if ((rc = m->upload(&d.poly_v4, pv))) return bail(rc);
@@ -1690,3 +1715,102 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
 }
 
 }  // namespace
+
+namespace {
+
+// Ray-cast buffers for up to n rays (grown, never shrunk).
+int ensure_ray_buffers(sgpu_mesh* m, int n) {
+  if (static_cast<size_t>(n) <= m->ray_cap && m->ray_in) return SGPU_OK;
+  const int L = m->dev.nleaf;
+  const size_t slots = static_cast<size_t>(n) * L;
+  const size_t items = static_cast<size_t>(n) * ray_items_per_ray(m->dev);
+  if (items > 0x7fffffffull) return fail(SGPU_ERR_UNSUPPORTED, "ray batch too large for the mesh");
+  void* p[10] = {m->ray_in, m->ray_out, m->ray_iout, m->ray.count, m->ray.slot_leaf,
+                 m->ray.slot_tmin, m->ray.slot_order, m->ray.slot_key, m->ray.items,
+                 m->ray.nitems};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  m->ray = RayBatch{};
+  m->ray_in = m->ray_out = nullptr;
+  m->ray_iout = nullptr;
+  m->ray_cap = 0;
+  CK(cudaMalloc(&m->ray_in, sizeof(float) * 7 * n), "cudaMalloc");
+  CK(cudaMalloc(&m->ray_out, sizeof(float) * 4 * n), "cudaMalloc");
+  CK(cudaMalloc(&m->ray_iout, sizeof(int) * 3 * n), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.count, sizeof(int) * n), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.slot_leaf, sizeof(int) * slots), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.slot_tmin, sizeof(float) * slots), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.slot_order, sizeof(int) * slots), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.slot_key, sizeof(unsigned long long) * slots), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.items, sizeof(int2) * items), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.nitems, sizeof(int)), "cudaMalloc");
+  m->ray.item_cap = static_cast<int>(items);
+  m->ray_cap = static_cast<size_t>(n);
+  return SGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const float* ray_normals,
+                 const float* ray_lengths, int original, float* r_depths, int* r_hits,
+                 int* r_active_vertices, int* r_active_faces, float* r_face_normals) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (mesh->host.type != kFaces) return fail(SGPU_ERR_UNSUPPORTED, "ray cast of PBVH_GRIDS");
+  if (nrays < 0) return fail(SGPU_ERR_INVALID_ARG, "negative ray count");
+  if (nrays == 0) return SGPU_OK;
+  if (!ray_starts || !ray_normals || !r_depths || !r_hits)
+    return fail(SGPU_ERR_INVALID_ARG, "NULL ray or result array");
+  if ((rc = ensure_ray_buffers(mesh, nrays))) return rc;
+  DevMesh& d = mesh->dev;
+  if (!mesh->ray_configured) {
+    CK(configure_ray_kernels(ray_leaves_smem(d), ray_finish_smem(d)), "ray kernel attributes");
+    mesh->ray_configured = true;
+  }
+  std::vector<float> in(7 * static_cast<size_t>(nrays));
+  for (int r = 0; r < nrays; r++) {
+    for (int k = 0; k < 3; k++) {
+      in[6 * r + k] = ray_starts[3 * r + k];
+      in[6 * r + 3 + k] = ray_normals[3 * r + k];
+    }
+    in[6 * static_cast<size_t>(nrays) + r] = ray_lengths ? ray_lengths[r] : FLT_MAX;
+  }
+  cudaStream_t s = mesh->stream;
+  CK(cudaMemcpyAsync(mesh->ray_in, in.data(), sizeof(float) * in.size(), cudaMemcpyHostToDevice, s),
+     "upload rays");
+  RayBatch rb = mesh->ray;
+  rb.rays = mesh->ray_in;
+  rb.depth_in = mesh->ray_in + 6 * static_cast<size_t>(nrays);
+  rb.original = original;
+  rb.n2o = mesh->d_n2o;
+  rb.depth_out = mesh->ray_out;
+  rb.face_normal = mesh->ray_out + nrays;
+  rb.hit = mesh->ray_iout;
+  rb.active_vertex = mesh->ray_iout + nrays;
+  rb.active_face = mesh->ray_iout + 2 * static_cast<size_t>(nrays);
+  int sms = 0, dev = 0;
+  CK(cudaGetDevice(&dev), "cudaGetDevice");
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+  CK(launch_raycast(d, rb, nrays, 8 * sms, s), "ray kernels");
+  std::vector<float> fo(4 * static_cast<size_t>(nrays));
+  std::vector<int> io(3 * static_cast<size_t>(nrays));
+  CK(cudaMemcpyAsync(fo.data(), mesh->ray_out, sizeof(float) * fo.size(), cudaMemcpyDeviceToHost, s),
+     "read results");
+  CK(cudaMemcpyAsync(io.data(), mesh->ray_iout, sizeof(int) * io.size(), cudaMemcpyDeviceToHost, s),
+     "read results");
+  CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  if ((rc = device_err(mesh))) return rc;
+  for (int r = 0; r < nrays; r++) {
+    r_depths[r] = fo[r];
+    r_hits[r] = io[r];
+    if (r_active_vertices) r_active_vertices[r] = io[nrays + r];
+    if (r_active_faces) r_active_faces[r] = io[2 * static_cast<size_t>(nrays) + r];
+    if (r_face_normals)
+      for (int k = 0; k < 3; k++) r_face_normals[3 * r + k] = fo[nrays + 3 * static_cast<size_t>(r) + k];
+  }
+  return SGPU_OK;
+}
+
+}  // extern "C"

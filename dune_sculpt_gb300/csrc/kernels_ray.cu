@@ -1,0 +1,417 @@
+// Ray cast of the PBVH (PBVH_FACES): BKE_pbvh_raycast (pbvh.c:3916-3929) with
+// the sculpt ray-cast callback, for a batch of independent rays.
+//
+// The reference walks the leaves whose box the ray line meets in order of
+// their entry distance (a binary tree keyed on tmin, ties after earlier DFS
+// leaves: BKE_pbvh_search_callback_occluded, pbvh.c:2853-2890), ray casts a
+// leaf when its tmin is below the running minimum (FLT_MAX until the first
+// hit, then the hit depth) and inside a leaf accepts a triangle when its hit
+// is strictly closer than the current depth (pbvh_faces_node_raycast,
+// pbvh.c:4042-4108).  The result only depends on each leaf's closest hit
+// (first triangle in prim order among equals) and on that leaf order, so:
+//   k_ray_leaves  one CTA per ray: every node box tested (isect_ray_aabb_v3),
+//                 leaves under passing ancestors listed in DFS order, their
+//                 processing order (stable by tmin; a NaN tmin is never below
+//                 the running minimum, and the binary tree orders the others
+//                 stably), and one work item per (leaf, 256 prims);
+//   k_ray_tris    every item's triangles tested (isect_ray_tri_watertight_v3),
+//                 the leaf's closest (depth, prim position) by atomicMin on a
+//                 64-bit key (depth bits of a non-negative float, -0 as +0);
+//   k_ray_finish  one CTA per ray: the leaves in order with the callback's
+//                 rule, then the winning triangle's depth, active vertex
+//                 (corner nearest the hit, first among equals), face and
+//                 normal (normal_tri_v3).
+#include <cuda_runtime.h>
+
+#include "sgpu_device.cuh"
+#include "sgpu_ray.h"
+
+namespace sgpu {
+
+namespace {
+
+constexpr int kRayThreads = 256;
+constexpr int kRayChunk = 256;  // prims per work item
+constexpr unsigned long long kNoKey = ~0ull;
+
+struct RayBox {
+  float org[3], inv[3];
+  int sign[3];
+};
+
+__device__ __forceinline__ void raybox_init(RayBox& r, const float* o, const float* d) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    r.org[i] = o[i];
+    r.inv[i] = 1.0f / d[i];
+    r.sign[i] = r.inv[i] < 0.0f;
+  }
+}
+
+// isect_ray_aabb_v3 (math_geom.cc:3032-3080): entry distance in *tmin_out.
+__device__ __forceinline__ bool raybox_hit(const RayBox& r, float4 mn, float4 mx, float* tmin_out) {
+  const float bb[2][3] = {{mn.x, mn.y, mn.z}, {mx.x, mx.y, mx.z}};
+  float tmin = (bb[r.sign[0]][0] - r.org[0]) * r.inv[0];
+  float tmax = (bb[1 - r.sign[0]][0] - r.org[0]) * r.inv[0];
+  const float tymin = (bb[r.sign[1]][1] - r.org[1]) * r.inv[1];
+  const float tymax = (bb[1 - r.sign[1]][1] - r.org[1]) * r.inv[1];
+  if ((tmin > tymax) || (tymin > tmax)) return false;
+  if (tymin > tmin) tmin = tymin;
+  if (tymax < tmax) tmax = tymax;
+  const float tzmin = (bb[r.sign[2]][2] - r.org[2]) * r.inv[2];
+  const float tzmax = (bb[1 - r.sign[2]][2] - r.org[2]) * r.inv[2];
+  if ((tmin > tzmax) || (tzmin > tmax)) return false;
+  if (tzmin > tmin) tmin = tzmin;
+  *tmin_out = tmin;
+  return true;
+}
+
+struct RayTri {
+  int kx, ky, kz;
+  float sx, sy, sz;
+};
+
+// isect_ray_tri_watertight_v3_precalc (math_geom.cc:1755-1780).
+__device__ __forceinline__ void raytri_init(RayTri& p, const float* d) {
+  const float x = fabsf(d[0]), y = fabsf(d[1]), z = fabsf(d[2]);
+  const int kz = (x > y) ? ((x > z) ? 0 : 2) : ((y > z) ? 1 : 2);  // axis_dominant_v3_single
+  int kx = (kz != 2) ? (kz + 1) : 0;
+  int ky = (kx != 2) ? (kx + 1) : 0;
+  if (d[kz] < 0.0f) {
+    const int t = kx;
+    kx = ky;
+    ky = t;
+  }
+  const float inv_dir_z = 1.0f / d[kz];
+  p.sx = d[kx] * inv_dir_z;
+  p.sy = d[ky] * inv_dir_z;
+  p.sz = inv_dir_z;
+  p.kx = kx;
+  p.ky = ky;
+  p.kz = kz;
+}
+
+__device__ __forceinline__ float comp(const float3& v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : v.z);
+}
+
+// isect_ray_tri_watertight_v3 (math_geom.cc:1782-1855).
+__device__ __forceinline__ bool raytri_hit(const float* o, const RayTri& p, float3 v0, float3 v1,
+                                           float3 v2, float* r_lambda) {
+  const float3 a = make_float3(v0.x - o[0], v0.y - o[1], v0.z - o[2]);
+  const float3 b = make_float3(v1.x - o[0], v1.y - o[1], v1.z - o[2]);
+  const float3 c = make_float3(v2.x - o[0], v2.y - o[1], v2.z - o[2]);
+  const float a_kx = comp(a, p.kx), a_ky = comp(a, p.ky), a_kz = comp(a, p.kz);
+  const float b_kx = comp(b, p.kx), b_ky = comp(b, p.ky), b_kz = comp(b, p.kz);
+  const float c_kx = comp(c, p.kx), c_ky = comp(c, p.ky), c_kz = comp(c, p.kz);
+  const float ax = a_kx - p.sx * a_kz;
+  const float ay = a_ky - p.sy * a_kz;
+  const float bx = b_kx - p.sx * b_kz;
+  const float by = b_ky - p.sy * b_kz;
+  const float cx = c_kx - p.sx * c_kz;
+  const float cy = c_ky - p.sy * c_kz;
+  const float u = cx * by - cy * bx;
+  const float v = ax * cy - ay * cx;
+  const float w = bx * ay - by * ax;
+  if ((u < 0.0f || v < 0.0f || w < 0.0f) && (u > 0.0f || v > 0.0f || w > 0.0f)) return false;
+  const float det = u + v + w;
+  if (det == 0.0f || !isfinite(det)) return false;
+  const int sign_det = __float_as_int(det) & static_cast<int>(0x80000000u);
+  const float t = (u * a_kz + v * b_kz + w * c_kz) * p.sz;
+  const float sign_t = __int_as_float(__float_as_int(t) ^ sign_det);
+  if (sign_t < 0.0f) return false;
+  const float inv_det = 1.0f / det;
+  *r_lambda = t * inv_det;
+  return true;
+}
+
+__device__ __forceinline__ unsigned long long depth_key(float depth, int pos) {
+  unsigned int bits = __float_as_uint(depth);
+  if (bits == 0x80000000u) bits = 0u;  // -0 compares equal to +0
+  return (static_cast<unsigned long long>(bits) << 32) | static_cast<unsigned int>(pos);
+}
+
+__device__ __forceinline__ float len_sq(float3 a, float3 b) {
+  const float d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z;
+  return d0 * d0 + d1 * d1 + d2 * d2;
+}
+
+// Block-wide exclusive scan of ints (kRayThreads threads).
+__device__ int ray_block_scan(int v, int* total, int* smem32) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nwarps = kRayThreads / 32;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem32[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < nwarps ? smem32[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    smem32[lane] = w;
+  }
+  __syncthreads();
+  const int base = warp > 0 ? smem32[warp - 1] : 0;
+  *total = smem32[nwarps - 1];
+  __syncthreads();
+  return base + x - v;
+}
+
+// Dynamic shared memory: node pass flags (char), node tmin and parents (4 B
+// each), listed leaves' tmin (float).
+__global__ void __launch_bounds__(kRayThreads) k_ray_leaves(DevMesh m, RayBatch rb) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int scan[32];
+  __shared__ int s_count;
+  const int ray = blockIdx.x;
+  const int N = m.totnode, L = m.nleaf;
+  float* s_t = reinterpret_cast<float*>(smem);
+  int* s_par = reinterpret_cast<int*>(s_t + N);
+  float* s_lt = reinterpret_cast<float*>(s_par + N);
+  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_lt + L);
+  float o[3], d[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    o[k] = rb.rays[6 * ray + k];
+    d[k] = rb.rays[6 * ray + 3 + k];
+  }
+  RayBox box;
+  raybox_init(box, o, d);
+  const float4* bb = rb.original ? m.orig_vb : m.vb;
+  for (int n = threadIdx.x; n < N; n += kRayThreads) {
+    float t = 0.0f;
+    s_pass[n] = raybox_hit(box, __ldcg(&bb[2 * n]), __ldcg(&bb[2 * n + 1]), &t);
+    s_t[n] = t;
+    s_par[n] = m.node_parent[n];
+  }
+  __syncthreads();
+  // pbvh_iter_next_occluded: a leaf is listed when it and all its ancestors
+  // pass; a NaN entry distance never passes the callback's test
+  const int seg = (L + kRayThreads - 1) / kRayThreads;
+  const int l0 = min(L, static_cast<int>(threadIdx.x) * seg), l1 = min(L, l0 + seg);
+  int mine = 0;
+  for (int id = l0; id < l1; id++) {
+    const int node = m.leaf_node[id];
+    bool ok = s_pass[node] && !isnan(s_t[node]);
+    for (int p = s_par[node]; ok && p >= 0; p = s_par[p]) ok = s_pass[p];
+    mine += ok;
+  }
+  int total;
+  int pos = ray_block_scan(mine, &total, scan);
+  int* slot_leaf = rb.slot_leaf + static_cast<size_t>(ray) * L;
+  float* slot_tmin = rb.slot_tmin + static_cast<size_t>(ray) * L;
+  for (int id = l0; id < l1; id++) {
+    const int node = m.leaf_node[id];
+    bool ok = s_pass[node] && !isnan(s_t[node]);
+    for (int p = s_par[node]; ok && p >= 0; p = s_par[p]) ok = s_pass[p];
+    if (!ok) continue;
+    slot_leaf[pos] = id;
+    slot_tmin[pos] = s_t[node];
+    s_lt[pos] = s_t[node];
+    pos++;
+  }
+  if (threadIdx.x == 0) {
+    rb.count[ray] = total;
+    s_count = total;
+  }
+  __syncthreads();
+  // processing order: stable by tmin (the reference's tree, ties after the
+  // earlier DFS leaf)
+  int* order = rb.slot_order + static_cast<size_t>(ray) * L;
+  unsigned long long* key = rb.slot_key + static_cast<size_t>(ray) * L;
+  for (int i = threadIdx.x; i < total; i += kRayThreads) {
+    const float ti = s_lt[i];
+    int rank = 0;
+    for (int j = 0; j < total; j++) {
+      const float tj = s_lt[j];
+      rank += (tj < ti) || (tj == ti && j < i);
+    }
+    order[rank] = i;
+    key[i] = kNoKey;
+  }
+  // work items: (ray-slot, chunk of kRayChunk prims)
+  int nch = 0;
+  const int s0 = min(total, static_cast<int>(threadIdx.x) * ((total + kRayThreads - 1) / kRayThreads));
+  const int s1 = min(total, s0 + (total + kRayThreads - 1) / kRayThreads);
+  for (int s = s0; s < s1; s++) {
+    const int leaf = slot_leaf[s];
+    nch += (m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf] + kRayChunk - 1) / kRayChunk;
+  }
+  int all;
+  int off = ray_block_scan(nch, &all, scan);
+  if (threadIdx.x == 0) scan[0] = atomicAdd(rb.nitems, all);
+  __syncthreads();
+  const int base = scan[0];
+  if (base + all > rb.item_cap) {
+    if (threadIdx.x == 0) atomicCAS(&m.work->err, 0, 5 /* SGPU_ERR_BOUNDS */);
+    return;
+  }
+  for (int s = s0; s < s1; s++) {
+    const int leaf = slot_leaf[s];
+    const int c = (m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf] + kRayChunk - 1) / kRayChunk;
+    for (int k = 0; k < c; k++) rb.items[base + off + k] = make_int2(ray * L + s, k);
+    off += c;
+  }
+}
+
+__global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb) {
+  __shared__ unsigned long long s_min[kRayThreads / 32];
+  const int L = m.nleaf;
+  const int total = __ldcg(rb.nitems);
+  for (int it = blockIdx.x; it < total; it += gridDim.x) {
+    const int2 item = rb.items[it];
+    const int ray = item.x / L;
+    float o[3], d[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      o[k] = rb.rays[6 * ray + k];
+      d[k] = rb.rays[6 * ray + 3 + k];
+    }
+    const int leaf = rb.slot_leaf[item.x];
+    const int p0 = m.leaf_prim_off[leaf], p1 = m.leaf_prim_off[leaf + 1];
+    const int pos = item.y * kRayChunk + static_cast<int>(threadIdx.x);
+    unsigned long long key = kNoKey;
+    if (p0 + pos < p1) {
+      const int4 tv = m.lt_v4[m.leaf_prims[p0 + pos]];
+      const float3 c0 = xyz(__ldcg(&m.co[tv.x])), c1 = xyz(__ldcg(&m.co[tv.y])),
+                   c2 = xyz(__ldcg(&m.co[tv.z]));
+      RayTri rt;
+      raytri_init(rt, d);
+      float depth;
+      if (raytri_hit(o, rt, c0, c1, c2, &depth)) key = depth_key(depth, pos);
+    }
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, s);
+      key = other < key ? other : key;
+    }
+    if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = key;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long k = s_min[0];
+      for (int w = 1; w < kRayThreads / 32; w++) k = s_min[w] < k ? s_min[w] : k;
+      if (k != kNoKey) atomicMin(&rb.slot_key[item.x], k);
+    }
+    __syncthreads();
+  }
+}
+
+// Dynamic shared memory: per listed leaf its order entry, tmin and key.
+__global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch rb) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ray = blockIdx.x;
+  const int L = m.nleaf;
+  const int cnt = rb.count[ray];
+  unsigned long long* s_key = reinterpret_cast<unsigned long long*>(smem);
+  float* s_tmin = reinterpret_cast<float*>(s_key + L);
+  int* s_order = reinterpret_cast<int*>(s_tmin + L);
+  const size_t base = static_cast<size_t>(ray) * L;
+  for (int i = threadIdx.x; i < cnt; i += kRayThreads) {
+    s_key[i] = __ldcg(&rb.slot_key[base + i]);
+    s_tmin[i] = rb.slot_tmin[base + i];
+    s_order[i] = rb.slot_order[base + i];
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  // traverse_tree with the callback: a leaf is cast when tmin < running
+  // minimum; its closest hit is taken when strictly closer than the depth
+  float run_tmin = FLT_MAX;
+  float depth = rb.depth_in ? rb.depth_in[ray] : FLT_MAX;
+  int win_slot = -1, win_pos = -1;
+  for (int k = 0; k < cnt; k++) {
+    const int s = s_order[k];
+    if (!(s_tmin[s] < run_tmin)) continue;
+    const unsigned long long key = s_key[s];
+    if (key == kNoKey) continue;
+    const float dmin = __uint_as_float(static_cast<unsigned int>(key >> 32));
+    if (dmin < depth) {
+      depth = dmin;
+      win_slot = s;
+      win_pos = static_cast<int>(key & 0xffffffffu);
+      run_tmin = depth;
+    }
+  }
+  float fn[3] = {0.0f, 0.0f, 0.0f};
+  int av = -1, af = -1;
+  if (win_slot >= 0) {
+    float o[3], d[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      o[k] = rb.rays[6 * ray + k];
+      d[k] = rb.rays[6 * ray + 3 + k];
+    }
+    const int leaf = rb.slot_leaf[base + win_slot];
+    const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + win_pos]];
+    const float3 c[3] = {xyz(__ldcg(&m.co[tv.x])), xyz(__ldcg(&m.co[tv.y])),
+                         xyz(__ldcg(&m.co[tv.z]))};
+    RayTri rt;
+    raytri_init(rt, d);
+    float dt = depth;
+    raytri_hit(o, rt, c[0], c[1], c[2], &dt);  // the exact value (-0 kept)
+    depth = dt;
+    const float3 n = normal_tri(c[0], c[1], c[2]);
+    fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
+    const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
+    const int ids[3] = {tv.x, tv.y, tv.z};
+    float3 nearest = c[0];
+    int best = 0;
+    for (int j = 1; j < 3; j++)
+      if (len_sq(loc, c[j]) < len_sq(loc, nearest)) {
+        nearest = c[j];
+        best = j;
+      }
+    av = rb.n2o ? rb.n2o[ids[best]] : ids[best];
+    af = tv.w;
+  }
+  rb.depth_out[ray] = depth;
+  rb.hit[ray] = win_slot >= 0;
+  rb.active_vertex[ray] = av;
+  rb.active_face[ray] = af;
+  rb.face_normal[3 * ray] = fn[0];
+  rb.face_normal[3 * ray + 1] = fn[1];
+  rb.face_normal[3 * ray + 2] = fn[2];
+}
+
+}  // namespace
+
+size_t ray_leaves_smem(const DevMesh& m) {
+  return sizeof(float) * m.totnode + sizeof(int) * m.totnode + sizeof(float) * m.nleaf +
+         static_cast<size_t>(m.totnode) + 16;
+}
+size_t ray_finish_smem(const DevMesh& m) {
+  return (sizeof(unsigned long long) + sizeof(float) + sizeof(int)) * static_cast<size_t>(m.nleaf) + 16;
+}
+int ray_items_per_ray(const DevMesh& m) {
+  return m.totlt / kRayChunk + m.nleaf;
+}
+
+cudaError_t configure_ray_kernels(size_t leaves_smem, size_t finish_smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_ray_leaves, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(leaves_smem));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_ray_finish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(finish_smem));
+}
+
+cudaError_t launch_raycast(const DevMesh& m, const RayBatch& rb, int nrays, int tris_grid,
+                           cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(rb.nitems, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  k_ray_leaves<<<nrays, kRayThreads, ray_leaves_smem(m), s>>>(m, rb);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_ray_tris<<<tris_grid, kRayThreads, 0, s>>>(m, rb);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_ray_finish<<<nrays, kRayThreads, ray_finish_smem(m), s>>>(m, rb);
+  return cudaGetLastError();
+}
+
+}  // namespace sgpu

@@ -61,6 +61,7 @@ struct DevMesh {
   const int2* poly;     // loopstart, totloop
   const int4* poly_v4;  // corner vertices of a triangle (w = -1) or quad; x = -1 otherwise
   const int* loop_v;
+  const int4* lt_v4;    // per looptri: its three corner vertices and its poly
   const int* vt_off;
   const int2* vt_meta;  // per vertex, its looptris in ascending order: (poly, leaf id)
   const int* nb_off;

@@ -1,0 +1,40 @@
+// Ray-cast batch of libsculptgpu (kernels_ray.cu): device arrays of one launch.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sgpu_device.cuh"
+
+namespace sgpu {
+
+struct RayBatch {
+  const float* rays;      // 6 per ray: start xyz, unit direction xyz
+  const float* depth_in;  // per ray: ray length (nullable: FLT_MAX)
+  int original;           // boxes from orig_vb instead of vb
+  const int* n2o;         // device -> caller vertex numbering (nullable: identity)
+  // per ray and listed leaf (nleaf slots per ray)
+  int* count;
+  int* slot_leaf;
+  float* slot_tmin;
+  int* slot_order;
+  unsigned long long* slot_key;
+  // work items (ray * nleaf + slot, chunk) and their count
+  int2* items;
+  int* nitems;
+  int item_cap;
+  // results per ray
+  float* depth_out;
+  int* hit;
+  int* active_vertex;
+  int* active_face;
+  float* face_normal;  // 3 per ray
+};
+
+size_t ray_leaves_smem(const DevMesh& m);
+size_t ray_finish_smem(const DevMesh& m);
+int ray_items_per_ray(const DevMesh& m);
+cudaError_t configure_ray_kernels(size_t leaves_smem, size_t finish_smem);
+cudaError_t launch_raycast(const DevMesh& m, const RayBatch& rb, int nrays, int tris_grid,
+                           cudaStream_t s);
+
+}  // namespace sgpu

@@ -84,6 +84,7 @@ EXPORTS = (
     "sgpu_stroke_host", "sgpu_mesh_snapshot", "sgpu_mesh_restore", "sgpu_stroke_profile",
     "sgpu_mesh_flush_l2", "sgpu_host_alloc", "sgpu_host_free", "sgpu_mesh_set_team",
     "sgpu_mesh_get_team", "sgpu_autotune_team", "sgpu_batch_stroke", "sgpu_stroke_team_profile",
+    "sgpu_raycast",
 )
 
 _lib = None
@@ -110,6 +111,7 @@ def load(path: str | None = None):
     L.sgpu_mesh_stream.argtypes = [vp]
     L.sgpu_mesh_stream.restype = vp
     L.sgpu_search_sphere.argtypes = [vp, vp, f, i, vp, vp]
+    L.sgpu_raycast.argtypes = [vp, i, vp, vp, vp, i, vp, vp, vp, vp, vp]
     for name in ("sgpu_do_draw_brush", "sgpu_do_smooth_brush", "sgpu_do_inflate_brush",
                  "sgpu_do_clay_strips_brush", "sgpu_do_brush"):
         getattr(L, name).argtypes = [vp, C.POINTER(SGPU_Brush), vp, vp, vp, i]
@@ -305,6 +307,23 @@ class PBVH:
         _check(load().sgpu_search_sphere(self._h, _p(c), radius_sq, original, _p(out),
                                          C.byref(tot)))
         return out[:tot.value]
+
+    def raycast(self, starts, normals, lengths=None, original: int = 0):
+        """BKE_pbvh_raycast with the sculpt callback for a batch of rays.
+        Returns (hit bool[n], depth float32[n], active vertex int32[n],
+        active face int32[n], face normal float32[n, 3])."""
+        o = np.ascontiguousarray(starts, dtype=np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        n = o.shape[0]
+        ln = None if lengths is None else np.ascontiguousarray(lengths, dtype=np.float32)
+        dep = np.zeros(n, dtype=np.float32)
+        hit = np.zeros(n, dtype=np.int32)
+        av = np.zeros(n, dtype=np.int32)
+        af = np.zeros(n, dtype=np.int32)
+        fn = np.zeros((n, 3), dtype=np.float32)
+        _check(load().sgpu_raycast(self._h, n, _p(o), _p(d), _p(ln), original, _p(dep), _p(hit),
+                                   _p(av), _p(af), _p(fn)))
+        return hit.astype(bool), dep, av, af, fn
 
     def search_sphere_device(self, center, radius_sq: float, original: int = 0):
         c = np.asarray(center, dtype=np.float32)

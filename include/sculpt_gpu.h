@@ -236,6 +236,23 @@ int sgpu_stroke_team_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGP
                              int ndabs, const int *dab_tools, SGPU_TeamProfile *out,
                              SGPU_StrokeStats *stats);
 
+/* ---- ray cast (PBVH_FACES) ----
+ * Replaces BKE_pbvh_raycast (pbvh.c:3916) driven by the sculpt ray-cast
+ * callback, which the reference calls but does not ship (sculpt.c is absent):
+ * leaves in order of their box entry distance (BKE_pbvh_search_callback_occluded,
+ * pbvh.c:2853), a leaf cast while its entry distance is below the running
+ * minimum, pbvh_faces_node_raycast (pbvh.c:4042) inside it.  nrays independent
+ * rays; ray_starts / ray_normals 3 floats each (unit directions);
+ * ray_lengths (nullable: FLT_MAX) the initial depth; original selects
+ * orig_vb.  Results per ray: depth (initial depth when no hit), hit 0/1,
+ * active vertex (caller numbering, -1 without a hit), active face (poly, -1)
+ * and the hit triangle's normal (3 floats, zero without a hit); the last three
+ * outputs are nullable.  The first call with more rays than any before it
+ * allocates the batch buffers. */
+int sgpu_raycast(sgpu_mesh *mesh, int nrays, const float *ray_starts, const float *ray_normals,
+                 const float *ray_lengths, int original, float *r_depths, int *r_hits,
+                 int *r_active_vertices, int *r_active_faces, float *r_face_normals);
+
 /* ---- batches of independent meshes ----
  * Mesh i strokes with brushes[i] over dabs[dab_offsets[i] .. dab_offsets[i+1]);
  * dab_tools (nullable) is indexed like dabs.
