@@ -32,7 +32,7 @@ command profiled with ncu).  --phases prints the persistent kernel's per-dab
 phase profile on all five workloads.
 
 --impl reference times the CPU restatement of the reference path (the
-reference itself does not build: its headers and brush code are missing).
+reference cannot run the path: its brush code and public headers are missing).
 Under torchrun (N>1) each rank runs an independent replica (the path does not
 shard within a mesh); rank 0 prints max-over-ranks timing.
 """
@@ -59,7 +59,7 @@ UNIT = "verts/s"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--cpu-sample-dabs", type=int, default=0,
@@ -185,6 +185,16 @@ class ClockSampler:
         except Exception:
             self.proc = None
 
+    def wait_first(self, timeout: float = 5.0):
+        """Blocks until the first sample is written, so that sampling covers
+        the timed region from its start."""
+        t0 = time.perf_counter()
+        while self.proc is not None and time.perf_counter() - t0 < timeout:
+            self.f.flush()
+            if os.path.getsize(self.path) > 0:
+                return
+            time.sleep(0.02)
+
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -272,8 +282,8 @@ def run_reference(args):
             "data": "synthetic (seeded)", "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"first {sample} of {st.dabs.shape[0]} dabs per step "
-                                       "(FP32 CPU restatement of the reference path; the "
-                                       "reference itself does not compile)"},
+                                       "(FP32 CPU restatement of the reference path: the "
+                                       "reference has no brush code to run)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -308,6 +318,8 @@ def run_gpu(args):
         g.stroke(st, mode=STROKE_TEAM)
     barrier()
     clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.wait_first()
     total_ms, total_v, launches = 0.0, 0, 0
     for _ in range(args.steps):
         g.restore()
@@ -362,6 +374,8 @@ def run_gpu(args):
 
     batch = None if args.no_batch else run_batch(args, synth, PBVH, batch_stroke, BATCH_TEAM,
                                                   BATCH_SEQUENTIAL)
+    g.restore()
+    ray = run_raycast_leg(g, m, leaf_limit, args.no_cpu)
 
     if world > 1:
         import torch
@@ -408,11 +422,57 @@ def run_gpu(args):
         "plain_graph": plain_graph,
         "plain_eager": plain_eager,
         "batch": batch,
+        "raycast": ray,
         "cpu_baseline": ({k: v for k, v in cpu.items() if k != "seconds"} if cpu else None),
         "clocks": clk,
     }
     print(json.dumps(line))
     return 0
+
+
+def run_raycast_leg(g, m, leaf_limit, no_cpu):
+    """Ray cast (BKE_pbvh_raycast with the sculpt callback) on the workload's
+    mesh: 1024 seeded rays from a sphere of radius 3 towards points near the
+    centre, through sgpu_raycast with host arrays (upload, three kernels,
+    read-back in the timed region); one ray per call for the latency; the
+    oracle's restatement on one host core for 128 of the rays."""
+    rng = np.random.default_rng(0x5EED0000 + 7)
+    n = 1024
+    s = rng.normal(size=(n, 3))
+    starts = (3.0 * s / np.linalg.norm(s, axis=1, keepdims=True)).astype(np.float32)
+    tgt = rng.normal(size=(n, 3)) * 0.3
+    d = tgt - starts
+    dirs = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    g.raycast(starts, dirs)  # batch buffers allocated outside the timing
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        hit, _, _, _, _ = g.raycast(starts, dirs)
+    batch_s = (time.perf_counter() - t0) / reps
+    one = 200
+    t0 = time.perf_counter()
+    for k in range(one):
+        g.raycast(starts[k % n:k % n + 1], dirs[k % n:k % n + 1])
+    single_s = (time.perf_counter() - t0) / one
+    out = {"workload": "1024 rays from radius 3 towards the centre (+/-0.3), icosphere level 8",
+           "hits": int(hit.sum()), "rays_per_s": n / batch_s, "ms_per_1024_rays": 1e3 * batch_s,
+           "single_ray_us": 1e6 * single_s, "timing": "wall clock around sgpu_raycast "
+           "(host arrays in and out)"}
+    if not no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        o = pyoracle.OracleMesh.faces(m, leaf_limit)
+        o.recalc_all_normals()
+        k = 128
+        t0 = time.perf_counter()
+        for r in range(k):
+            o.raycast(starts[r], dirs[r])
+        cpu_s = time.perf_counter() - t0
+        out["cpu_baseline"] = {"rays_per_s": k / cpu_s, "cores": 1, "kind": "port",
+                               "sample": f"{k} of the rays, FP32 restatement, one thread"}
+        o.close()
+    return out
 
 
 def run_batch(args, synth, PBVH, batch_stroke, BATCH_TEAM, BATCH_SEQUENTIAL):
