@@ -69,6 +69,9 @@ def parse_args():
     ap.add_argument("--quick", action="store_true",
                     help="three persistent strokes of the workload, no report (for ncu)")
     ap.add_argument("--cluster", type=int, default=16, help="cluster size for --quick")
+    ap.add_argument("--raycast-only", action="store_true",
+                    help="three 1024-ray sgpu_raycast batches on the workload mesh and exit "
+                         "(the command profiled with ncu for the ray kernels)")
     ap.add_argument("--phases", action="store_true",
                     help="per-phase profile of the persistent stroke on all five workloads "
                          "(one JSON line each), no report")
@@ -526,6 +529,18 @@ def main():
         return run_quick(args)
     if args.phases:
         return run_phases(args)
+    if args.raycast_only:
+        from dune_sculpt_gb300 import build as libbuild
+
+        libbuild.build()
+        from dune_sculpt_gb300.sculpt import PBVH
+
+        m, _, leaf_limit, _ = workload()
+        g = PBVH.build_mesh(m, leaf_limit)
+        for _ in range(3):
+            r = run_raycast_leg(g, m, leaf_limit, True)
+        print(f"raycast: {r['hits']} hits, {r['ms_per_1024_rays']:.3f} ms per 1024 rays")
+        return 0
     return run_gpu(args)
 
 

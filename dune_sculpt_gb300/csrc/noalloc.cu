@@ -2,7 +2,8 @@
 //
 // For callers that cannot allocate device memory: a host that runs inside a
 // memory budget fixed up front (an embedding application's pool, a plug-in
-// sandbox, a CUDA graph built by someone else), so it can neither create a
+// sandbox, an interactive loop that must not allocate while a stroke runs), so
+// it can neither create a
 // mesh handle (which allocates) nor call cudaMalloc itself.  They keep the
 // mesh arrays in device memory they already own and pass them in; the
 // Jacobi scratch of the smooth sweeps lives in a fixed file-scope device array

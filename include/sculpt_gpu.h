@@ -305,8 +305,8 @@ int sgpu_host_free(void *ptr);
 /* ---- allocation-free smooth dab ----
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory — an application embedding this library under a device-memory budget
- * it fixed up front, a plug-in host that forbids allocation, code recorded
- * into a CUDA graph someone else owns — and so cannot create a mesh handle
+ * it fixed up front, a plug-in host that forbids allocation, an interactive
+ * loop that must not allocate while a stroke runs — and so cannot create a mesh handle
  * (creating one allocates).  They pass device arrays they already own: co (4
  * floats per vertex, the MVert layout, moved in place), normals (4 floats per
  * vertex, read only for SGPU_BRUSH_FRONTFACE; may be NULL otherwise), mask and
