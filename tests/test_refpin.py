@@ -37,7 +37,7 @@ import pytest
 
 import pyrefpin
 from dune_sculpt_gb300 import synth
-from helpers import bits_equal, first_diff, small_icosphere, small_uvsphere
+from helpers import bits_equal, first_diff, material_grid, ngon_mesh, small_icosphere, small_uvsphere
 
 pytestmark = pytest.mark.skipif(not pyrefpin.available(),
                                 reason="reference tree absent: the pinning library cannot be built")
@@ -46,59 +46,6 @@ LEAF = 1          # PBVH_Leaf
 UPD_BB = 4        # PBVH_UpdateBB
 UPD_ORIG_BB = 8   # PBVH_UpdateOriginalBB
 NORMAL_ATOL = 1e-6
-
-
-def ngon_mesh(nq: int = 120) -> synth.FacesMesh:
-    """A grid whose quads are merged in pairs into hexagons (n-gon polys,
-    fan looptris), with a few triangles and quads left over at the row ends,
-    and a smooth height field so the Newell normals are not all +Z."""
-    n = nq + 1
-    j, i = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
-    x = i.reshape(-1) / nq
-    y = j.reshape(-1) / nq
-    z = 0.05 * np.sin(6.0 * x) * np.cos(5.0 * y)
-    co = synth._f32(np.stack([x, y, z], 1))
-    polys = []
-    for qj in range(nq):
-        qi = 0
-        while qi < nq:
-            v00 = qj * n + qi
-            if qi + 1 < nq and (qi + qj) % 5 != 4:
-                polys.append([v00, v00 + 1, v00 + 2, v00 + 2 + n, v00 + 1 + n, v00 + n])
-                qi += 2
-            else:
-                polys.append([v00, v00 + 1, v00 + 1 + n])
-                polys.append([v00, v00 + 1 + n, v00 + n])
-                qi += 1
-    P = len(polys)
-    sizes = np.array([len(p) for p in polys], dtype=np.int32)
-    verts = np.zeros(n * n, dtype=synth.MVERT_DT)
-    verts["co"] = co
-    mp = np.zeros(P, dtype=synth.MPOLY_DT)
-    mp["totloop"] = sizes
-    mp["loopstart"] = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int32)
-    mp["flag"] = 1
-    loops = np.zeros(int(sizes.sum()), dtype=synth.MLOOP_DT)
-    loops["v"] = np.concatenate(polys).astype(np.uint32)
-    tris = []
-    for p, ls in enumerate(mp["loopstart"]):
-        for k in range(1, sizes[p] - 1):
-            tris.append((ls, ls + k, ls + k + 1, p))
-    lt = np.zeros(len(tris), dtype=synth.MLOOPTRI_DT)
-    t = np.array(tris, dtype=np.uint32)
-    lt["tri"] = t[:, :3]
-    lt["poly"] = t[:, 3]
-    return synth.FacesMesh(verts=verts, polys=mp, loops=loops, looptris=lt, kind="ngon")
-
-
-def material_grid(nq: int = 96) -> synth.FacesMesh:
-    """A flat grid whose polys carry four materials in stripes and a flat/smooth
-    checker, so leaves are split by material (partition_indices_material)."""
-    m = synth.grid_mesh(nq)
-    p = np.arange(m.polys.shape[0])
-    m.polys["mat_nr"] = ((p % nq) * 4 // nq).astype(np.int16)
-    m.polys["flag"] = np.where((p // (nq * 8)) % 2 == 0, 1, 0).astype(m.polys["flag"].dtype)
-    return m
 
 
 MESHES = {
