@@ -102,13 +102,19 @@ struct sgpu_mesh {
   // page-locked displaced counters of the last persistent launch
   unsigned long long* h_disp = nullptr;
   size_t h_disp_cap = 0;
-  // ray-cast batch buffers (grown to the largest batch; see sgpu_raycast)
+  // ray-cast batch buffers (grown to the largest batch; see sgpu_raycast):
+  // one device block and one page-locked host block with the same layout,
+  // 7 floats in per ray (start, direction, length), 4 floats and 3 ints out
+  // per ray (depth, face normal; hit, active vertex, active face), then the
+  // error word
   RayBatch ray{};
-  float* ray_in = nullptr;   // 7 per ray: start, direction, length
-  float* ray_out = nullptr;  // 4 per ray: depth, face normal
-  int* ray_iout = nullptr;   // 3 per ray: hit, active vertex, active face
+  unsigned char* ray_dev = nullptr;
+  unsigned char* ray_host = nullptr;
   size_t ray_cap = 0;
   bool ray_configured = false;
+  // the captured call (copies in, kernels, copies out) for (rays, original)
+  cudaGraphExec_t ray_graph = nullptr;
+  int ray_graph_n = -1, ray_graph_orig = -1;
 
   cudaEvent_t prof_event() {
     if (ev_used == ev_pool.size()) {
@@ -178,15 +184,16 @@ struct sgpu_mesh {
     if (h_disp) cudaFreeHost(h_disp);
     h_disp = nullptr;
     h_disp_cap = 0;
-    for (void* p : {static_cast<void*>(ray_in), static_cast<void*>(ray_out),
-                    static_cast<void*>(ray_iout), static_cast<void*>(ray.count),
+    if (ray_graph) cudaGraphExecDestroy(ray_graph);
+    ray_graph = nullptr;
+    for (void* p : {static_cast<void*>(ray_dev), static_cast<void*>(ray.count),
                     static_cast<void*>(ray.slot_leaf), static_cast<void*>(ray.slot_tmin),
                     static_cast<void*>(ray.slot_order), static_cast<void*>(ray.slot_key),
                     static_cast<void*>(ray.items), static_cast<void*>(ray.nitems)})
       if (p) cudaFree(p);
+    if (ray_host) cudaFreeHost(ray_host);
     ray = RayBatch{};
-    ray_in = ray_out = nullptr;
-    ray_iout = nullptr;
+    ray_dev = ray_host = nullptr;
     ray_cap = 0;
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -1718,25 +1725,37 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
 
 namespace {
 
-// Ray-cast buffers for up to n rays (grown, never shrunk).
+// Byte offsets in the ray-cast blocks for a capacity of n rays.
+struct RayLayout {
+  size_t in, out_f, out_i, err, total;
+  explicit RayLayout(size_t n)
+      : in(0), out_f(sizeof(float) * 7 * n), out_i(out_f + sizeof(float) * 4 * n),
+        err(out_i + sizeof(int) * 3 * n), total(err + 16) {}
+};
+
+// Ray-cast buffers for up to n rays (grown, never shrunk; growing drops the
+// captured call).
 int ensure_ray_buffers(sgpu_mesh* m, int n) {
-  if (static_cast<size_t>(n) <= m->ray_cap && m->ray_in) return SGPU_OK;
+  if (static_cast<size_t>(n) <= m->ray_cap && m->ray_dev) return SGPU_OK;
   const int L = m->dev.nleaf;
   const size_t slots = static_cast<size_t>(n) * L;
   const size_t items = static_cast<size_t>(n) * ray_items_per_ray(m->dev);
   if (items > 0x7fffffffull) return fail(SGPU_ERR_UNSUPPORTED, "ray batch too large for the mesh");
-  void* p[10] = {m->ray_in, m->ray_out, m->ray_iout, m->ray.count, m->ray.slot_leaf,
-                 m->ray.slot_tmin, m->ray.slot_order, m->ray.slot_key, m->ray.items,
-                 m->ray.nitems};
+  if (m->ray_graph) cudaGraphExecDestroy(m->ray_graph);
+  m->ray_graph = nullptr;
+  m->ray_graph_n = m->ray_graph_orig = -1;
+  void* p[8] = {m->ray_dev, m->ray.count, m->ray.slot_leaf, m->ray.slot_tmin,
+                m->ray.slot_order, m->ray.slot_key, m->ray.items, m->ray.nitems};
   for (void* q : p)
     if (q) cudaFree(q);
+  if (m->ray_host) cudaFreeHost(m->ray_host);
   m->ray = RayBatch{};
-  m->ray_in = m->ray_out = nullptr;
-  m->ray_iout = nullptr;
+  m->ray_dev = m->ray_host = nullptr;
   m->ray_cap = 0;
-  CK(cudaMalloc(&m->ray_in, sizeof(float) * 7 * n), "cudaMalloc");
-  CK(cudaMalloc(&m->ray_out, sizeof(float) * 4 * n), "cudaMalloc");
-  CK(cudaMalloc(&m->ray_iout, sizeof(int) * 3 * n), "cudaMalloc");
+  const RayLayout lay(static_cast<size_t>(n));
+  CK(cudaMalloc(&m->ray_dev, lay.total), "cudaMalloc");
+  CK(cudaHostAlloc(reinterpret_cast<void**>(&m->ray_host), lay.total, cudaHostAllocDefault),
+     "cudaHostAlloc");
   CK(cudaMalloc(&m->ray.count, sizeof(int) * n), "cudaMalloc");
   CK(cudaMalloc(&m->ray.slot_leaf, sizeof(int) * slots), "cudaMalloc");
   CK(cudaMalloc(&m->ray.slot_tmin, sizeof(float) * slots), "cudaMalloc");
@@ -1769,39 +1788,69 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
     CK(configure_ray_kernels(ray_leaves_smem(d), ray_finish_smem(d)), "ray kernel attributes");
     mesh->ray_configured = true;
   }
-  std::vector<float> in(7 * static_cast<size_t>(nrays));
+  // inputs and outputs live at the offsets of a batch of exactly nrays rays
+  const RayLayout lay(static_cast<size_t>(nrays));
+  float* hin = reinterpret_cast<float*>(mesh->ray_host + lay.in);
   for (int r = 0; r < nrays; r++) {
     for (int k = 0; k < 3; k++) {
-      in[6 * r + k] = ray_starts[3 * r + k];
-      in[6 * r + 3 + k] = ray_normals[3 * r + k];
+      hin[6 * r + k] = ray_starts[3 * r + k];
+      hin[6 * r + 3 + k] = ray_normals[3 * r + k];
     }
-    in[6 * static_cast<size_t>(nrays) + r] = ray_lengths ? ray_lengths[r] : FLT_MAX;
+    hin[6 * static_cast<size_t>(nrays) + r] = ray_lengths ? ray_lengths[r] : FLT_MAX;
   }
   cudaStream_t s = mesh->stream;
-  CK(cudaMemcpyAsync(mesh->ray_in, in.data(), sizeof(float) * in.size(), cudaMemcpyHostToDevice, s),
-     "upload rays");
-  RayBatch rb = mesh->ray;
-  rb.rays = mesh->ray_in;
-  rb.depth_in = mesh->ray_in + 6 * static_cast<size_t>(nrays);
-  rb.original = original;
-  rb.n2o = mesh->d_n2o;
-  rb.depth_out = mesh->ray_out;
-  rb.face_normal = mesh->ray_out + nrays;
-  rb.hit = mesh->ray_iout;
-  rb.active_vertex = mesh->ray_iout + nrays;
-  rb.active_face = mesh->ray_iout + 2 * static_cast<size_t>(nrays);
-  int sms = 0, dev = 0;
-  CK(cudaGetDevice(&dev), "cudaGetDevice");
-  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
-  CK(launch_raycast(d, rb, nrays, 8 * sms, s), "ray kernels");
-  std::vector<float> fo(4 * static_cast<size_t>(nrays));
-  std::vector<int> io(3 * static_cast<size_t>(nrays));
-  CK(cudaMemcpyAsync(fo.data(), mesh->ray_out, sizeof(float) * fo.size(), cudaMemcpyDeviceToHost, s),
-     "read results");
-  CK(cudaMemcpyAsync(io.data(), mesh->ray_iout, sizeof(int) * io.size(), cudaMemcpyDeviceToHost, s),
-     "read results");
+  if (!mesh->ray_graph || mesh->ray_graph_n != nrays || mesh->ray_graph_orig != original) {
+    if (mesh->ray_graph) cudaGraphExecDestroy(mesh->ray_graph);
+    mesh->ray_graph = nullptr;
+    RayBatch rb = mesh->ray;
+    float* din = reinterpret_cast<float*>(mesh->ray_dev + lay.in);
+    float* dout = reinterpret_cast<float*>(mesh->ray_dev + lay.out_f);
+    int* diout = reinterpret_cast<int*>(mesh->ray_dev + lay.out_i);
+    rb.rays = din;
+    rb.depth_in = din + 6 * static_cast<size_t>(nrays);
+    rb.original = original;
+    rb.n2o = mesh->d_n2o;
+    rb.depth_out = dout;
+    rb.face_normal = dout + nrays;
+    rb.hit = diout;
+    rb.active_vertex = diout + nrays;
+    rb.active_face = diout + 2 * static_cast<size_t>(nrays);
+    int sms = 0, dev = 0;
+    CK(cudaGetDevice(&dev), "cudaGetDevice");
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    // one graph: rays in, the three kernels, results and error word out
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t e = cudaMemcpyAsync(mesh->ray_dev + lay.in, mesh->ray_host + lay.in,
+                                    lay.out_f - lay.in, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_raycast(d, rb, nrays, 8 * sms, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(mesh->ray_host + lay.out_f, mesh->ray_dev + lay.out_f,
+                          lay.err - lay.out_f, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(mesh->ray_host + lay.err, &d.work->err, sizeof(int),
+                          cudaMemcpyDeviceToHost, s);
+    const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&mesh->ray_graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      mesh->ray_graph = nullptr;
+      return cuda_fail(e, "ray-cast graph");
+    }
+    mesh->ray_graph_n = nrays;
+    mesh->ray_graph_orig = original;
+  }
+  CK(cudaGraphLaunch(mesh->ray_graph, s), "ray-cast graph launch");
   CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-  if ((rc = device_err(mesh))) return rc;
+  const int err = *reinterpret_cast<int*>(mesh->ray_host + lay.err);
+  if (err) {
+    CK(cudaMemsetAsync(&d.work->err, 0, sizeof(int), s), "reset error word");
+    CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    return fail(err, "a ray-cast kernel reported error code %d", err);
+  }
+  const float* fo = reinterpret_cast<const float*>(mesh->ray_host + lay.out_f);
+  const int* io = reinterpret_cast<const int*>(mesh->ray_host + lay.out_i);
   for (int r = 0; r < nrays; r++) {
     r_depths[r] = fo[r];
     r_hits[r] = io[r];

@@ -248,7 +248,9 @@ int sgpu_stroke_team_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGP
  * active vertex (caller numbering, -1 without a hit), active face (poly, -1)
  * and the hit triangle's normal (3 floats, zero without a hit); the last three
  * outputs are nullable.  The first call with more rays than any before it
- * allocates the batch buffers. */
+ * allocates the batch buffers (device and page-locked host); the first call
+ * for a given (nrays, original) captures the call (copies in, kernels, copies
+ * out) as a CUDA graph that later calls with the same shape replay. */
 int sgpu_raycast(sgpu_mesh *mesh, int nrays, const float *ray_starts, const float *ray_normals,
                  const float *ray_lengths, int original, float *r_depths, int *r_hits,
                  int *r_active_vertices, int *r_active_faces, float *r_face_normals);
