@@ -114,6 +114,10 @@ int or_raycast(OrMesh *m, const float ray_start[3], const float ray_normal[3], i
                float *depth, int *active_vertex, int *active_face, float face_normal[3],
                int *r_nleaves);
 
+/* Test helper: grid quads whose two triangles both meet the ray, the second
+ * one closer. */
+int or_grids_special_quads(OrMesh *m, const float ray_start[3], const float ray_normal[3]);
+
 /* Falloff curve of a brush preset (colortools.c): table 257*(x,y), params
  * {mintable, maxtable, range, ext_in[2], ext_out[2]}. */
 void or_curve_table(int preset, float *table_xy, float *params);

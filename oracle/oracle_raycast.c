@@ -1,6 +1,6 @@
 /*
- * CPU oracle, part 3: the PBVH ray cast (PBVH_FACES) — TEST INFRASTRUCTURE
- * ONLY (see oracle.h).
+ * CPU oracle, part 3: the PBVH ray cast (PBVH_FACES and PBVH_GRIDS) — TEST
+ * INFRASTRUCTURE ONLY (see oracle.h).
  *
  * Restates, in FP32:
  *   isect_ray_aabb_v3_precalc / isect_ray_aabb_v3        math_geom.cc:3017-3079
@@ -10,8 +10,9 @@
  *   pbvh_iter_next_occluded                               pbvh.c:2708-2735
  *   node_tree_insert, traverse_tree                       pbvh.c:2797-2831
  *   BKE_pbvh_search_callback_occluded                     pbvh.c:2853-2890
- *   ray_face_intersection_tri                             pbvh.c:3952-3967
+ *   ray_face_intersection_tri / _quad                     pbvh.c:3930-3967
  *   pbvh_faces_node_raycast                               pbvh.c:4042-4108
+ *   pbvh_grids_node_raycast                               pbvh.c:4110-4201
  * and the sculpt ray-cast callback the reference calls but does not ship
  * (its sculpt.c is absent), fixed by the brush specification: a leaf is ray
  * cast when its entry distance is below the running minimum (FLT_MAX until
@@ -176,11 +177,89 @@ static void tri_normal(float n[3], const float *v1, const float *v2, const float
   }
 }
 
+/* normal_quad_v3 (math_geom.cc:48-71) followed by normalize_v3 */
+static void quad_normal(float n[3], const float *v1, const float *v2, const float *v3,
+                        const float *v4)
+{
+  float n1[3], n2[3];
+  n1[0] = v1[0] - v3[0];
+  n1[1] = v1[1] - v3[1];
+  n1[2] = v1[2] - v3[2];
+  n2[0] = v2[0] - v4[0];
+  n2[1] = v2[1] - v4[1];
+  n2[2] = v2[2] - v4[2];
+  n[0] = n1[1] * n2[2] - n1[2] * n2[1];
+  n[1] = n1[2] * n2[0] - n1[0] * n2[2];
+  n[2] = n1[0] * n2[1] - n1[1] * n2[0];
+  float d = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+  if (d > 1.0e-35f) {
+    d = sqrtf(d);
+    const float s = 1.0f / d;
+    n[0] = n[0] * s;
+    n[1] = n[1] * s;
+    n[2] = n[2] * s;
+  }
+  else {
+    n[0] = n[1] = n[2] = 0.0f;
+  }
+}
+
+/* pbvh_grids_node_raycast: the grid quads of a leaf in prim / row / column
+ * order; per quad ray_face_intersection_quad, whose second triangle is tried
+ * only when the first one is not taken.  Active vertex = grid element index
+ * (grid * area + y * size + x) of the corner nearest the hit; active face =
+ * the grid index. */
+static int grids_node_raycast(const OrMesh *m, const OrNode *nd, const float *o, const float *dir,
+                              const RayTri *rt, float *depth, int *active_vertex,
+                              int *active_grid, float face_normal[3])
+{
+  const int gs = m->grid_size, area = m->grid_area;
+  static const int x_it[4] = {0, 1, 1, 0};
+  static const int y_it[4] = {0, 0, 1, 1};
+  int hit = 0;
+  for (int i = 0; i < nd->totprim; i++) {
+    const int g = m->prim_indices[nd->prim_off + i];
+    const float *base = m->sf.co + 3 * (size_t)g * area;
+    for (int y = 0; y < gs - 1; y++) {
+      for (int x = 0; x < gs - 1; x++) {
+        const float *co[4] = {base + 3 * (y * gs + x), base + 3 * (y * gs + x + 1),
+                              base + 3 * ((y + 1) * gs + x + 1), base + 3 * ((y + 1) * gs + x)};
+        float dt;
+        int take = 0;
+        if (raytri_hit(o, rt, co[0], co[1], co[2], &dt) && dt < *depth) {
+          take = 1;
+        }
+        else if (raytri_hit(o, rt, co[0], co[2], co[3], &dt) && dt < *depth) {
+          take = 1;
+        }
+        if (!take) {
+          continue;
+        }
+        *depth = dt;
+        hit = 1;
+        quad_normal(face_normal, co[0], co[1], co[2], co[3]);
+        const float loc[3] = {o[0] + dir[0] * dt, o[1] + dir[1] * dt, o[2] + dir[2] * dt};
+        float nearest[3];
+        for (int j = 0; j < 4; j++) {
+          if (j == 0 || len_sq3(loc, co[j]) < len_sq3(loc, nearest)) {
+            nearest[0] = co[j][0];
+            nearest[1] = co[j][1];
+            nearest[2] = co[j][2];
+            *active_vertex = area * g + (y + y_it[j]) * gs + (x + x_it[j]);
+          }
+        }
+        *active_grid = g;
+      }
+    }
+  }
+  return hit;
+}
+
 int or_raycast(OrMesh *m, const float ray_start[3], const float ray_normal[3], int original,
                float *depth, int *active_vertex, int *active_face, float face_normal[3],
                int *r_nleaves)
 {
-  if (m->type != OR_FACES || m->totnode == 0) {
+  if (m->totnode == 0) {
     if (r_nleaves) {
       *r_nleaves = 0;
     }
@@ -245,7 +324,14 @@ int or_raycast(OrMesh *m, const float ray_start[3], const float ray_normal[3], i
       cur = left[cur];
     }
     cur = st[--sp];
-    if (tmin[cur] < run_tmin) {
+    if (tmin[cur] < run_tmin && m->type == OR_GRIDS) {
+      if (grids_node_raycast(m, &m->nodes[leaf[cur]], ray_start, ray_normal, &rt, &d,
+                             active_vertex, active_face, face_normal)) {
+        hit = 1;
+        run_tmin = d;
+      }
+    }
+    else if (tmin[cur] < run_tmin) {
       /* pbvh_faces_node_raycast over the leaf's looptris in prim order */
       const OrNode *nd = &m->nodes[leaf[cur]];
       int node_hit = 0;
@@ -288,4 +374,33 @@ int or_raycast(OrMesh *m, const float ray_start[3], const float ray_normal[3], i
   free(left);
   free(right);
   return hit;
+}
+
+/* Test helper: quads of the whole grid mesh where both triangles meet the ray
+ * and the second one is closer (dB < dA) — the case in which
+ * ray_face_intersection_quad's order matters. */
+int or_grids_special_quads(OrMesh *m, const float ray_start[3], const float ray_normal[3])
+{
+  if (m->type != OR_GRIDS) {
+    return 0;
+  }
+  RayTri rt;
+  raytri_init(&rt, ray_normal);
+  const int gs = m->grid_size, area = m->grid_area;
+  int n = 0;
+  for (int g = 0; g < m->num_grids; g++) {
+    const float *base = m->sf.co + 3 * (size_t)g * area;
+    for (int y = 0; y < gs - 1; y++) {
+      for (int x = 0; x < gs - 1; x++) {
+        const float *co[4] = {base + 3 * (y * gs + x), base + 3 * (y * gs + x + 1),
+                              base + 3 * ((y + 1) * gs + x + 1), base + 3 * ((y + 1) * gs + x)};
+        float da, db;
+        if (raytri_hit(ray_start, &rt, co[0], co[1], co[2], &da) &&
+            raytri_hit(ray_start, &rt, co[0], co[2], co[3], &db) && db < da) {
+          n++;
+        }
+      }
+    }
+  }
+  return n;
 }

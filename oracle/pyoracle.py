@@ -64,6 +64,8 @@ def lib():
         L.or_stroke.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
         L.or_raycast.restype = i
         L.or_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp, vp]
+        L.or_grids_special_quads.restype = i
+        L.or_grids_special_quads.argtypes = [vp, vp, vp]
         L.or_curve_table.argtypes = [i, vp, vp]
         L.or_curve_strength.restype = f
         L.or_curve_strength.argtypes = [i, f, f]
@@ -265,6 +267,11 @@ class OracleMesh:
         hit = lib().or_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(af), _p(fn),
                                _p(nl))
         return bool(hit), dep[0], int(av[0]), int(af[0]), fn, int(nl[0])
+
+    def grids_special_quads(self, ray_start, ray_normal) -> int:
+        o = np.asarray(ray_start, dtype=np.float32)
+        d = np.asarray(ray_normal, dtype=np.float32)
+        return int(lib().or_grids_special_quads(self.h, _p(o), _p(d)))
 
     def stroke(self, st, which: int = 3, nthreads: int = 0, dabs=None, dab_tools=None):
         b = make_brush(st)

@@ -81,6 +81,8 @@ def lib():
         L.rg_vertex_num_faces.restype = i
         L.rg_vertex_num_faces.argtypes = [vp, i]
         L.rg_vertex_coords.argtypes = [vp, i, vp]
+        L.rg_raycast.restype = i
+        L.rg_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
         L.rp_raycast.restype = i
         L.rp_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
         L.rp_curve_table.argtypes = [i, vp, vp]
@@ -303,6 +305,19 @@ class RefGrids:
         for f in range(nf):
             lib().rg_edge_coords(self.h, edge, f, _p(out[f]))
         return out
+
+    def raycast(self, ray_start, ray_normal, depth: float = 3.4028234663852886e38,
+                original: int = 0):
+        """BKE_pbvh_raycast on the grids: (hit, depth, active element, active
+        grid, face normal)."""
+        o = np.asarray(ray_start, dtype=np.float32)
+        d = np.asarray(ray_normal, dtype=np.float32)
+        dep = np.array([depth], dtype=np.float32)
+        av = np.array([-1], dtype=np.int32)
+        ag = np.array([-1], dtype=np.int32)
+        fn = np.zeros(3, dtype=np.float32)
+        hit = lib().rg_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(ag), _p(fn))
+        return bool(hit), dep[0], int(av[0]), int(ag[0]), fn
 
     def vertex_coords(self, vertex: int) -> np.ndarray:
         nf = lib().rg_vertex_num_faces(self.h, vertex)

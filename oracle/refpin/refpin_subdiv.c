@@ -380,3 +380,47 @@ int poly_find_loop_from_vert(const MPoly *poly, const MLoop *loopstart, unsigned
   subdiv_unreachable("coarse mesh adjacency");
   return -1;
 }
+
+/* BKE_pbvh_raycast on the grids PBVH with the sculpt ray-cast callback of the
+ * brush specification (the same rule as rp_raycast): active vertex = grid
+ * element index, active face = grid index. */
+typedef struct GridRaycastCb {
+  PBVH *pbvh;
+  const float *start, *normal;
+  IsectRayPrecalc isect;
+  float depth;
+  int active_vertex, active_grid;
+  float face_normal[3];
+  bool hit;
+} GridRaycastCb;
+
+static void grid_raycast_cb(PBVHNode *node, void *data_v, float *tmin)
+{
+  GridRaycastCb *d = data_v;
+  if (BKE_pbvh_node_get_tmin(node) < *tmin) {
+    if (BKE_pbvh_node_raycast(d->pbvh, node, NULL, false, d->start, d->normal, &d->isect,
+                              &d->depth, &d->active_vertex, &d->active_grid, d->face_normal)) {
+      d->hit = true;
+      *tmin = d->depth;
+    }
+  }
+}
+
+int rg_raycast(RefGrids *g, const float start[3], const float normal[3], int original,
+               float *depth, int *active_vertex, int *active_grid, float face_normal[3])
+{
+  GridRaycastCb d;
+  memset(&d, 0, sizeof(d));
+  d.pbvh = g->pbvh;
+  d.start = start;
+  d.normal = normal;
+  d.depth = *depth;
+  d.active_vertex = d.active_grid = -1;
+  isect_ray_tri_watertight_v3_precalc(&d.isect, normal);
+  BKE_pbvh_raycast(g->pbvh, grid_raycast_cb, &d, start, normal, original != 0);
+  *depth = d.depth;
+  *active_vertex = d.active_vertex;
+  *active_grid = d.active_grid;
+  memcpy(face_normal, d.face_normal, sizeof(float[3]));
+  return d.hit ? 1 : 0;
+}

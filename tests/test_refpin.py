@@ -398,3 +398,37 @@ def test_raycast_matches_reference(oracle, name):
         a = o.raycast(s, d, original=k % 2)
         b = r.raycast(s, d, original=k % 2)
         assert _same_hit(a[:5], b), (k, a, b)
+
+
+@pytest.mark.parametrize("jitter", [0.0, 0.02])
+def test_grids_raycast_matches_reference(oracle, jitter):
+    """pbvh_grids_node_raycast through BKE_pbvh_raycast (pbvh.c:4110-4201):
+    grid quads, the second triangle tried only when the first is not taken.
+    The jittered torus has folded quads where both triangles meet the ray with
+    the second closer, the case in which that order decides the result."""
+    g = synth.torus_grids(16, 6, 4)
+    rng = np.random.default_rng(9)
+    if jitter:
+        g.co = (g.co + rng.normal(size=g.co.shape) * jitter).astype(np.float32)
+    o = oracle.OracleMesh.grids(g, 0)
+    o.recalc_all_normals()
+    r = pyrefpin.RefGrids(g, np.zeros_like(g.co))
+    for n in np.nonzero(o.nodes()["flag"] & LEAF)[0]:
+        r.node_mark_update(int(n))
+    r.update_normals()
+    r.update_bounds(UPD_BB)
+    hits = special = 0
+    for k in range(300):
+        s = rng.normal(size=3)
+        s = (2.5 * s / np.linalg.norm(s)).astype(np.float32)
+        t = rng.normal(size=3) * 0.6
+        d = ((t - s) / np.linalg.norm(t - s)).astype(np.float32)
+        length = np.float32(3.4028235e38) if k % 3 else np.float32(2.4)
+        a = o.raycast(s, d, length, original=k % 2)
+        b = r.raycast(s, d, length, original=k % 2)
+        assert _same_hit(a[:5], b), (k, a, b)
+        hits += a[0]
+        special += o.grids_special_quads(s, d) > 0
+    assert hits > 100
+    if jitter:
+        assert special > 20
