@@ -189,7 +189,8 @@ struct sgpu_mesh {
     for (void* p : {static_cast<void*>(ray_dev), static_cast<void*>(ray.count),
                     static_cast<void*>(ray.slot_leaf), static_cast<void*>(ray.slot_tmin),
                     static_cast<void*>(ray.slot_order), static_cast<void*>(ray.slot_key),
-                    static_cast<void*>(ray.items), static_cast<void*>(ray.nitems)})
+                    static_cast<void*>(ray.items), static_cast<void*>(ray.nitems),
+                    static_cast<void*>(ray.slot_special)})
       if (p) cudaFree(p);
     if (ray_host) cudaFreeHost(ray_host);
     ray = RayBatch{};
@@ -1744,8 +1745,9 @@ int ensure_ray_buffers(sgpu_mesh* m, int n) {
   if (m->ray_graph) cudaGraphExecDestroy(m->ray_graph);
   m->ray_graph = nullptr;
   m->ray_graph_n = m->ray_graph_orig = -1;
-  void* p[8] = {m->ray_dev, m->ray.count, m->ray.slot_leaf, m->ray.slot_tmin,
-                m->ray.slot_order, m->ray.slot_key, m->ray.items, m->ray.nitems};
+  void* p[9] = {m->ray_dev, m->ray.count, m->ray.slot_leaf, m->ray.slot_tmin,
+                m->ray.slot_order, m->ray.slot_key, m->ray.items, m->ray.nitems,
+                m->ray.slot_special};
   for (void* q : p)
     if (q) cudaFree(q);
   if (m->ray_host) cudaFreeHost(m->ray_host);
@@ -1761,6 +1763,7 @@ int ensure_ray_buffers(sgpu_mesh* m, int n) {
   CK(cudaMalloc(&m->ray.slot_tmin, sizeof(float) * slots), "cudaMalloc");
   CK(cudaMalloc(&m->ray.slot_order, sizeof(int) * slots), "cudaMalloc");
   CK(cudaMalloc(&m->ray.slot_key, sizeof(unsigned long long) * slots), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.slot_special, sizeof(int) * slots), "cudaMalloc");
   CK(cudaMalloc(&m->ray.items, sizeof(int2) * items), "cudaMalloc");
   CK(cudaMalloc(&m->ray.nitems, sizeof(int)), "cudaMalloc");
   m->ray.item_cap = static_cast<int>(items);
@@ -1777,7 +1780,6 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
                  int* r_active_vertices, int* r_active_faces, float* r_face_normals) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
-  if (mesh->host.type != kFaces) return fail(SGPU_ERR_UNSUPPORTED, "ray cast of PBVH_GRIDS");
   if (nrays < 0) return fail(SGPU_ERR_INVALID_ARG, "negative ray count");
   if (nrays == 0) return SGPU_OK;
   if (!ray_starts || !ray_normals || !r_depths || !r_hits)

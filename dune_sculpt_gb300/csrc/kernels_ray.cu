@@ -1,5 +1,6 @@
-// Ray cast of the PBVH (PBVH_FACES): BKE_pbvh_raycast (pbvh.c:3916-3929) with
-// the sculpt ray-cast callback, for a batch of independent rays.
+// Ray cast of the PBVH: BKE_pbvh_raycast (pbvh.c:3916-3929) with the sculpt
+// ray-cast callback, for a batch of independent rays, PBVH_FACES and
+// PBVH_GRIDS.
 //
 // The reference walks the leaves whose box the ray line meets in order of
 // their entry distance (a binary tree keyed on tmin, ties after earlier DFS
@@ -20,7 +21,14 @@
 //   k_ray_finish  one CTA per ray: the leaves in order with the callback's
 //                 rule, then the winning triangle's depth, active vertex
 //                 (corner nearest the hit, first among equals), face and
-//                 normal (normal_tri_v3).
+//                 normal (normal_tri_v3 / normal_quad_v3).
+// GRIDS (pbvh_grids_node_raycast, pbvh.c:4110-4201): the units are grid quads
+// (grid, row, column order) and ray_face_intersection_quad tries the second
+// triangle only when the first is not taken, so a quad whose two triangles
+// both meet the ray with the second closer does not reduce to a minimum.
+// k_ray_tris flags such a leaf; k_ray_finish replays a flagged leaf quad by
+// quad in order (256 quads at a time, their tests in parallel, the rule
+// sequentially), and every other leaf by its minimum key.
 #include <cuda_runtime.h>
 
 #include "sgpu_device.cuh"
@@ -136,6 +144,34 @@ __device__ __forceinline__ float len_sq(float3 a, float3 b) {
   return d0 * d0 + d1 * d1 + d2 * d2;
 }
 
+// Units per leaf: looptris (FACES) or grid quads (GRIDS).
+__device__ __forceinline__ int leaf_units(const DevMesh& m, int leaf) {
+  const int n = m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf];
+  return m.type == kFaces ? n : n * (m.grid_size - 1) * (m.grid_size - 1);
+}
+
+// Corners of grid quad `unit` of a leaf: (x, y), (x+1, y), (x+1, y+1),
+// (x, y+1) as pbvh_grids_node_raycast orders them.
+struct GridQuad {
+  int grid, x, y;
+  float3 c[4];
+};
+
+__device__ __forceinline__ GridQuad grid_quad(const DevMesh& m, int leaf, int unit) {
+  const int g1 = m.grid_size - 1, nq = g1 * g1, gs = m.grid_size;
+  GridQuad q;
+  q.grid = m.leaf_prims[m.leaf_prim_off[leaf] + unit / nq];
+  const int r = unit % nq;
+  q.y = r / g1;
+  q.x = r % g1;
+  const float4* base = m.co + static_cast<size_t>(q.grid) * m.grid_area;
+  q.c[0] = xyz(__ldcg(&base[q.y * gs + q.x]));
+  q.c[1] = xyz(__ldcg(&base[q.y * gs + q.x + 1]));
+  q.c[2] = xyz(__ldcg(&base[(q.y + 1) * gs + q.x + 1]));
+  q.c[3] = xyz(__ldcg(&base[(q.y + 1) * gs + q.x]));
+  return q;
+}
+
 // Block-wide exclusive scan of ints (kRayThreads threads).
 __device__ int ray_block_scan(int v, int* total, int* smem32) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -235,15 +271,13 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_leaves(DevMesh m, RayBatch 
     }
     order[rank] = i;
     key[i] = kNoKey;
+    rb.slot_special[static_cast<size_t>(ray) * L + i] = 0;
   }
   // work items: (ray-slot, chunk of kRayChunk prims)
   int nch = 0;
   const int s0 = min(total, static_cast<int>(threadIdx.x) * ((total + kRayThreads - 1) / kRayThreads));
   const int s1 = min(total, s0 + (total + kRayThreads - 1) / kRayThreads);
-  for (int s = s0; s < s1; s++) {
-    const int leaf = slot_leaf[s];
-    nch += (m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf] + kRayChunk - 1) / kRayChunk;
-  }
+  for (int s = s0; s < s1; s++) nch += (leaf_units(m, slot_leaf[s]) + kRayChunk - 1) / kRayChunk;
   int all;
   int off = ray_block_scan(nch, &all, scan);
   if (threadIdx.x == 0) scan[0] = atomicAdd(rb.nitems, all);
@@ -254,8 +288,7 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_leaves(DevMesh m, RayBatch 
     return;
   }
   for (int s = s0; s < s1; s++) {
-    const int leaf = slot_leaf[s];
-    const int c = (m.leaf_prim_off[leaf + 1] - m.leaf_prim_off[leaf] + kRayChunk - 1) / kRayChunk;
+    const int c = (leaf_units(m, slot_leaf[s]) + kRayChunk - 1) / kRayChunk;
     for (int k = 0; k < c; k++) rb.items[base + off + k] = make_int2(ray * L + s, k);
     off += c;
   }
@@ -275,17 +308,30 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb
       d[k] = rb.rays[6 * ray + 3 + k];
     }
     const int leaf = rb.slot_leaf[item.x];
-    const int p0 = m.leaf_prim_off[leaf], p1 = m.leaf_prim_off[leaf + 1];
     const int pos = item.y * kRayChunk + static_cast<int>(threadIdx.x);
     unsigned long long key = kNoKey;
-    if (p0 + pos < p1) {
-      const int4 tv = m.lt_v4[m.leaf_prims[p0 + pos]];
-      const float3 c0 = xyz(__ldcg(&m.co[tv.x])), c1 = xyz(__ldcg(&m.co[tv.y])),
-                   c2 = xyz(__ldcg(&m.co[tv.z]));
+    if (pos < leaf_units(m, leaf)) {
       RayTri rt;
       raytri_init(rt, d);
-      float depth;
-      if (raytri_hit(o, rt, c0, c1, c2, &depth)) key = depth_key(depth, pos);
+      if (m.type == kFaces) {
+        const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + pos]];
+        const float3 c0 = xyz(__ldcg(&m.co[tv.x])), c1 = xyz(__ldcg(&m.co[tv.y])),
+                     c2 = xyz(__ldcg(&m.co[tv.z]));
+        float depth;
+        if (raytri_hit(o, rt, c0, c1, c2, &depth)) key = depth_key(depth, pos);
+      } else {
+        const GridQuad q = grid_quad(m, leaf, pos);
+        float da = 0.0f, db = 0.0f;
+        const bool ha = raytri_hit(o, rt, q.c[0], q.c[1], q.c[2], &da);
+        const bool hb = raytri_hit(o, rt, q.c[0], q.c[2], q.c[3], &db);
+        if (ha && hb && db < da) {
+          rb.slot_special[item.x] = 1;  // the leaf is replayed in order
+        } else if (ha) {
+          key = depth_key(da, pos);
+        } else if (hb) {
+          key = depth_key(db, pos);
+        }
+      }
     }
 #pragma unroll
     for (int s = 16; s >= 1; s >>= 1) {
@@ -306,69 +352,184 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb
 // Dynamic shared memory: per listed leaf its order entry, tmin and key.
 __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch rb) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float s_da[kRayThreads], s_db[kRayThreads];
+  __shared__ unsigned char s_ha[kRayThreads], s_hb[kRayThreads];
+  __shared__ float s_depth, s_run_tmin;
+  __shared__ int s_slot, s_cast, s_special, s_win_slot, s_win_pos, s_win_tri, s_leaf_hit;
   const int ray = blockIdx.x;
   const int L = m.nleaf;
   const int cnt = rb.count[ray];
+  int cnt_replay = cnt;  // leaves walked by the whole CTA
   unsigned long long* s_key = reinterpret_cast<unsigned long long*>(smem);
   float* s_tmin = reinterpret_cast<float*>(s_key + L);
   int* s_order = reinterpret_cast<int*>(s_tmin + L);
   const size_t base = static_cast<size_t>(ray) * L;
+  if (threadIdx.x == 0) {
+    s_run_tmin = FLT_MAX;
+    s_depth = rb.depth_in ? rb.depth_in[ray] : FLT_MAX;
+    s_win_slot = s_win_pos = s_win_tri = -1;
+  }
+  int special = 0;
   for (int i = threadIdx.x; i < cnt; i += kRayThreads) {
     s_key[i] = __ldcg(&rb.slot_key[base + i]);
     s_tmin[i] = rb.slot_tmin[base + i];
     s_order[i] = rb.slot_order[base + i];
+    if (m.type == kGrids) special |= __ldcg(&rb.slot_special[base + i]);
+  }
+  float o[3], d[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    o[k] = rb.rays[6 * ray + k];
+    d[k] = rb.rays[6 * ray + 3 + k];
+  }
+  RayTri rt;
+  raytri_init(rt, d);
+  // traverse_tree with the callback: a leaf is cast when tmin < running
+  // minimum; a hit inside it is taken when strictly closer than the depth
+  if (!__syncthreads_or(special)) {
+    // every listed leaf reduces to its minimum key: one thread walks them
+    if (threadIdx.x == 0) {
+      float run_tmin = FLT_MAX, depth = s_depth;
+      int win_slot = -1, win_pos = -1;
+      for (int k = 0; k < cnt; k++) {
+        const int sl = s_order[k];
+        if (!(s_tmin[sl] < run_tmin)) continue;
+        const unsigned long long key = s_key[sl];
+        if (key == kNoKey) continue;
+        const float dmin = __uint_as_float(static_cast<unsigned int>(key >> 32));
+        if (dmin < depth) {
+          depth = dmin;
+          win_slot = sl;
+          win_pos = static_cast<int>(key & 0xffffffffu);
+          run_tmin = depth;
+        }
+      }
+      s_depth = depth;
+      s_win_slot = win_slot;
+      s_win_pos = win_pos;
+    }
+    cnt_replay = 0;
+  }
+  for (int k = 0; k < cnt_replay; k++) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int sl = s_order[k];
+      s_slot = sl;
+      s_cast = s_tmin[sl] < s_run_tmin;
+      s_special = m.type == kGrids && __ldcg(&rb.slot_special[base + sl]);
+      s_leaf_hit = 0;
+    }
+    __syncthreads();
+    if (!s_cast) continue;
+    const int sl = s_slot;
+    if (!s_special) {
+      // the leaf's closest hit: taken when strictly below the depth
+      if (threadIdx.x == 0) {
+        const unsigned long long key = s_key[sl];
+        if (key != kNoKey) {
+          const float dmin = __uint_as_float(static_cast<unsigned int>(key >> 32));
+          if (dmin < s_depth) {
+            s_depth = dmin;
+            s_win_slot = sl;
+            s_win_pos = static_cast<int>(key & 0xffffffffu);
+            s_win_tri = -1;  // decided below
+            s_run_tmin = dmin;
+          }
+        }
+      }
+      continue;
+    }
+    // GRIDS leaf with a folded quad: ray_face_intersection_quad quad by quad
+    const int leaf = rb.slot_leaf[base + sl];
+    const int units = leaf_units(m, leaf);
+    for (int c0 = 0; c0 < units; c0 += kRayThreads) {
+      const int u = c0 + static_cast<int>(threadIdx.x);
+      bool ha = false, hb = false;
+      float da = 0.0f, db = 0.0f;
+      if (u < units) {
+        const GridQuad q = grid_quad(m, leaf, u);
+        ha = raytri_hit(o, rt, q.c[0], q.c[1], q.c[2], &da);
+        hb = raytri_hit(o, rt, q.c[0], q.c[2], q.c[3], &db);
+      }
+      s_ha[threadIdx.x] = ha;
+      s_hb[threadIdx.x] = hb;
+      s_da[threadIdx.x] = da;
+      s_db[threadIdx.x] = db;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const int n = min(kRayThreads, units - c0);
+        float dep = s_depth;
+        for (int t = 0; t < n; t++) {
+          if (s_ha[t] && s_da[t] < dep) {
+            dep = s_da[t];
+            s_win_tri = 0;
+          } else if (s_hb[t] && s_db[t] < dep) {
+            dep = s_db[t];
+            s_win_tri = 1;
+          } else {
+            continue;
+          }
+          s_win_slot = sl;
+          s_win_pos = c0 + t;
+          s_leaf_hit = 1;
+        }
+        s_depth = dep;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0 && s_leaf_hit) s_run_tmin = s_depth;
   }
   __syncthreads();
   if (threadIdx.x != 0) return;
-  // traverse_tree with the callback: a leaf is cast when tmin < running
-  // minimum; its closest hit is taken when strictly closer than the depth
-  float run_tmin = FLT_MAX;
-  float depth = rb.depth_in ? rb.depth_in[ray] : FLT_MAX;
-  int win_slot = -1, win_pos = -1;
-  for (int k = 0; k < cnt; k++) {
-    const int s = s_order[k];
-    if (!(s_tmin[s] < run_tmin)) continue;
-    const unsigned long long key = s_key[s];
-    if (key == kNoKey) continue;
-    const float dmin = __uint_as_float(static_cast<unsigned int>(key >> 32));
-    if (dmin < depth) {
-      depth = dmin;
-      win_slot = s;
-      win_pos = static_cast<int>(key & 0xffffffffu);
-      run_tmin = depth;
-    }
-  }
+  float depth = s_depth;
+  const int win_slot = s_win_slot, win_pos = s_win_pos;
   float fn[3] = {0.0f, 0.0f, 0.0f};
   int av = -1, af = -1;
   if (win_slot >= 0) {
-    float o[3], d[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      o[k] = rb.rays[6 * ray + k];
-      d[k] = rb.rays[6 * ray + 3 + k];
-    }
     const int leaf = rb.slot_leaf[base + win_slot];
-    const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + win_pos]];
-    const float3 c[3] = {xyz(__ldcg(&m.co[tv.x])), xyz(__ldcg(&m.co[tv.y])),
-                         xyz(__ldcg(&m.co[tv.z]))};
-    RayTri rt;
-    raytri_init(rt, d);
-    float dt = depth;
-    raytri_hit(o, rt, c[0], c[1], c[2], &dt);  // the exact value (-0 kept)
-    depth = dt;
-    const float3 n = normal_tri(c[0], c[1], c[2]);
-    fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
-    const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
-    const int ids[3] = {tv.x, tv.y, tv.z};
-    float3 nearest = c[0];
-    int best = 0;
-    for (int j = 1; j < 3; j++)
-      if (len_sq(loc, c[j]) < len_sq(loc, nearest)) {
-        nearest = c[j];
-        best = j;
-      }
-    av = rb.n2o ? rb.n2o[ids[best]] : ids[best];
-    af = tv.w;
+    if (m.type == kFaces) {
+      const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + win_pos]];
+      const float3 c[3] = {xyz(__ldcg(&m.co[tv.x])), xyz(__ldcg(&m.co[tv.y])),
+                           xyz(__ldcg(&m.co[tv.z]))};
+      float dt = depth;
+      raytri_hit(o, rt, c[0], c[1], c[2], &dt);  // the exact value (-0 kept)
+      depth = dt;
+      const float3 n = normal_tri(c[0], c[1], c[2]);
+      fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
+      const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
+      const int ids[3] = {tv.x, tv.y, tv.z};
+      float3 nearest = c[0];
+      int best = 0;
+      for (int j = 1; j < 3; j++)
+        if (len_sq(loc, c[j]) < len_sq(loc, nearest)) {
+          nearest = c[j];
+          best = j;
+        }
+      av = rb.n2o ? rb.n2o[ids[best]] : ids[best];
+      af = tv.w;
+    } else {
+      const GridQuad q = grid_quad(m, leaf, win_pos);
+      float da = depth, db = depth;
+      const bool ha = raytri_hit(o, rt, q.c[0], q.c[1], q.c[2], &da);
+      raytri_hit(o, rt, q.c[0], q.c[2], q.c[3], &db);
+      // the taken triangle: from the in-order replay, or for a minimum-key
+      // leaf the first triangle when it meets the ray
+      const int tri = s_win_tri >= 0 ? s_win_tri : (ha ? 0 : 1);
+      depth = tri == 0 ? da : db;
+      const float3 n = normal_quad(q.c[0], q.c[1], q.c[2], q.c[3]);
+      fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
+      const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
+      const int x_it[4] = {0, 1, 1, 0}, y_it[4] = {0, 0, 1, 1};
+      float3 nearest = q.c[0];
+      int best = 0;
+      for (int j = 1; j < 4; j++)
+        if (len_sq(loc, q.c[j]) < len_sq(loc, nearest)) {
+          nearest = q.c[j];
+          best = j;
+        }
+      av = m.grid_area * q.grid + (q.y + y_it[best]) * m.grid_size + (q.x + x_it[best]);
+      af = q.grid;
+    }
   }
   rb.depth_out[ray] = depth;
   rb.hit[ray] = win_slot >= 0;
@@ -389,7 +550,10 @@ size_t ray_finish_smem(const DevMesh& m) {
   return (sizeof(unsigned long long) + sizeof(float) + sizeof(int)) * static_cast<size_t>(m.nleaf) + 16;
 }
 int ray_items_per_ray(const DevMesh& m) {
-  return m.totlt / kRayChunk + m.nleaf;
+  if (m.type == kFaces) return m.totlt / kRayChunk + m.nleaf;
+  const long long g1 = m.grid_size - 1;
+  const long long units = static_cast<long long>(m.totvert / m.grid_area) * g1 * g1;
+  return static_cast<int>(units / kRayChunk) + m.nleaf;
 }
 
 cudaError_t configure_ray_kernels(size_t leaves_smem, size_t finish_smem) {

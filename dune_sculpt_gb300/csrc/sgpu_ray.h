@@ -18,6 +18,7 @@ struct RayBatch {
   float* slot_tmin;
   int* slot_order;
   unsigned long long* slot_key;
+  int* slot_special;  // GRIDS: the leaf has a quad whose second triangle is the closer hit
   // work items (ray * nleaf + slot, chunk) and their count
   int2* items;
   int* nitems;

@@ -236,12 +236,14 @@ int sgpu_stroke_team_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGP
                              int ndabs, const int *dab_tools, SGPU_TeamProfile *out,
                              SGPU_StrokeStats *stats);
 
-/* ---- ray cast (PBVH_FACES) ----
+/* ---- ray cast ----
  * Replaces BKE_pbvh_raycast (pbvh.c:3916) driven by the sculpt ray-cast
  * callback, which the reference calls but does not ship (sculpt.c is absent):
  * leaves in order of their box entry distance (BKE_pbvh_search_callback_occluded,
  * pbvh.c:2853), a leaf cast while its entry distance is below the running
- * minimum, pbvh_faces_node_raycast (pbvh.c:4042) inside it.  nrays independent
+ * minimum, pbvh_faces_node_raycast (pbvh.c:4042) or pbvh_grids_node_raycast
+ * (pbvh.c:4110) inside it.  GRIDS: the active vertex is the grid element index
+ * and the active face the grid index.  nrays independent
  * rays; ray_starts / ray_normals 3 floats each (unit directions);
  * ray_lengths (nullable: FLT_MAX) the initial depth; original selects
  * orig_vb.  Results per ray: depth (initial depth when no hit), hit 0/1,

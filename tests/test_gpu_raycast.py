@@ -94,3 +94,54 @@ def test_raycast_edge_cases(gpu, oracle):
     # zero rays is a no-op
     hit, dep, _, _, _ = gp.raycast(np.zeros((0, 3)), np.zeros((0, 3)))
     assert hit.shape == (0,)
+
+
+def _torus_rays(seed, n):
+    rng = np.random.default_rng(seed)
+    starts, dirs = [], []
+    for _ in range(n):
+        s = rng.normal(size=3)
+        s = 2.5 * s / np.linalg.norm(s)
+        t = rng.normal(size=3) * 0.6
+        starts.append(s)
+        dirs.append((t - s) / np.linalg.norm(t - s))
+    return np.asarray(starts, np.float32), np.asarray(dirs, np.float32)
+
+
+@pytest.mark.parametrize("level,leaf_limit,jitter", [(4, 0, 0.0), (4, 0, 0.02), (5, 4, 0.01),
+                                                     (3, 1, 0.03)])
+def test_grids_raycast_matches_oracle(gpu, oracle, level, leaf_limit, jitter):
+    """PBVH_GRIDS (pbvh_grids_node_raycast, pbvh.c:4110-4201): the jittered
+    tori hold folded quads whose second triangle is the closer hit, which the
+    GPU replays in order; the active vertex is the grid element, the face the
+    grid."""
+    g = synth.torus_grids(16, 6, level=level)
+    if jitter:
+        rng = np.random.default_rng(9)
+        g.co = (g.co + rng.normal(size=g.co.shape) * jitter).astype(np.float32)
+    gp = PBVH.build_grids(g, leaf_limit)
+    o = oracle.OracleMesh.grids(g, leaf_limit)
+    o.recalc_all_normals()
+    starts, dirs = _torus_rays(5, 300)
+    lengths = np.where(np.arange(300) % 3 == 0, np.float32(2.4), FLT_MAX).astype(np.float32)
+    assert compare(gp, o, starts, dirs, None, 0) > 100
+    compare(gp, o, starts, dirs, lengths, 1)
+    if jitter:
+        special = sum(o.grids_special_quads(starts[r], dirs[r]) > 0 for r in range(300))
+        assert special > 20
+    compare(gp, o, starts[:3], dirs[:3], None, 0)
+
+
+def test_grids_raycast_after_stroke(gpu, oracle):
+    g = synth.torus_grids(16, 6, level=4)
+    st = synth.Stroke(synth.TOOL_DRAW, 0.15, 0.9, synth.CURVE_SMOOTH, synth.SYMM_X,
+                      synth.torus_dabs(31, 16, 0.15))
+    gp = PBVH.build_grids(g, 4)
+    gp.stroke(st, mode=STROKE_TEAM)
+    o = oracle.OracleMesh.grids(g, 4)
+    o.recalc_all_normals()
+    o.stroke(st, which=1)
+    assert bits_equal(gp.positions(), o.co())
+    starts, dirs = _torus_rays(13, 200)
+    assert compare(gp, o, starts, dirs, None, 0) > 80
+    compare(gp, o, starts, dirs, None, 1)
