@@ -70,8 +70,11 @@ def parse_args():
                     help="three persistent strokes of the workload, no report (for ncu)")
     ap.add_argument("--cluster", type=int, default=16, help="cluster size for --quick")
     ap.add_argument("--raycast-only", action="store_true",
-                    help="three 1024-ray sgpu_raycast batches on the workload mesh and exit "
-                         "(the command profiled with ncu for the ray kernels)")
+                    help="1024-ray sgpu_raycast batches on the workload mesh and on the "
+                         "multires torus, one JSON line, and exit (the command profiled "
+                         "with ncu for the ray kernels)")
+    ap.add_argument("--raycast-mesh", choices=["faces", "grids", "both"], default="both",
+                    help="meshes of --raycast-only")
     ap.add_argument("--phases", action="store_true",
                     help="per-phase profile of the persistent stroke on all five workloads "
                          "(one JSON line each), no report")
@@ -433,6 +436,44 @@ def run_gpu(args):
     return 0
 
 
+def time_raycast(g, starts, dirs, reps=20, one=200):
+    """Wall-clock seconds per batch call and per one-ray call of
+    sgpu_raycast (host arrays), and the batch's hit count."""
+    n = starts.shape[0]
+    g.raycast(starts, dirs)  # batch buffers allocated outside the timing
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        hit, _, _, _, _ = g.raycast(starts, dirs)
+    batch_s = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for k in range(one):
+        g.raycast(starts[k % n:k % n + 1], dirs[k % n:k % n + 1])
+    single_s = (time.perf_counter() - t0) / one
+    return batch_s, single_s, int(hit.sum())
+
+
+def run_raycast_grids(synth, PBVH):
+    """Multires ray cast on the 50,000-grid torus (17x17 elements per grid):
+    1024 seeded rays from radius 3 aimed at seeded grid elements."""
+    g5, _ = synth.cfg5_multires()
+    gp = PBVH.build_grids(g5)
+    rng = np.random.default_rng(0x5EED0000 + 8)
+    n = 1024
+    s = rng.normal(size=(n, 3))
+    starts = (3.0 * s / np.linalg.norm(s, axis=1, keepdims=True)).astype(np.float32)
+    tgt = g5.co[rng.integers(0, g5.co.shape[0], size=n)].astype(np.float64)
+    d = tgt - starts
+    dirs = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    best = None
+    for _ in range(3):
+        r = time_raycast(gp, starts, dirs)
+        best = r if best is None or r[0] < best[0] else best
+    batch_s, single_s, nhit = best
+    return {"workload": "1024 rays from radius 3 at seeded grid elements, multires torus "
+            "50,000 grids of 17x17", "hits": nhit, "rays_per_s": n / batch_s,
+            "ms_per_1024_rays": 1e3 * batch_s, "single_ray_us": 1e6 * single_s}
+
+
 def run_raycast_leg(g, m, leaf_limit, no_cpu):
     """Ray cast (BKE_pbvh_raycast with the sculpt callback) on the workload's
     mesh: 1024 seeded rays from a sphere of radius 3 towards points near the
@@ -446,19 +487,9 @@ def run_raycast_leg(g, m, leaf_limit, no_cpu):
     tgt = rng.normal(size=(n, 3)) * 0.3
     d = tgt - starts
     dirs = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
-    g.raycast(starts, dirs)  # batch buffers allocated outside the timing
-    reps = 20
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        hit, _, _, _, _ = g.raycast(starts, dirs)
-    batch_s = (time.perf_counter() - t0) / reps
-    one = 200
-    t0 = time.perf_counter()
-    for k in range(one):
-        g.raycast(starts[k % n:k % n + 1], dirs[k % n:k % n + 1])
-    single_s = (time.perf_counter() - t0) / one
+    batch_s, single_s, nhit = time_raycast(g, starts, dirs)
     out = {"workload": "1024 rays from radius 3 towards the centre (+/-0.3), icosphere level 8",
-           "hits": int(hit.sum()), "rays_per_s": n / batch_s, "ms_per_1024_rays": 1e3 * batch_s,
+           "hits": nhit, "rays_per_s": n / batch_s, "ms_per_1024_rays": 1e3 * batch_s,
            "single_ray_us": 1e6 * single_s, "timing": "wall clock around sgpu_raycast "
            "(host arrays in and out)"}
     if not no_cpu:
@@ -533,13 +564,19 @@ def main():
         from dune_sculpt_gb300 import build as libbuild
 
         libbuild.build()
+        from dune_sculpt_gb300 import synth
         from dune_sculpt_gb300.sculpt import PBVH
 
-        m, _, leaf_limit, _ = workload()
-        g = PBVH.build_mesh(m, leaf_limit)
-        for _ in range(3):
-            r = run_raycast_leg(g, m, leaf_limit, True)
-        print(f"raycast: {r['hits']} hits, {r['ms_per_1024_rays']:.3f} ms per 1024 rays")
+        out = {}
+        if args.raycast_mesh in ("faces", "both"):
+            m, _, leaf_limit, _ = workload()
+            g = PBVH.build_mesh(m, leaf_limit)
+            for _ in range(3):
+                out["raycast_faces"] = run_raycast_leg(g, m, leaf_limit, True)
+            g.free()
+        if args.raycast_mesh in ("grids", "both"):
+            out["raycast_grids"] = run_raycast_grids(synth, PBVH)
+        print(json.dumps(out))
         return 0
     return run_gpu(args)
 

@@ -354,6 +354,7 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float s_da[kRayThreads], s_db[kRayThreads];
   __shared__ unsigned char s_ha[kRayThreads], s_hb[kRayThreads];
+  __shared__ unsigned s_mask[kRayThreads / 32];
   __shared__ float s_depth, s_run_tmin;
   __shared__ int s_slot, s_cast, s_special, s_win_slot, s_win_pos, s_win_tri, s_leaf_hit;
   const int ray = blockIdx.x;
@@ -455,23 +456,28 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
       s_hb[threadIdx.x] = hb;
       s_da[threadIdx.x] = da;
       s_db[threadIdx.x] = db;
+      // quads meeting the ray, one bit per thread; the rule visits only those
+      const unsigned bal = __ballot_sync(0xffffffffu, ha || hb);
+      if ((threadIdx.x & 31) == 0) s_mask[threadIdx.x >> 5] = bal;
       __syncthreads();
       if (threadIdx.x == 0) {
-        const int n = min(kRayThreads, units - c0);
         float dep = s_depth;
-        for (int t = 0; t < n; t++) {
-          if (s_ha[t] && s_da[t] < dep) {
-            dep = s_da[t];
-            s_win_tri = 0;
-          } else if (s_hb[t] && s_db[t] < dep) {
-            dep = s_db[t];
-            s_win_tri = 1;
-          } else {
-            continue;
+        for (int w = 0; w < kRayThreads / 32; w++) {
+          for (unsigned b = s_mask[w]; b; b &= b - 1) {
+            const int t = 32 * w + __ffs(static_cast<int>(b)) - 1;
+            if (s_ha[t] && s_da[t] < dep) {
+              dep = s_da[t];
+              s_win_tri = 0;
+            } else if (s_hb[t] && s_db[t] < dep) {
+              dep = s_db[t];
+              s_win_tri = 1;
+            } else {
+              continue;
+            }
+            s_win_slot = sl;
+            s_win_pos = c0 + t;
+            s_leaf_hit = 1;
           }
-          s_win_slot = sl;
-          s_win_pos = c0 + t;
-          s_leaf_hit = 1;
         }
         s_depth = dep;
       }
@@ -497,7 +503,6 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
       const float3 n = normal_tri(c[0], c[1], c[2]);
       fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
       const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
-      const int ids[3] = {tv.x, tv.y, tv.z};
       float3 nearest = c[0];
       int best = 0;
       for (int j = 1; j < 3; j++)
@@ -505,7 +510,8 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
           nearest = c[j];
           best = j;
         }
-      av = rb.n2o ? rb.n2o[ids[best]] : ids[best];
+      const int id = best == 0 ? tv.x : (best == 1 ? tv.y : tv.z);
+      av = rb.n2o ? rb.n2o[id] : id;
       af = tv.w;
     } else {
       const GridQuad q = grid_quad(m, leaf, win_pos);
@@ -519,7 +525,6 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
       const float3 n = normal_quad(q.c[0], q.c[1], q.c[2], q.c[3]);
       fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
       const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
-      const int x_it[4] = {0, 1, 1, 0}, y_it[4] = {0, 0, 1, 1};
       float3 nearest = q.c[0];
       int best = 0;
       for (int j = 1; j < 4; j++)
@@ -527,7 +532,9 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
           nearest = q.c[j];
           best = j;
         }
-      av = m.grid_area * q.grid + (q.y + y_it[best]) * m.grid_size + (q.x + x_it[best]);
+      // corner j of the quad is (x + {0,1,1,0}[j], y + {0,0,1,1}[j])
+      const int xi = best == 1 || best == 2, yi = best >= 2;
+      av = m.grid_area * q.grid + (q.y + yi) * m.grid_size + (q.x + xi);
       af = q.grid;
     }
   }
