@@ -12,6 +12,7 @@
 
 #include "../../include/sculpt_gpu.h"
 #include "sgpu_device.cuh"
+#include "sgpu_draw.h"
 #include "sgpu_host.h"
 #include "sgpu_kernels.h"
 #include "sgpu_ray.h"
@@ -115,6 +116,20 @@ struct sgpu_mesh {
   // the captured call (copies in, kernels, copies out) for (rays, original)
   cudaGraphExec_t ray_graph = nullptr;
   int ray_graph_n = -1, ray_graph_orig = -1;
+  // headless draw buffers (sgpu_draw_buffers_build): host layout, device view
+  // and its allocations
+  DrawLayout draw;
+  DrawDev draw_dev{};
+  std::vector<void*> draw_allocs;
+  bool draw_built = false;
+
+  void free_draw() {
+    for (void* p : draw_allocs) cudaFree(p);
+    draw_allocs.clear();
+    draw_dev = DrawDev{};
+    draw = DrawLayout{};
+    draw_built = false;
+  }
 
   cudaEvent_t prof_event() {
     if (ev_used == ev_pool.size()) {
@@ -193,6 +208,7 @@ struct sgpu_mesh {
                     static_cast<void*>(ray.slot_special)})
       if (p) cudaFree(p);
     if (ray_host) cudaFreeHost(ray_host);
+    free_draw();
     ray = RayBatch{};
     ray_dev = ray_host = nullptr;
     ray_cap = 0;
@@ -593,6 +609,7 @@ int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPol
   h.loop_v.resize(totloop);
   for (int l = 0; l < totloop; l++) h.loop_v[l] = static_cast<int>(loops[l].v);
   h.lt_v.resize(3 * static_cast<size_t>(totlooptri));
+  h.lt_loop.resize(3 * static_cast<size_t>(totlooptri));
   h.lt_poly.resize(totlooptri);
   for (int t = 0; t < totlooptri; t++) {
     for (int j = 0; j < 3; j++) {
@@ -602,6 +619,7 @@ int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPol
         return fail(SGPU_ERR_INVALID_ARG, "looptri %d loop index out of range", t);
       }
       h.lt_v[3 * t + j] = h.loop_v[l];
+      h.lt_loop[3 * t + j] = static_cast<int>(l);
     }
     h.lt_poly[t] = static_cast<int>(looptris[t].poly);
   }
@@ -1861,6 +1879,153 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
     if (r_face_normals)
       for (int k = 0; k < 3; k++) r_face_normals[3 * r + k] = fo[nrays + 3 * static_cast<size_t>(r) + k];
   }
+  return SGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// One device array for the draw buffers, copied from src (count elements) or
+// zeroed when src is null.
+template <class T>
+int draw_array(sgpu_mesh* m, T** out, const T* src, size_t count) {
+  void* p = nullptr;
+  const size_t bytes = (count > 0 ? count : 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (draw buffers)");
+  m->draw_allocs.push_back(p);
+  if (src && count > 0)
+    e = cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, m->stream);
+  else
+    e = cudaMemsetAsync(p, 0, bytes, m->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "draw buffer upload");
+  *out = static_cast<T*>(p);
+  return SGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgpu_draw_buffers_build(sgpu_mesh* mesh, const SGPU_DrawSetup* setup) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  HostMesh& h = mesh->host;
+  DevMesh& d = mesh->dev;
+  DrawInputs in;
+  if (setup) {
+    in.face_sets = setup->face_sets;
+    in.seed = setup->face_sets_color_seed;
+    in.color_default = setup->face_sets_color_default;
+    in.loop_colors = h.type == kFaces ? setup->loop_colors : nullptr;
+    in.vert_colors = h.type == kFaces ? setup->vert_colors : nullptr;
+    in.use_vert_colors = setup->use_sculpt_vertex_colors != 0;
+    in.grid_flag_mats = reinterpret_cast<const unsigned char*>(setup->grid_flag_mats);
+  }
+  if (h.type == kFaces) {
+    // the current MVert flags (ME_HIDE) ride in the w word of the device positions
+    std::vector<float4> co4(h.totvert);
+    CK(cudaMemcpyAsync(co4.data(), d.co, sizeof(float4) * co4.size(), cudaMemcpyDeviceToHost,
+                       mesh->stream),
+       "read vertex flags");
+    CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+    in.vert_flag.resize(h.totvert);
+    for (int v = 0; v < h.totvert; v++) {
+      unsigned char b[4];
+      std::memcpy(b, &co4[mesh->o2n[v]].w, 4);
+      in.vert_flag[v] = b[0];
+    }
+  }
+  mesh->free_draw();
+  std::string err;
+  if (!build_draw_layout(h, in, &mesh->draw, &err)) return fail(SGPU_ERR_INVALID_ARG, "%s", err.c_str());
+  const DrawLayout& L = mesh->draw;
+  DrawDev& dd = mesh->draw_dev;
+  const size_t words = static_cast<size_t>(L.total_verts) * kDrawWords;
+  if ((rc = draw_array<unsigned int>(mesh, &dd.vbo, nullptr, words))) return rc;
+  long long* lvo = nullptr;
+  int *lts = nullptr, *ltc = nullptr, *lsm = nullptr, *tris = nullptr;
+  unsigned int *fset = nullptr, *col = nullptr;
+  if ((rc = draw_array(mesh, &lvo, L.leaf_vert_off.data(), L.leaf_vert_off.size())) ||
+      (rc = draw_array(mesh, &lts, L.leaf_tri_start.data(), L.leaf_tri_start.size())) ||
+      (rc = draw_array(mesh, &ltc, L.leaf_tri_count.data(), L.leaf_tri_count.size())) ||
+      (rc = draw_array(mesh, &lsm, L.leaf_smooth.data(), L.leaf_smooth.size())) ||
+      (rc = draw_array(mesh, &tris, L.tris.data(), L.tris.size())) ||
+      (rc = draw_array<int>(mesh, &dd.overlay, nullptr, static_cast<size_t>(d.nleaf))))
+    return rc;
+  if (L.has_fset && (rc = draw_array(mesh, &fset, L.fset.data(), L.fset.size()))) return rc;
+  if (L.show_vcol && (rc = draw_array(mesh, &col, L.col.data(), L.col.size()))) return rc;
+  dd.leaf_vert_off = lvo;
+  dd.leaf_tri_start = lts;
+  dd.leaf_tri_count = ltc;
+  dd.leaf_smooth = lsm;
+  dd.tris = tris;
+  dd.fset = fset;
+  dd.col = col;
+  // every leaf rebuilt and refilled at the next update (BKE_pbvh_node_mark_rebuild_draw)
+  CK(launch_mark_all(d, kRebuildDrawBuffers | kUpdateDrawBuffers, mesh->stream), "mark kernel");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  mesh->draw_built = true;
+  return SGPU_OK;
+}
+
+int sgpu_draw_buffers_update(sgpu_mesh* mesh) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->draw_built) return fail(SGPU_ERR_INVALID_ARG, "draw buffers not built");
+  CK(launch_draw_fill(mesh->dev, mesh->draw_dev, mesh->stream), "draw fill kernel");
+  return SGPU_OK;
+}
+
+int sgpu_draw_buffers_layout(sgpu_mesh* mesh, int64_t* vert_off, int* tot_tri, int* smooth,
+                             int* material_index) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->draw_built) return fail(SGPU_ERR_INVALID_ARG, "draw buffers not built");
+  const DrawLayout& L = mesh->draw;
+  const size_t n = L.node_tot_tri.size();
+  if (vert_off) std::memcpy(vert_off, L.node_vert_off.data(), sizeof(int64_t) * (n + 1));
+  if (tot_tri) std::memcpy(tot_tri, L.node_tot_tri.data(), sizeof(int) * n);
+  if (smooth) std::memcpy(smooth, L.node_smooth.data(), sizeof(int) * n);
+  if (material_index) std::memcpy(material_index, L.node_material.data(), sizeof(int) * n);
+  return SGPU_OK;
+}
+
+int sgpu_draw_buffers_overlay(sgpu_mesh* mesh, int* show_overlay) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->draw_built) return fail(SGPU_ERR_INVALID_ARG, "draw buffers not built");
+  if (!show_overlay) return fail(SGPU_ERR_INVALID_ARG, "NULL output");
+  std::vector<int> ov(mesh->dev.nleaf);
+  CK(cudaMemcpyAsync(ov.data(), mesh->draw_dev.overlay, sizeof(int) * ov.size(),
+                     cudaMemcpyDeviceToHost, mesh->stream),
+     "read overlay flags");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  const HostMesh& h = mesh->host;
+  for (int n = 0; n < h.totnode; n++) show_overlay[n] = h.node_leaf[n] >= 0 ? ov[h.node_leaf[n]] : 0;
+  return SGPU_OK;
+}
+
+int sgpu_draw_buffers_get(sgpu_mesh* mesh, void* dst, size_t bytes) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->draw_built) return fail(SGPU_ERR_INVALID_ARG, "draw buffers not built");
+  const size_t need = static_cast<size_t>(mesh->draw.total_verts) * SGPU_DRAW_STRIDE;
+  if (!dst || bytes < need) return fail(SGPU_ERR_INVALID_ARG, "destination smaller than %zu bytes", need);
+  if (need > 0)
+    CK(cudaMemcpyAsync(dst, mesh->draw_dev.vbo, need, cudaMemcpyDeviceToHost, mesh->stream),
+       "read draw buffers");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
+
+int sgpu_draw_buffers_device(sgpu_mesh* mesh, void** d_vbo, size_t* bytes) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->draw_built) return fail(SGPU_ERR_INVALID_ARG, "draw buffers not built");
+  if (d_vbo) *d_vbo = mesh->draw_dev.vbo;
+  if (bytes) *bytes = static_cast<size_t>(mesh->draw.total_verts) * SGPU_DRAW_STRIDE;
   return SGPU_OK;
 }
 

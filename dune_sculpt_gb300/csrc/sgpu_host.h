@@ -49,6 +49,7 @@ struct HostMesh {
   std::vector<int> loop_v;
   std::vector<int> lt_v;     // 3 per looptri (vertex indices)
   std::vector<int> lt_poly;  // per looptri
+  std::vector<int> lt_loop;  // 3 per looptri (loop indices)
   std::vector<int> vt_off, vt_idx;  // vertex -> looptri (ascending)
   std::vector<int> nb_off, nb_idx;  // vertex -> one-ring
   // GRIDS topology

@@ -5,6 +5,8 @@
 
 #include "sgpu_device.cuh"
 
+#include "sgpu_draw.h"
+
 namespace sgpu {
 
 cudaError_t launch_cull(const DevMesh& m, const PassParams& pp, cudaStream_t s);
@@ -31,6 +33,8 @@ cudaError_t launch_grid_seams(const DevMesh& m, cudaStream_t s);
 cudaError_t launch_l2_flush(void* buf, size_t bytes, cudaStream_t s);
 cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s);
 cudaError_t launch_mark_all(const DevMesh& m, int bits, cudaStream_t s);
+// Headless draw buffers: fill every leaf flagged PBVH_UpdateDrawBuffers.
+cudaError_t launch_draw_fill(const DevMesh& m, const DrawDev& dd, cudaStream_t s);
 // Refit-chunk boxes of every leaf from the current positions.
 cudaError_t launch_chunk_boxes_all(const DevMesh& m, int nchunks, cudaStream_t s);
 // out[i] = in[idx[i]]: float4 or float.

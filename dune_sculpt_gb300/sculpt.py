@@ -84,8 +84,25 @@ EXPORTS = (
     "sgpu_stroke_host", "sgpu_mesh_snapshot", "sgpu_mesh_restore", "sgpu_stroke_profile",
     "sgpu_mesh_flush_l2", "sgpu_host_alloc", "sgpu_host_free", "sgpu_mesh_set_team",
     "sgpu_mesh_get_team", "sgpu_autotune_team", "sgpu_batch_stroke", "sgpu_stroke_team_profile",
-    "sgpu_raycast",
+    "sgpu_raycast", "sgpu_draw_buffers_build", "sgpu_draw_buffers_update",
+    "sgpu_draw_buffers_layout", "sgpu_draw_buffers_overlay", "sgpu_draw_buffers_get",
+    "sgpu_draw_buffers_device",
 )
+
+DRAW_STRIDE = 36  # SGPU_DRAW_STRIDE
+# numpy view of one vertex of the draw buffer (VertexFormat_pack of pos, nor,
+# msk, ac, fset; the padding bytes named _pad*)
+DRAW_VERTEX_DT = np.dtype({"names": ["pos", "nor", "msk", "ac", "fset"],
+                           "formats": [("<f4", (3,)), ("<i2", (3,)), "u1", ("<u2", (4,)),
+                                       ("u1", (3,))],
+                           "offsets": [0, 16, 22, 24, 32], "itemsize": DRAW_STRIDE})
+
+
+class SGPU_DrawSetup(C.Structure):
+    _fields_ = [("face_sets", C.c_void_p), ("face_sets_color_seed", C.c_int),
+                ("face_sets_color_default", C.c_int), ("loop_colors", C.c_void_p),
+                ("vert_colors", C.c_void_p), ("use_sculpt_vertex_colors", C.c_int),
+                ("grid_flag_mats", C.c_void_p)]
 
 _lib = None
 
@@ -144,6 +161,12 @@ def load(path: str | None = None):
     L.sgpu_mesh_get_team.argtypes = [vp, vp]
     L.sgpu_autotune_team.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp]
     L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
+    L.sgpu_draw_buffers_build.argtypes = [vp, C.POINTER(SGPU_DrawSetup)]
+    L.sgpu_draw_buffers_update.argtypes = [vp]
+    L.sgpu_draw_buffers_layout.argtypes = [vp, vp, vp, vp, vp]
+    L.sgpu_draw_buffers_overlay.argtypes = [vp, vp]
+    L.sgpu_draw_buffers_get.argtypes = [vp, vp, C.c_size_t]
+    L.sgpu_draw_buffers_device.argtypes = [vp, vp, vp]
     _lib = L
     return L
 
@@ -324,6 +347,55 @@ class PBVH:
         _check(load().sgpu_raycast(self._h, n, _p(o), _p(d), _p(ln), original, _p(dep), _p(hit),
                                    _p(av), _p(af), _p(fn)))
         return hit.astype(bool), dep, av, af, fn
+
+    # -- headless draw buffers (GPU_pbvh_*_buffers_build / _update)
+    def draw_buffers_build(self, face_sets=None, seed: int = 0, color_default: int = 1,
+                           loop_colors=None, vert_colors=None, use_vert_colors: bool = False,
+                           grid_flag_mats=None):
+        """grid_flag_mats: (num_grids, 2) ints (mat_nr, flag) or None."""
+        keep = []
+
+        def arr(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data_as(C.c_void_p)
+
+        fm = None
+        if grid_flag_mats is not None:
+            g = np.asarray(grid_flag_mats)
+            fm = np.zeros(g.shape[0], dtype=np.dtype([("mat_nr", "<i2"), ("flag", "i1"),
+                                                      ("_pad", "i1")]))
+            fm["mat_nr"] = g[:, 0]
+            fm["flag"] = g[:, 1]
+        s = SGPU_DrawSetup(arr(face_sets, np.int32), seed, color_default,
+                           arr(loop_colors, np.uint8), arr(vert_colors, np.float32),
+                           int(bool(use_vert_colors)), arr(fm, fm.dtype) if fm is not None else None)
+        _check(load().sgpu_draw_buffers_build(self._h, C.byref(s)))
+
+    def draw_buffers_update(self):
+        _check(load().sgpu_draw_buffers_update(self._h))
+
+    def draw_buffers_layout(self) -> dict:
+        n = self.num_nodes
+        out = {"vert_off": np.zeros(n + 1, dtype=np.int64), "tot_tri": np.zeros(n, np.int32),
+               "smooth": np.zeros(n, np.int32), "material_index": np.zeros(n, np.int32)}
+        _check(load().sgpu_draw_buffers_layout(self._h, _p(out["vert_off"]), _p(out["tot_tri"]),
+                                               _p(out["smooth"]), _p(out["material_index"])))
+        return out
+
+    def draw_buffers_overlay(self) -> np.ndarray:
+        out = np.zeros(self.num_nodes, dtype=np.int32)
+        _check(load().sgpu_draw_buffers_overlay(self._h, _p(out)))
+        return out
+
+    def draw_buffers_get(self) -> np.ndarray:
+        """The whole vertex buffer as bytes (vert_off[-1] * 36)."""
+        n = int(self.draw_buffers_layout()["vert_off"][-1])
+        out = np.zeros(max(n, 1) * DRAW_STRIDE, dtype=np.uint8)
+        _check(load().sgpu_draw_buffers_get(self._h, _p(out), out.nbytes))
+        return out[:n * DRAW_STRIDE]
 
     def search_sphere_device(self, center, radius_sq: float, original: int = 0):
         c = np.asarray(center, dtype=np.float32)

@@ -257,6 +257,70 @@ int sgpu_raycast(sgpu_mesh *mesh, int nrays, const float *ray_starts, const floa
                  const float *ray_lengths, int original, float *r_depths, int *r_hits,
                  int *r_active_vertices, int *r_active_faces, float *r_face_normals);
 
+/* ---- headless draw buffers ----
+ * Replaces the PBVH draw-buffer path without GL: pbvh_update_draw_buffers
+ * (pbvh.c:3240-3290) reached from BKE_pbvh_draw_cb (pbvh.c:4615) with every
+ * node that needs an update, and inside it GPU_pbvh_mesh_buffers_build /
+ * _update (gpu_buffers.c:174-305, 307-400) and GPU_pbvh_grid_buffers_update
+ * (gpu_buffers.c:548-725) with the update flags pbvh.c always passes (mask,
+ * vertex colours, face sets).  The vertex buffer is one device array holding
+ * every leaf's buffer in node order, in the reference's interleaved vertex
+ * format ("pos" f32x3, "nor" i16x3, "msk" u8, "ac" u16x4, "fset" u8x3, packed
+ * by VertexFormat_pack, gpu_vertex_format.cc:300-330): */
+#define SGPU_DRAW_STRIDE 36   /* bytes per vertex */
+#define SGPU_DRAW_OFS_POS 0
+#define SGPU_DRAW_OFS_NOR 16
+#define SGPU_DRAW_OFS_MSK 22
+#define SGPU_DRAW_OFS_COL 24
+#define SGPU_DRAW_OFS_FSET 32
+/* Padding bytes and attributes the reference leaves unwritten (colours of a
+ * mesh without colour layers, the mask of grids without a mask) are zero.
+ * FACES: 3 vertices per visible looptri (visible: no corner has ME_HIDE and
+ * face_sets[poly] > 0; without face sets nothing is visible, as
+ * gpu_pbvh_is_looptri_visible has it).  GRIDS: grid_size^2 vertices per grid
+ * when smooth, 4 per grid quad when flat. */
+#define SGPU_ME_SMOOTH 1 /* MPoly.flag, DMFlagMat.flag */
+#define SGPU_ME_HIDE 16  /* MVert.flag */
+typedef struct SGPU_DMFlagMat { /* DMFlagMat: per grid, its face's material and flag */
+  short mat_nr;
+  char flag;
+  char _pad;
+} SGPU_DMFlagMat;
+typedef struct SGPU_DrawSetup {
+  const int *face_sets;     /* CD_SCULPT_FACE_SETS per poly (FACES) / base face (GRIDS); nullable */
+  int face_sets_color_seed; /* BKE_pbvh_face_sets_color_set */
+  int face_sets_color_default;
+  const unsigned char *loop_colors; /* FACES: CD_MLOOPCOL, r g b a per loop; nullable */
+  const float *vert_colors;         /* FACES: CD_PROP_COLOR, rgba per vertex; nullable */
+  int use_sculpt_vertex_colors;     /* U.experimental.use_sculpt_vertex_colors */
+  const SGPU_DMFlagMat *grid_flag_mats; /* GRIDS: per grid; NULL = every grid ME_SMOOTH, mat 0 */
+} SGPU_DrawSetup;
+/* GPU_pbvh_*_buffers_build for every leaf: the visible prims, smooth or flat
+ * (from the leaf's first prim), material, and each leaf's place in the vertex
+ * buffer; allocates the buffer and marks every leaf PBVH_RebuildDrawBuffers |
+ * PBVH_UpdateDrawBuffers.  Face-set and colour layers are read here: call it
+ * again after they change (the reference rebuilds on PBVH_RebuildDrawBuffers).
+ * Synchronous. */
+int sgpu_draw_buffers_build(sgpu_mesh *mesh, const SGPU_DrawSetup *setup);
+/* The update: every leaf flagged PBVH_UpdateDrawBuffers gets its buffer filled
+ * from the current positions, normals and mask, its show_overlay recomputed,
+ * and PBVH_RebuildDrawBuffers | PBVH_UpdateDrawBuffers cleared on every leaf.
+ * One kernel on the mesh stream; returns without waiting. */
+int sgpu_draw_buffers_update(sgpu_mesh *mesh);
+/* Layout per node (reference node order, internal nodes empty):
+ * vert_off[totnode + 1] first vertex of the node's buffer, and the buffer's
+ * tot_tri (visible looptris; 0 for grids, as the grid buffers leave it),
+ * smooth 0/1 and material_index.  Any output may be NULL.  Host data, no GPU
+ * work. */
+int sgpu_draw_buffers_layout(sgpu_mesh *mesh, int64_t *vert_off, int *tot_tri, int *smooth,
+                             int *material_index);
+/* show_overlay per node after the last update (!empty_mask || !default_face_set). */
+int sgpu_draw_buffers_overlay(sgpu_mesh *mesh, int *show_overlay);
+/* Copies the whole vertex buffer (vert_off[totnode] * SGPU_DRAW_STRIDE bytes). */
+int sgpu_draw_buffers_get(sgpu_mesh *mesh, void *dst, size_t bytes);
+/* The device address and size of the vertex buffer (owned by the handle). */
+int sgpu_draw_buffers_device(sgpu_mesh *mesh, void **d_vbo, size_t *bytes);
+
 /* ---- batches of independent meshes ----
  * Mesh i strokes with brushes[i] over dabs[dab_offsets[i] .. dab_offsets[i+1]);
  * dab_tools (nullable) is indexed like dabs.

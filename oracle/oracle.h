@@ -127,4 +127,32 @@ float or_curve_strength(int preset, float dist, float radius);
 }
 #endif
 
+/* ---- headless draw buffers ----
+ * pbvh_update_draw_buffers (pbvh.c:3240-3290) with GPU_pbvh_mesh_buffers_build
+ * / _update (gpu_buffers.c:174-400) and GPU_pbvh_grid_buffers_update
+ * (gpu_buffers.c:548-725), writing the 36-byte interleaved vertex format into
+ * one buffer, node after node.  Bytes the reference leaves unwritten are left
+ * as the caller initialised them. */
+typedef struct OrDrawSetup {
+  const int *face_sets;              /* per poly (FACES) / base face (GRIDS), nullable */
+  int face_sets_color_seed, face_sets_color_default;
+  const unsigned char *loop_colors;  /* FACES: r g b a per loop, nullable */
+  const float *vert_colors;          /* FACES: rgba per vertex, nullable */
+  int use_sculpt_vertex_colors;
+  const unsigned char *grid_flag_mats; /* GRIDS: DMFlagMat records (4 bytes), nullable */
+  const unsigned char *vert_flag;    /* FACES: MVert.flag per vertex, nullable (none hidden) */
+  const int *lt_loops;               /* FACES: 3 loop indices per looptri (loop colours) */
+} OrDrawSetup;
+/* Layout per node: vert_off[totnode + 1], tot_tri, smooth, material (nullable
+ * outputs); marks every leaf PBVH_RebuildDrawBuffers | PBVH_UpdateDrawBuffers.
+ * Returns the vertex count. */
+int64_t or_draw_build(OrMesh *m, const OrDrawSetup *s, int64_t *vert_off, int *tot_tri,
+                      int *smooth, int *material);
+/* Fills every leaf flagged PBVH_UpdateDrawBuffers at vert_off * 36 in vbo,
+ * sets overlay[node] (show_overlay) for those, clears the two draw flags. */
+void or_draw_update(OrMesh *m, const OrDrawSetup *s, const int64_t *vert_off, unsigned char *vbo,
+                    int *overlay);
+/* BKE_paint_face_set_overlay_color_get (paint.c:2219-2236), rgb bytes. */
+void or_face_set_color(int face_set, int seed, unsigned char rgb[3]);
+
 #endif

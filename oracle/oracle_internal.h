@@ -95,4 +95,8 @@ struct OrMesh {
   OrStateD sd;
 };
 
+void or_poly_normal_fp32(const OrMesh *m, int p, float r[3]);
+void or_normal_quad_fp32(float n[3], const float *v1, const float *v2, const float *v3,
+                         const float *v4);
+
 #endif

@@ -38,6 +38,17 @@ void or_curve_build(int preset, OrCurve *cu);
 #undef RSQRT
 #undef RFABS
 
+/* FP32 face normals for the draw-buffer restatement (oracle_draw.c). */
+void or_poly_normal_fp32(const OrMesh *m, int p, float r[3])
+{
+  poly_normal_f(m, m->sf.co, p, r);
+}
+void or_normal_quad_fp32(float n[3], const float *v1, const float *v2, const float *v3,
+                         const float *v4)
+{
+  normal_quad_f(n, v1, v2, v3, v4);
+}
+
 int or_search_sphere(OrMesh *m, const float center[3], float radius_sq, int original,
                      int *out_nodes)
 {

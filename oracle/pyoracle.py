@@ -29,6 +29,14 @@ class OrBrush(C.Structure):
                 ("use_original_bb", C.c_int)]
 
 
+class OrDrawSetup(C.Structure):
+    _fields_ = [("face_sets", C.c_void_p), ("face_sets_color_seed", C.c_int),
+                ("face_sets_color_default", C.c_int), ("loop_colors", C.c_void_p),
+                ("vert_colors", C.c_void_p), ("use_sculpt_vertex_colors", C.c_int),
+                ("grid_flag_mats", C.c_void_p), ("vert_flag", C.c_void_p),
+                ("lt_loops", C.c_void_p)]
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -62,6 +70,10 @@ def lib():
         L.or_get_vert_tags.argtypes = [vp, vp]
         L.or_stroke.restype = C.c_int64
         L.or_stroke.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
+        L.or_draw_build.restype = C.c_int64
+        L.or_draw_build.argtypes = [vp, C.POINTER(OrDrawSetup), vp, vp, vp, vp]
+        L.or_draw_update.argtypes = [vp, C.POINTER(OrDrawSetup), vp, vp, vp]
+        L.or_face_set_color.argtypes = [i, i, vp]
         L.or_raycast.restype = i
         L.or_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp, vp]
         L.or_grids_special_quads.restype = i
@@ -253,6 +265,48 @@ class OracleMesh:
     def update_bounds(self, flag: int):
         lib().or_update_bounds(self.h, flag)
 
+    def draw_build(self, face_sets=None, seed: int = 0, color_default: int = 1,
+                   loop_colors=None, vert_colors=None, use_vert_colors: bool = False,
+                   grid_flag_mats=None, vert_flag=None, lt_loops=None) -> dict:
+        """The draw-buffer layout per node; keeps the inputs for draw_update.
+        grid_flag_mats: (num_grids, 2) ints (mat_nr, flag)."""
+        keep = []
+
+        def arr(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data_as(C.c_void_p)
+
+        fm = None
+        if grid_flag_mats is not None:
+            g = np.asarray(grid_flag_mats)
+            fm = np.zeros(g.shape[0], dtype=np.dtype([("mat_nr", "<i2"), ("flag", "i1"),
+                                                      ("_pad", "i1")]))
+            fm["mat_nr"] = g[:, 0]
+            fm["flag"] = g[:, 1]
+        st = OrDrawSetup(arr(face_sets, np.int32), seed, color_default, arr(loop_colors, np.uint8),
+                         arr(vert_colors, np.float32), int(bool(use_vert_colors)),
+                         arr(fm, fm.dtype) if fm is not None else None, arr(vert_flag, np.uint8),
+                         arr(lt_loops, np.int32))
+        n = self.num_nodes
+        out = {"vert_off": np.zeros(n + 1, dtype=np.int64), "tot_tri": np.zeros(n, np.int32),
+               "smooth": np.zeros(n, np.int32), "material_index": np.zeros(n, np.int32)}
+        lib().or_draw_build(self.h, C.byref(st), _p(out["vert_off"]), _p(out["tot_tri"]),
+                            _p(out["smooth"]), _p(out["material_index"]))
+        self._draw = (st, keep, out["vert_off"])
+        return out
+
+    def draw_update(self, vbo: np.ndarray) -> np.ndarray:
+        """Fills the flagged leaves into vbo (uint8, vert_off[-1] * 36 bytes);
+        returns show_overlay per node (-1 where not updated)."""
+        st, _, vert_off = self._draw
+        assert vbo.dtype == np.uint8 and vbo.nbytes >= int(vert_off[-1]) * 36
+        ov = np.full(self.num_nodes, -1, dtype=np.int32)
+        lib().or_draw_update(self.h, C.byref(st), _p(vert_off), _p(vbo), _p(ov))
+        return ov
+
     def raycast(self, ray_start, ray_normal, depth: float = 3.4028234663852886e38,
                 original: int = 0):
         """BKE_pbvh_raycast with the spec'd callback: (hit, depth, active vertex,
@@ -281,6 +335,12 @@ class OracleMesh:
         tot = lib().or_stroke(self.h, C.byref(b), _p(d), d.shape[0], _p(tools), which, nthreads,
                               _p(per))
         return int(tot), per
+
+
+def face_set_color(face_set: int, seed: int) -> np.ndarray:
+    out = np.zeros(3, dtype=np.uint8)
+    lib().or_face_set_color(face_set, seed, _p(out))
+    return out
 
 
 def curve_table(preset: int):

@@ -87,12 +87,63 @@ def lib():
         L.rp_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
         L.rp_curve_table.argtypes = [i, vp, vp]
         L.rp_curve_evaluate.argtypes = [i, vp, i, vp]
+        L.rp_pbvh.restype = vp
+        L.rp_pbvh.argtypes = [vp]
+        L.rg_pbvh.restype = vp
+        L.rg_pbvh.argtypes = [vp]
+        L.rp_draw_setup_faces.argtypes = [vp, i, vp, vp, i, vp, vp, vp, i, i, i]
+        L.rp_draw_setup_grids.argtypes = [vp, vp, vp, i, i]
+        L.rp_draw.argtypes = [vp]
+        L.rp_draw_node_info.argtypes = [vp, i, vp]
+        L.rp_draw_stride.restype = i
+        L.rp_draw_node_bytes.argtypes = [vp, i, vp]
+        L.rp_draw_format.argtypes = [vp, vp]
+        L.rp_face_set_color.argtypes = [i, i, vp]
+        L.rp_hash_int_01.restype = f
+        L.rp_hash_int_01.argtypes = [C.c_uint]
         _lib = L
     return _lib
 
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def draw_format():
+    """(offsets, sizes) of pos, nor, msk, ac, fset and the stride, as the
+    reference's VertexFormat_pack lays them out."""
+    off = np.zeros(5, dtype=np.int32)
+    sz = np.zeros(5, dtype=np.int32)
+    lib().rp_draw_format(_p(off), _p(sz))
+    return off, sz, lib().rp_draw_stride()
+
+
+def face_set_color(face_set: int, seed: int) -> np.ndarray:
+    out = np.zeros(3, dtype=np.uint8)
+    lib().rp_face_set_color(face_set, seed, _p(out))
+    return out
+
+
+def hash_int_01(k: int) -> float:
+    return float(lib().rp_hash_int_01(k))
+
+
+def _draw_collect(pbvh, num_nodes: int) -> dict:
+    """BKE_pbvh_draw_cb on every node that needs an update, then per node its
+    buffer: vertex count (-1: none), tot_tri, smooth, material_index,
+    show_overlay, and its bytes."""
+    lib().rp_draw(pbvh)
+    info = np.zeros((num_nodes, 5), dtype=np.int32)
+    stride = lib().rp_draw_stride()
+    data = []
+    for n in range(num_nodes):
+        lib().rp_draw_node_info(pbvh, n, _p(info[n]))
+        b = np.zeros(max(int(info[n, 0]), 0) * stride, dtype=np.uint8)
+        if b.size:
+            lib().rp_draw_node_bytes(pbvh, n, _p(b))
+        data.append(b)
+    return {"nverts": info[:, 0], "tot_tri": info[:, 1], "smooth": info[:, 2],
+            "material_index": info[:, 3], "show_overlay": info[:, 4], "bytes": data}
 
 
 def curve_table(preset: int):
@@ -237,6 +288,27 @@ class RefPBVH:
         return bool(hit), dep[0], int(av[0]), int(af[0]), fn
 
 
+def _refpbvh_draw_setup(self, m, face_sets=None, loop_colors=None, vert_colors=None,
+                        use_vert_colors=False, seed: int = 0, color_default: int = 1):
+    ls = np.ascontiguousarray(m.polys["loopstart"], dtype=np.int32)
+    tl = np.ascontiguousarray(m.polys["totloop"], dtype=np.int32)
+    fs = None if face_sets is None else np.ascontiguousarray(face_sets, dtype=np.int32)
+    lc = None if loop_colors is None else np.ascontiguousarray(loop_colors, dtype=np.uint8)
+    vc = None if vert_colors is None else np.ascontiguousarray(vert_colors, dtype=np.float32)
+    self._draw_keep = (ls, tl, fs, lc, vc)
+    lib().rp_draw_setup_faces(lib().rp_pbvh(self.h), ls.shape[0], _p(ls), _p(tl),
+                              m.loops.shape[0], _p(fs), _p(lc), _p(vc), int(bool(use_vert_colors)),
+                              seed, color_default)
+
+
+def _refpbvh_draw(self) -> dict:
+    return _draw_collect(lib().rp_pbvh(self.h), self.num_nodes)
+
+
+RefPBVH.draw_setup = _refpbvh_draw_setup
+RefPBVH.draw = _refpbvh_draw
+
+
 class RefGrids:
     """Multires grids driven by the reference's own subdiv_ccg.c and pbvh.c:
     adjacency, PBVH, normal update with seam stitching, bounds refit."""
@@ -318,6 +390,22 @@ class RefGrids:
         fn = np.zeros(3, dtype=np.float32)
         hit = lib().rg_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(ag), _p(fn))
         return bool(hit), dep[0], int(av[0]), int(ag[0]), fn
+
+    def draw_setup(self, face_sets=None, grid_flag_mats=None, seed: int = 0,
+                   color_default: int = 1):
+        """grid_flag_mats: (num_grids, 2) ints (mat_nr, flag)."""
+        fs = None if face_sets is None else np.ascontiguousarray(face_sets, dtype=np.int32)
+        fm = None
+        if grid_flag_mats is not None:
+            g = np.asarray(grid_flag_mats)
+            fm = np.zeros((g.shape[0], 4), dtype=np.uint8)
+            fm[:, 0:2] = g[:, 0].astype("<i2").view(np.uint8).reshape(-1, 2)
+            fm[:, 2] = g[:, 1].astype(np.uint8)
+        self._draw_keep = (fs, fm)
+        lib().rp_draw_setup_grids(lib().rg_pbvh(self.h), _p(fs), _p(fm), seed, color_default)
+
+    def draw(self) -> dict:
+        return _draw_collect(lib().rg_pbvh(self.h), self.num_nodes)
 
     def vertex_coords(self, vertex: int) -> np.ndarray:
         nf = lib().rg_vertex_num_faces(self.h, vertex)

@@ -376,3 +376,9 @@ int rp_raycast(RefPin *r, const float start[3], const float normal[3], int origi
   memcpy(face_normal, d.face_normal, sizeof(float[3]));
   return d.hit ? 1 : 0;
 }
+
+/* The PBVH of a harness mesh (the draw-buffer functions of refpin_draw.c take it). */
+PBVH *rp_pbvh(RefPin *r)
+{
+  return r->pbvh;
+}

@@ -197,7 +197,6 @@ static inline void LIB_rctf_init(rctf *r, float xmin, float xmax, float ymin, fl
   r->ymin = ymin;
   r->ymax = ymax;
 }
-unsigned char unit_float_to_uchar_clamp(float val);
 
 /* ---- guarded allocator stand-ins (intern/guardedalloc) ---- */
 void *MEM_mallocN(size_t len, const char *str);
@@ -663,7 +662,7 @@ void BKE_mesh_calc_normals_looptri(MVert *mverts, int numVerts, const MLoop *mlo
 bool paint_is_face_hidden(const MLoopTri *lt, const MVert *mvert, const MLoop *mloop);
 bool paint_is_grid_face_hidden(const unsigned int *grid_hidden, int gridsize, int x, int y);
 
-/* ---- draw buffers (OpenGL; not built: no graphics stack) ---- */
+/* ---- draw buffers (gpu_buffers.c, compiled by refpin_draw.c over host arrays) ---- */
 typedef struct GPU_PBVH_Buffers GPU_PBVH_Buffers;
 #define GPU_PBVH_BUFFERS_SHOW_MASK (1 << 1)
 #define GPU_PBVH_BUFFERS_SHOW_VCOL (1 << 2)
@@ -675,9 +674,18 @@ GPU_PBVH_Buffers *GPU_pbvh_mesh_buffers_build(const MPoly *mpoly, const MLoop *m
                                               int face_indices_len, const struct Mesh *mesh);
 GPU_PBVH_Buffers *GPU_pbvh_grid_buffers_build(int totgrid, BLI_bitmap **grid_hidden);
 GPU_PBVH_Buffers *GPU_pbvh_bmesh_buffers_build(bool smooth_shading);
-void GPU_pbvh_mesh_buffers_update(GPU_PBVH_Buffers *buffers, ...);
-void GPU_pbvh_grid_buffers_update(GPU_PBVH_Buffers *buffers, ...);
+void GPU_pbvh_mesh_buffers_update(GPU_PBVH_Buffers *buffers, const MVert *mvert,
+                                  const float (*vert_normals)[3], const float *vmask,
+                                  const MLoopCol *vcol, const int *sculpt_face_sets,
+                                  int face_sets_color_seed, int face_sets_color_default,
+                                  const MPropCol *vtcol, int update_flags);
+void GPU_pbvh_grid_buffers_update(GPU_PBVH_Buffers *buffers, struct SubdivCCG *subdiv_ccg,
+                                  CCGElem **grids, const DMFlagMat *grid_flag_mats,
+                                  int *grid_indices, int totgrid, const int *sculpt_face_sets,
+                                  int face_sets_color_seed, int face_sets_color_default,
+                                  const CCGKey *key, int update_flags);
 void GPU_pbvh_bmesh_buffers_update(GPU_PBVH_Buffers *buffers, ...);
-void GPU_pbvh_grid_buffers_update_free(GPU_PBVH_Buffers *buffers, ...);
+void GPU_pbvh_grid_buffers_update_free(GPU_PBVH_Buffers *buffers, const DMFlagMat *grid_flag_mats,
+                                       const int *grid_indices);
 void GPU_pbvh_bmesh_buffers_update_free(GPU_PBVH_Buffers *buffers);
 void GPU_pbvh_buffers_update_flush(GPU_PBVH_Buffers *buffers);

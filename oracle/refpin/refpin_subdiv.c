@@ -424,3 +424,8 @@ int rg_raycast(RefGrids *g, const float start[3], const float normal[3], int ori
   memcpy(face_normal, d.face_normal, sizeof(float[3]));
   return d.hit ? 1 : 0;
 }
+
+PBVH *rg_pbvh(RefGrids *g)
+{
+  return g->pbvh;
+}

@@ -402,52 +402,19 @@ void BM_mesh_elem_index_ensure(BMesh *bm, int htype)
 {
   refpin_unreachable("dyntopo");
 }
-void GPU_pbvh_buffers_free(GPU_PBVH_Buffers *buffers)
-{
-  (void)buffers;
-}
-GPU_PBVH_Buffers *GPU_pbvh_mesh_buffers_build(const MPoly *mpoly, const MLoop *mloop,
-                                              const MLoopTri *looptri, const MVert *verts,
-                                              const int *face_indices,
-                                              const int *sculpt_face_sets, int face_indices_len,
-                                              const struct Mesh *mesh)
-{
-  refpin_unreachable("draw buffers");
-  return NULL;
-}
-GPU_PBVH_Buffers *GPU_pbvh_grid_buffers_build(int totgrid, BLI_bitmap **grid_hidden)
-{
-  refpin_unreachable("draw buffers");
-  return NULL;
-}
+/* Draw buffers: refpin_draw.c compiles the reference's; BMesh stays out. */
 GPU_PBVH_Buffers *GPU_pbvh_bmesh_buffers_build(bool smooth_shading)
 {
-  refpin_unreachable("draw buffers");
+  refpin_unreachable("dyntopo draw buffers");
   return NULL;
-}
-void GPU_pbvh_mesh_buffers_update(GPU_PBVH_Buffers *buffers, ...)
-{
-  refpin_unreachable("draw buffers");
-}
-void GPU_pbvh_grid_buffers_update(GPU_PBVH_Buffers *buffers, ...)
-{
-  refpin_unreachable("draw buffers");
 }
 void GPU_pbvh_bmesh_buffers_update(GPU_PBVH_Buffers *buffers, ...)
 {
-  refpin_unreachable("draw buffers");
-}
-void GPU_pbvh_grid_buffers_update_free(GPU_PBVH_Buffers *buffers, ...)
-{
-  refpin_unreachable("draw buffers");
+  refpin_unreachable("dyntopo draw buffers");
 }
 void GPU_pbvh_bmesh_buffers_update_free(GPU_PBVH_Buffers *buffers)
 {
-  refpin_unreachable("draw buffers");
-}
-void GPU_pbvh_buffers_update_flush(GPU_PBVH_Buffers *buffers)
-{
-  refpin_unreachable("draw buffers");
+  refpin_unreachable("dyntopo draw buffers");
 }
 
 /* Nearest-to-ray queries are not pinned: dist_squared_ray_to_seg_v3
@@ -475,8 +442,3 @@ void mid_v3_v3v3(float r[3], const float a[3], const float b[3])
   refpin_unreachable("raycast root projection");
 }
 
-unsigned char unit_float_to_uchar_clamp(float val)
-{
-  refpin_unreachable("curve premultiply / display");
-  return 0;
-}
