@@ -11,7 +11,8 @@ normal update and bounding-box refit, as the reference's stroke does.
            time), stroke time from CUDA events on the mesh stream; the stroke
            runs as one launch of the persistent stroke kernel (cluster size
            picked by the autotuner); positions, normals and node boxes are
-           restored from a device snapshot and L2 flushed (256 MiB write)
+           restored from a device snapshot and L2 flushed (256 MiB write, then a
+           256 MiB read of another buffer)
            before every step, both outside the timed region.
   e2e    : the same through sgpu_stroke_host with page-locked host buffers:
            H2D of positions and normals, full box refit, stroke, D2H of
@@ -75,6 +76,12 @@ def parse_args():
                          "with ncu for the ray kernels)")
     ap.add_argument("--raycast-mesh", choices=["faces", "grids", "both"], default="both",
                     help="meshes of --raycast-only")
+    ap.add_argument("--draw-only", action="store_true",
+                    help="full draw-buffer refreshes on the workload mesh and on the multires "
+                         "torus, one JSON line, and exit (the command profiled with ncu for "
+                         "the draw kernels)")
+    ap.add_argument("--draw-mesh", choices=["faces", "grids", "both"], default="both",
+                    help="meshes of --draw-only")
     ap.add_argument("--phases", action="store_true",
                     help="per-phase profile of the persistent stroke on all five workloads "
                          "(one JSON line each), no report")
@@ -167,7 +174,7 @@ def workload():
            "looptris": int(m.looptris.shape[0]), "dabs": int(st.dabs.shape[0]),
            "radius": st.radius, "strength": st.strength, "symmetry": "X",
            "curve": "smooth", "leaf_limit": leaf_limit, "mask": "seeded smooth noise",
-           "l2": "flushed before every step (256 MiB device write)"}
+           "l2": "flushed before every step (256 MiB device write, then 256 MiB read)"}
     return m, st, leaf_limit, cfg
 
 
@@ -382,6 +389,8 @@ def run_gpu(args):
                                                   BATCH_SEQUENTIAL)
     g.restore()
     ray = run_raycast_leg(g, m, leaf_limit, args.no_cpu)
+    g.restore()
+    draw = run_draw_leg(g, m, st, leaf_limit, args.no_cpu, peak=measured_peaks()[0])
 
     if world > 1:
         import torch
@@ -429,11 +438,106 @@ def run_gpu(args):
         "plain_eager": plain_eager,
         "batch": batch,
         "raycast": ray,
+        "draw_buffers": draw,
         "cpu_baseline": ({k: v for k, v in cpu.items() if k != "seconds"} if cpu else None),
         "clocks": clk,
     }
     print(json.dumps(line))
     return 0
+
+
+def draw_alg_bytes(g, masked: bool) -> int:
+    """Algorithmic bytes of a full draw-buffer refresh: the vertex buffer
+    written once (36 B per vertex) and each input read once: FACES per visible
+    looptri its corner record (16 B) and per mesh vertex its
+    position, normal (float4 each) and mask; GRIDS per element the same three."""
+    lay = g.draw_buffers_layout()
+    nverts = int(lay["vert_off"][-1])
+    per_vert_in = 16 + 16 + (4 if masked else 0)
+    if g.info.type == 0:
+        tris = int(lay["tot_tri"].sum())
+        return nverts * 36 + tris * 16 + g.num_verts * per_vert_in
+    return nverts * 36 + g.num_verts * per_vert_in
+
+
+def time_draw(g, reps: int = 20):
+    """Full refreshes (every leaf flagged) timed with CUDA events; L2 flushed
+    before each.  Returns the per-call times in ms."""
+    g.draw_buffers_update_timed(all_leaves=True)
+    out = []
+    for _ in range(reps):
+        g.flush_l2()
+        out.append(g.draw_buffers_update_timed(all_leaves=True))
+    return out
+
+
+def run_draw_leg(g, m, st, leaf_limit, no_cpu, peak):
+    """Headless draw buffers (pbvh_update_draw_buffers without GL) on the
+    workload mesh: seeded face sets 1..8 on every poly, the mesh's mask,
+    smooth shading.  A full refresh (all leaves) and the refresh after one
+    stroke (the leaves it touched), CUDA-event timed; the oracle's full
+    refresh on one host core."""
+    from dune_sculpt_gb300.sculpt import STROKE_TEAM
+
+    rng = np.random.default_rng(0x5EED0000 + 9)
+    fs = rng.integers(1, 9, size=m.polys.shape[0]).astype(np.int32)
+    t0 = time.perf_counter()
+    g.draw_buffers_build(face_sets=fs, seed=3, color_default=1)
+    build_s = time.perf_counter() - t0
+    times = time_draw(g)
+    ms = statistics.median(times)
+    alg = draw_alg_bytes(g, m.mask is not None)
+    achieved = alg / (ms / 1e3) / 1e9
+    g.restore()
+    g.draw_buffers_update_timed(all_leaves=False)  # consumes the flags the restore brought back
+    g.stroke(st, mode=STROKE_TEAM)
+    touched = int(np.count_nonzero(g.nodes()["flag"] & 16))
+    g.flush_l2()
+    partial_ms = g.draw_buffers_update_timed(all_leaves=False)
+    lay = g.draw_buffers_layout()
+    out = {"workload": "icosphere level 8, face sets 1..8, masked, smooth",
+           "vertices": int(lay["vert_off"][-1]), "bytes_written": int(lay["vert_off"][-1]) * 36,
+           "full_refresh_ms": ms, "full_refresh_min_ms": min(times),
+           "roofline": {"bound": "hbm", "kernel": "k_draw_faces", "alg_bytes": alg,
+                        "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak},
+           "after_stroke": {"leaves_refilled": touched, "ms": partial_ms},
+           "layout_build_s": build_s,
+           "timing": "CUDA events on the mesh stream, L2 flushed before each refresh"}
+    if not no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        o = pyoracle.OracleMesh.faces(m, leaf_limit)
+        o.recalc_all_normals()
+        L = o.draw_build(face_sets=fs, seed=3, color_default=1, vert_flag=m.verts["flag"])
+        vbo = np.zeros(int(L["vert_off"][-1]) * 36, dtype=np.uint8)
+        t0 = time.perf_counter()
+        o.draw_update(vbo)
+        cpu_s = time.perf_counter() - t0
+        out["cpu_baseline"] = {"full_refresh_ms": 1e3 * cpu_s, "cores": 1, "kind": "port",
+                               "sample": "one full refresh, FP32 restatement, one thread"}
+        o.close()
+    return out
+
+
+def run_draw_grids(synth, PBVH, peak):
+    """Full draw-buffer refresh on the multires torus (50,000 grids of 17x17),
+    smooth, masked, face sets per base face."""
+    g5, _ = synth.cfg5_multires()
+    gp = PBVH.build_grids(g5)
+    fs = ((np.arange(g5.num_faces) % 8) + 1).astype(np.int32)
+    gp.draw_buffers_build(face_sets=fs, seed=3, color_default=1)
+    times = time_draw(gp)
+    ms = statistics.median(times)
+    alg = draw_alg_bytes(gp, g5.mask is not None)
+    achieved = alg / (ms / 1e3) / 1e9
+    return {"workload": "multires torus 50,000 grids of 17x17, smooth, masked",
+            "vertices": int(gp.draw_buffers_layout()["vert_off"][-1]),
+            "full_refresh_ms": ms, "full_refresh_min_ms": min(times),
+            "roofline": {"bound": "hbm", "kernel": "k_draw_grids", "alg_bytes": alg,
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak}}
 
 
 def time_raycast(g, starts, dirs, reps=20, one=200):
@@ -560,6 +664,25 @@ def main():
         return run_quick(args)
     if args.phases:
         return run_phases(args)
+    if args.draw_only:
+        from dune_sculpt_gb300 import build as libbuild
+
+        libbuild.build()
+        from dune_sculpt_gb300 import synth
+        from dune_sculpt_gb300.sculpt import PBVH
+
+        peak = measured_peaks()[0]
+        out = {}
+        if args.draw_mesh in ("faces", "both"):
+            m, st, leaf_limit, _ = workload()
+            g = PBVH.build_mesh(m, leaf_limit)
+            g.snapshot()
+            out["draw_faces"] = run_draw_leg(g, m, st, leaf_limit, True, peak)
+            g.free()
+        if args.draw_mesh in ("grids", "both"):
+            out["draw_grids"] = run_draw_grids(synth, PBVH, peak)
+        print(json.dumps(out))
+        return 0
     if args.raycast_only:
         from dune_sculpt_gb300 import build as libbuild
 

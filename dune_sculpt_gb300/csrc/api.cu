@@ -1343,7 +1343,9 @@ int sgpu_mesh_restore(sgpu_mesh* mesh) {
 int sgpu_mesh_flush_l2(sgpu_mesh* mesh) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
-  const size_t bytes = 256ull << 20;
+  // 256 MiB written, then another 256 MiB read (the dirty lines the write left
+  // are written back before the next timed kernel)
+  const size_t bytes = 512ull << 20;
   if (!mesh->flush_buf) {
     void* p = nullptr;
     if ((rc = mesh->alloc(reinterpret_cast<char**>(&p), bytes))) return rc;
@@ -1930,6 +1932,7 @@ int sgpu_draw_buffers_build(sgpu_mesh* mesh, const SGPU_DrawSetup* setup) {
                        mesh->stream),
        "read vertex flags");
     CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+    in.o2n = mesh->o2n.data();
     in.vert_flag.resize(h.totvert);
     for (int v = 0; v < h.totvert; v++) {
       unsigned char b[4];
@@ -1945,14 +1948,15 @@ int sgpu_draw_buffers_build(sgpu_mesh* mesh, const SGPU_DrawSetup* setup) {
   const size_t words = static_cast<size_t>(L.total_verts) * kDrawWords;
   if ((rc = draw_array<unsigned int>(mesh, &dd.vbo, nullptr, words))) return rc;
   long long* lvo = nullptr;
-  int *lts = nullptr, *ltc = nullptr, *lsm = nullptr, *tris = nullptr;
+  int *lts = nullptr, *ltc = nullptr, *lsm = nullptr, *tv4 = nullptr;
   unsigned int *fset = nullptr, *col = nullptr;
   if ((rc = draw_array(mesh, &lvo, L.leaf_vert_off.data(), L.leaf_vert_off.size())) ||
       (rc = draw_array(mesh, &lts, L.leaf_tri_start.data(), L.leaf_tri_start.size())) ||
       (rc = draw_array(mesh, &ltc, L.leaf_tri_count.data(), L.leaf_tri_count.size())) ||
       (rc = draw_array(mesh, &lsm, L.leaf_smooth.data(), L.leaf_smooth.size())) ||
-      (rc = draw_array(mesh, &tris, L.tris.data(), L.tris.size())) ||
-      (rc = draw_array<int>(mesh, &dd.overlay, nullptr, static_cast<size_t>(d.nleaf))))
+      (rc = draw_array(mesh, &tv4, L.tri_v4.data(), L.tri_v4.size())) ||
+      (rc = draw_array<int>(mesh, &dd.overlay, nullptr, static_cast<size_t>(d.nleaf))) ||
+      (rc = draw_array<int>(mesh, &dd.overlay_acc, nullptr, static_cast<size_t>(d.nleaf))))
     return rc;
   if (L.has_fset && (rc = draw_array(mesh, &fset, L.fset.data(), L.fset.size()))) return rc;
   if (L.show_vcol && (rc = draw_array(mesh, &col, L.col.data(), L.col.size()))) return rc;
@@ -1960,7 +1964,7 @@ int sgpu_draw_buffers_build(sgpu_mesh* mesh, const SGPU_DrawSetup* setup) {
   dd.leaf_tri_start = lts;
   dd.leaf_tri_count = ltc;
   dd.leaf_smooth = lsm;
-  dd.tris = tris;
+  dd.tri_v4 = tv4;
   dd.fset = fset;
   dd.col = col;
   // every leaf rebuilt and refilled at the next update (BKE_pbvh_node_mark_rebuild_draw)
@@ -1974,7 +1978,24 @@ int sgpu_draw_buffers_update(sgpu_mesh* mesh) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   if (!mesh->draw_built) return fail(SGPU_ERR_INVALID_ARG, "draw buffers not built");
-  CK(launch_draw_fill(mesh->dev, mesh->draw_dev, mesh->stream), "draw fill kernel");
+  CK(launch_draw_fill(mesh->dev, mesh->draw_dev, mesh->draw.max_units_smooth,
+                      mesh->draw.max_units_flat, mesh->stream), "draw fill kernel");
+  return SGPU_OK;
+}
+
+int sgpu_draw_buffers_update_timed(sgpu_mesh* mesh, int all_leaves, float* gpu_ms) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!mesh->draw_built) return fail(SGPU_ERR_INVALID_ARG, "draw buffers not built");
+  if (all_leaves) CK(launch_mark_all(mesh->dev, kUpdateDrawBuffers, mesh->stream), "mark kernel");
+  CK(cudaEventRecord(mesh->ev0, mesh->stream), "cudaEventRecord");
+  CK(launch_draw_fill(mesh->dev, mesh->draw_dev, mesh->draw.max_units_smooth,
+                      mesh->draw.max_units_flat, mesh->stream), "draw fill kernel");
+  CK(cudaEventRecord(mesh->ev1, mesh->stream), "cudaEventRecord");
+  CK(cudaEventSynchronize(mesh->ev1), "cudaEventSynchronize");
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, mesh->ev0, mesh->ev1), "elapsed");
+  if (gpu_ms) *gpu_ms = ms;
   return SGPU_OK;
 }
 

@@ -5,6 +5,7 @@
 // (gpu_buffers.c:307-400) and the set-up half of the update functions do on
 // the host in the reference; the per-update fill runs on the device.
 // Compiled with -ffp-contract=off.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -125,8 +126,8 @@ bool build_draw_layout(const HostMesh& h, const DrawInputs& in, DrawLayout* out,
   L.leaf_tri_count.assign(nleaf, 0);
   L.leaf_smooth.assign(nleaf, 0);
   if (h.type == kFaces) {
-    if (static_cast<int>(in.vert_flag.size()) != h.totvert) {
-      *err = "vertex flags missing";
+    if (static_cast<int>(in.vert_flag.size()) != h.totvert || !in.o2n) {
+      *err = "vertex flags or numbering missing";
       return false;
     }
     // fset per poly; faces are drawn only with a face-set layer
@@ -157,6 +158,8 @@ bool build_draw_layout(const HostMesh& h, const DrawInputs& in, DrawLayout* out,
         for (int j = 0; j < 3; j++) hidden = hidden || (in.vert_flag[h.lt_v[3 * lt + j]] & kMeHide);
         if (hidden || !L.has_fset || in.face_sets[poly] <= 0) continue;
         L.tris.push_back(lt);
+        for (int j = 0; j < 3; j++) L.tri_v4.push_back(in.o2n[h.lt_v[3 * lt + j]]);
+        L.tri_v4.push_back(poly);
         if (!L.show_vcol) continue;
         for (int j = 0; j < 3; j++) {
           unsigned short s[4];
@@ -179,6 +182,8 @@ bool build_draw_layout(const HostMesh& h, const DrawInputs& in, DrawLayout* out,
       L.leaf_tri_start[leaf] = start;
       L.leaf_tri_count[leaf] = cnt;
       L.leaf_smooth[leaf] = L.node_smooth[n];
+      int& mu = L.node_smooth[n] ? L.max_units_smooth : L.max_units_flat;
+      mu = std::max(mu, cnt);
       off += 3 * static_cast<int64_t>(cnt);
     }
     L.node_vert_off[totnode] = off;
@@ -211,6 +216,9 @@ bool build_draw_layout(const HostMesh& h, const DrawInputs& in, DrawLayout* out,
     const int leaf = h.node_leaf[n];
     L.leaf_vert_off[leaf] = off;
     L.leaf_smooth[leaf] = smooth;
+    const int units = ng * (smooth ? gs * gs : (gs - 1) * (gs - 1));
+    int& mu = smooth ? L.max_units_smooth : L.max_units_flat;
+    mu = std::max(mu, units);
     off += static_cast<int64_t>(ng) * (smooth ? gs * gs : (gs - 1) * (gs - 1) * 4);
   }
   L.node_vert_off[totnode] = off;

@@ -26,6 +26,7 @@ struct DrawInputs {
   bool use_vert_colors = false;
   const unsigned char* grid_flag_mats = nullptr;  // 4-byte DMFlagMat records
   std::vector<unsigned char> vert_flag;           // FACES: MVert.flag per vertex (caller order)
+  const int* o2n = nullptr;                       // FACES: caller vertex -> device vertex
 };
 
 struct DrawLayout {
@@ -36,11 +37,14 @@ struct DrawLayout {
   std::vector<long long> leaf_vert_off;
   std::vector<int> leaf_tri_start, leaf_tri_count, leaf_smooth;
   std::vector<int> tris;        // FACES: visible looptris, node order
+  std::vector<int> tri_v4;      // FACES: per visible looptri its device corners and poly
   std::vector<uint32_t> fset;   // per poly (FACES) / grid (GRIDS): r | g << 8 | b << 16 | nondefault << 24
   bool has_fset = false;        // face sets drawn (show_face_sets)
   std::vector<uint32_t> col;    // FACES with colours: ushort4 per vertex (2 words), buffer order
   bool show_vcol = false;
   int64_t total_verts = 0;
+  int max_units_smooth = 0;     // most units of a smooth / flat leaf (looptris,
+  int max_units_flat = 0;       // grid elements or grid quads)
 };
 
 // GPU_pbvh_*_buffers_build for every leaf.  Returns false with a message on
@@ -57,10 +61,11 @@ struct DrawDev {
   const int* leaf_tri_start;       // FACES
   const int* leaf_tri_count;       // FACES
   const int* leaf_smooth;
-  const int* tris;                 // FACES: visible looptris
+  const int* tri_v4;               // FACES: 4 ints per visible looptri (device corners, poly)
   const unsigned int* fset;        // per poly / grid, or null
   const unsigned int* col;         // FACES: 2 words per vertex, or null
   int* overlay;                    // per leaf id
+  int* overlay_acc;                // per leaf id: OR of the chunks of the running fill
 };
 
 }  // namespace sgpu

@@ -34,7 +34,8 @@ cudaError_t launch_l2_flush(void* buf, size_t bytes, cudaStream_t s);
 cudaError_t launch_mark_node(const DevMesh& m, int node, cudaStream_t s);
 cudaError_t launch_mark_all(const DevMesh& m, int bits, cudaStream_t s);
 // Headless draw buffers: fill every leaf flagged PBVH_UpdateDrawBuffers.
-cudaError_t launch_draw_fill(const DevMesh& m, const DrawDev& dd, cudaStream_t s);
+cudaError_t launch_draw_fill(const DevMesh& m, const DrawDev& dd, int max_units_smooth,
+                             int max_units_flat, cudaStream_t s);
 // Refit-chunk boxes of every leaf from the current positions.
 cudaError_t launch_chunk_boxes_all(const DevMesh& m, int nchunks, cudaStream_t s);
 // out[i] = in[idx[i]]: float4 or float.

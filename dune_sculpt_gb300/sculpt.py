@@ -86,7 +86,7 @@ EXPORTS = (
     "sgpu_mesh_get_team", "sgpu_autotune_team", "sgpu_batch_stroke", "sgpu_stroke_team_profile",
     "sgpu_raycast", "sgpu_draw_buffers_build", "sgpu_draw_buffers_update",
     "sgpu_draw_buffers_layout", "sgpu_draw_buffers_overlay", "sgpu_draw_buffers_get",
-    "sgpu_draw_buffers_device",
+    "sgpu_draw_buffers_device", "sgpu_draw_buffers_update_timed",
 )
 
 DRAW_STRIDE = 36  # SGPU_DRAW_STRIDE
@@ -163,6 +163,7 @@ def load(path: str | None = None):
     L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
     L.sgpu_draw_buffers_build.argtypes = [vp, C.POINTER(SGPU_DrawSetup)]
     L.sgpu_draw_buffers_update.argtypes = [vp]
+    L.sgpu_draw_buffers_update_timed.argtypes = [vp, i, vp]
     L.sgpu_draw_buffers_layout.argtypes = [vp, vp, vp, vp, vp]
     L.sgpu_draw_buffers_overlay.argtypes = [vp, vp]
     L.sgpu_draw_buffers_get.argtypes = [vp, vp, C.c_size_t]
@@ -376,6 +377,13 @@ class PBVH:
 
     def draw_buffers_update(self):
         _check(load().sgpu_draw_buffers_update(self._h))
+
+    def draw_buffers_update_timed(self, all_leaves: bool = False) -> float:
+        """The update timed with CUDA events (ms); all_leaves: full refresh."""
+        ms = C.c_float()
+        _check(load().sgpu_draw_buffers_update_timed(self._h, int(bool(all_leaves)),
+                                                     C.byref(ms)))
+        return ms.value
 
     def draw_buffers_layout(self) -> dict:
         n = self.num_nodes

@@ -307,6 +307,10 @@ int sgpu_draw_buffers_build(sgpu_mesh *mesh, const SGPU_DrawSetup *setup);
  * and PBVH_RebuildDrawBuffers | PBVH_UpdateDrawBuffers cleared on every leaf.
  * One kernel on the mesh stream; returns without waiting. */
 int sgpu_draw_buffers_update(sgpu_mesh *mesh);
+/* The update timed with CUDA events on the mesh stream (synchronous); with
+ * all_leaves every leaf is flagged PBVH_UpdateDrawBuffers first (outside the
+ * timed interval), a full refresh. */
+int sgpu_draw_buffers_update_timed(sgpu_mesh *mesh, int all_leaves, float *gpu_ms);
 /* Layout per node (reference node order, internal nodes empty):
  * vert_off[totnode + 1] first vertex of the node's buffer, and the buffer's
  * tot_tri (visible looptris; 0 for grids, as the grid buffers leave it),
@@ -364,7 +368,9 @@ typedef struct SGPU_KernelProfile {
 int sgpu_stroke_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
                         int ndabs, const int *dab_tools, SGPU_KernelProfile *out,
                         SGPU_StrokeStats *stats);
-/* Writes a device buffer larger than L2 (256 MiB) on the mesh stream. */
+/* Evicts L2 on the mesh stream: writes a 256 MiB device buffer (larger than
+ * L2), then reads another 256 MiB buffer so that the dirty lines of the write
+ * are written back before the next kernel. */
 int sgpu_mesh_flush_l2(sgpu_mesh *mesh);
 /* Page-locked host memory for the host-buffer path. */
 void *sgpu_host_alloc(size_t bytes);
