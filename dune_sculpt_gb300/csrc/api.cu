@@ -374,6 +374,7 @@ bool make_brush(const SGPU_Brush* b, int tool, DevBrush* out) {
   out->normal_radius_factor = b->normal_radius_factor;
   out->area_radius_factor = b->area_radius_factor;
   out->plane_offset = b->plane_offset;
+  out->crease_pinch_factor = b->crease_pinch_factor;
   out->x_first = c.x_first;
   out->x_last = c.x_last;
   out->mintable = c.mintable;
@@ -384,7 +385,7 @@ bool make_brush(const SGPU_Brush* b, int tool, DevBrush* out) {
 
 bool tool_ok(int tool) {
   return tool == kToolDraw || tool == kToolSmooth || tool == kToolInflate ||
-         tool == kToolClayStrips;
+         tool == kToolClayStrips || tool == kToolPinch || tool == kToolCrease;
 }
 
 // Launch bookkeeping: counts launches and, while profiling, brackets each one
@@ -423,7 +424,7 @@ struct Launcher {
 int launch_tool(Launcher& L, const DevBrush& b, PassParams pp) {
   const DevMesh& d = L.m->dev;
   cudaStream_t s = L.m->stream;
-  if (b.tool == kToolDraw || b.tool == kToolClayStrips) {
+  if (uses_area(b.tool)) {
     LAUNCH(L, kKArea, "area kernel", launch_area(d, b, pp, s));
     LAUNCH(L, kKBrush, "brush kernel", launch_brush(d, b, pp, s));
   } else if (b.tool == kToolInflate) {
@@ -957,6 +958,14 @@ int sgpu_do_inflate_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float 
 int sgpu_do_clay_strips_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
                               const float grab_delta[3], const int* nodes, int totnode) {
   return do_brush_tool(mesh, brush, kToolClayStrips, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_pinch_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                        const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolPinch, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_crease_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                         const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolCrease, location, grab_delta, nodes, totnode);
 }
 int sgpu_do_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
                   const float grab_delta[3], const int* nodes, int totnode) {

@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
   const int cnt = m.work->cull_count;
   const int total = m.cull_off[cnt];
   float area_no[3] = {0.0f, 0.0f, 0.0f}, area_co[3] = {0.0f, 0.0f, 0.0f};
-  if (b.tool == kToolDraw || b.tool == kToolClayStrips) {
+  if (uses_area(b.tool)) {
     for (int k = 0; k < 3; k++) {
       area_no[k] = __ldcg(&m.work->area_no[k]);
       area_co[k] = __ldcg(&m.work->area_co[k]);

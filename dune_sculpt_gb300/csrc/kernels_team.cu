@@ -776,7 +776,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
         clk.mark(a, rank, kPhCull);
         float area_no[3] = {0.0f, 0.0f, 0.0f}, area_co[3] = {0.0f, 0.0f, 0.0f};
-        if (tool == kToolDraw || tool == kToolClayStrips) {
+        if (uses_area(tool)) {
           const float rn = b.radius * b.normal_radius_factor;
           const float ra = b.radius * b.area_radius_factor;
           unsigned long long ab = 0;

@@ -161,6 +161,7 @@ struct DevBrush {
   float normal_radius_factor;
   float area_radius_factor;
   float plane_offset;
+  float crease_pinch_factor;
   float x_first, x_last;
   float mintable, range;
   float y[kCurveTable + 1];
@@ -179,7 +180,12 @@ struct PassParams {
 };
 
 constexpr int kBrushFrontFace = 1 << 27;
-constexpr int kToolDraw = 1, kToolSmooth = 2, kToolInflate = 4, kToolClayStrips = 18;
+constexpr int kToolDraw = 1, kToolSmooth = 2, kToolPinch = 3, kToolInflate = 4, kToolCrease = 16,
+              kToolClayStrips = 18;
+// Tools that reduce the area normal (and centre) before their sweep.
+__host__ __device__ __forceinline__ bool uses_area(int tool) {
+  return tool == kToolDraw || tool == kToolClayStrips || tool == kToolPinch || tool == kToolCrease;
+}
 
 // ---------------------------------------------------------------------------
 // Math (lib/intern/math_vector_inline.c, math_geom.cc, mesh_evaluate.c)
@@ -442,8 +448,10 @@ __device__ __forceinline__ void cross3(float* r, const float* a, const float* b)
 struct BrushFrame {
   float area_no[3];
   float off[3];  // draw: area_no * radius * strength
-  float xa[3], ya[3];  // clay strips: in-plane axes
+  float xa[3], ya[3];  // clay strips: in-plane axes; pinch: xa = stroke side axis
   float pd, inv_r, inv_rz;  // clay strips: plane offset, inverse extents
+  float pinch_k;   // crease: pinch factor^2 * |strength|
+  float inv_nlen;  // crease: -1 / |area_no|^2 (0 for a zero normal)
 };
 
 // Returns false when the clay-strips frame is degenerate (the pass then does
@@ -455,7 +463,17 @@ __device__ __forceinline__ bool make_frame(const DevBrush& b, const PassParams& 
   for (int k = 0; k < 3; k++) f.area_no[k] = area_no[k];
   const float dd = radius * b.strength;
   for (int k = 0; k < 3; k++) f.off[k] = area_no[k] * dd;
-  f.pd = f.inv_r = f.inv_rz = 0.0f;
+  f.pd = f.inv_r = f.inv_rz = f.pinch_k = f.inv_nlen = 0.0f;
+  if (b.tool == kToolPinch) {
+    cross3(f.xa, area_no, pp.delta);
+    if (normalize3(f.xa[0], f.xa[1], f.xa[2]) == 0.0f) return false;
+  }
+  if (b.tool == kToolCrease) {
+    const float corr = b.crease_pinch_factor * b.crease_pinch_factor;
+    f.pinch_k = b.strength < 0.0f ? -corr * b.strength : corr * b.strength;
+    const float nl = area_no[0] * area_no[0] + area_no[1] * area_no[1] + area_no[2] * area_no[2];
+    f.inv_nlen = nl > FLT_EPSILON ? -1.0f / nl : 0.0f;
+  }
   if (b.tool == kToolClayStrips) {
     cross3(f.xa, area_no, pp.delta);
     if (normalize3(f.xa[0], f.xa[1], f.xa[2]) == 0.0f) return false;
@@ -500,6 +518,43 @@ __device__ __forceinline__ bool brush_vertex(const DevMesh& m, const DevBrush& b
     co.y = co.y + no.y * kk;
     co.z = co.z + no.z * kk;
     moved = fade != 0.0f;
+    return true;
+  }
+  if (b.tool == kToolPinch) {
+    // toward the brush centre within the plane of the side axis and the normal
+    const float d2 = dist_sq(co, pp.loc);
+    if (!(d2 <= radius * radius)) return false;
+    const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+    const float fade = b.strength * sf;
+    const float* an = f.area_no;
+    const float c0 = pp.loc[0] - co.x, c1 = pp.loc[1] - co.y, c2 = pp.loc[2] - co.z;
+    const float px = c0 * f.xa[0] + c1 * f.xa[1] + c2 * f.xa[2];
+    const float pz = c0 * an[0] + c1 * an[1] + c2 * an[2];
+    const float v0 = f.xa[0] * px + an[0] * pz;
+    const float v1 = f.xa[1] * px + an[1] * pz;
+    const float v2 = f.xa[2] * px + an[2] * pz;
+    co.x = co.x + v0 * fade;
+    co.y = co.y + v1 * fade;
+    co.z = co.z + v2 * fade;
+    moved = fade != 0.0f;
+    return true;
+  }
+  if (b.tool == kToolCrease) {
+    // pinch toward the centre within the area plane, then draw along the normal
+    const float d2 = dist_sq(co, pp.loc);
+    if (!(d2 <= radius * radius)) return false;
+    const float sf = strength_factor(m, b, ys, pp, v, sqrtf(d2), radius);
+    const float* an = f.area_no;
+    const float k = sf * f.pinch_k;
+    float v0 = (pp.loc[0] - co.x) * k, v1 = (pp.loc[1] - co.y) * k, v2 = (pp.loc[2] - co.z) * k;
+    const float t = (v0 * an[0] + v1 * an[1] + v2 * an[2]) * f.inv_nlen;
+    v0 = v0 + an[0] * t;
+    v1 = v1 + an[1] * t;
+    v2 = v2 + an[2] * t;
+    co.x = co.x + (v0 + f.off[0] * sf);
+    co.y = co.y + (v1 + f.off[1] * sf);
+    co.z = co.z + (v2 + f.off[2] * sf);
+    moved = (b.strength * sf) != 0.0f;
     return true;
   }
   // clay strips

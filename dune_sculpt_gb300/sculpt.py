@@ -41,7 +41,7 @@ class SGPU_Brush(C.Structure):
                 ("curve_preset", C.c_int), ("radius", C.c_float), ("strength", C.c_float),
                 ("normal_radius_factor", C.c_float), ("area_radius_factor", C.c_float),
                 ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
-                ("use_original_bb", C.c_int)]
+                ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float)]
 
 
 class SGPU_MeshInfo(C.Structure):
@@ -77,6 +77,7 @@ EXPORTS = (
     "sgpu_mesh_create_grids", "sgpu_mesh_destroy", "sgpu_mesh_info", "sgpu_mesh_sync",
     "sgpu_mesh_stream", "sgpu_search_sphere", "sgpu_do_draw_brush", "sgpu_do_smooth_brush",
     "sgpu_do_inflate_brush", "sgpu_do_clay_strips_brush", "sgpu_do_brush",
+    "sgpu_do_pinch_brush", "sgpu_do_crease_brush",
     "sgpu_pbvh_update_normals", "sgpu_pbvh_update_bounds", "sgpu_pbvh_node_mark_update",
     "sgpu_stroke", "sgpu_get_verts", "sgpu_set_verts", "sgpu_get_positions",
     "sgpu_set_positions", "sgpu_get_normals", "sgpu_get_mask", "sgpu_get_node_bbs",
@@ -130,7 +131,8 @@ def load(path: str | None = None):
     L.sgpu_search_sphere.argtypes = [vp, vp, f, i, vp, vp]
     L.sgpu_raycast.argtypes = [vp, i, vp, vp, vp, i, vp, vp, vp, vp, vp]
     for name in ("sgpu_do_draw_brush", "sgpu_do_smooth_brush", "sgpu_do_inflate_brush",
-                 "sgpu_do_clay_strips_brush", "sgpu_do_brush"):
+                 "sgpu_do_clay_strips_brush", "sgpu_do_brush", "sgpu_do_pinch_brush",
+                 "sgpu_do_crease_brush"):
         getattr(L, name).argtypes = [vp, C.POINTER(SGPU_Brush), vp, vp, vp, i]
     L.sgpu_pbvh_update_normals.argtypes = [vp]
     L.sgpu_pbvh_update_bounds.argtypes = [vp, i]
@@ -237,6 +239,7 @@ def make_brush(st) -> SGPU_Brush:
     for k in range(3):
         b.view_normal[k] = st.view_normal[k]
     b.use_original_bb = st.use_original_bb
+    b.crease_pinch_factor = st.crease_pinch_factor
     return b
 
 
@@ -428,6 +431,12 @@ class PBVH:
 
     def do_clay_strips_brush(self, st, location, grab_delta, nodes=None):
         self._brush("sgpu_do_clay_strips_brush", st, location, grab_delta, nodes)
+
+    def do_pinch_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_pinch_brush", st, location, grab_delta, nodes)
+
+    def do_crease_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_crease_brush", st, location, grab_delta, nodes)
 
     def do_brush(self, st, location, grab_delta, nodes=None):
         self._brush("sgpu_do_brush", st, location, grab_delta, nodes)

@@ -205,9 +205,11 @@ class Stroke:
     flag: int = 0
     view_normal: tuple = (0.0, 0.0, 1.0)
     use_original_bb: int = 0
+    crease_pinch_factor: float = 0.5  # types_brush_defaults.h:23
 
 
 TOOL_DRAW, TOOL_SMOOTH, TOOL_INFLATE, TOOL_CLAY_STRIPS = 1, 2, 4, 18
+TOOL_PINCH, TOOL_CREASE = 3, 16
 CURVE_SHARP, CURVE_SMOOTH = 1, 2
 SYMM_X = 1
 

@@ -74,9 +74,11 @@ typedef struct SGPU_MLoopTri { /* MLoopTri, types_meshdata.h:178-181 */
 #define SGPU_PBVH_UpdateRedraw 32
 
 /* ---- brush (subset of Brush, types_brush.h:138-362) ---- */
-#define SGPU_TOOL_DRAW 1         /* SCULPT_TOOL_DRW */
+#define SGPU_TOOL_DRAW 1         /* SCULPT_TOOL_DRW (types_brush_enums.h:411) */
 #define SGPU_TOOL_SMOOTH 2       /* SCULPT_TOOL_SMOOTH */
+#define SGPU_TOOL_PINCH 3        /* SCULPT_TOOL_PINCH */
 #define SGPU_TOOL_INFLATE 4      /* SCULPT_TOOL_INFLATE */
+#define SGPU_TOOL_CREASE 16      /* SCULPT_TOOL_CREASE */
 #define SGPU_TOOL_CLAY_STRIPS 18 /* SCULPT_TOOL_CLAY_STRIPS */
 #define SGPU_BRUSH_FRONTFACE (1 << 27)
 #define SGPU_SYMM_X 1 /* PAINT_SYMM_X, types_scene.h:2174 */
@@ -101,6 +103,7 @@ typedef struct SGPU_Brush {
   float plane_offset;         /* clay strips plane offset */
   float view_normal[3];       /* front-face reference direction */
   int use_original_bb;        /* cull against orig_vb instead of vb */
+  float crease_pinch_factor;  /* crease: pinch strength (default 0.5, types_brush_defaults.h:23) */
 } SGPU_Brush;
 
 /* One dab of a stroke: location and grab delta (stroke direction). */
@@ -186,6 +189,10 @@ int sgpu_do_inflate_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float 
                           const float grab_delta[3], const int *nodes, int totnode);
 int sgpu_do_clay_strips_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
                               const float grab_delta[3], const int *nodes, int totnode);
+int sgpu_do_pinch_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                        const float grab_delta[3], const int *nodes, int totnode);
+int sgpu_do_crease_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                         const float grab_delta[3], const int *nodes, int totnode);
 /* Dispatch on brush->sculpt_tool. */
 int sgpu_do_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
                   const float grab_delta[3], const int *nodes, int totnode);

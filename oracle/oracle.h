@@ -36,7 +36,8 @@ typedef struct OrMesh OrMesh;
 
 /* Field order matches SGPU_Brush in include/sculpt_gpu.h. */
 typedef struct OrBrush {
-  int sculpt_tool; /* 1 draw, 2 smooth, 4 inflate, 18 clay strips (eBrushSculptTool) */
+  int sculpt_tool; /* 1 draw, 2 smooth, 3 pinch, 4 inflate, 16 crease, 18 clay strips
+                      (eBrushSculptTool) */
   int flag;        /* eBrushFlags subset: BRUSH_FRONTFACE (1 << 27) */
   int symmetry;    /* PAINT_SYMM_X | _Y | _Z */
   int curve_preset;
@@ -47,6 +48,7 @@ typedef struct OrBrush {
   float plane_offset;
   float view_normal[3];
   int use_original_bb;
+  float crease_pinch_factor;
 } OrBrush;
 
 /* ---- mesh (PBVH_FACES) ---- */

@@ -26,6 +26,8 @@
 #define OR_TOOL_SMOOTH 2
 #define OR_TOOL_INFLATE 4
 #define OR_TOOL_CLAY_STRIPS 18
+#define OR_TOOL_PINCH 3
+#define OR_TOOL_CREASE 16
 #define OR_BRUSH_FRONTFACE (1 << 27)
 
 #define OR_CM_TABLE 256

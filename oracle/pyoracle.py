@@ -26,7 +26,7 @@ class OrBrush(C.Structure):
                 ("curve_preset", C.c_int), ("radius", C.c_float), ("strength", C.c_float),
                 ("normal_radius_factor", C.c_float), ("area_radius_factor", C.c_float),
                 ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
-                ("use_original_bb", C.c_int)]
+                ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float)]
 
 
 class OrDrawSetup(C.Structure):
@@ -104,6 +104,7 @@ def make_brush(st) -> OrBrush:
     for k in range(3):
         b.view_normal[k] = st.view_normal[k]
     b.use_original_bb = st.use_original_bb
+    b.crease_pinch_factor = st.crease_pinch_factor
     return b
 
 

@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 # strokes, so the bound here is 2e-6 (FACES strokes stay under 1e-6).
 FP64_TOL_GRIDS = 2e-6
 
-TOOLS = [synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS]
+TOOLS = [synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS,
+         synth.TOOL_PINCH, synth.TOOL_CREASE]
 
 
 def small_torus(level=4):

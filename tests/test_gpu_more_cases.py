@@ -14,7 +14,9 @@ from helpers import bits_equal, first_diff, material_grid, ngon_mesh, rel_err, s
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-6
-TOOLS = (synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS)
+FP64_TOL_PINCHING = 2e-6  # pinch / crease: FP32 drift of the centre pull (GPU = FP32 exactly)
+TOOLS = (synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS,
+         synth.TOOL_PINCH, synth.TOOL_CREASE)
 
 
 def _pair(oracle, m, ll):
@@ -32,7 +34,9 @@ def _check(g, o, st, mode, tools=None, what=""):
     assert bits_equal(g.normals(), o.no()), what + " no " + first_diff(g.normals(), o.no())
     for a, b in zip(g.bbs(), o.bbs()):
         assert bits_equal(a, b), what + " bb " + first_diff(a, b)
-    assert rel_err(g.positions(), o.co64()) < FP64_TOL, what
+    pinching = (st.tool in (synth.TOOL_PINCH, synth.TOOL_CREASE) or
+                (tools is not None and np.isin(tools, (synth.TOOL_PINCH, synth.TOOL_CREASE)).any()))
+    assert rel_err(g.positions(), o.co64()) < (FP64_TOL_PINCHING if pinching else FP64_TOL), what
     return tot
 
 
@@ -50,7 +54,7 @@ def test_ngon_mesh_strokes(gpu, oracle, tool, mode):
 def test_material_split_mesh(gpu, oracle, mode):
     m = material_grid(64)
     g, o = _pair(oracle, m, 500)
-    tools = np.array([TOOLS[d % 4] for d in range(20)], dtype=np.int32)
+    tools = np.array([TOOLS[d % len(TOOLS)] for d in range(20)], dtype=np.int32)
     st = synth.Stroke(synth.TOOL_DRAW, 0.1, 0.6, synth.CURVE_SMOOTH, 0,
                       synth.line_dabs(synth.SEED_BASE + 4, 20))
     assert _check(g, o, st, mode, tools, "materials") > 0

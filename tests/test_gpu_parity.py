@@ -17,6 +17,15 @@ from helpers import bits_equal, first_diff, rel_err, small_grid, small_icosphere
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-6  # positions vs the FP64 oracle, norm-wise relative
+# Pinch and crease pull every vertex toward the centre by a fraction of its
+# offset; FP32 rounding of that offset (and of the area normal it is projected
+# on) drifts up to ~1.3e-6 from FP64 over these strokes.  The GPU still equals
+# the FP32 restatement bit for bit.
+FP64_TOL_PINCHING = 2e-6
+
+
+def fp64_tol(tool: int) -> float:
+    return FP64_TOL_PINCHING if tool in (synth.TOOL_PINCH, synth.TOOL_CREASE) else FP64_TOL
 
 
 def _cases():
@@ -81,7 +90,8 @@ def test_search_matches_oracle(gpu, oracle, case):
     assert g.search_gather_sphere([50, 50, 50], 0.01).size == 0
 
 
-TOOLS = [synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS]
+TOOLS = [synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE, synth.TOOL_CLAY_STRIPS,
+         synth.TOOL_PINCH, synth.TOOL_CREASE]
 
 
 @pytest.mark.parametrize("tool", TOOLS)
@@ -153,7 +163,7 @@ def test_stroke_parity(gpu, oracle, case, tool, mode):
     tot, _ = o.stroke(st, which=3)
     assert stats.verts_displaced == tot
     _assert_state_equal(g, o, f"{name} tool {tool} mode {mode}")
-    assert rel_err(g.positions(), o.co64()) < FP64_TOL
+    assert rel_err(g.positions(), o.co64()) < fp64_tol(tool)
     assert stats.kernel_launches > 0
     if mode == STROKE_GRAPH:
         # replaying the cached graph reproduces the eager result of a second stroke

@@ -6,7 +6,7 @@ reference's own code: curve-table end points of the presets
 (colortools.c:298-316), flat-grid normals, radial sphere normals, the
 bounding-box union invariant of the build (pbvh.c:2240-2247, 3287-3317), the
 DFS search order (pbvh.c:2664-2705), an analytic draw displacement on a flat
-grid, and a zero-strength no-op.
+grid (draw, pinch, crease), and a zero-strength no-op.
 """
 import math
 
@@ -154,12 +154,61 @@ def test_flat_grid_draw_analytic(oracle):
     assert tot == int(np.count_nonzero(fall > 0))
 
 
+def _flat_fall(oracle, co0, c, r):
+    d = np.linalg.norm(co0 - c, axis=1)
+    t, _ = oracle.curve_table(synth.CURVE_SMOOTH)
+    fi = d / r * 256.0
+    i = np.minimum(fi.astype(int), 255)
+    f = fi - i
+    fall = np.where(d < r, (1 - f) * t[i, 1] + f * t[np.minimum(i + 1, 256), 1], 0.0)
+    return np.clip(fall, 0, 1)
+
+
+def test_flat_grid_pinch_analytic(oracle):
+    """Pinch on a flat +Z grid with the stroke along +X: the side axis is
+    z x delta = +Y, so each vertex within the radius moves along y toward the
+    brush centre by strength * falloff of its offset; x and z stay put."""
+    m = small_grid(64)
+    st = synth.Stroke(synth.TOOL_PINCH, 0.1, 0.5, synth.CURVE_SMOOTH, 0,
+                      np.array([[0.5, 0.5, 0.0, 1.0, 0.0, 0.0]], dtype=np.float32))
+    om = oracle.OracleMesh.faces(m, 400)
+    om.recalc_all_normals()
+    co0 = om.co().astype(np.float64)
+    tot, _ = om.stroke(st, which=3)
+    co = om.co64()
+    fall = _flat_fall(oracle, co0, [0.5, 0.5, 0.0], 0.1)
+    assert np.abs(co[:, [0, 2]] - co0[:, [0, 2]]).max() == 0.0
+    assert np.abs(co[:, 1] - (co0[:, 1] + (0.5 - co0[:, 1]) * 0.5 * fall)).max() < 1e-6
+    assert tot == int(np.count_nonzero(fall > 0))
+
+
+def test_flat_grid_crease_analytic(oracle):
+    """Crease on a flat +Z grid: the draw offset along z (radius * strength *
+    falloff) plus an in-plane pull toward the centre by
+    crease_pinch_factor^2 * strength * falloff."""
+    m = small_grid(64)
+    st = synth.Stroke(synth.TOOL_CREASE, 0.1, 0.5, synth.CURVE_SMOOTH, 0,
+                      np.array([[0.5, 0.5, 0.0, 0.0, 1.0, 0.0]], dtype=np.float32),
+                      crease_pinch_factor=0.6)
+    om = oracle.OracleMesh.faces(m, 400)
+    om.recalc_all_normals()
+    co0 = om.co().astype(np.float64)
+    om.stroke(st, which=3)
+    co = om.co64()
+    fall = _flat_fall(oracle, co0, [0.5, 0.5, 0.0], 0.1)
+    k = 0.36 * 0.5 * fall
+    assert np.abs(co[:, 0] - (co0[:, 0] + (0.5 - co0[:, 0]) * k)).max() < 1e-6
+    assert np.abs(co[:, 1] - (co0[:, 1] + (0.5 - co0[:, 1]) * k)).max() < 1e-6
+    assert np.abs(co[:, 2] - 0.1 * 0.5 * fall).max() < 1e-6
+
+
 def test_zero_strength_is_noop(oracle):
     m = small_icosphere(3)
     om = oracle.OracleMesh.faces(m, 150)
     om.recalc_all_normals()
     co0 = om.co().copy()
-    for tool in (synth.TOOL_DRAW, synth.TOOL_INFLATE, synth.TOOL_SMOOTH, synth.TOOL_CLAY_STRIPS):
+    for tool in (synth.TOOL_DRAW, synth.TOOL_INFLATE, synth.TOOL_SMOOTH, synth.TOOL_CLAY_STRIPS,
+                 synth.TOOL_PINCH, synth.TOOL_CREASE):
         st = synth.Stroke(tool, 0.2, 0.0, synth.CURVE_SMOOTH, synth.SYMM_X,
                           synth.arc_dabs(1, 4, 0.05))
         om.stroke(st, which=1)

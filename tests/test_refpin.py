@@ -175,6 +175,8 @@ REPLAY = [
     ("uvsphere", synth.TOOL_CLAY_STRIPS, 0.1, 0.8, synth.CURVE_SHARP, synth.SYMM_X),
     ("icosphere", synth.TOOL_INFLATE, 0.1, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X),
     ("ngon", synth.TOOL_DRAW, 0.06, 0.9, synth.CURVE_SHARP, synth.SYMM_X),
+    ("icosphere", synth.TOOL_PINCH, 0.1, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X),
+    ("uvsphere", synth.TOOL_CREASE, 0.1, 0.7, synth.CURVE_SHARP, synth.SYMM_X),
 ]
 
 
