@@ -116,6 +116,8 @@ struct sgpu_mesh {
   // the captured call (copies in, kernels, copies out) for (rays, original)
   cudaGraphExec_t ray_graph = nullptr;
   int ray_graph_n = -1, ray_graph_orig = -1;
+  // stroke-start positions and normals stored (grab, elastic deform)
+  bool orig_stored = false;
   // headless draw buffers (sgpu_draw_buffers_build): host layout, device view
   // and its allocations
   DrawLayout draw;
@@ -375,6 +377,7 @@ bool make_brush(const SGPU_Brush* b, int tool, DevBrush* out) {
   out->area_radius_factor = b->area_radius_factor;
   out->plane_offset = b->plane_offset;
   out->crease_pinch_factor = b->crease_pinch_factor;
+  out->elastic_type = b->elastic_deform_type;
   out->x_first = c.x_first;
   out->x_last = c.x_last;
   out->mintable = c.mintable;
@@ -385,7 +388,67 @@ bool make_brush(const SGPU_Brush* b, int tool, DevBrush* out) {
 
 bool tool_ok(int tool) {
   return tool == kToolDraw || tool == kToolSmooth || tool == kToolInflate ||
-         tool == kToolClayStrips || tool == kToolPinch || tool == kToolCrease;
+         tool == kToolClayStrips || tool == kToolPinch || tool == kToolCrease ||
+         tool == kToolGrab || tool == kToolElasticDeform;
+}
+
+bool stroke_has_original(const SGPU_Brush* brush, const int* dab_tools, int ndabs) {
+  for (int d = 0; d < ndabs; d++)
+    if (uses_original(dab_tools ? dab_tools[d] : brush->sculpt_tool)) return true;
+  return false;
+}
+
+// Device buffers of the stroke-start positions and normals (allocated once,
+// outside any stream capture).
+int ensure_original(sgpu_mesh* m) {
+  if (m->dev.orig_co) return SGPU_OK;
+  float4 *a = nullptr, *b = nullptr;
+  int rc;
+  if ((rc = m->alloc(&a, m->dev.totvert)) || (rc = m->alloc(&b, m->dev.totvert))) return rc;
+  m->dev.orig_co = a;
+  m->dev.orig_no = b;
+  return SGPU_OK;
+}
+
+// The undo push of the stroke start: positions and normals kept as originals
+// (stream-ordered, capturable).
+int copy_original(sgpu_mesh* m) {
+  const size_t bytes = sizeof(float4) * m->dev.totvert;
+  CK(cudaMemcpyAsync(m->dev.orig_co, m->dev.co, bytes, cudaMemcpyDeviceToDevice, m->stream),
+     "copy original positions");
+  CK(cudaMemcpyAsync(m->dev.orig_no, m->dev.no, bytes, cudaMemcpyDeviceToDevice, m->stream),
+     "copy original normals");
+  m->orig_stored = true;
+  return SGPU_OK;
+}
+
+// The symmetry passes of one dab.
+DabPasses dab_passes(const SGPU_Brush* brush, const float loc[3], const float delta[3]) {
+  DabPasses dp{};
+  for (int pass = 0; pass < 8; pass++) {
+    if ((pass & ~brush->symmetry) != 0) continue;
+    for (int k = 0; k < 3; k++) {
+      const float sgn = (pass & (1 << k)) ? -1.0f : 1.0f;
+      dp.loc[dp.npass][k] = sgn * loc[k];
+      dp.delta[dp.npass][k] = sgn * delta[k];
+      dp.view[dp.npass][k] = sgn * brush->view_normal[k];
+    }
+    dp.npass++;
+  }
+  return dp;
+}
+
+// BKE_kelvinlet_init_params (kelvinlet.c:6-21) with shear modulus 1 and the
+// force |grab_delta| * strength (the mouse-direction sign taken as +1).
+void kelvinlet_params(DevBrush* b, const float delta[3], float poisson) {
+  const float len = sqrtf(delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2]);
+  b->kl_a = 1.0f / (4.0f * 3.14159265358979323846f * 1.0f);
+  b->kl_b = b->kl_a / (4.0f * (1.0f - poisson));
+  b->kl_c = 2.0f * (3.0f * b->kl_a - 2.0f * b->kl_b);
+  b->kl_f = len * b->strength;
+  b->kl_rs[0] = b->radius * 1.0f;
+  b->kl_rs[1] = b->kl_rs[0] * 2.0f;
+  b->kl_rs[2] = b->kl_rs[1] * 2.0f;
 }
 
 // Launch bookkeeping: counts launches and, while profiling, brackets each one
@@ -446,6 +509,19 @@ int launch_tool(Launcher& L, const DevBrush& b, PassParams pp) {
   return SGPU_OK;
 }
 
+// One dab of grab / elastic deform: the union gather, then the dab.
+int launch_orig_tool(Launcher& L, DevBrush b, const SGPU_Brush* brush, const float loc[3],
+                     const float delta[3]) {
+  const DevMesh& d = L.m->dev;
+  cudaStream_t s = L.m->stream;
+  const DabPasses dp = dab_passes(brush, loc, delta);
+  const bool elastic = b.tool == kToolElasticDeform;
+  if (elastic) kelvinlet_params(&b, delta, brush->elastic_deform_volume_preservation);
+  LAUNCH(L, kKCull, "cull kernel", launch_cull_dab(d, dp, b.radius * b.radius, elastic ? 1 : 0, s));
+  LAUNCH(L, kKBrush, "brush kernel", launch_orig_dab(d, b, dp, s));
+  return SGPU_OK;
+}
+
 int launch_update_normals(Launcher& L, int bounds_flag) {
   const DevMesh& d = L.m->dev;
   cudaStream_t s = L.m->stream;
@@ -470,9 +546,19 @@ int enqueue_stroke(Launcher& L, const SGPU_Brush* brush, const SGPU_Dab* dabs, i
     return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brush->curve_preset);
   CK(cudaMemsetAsync(&m->dev.work->displaced, 0, sizeof(unsigned long long), m->stream),
      "reset counter");
+  if (stroke_has_original(brush, dab_tools, ndabs)) {
+    const int rc = copy_original(m);
+    if (rc) return rc;
+  }
   for (int d = 0; d < ndabs; d++) {
     const int tool = dab_tools ? dab_tools[d] : brush->sculpt_tool;
     base.tool = tool;
+    if (uses_original(tool)) {
+      int rc = launch_orig_tool(L, base, brush, dabs[d].location, dabs[d].grab_delta);
+      if (rc) return rc;
+      if ((rc = launch_update_normals(L, kUpdateBB))) return rc;
+      continue;
+    }
     const float scale = (tool == kToolClayStrips) ? 1.41421356237309504880f : 1.0f;
     const float r = brush->radius * scale;
     for (int pass = 0; pass < 8; pass++) {
@@ -540,10 +626,22 @@ int do_brush_tool(sgpu_mesh* m, const SGPU_Brush* brush, int tool, const float l
   if (!brush || !location || !grab_delta) return fail(SGPU_ERR_INVALID_ARG, "NULL argument");
   if (!tool_ok(tool)) return fail(SGPU_ERR_INVALID_ARG, "unsupported sculpt tool %d", tool);
   if (!(brush->radius > 0.0f)) return fail(SGPU_ERR_INVALID_ARG, "radius must be positive");
+  if (uses_original(tool)) {
+    if (nodes) return fail(SGPU_ERR_INVALID_ARG, "grab / elastic deform gather their own leaves");
+    if (!m->orig_stored)
+      return fail(SGPU_ERR_INVALID_ARG, "no stroke-start positions (sgpu_mesh_store_original)");
+    if (brush->elastic_deform_type < 0 || brush->elastic_deform_type > 4)
+      return fail(SGPU_ERR_INVALID_ARG, "elastic deform type out of range");
+  }
   if (nodes && (rc = upload_node_list(m, nodes, totnode))) return rc;
   DevBrush b;
   if (!make_brush(brush, tool, &b))
     return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brush->curve_preset);
+  if (uses_original(tool)) {
+    Launcher L{m};
+    if ((rc = launch_orig_tool(L, b, brush, location, grab_delta))) return rc;
+    return device_err(m);
+  }
   PassParams pp{};
   for (int k = 0; k < 3; k++) {
     pp.loc[k] = location[k];
@@ -967,6 +1065,22 @@ int sgpu_do_crease_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float l
                          const float grab_delta[3], const int* nodes, int totnode) {
   return do_brush_tool(mesh, brush, kToolCrease, location, grab_delta, nodes, totnode);
 }
+int sgpu_do_grab_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                       const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolGrab, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_elastic_deform_brush(sgpu_mesh* mesh, const SGPU_Brush* brush,
+                                 const float location[3], const float grab_delta[3],
+                                 const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolElasticDeform, location, grab_delta, nodes, totnode);
+}
+int sgpu_mesh_store_original(sgpu_mesh* mesh) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if ((rc = ensure_original(mesh)) || (rc = copy_original(mesh))) return rc;
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  return SGPU_OK;
+}
 int sgpu_do_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
                   const float grab_delta[3], const int* nodes, int totnode) {
   if (!brush) return fail(SGPU_ERR_INVALID_ARG, "brush is NULL");
@@ -1010,6 +1124,9 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   if (brush->symmetry < 0 || brush->symmetry > 7)
     return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
+  // the persistent kernel has no original-data brushes: such strokes take the graph path
+  if (mode == SGPU_STROKE_TEAM && stroke_has_original(brush, dab_tools, ndabs))
+    mode = SGPU_STROKE_GRAPH;
   if (mode == SGPU_STROKE_TEAM) {
     const int offs[2] = {0, ndabs};
     sgpu_mesh* one[1] = {mesh};
@@ -1388,6 +1505,7 @@ namespace {
 int run_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
                const int* dab_tools, int mode, int* launches_out) {
   int rc;
+  if (stroke_has_original(brush, dab_tools, ndabs) && (rc = ensure_original(mesh))) return rc;
   Launcher L{mesh};
   int& launches = *launches_out;
   if (mode == SGPU_STROKE_GRAPH) {
@@ -1646,6 +1764,10 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
                const int* offs, const int* tools, int cluster, cudaStream_t s,
                SGPU_StrokeStats* stats, float* total_ms, bool wait) {
   sgpu_mesh* m0 = meshes[0];
+  for (int i = 0; i < n; i++)
+    if (stroke_has_original(&brushes[i], tools ? tools + offs[i] : nullptr, offs[i + 1] - offs[i]))
+      return fail(SGPU_ERR_UNSUPPORTED,
+                  "grab and elastic deform do not run in the persistent stroke kernel");
   int max_nodes = 0, max_leaves = 0;
   for (int i = 0; i < n; i++) {
     max_nodes = std::max(max_nodes, meshes[i]->dev.totnode);

@@ -55,6 +55,8 @@ struct DevMesh {
   int nlevels;
   float4* co;  // FACES: the MVert bytes (xyz + flag/bweight/pad in w); GRIDS: xyz, 0
   float4* no;
+  float4* orig_co;  // stroke-start positions and normals (grab, elastic deform); may be null
+  float4* orig_no;
   float* mask;      // nullable
   const float* automask;  // nullable
   // FACES topology
@@ -162,6 +164,9 @@ struct DevBrush {
   float area_radius_factor;
   float plane_offset;
   float crease_pinch_factor;
+  int elastic_type;                   // BRUSH_ELASTIC_DEFORM_*
+  float kl_a, kl_b, kl_c, kl_f;       // BKE_kelvinlet_init_params of the dab
+  float kl_rs[3];
   float x_first, x_last;
   float mintable, range;
   float y[kCurveTable + 1];
@@ -180,8 +185,19 @@ struct PassParams {
 };
 
 constexpr int kBrushFrontFace = 1 << 27;
-constexpr int kToolDraw = 1, kToolSmooth = 2, kToolPinch = 3, kToolInflate = 4, kToolCrease = 16,
-              kToolClayStrips = 18;
+constexpr int kToolDraw = 1, kToolSmooth = 2, kToolPinch = 3, kToolInflate = 4, kToolGrab = 5,
+              kToolCrease = 16, kToolClayStrips = 18, kToolElasticDeform = 21;
+// Tools that rebuild positions from the stroke-start ones (one dab, all passes).
+__host__ __device__ __forceinline__ bool uses_original(int tool) {
+  return tool == kToolGrab || tool == kToolElasticDeform;
+}
+// The symmetry passes of one dab (mirrored location, grab delta, view normal).
+struct DabPasses {
+  int npass;
+  float loc[8][3];
+  float delta[8][3];
+  float view[8][3];
+};
 // Tools that reduce the area normal (and centre) before their sweep.
 __host__ __device__ __forceinline__ bool uses_area(int tool) {
   return tool == kToolDraw || tool == kToolClayStrips || tool == kToolPinch || tool == kToolCrease;

@@ -11,6 +11,11 @@ namespace sgpu {
 
 cudaError_t launch_cull(const DevMesh& m, const PassParams& pp, cudaStream_t s);
 cudaError_t launch_set_list(const DevMesh& m, const int* dev_nodes, int totnode, cudaStream_t s);
+// Grab / elastic deform: the union gather of a dab's passes, then the dab.
+cudaError_t launch_cull_dab(const DevMesh& m, const DabPasses& dp, float radius_sq, int all,
+                            cudaStream_t s);
+cudaError_t launch_orig_dab(const DevMesh& m, const DevBrush& b, const DabPasses& dp,
+                            cudaStream_t s);
 cudaError_t launch_area(const DevMesh& m, const DevBrush& b, const PassParams& pp,
                         cudaStream_t s);
 cudaError_t launch_brush(const DevMesh& m, const DevBrush& b, const PassParams& pp,

@@ -41,7 +41,9 @@ class SGPU_Brush(C.Structure):
                 ("curve_preset", C.c_int), ("radius", C.c_float), ("strength", C.c_float),
                 ("normal_radius_factor", C.c_float), ("area_radius_factor", C.c_float),
                 ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
-                ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float)]
+                ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float),
+                ("elastic_deform_type", C.c_int),
+                ("elastic_deform_volume_preservation", C.c_float)]
 
 
 class SGPU_MeshInfo(C.Structure):
@@ -77,7 +79,8 @@ EXPORTS = (
     "sgpu_mesh_create_grids", "sgpu_mesh_destroy", "sgpu_mesh_info", "sgpu_mesh_sync",
     "sgpu_mesh_stream", "sgpu_search_sphere", "sgpu_do_draw_brush", "sgpu_do_smooth_brush",
     "sgpu_do_inflate_brush", "sgpu_do_clay_strips_brush", "sgpu_do_brush",
-    "sgpu_do_pinch_brush", "sgpu_do_crease_brush",
+    "sgpu_do_pinch_brush", "sgpu_do_crease_brush", "sgpu_do_grab_brush",
+    "sgpu_do_elastic_deform_brush", "sgpu_mesh_store_original",
     "sgpu_pbvh_update_normals", "sgpu_pbvh_update_bounds", "sgpu_pbvh_node_mark_update",
     "sgpu_stroke", "sgpu_get_verts", "sgpu_set_verts", "sgpu_get_positions",
     "sgpu_set_positions", "sgpu_get_normals", "sgpu_get_mask", "sgpu_get_node_bbs",
@@ -132,7 +135,7 @@ def load(path: str | None = None):
     L.sgpu_raycast.argtypes = [vp, i, vp, vp, vp, i, vp, vp, vp, vp, vp]
     for name in ("sgpu_do_draw_brush", "sgpu_do_smooth_brush", "sgpu_do_inflate_brush",
                  "sgpu_do_clay_strips_brush", "sgpu_do_brush", "sgpu_do_pinch_brush",
-                 "sgpu_do_crease_brush"):
+                 "sgpu_do_crease_brush", "sgpu_do_grab_brush", "sgpu_do_elastic_deform_brush"):
         getattr(L, name).argtypes = [vp, C.POINTER(SGPU_Brush), vp, vp, vp, i]
     L.sgpu_pbvh_update_normals.argtypes = [vp]
     L.sgpu_pbvh_update_bounds.argtypes = [vp, i]
@@ -163,6 +166,7 @@ def load(path: str | None = None):
     L.sgpu_mesh_get_team.argtypes = [vp, vp]
     L.sgpu_autotune_team.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp]
     L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
+    L.sgpu_mesh_store_original.argtypes = [vp]
     L.sgpu_draw_buffers_build.argtypes = [vp, C.POINTER(SGPU_DrawSetup)]
     L.sgpu_draw_buffers_update.argtypes = [vp]
     L.sgpu_draw_buffers_update_timed.argtypes = [vp, i, vp]
@@ -240,6 +244,8 @@ def make_brush(st) -> SGPU_Brush:
         b.view_normal[k] = st.view_normal[k]
     b.use_original_bb = st.use_original_bb
     b.crease_pinch_factor = st.crease_pinch_factor
+    b.elastic_deform_type = st.elastic_deform_type
+    b.elastic_deform_volume_preservation = st.elastic_deform_volume_preservation
     return b
 
 
@@ -437,6 +443,16 @@ class PBVH:
 
     def do_crease_brush(self, st, location, grab_delta, nodes=None):
         self._brush("sgpu_do_crease_brush", st, location, grab_delta, nodes)
+
+    def do_grab_brush(self, st, location, grab_delta):
+        """One dab over all symmetry passes (the library gathers the leaves)."""
+        self._brush("sgpu_do_grab_brush", st, location, grab_delta, None)
+
+    def do_elastic_deform_brush(self, st, location, grab_delta):
+        self._brush("sgpu_do_elastic_deform_brush", st, location, grab_delta, None)
+
+    def store_original(self):
+        _check(load().sgpu_mesh_store_original(self._h))
 
     def do_brush(self, st, location, grab_delta, nodes=None):
         self._brush("sgpu_do_brush", st, location, grab_delta, nodes)

@@ -206,10 +206,13 @@ class Stroke:
     view_normal: tuple = (0.0, 0.0, 1.0)
     use_original_bb: int = 0
     crease_pinch_factor: float = 0.5  # types_brush_defaults.h:23
+    elastic_deform_type: int = 0      # BRUSH_ELASTIC_DEFORM_GRAB
+    elastic_deform_volume_preservation: float = 0.4
 
 
 TOOL_DRAW, TOOL_SMOOTH, TOOL_INFLATE, TOOL_CLAY_STRIPS = 1, 2, 4, 18
 TOOL_PINCH, TOOL_CREASE = 3, 16
+TOOL_GRAB, TOOL_ELASTIC_DEFORM = 5, 21
 CURVE_SHARP, CURVE_SMOOTH = 1, 2
 SYMM_X = 1
 
@@ -241,6 +244,20 @@ def arc_dabs(seed: int, n: int, step: float, surf_radius: float = 1.0) -> np.nda
     ang = step * np.arange(n)[:, None]
     pts = (np.cos(ang) * p0 + np.sin(ang) * q) * surf_radius
     return _dabs_from_points(pts)
+
+
+def grab_dabs(seed: int, n: int, step: float, surf_radius: float = 1.0) -> np.ndarray:
+    """A grab stroke: the location stays at the anchor on a sphere of
+    surf_radius, the grab delta grows by step per dab along a seeded
+    direction (the reference's grab keeps the stroke's first location and
+    accumulates the delta)."""
+    g = gaussian(seed, 10, 6)
+    p = g[:3] / np.linalg.norm(g[:3]) * surf_radius
+    d = g[3:] / np.linalg.norm(g[3:])
+    out = np.zeros((n, 6), dtype=np.float64)
+    out[:, :3] = p
+    out[:, 3:] = d[None, :] * (step * (np.arange(n)[:, None] + 1))
+    return _f32(out)
 
 
 # ---------------------------------------------------------------------------

@@ -78,8 +78,16 @@ typedef struct SGPU_MLoopTri { /* MLoopTri, types_meshdata.h:178-181 */
 #define SGPU_TOOL_SMOOTH 2       /* SCULPT_TOOL_SMOOTH */
 #define SGPU_TOOL_PINCH 3        /* SCULPT_TOOL_PINCH */
 #define SGPU_TOOL_INFLATE 4      /* SCULPT_TOOL_INFLATE */
+#define SGPU_TOOL_GRAB 5         /* SCULPT_TOOL_GRAB */
 #define SGPU_TOOL_CREASE 16      /* SCULPT_TOOL_CREASE */
 #define SGPU_TOOL_CLAY_STRIPS 18 /* SCULPT_TOOL_CLAY_STRIPS */
+#define SGPU_TOOL_ELASTIC_DEFORM 21 /* SCULPT_TOOL_ELASTIC_DEFORM (Kelvinlets, kelvinlet.c) */
+/* Brush.elastic_deform_type (types_brush_enums.h:195-199) */
+#define SGPU_ELASTIC_DEFORM_GRAB 0
+#define SGPU_ELASTIC_DEFORM_GRAB_BISCALE 1
+#define SGPU_ELASTIC_DEFORM_GRAB_TRISCALE 2
+#define SGPU_ELASTIC_DEFORM_SCALE 3
+#define SGPU_ELASTIC_DEFORM_TWIST 4
 #define SGPU_BRUSH_FRONTFACE (1 << 27)
 #define SGPU_SYMM_X 1 /* PAINT_SYMM_X, types_scene.h:2174 */
 #define SGPU_SYMM_Y 2
@@ -104,6 +112,8 @@ typedef struct SGPU_Brush {
   float view_normal[3];       /* front-face reference direction */
   int use_original_bb;        /* cull against orig_vb instead of vb */
   float crease_pinch_factor;  /* crease: pinch strength (default 0.5, types_brush_defaults.h:23) */
+  int elastic_deform_type;    /* SGPU_ELASTIC_DEFORM_* */
+  float elastic_deform_volume_preservation; /* Kelvinlet Poisson ratio, in [0, 1) */
 } SGPU_Brush;
 
 /* One dab of a stroke: location and grab delta (stroke direction). */
@@ -193,6 +203,22 @@ int sgpu_do_pinch_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float lo
                         const float grab_delta[3], const int *nodes, int totnode);
 int sgpu_do_crease_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
                          const float grab_delta[3], const int *nodes, int totnode);
+/* Original-data brushes (grab, elastic deform): one DAB over all symmetry
+ * passes of brush->symmetry, from the unmirrored location and grab delta — the
+ * reference combines these brushes' proxies once per dab onto the original
+ * coordinates, so every vertex of the gathered leaves is rebuilt from its
+ * stroke-start position.  The library gathers the leaves itself (grab: leaves
+ * whose orig_vb meets any pass sphere; elastic deform: every leaf, as
+ * SCULPT_tool_needs_all_pbvh_nodes has it): nodes must be NULL.  Needs
+ * sgpu_mesh_store_original at the stroke start (the undo push that keeps
+ * the original coordinates); sgpu_stroke stores them itself. */
+int sgpu_do_grab_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                       const float grab_delta[3], const int *nodes, int totnode);
+int sgpu_do_elastic_deform_brush(sgpu_mesh *mesh, const SGPU_Brush *brush,
+                                 const float location[3], const float grab_delta[3],
+                                 const int *nodes, int totnode);
+/* Copies the current positions and normals as the stroke-start ones. */
+int sgpu_mesh_store_original(sgpu_mesh *mesh);
 /* Dispatch on brush->sculpt_tool. */
 int sgpu_do_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
                   const float grab_delta[3], const int *nodes, int totnode);

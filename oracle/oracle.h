@@ -49,6 +49,8 @@ typedef struct OrBrush {
   float view_normal[3];
   int use_original_bb;
   float crease_pinch_factor;
+  int elastic_deform_type;                /* BRUSH_ELASTIC_DEFORM_* */
+  float elastic_deform_volume_preservation; /* Kelvinlet Poisson ratio */
 } OrBrush;
 
 /* ---- mesh (PBVH_FACES) ---- */
@@ -67,6 +69,19 @@ OrMesh *or_mesh_create_grids(int num_grids, int grid_size, const float *grids_co
                              const int *face_start, const int *face_ngrids, const int *face_verts,
                              const int *face_edges, int num_base_verts, int num_base_edges,
                              const int *edge_verts, int leaf_limit);
+
+/* The stroke-start positions and normals that grab and elastic deform read
+ * (the undo node's original coordinates); or_stroke stores them itself at the
+ * start of a stroke that uses one of those tools. */
+void or_store_original(OrMesh *m);
+/* One dab of grab / elastic deform over all symmetry passes (b->symmetry) of
+ * the unmirrored location and grab delta; the leaves come from the library's
+ * own gather.  Returns vertex-passes displaced (FP32 state). */
+int or_orig_dab(OrMesh *m, const OrBrush *b, const float location[3], const float grab_delta[3]);
+/* The Kelvinlet displacement (kelvinlet.c:6-190) of one element, FP32:
+ * params from BKE_kelvinlet_init_params(radius, force, 1, poisson); type 0-4. */
+void or_kelvinlet(int type, float radius, float force, float poisson, const float co[3],
+                  const float location[3], const float delta_or_normal[3], float out[3]);
 
 int or_num_nodes(const OrMesh *m);
 int or_num_leaves(const OrMesh *m);

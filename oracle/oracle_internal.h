@@ -28,6 +28,14 @@
 #define OR_TOOL_CLAY_STRIPS 18
 #define OR_TOOL_PINCH 3
 #define OR_TOOL_CREASE 16
+#define OR_TOOL_GRAB 5
+#define OR_TOOL_ELASTIC_DEFORM 21
+/* eBrushElasticDeformType (types_brush_enums.h:195-199) */
+#define OR_ELASTIC_GRAB 0
+#define OR_ELASTIC_GRAB_BISCALE 1
+#define OR_ELASTIC_GRAB_TRISCALE 2
+#define OR_ELASTIC_SCALE 3
+#define OR_ELASTIC_TWIST 4
 #define OR_BRUSH_FRONTFACE (1 << 27)
 
 #define OR_CM_TABLE 256
@@ -49,13 +57,15 @@ typedef struct OrCurve {
 } OrCurve;
 
 typedef struct OrStateF {
-  float *co, *no, *mask; /* 3V, 3V, V (mask may be NULL) */
-  float *vb, *orig_vb;   /* 6N */
+  float *co, *no, *mask;     /* 3V, 3V, V (mask may be NULL) */
+  float *vb, *orig_vb;       /* 6N */
+  float *orig_co, *orig_no;  /* 3V each: positions / normals at the stroke start */
 } OrStateF;
 
 typedef struct OrStateD {
   double *co, *no, *mask;
   double *vb, *orig_vb;
+  double *orig_co, *orig_no;
 } OrStateD;
 
 struct OrMesh {

@@ -119,6 +119,33 @@ int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
   return total;
 }
 
+void or_store_original(OrMesh *m)
+{
+  store_original_f(m, &m->sf);
+  store_original_d(m, &m->sd);
+}
+
+int or_orig_dab(OrMesh *m, const OrBrush *b, const float location[3], const float grab_delta[3])
+{
+  OrCurve cu;
+  or_curve_build(b->curve_preset, &cu);
+  if (!m->sf.orig_co) {
+    store_original_f(m, &m->sf);
+  }
+  int *nodes = (int *)malloc(sizeof(int) * (m->totnode + 1));
+  const int64_t n = orig_dab_full_f(m, &m->sf, &cu, b, location, grab_delta, nodes);
+  free(nodes);
+  return (int)n;
+}
+
+void or_kelvinlet(int type, float radius, float force, float poisson, const float co[3],
+                  const float location[3], const float delta_or_normal[3], float out[3])
+{
+  Kelvinlet_f p;
+  kelvinlet_init_f(&p, radius, force, 1.0f, poisson);
+  kelvinlet_disp_f(type, &p, co, location, delta_or_normal, out);
+}
+
 float or_curve_strength(int preset, float dist, float radius)
 {
   OrCurve cu;

@@ -26,7 +26,9 @@ class OrBrush(C.Structure):
                 ("curve_preset", C.c_int), ("radius", C.c_float), ("strength", C.c_float),
                 ("normal_radius_factor", C.c_float), ("area_radius_factor", C.c_float),
                 ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
-                ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float)]
+                ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float),
+                ("elastic_deform_type", C.c_int),
+                ("elastic_deform_volume_preservation", C.c_float)]
 
 
 class OrDrawSetup(C.Structure):
@@ -74,6 +76,10 @@ def lib():
         L.or_draw_build.argtypes = [vp, C.POINTER(OrDrawSetup), vp, vp, vp, vp]
         L.or_draw_update.argtypes = [vp, C.POINTER(OrDrawSetup), vp, vp, vp]
         L.or_face_set_color.argtypes = [i, i, vp]
+        L.or_kelvinlet.argtypes = [i, f, f, f, vp, vp, vp, vp]
+        L.or_store_original.argtypes = [vp]
+        L.or_orig_dab.restype = i
+        L.or_orig_dab.argtypes = [vp, C.POINTER(OrBrush), vp, vp]
         L.or_raycast.restype = i
         L.or_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp, vp]
         L.or_grids_special_quads.restype = i
@@ -105,6 +111,8 @@ def make_brush(st) -> OrBrush:
         b.view_normal[k] = st.view_normal[k]
     b.use_original_bb = st.use_original_bb
     b.crease_pinch_factor = st.crease_pinch_factor
+    b.elastic_deform_type = st.elastic_deform_type
+    b.elastic_deform_volume_preservation = st.elastic_deform_volume_preservation
     return b
 
 
@@ -266,6 +274,16 @@ class OracleMesh:
     def update_bounds(self, flag: int):
         lib().or_update_bounds(self.h, flag)
 
+    def store_original(self):
+        lib().or_store_original(self.h)
+
+    def orig_dab(self, st, location, grab_delta) -> int:
+        """One dab of grab / elastic deform (all symmetry passes), FP32."""
+        b = make_brush(st)
+        loc = np.asarray(location, dtype=np.float32)
+        gd = np.asarray(grab_delta, dtype=np.float32)
+        return int(lib().or_orig_dab(self.h, C.byref(b), _p(loc), _p(gd)))
+
     def draw_build(self, face_sets=None, seed: int = 0, color_default: int = 1,
                    loop_colors=None, vert_colors=None, use_vert_colors: bool = False,
                    grid_flag_mats=None, vert_flag=None, lt_loops=None) -> dict:
@@ -336,6 +354,15 @@ class OracleMesh:
         tot = lib().or_stroke(self.h, C.byref(b), _p(d), d.shape[0], _p(tools), which, nthreads,
                               _p(per))
         return int(tot), per
+
+
+def kelvinlet(kind: int, radius: float, force: float, poisson: float, co, location, dn):
+    out = np.zeros(3, dtype=np.float32)
+    c = np.asarray(co, dtype=np.float32)
+    lo = np.asarray(location, dtype=np.float32)
+    d = np.asarray(dn, dtype=np.float32)
+    lib().or_kelvinlet(kind, radius, force, poisson, _p(c), _p(lo), _p(d), _p(out))
+    return out
 
 
 def face_set_color(face_set: int, seed: int) -> np.ndarray:

@@ -99,6 +99,7 @@ def lib():
         L.rp_draw_node_bytes.argtypes = [vp, i, vp]
         L.rp_draw_format.argtypes = [vp, vp]
         L.rp_face_set_color.argtypes = [i, i, vp]
+        L.rp_kelvinlet.argtypes = [i, f, f, f, vp, vp, vp, vp]
         L.rp_hash_int_01.restype = f
         L.rp_hash_int_01.argtypes = [C.c_uint]
         _lib = L
@@ -121,6 +122,16 @@ def draw_format():
 def face_set_color(face_set: int, seed: int) -> np.ndarray:
     out = np.zeros(3, dtype=np.uint8)
     lib().rp_face_set_color(face_set, seed, _p(out))
+    return out
+
+
+def kelvinlet(kind: int, radius: float, force: float, poisson: float, co, location, dn):
+    """The reference's Kelvinlet displacement (kelvinlet.c) of one element."""
+    out = np.zeros(3, dtype=np.float32)
+    c = np.asarray(co, dtype=np.float32)
+    lo = np.asarray(location, dtype=np.float32)
+    d = np.asarray(dn, dtype=np.float32)
+    lib().rp_kelvinlet(kind, radius, force, poisson, _p(c), _p(lo), _p(d), _p(out))
     return out
 
 

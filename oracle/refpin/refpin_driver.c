@@ -382,3 +382,32 @@ PBVH *rp_pbvh(RefPin *r)
 {
   return r->pbvh;
 }
+
+/* The reference's Kelvinlet displacement of one element (kelvinlet.c):
+ * BKE_kelvinlet_init_params(radius, force, 1, poisson), then type 0 grab,
+ * 1 grab_biscale, 2 grab_triscale (dn = brush delta), 3 scale, 4 twist
+ * (dn = surface normal). */
+#include "BKE_kelvinlet.h"
+void rp_kelvinlet(int type, float radius, float force, float poisson, const float co[3],
+                  const float location[3], const float dn[3], float out[3])
+{
+  KelvinletParams p;
+  BKE_kelvinlet_init_params(&p, radius, force, 1.0f, poisson);
+  switch (type) {
+    case 0:
+      BKE_kelvinlet_grab(out, &p, co, location, dn);
+      break;
+    case 1:
+      BKE_kelvinlet_grab_biscale(out, &p, co, location, dn);
+      break;
+    case 2:
+      BKE_kelvinlet_grab_triscale(out, &p, co, location, dn);
+      break;
+    case 3:
+      BKE_kelvinlet_scale(out, &p, co, location, dn);
+      break;
+    default:
+      BKE_kelvinlet_twist(out, &p, co, location, dn);
+      break;
+  }
+}

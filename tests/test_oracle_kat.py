@@ -202,6 +202,54 @@ def test_flat_grid_crease_analytic(oracle):
     assert np.abs(co[:, 2] - 0.1 * 0.5 * fall).max() < 1e-6
 
 
+def test_flat_grid_grab_analytic(oracle):
+    """Grab rebuilds each dab from the stroke-start positions: on a flat grid
+    every vertex within the radius of the anchor ends at
+    orig + delta_last * strength * falloff(|orig - anchor|), whatever the
+    earlier dabs did."""
+    m = small_grid(64)
+    d1 = [0.01, 0.0, 0.02]
+    d2 = [0.02, -0.01, 0.05]
+    dabs = np.array([[0.5, 0.5, 0.0] + d1, [0.5, 0.5, 0.0] + d2], dtype=np.float32)
+    st = synth.Stroke(synth.TOOL_GRAB, 0.1, 0.5, synth.CURVE_SMOOTH, 0, dabs)
+    om = oracle.OracleMesh.faces(m, 400)
+    om.recalc_all_normals()
+    co0 = om.co().astype(np.float64)
+    tot, per = om.stroke(st, which=3)
+    co = om.co64()
+    fall = _flat_fall(oracle, co0, [0.5, 0.5, 0.0], 0.1)
+    want = co0 + np.outer(0.5 * fall, np.asarray(d2, np.float32).astype(np.float64))
+    assert np.abs(co - want).max() < 1e-6
+    assert per[0] == per[1] == int(np.count_nonzero(fall > 0))
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4])
+def test_flat_grid_elastic_deform(oracle, kind):
+    """Elastic deform moves every vertex (all leaves) by the Kelvinlet
+    displacement of its stroke-start position (grab types scaled by
+    strength * 20); scale and twist about the +Z normal keep a flat grid flat."""
+    m = small_grid(32)
+    delta = [0.02, 0.01, 0.0] if kind >= 3 else [0.01, 0.0, 0.02]
+    dabs = np.array([[0.5, 0.5, 0.0] + delta], dtype=np.float32)
+    st = synth.Stroke(synth.TOOL_ELASTIC_DEFORM, 0.1, 0.5, synth.CURVE_SMOOTH, 0, dabs,
+                      view_normal=(0.0, 0.0, 1.0), elastic_deform_type=kind)
+    om = oracle.OracleMesh.faces(m, 100)
+    om.recalc_all_normals()
+    co0 = om.co().copy()
+    tot, _ = om.stroke(st, which=1)
+    co = om.co()
+    force = np.float32(np.float32(np.linalg.norm(np.asarray(delta, np.float32))) * np.float32(0.5))
+    dn = np.asarray(delta if kind <= 2 else st.view_normal, np.float32)
+    for v in range(0, co0.shape[0], 37):
+        k = oracle.kelvinlet(kind, 0.1, force, 0.4, co0[v], dabs[0, :3], dn)
+        if kind <= 2:
+            k = k * np.float32(np.float32(0.5) * np.float32(20.0))
+        assert np.array_equal((co0[v] + k).view(np.uint32), co[v].view(np.uint32)), v
+    assert tot == co0.shape[0] - 1 or tot == co0.shape[0]  # all but the centre may move
+    if kind >= 3:
+        assert np.abs(co[:, 2]).max() == 0.0
+
+
 def test_zero_strength_is_noop(oracle):
     m = small_icosphere(3)
     om = oracle.OracleMesh.faces(m, 150)
