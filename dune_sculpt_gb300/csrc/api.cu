@@ -378,6 +378,7 @@ bool make_brush(const SGPU_Brush* b, int tool, DevBrush* out) {
   out->plane_offset = b->plane_offset;
   out->crease_pinch_factor = b->crease_pinch_factor;
   out->elastic_type = b->elastic_deform_type;
+  out->height = b->height;
   out->x_first = c.x_first;
   out->x_last = c.x_last;
   out->mintable = c.mintable;
@@ -389,12 +390,12 @@ bool make_brush(const SGPU_Brush* b, int tool, DevBrush* out) {
 bool tool_ok(int tool) {
   return tool == kToolDraw || tool == kToolSmooth || tool == kToolInflate ||
          tool == kToolClayStrips || tool == kToolPinch || tool == kToolCrease ||
-         tool == kToolGrab || tool == kToolElasticDeform;
+         tool == kToolGrab || tool == kToolElasticDeform || tool == kToolLayer;
 }
 
 bool stroke_has_original(const SGPU_Brush* brush, const int* dab_tools, int ndabs) {
   for (int d = 0; d < ndabs; d++)
-    if (uses_original(dab_tools ? dab_tools[d] : brush->sculpt_tool)) return true;
+    if (needs_stroke_start(dab_tools ? dab_tools[d] : brush->sculpt_tool)) return true;
   return false;
 }
 
@@ -403,10 +404,14 @@ bool stroke_has_original(const SGPU_Brush* brush, const int* dab_tools, int ndab
 int ensure_original(sgpu_mesh* m) {
   if (m->dev.orig_co) return SGPU_OK;
   float4 *a = nullptr, *b = nullptr;
+  float* l = nullptr;
   int rc;
-  if ((rc = m->alloc(&a, m->dev.totvert)) || (rc = m->alloc(&b, m->dev.totvert))) return rc;
+  if ((rc = m->alloc(&a, m->dev.totvert)) || (rc = m->alloc(&b, m->dev.totvert)) ||
+      (rc = m->alloc(&l, m->dev.totvert)))
+    return rc;
   m->dev.orig_co = a;
   m->dev.orig_no = b;
+  m->dev.layer_disp = l;
   return SGPU_OK;
 }
 
@@ -418,6 +423,8 @@ int copy_original(sgpu_mesh* m) {
      "copy original positions");
   CK(cudaMemcpyAsync(m->dev.orig_no, m->dev.no, bytes, cudaMemcpyDeviceToDevice, m->stream),
      "copy original normals");
+  CK(cudaMemsetAsync(m->dev.layer_disp, 0, sizeof(float) * m->dev.totvert, m->stream),
+     "reset layer heights");
   m->orig_stored = true;
   return SGPU_OK;
 }
@@ -490,7 +497,7 @@ int launch_tool(Launcher& L, const DevBrush& b, PassParams pp) {
   if (uses_area(b.tool)) {
     LAUNCH(L, kKArea, "area kernel", launch_area(d, b, pp, s));
     LAUNCH(L, kKBrush, "brush kernel", launch_brush(d, b, pp, s));
-  } else if (b.tool == kToolInflate) {
+  } else if (b.tool == kToolInflate || b.tool == kToolLayer) {
     LAUNCH(L, kKBrush, "brush kernel", launch_brush(d, b, pp, s));
   } else {
     // Smooth: 4 sub-steps per unit strength, the last one fractional.
@@ -571,7 +578,7 @@ int enqueue_stroke(Launcher& L, const SGPU_Brush* brush, const SGPU_Dab* dabs, i
         pp.view[k] = sgn * brush->view_normal[k];
       }
       pp.cull_radius_sq = r * r;
-      pp.original = brush->use_original_bb;
+      pp.original = brush->use_original_bb || tool == kToolLayer;  // layer: original bounds
       pp.iter_strength = 1.0f;
       LAUNCH(L, kKCull, "cull kernel", launch_cull(m->dev, pp, m->stream));
       const int rc = launch_tool(L, base, pp);
@@ -626,6 +633,8 @@ int do_brush_tool(sgpu_mesh* m, const SGPU_Brush* brush, int tool, const float l
   if (!brush || !location || !grab_delta) return fail(SGPU_ERR_INVALID_ARG, "NULL argument");
   if (!tool_ok(tool)) return fail(SGPU_ERR_INVALID_ARG, "unsupported sculpt tool %d", tool);
   if (!(brush->radius > 0.0f)) return fail(SGPU_ERR_INVALID_ARG, "radius must be positive");
+  if (needs_stroke_start(tool) && !m->orig_stored)
+    return fail(SGPU_ERR_INVALID_ARG, "no stroke-start positions (sgpu_mesh_store_original)");
   if (uses_original(tool)) {
     if (nodes) return fail(SGPU_ERR_INVALID_ARG, "grab / elastic deform gather their own leaves");
     if (!m->orig_stored)
@@ -1064,6 +1073,10 @@ int sgpu_do_pinch_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float lo
 int sgpu_do_crease_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
                          const float grab_delta[3], const int* nodes, int totnode) {
   return do_brush_tool(mesh, brush, kToolCrease, location, grab_delta, nodes, totnode);
+}
+int sgpu_do_layer_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
+                        const float grab_delta[3], const int* nodes, int totnode) {
+  return do_brush_tool(mesh, brush, kToolLayer, location, grab_delta, nodes, totnode);
 }
 int sgpu_do_grab_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location[3],
                        const float grab_delta[3], const int* nodes, int totnode) {

@@ -503,6 +503,35 @@ __global__ void __launch_bounds__(kThreads) k_orig_dab(DevMesh m, DevBrush b, Da
 }
 
 
+// Layer brush on one vertex: the sphere test on the stroke-start position,
+// the layer height raised by fade * strength * (1.05 - |height|) and clamped
+// to +-(1 - mask), the target o + on * (height_brush * layer), approached by
+// |fade| of the way from the current position.
+__device__ __forceinline__ bool layer_vertex(const DevMesh& m, const DevBrush& b, const float* ys,
+                                             const PassParams& pp, int v, float4& co,
+                                             bool& moved) {
+  const float4 o = m.orig_co[v];
+  const float e0 = o.x - pp.loc[0], e1 = o.y - pp.loc[1], e2 = o.z - pp.loc[2];
+  const float d2 = e0 * e0 + e1 * e1 + e2 * e2;
+  if (!(d2 <= b.radius * b.radius)) return false;
+  const float fade = strength_factor(m, b, ys, pp, v, sqrtf(d2), b.radius);
+  float disp = m.layer_disp[v];
+  disp = disp + fade * b.strength * (1.05f - fabsf(disp));
+  const float lim = m.mask ? 1.0f - m.mask[v] : 1.0f;
+  disp = disp < -lim ? -lim : (disp > lim ? lim : disp);
+  m.layer_disp[v] = disp;
+  const float4 on = m.orig_no[v];
+  const float n0 = on.x * b.height, n1 = on.y * b.height, n2 = on.z * b.height;
+  const float f0 = o.x + n0 * disp, f1 = o.y + n1 * disp, f2 = o.z + n2 * disp;
+  const float af = fabsf(fade);
+  const float v0 = (f0 - co.x) * af, v1 = (f1 - co.y) * af, v2 = (f2 - co.z) * af;
+  co.x = co.x + v0;
+  co.y = co.y + v1;
+  co.z = co.z + v2;
+  moved = fade != 0.0f;
+  return true;
+}
+
 // Draw, inflate and clay strips (one pass each; positions written in place,
 // each vertex by exactly one thread since leaves expose unique vertices).
 __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassParams pp) {
@@ -529,7 +558,8 @@ __global__ void __launch_bounds__(kThreads) k_brush(DevMesh m, DevBrush b, PassP
       const int k = find_slot(m.cull_off, cnt, i);
       const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
       float4 co = m.co[v];
-      const bool hit = brush_vertex(m, b, ys, pp, f, v, co, moved);
+      const bool hit = b.tool == kToolLayer ? layer_vertex(m, b, ys, pp, v, co, moved)
+                                            : brush_vertex(m, b, ys, pp, f, v, co, moved);
       if (hit) {
         m.co[v] = co;
         if (m.type == kFaces) m.vtag[v] = 1;

@@ -55,8 +55,9 @@ struct DevMesh {
   int nlevels;
   float4* co;  // FACES: the MVert bytes (xyz + flag/bweight/pad in w); GRIDS: xyz, 0
   float4* no;
-  float4* orig_co;  // stroke-start positions and normals (grab, elastic deform); may be null
+  float4* orig_co;  // stroke-start positions and normals (grab, elastic deform, layer); may be null
   float4* orig_no;
+  float* layer_disp;  // layer brush: per-vertex layer height of the stroke
   float* mask;      // nullable
   const float* automask;  // nullable
   // FACES topology
@@ -165,6 +166,7 @@ struct DevBrush {
   float plane_offset;
   float crease_pinch_factor;
   int elastic_type;                   // BRUSH_ELASTIC_DEFORM_*
+  float height;                       // layer height
   float kl_a, kl_b, kl_c, kl_f;       // BKE_kelvinlet_init_params of the dab
   float kl_rs[3];
   float x_first, x_last;
@@ -186,7 +188,11 @@ struct PassParams {
 
 constexpr int kBrushFrontFace = 1 << 27;
 constexpr int kToolDraw = 1, kToolSmooth = 2, kToolPinch = 3, kToolInflate = 4, kToolGrab = 5,
-              kToolCrease = 16, kToolClayStrips = 18, kToolElasticDeform = 21;
+              kToolLayer = 6, kToolCrease = 16, kToolClayStrips = 18, kToolElasticDeform = 21;
+// Tools that read the stroke-start positions (stored when a stroke starts).
+__host__ __device__ __forceinline__ bool needs_stroke_start(int tool) {
+  return tool == kToolGrab || tool == kToolElasticDeform || tool == kToolLayer;
+}
 // Tools that rebuild positions from the stroke-start ones (one dab, all passes).
 __host__ __device__ __forceinline__ bool uses_original(int tool) {
   return tool == kToolGrab || tool == kToolElasticDeform;

@@ -43,7 +43,7 @@ class SGPU_Brush(C.Structure):
                 ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
                 ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float),
                 ("elastic_deform_type", C.c_int),
-                ("elastic_deform_volume_preservation", C.c_float)]
+                ("elastic_deform_volume_preservation", C.c_float), ("height", C.c_float)]
 
 
 class SGPU_MeshInfo(C.Structure):
@@ -80,7 +80,7 @@ EXPORTS = (
     "sgpu_mesh_stream", "sgpu_search_sphere", "sgpu_do_draw_brush", "sgpu_do_smooth_brush",
     "sgpu_do_inflate_brush", "sgpu_do_clay_strips_brush", "sgpu_do_brush",
     "sgpu_do_pinch_brush", "sgpu_do_crease_brush", "sgpu_do_grab_brush",
-    "sgpu_do_elastic_deform_brush", "sgpu_mesh_store_original",
+    "sgpu_do_elastic_deform_brush", "sgpu_mesh_store_original", "sgpu_do_layer_brush",
     "sgpu_pbvh_update_normals", "sgpu_pbvh_update_bounds", "sgpu_pbvh_node_mark_update",
     "sgpu_stroke", "sgpu_get_verts", "sgpu_set_verts", "sgpu_get_positions",
     "sgpu_set_positions", "sgpu_get_normals", "sgpu_get_mask", "sgpu_get_node_bbs",
@@ -135,7 +135,8 @@ def load(path: str | None = None):
     L.sgpu_raycast.argtypes = [vp, i, vp, vp, vp, i, vp, vp, vp, vp, vp]
     for name in ("sgpu_do_draw_brush", "sgpu_do_smooth_brush", "sgpu_do_inflate_brush",
                  "sgpu_do_clay_strips_brush", "sgpu_do_brush", "sgpu_do_pinch_brush",
-                 "sgpu_do_crease_brush", "sgpu_do_grab_brush", "sgpu_do_elastic_deform_brush"):
+                 "sgpu_do_crease_brush", "sgpu_do_grab_brush", "sgpu_do_elastic_deform_brush",
+                 "sgpu_do_layer_brush"):
         getattr(L, name).argtypes = [vp, C.POINTER(SGPU_Brush), vp, vp, vp, i]
     L.sgpu_pbvh_update_normals.argtypes = [vp]
     L.sgpu_pbvh_update_bounds.argtypes = [vp, i]
@@ -246,6 +247,7 @@ def make_brush(st) -> SGPU_Brush:
     b.crease_pinch_factor = st.crease_pinch_factor
     b.elastic_deform_type = st.elastic_deform_type
     b.elastic_deform_volume_preservation = st.elastic_deform_volume_preservation
+    b.height = st.height
     return b
 
 
@@ -443,6 +445,9 @@ class PBVH:
 
     def do_crease_brush(self, st, location, grab_delta, nodes=None):
         self._brush("sgpu_do_crease_brush", st, location, grab_delta, nodes)
+
+    def do_layer_brush(self, st, location, grab_delta, nodes=None):
+        self._brush("sgpu_do_layer_brush", st, location, grab_delta, nodes)
 
     def do_grab_brush(self, st, location, grab_delta):
         """One dab over all symmetry passes (the library gathers the leaves)."""

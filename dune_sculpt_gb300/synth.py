@@ -208,11 +208,12 @@ class Stroke:
     crease_pinch_factor: float = 0.5  # types_brush_defaults.h:23
     elastic_deform_type: int = 0      # BRUSH_ELASTIC_DEFORM_GRAB
     elastic_deform_volume_preservation: float = 0.4
+    height: float = 0.5  # Brush.height (layer)
 
 
 TOOL_DRAW, TOOL_SMOOTH, TOOL_INFLATE, TOOL_CLAY_STRIPS = 1, 2, 4, 18
 TOOL_PINCH, TOOL_CREASE = 3, 16
-TOOL_GRAB, TOOL_ELASTIC_DEFORM = 5, 21
+TOOL_GRAB, TOOL_ELASTIC_DEFORM, TOOL_LAYER = 5, 21, 6
 CURVE_SHARP, CURVE_SMOOTH = 1, 2
 SYMM_X = 1
 

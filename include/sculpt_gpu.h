@@ -79,6 +79,7 @@ typedef struct SGPU_MLoopTri { /* MLoopTri, types_meshdata.h:178-181 */
 #define SGPU_TOOL_PINCH 3        /* SCULPT_TOOL_PINCH */
 #define SGPU_TOOL_INFLATE 4      /* SCULPT_TOOL_INFLATE */
 #define SGPU_TOOL_GRAB 5         /* SCULPT_TOOL_GRAB */
+#define SGPU_TOOL_LAYER 6        /* SCULPT_TOOL_LAYER */
 #define SGPU_TOOL_CREASE 16      /* SCULPT_TOOL_CREASE */
 #define SGPU_TOOL_CLAY_STRIPS 18 /* SCULPT_TOOL_CLAY_STRIPS */
 #define SGPU_TOOL_ELASTIC_DEFORM 21 /* SCULPT_TOOL_ELASTIC_DEFORM (Kelvinlets, kelvinlet.c) */
@@ -114,6 +115,7 @@ typedef struct SGPU_Brush {
   float crease_pinch_factor;  /* crease: pinch strength (default 0.5, types_brush_defaults.h:23) */
   int elastic_deform_type;    /* SGPU_ELASTIC_DEFORM_* */
   float elastic_deform_volume_preservation; /* Kelvinlet Poisson ratio, in [0, 1) */
+  float height;               /* Brush.height: the layer brush's layer height */
 } SGPU_Brush;
 
 /* One dab of a stroke: location and grab delta (stroke direction). */
@@ -203,6 +205,11 @@ int sgpu_do_pinch_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float lo
                         const float grab_delta[3], const int *nodes, int totnode);
 int sgpu_do_crease_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
                          const float grab_delta[3], const int *nodes, int totnode);
+/* Layer: per pass like the above, from the stroke-start positions and
+ * normals and a per-vertex layer height that sgpu_mesh_store_original resets
+ * (needs it at the stroke start; sgpu_stroke does it itself). */
+int sgpu_do_layer_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
+                        const float grab_delta[3], const int *nodes, int totnode);
 /* Original-data brushes (grab, elastic deform): one DAB over all symmetry
  * passes of brush->symmetry, from the unmirrored location and grab delta — the
  * reference combines these brushes' proxies once per dab onto the original
@@ -217,7 +224,8 @@ int sgpu_do_grab_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float loc
 int sgpu_do_elastic_deform_brush(sgpu_mesh *mesh, const SGPU_Brush *brush,
                                  const float location[3], const float grab_delta[3],
                                  const int *nodes, int totnode);
-/* Copies the current positions and normals as the stroke-start ones. */
+/* Copies the current positions and normals as the stroke-start ones and
+ * resets the layer heights. */
 int sgpu_mesh_store_original(sgpu_mesh *mesh);
 /* Dispatch on brush->sculpt_tool. */
 int sgpu_do_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],

@@ -51,6 +51,7 @@ typedef struct OrBrush {
   float crease_pinch_factor;
   int elastic_deform_type;                /* BRUSH_ELASTIC_DEFORM_* */
   float elastic_deform_volume_preservation; /* Kelvinlet Poisson ratio */
+  float height;                            /* layer height */
 } OrBrush;
 
 /* ---- mesh (PBVH_FACES) ---- */

@@ -711,7 +711,7 @@ void or_mesh_free(OrMesh *m)
                   m->vert_indices,   m->leaf_nodes,   m->sf.co,      m->sf.no,     m->sf.mask,
                   m->sf.vb,          m->sf.orig_vb,   m->sd.co,      m->sd.no,     m->sd.mask,
                   m->sd.vb,          m->sd.orig_vb,   m->sf.orig_co, m->sf.orig_no, m->sd.orig_co,
-                  m->sd.orig_no};
+                  m->sd.orig_no,     m->sf.layer_disp, m->sd.layer_disp};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) {
     free(ptrs[i]);
   }

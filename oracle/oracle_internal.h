@@ -29,6 +29,7 @@
 #define OR_TOOL_PINCH 3
 #define OR_TOOL_CREASE 16
 #define OR_TOOL_GRAB 5
+#define OR_TOOL_LAYER 6
 #define OR_TOOL_ELASTIC_DEFORM 21
 /* eBrushElasticDeformType (types_brush_enums.h:195-199) */
 #define OR_ELASTIC_GRAB 0
@@ -60,12 +61,14 @@ typedef struct OrStateF {
   float *co, *no, *mask;     /* 3V, 3V, V (mask may be NULL) */
   float *vb, *orig_vb;       /* 6N */
   float *orig_co, *orig_no;  /* 3V each: positions / normals at the stroke start */
+  float *layer_disp;         /* V: the layer brush's per-vertex layer height */
 } OrStateF;
 
 typedef struct OrStateD {
   double *co, *no, *mask;
   double *vb, *orig_vb;
   double *orig_co, *orig_no;
+  double *layer_disp;
 } OrStateD;
 
 struct OrMesh {

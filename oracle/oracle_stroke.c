@@ -66,6 +66,9 @@ int or_brush_pass(OrMesh *m, const OrBrush *b, const float location[3],
 {
   OrCurve cu;
   or_curve_build(b->curve_preset, &cu);
+  if (b->sculpt_tool == OR_TOOL_LAYER && !m->sf.orig_co) {
+    store_original_f(m, &m->sf); /* the layer reads the stroke-start positions */
+  }
   return (int)brush_pass_f(m, &m->sf, &cu, b, location, grab_delta, b->view_normal, nodes,
                            totnode, area_out);
 }

@@ -28,7 +28,7 @@ class OrBrush(C.Structure):
                 ("plane_offset", C.c_float), ("view_normal", C.c_float * 3),
                 ("use_original_bb", C.c_int), ("crease_pinch_factor", C.c_float),
                 ("elastic_deform_type", C.c_int),
-                ("elastic_deform_volume_preservation", C.c_float)]
+                ("elastic_deform_volume_preservation", C.c_float), ("height", C.c_float)]
 
 
 class OrDrawSetup(C.Structure):
@@ -113,6 +113,7 @@ def make_brush(st) -> OrBrush:
     b.crease_pinch_factor = st.crease_pinch_factor
     b.elastic_deform_type = st.elastic_deform_type
     b.elastic_deform_volume_preservation = st.elastic_deform_volume_preservation
+    b.height = st.height
     return b
 
 

@@ -1,5 +1,5 @@
-"""Grab and elastic deform (the original-data brushes) on the GPU against the
-oracle, bit for bit: strokes through every path (eager, graph; the persistent
+"""Grab, elastic deform and layer (the brushes that read the stroke-start
+positions) on the GPU against the oracle, bit for bit: strokes through every path (eager, graph; the persistent
 mode falls back to the graph path for them), per-call dabs after
 sgpu_mesh_store_original, FACES and GRIDS, symmetry, front face and masks.
 The oracle's Kelvinlet displacement is pinned to the reference's compiled
@@ -67,13 +67,36 @@ def test_elastic_deform_stroke(gpu, oracle, kind):
     assert rel_err(g.positions(), o.co64()) < FP64_TOL
 
 
+@pytest.mark.parametrize("mode", [STROKE_EAGER, STROKE_GRAPH, STROKE_TEAM])
+def test_layer_stroke(gpu, oracle, mode):
+    m = small_icosphere(5)  # masked
+    g, o = _pair(oracle, m, 600)
+    st = synth.Stroke(synth.TOOL_LAYER, 0.15, 0.7, synth.CURVE_SMOOTH, synth.SYMM_X,
+                      synth.arc_dabs(13, 20, 0.04), height=0.3)
+    s = g.stroke(st, mode=mode)
+    tot, _ = o.stroke(st, which=3)
+    assert s.verts_displaced == tot and tot > 0
+    _assert_equal(g, o, f"layer mode {mode}")
+    assert rel_err(g.positions(), o.co64()) < FP64_TOL
+    gr = synth.torus_grids(16, 6, level=4)
+    gp = PBVH.build_grids(gr, 4)
+    og = oracle.OracleMesh.grids(gr, 4)
+    og.recalc_all_normals()
+    st = synth.Stroke(synth.TOOL_LAYER, 0.15, -0.5, synth.CURVE_SHARP, synth.SYMM_X,
+                      synth.torus_dabs(31, 12, 0.1), height=0.2)
+    s = gp.stroke(st, mode=mode)
+    tot, _ = og.stroke(st, which=1)
+    assert s.verts_displaced == tot and tot > 0
+    assert bits_equal(gp.positions(), og.co()), first_diff(gp.positions(), og.co())
+
+
 def test_mixed_stroke_with_grab(gpu, oracle):
     """Draw, grab and smooth dabs in one stroke: the grab dabs rebuild their
     leaves from the positions stored at the stroke start."""
     m = small_icosphere(5)
     g, o = _pair(oracle, m, 600)
     dabs = synth.grab_dabs(7, 12, 0.02)
-    tools = np.array([(synth.TOOL_DRAW, synth.TOOL_GRAB, synth.TOOL_SMOOTH)[d % 3]
+    tools = np.array([(synth.TOOL_DRAW, synth.TOOL_GRAB, synth.TOOL_SMOOTH, synth.TOOL_LAYER)[d % 4]
                       for d in range(12)], dtype=np.int32)
     st = synth.Stroke(synth.TOOL_DRAW, 0.2, 0.5, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
     s = g.stroke(st, mode=STROKE_EAGER, dab_tools=tools)

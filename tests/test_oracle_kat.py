@@ -223,6 +223,24 @@ def test_flat_grid_grab_analytic(oracle):
     assert per[0] == per[1] == int(np.count_nonzero(fall > 0))
 
 
+def test_flat_grid_layer_analytic(oracle):
+    """Layer on a flat +Z grid, one dab: the layer height becomes
+    fade * strength * 1.05 and each vertex moves |fade| of the way to
+    orig + normal * brush_height * layer, i.e. z = height * 0.525 * fade^2
+    for strength 0.5."""
+    m = small_grid(64)
+    st = synth.Stroke(synth.TOOL_LAYER, 0.1, 0.5, synth.CURVE_SMOOTH, 0,
+                      np.array([[0.5, 0.5, 0.0, 1.0, 0.0, 0.0]], dtype=np.float32), height=0.5)
+    om = oracle.OracleMesh.faces(m, 400)
+    om.recalc_all_normals()
+    co0 = om.co().astype(np.float64)
+    om.stroke(st, which=3)
+    co = om.co64()
+    fall = _flat_fall(oracle, co0, [0.5, 0.5, 0.0], 0.1)
+    assert np.abs(co[:, :2] - co0[:, :2]).max() == 0.0
+    assert np.abs(co[:, 2] - 0.5 * (0.5 * 1.05 * fall) * fall).max() < 1e-6
+
+
 @pytest.mark.parametrize("kind", [0, 1, 2, 3, 4])
 def test_flat_grid_elastic_deform(oracle, kind):
     """Elastic deform moves every vertex (all leaves) by the Kelvinlet

@@ -177,6 +177,7 @@ REPLAY = [
     ("ngon", synth.TOOL_DRAW, 0.06, 0.9, synth.CURVE_SHARP, synth.SYMM_X),
     ("icosphere", synth.TOOL_PINCH, 0.1, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X),
     ("uvsphere", synth.TOOL_CREASE, 0.1, 0.7, synth.CURVE_SHARP, synth.SYMM_X),
+    ("icosphere", synth.TOOL_LAYER, 0.12, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X),
 ]
 
 
@@ -194,6 +195,9 @@ def test_stroke_replay_in_reference(oracle, case):
     rr = np.float32(radius) * scale
     rsq = rr * rr
     moved = 0
+    original = 1 if tool == synth.TOOL_LAYER else 0  # layer culls on the original boxes
+    if tool == synth.TOOL_LAYER:
+        o.store_original()
     for d in range(dabs.shape[0]):
         for p in range(8):
             if p & ~symm:
@@ -201,8 +205,8 @@ def test_stroke_replay_in_reference(oracle, case):
             sgn = np.array([-1 if p & (1 << k) else 1 for k in range(3)], np.float32)
             loc = dabs[d, :3] * sgn
             delta = dabs[d, 3:] * sgn
-            nodes = o.search_sphere(loc, rsq, 0)
-            assert np.array_equal(nodes, r.search_sphere(loc, rsq, 0)), (d, p)
+            nodes = o.search_sphere(loc, rsq, original)
+            assert np.array_equal(nodes, r.search_sphere(loc, rsq, original)), (d, p)
             n, _ = o.brush_pass(st, loc, delta, nodes)
             moved += n
             for nd in nodes:
