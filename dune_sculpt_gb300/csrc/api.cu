@@ -207,7 +207,9 @@ struct sgpu_mesh {
                     static_cast<void*>(ray.slot_leaf), static_cast<void*>(ray.slot_tmin),
                     static_cast<void*>(ray.slot_order), static_cast<void*>(ray.slot_key),
                     static_cast<void*>(ray.items), static_cast<void*>(ray.nitems),
-                    static_cast<void*>(ray.slot_special)})
+                    static_cast<void*>(ray.slot_special), static_cast<void*>(ray.items2),
+                    static_cast<void*>(ray.nitems2), static_cast<void*>(ray.st_depth),
+                    static_cast<void*>(ray.st_run), static_cast<void*>(ray.st_win)})
       if (p) cudaFree(p);
     if (ray_host) cudaFreeHost(ray_host);
     free_draw();
@@ -1909,9 +1911,10 @@ int ensure_ray_buffers(sgpu_mesh* m, int n) {
   if (m->ray_graph) cudaGraphExecDestroy(m->ray_graph);
   m->ray_graph = nullptr;
   m->ray_graph_n = m->ray_graph_orig = -1;
-  void* p[9] = {m->ray_dev, m->ray.count, m->ray.slot_leaf, m->ray.slot_tmin,
-                m->ray.slot_order, m->ray.slot_key, m->ray.items, m->ray.nitems,
-                m->ray.slot_special};
+  void* p[14] = {m->ray_dev,         m->ray.count,    m->ray.slot_leaf, m->ray.slot_tmin,
+                 m->ray.slot_order,  m->ray.slot_key, m->ray.items,     m->ray.nitems,
+                 m->ray.slot_special, m->ray.items2,  m->ray.nitems2,   m->ray.st_depth,
+                 m->ray.st_run,      m->ray.st_win};
   for (void* q : p)
     if (q) cudaFree(q);
   if (m->ray_host) cudaFreeHost(m->ray_host);
@@ -1930,6 +1933,11 @@ int ensure_ray_buffers(sgpu_mesh* m, int n) {
   CK(cudaMalloc(&m->ray.slot_special, sizeof(int) * slots), "cudaMalloc");
   CK(cudaMalloc(&m->ray.items, sizeof(int2) * items), "cudaMalloc");
   CK(cudaMalloc(&m->ray.nitems, sizeof(int)), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.items2, sizeof(int2) * items), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.nitems2, sizeof(int)), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.st_depth, sizeof(float) * n), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.st_run, sizeof(float) * n), "cudaMalloc");
+  CK(cudaMalloc(&m->ray.st_win, sizeof(int4) * n), "cudaMalloc");
   m->ray.item_cap = static_cast<int>(items);
   m->ray_cap = static_cast<size_t>(n);
   return SGPU_OK;
@@ -1976,6 +1984,9 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
     rb.depth_in = din + 6 * static_cast<size_t>(nrays);
     rb.original = original;
     rb.n2o = mesh->d_n2o;
+    // small batches (an interactive cursor ray) in one round: the second
+    // round's launches cost more latency than its saved work
+    rb.first_leaves = nrays <= 64 ? d.nleaf : 2;
     rb.depth_out = dout;
     rb.face_normal = dout + nrays;
     rb.hit = diout;

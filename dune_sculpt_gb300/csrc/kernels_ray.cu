@@ -22,6 +22,11 @@
 //                 rule, then the winning triangle's depth, active vertex
 //                 (corner nearest the hit, first among equals), face and
 //                 normal (normal_tri_v3 / normal_quad_v3).
+// The leaves are tested front to back in two rounds: k_ray_tris first tests
+// the first_leaves leaves of smallest entry distance; k_ray_finish (round 0)
+// walks them and settles every ray whose next leaf starts at or beyond the
+// running minimum (the reference never casts it, nor any later one); only the
+// other rays get their remaining leaves tested (round 1) and walked.
 // GRIDS (pbvh_grids_node_raycast, pbvh.c:4110-4201): the units are grid quads
 // (grid, row, column order) and ray_face_intersection_quad tries the second
 // triangle only when the first is not taken, so a quad whose two triangles
@@ -273,33 +278,35 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_leaves(DevMesh m, RayBatch 
     key[i] = kNoKey;
     rb.slot_special[static_cast<size_t>(ray) * L + i] = 0;
   }
-  // work items: (ray-slot, chunk of kRayChunk prims)
-  int nch = 0;
-  const int s0 = min(total, static_cast<int>(threadIdx.x) * ((total + kRayThreads - 1) / kRayThreads));
-  const int s1 = min(total, s0 + (total + kRayThreads - 1) / kRayThreads);
-  for (int s = s0; s < s1; s++) nch += (leaf_units(m, slot_leaf[s]) + kRayChunk - 1) / kRayChunk;
-  int all;
-  int off = ray_block_scan(nch, &all, scan);
-  if (threadIdx.x == 0) scan[0] = atomicAdd(rb.nitems, all);
   __syncthreads();
-  const int base = scan[0];
-  if (base + all > rb.item_cap) {
-    if (threadIdx.x == 0) atomicCAS(&m.work->err, 0, 5 /* SGPU_ERR_BOUNDS */);
-    return;
-  }
-  for (int s = s0; s < s1; s++) {
-    const int c = (leaf_units(m, slot_leaf[s]) + kRayChunk - 1) / kRayChunk;
-    for (int k = 0; k < c; k++) rb.items[base + off + k] = make_int2(ray * L + s, k);
-    off += c;
+  // round-0 work items: (ray-slot, chunk of kRayChunk units) of the first
+  // leaves in entry order
+  if (threadIdx.x == 0) {
+    const int first = min(total, rb.first_leaves);
+    int nch = 0;
+    for (int r = 0; r < first; r++)
+      nch += (leaf_units(m, slot_leaf[order[r]]) + kRayChunk - 1) / kRayChunk;
+    const int base = atomicAdd(rb.nitems, nch);
+    if (base + nch > rb.item_cap) {
+      atomicCAS(&m.work->err, 0, 5 /* SGPU_ERR_BOUNDS */);
+    } else {
+      int at = base;
+      for (int r = 0; r < first; r++) {
+        const int sl = order[r];
+        const int c = (leaf_units(m, slot_leaf[sl]) + kRayChunk - 1) / kRayChunk;
+        for (int k = 0; k < c; k++) rb.items[at++] = make_int2(ray * L + sl, k);
+      }
+    }
   }
 }
 
-__global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb) {
+__global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb, int round) {
   __shared__ unsigned long long s_min[kRayThreads / 32];
   const int L = m.nleaf;
-  const int total = __ldcg(rb.nitems);
+  const int2* items = round == 0 ? rb.items : rb.items2;
+  const int total = __ldcg(round == 0 ? rb.nitems : rb.nitems2);
   for (int it = blockIdx.x; it < total; it += gridDim.x) {
-    const int2 item = rb.items[it];
+    const int2 item = items[it];
     const int ray = item.x / L;
     float o[3], d[3];
 #pragma unroll
@@ -349,34 +356,120 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb
   }
 }
 
-// Dynamic shared memory: per listed leaf its order entry, tmin and key.
-__global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch rb) {
+// The winning triangle's exact depth, its normal, the active vertex (corner
+// nearest the hit, first among equals) and face; one thread.
+__device__ void ray_write_result(const DevMesh& m, const RayBatch& rb, int ray, const float* o,
+                                 const float* d, const RayTri& rt, float depth, int win_slot,
+                                 int win_pos, int win_tri) {
+  const size_t base = static_cast<size_t>(ray) * m.nleaf;
+  float fn[3] = {0.0f, 0.0f, 0.0f};
+  int av = -1, af = -1;
+  if (win_slot >= 0) {
+    const int leaf = rb.slot_leaf[base + win_slot];
+    if (m.type == kFaces) {
+      const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + win_pos]];
+      const float3 c[3] = {xyz(__ldcg(&m.co[tv.x])), xyz(__ldcg(&m.co[tv.y])),
+                           xyz(__ldcg(&m.co[tv.z]))};
+      float dt = depth;
+      raytri_hit(o, rt, c[0], c[1], c[2], &dt);  // the exact value (-0 kept)
+      depth = dt;
+      const float3 n = normal_tri(c[0], c[1], c[2]);
+      fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
+      const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
+      float3 nearest = c[0];
+      int best = 0;
+      for (int j = 1; j < 3; j++)
+        if (len_sq(loc, c[j]) < len_sq(loc, nearest)) {
+          nearest = c[j];
+          best = j;
+        }
+      const int id = best == 0 ? tv.x : (best == 1 ? tv.y : tv.z);
+      av = rb.n2o ? rb.n2o[id] : id;
+      af = tv.w;
+    } else {
+      const GridQuad q = grid_quad(m, leaf, win_pos);
+      float da = depth, db = depth;
+      const bool ha = raytri_hit(o, rt, q.c[0], q.c[1], q.c[2], &da);
+      raytri_hit(o, rt, q.c[0], q.c[2], q.c[3], &db);
+      // the taken triangle: from the in-order replay, or for a minimum-key
+      // leaf the first triangle when it meets the ray
+      const int tri = win_tri >= 0 ? win_tri : (ha ? 0 : 1);
+      depth = tri == 0 ? da : db;
+      const float3 n = normal_quad(q.c[0], q.c[1], q.c[2], q.c[3]);
+      fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
+      const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
+      float3 nearest = q.c[0];
+      int best = 0;
+      for (int j = 1; j < 4; j++)
+        if (len_sq(loc, q.c[j]) < len_sq(loc, nearest)) {
+          nearest = q.c[j];
+          best = j;
+        }
+      // corner j of the quad is (x + {0,1,1,0}[j], y + {0,0,1,1}[j])
+      const int xi = best == 1 || best == 2, yi = best >= 2;
+      av = m.grid_area * q.grid + (q.y + yi) * m.grid_size + (q.x + xi);
+      af = q.grid;
+    }
+  }
+  rb.depth_out[ray] = depth;
+  rb.hit[ray] = win_slot >= 0;
+  rb.active_vertex[ray] = av;
+  rb.active_face[ray] = af;
+  rb.face_normal[3 * ray] = fn[0];
+  rb.face_normal[3 * ray + 1] = fn[1];
+  rb.face_normal[3 * ray + 2] = fn[2];
+}
+
+// One CTA per ray.  Round 0 walks the first first_leaves leaves in entry
+// order, then either settles the ray (its next leaf would not be cast) or
+// saves the state and lists the remaining leaves' work items; round 1 walks
+// those for the unsettled rays.  Dynamic shared memory: per listed leaf its
+// order entry, tmin and key.
+__global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch rb, int round) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float s_da[kRayThreads], s_db[kRayThreads];
   __shared__ unsigned char s_ha[kRayThreads], s_hb[kRayThreads];
   __shared__ unsigned s_mask[kRayThreads / 32];
+  __shared__ int scan[32];
   __shared__ float s_depth, s_run_tmin;
   __shared__ int s_slot, s_cast, s_special, s_win_slot, s_win_pos, s_win_tri, s_leaf_hit;
   const int ray = blockIdx.x;
   const int L = m.nleaf;
+  int k0 = 0;
+  if (round == 1) {
+    k0 = __ldcg(&rb.st_win[ray].w);
+    if (k0 < 0) return;  // settled in round 0 (uniform over the CTA)
+  }
   const int cnt = rb.count[ray];
-  int cnt_replay = cnt;  // leaves walked by the whole CTA
+  const int k1 = round == 0 ? min(cnt, rb.first_leaves) : cnt;
   unsigned long long* s_key = reinterpret_cast<unsigned long long*>(smem);
   float* s_tmin = reinterpret_cast<float*>(s_key + L);
   int* s_order = reinterpret_cast<int*>(s_tmin + L);
   const size_t base = static_cast<size_t>(ray) * L;
   if (threadIdx.x == 0) {
-    s_run_tmin = FLT_MAX;
-    s_depth = rb.depth_in ? rb.depth_in[ray] : FLT_MAX;
-    s_win_slot = s_win_pos = s_win_tri = -1;
+    if (round == 0) {
+      s_run_tmin = FLT_MAX;
+      s_depth = rb.depth_in ? rb.depth_in[ray] : FLT_MAX;
+      s_win_slot = s_win_pos = s_win_tri = -1;
+    } else {
+      const int4 w = __ldcg(&rb.st_win[ray]);
+      s_run_tmin = __ldcg(&rb.st_run[ray]);
+      s_depth = __ldcg(&rb.st_depth[ray]);
+      s_win_slot = w.x;
+      s_win_pos = w.y;
+      s_win_tri = w.z;
+    }
   }
-  int special = 0;
   for (int i = threadIdx.x; i < cnt; i += kRayThreads) {
     s_key[i] = __ldcg(&rb.slot_key[base + i]);
     s_tmin[i] = rb.slot_tmin[base + i];
     s_order[i] = rb.slot_order[base + i];
-    if (m.type == kGrids) special |= __ldcg(&rb.slot_special[base + i]);
   }
+  __syncthreads();
+  int special = 0;
+  if (m.type == kGrids)
+    for (int k = k0 + static_cast<int>(threadIdx.x); k < k1; k += kRayThreads)
+      special |= __ldcg(&rb.slot_special[base + s_order[k]]);
   float o[3], d[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -387,12 +480,13 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
   raytri_init(rt, d);
   // traverse_tree with the callback: a leaf is cast when tmin < running
   // minimum; a hit inside it is taken when strictly closer than the depth
+  int kr = k1;  // leaves walked by the whole CTA
   if (!__syncthreads_or(special)) {
-    // every listed leaf reduces to its minimum key: one thread walks them
+    // every leaf of the range reduces to its minimum key: one thread walks them
     if (threadIdx.x == 0) {
-      float run_tmin = FLT_MAX, depth = s_depth;
-      int win_slot = -1, win_pos = -1;
-      for (int k = 0; k < cnt; k++) {
+      float run_tmin = s_run_tmin, depth = s_depth;
+      int win_slot = s_win_slot, win_pos = s_win_pos, win_tri = s_win_tri;
+      for (int k = k0; k < k1; k++) {
         const int sl = s_order[k];
         if (!(s_tmin[sl] < run_tmin)) continue;
         const unsigned long long key = s_key[sl];
@@ -402,16 +496,19 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
           depth = dmin;
           win_slot = sl;
           win_pos = static_cast<int>(key & 0xffffffffu);
+          win_tri = -1;
           run_tmin = depth;
         }
       }
       s_depth = depth;
+      s_run_tmin = run_tmin;
       s_win_slot = win_slot;
       s_win_pos = win_pos;
+      s_win_tri = win_tri;
     }
-    cnt_replay = 0;
+    kr = k0;
   }
-  for (int k = 0; k < cnt_replay; k++) {
+  for (int k = k0; k < kr; k++) {
     __syncthreads();
     if (threadIdx.x == 0) {
       const int sl = s_order[k];
@@ -486,65 +583,36 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
     if (threadIdx.x == 0 && s_leaf_hit) s_run_tmin = s_depth;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  float depth = s_depth;
-  const int win_slot = s_win_slot, win_pos = s_win_pos;
-  float fn[3] = {0.0f, 0.0f, 0.0f};
-  int av = -1, af = -1;
-  if (win_slot >= 0) {
-    const int leaf = rb.slot_leaf[base + win_slot];
-    if (m.type == kFaces) {
-      const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + win_pos]];
-      const float3 c[3] = {xyz(__ldcg(&m.co[tv.x])), xyz(__ldcg(&m.co[tv.y])),
-                           xyz(__ldcg(&m.co[tv.z]))};
-      float dt = depth;
-      raytri_hit(o, rt, c[0], c[1], c[2], &dt);  // the exact value (-0 kept)
-      depth = dt;
-      const float3 n = normal_tri(c[0], c[1], c[2]);
-      fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
-      const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
-      float3 nearest = c[0];
-      int best = 0;
-      for (int j = 1; j < 3; j++)
-        if (len_sq(loc, c[j]) < len_sq(loc, nearest)) {
-          nearest = c[j];
-          best = j;
-        }
-      const int id = best == 0 ? tv.x : (best == 1 ? tv.y : tv.z);
-      av = rb.n2o ? rb.n2o[id] : id;
-      af = tv.w;
-    } else {
-      const GridQuad q = grid_quad(m, leaf, win_pos);
-      float da = depth, db = depth;
-      const bool ha = raytri_hit(o, rt, q.c[0], q.c[1], q.c[2], &da);
-      raytri_hit(o, rt, q.c[0], q.c[2], q.c[3], &db);
-      // the taken triangle: from the in-order replay, or for a minimum-key
-      // leaf the first triangle when it meets the ray
-      const int tri = s_win_tri >= 0 ? s_win_tri : (ha ? 0 : 1);
-      depth = tri == 0 ? da : db;
-      const float3 n = normal_quad(q.c[0], q.c[1], q.c[2], q.c[3]);
-      fn[0] = n.x, fn[1] = n.y, fn[2] = n.z;
-      const float3 loc = make_float3(o[0] + d[0] * depth, o[1] + d[1] * depth, o[2] + d[2] * depth);
-      float3 nearest = q.c[0];
-      int best = 0;
-      for (int j = 1; j < 4; j++)
-        if (len_sq(loc, q.c[j]) < len_sq(loc, nearest)) {
-          nearest = q.c[j];
-          best = j;
-        }
-      // corner j of the quad is (x + {0,1,1,0}[j], y + {0,0,1,1}[j])
-      const int xi = best == 1 || best == 2, yi = best >= 2;
-      av = m.grid_area * q.grid + (q.y + yi) * m.grid_size + (q.x + xi);
-      af = q.grid;
+  if (round == 0 && k1 < cnt && s_tmin[s_order[k1]] < s_run_tmin) {
+    // the next leaf would be cast: keep the state, list the remaining leaves
+    if (threadIdx.x == 0) {
+      rb.st_depth[ray] = s_depth;
+      rb.st_run[ray] = s_run_tmin;
+      rb.st_win[ray] = make_int4(s_win_slot, s_win_pos, s_win_tri, k1);
     }
+    int nch = 0;
+    for (int k = k1 + static_cast<int>(threadIdx.x); k < cnt; k += kRayThreads)
+      nch += (leaf_units(m, rb.slot_leaf[base + s_order[k]]) + kRayChunk - 1) / kRayChunk;
+    int all;
+    int off = ray_block_scan(nch, &all, scan);
+    if (threadIdx.x == 0) scan[0] = atomicAdd(rb.nitems2, all);
+    __syncthreads();
+    const int at = scan[0];
+    if (at + all > rb.item_cap) {
+      if (threadIdx.x == 0) atomicCAS(&m.work->err, 0, 5 /* SGPU_ERR_BOUNDS */);
+      return;
+    }
+    for (int k = k1 + static_cast<int>(threadIdx.x); k < cnt; k += kRayThreads) {
+      const int sl = s_order[k];
+      const int c = (leaf_units(m, rb.slot_leaf[base + sl]) + kRayChunk - 1) / kRayChunk;
+      for (int j = 0; j < c; j++) rb.items2[at + off + j] = make_int2(ray * L + sl, j);
+      off += c;
+    }
+    return;
   }
-  rb.depth_out[ray] = depth;
-  rb.hit[ray] = win_slot >= 0;
-  rb.active_vertex[ray] = av;
-  rb.active_face[ray] = af;
-  rb.face_normal[3 * ray] = fn[0];
-  rb.face_normal[3 * ray + 1] = fn[1];
-  rb.face_normal[3 * ray + 2] = fn[2];
+  if (threadIdx.x != 0) return;
+  if (round == 0) rb.st_win[ray] = make_int4(-1, -1, -1, -1);  // settled
+  ray_write_result(m, rb, ray, o, d, rt, s_depth, s_win_slot, s_win_pos, s_win_tri);
 }
 
 }  // namespace
@@ -574,14 +642,20 @@ cudaError_t configure_ray_kernels(size_t leaves_smem, size_t finish_smem) {
 cudaError_t launch_raycast(const DevMesh& m, const RayBatch& rb, int nrays, int tris_grid,
                            cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(rb.nitems, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(rb.nitems2, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
   k_ray_leaves<<<nrays, kRayThreads, ray_leaves_smem(m), s>>>(m, rb);
-  e = cudaGetLastError();
+  // every leaf in round 0 settles every ray there: no second round
+  const int rounds = rb.first_leaves >= m.nleaf ? 1 : 2;
+  for (int round = 0; round < rounds && e == cudaSuccess; round++) {
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    k_ray_tris<<<tris_grid, kRayThreads, 0, s>>>(m, rb, round);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    k_ray_finish<<<nrays, kRayThreads, ray_finish_smem(m), s>>>(m, rb, round);
+  }
   if (e != cudaSuccess) return e;
-  k_ray_tris<<<tris_grid, kRayThreads, 0, s>>>(m, rb);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_ray_finish<<<nrays, kRayThreads, ray_finish_smem(m), s>>>(m, rb);
   return cudaGetLastError();
 }
 

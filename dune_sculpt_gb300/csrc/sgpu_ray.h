@@ -19,10 +19,18 @@ struct RayBatch {
   int* slot_order;
   unsigned long long* slot_key;
   int* slot_special;  // GRIDS: the leaf has a quad whose second triangle is the closer hit
-  // work items (ray * nleaf + slot, chunk) and their count
+  // work items (ray * nleaf + slot, chunk) and their count: the first leaves
+  // in entry order (round 0), the rest for the rays they did not settle (round 1)
   int2* items;
   int* nitems;
+  int2* items2;
+  int* nitems2;
   int item_cap;
+  int first_leaves;  // leaves tested in round 0 (every leaf: one round)
+  // per ray: the traversal state between the rounds (next rank; -1 = done)
+  float* st_depth;
+  float* st_run;
+  int4* st_win;  // winning slot, position, triangle, next rank
   // results per ray
   float* depth_out;
   int* hit;
