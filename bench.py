@@ -303,6 +303,18 @@ def run_reference(args):
     return 0
 
 
+def combine_ranks(dist, total_ms, e2e_ms, total_v, e2e_v):
+    """Replicas: the slowest rank's times (max) and every rank's vertices
+    (sum), so that value = all vertices / the job's time."""
+    import torch
+
+    t = torch.tensor([total_ms, e2e_ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([total_v, e2e_v], dtype=torch.float64)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), int(c[0]), int(c[1])
+
+
 def run_gpu(args):
     world, rank, local = dist_env()
     if world > 1:
@@ -393,14 +405,7 @@ def run_gpu(args):
     draw = run_draw_leg(g, m, st, leaf_limit, args.no_cpu, peak=measured_peaks()[0])
 
     if world > 1:
-        import torch
-
-        t = torch.tensor([total_ms, e2e_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_ms = float(t[0]), float(t[1])
-        c = torch.tensor([total_v, e2e_v], dtype=torch.float64)
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        total_v, e2e_v = int(c[0]), int(c[1])
+        total_ms, e2e_ms, total_v, e2e_v = combine_ranks(dist, total_ms, e2e_ms, total_v, e2e_v)
     if rank != 0:
         return 0
 
