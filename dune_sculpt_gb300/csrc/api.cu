@@ -419,13 +419,13 @@ int ensure_original(sgpu_mesh* m) {
 
 // The undo push of the stroke start: positions and normals kept as originals
 // (stream-ordered, capturable).
-int copy_original(sgpu_mesh* m) {
+int copy_original(sgpu_mesh* m, cudaStream_t s) {
   const size_t bytes = sizeof(float4) * m->dev.totvert;
-  CK(cudaMemcpyAsync(m->dev.orig_co, m->dev.co, bytes, cudaMemcpyDeviceToDevice, m->stream),
+  CK(cudaMemcpyAsync(m->dev.orig_co, m->dev.co, bytes, cudaMemcpyDeviceToDevice, s),
      "copy original positions");
-  CK(cudaMemcpyAsync(m->dev.orig_no, m->dev.no, bytes, cudaMemcpyDeviceToDevice, m->stream),
+  CK(cudaMemcpyAsync(m->dev.orig_no, m->dev.no, bytes, cudaMemcpyDeviceToDevice, s),
      "copy original normals");
-  CK(cudaMemsetAsync(m->dev.layer_disp, 0, sizeof(float) * m->dev.totvert, m->stream),
+  CK(cudaMemsetAsync(m->dev.layer_disp, 0, sizeof(float) * m->dev.totvert, s),
      "reset layer heights");
   m->orig_stored = true;
   return SGPU_OK;
@@ -556,7 +556,7 @@ int enqueue_stroke(Launcher& L, const SGPU_Brush* brush, const SGPU_Dab* dabs, i
   CK(cudaMemsetAsync(&m->dev.work->displaced, 0, sizeof(unsigned long long), m->stream),
      "reset counter");
   if (stroke_has_original(brush, dab_tools, ndabs)) {
-    const int rc = copy_original(m);
+    const int rc = copy_original(m, m->stream);
     if (rc) return rc;
   }
   for (int d = 0; d < ndabs; d++) {
@@ -1092,7 +1092,7 @@ int sgpu_do_elastic_deform_brush(sgpu_mesh* mesh, const SGPU_Brush* brush,
 int sgpu_mesh_store_original(sgpu_mesh* mesh) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
-  if ((rc = ensure_original(mesh)) || (rc = copy_original(mesh))) return rc;
+  if ((rc = ensure_original(mesh)) || (rc = copy_original(mesh, mesh->stream))) return rc;
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
   return SGPU_OK;
 }
@@ -1139,9 +1139,6 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   if (brush->symmetry < 0 || brush->symmetry > 7)
     return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
-  // the persistent kernel has no original-data brushes: such strokes take the graph path
-  if (mode == SGPU_STROKE_TEAM && stroke_has_original(brush, dab_tools, ndabs))
-    mode = SGPU_STROKE_GRAPH;
   if (mode == SGPU_STROKE_TEAM) {
     const int offs[2] = {0, ndabs};
     sgpu_mesh* one[1] = {mesh};
@@ -1779,10 +1776,16 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
                const int* offs, const int* tools, int cluster, cudaStream_t s,
                SGPU_StrokeStats* stats, float* total_ms, bool wait) {
   sgpu_mesh* m0 = meshes[0];
+  // strokes with grab, elastic deform or layer dabs keep the stroke-start
+  // positions (stored on the launch stream below)
+  static thread_local std::vector<char> h_orig;
+  h_orig.assign(n, 0);
+  int rc;
   for (int i = 0; i < n; i++)
-    if (stroke_has_original(&brushes[i], tools ? tools + offs[i] : nullptr, offs[i + 1] - offs[i]))
-      return fail(SGPU_ERR_UNSUPPORTED,
-                  "grab and elastic deform do not run in the persistent stroke kernel");
+    if (stroke_has_original(&brushes[i], tools ? tools + offs[i] : nullptr, offs[i + 1] - offs[i])) {
+      if ((rc = ensure_original(meshes[i]))) return rc;
+      h_orig[i] = 1;
+    }
   int max_nodes = 0, max_leaves = 0;
   for (int i = 0; i < n; i++) {
     max_nodes = std::max(max_nodes, meshes[i]->dev.totnode);
@@ -1793,7 +1796,6 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   const int nteams_max = team_max_active_clusters(cluster, max_nodes, max_leaves);
   if (nteams_max <= 0)
     return fail(SGPU_ERR_UNSUPPORTED, "cluster size %d cannot be launched", cluster);
-  int rc;
   // staging buffers live on the first mesh; re-create when too small
   static thread_local std::vector<DevMesh> h_meshes;
   static thread_local std::vector<TeamJob> h_jobs;
@@ -1830,8 +1832,13 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
     job.tools = tools ? m0->t_tools + offs[i] : nullptr;
     if (!make_brush(&brushes[i], brushes[i].sculpt_tool, &job.brush))
       return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brushes[i].curve_preset);
+    // Kelvinlet constants of the stroke; the kernel sets the force per dab
+    const float no_delta[3] = {0.0f, 0.0f, 0.0f};
+    kelvinlet_params(&job.brush, no_delta, brushes[i].elastic_deform_volume_preservation);
   }
   CK(cudaEventRecord(m0->ev0, s), "event");
+  for (int i = 0; i < n; i++)
+    if (h_orig[i] && (rc = copy_original(meshes[i], s))) return rc;
   if (ndab)
     CK(cudaMemcpyAsync(m0->t_dabs, dabs, sizeof(SGPU_Dab) * ndab, cudaMemcpyHostToDevice, s),
        "upload dabs");

@@ -354,89 +354,13 @@ __global__ void __launch_bounds__(kCullThreads) k_cull_dab(DevMesh m, DabPasses 
   prof_add(m, kKCull, threadIdx.x == 0 ? 24ull * m.totnode + 8ull * run_cnt : 0ull);
 }
 
-__device__ __forceinline__ float kp2(float x) { return x * x; }
-__device__ __forceinline__ float kp3(float x) { return kp2(x) * x; }
-__device__ __forceinline__ float kp5(float x) { return kp2(kp2(x)) * x; }
-
-// init_kelvinlet_grab (kelvinlet.c:23-44) for n scales.
-__device__ __forceinline__ void kelvinlet_grab_k(const DevBrush& b, float radius, int n,
-                                                 float* k) {
-  for (int i = 0; i < n; i++) {
-    const float re = sqrtf(kp2(radius) + kp2(b.kl_rs[i]));
-    k[i] = ((b.kl_a - b.kl_b) / re) + ((b.kl_b * kp2(radius)) / kp3(re)) +
-           ((b.kl_a * kp2(b.kl_rs[i])) / (2.0f * kp3(re)));
-  }
-}
-
-// kelvinlet_scale / kelvinlet_twist (kelvinlet.c:131-186) at one point.
-__device__ __forceinline__ float3 kelvinlet_field(const DevBrush& b, float3 co, const float* loc,
-                                                  const float* nrm) {
-  const float r0 = co.x - loc[0], r1 = co.y - loc[1], r2 = co.z - loc[2];
-  const float radius = sqrtf(r0 * r0 + r1 * r1 + r2 * r2);
-  const float re = sqrtf(kp2(radius) + kp2(b.kl_rs[0]));
-  const float head = b.elastic_type == 3 ? (2.0f * b.kl_b - b.kl_a) : -b.kl_a;
-  const float u = head * (1.0f / kp3(re)) + ((3.0f * kp2(b.kl_rs[0])) / (2.0f * kp5(re)));
-  const float s = (u * b.kl_c) * b.kl_f;
-  if (b.elastic_type == 3) return make_float3(r0 * s, r1 * s, r2 * s);
-  const float q0 = nrm[1] * r2 - nrm[2] * r1;
-  const float q1 = nrm[2] * r0 - nrm[0] * r2;
-  const float q2 = nrm[0] * r1 - nrm[1] * r0;
-  return make_float3(q0 * s, q1 * s, q2 * s);
-}
-
-// The Kelvinlet displacement of one element for one pass (kelvinlet.c):
-// grab types scale delta, scale / twist integrate the field in four steps.
-__device__ __forceinline__ float3 kelvinlet_disp(const DevBrush& b, float3 co, const float* loc,
-                                                 const float* dn) {
-  if (b.elastic_type <= 2) {
-    const float d0 = co.x - loc[0], d1 = co.y - loc[1], d2 = co.z - loc[2];
-    const float radius = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-    float k[3];
-    float fade;
-    if (b.elastic_type == 0) {
-      kelvinlet_grab_k(b, radius, 1, k);
-      fade = k[0] * b.kl_c;
-    } else if (b.elastic_type == 1) {
-      kelvinlet_grab_k(b, radius, 2, k);
-      const float u = k[0] - k[1];
-      fade = u * b.kl_c / ((1.0f / b.kl_rs[0]) - (1.0f / b.kl_rs[1]));
-    } else {
-      kelvinlet_grab_k(b, radius, 3, k);
-      const float s0 = kp2(b.kl_rs[0]), s1 = kp2(b.kl_rs[1]), s2 = kp2(b.kl_rs[2]);
-      const float w1 = -((s2 - s0) / (s2 - s1));
-      const float w2 = ((s1 - s0) / (s2 - s1));
-      const float u = 1.0f * k[0] + w1 * k[1] + w2 * k[2];
-      fade = u * b.kl_c / (1.0f / b.kl_rs[0] + w1 / b.kl_rs[1] + w2 / b.kl_rs[2]);
-    }
-    return make_float3(dn[0] * fade, dn[1] * fade, dn[2] * fade);
-  }
-  // sculpt_kelvinet_integrate (kelvinlet.c:104-128), third step as written there
-  const float3 k0 = kelvinlet_field(b, co, loc, dn);
-  const float3 k1 = kelvinlet_field(
-      b, make_float3(co.x + k0.x * 0.5f, co.y + k0.y * 0.5f, co.z + k0.z * 0.5f), loc, dn);
-  const float3 k2 = kelvinlet_field(
-      b, make_float3(co.x + k1.x * 0.5f, co.y + k1.y * 0.5f, co.z + k1.z * 0.5f), loc, dn);
-  const float3 k3 = kelvinlet_field(
-      b, make_float3((co.x + k2.x) - loc[0], (co.y + k2.y) - loc[1], (co.z + k2.z) - loc[2]), loc,
-      dn);
-  const float sixth = 1.0f / 6.0f;
-  return make_float3((((k0.x + k1.x * 2.0f) + k2.x * 2.0f) + k3.x) * sixth,
-                     (((k0.y + k1.y * 2.0f) + k2.y * 2.0f) + k3.y) * sixth,
-                     (((k0.z + k1.z * 2.0f) + k2.z * 2.0f) + k3.z) * sixth);
-}
-
-// One dab of grab / elastic deform: each brush-visible vertex of the gathered
-// leaves is rebuilt from its stroke-start position plus each pass's
-// displacement in pass order (the reference combines its proxies once per dab
-// onto the original coordinates).
+// One dab of grab / elastic deform over the gathered leaves (orig_vertex).
 __global__ void __launch_bounds__(kThreads) k_orig_dab(DevMesh m, DevBrush b, DabPasses dp) {
   __shared__ float ys[kCurveTable + 1];
   load_curve(b, ys);
   const int cnt = m.work->cull_count;
   const int total = m.cull_off[cnt];
   mark_culled(m, cnt);
-  const bool elastic = b.tool == kToolElasticDeform;
-  const float radius = b.radius, rsq = radius * radius;
   unsigned long long ab = 0;
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < total; base += stride) {
@@ -445,51 +369,8 @@ __global__ void __launch_bounds__(kThreads) k_orig_dab(DevMesh m, DevBrush b, Da
     if (i < total) {
       const int k = find_slot(m.cull_off, cnt, i);
       const int v = leaf_vert(m, m.cull_list[k], i - m.cull_off[k]);
-      const float4 o4 = m.orig_co[v];
-      const float3 o = make_float3(o4.x, o4.y, o4.z);
-      float c0 = o.x, c1 = o.y, c2 = o.z;
-      for (int p = 0; p < dp.npass; p++) {
-        if (elastic) {
-          float3 d = kelvinlet_disp(b, o, dp.loc[p], b.elastic_type <= 2 ? dp.delta[p] : dp.view[p]);
-          if (b.elastic_type <= 2) {
-            const float s = b.strength * 20.0f;
-            d = make_float3(d.x * s, d.y * s, d.z * s);
-          }
-          if (m.mask) {
-            const float mk = 1.0f - m.mask[v];
-            d = make_float3(d.x * mk, d.y * mk, d.z * mk);
-          }
-          if (m.automask) {
-            const float am = m.automask[v];
-            d = make_float3(d.x * am, d.y * am, d.z * am);
-          }
-          c0 = c0 + d.x;
-          c1 = c1 + d.y;
-          c2 = c2 + d.z;
-          moved += (d.x != 0.0f || d.y != 0.0f || d.z != 0.0f) ? 1u : 0u;
-        } else {
-          const float e0 = o.x - dp.loc[p][0], e1 = o.y - dp.loc[p][1], e2 = o.z - dp.loc[p][2];
-          const float d2 = e0 * e0 + e1 * e1 + e2 * e2;
-          if (!(d2 <= rsq)) continue;
-          float f = curve_strength(b, ys, sqrtf(d2), radius);
-          if (b.flag & kBrushFrontFace) {
-            const float4 n = m.orig_no[v];
-            const float dot = dp.view[p][0] * n.x + dp.view[p][1] * n.y + dp.view[p][2] * n.z;
-            f = f * (dot > 0.0f ? dot : 0.0f);
-          }
-          if (m.mask) f = f * (1.0f - m.mask[v]);
-          if (m.automask) f = f * m.automask[v];
-          const float fade = b.strength * f;
-          c0 = c0 + dp.delta[p][0] * fade;
-          c1 = c1 + dp.delta[p][1] * fade;
-          c2 = c2 + dp.delta[p][2] * fade;
-          moved += fade != 0.0f ? 1u : 0u;
-        }
-      }
       float4 co = m.co[v];
-      co.x = c0;
-      co.y = c1;
-      co.z = c2;
+      moved = orig_vertex(m, b, ys, dp, v, co);
       m.co[v] = co;
       if (m.type == kFaces) m.vtag[v] = 1;
       // index, original position (+ normal for the front face), mask, automask; position write
@@ -500,36 +381,6 @@ __global__ void __launch_bounds__(kThreads) k_orig_dab(DevMesh m, DevBrush b, Da
     if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&m.work->displaced, (unsigned long long)sum);
   }
   prof_add(m, kKBrush, ab);
-}
-
-
-// Layer brush on one vertex: the sphere test on the stroke-start position,
-// the layer height raised by fade * strength * (1.05 - |height|) and clamped
-// to +-(1 - mask), the target o + on * (height_brush * layer), approached by
-// |fade| of the way from the current position.
-__device__ __forceinline__ bool layer_vertex(const DevMesh& m, const DevBrush& b, const float* ys,
-                                             const PassParams& pp, int v, float4& co,
-                                             bool& moved) {
-  const float4 o = m.orig_co[v];
-  const float e0 = o.x - pp.loc[0], e1 = o.y - pp.loc[1], e2 = o.z - pp.loc[2];
-  const float d2 = e0 * e0 + e1 * e1 + e2 * e2;
-  if (!(d2 <= b.radius * b.radius)) return false;
-  const float fade = strength_factor(m, b, ys, pp, v, sqrtf(d2), b.radius);
-  float disp = m.layer_disp[v];
-  disp = disp + fade * b.strength * (1.05f - fabsf(disp));
-  const float lim = m.mask ? 1.0f - m.mask[v] : 1.0f;
-  disp = disp < -lim ? -lim : (disp > lim ? lim : disp);
-  m.layer_disp[v] = disp;
-  const float4 on = m.orig_no[v];
-  const float n0 = on.x * b.height, n1 = on.y * b.height, n2 = on.z * b.height;
-  const float f0 = o.x + n0 * disp, f1 = o.y + n1 * disp, f2 = o.z + n2 * disp;
-  const float af = fabsf(fade);
-  const float v0 = (f0 - co.x) * af, v1 = (f1 - co.y) * af, v2 = (f2 - co.z) * af;
-  co.x = co.x + v0;
-  co.y = co.y + v1;
-  co.z = co.z + v2;
-  moved = fade != 0.0f;
-  return true;
 }
 
 // Draw, inflate and clay strips (one pass each; positions written in place,

@@ -44,6 +44,7 @@ struct TeamShared {
   float4 hco[kTeamThreads];
   float area[6];
   int nmark;
+  DabPasses dp;  // passes of a grab / elastic deform dab
 };
 
 // Block-wide exclusive scan (kTeamThreads threads).
@@ -164,11 +165,10 @@ struct CullTabs {
 // leaves (at most 64: the team kernel takes at most 64 * 256 leaves); block
 // scans give the coverage entering the run and the list positions.  s_coff
 // doubles as the difference array.
-template <int kBox>
-__device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_par,
-                          unsigned char* s_pass, int* s_cl, int* s_coff, const CullTabs& ct,
-                          TeamShared& sh) {
-  const float4* bb = pp.original ? m.orig_vb : m.vb;
+template <int kBox, class Hit>
+__device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb, Hit hits,
+                                             unsigned char* s_pass, int* s_cl, int* s_coff,
+                                             const CullTabs& ct, TeamShared& sh) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
   __syncthreads();
@@ -189,7 +189,7 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_p
     for (int j = 0; j < kBox; j++) {
       const int n = n0 + j * kTeamThreads;
       if (n >= m.totnode) continue;
-      const bool hit = box_hits(lo[j], hi[j], pp.loc, pp.cull_radius_sq);
+      const bool hit = hits(lo[j], hi[j]);
       s_pass[n] = hit;
       if (!hit && lhi[j] - llo[j] > 1) {  // internal node (leaves own a range of one)
         atomicAdd(&s_coff[llo[j]], 1);
@@ -233,6 +233,61 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, const int* s_p
     s_coff[sh.cnt] = sh.total;
   }
   __syncthreads();
+}
+
+// The sweep of one grab / elastic deform dab over the gathered leaves (every
+// CTA of the team, strided by GT threads); returns the algorithmic bytes.
+__device__ __forceinline__ unsigned long long team_orig_sweep(const DevMesh& m, const DevBrush& b,
+                                                           const DabPasses& dp, const int* s_cl,
+                                                           const int* s_coff, int cnt, int total,
+                                                           int gt, int GT, int* tag_cnt) {
+  // index, original position (+ normal for the front face), mask, automask; position write
+  const unsigned vbytes = (m.type == kFaces ? 4u : 0u) + 12u +
+                          ((b.flag & kBrushFrontFace) ? 12u : 0u) + (m.mask ? 4u : 0u) +
+                          (m.automask ? 4u : 0u) + 12u;
+  const int lane = threadIdx.x & 31;
+  unsigned long long ab = 0;
+  for (int base = gt - lane; base < total; base += GT) {
+    const int i = base + lane;
+    unsigned int moved = 0u;
+    if (i < total) {
+      const int k = smem_find_slot(s_coff, cnt, i);
+      const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+      float4 co = __ldcg(&m.co[v]);
+      moved = orig_vertex(m, b, b.y, dp, v, co);
+      m.co[v] = co;
+      ab += vbytes;
+      if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+    }
+    const unsigned int sum = __reduce_add_sync(0xffffffffu, moved);
+    if (lane == 0 && sum) atomicAdd(&m.work->displaced, (unsigned long long)sum);
+  }
+  return ab;
+}
+
+// The node search of one pass (sphere at the pass location).
+template <int kBox>
+__device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char* s_pass,
+                          int* s_cl, int* s_coff, const CullTabs& ct, TeamShared& sh) {
+  team_cull_by<kBox>(
+      m, pp.original ? m.orig_vb : m.vb,
+      [&](float4 lo, float4 hi) { return box_hits(lo, hi, pp.loc, pp.cull_radius_sq); }, s_pass,
+      s_cl, s_coff, ct, sh);
+}
+
+// The gather of one grab / elastic deform dab (k_cull_dab): orig_vb boxes that
+// meet any pass sphere, or every leaf (all != 0).
+__device__ __forceinline__ void team_cull_union(const DevMesh& m, const DabPasses& dp, float rsq,
+                                             int all, unsigned char* s_pass, int* s_cl,
+                                             int* s_coff, const CullTabs& ct, TeamShared& sh) {
+  team_cull_by<2>(
+      m, m.orig_vb,
+      [&](float4 lo, float4 hi) {
+        bool ok = all != 0;
+        for (int p = 0; p < dp.npass && !ok; p++) ok = box_hits(lo, hi, dp.loc[p], rsq);
+        return ok;
+      },
+      s_pass, s_cl, s_coff, ct, sh);
 }
 
 constexpr int kFlushTab = 128;  // ancestors whose boxes stay on chip
@@ -757,7 +812,44 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       const float r = b.radius * scale;
       int* tag_cnt = &w->tag_count[par];
       int* touch_cnt = &w->touch_count[par];
-      for (int pass = 0; pass < 8; pass++) {
+      if (uses_original(tool)) {
+        // grab / elastic deform: one gather over all passes, then each vertex
+        // rebuilt from its stroke-start position (k_cull_dab, k_orig_dab)
+        if (threadIdx.x == 0) {
+          DabPasses& dp = sh.dp;
+          dp.npass = 0;
+          for (int pass = 0; pass < 8; pass++) {
+            if ((pass & ~sh.job.symmetry) != 0) continue;
+            for (int k = 0; k < 3; k++) {
+              const float sgn = (pass & (1 << k)) ? -1.0f : 1.0f;
+              dp.loc[dp.npass][k] = sgn * sh.job.dabs[6 * d + k];
+              dp.delta[dp.npass][k] = sgn * sh.job.dabs[6 * d + 3 + k];
+              dp.view[dp.npass][k] = sgn * sh.job.view[k];
+            }
+            dp.npass++;
+          }
+          // the Kelvinlet force of the dab (BKE_kelvinlet_init_params,
+          // kelvinlet.c:6-21): |grab delta| * strength
+          const float* gd = &sh.job.dabs[6 * d + 3];
+          b.kl_f = sqrtf(gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2]) * b.strength;
+        }
+        __syncthreads();
+        team_cull_union(m, sh.dp, b.radius * b.radius, tool == kToolElasticDeform ? 1 : 0, s_pass,
+                        s_cl, s_coff, ct, sh);
+        const int cnt = sh.cnt, total = sh.total;
+        team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
+        clk.mark(a, rank, kPhCull);
+        if (rank == 0)
+          for (int k = threadIdx.x; k < cnt; k += kTeamThreads) {
+            const int leaf = s_cl[k];
+            const int old = atomicOr(&m.leaf_flag[leaf], kMarkUpdate);
+            if (!(old & kUpdateNormals)) append(m.touch_list, touch_cnt, leaf);
+          }
+        team_bytes(a, kPhBrush, team_orig_sweep(m, b, sh.dp, s_cl, s_coff, cnt, total, gt, GT, tag_cnt));
+        team_sync(cluster, C);
+        clk.mark(a, rank, kPhBrush);
+      }
+      for (int pass = 0; pass < 8 && !uses_original(tool); pass++) {
         if ((pass & ~sh.job.symmetry) != 0) continue;
         PassParams pp;
         for (int k = 0; k < 3; k++) {
@@ -767,10 +859,10 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           pp.view[k] = sgn * sh.job.view[k];
         }
         pp.cull_radius_sq = r * r;
-        pp.original = sh.job.use_orig;
+        pp.original = sh.job.use_orig || tool == kToolLayer;  // layer: stroke-start boxes
         pp.iter_strength = 1.0f;
         pp.iteration = 0;
-        team_cull<kMinBlocks == 1 ? 8 : 2>(m, pp, s_par, s_pass, s_cl, s_coff, ct, sh);
+        team_cull<kMinBlocks == 1 ? 8 : 2>(m, pp, s_pass, s_cl, s_coff, ct, sh);
         const int cnt = sh.cnt, total = sh.total;
         // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
         team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
@@ -817,7 +909,9 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
               const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
               float4 co = __ldcg(&m.co[v]);
               ab += vbytes;
-              if (brush_vertex(m, b, b.y, pp, f, v, co, moved)) {
+              const bool hit = tool == kToolLayer ? layer_vertex(m, b, b.y, pp, v, co, moved)
+                                                  : brush_vertex(m, b, b.y, pp, f, v, co, moved);
+              if (hit) {
                 m.co[v] = co;
                 ab += 12u;
                 if (m.type == kFaces) tag_vertex(m, v, tag_cnt);

@@ -243,8 +243,10 @@ int sgpu_pbvh_node_mark_update(sgpu_mesh *mesh, int node);
  * Per dab: for every enabled symmetry pass the sphere search and the brush,
  * then the normal update and update_bounds(UpdateBB); update_bounds(
  * UpdateOriginalBB) once at the end.  dab_tools (nullable) overrides the tool
- * per dab (mixed strokes).  mode: 0 = launched call by call, 1 = the stroke
- * captured once as a CUDA graph and replayed.  stats may be NULL. */
+ * per dab (mixed strokes).  A stroke with grab, elastic deform or layer dabs
+ * first stores the stroke-start positions and normals (every mode).  mode:
+ * 0 = launched call by call, 1 = the stroke captured once as a CUDA graph and
+ * replayed.  stats may be NULL. */
 #define SGPU_STROKE_EAGER 0
 #define SGPU_STROKE_GRAPH 1
 #define SGPU_STROKE_TEAM 2 /* one persistent launch of the whole stroke (cluster team) */

@@ -1,7 +1,8 @@
 """Grab, elastic deform and layer (the brushes that read the stroke-start
-positions) on the GPU against the oracle, bit for bit: strokes through every path (eager, graph; the persistent
-mode falls back to the graph path for them), per-call dabs after
-sgpu_mesh_store_original, FACES and GRIDS, symmetry, front face and masks.
+positions) on the GPU against the oracle, bit for bit: strokes through every
+path (eager, graph, the persistent stroke kernel, the persistent batch),
+per-call dabs after sgpu_mesh_store_original, FACES and GRIDS, symmetry, front
+face and masks.
 The oracle's Kelvinlet displacement is pinned to the reference's compiled
 kelvinlet.c in test_refpin_kelvinlet.py."""
 import numpy as np
@@ -53,17 +54,18 @@ def test_grab_stroke(gpu, oracle, mode, frontface):
     _assert_equal(g, o, "grab second stroke")
 
 
+@pytest.mark.parametrize("mode", [STROKE_GRAPH, STROKE_TEAM])
 @pytest.mark.parametrize("kind", [0, 1, 2, 3, 4])
-def test_elastic_deform_stroke(gpu, oracle, kind):
+def test_elastic_deform_stroke(gpu, oracle, kind, mode):
     m = small_icosphere(4)
     g, o = _pair(oracle, m, 300)
     st = synth.Stroke(synth.TOOL_ELASTIC_DEFORM, 0.2, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X,
                       synth.grab_dabs(5, 8, 0.015), view_normal=(0.0, 0.6, 0.8),
                       elastic_deform_type=kind, elastic_deform_volume_preservation=0.35)
-    s = g.stroke(st, mode=STROKE_GRAPH)
+    s = g.stroke(st, mode=mode)
     tot, _ = o.stroke(st, which=3)
     assert s.verts_displaced == tot and tot > 0
-    _assert_equal(g, o, f"elastic {kind}")
+    _assert_equal(g, o, f"elastic {kind} mode {mode}")
     assert rel_err(g.positions(), o.co64()) < FP64_TOL
 
 
@@ -90,7 +92,8 @@ def test_layer_stroke(gpu, oracle, mode):
     assert bits_equal(gp.positions(), og.co()), first_diff(gp.positions(), og.co())
 
 
-def test_mixed_stroke_with_grab(gpu, oracle):
+@pytest.mark.parametrize("mode", [STROKE_EAGER, STROKE_TEAM])
+def test_mixed_stroke_with_grab(gpu, oracle, mode):
     """Draw, grab and smooth dabs in one stroke: the grab dabs rebuild their
     leaves from the positions stored at the stroke start."""
     m = small_icosphere(5)
@@ -99,13 +102,14 @@ def test_mixed_stroke_with_grab(gpu, oracle):
     tools = np.array([(synth.TOOL_DRAW, synth.TOOL_GRAB, synth.TOOL_SMOOTH, synth.TOOL_LAYER)[d % 4]
                       for d in range(12)], dtype=np.int32)
     st = synth.Stroke(synth.TOOL_DRAW, 0.2, 0.5, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
-    s = g.stroke(st, mode=STROKE_EAGER, dab_tools=tools)
+    s = g.stroke(st, mode=mode, dab_tools=tools)
     tot, _ = o.stroke(st, which=1, dab_tools=tools)
     assert s.verts_displaced == tot
     _assert_equal(g, o, "mixed")
 
 
-def test_grab_and_elastic_on_grids(gpu, oracle):
+@pytest.mark.parametrize("mode", [STROKE_GRAPH, STROKE_TEAM])
+def test_grab_and_elastic_on_grids(gpu, oracle, mode):
     gr = synth.torus_grids(16, 6, level=4)
     for tool, kind in ((synth.TOOL_GRAB, 0), (synth.TOOL_ELASTIC_DEFORM, 2),
                        (synth.TOOL_ELASTIC_DEFORM, 4)):
@@ -114,7 +118,7 @@ def test_grab_and_elastic_on_grids(gpu, oracle):
         o.recalc_all_normals()
         st = synth.Stroke(tool, 0.3, 0.7, synth.CURVE_SMOOTH, synth.SYMM_X,
                           synth.grab_dabs(9, 6, 0.02, surf_radius=1.3), elastic_deform_type=kind)
-        s = gp.stroke(st, mode=STROKE_GRAPH)
+        s = gp.stroke(st, mode=mode)
         tot, _ = o.stroke(st, which=1)
         assert s.verts_displaced == tot and tot > 0
         assert bits_equal(gp.positions(), o.co()), (tool, kind, first_diff(gp.positions(), o.co()))
@@ -144,9 +148,25 @@ def test_per_call_dabs(gpu, oracle):
         g._brush("sgpu_do_grab_brush", st, dabs[0, :3], dabs[0, 3:], np.array([0], np.int32))
 
 
-def test_batch_rejects_original_brushes(gpu):
-    m = small_icosphere(4)
-    g = PBVH.build_mesh(m, 300)
-    st = synth.Stroke(synth.TOOL_GRAB, 0.2, 0.5, synth.CURVE_SMOOTH, 0, synth.grab_dabs(1, 3, 0.02))
-    with pytest.raises(SculptGPUError):
-        batch_stroke([g], [st], mode=BATCH_TEAM, cluster=4)
+def test_batch_original_brushes(gpu, oracle):
+    """Grab, elastic deform and layer strokes on three meshes in one
+    persistent launch, next to a draw stroke."""
+    m4, m5 = small_icosphere(4), small_icosphere(5)
+    cases = [
+        (m5, 600, synth.Stroke(synth.TOOL_GRAB, 0.25, 0.8, synth.CURVE_SMOOTH, synth.SYMM_X,
+                               synth.grab_dabs(3, 12, 0.02))),
+        (m4, 300, synth.Stroke(synth.TOOL_ELASTIC_DEFORM, 0.2, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X,
+                               synth.grab_dabs(5, 8, 0.015), view_normal=(0.0, 0.6, 0.8),
+                               elastic_deform_type=3, elastic_deform_volume_preservation=0.35)),
+        (m5, 600, synth.Stroke(synth.TOOL_LAYER, 0.15, 0.7, synth.CURVE_SMOOTH, synth.SYMM_X,
+                               synth.arc_dabs(13, 20, 0.04), height=0.3)),
+        (m4, 300, synth.Stroke(synth.TOOL_DRAW, 0.2, 0.5, synth.CURVE_SMOOTH, synth.SYMM_X,
+                               synth.arc_dabs(17, 10, 0.04))),
+    ]
+    pairs = [_pair(oracle, m, ll) for m, ll, _ in cases]
+    stats, _ = batch_stroke([g for g, _ in pairs], [st for _, _, st in cases], mode=BATCH_TEAM,
+                            cluster=4)
+    for (g, o), (_, _, st), s in zip(pairs, cases, stats):
+        tot, _ = o.stroke(st, which=3)
+        assert s.verts_displaced == tot and tot > 0
+        _assert_equal(g, o, f"batch tool {st.tool}")
