@@ -83,7 +83,8 @@ def parse_args():
     ap.add_argument("--draw-mesh", choices=["faces", "grids", "both"], default="both",
                     help="meshes of --draw-only")
     ap.add_argument("--phases", action="store_true",
-                    help="per-phase profile of the persistent stroke on all five workloads "
+                    help="per-phase profile of the persistent stroke on the five workloads "
+                         "and the stroke-start brushes "
                          "(one JSON line each), no report")
     return ap.parse_args()
 
@@ -113,9 +114,9 @@ def run_phases(args):
 
     libbuild.build()
     from dune_sculpt_gb300 import synth
-    from dune_sculpt_gb300.sculpt import PBVH, STROKE_TEAM
+    from dune_sculpt_gb300.sculpt import PBVH, STROKE_GRAPH, STROKE_TEAM
 
-    def one(name, g, st, tools=None):
+    def one(name, g, st, tools=None, graph=False):
         g.snapshot()
         best, _ = g.autotune_team(st, dab_tools=tools)
         times = []
@@ -123,6 +124,14 @@ def run_phases(args):
             g.restore()
             g.flush_l2()
             times.append(g.stroke(st, mode=STROKE_TEAM, dab_tools=tools).gpu_ms)
+        extra = {}
+        if graph:  # the same stroke replayed from a CUDA graph of the per-call kernels
+            gt = []
+            for _ in range(3):
+                g.restore()
+                g.flush_l2()
+                gt.append(g.stroke(st, mode=STROKE_GRAPH, dab_tools=tools).gpu_ms)
+            extra["graph_ms_per_stroke"] = round(min(gt), 3)
         g.restore()
         g.flush_l2()
         ph, _, stats = g.stroke_team_profile(st, dab_tools=tools)
@@ -130,7 +139,7 @@ def run_phases(args):
         print(json.dumps({
             "workload": name, "cluster": best, "ms_per_stroke": round(min(times), 3),
             "us_per_dab": round(1000 * min(times) / nd, 2),
-            "verts_displaced": stats.verts_displaced,
+            "verts_displaced": stats.verts_displaced, **extra,
             "phase_us_per_dab": {k: round(1000 * v["ms"] / nd, 2) for k, v in ph.items()},
             "phase_alg_MB_per_stroke": {k: round(v["bytes"] / 1e6, 2) for k, v in ph.items()}}),
             flush=True)
@@ -147,6 +156,15 @@ def run_phases(args):
                       for d in range(dabs.shape[0])], dtype=np.int32)
     st = synth.Stroke(synth.TOOL_DRAW, 0.04, 0.6, synth.CURVE_SMOOTH, 0, dabs)
     one("multires_torus_50000x17x17_mixed", PBVH.build_grids(g), st, tools)
+    # the stroke-start brushes on the icosphere of the bench workload (128
+    # dabs, X mirror): persistent and graph-replayed
+    m, st, ll = synth.cfg2_icosphere_smooth()
+    grab = synth.grab_dabs(synth.SEED_BASE + 40, st.dabs.shape[0], 0.0005)
+    for name, tool, dabs, kw in (
+            ("grab", synth.TOOL_GRAB, grab, {}),
+            ("layer", synth.TOOL_LAYER, st.dabs, {"height": 0.3})):
+        so = synth.Stroke(tool, st.radius, st.strength, synth.CURVE_SMOOTH, synth.SYMM_X, dabs, **kw)
+        one(f"icosphere8_{name}_xmirror", PBVH.build_mesh(m, ll), so, graph=True)
     return 0
 
 

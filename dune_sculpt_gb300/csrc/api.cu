@@ -395,6 +395,16 @@ bool tool_ok(int tool) {
          tool == kToolGrab || tool == kToolElasticDeform || tool == kToolLayer;
 }
 
+// Elastic deform moves every vertex of the mesh in every dab: the per-call
+// kernels spread that sweep over the whole GPU, the persistent kernel over one
+// cluster (measured about 8x slower on a 655k-vertex mesh), so single-mesh
+// strokes with such dabs take the graph path.
+bool stroke_has_whole_mesh(const SGPU_Brush* brush, const int* dab_tools, int ndabs) {
+  for (int d = 0; d < ndabs; d++)
+    if ((dab_tools ? dab_tools[d] : brush->sculpt_tool) == kToolElasticDeform) return true;
+  return false;
+}
+
 bool stroke_has_original(const SGPU_Brush* brush, const int* dab_tools, int ndabs) {
   for (int d = 0; d < ndabs; d++)
     if (needs_stroke_start(dab_tools ? dab_tools[d] : brush->sculpt_tool)) return true;
@@ -1139,6 +1149,8 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   if (brush->symmetry < 0 || brush->symmetry > 7)
     return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
+  if (mode == SGPU_STROKE_TEAM && stroke_has_whole_mesh(brush, dab_tools, ndabs))
+    mode = SGPU_STROKE_GRAPH;
   if (mode == SGPU_STROKE_TEAM) {
     const int offs[2] = {0, ndabs};
     sgpu_mesh* one[1] = {mesh};
@@ -1315,6 +1327,8 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
   if (!verts_in || !verts_out) return fail(SGPU_ERR_INVALID_ARG, "NULL host buffers");
   if (mode != SGPU_STROKE_EAGER && mode != SGPU_STROKE_GRAPH && mode != SGPU_STROKE_TEAM)
     return fail(SGPU_ERR_INVALID_ARG, "unknown stroke mode %d", mode);
+  if (mode == SGPU_STROKE_TEAM && stroke_has_whole_mesh(brush, dab_tools, ndabs))
+    mode = SGPU_STROKE_GRAPH;
   if (!mesh->ev_h0) {
     CK(cudaEventCreate(&mesh->ev_h0), "cudaEventCreate");
     CK(cudaEventCreate(&mesh->ev_h1), "cudaEventCreate");

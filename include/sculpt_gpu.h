@@ -249,7 +249,9 @@ int sgpu_pbvh_node_mark_update(sgpu_mesh *mesh, int node);
  * replayed.  stats may be NULL. */
 #define SGPU_STROKE_EAGER 0
 #define SGPU_STROKE_GRAPH 1
-#define SGPU_STROKE_TEAM 2 /* one persistent launch of the whole stroke (cluster team) */
+/* 2: one persistent launch of the whole stroke (cluster team); a stroke with
+ * elastic deform dabs (every vertex moves in every dab) runs as mode 1 */
+#define SGPU_STROKE_TEAM 2
 int sgpu_stroke(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, int ndabs,
                 const int *dab_tools, int mode, SGPU_StrokeStats *stats);
 

@@ -1,6 +1,7 @@
 """Grab, elastic deform and layer (the brushes that read the stroke-start
 positions) on the GPU against the oracle, bit for bit: strokes through every
-path (eager, graph, the persistent stroke kernel, the persistent batch),
+path (eager, graph, the persistent stroke kernel — elastic deform strokes of
+one mesh take the graph path there — and the persistent batch),
 per-call dabs after sgpu_mesh_store_original, FACES and GRIDS, symmetry, front
 face and masks.
 The oracle's Kelvinlet displacement is pinned to the reference's compiled
@@ -149,8 +150,9 @@ def test_per_call_dabs(gpu, oracle):
 
 
 def test_batch_original_brushes(gpu, oracle):
-    """Grab, elastic deform and layer strokes on three meshes in one
-    persistent launch, next to a draw stroke."""
+    """Grab, elastic deform and layer strokes in one persistent launch, next
+    to a draw stroke (single-mesh elastic deform strokes take the graph path,
+    so the batch is where the persistent kernel runs them)."""
     m4, m5 = small_icosphere(4), small_icosphere(5)
     cases = [
         (m5, 600, synth.Stroke(synth.TOOL_GRAB, 0.25, 0.8, synth.CURVE_SMOOTH, synth.SYMM_X,
@@ -162,6 +164,9 @@ def test_batch_original_brushes(gpu, oracle):
                                synth.arc_dabs(13, 20, 0.04), height=0.3)),
         (m4, 300, synth.Stroke(synth.TOOL_DRAW, 0.2, 0.5, synth.CURVE_SMOOTH, synth.SYMM_X,
                                synth.arc_dabs(17, 10, 0.04))),
+        (m4, 300, synth.Stroke(synth.TOOL_ELASTIC_DEFORM, 0.25, 0.4, synth.CURVE_SMOOTH, 0,
+                               synth.grab_dabs(19, 6, 0.02), elastic_deform_type=1,
+                               elastic_deform_volume_preservation=0.2)),
     ]
     pairs = [_pair(oracle, m, ll) for m, ll, _ in cases]
     stats, _ = batch_stroke([g for g, _ in pairs], [st for _, _, st in cases], mode=BATCH_TEAM,
