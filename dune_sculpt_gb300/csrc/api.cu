@@ -1872,6 +1872,8 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.jobs = m0->t_jobs;
   a.njobs = n;
   a.next_job = m0->t_counter;
+  a.orig = 0;
+  for (int i = 0; i < n; i++) a.orig |= h_orig[i];
   a.max_nodes = max_nodes;
   a.max_leaves = max_leaves;
   a.prof_bytes = g_team_prof_bytes;

@@ -702,7 +702,9 @@ struct PhaseClock {
 
 // Two builds of the kernel: one CTA per SM with the full register file (the
 // fastest single strokes), or two CTAs per SM (twice the teams for batches).
-template <int kMinBlocks>
+// kOrig: the build that also runs grab, elastic deform and layer dabs (the
+// other build carries none of their code).
+template <int kMinBlocks, bool kOrig>
 __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamArgs a) {
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned C = cluster.num_blocks();
@@ -812,7 +814,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       const float r = b.radius * scale;
       int* tag_cnt = &w->tag_count[par];
       int* touch_cnt = &w->touch_count[par];
-      if (uses_original(tool)) {
+      if (kOrig && uses_original(tool)) {
         // grab / elastic deform: one gather over all passes, then each vertex
         // rebuilt from its stroke-start position (k_cull_dab, k_orig_dab)
         if (threadIdx.x == 0) {
@@ -849,7 +851,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         team_sync(cluster, C);
         clk.mark(a, rank, kPhBrush);
       }
-      for (int pass = 0; pass < 8 && !uses_original(tool); pass++) {
+      for (int pass = 0; pass < 8 && !(kOrig && uses_original(tool)); pass++) {
         if ((pass & ~sh.job.symmetry) != 0) continue;
         PassParams pp;
         for (int k = 0; k < 3; k++) {
@@ -859,7 +861,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           pp.view[k] = sgn * sh.job.view[k];
         }
         pp.cull_radius_sq = r * r;
-        pp.original = sh.job.use_orig || tool == kToolLayer;  // layer: stroke-start boxes
+        pp.original = sh.job.use_orig || (kOrig && tool == kToolLayer);  // layer: stroke-start boxes
         pp.iter_strength = 1.0f;
         pp.iteration = 0;
         team_cull<kMinBlocks == 1 ? 8 : 2>(m, pp, s_pass, s_cl, s_coff, ct, sh);
@@ -909,7 +911,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
               const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
               float4 co = __ldcg(&m.co[v]);
               ab += vbytes;
-              const bool hit = tool == kToolLayer ? layer_vertex(m, b, b.y, pp, v, co, moved)
+              const bool hit = (kOrig && tool == kToolLayer) ? layer_vertex(m, b, b.y, pp, v, co, moved)
                                                   : brush_vertex(m, b, b.y, pp, f, v, co, moved);
               if (hit) {
                 m.co[v] = co;
@@ -1214,12 +1216,19 @@ size_t team_smem_bytes(int max_nodes, int max_leaves) {
 
 int team_max_cluster() { return 16; }
 
+template <int kMinBlocks, bool kOrig>
+cudaError_t configure_team_build(size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_team_stroke<kMinBlocks, kOrig>,
+                                       cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_team_stroke<kMinBlocks, kOrig>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+}
+
 template <int kMinBlocks>
 cudaError_t configure_team_kernel(size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_team_stroke<kMinBlocks>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_team_stroke<kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(smem));
+  const cudaError_t e = configure_team_build<kMinBlocks, false>(smem);
+  return e != cudaSuccess ? e : configure_team_build<kMinBlocks, true>(smem);
 }
 
 static cudaLaunchConfig_t team_config(int cluster, int nteams, size_t smem, cudaStream_t s,
@@ -1262,7 +1271,8 @@ static int active_clusters(int cluster, size_t smem) {
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = team_config(cluster, 1, smem, nullptr, attr);
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_team_stroke<kMinBlocks>, &cfg) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_team_stroke<kMinBlocks, false>, &cfg) != cudaSuccess)
+    return 0;
   cache[key] = n;
   return n;
 }
@@ -1281,8 +1291,11 @@ cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s) {
   const int nteams = std::max(1, std::min(a.njobs, wide ? n2 : n1));
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = team_config(cluster, nteams, smem, s, attr);
-  if (wide) return cudaLaunchKernelEx(&cfg, k_team_stroke<2>, a);
-  return cudaLaunchKernelEx(&cfg, k_team_stroke<1>, a);
+  if (wide)
+    return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<2, true>, a)
+                  : cudaLaunchKernelEx(&cfg, k_team_stroke<2, false>, a);
+  return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true>, a)
+                : cudaLaunchKernelEx(&cfg, k_team_stroke<1, false>, a);
 }
 
 }  // namespace sgpu

@@ -25,6 +25,7 @@ struct TeamArgs {
   const TeamJob* jobs;
   int njobs;
   int* next_job;  // job counter, zero at launch
+  int orig;       // some job has grab, elastic deform or layer dabs
   int max_nodes, max_leaves;  // shared-memory sizing over the meshes
   // profiling (nullable): algorithmic bytes and nanoseconds per phase
   unsigned long long* prof_bytes;  // kTeamPhases entries
