@@ -175,3 +175,23 @@ def test_batch_original_brushes(gpu, oracle):
         tot, _ = o.stroke(st, which=3)
         assert s.verts_displaced == tot and tot > 0
         _assert_equal(g, o, f"batch tool {st.tool}")
+
+
+@pytest.mark.parametrize("tool", [synth.TOOL_GRAB, synth.TOOL_LAYER, synth.TOOL_ELASTIC_DEFORM])
+def test_stroke_host_original_brushes(gpu, oracle, tool):
+    """sgpu_stroke_host in persistent mode: the uploaded positions become the
+    stroke-start positions (elastic deform runs as a graph replay there)."""
+    m = small_icosphere(5)
+    g, o = _pair(oracle, m, 600)
+    dabs = synth.arc_dabs(13, 20, 0.04) if tool == synth.TOOL_LAYER else synth.grab_dabs(3, 12, 0.02)
+    st = synth.Stroke(tool, 0.2, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X, dabs, height=0.3,
+                      elastic_deform_type=2)
+    vin = m.verts.copy()
+    vout = np.zeros_like(vin)
+    nin = np.ascontiguousarray(g.normals(), dtype=np.float32)
+    s = g.stroke_host(st, vin, vout, nin, mode=STROKE_TEAM)
+    tot, _ = o.stroke(st, which=3)
+    assert s.verts_displaced == tot and tot > 0
+    co = np.ascontiguousarray(vout["co"])
+    assert bits_equal(co, o.co()), first_diff(co, o.co())
+    _assert_equal(g, o, f"stroke_host tool {tool}")
