@@ -19,6 +19,7 @@
 #include "sgpu_team.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 
 using namespace sgpu;
@@ -48,6 +49,23 @@ int cuda_fail(cudaError_t e, const char* what) {
     cudaError_t _e = (expr);                        \
     if (_e != cudaSuccess) return cuda_fail(_e, what); \
   } while (0)
+
+// Host-side test hooks (sgpu_debug_inject).  g_inject_alloc > 0: the mesh
+// allocation that brings it to zero fails as out of memory.  g_wait_ns: the
+// whole-GPU team's barrier wait limit.  g_bar_extra: arrivals its barriers
+// wait for beyond the launch's CTAs (1 makes every wait run out).
+constexpr unsigned long long kDefaultWaitNs = 2000000000ull;
+std::atomic<long long> g_inject_alloc{0};
+std::atomic<unsigned long long> g_wait_ns{kDefaultWaitNs};
+std::atomic<int> g_bar_extra{0};
+
+bool injected_alloc_failure() {
+  long long n = g_inject_alloc.load();
+  while (n > 0) {
+    if (g_inject_alloc.compare_exchange_weak(n, n - 1)) return n == 1;
+  }
+  return false;
+}
 
 }  // namespace
 
@@ -146,6 +164,8 @@ struct sgpu_mesh {
   int alloc(T** out, size_t count) {
     void* p = nullptr;
     const size_t bytes = (count > 0 ? count : 1) * sizeof(T);
+    if (injected_alloc_failure())
+      return fail(SGPU_ERR_OOM, "cudaMalloc: injected allocation failure (test hook)");
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     allocs.push_back(p);
@@ -316,8 +336,8 @@ int upload_pbvh(sgpu_mesh* m) {
     m->nchunks = choff[L];
   }
   // smooth slot arrays: the persistent kernel's per-CTA slot ranges may end
-  // up to 32 entries per CTA (at most 16 CTAs) past the vertex count
-  const size_t nslot = static_cast<size_t>(h.totvert) + 32 * 16;
+  // up to 32 entries per CTA of the team past the vertex count
+  const size_t nslot = static_cast<size_t>(h.totvert) + 32 * static_cast<size_t>(kTeamMaxWideCtas);
   if ((rc = m->alloc(&d.hit_list[0], nslot))) return rc;
   if ((rc = m->alloc(&d.hit_list[1], static_cast<size_t>(h.totvert)))) return rc;
   if ((rc = m->alloc(&d.tag_list, static_cast<size_t>(h.totvert)))) return rc;
@@ -396,9 +416,10 @@ bool tool_ok(int tool) {
 }
 
 // Elastic deform moves every vertex of the mesh in every dab: the per-call
-// kernels spread that sweep over the whole GPU, the persistent kernel over one
+// kernels spread that sweep over the whole GPU, a cluster team over one
 // cluster (measured about 8x slower on a 655k-vertex mesh), so single-mesh
-// strokes with such dabs take the graph path.
+// strokes with such dabs on a cluster team take the graph path; the
+// whole-GPU team keeps them.
 bool stroke_has_whole_mesh(const SGPU_Brush* brush, const int* dab_tools, int ndabs) {
   for (int d = 0; d < ndabs; d++)
     if ((dab_tools ? dab_tools[d] : brush->sculpt_tool) == kToolElasticDeform) return true;
@@ -1149,7 +1170,8 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   if (brush->symmetry < 0 || brush->symmetry > 7)
     return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
-  if (mode == SGPU_STROKE_TEAM && stroke_has_whole_mesh(brush, dab_tools, ndabs))
+  if (mode == SGPU_STROKE_TEAM && mesh->team_cluster != SGPU_TEAM_GRID &&
+      stroke_has_whole_mesh(brush, dab_tools, ndabs))
     mode = SGPU_STROKE_GRAPH;
   if (mode == SGPU_STROKE_TEAM) {
     const int offs[2] = {0, ndabs};
@@ -1204,10 +1226,29 @@ int sgpu_mesh_set_team(sgpu_mesh* mesh, int cluster_size) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   if (cluster_size != 1 && cluster_size != 2 && cluster_size != 4 && cluster_size != 8 &&
-      cluster_size != 16)
-    return fail(SGPU_ERR_INVALID_ARG, "cluster size must be 1, 2, 4, 8 or 16");
+      cluster_size != 16 && cluster_size != SGPU_TEAM_GRID)
+    return fail(SGPU_ERR_INVALID_ARG, "cluster size must be 1, 2, 4, 8, 16 or SGPU_TEAM_GRID");
   mesh->team_cluster = cluster_size;
   return SGPU_OK;
+}
+
+int sgpu_debug_inject(int what, int64_t value) {
+  switch (what) {
+    case SGPU_INJECT_ALLOC_FAIL:
+      if (value < 0) return fail(SGPU_ERR_INVALID_ARG, "allocation count must be >= 0");
+      g_inject_alloc.store(value);
+      return SGPU_OK;
+    case SGPU_INJECT_WAIT_NS:
+      if (value < 0) return fail(SGPU_ERR_INVALID_ARG, "wait limit must be >= 0");
+      g_wait_ns.store(value > 0 ? static_cast<unsigned long long>(value) : kDefaultWaitNs);
+      return SGPU_OK;
+    case SGPU_INJECT_BARRIER_EXTRA:
+      if (value < 0 || value > 1) return fail(SGPU_ERR_INVALID_ARG, "barrier extra must be 0 or 1");
+      g_bar_extra.store(static_cast<int>(value));
+      return SGPU_OK;
+    default:
+      return fail(SGPU_ERR_INVALID_ARG, "unknown injection hook %d", what);
+  }
 }
 
 int sgpu_mesh_get_team(const sgpu_mesh* mesh, int* cluster_size) {
@@ -1327,7 +1368,8 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
   if (!verts_in || !verts_out) return fail(SGPU_ERR_INVALID_ARG, "NULL host buffers");
   if (mode != SGPU_STROKE_EAGER && mode != SGPU_STROKE_GRAPH && mode != SGPU_STROKE_TEAM)
     return fail(SGPU_ERR_INVALID_ARG, "unknown stroke mode %d", mode);
-  if (mode == SGPU_STROKE_TEAM && stroke_has_whole_mesh(brush, dab_tools, ndabs))
+  if (mode == SGPU_STROKE_TEAM && mesh->team_cluster != SGPU_TEAM_GRID &&
+      stroke_has_whole_mesh(brush, dab_tools, ndabs))
     mode = SGPU_STROKE_GRAPH;
   if (!mesh->ev_h0) {
     CK(cudaEventCreate(&mesh->ev_h0), "cudaEventCreate");
@@ -1376,7 +1418,12 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
                        mesh->stream),
        "read counter");
   CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
-  if (mode == SGPU_STROKE_TEAM) displaced = mesh->h_disp[0];
+  if (mode == SGPU_STROKE_TEAM) {
+    displaced = mesh->h_disp[0];
+    if (const int status = static_cast<int>(mesh->h_disp[1]))
+      return fail(status, "persistent stroke kernel: a team barrier wait ran out (error %d); the "
+                  "stroke is incomplete", status);
+  }
   if ((rc = device_err(mesh))) return rc;
   if (stats) {
     float ms = 0.0f;
@@ -1807,9 +1854,21 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   }
   if (max_leaves > 64 * 256 || team_smem_bytes(max_nodes, max_leaves) > 160 * 1024)
     return fail(SGPU_ERR_UNSUPPORTED, "PBVH too large for the persistent stroke kernel");
-  const int nteams_max = team_max_active_clusters(cluster, max_nodes, max_leaves);
-  if (nteams_max <= 0)
+  const bool wide = cluster == SGPU_TEAM_GRID;
+  int wide_ctas = 0;
+  if (wide) {
+    wide_ctas = team_wide_ctas(max_nodes, max_leaves);
+    if (wide_ctas <= 0)
+      return fail(SGPU_ERR_UNSUPPORTED, "the whole-GPU team cannot be launched on this device");
+    // the barrier counter holds (barriers so far) * CTAs below its abort bit:
+    // at most 8 passes of at most 8 barriers per dab, plus 8 per stroke
+    double barriers = 0.0;
+    for (int i = 0; i < n; i++) barriers += 64.0 * (offs[i + 1] - offs[i]) + 8.0;
+    if (barriers * (wide_ctas + 1) >= 2147483648.0)
+      return fail(SGPU_ERR_UNSUPPORTED, "too many dabs for one whole-GPU launch");
+  } else if (team_max_active_clusters(cluster, max_nodes, max_leaves) <= 0) {
     return fail(SGPU_ERR_UNSUPPORTED, "cluster size %d cannot be launched", cluster);
+  }
   // staging buffers live on the first mesh; re-create when too small
   static thread_local std::vector<DevMesh> h_meshes;
   static thread_local std::vector<TeamJob> h_jobs;
@@ -1820,7 +1879,8 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   if (tools && (rc = ensure_dev(&m0->t_tools, &m0->t_tool_cap, ndab))) return rc;
   if ((rc = ensure_dev(&m0->t_meshes, &m0->t_mesh_cap, static_cast<size_t>(n)))) return rc;
   if ((rc = ensure_dev(&m0->t_jobs, &m0->t_job_cap, static_cast<size_t>(n)))) return rc;
-  if ((rc = ensure_dev(&m0->t_counter, &m0->t_counter_cap, 1))) return rc;
+  // [0] job counter, [1] whole-GPU barrier counter, [2] status word
+  if ((rc = ensure_dev(&m0->t_counter, &m0->t_counter_cap, 4))) return rc;
   std::vector<int> order(n);
   std::vector<double> est(n);
   for (int i = 0; i < n; i++) {
@@ -1863,7 +1923,7 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
      "upload mesh table");
   CK(cudaMemcpyAsync(m0->t_jobs, h_jobs.data(), sizeof(TeamJob) * n, cudaMemcpyHostToDevice, s),
      "upload jobs");
-  CK(cudaMemsetAsync(m0->t_counter, 0, sizeof(int), s), "reset job counter");
+  CK(cudaMemsetAsync(m0->t_counter, 0, 3 * sizeof(int), s), "reset job and barrier counters");
   for (int i = 0; i < n; i++)
     CK(cudaMemsetAsync(&meshes[i]->dev.work->displaced, 0, sizeof(unsigned long long), s),
        "reset counter");
@@ -1878,26 +1938,40 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.max_leaves = max_leaves;
   a.prof_bytes = g_team_prof_bytes;
   a.phase_ns = g_team_phase_ns;
-  CK(launch_team_stroke(a, cluster, s), "persistent stroke kernel");
+  a.bar = reinterpret_cast<unsigned int*>(m0->t_counter + 1);
+  a.status = m0->t_counter + 2;
+  a.wait_ns = g_wait_ns.load();
+  a.bar_extra = g_bar_extra.load();
+  if (wide) {
+    CK(launch_team_stroke_wide(a, wide_ctas, s), "persistent stroke kernel (whole GPU)");
+  } else {
+    CK(launch_team_stroke(a, cluster, s), "persistent stroke kernel");
+  }
   CK(cudaEventRecord(m0->ev1, s), "event");
-  if (m0->h_disp_cap < static_cast<size_t>(n)) {
+  // page-locked: n displaced counters, then the status word
+  if (m0->h_disp_cap < static_cast<size_t>(n) + 1) {
     if (m0->h_disp) cudaFreeHost(m0->h_disp);
     m0->h_disp = nullptr;
     m0->h_disp_cap = 0;
-    CK(cudaHostAlloc(reinterpret_cast<void**>(&m0->h_disp), sizeof(unsigned long long) * n,
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&m0->h_disp), sizeof(unsigned long long) * (n + 1),
                      cudaHostAllocDefault),
        "cudaHostAlloc");
-    m0->h_disp_cap = static_cast<size_t>(n);
+    m0->h_disp_cap = static_cast<size_t>(n) + 1;
   }
   unsigned long long* disp = m0->h_disp;
   for (int i = 0; i < n; i++)
     CK(cudaMemcpyAsync(&disp[i], &meshes[i]->dev.work->displaced, sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, s),
        "read counter");
+  disp[n] = 0ull;
+  CK(cudaMemcpyAsync(&disp[n], a.status, sizeof(int), cudaMemcpyDeviceToHost, s), "read status");
   if (!wait) return SGPU_OK;
   CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   float ms = 0.0f;
   CK(cudaEventElapsedTime(&ms, m0->ev0, m0->ev1), "elapsed");
+  if (const int status = static_cast<int>(disp[n]))
+    return fail(status, "persistent stroke kernel: a team barrier wait ran out (error %d); the "
+                "stroke is incomplete", status);
   for (int i = 0; i < n; i++) {
     if ((rc = device_err(meshes[i]))) return rc;
     if (stats) {

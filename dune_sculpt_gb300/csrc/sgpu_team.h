@@ -25,6 +25,13 @@ struct TeamArgs {
   const TeamJob* jobs;
   int njobs;
   int* next_job;  // job counter, zero at launch
+  // whole-GPU team: barrier counter (zero at launch), status word (zero at
+  // launch; SGPU_ERR_TIMEOUT when a barrier wait ran out), the wait limit,
+  // and extra arrivals the barrier waits for (0; a test hook sets 1)
+  unsigned int* bar;
+  int* status;
+  unsigned long long wait_ns;
+  int bar_extra;
   int orig;       // some job has grab, elastic deform or layer dabs
   int max_nodes, max_leaves;  // shared-memory sizing over the meshes
   // profiling (nullable): algorithmic bytes and nanoseconds per phase
@@ -49,5 +56,11 @@ int team_max_cluster();
 int team_max_active_clusters(int cluster, int max_nodes, int max_leaves);
 // Launches min(njobs, resident teams) teams of the build that holds the most.
 cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s);
+// The whole-GPU team: CTAs of one cooperative launch (one per SM), or 0 when
+// the device or the shared-memory size does not allow it.
+int team_wide_ctas(int max_nodes, int max_leaves);
+// Upper bound of team_wide_ctas on any device (sizes the smooth slot arrays).
+constexpr int kTeamMaxWideCtas = 1024;
+cudaError_t launch_team_stroke_wide(const TeamArgs& a, int nctas, cudaStream_t s);
 
 }  // namespace sgpu

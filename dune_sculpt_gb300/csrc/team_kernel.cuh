@@ -1,0 +1,1303 @@
+// Persistent stroke kernel of libsculptgpu (device code).  kernels_team.cu
+// launches it as cluster teams, kernels_wide.cu as one team over the whole
+// GPU.
+//
+// One launch runs whole strokes.  A team (a thread-block cluster of C CTAs of
+// 256 threads, C chosen by the autotuner, or every CTA of a cooperative launch
+// with one CTA per SM) takes a mesh's stroke and runs every dab of it: per
+// symmetry pass the node search, the area normal/centre, the brush (smooth as
+// Jacobi sweeps over a compacted list of vertices inside the sphere), then
+// the normal update and the bounding-box refit with its flush;
+// UpdateOriginalBB at the end of the stroke.  Phases are separated by team
+// barriers: barrier.cluster arrive.release / wait.acquire for a cluster, a
+// counter in global memory (release add, bounded wait, acquire fence) for the
+// whole GPU, so no phase waits for a kernel boundary.  Cluster teams take
+// meshes from a work queue (an atomic job counter); meshes are independent,
+// teams never wait for one another, and a team that starts late simply finds
+// fewer jobs.  The whole-GPU team runs its jobs in order.
+//
+// The arithmetic is the same device code as the per-call kernels
+// (sgpu_device.cuh), so results are bit-identical to them and to the FP32
+// restatement of the reference.
+#pragma once
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "sgpu_device.cuh"
+#include "sgpu_grids.cuh"
+#include "sgpu_kernels.h"
+#include "sgpu_team.h"
+
+namespace cg = cooperative_groups;
+
+namespace sgpu {
+
+constexpr int kTeamThreads = 256;
+
+struct TeamShared {
+  DevMesh m;
+  TeamJob job;
+  int jobid;
+  int cnt, total;
+  int scan[32];
+  unsigned long long scan64[32];
+  int nh;                  // smooth hits of this CTA in the current pass
+  int hv[kTeamThreads];    // their vertices and positions (first kTeamThreads)
+  float4 hco[kTeamThreads];
+  float area[6];
+  int nmark;
+  int bar_ok;    // outcome of the whole-GPU team barrier's wait
+  DabPasses dp;  // passes of a grab / elastic deform dab
+};
+
+// Block-wide exclusive scan (kTeamThreads threads).
+static __device__ int team_block_scan(int v, int* total, int* smem32) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nwarps = kTeamThreads / 32;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem32[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < nwarps ? smem32[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    smem32[lane] = w;
+  }
+  __syncthreads();
+  const int warp_base = warp > 0 ? smem32[warp - 1] : 0;
+  *total = smem32[nwarps - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+__device__ __forceinline__ bool box_hits(float4 mn, float4 mx, const float* c, float rsq) {
+  const float bmin[3] = {mn.x, mn.y, mn.z};
+  const float bmax[3] = {mx.x, mx.y, mx.z};
+  float t[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    float nearest;
+    if (bmin[i] > c[i]) {
+      nearest = bmin[i];
+    } else if (bmax[i] < c[i]) {
+      nearest = bmax[i];
+    } else {
+      nearest = c[i];
+    }
+    t[i] = c[i] - nearest;
+  }
+  return (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]) < rsq;
+}
+
+__device__ __forceinline__ int smem_find_slot(const int* off, int cnt, int i) {
+  int lo = 0, hi = cnt;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= i) {
+      lo = mid;
+    } else {
+      hi = mid;
+    }
+  }
+  return lo;
+}
+
+// Appends v to list (counter cnt) with one atomic per coalesced group.
+__device__ __forceinline__ void append(int* list, int* cnt, int v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(cnt, static_cast<int>(g.size()));
+  base = g.shfl(base, 0);
+  list[base + g.thread_rank()] = v;
+}
+
+__device__ __forceinline__ void tag_vertex(const DevMesh& m, int v, int* tag_cnt) {
+  if (atomicExch(&m.vtag[v], 1u) == 0u) append(m.tag_list, tag_cnt, v);
+}
+
+// Block-wide exclusive scan of 64-bit values (kTeamThreads threads).
+static __device__ unsigned long long team_block_scan64(unsigned long long v, unsigned long long* total,
+                                                unsigned long long* smem32) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nwarps = kTeamThreads / 32;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem32[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < nwarps ? smem32[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    smem32[lane] = w;
+  }
+  __syncthreads();
+  const unsigned long long warp_base = warp > 0 ? smem32[warp - 1] : 0ull;
+  *total = smem32[nwarps - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+// Per-job tables of the node search in shared memory.
+struct CullTabs {
+  const unsigned short* lnode;  // leaf -> node
+  const int* lnv;               // leaf -> brush-visible vertex count
+};
+
+// Node search of one pass into this CTA's shared memory (every CTA of the team
+// computes the same list).  Same result and order as k_cull: a leaf is listed
+// when its box and the boxes of all its ancestors pass.  Every node box is
+// tested (kBox loads in flight per thread); a failing internal node covers
+// the leaf-id range of its subtree (left-first DFS ranks), recorded as +1/-1
+// in a difference array; a running sum over the leaves then says which
+// leaves lie under a failing ancestor.  Each thread owns a run of consecutive
+// leaves (at most 64: the team kernel takes at most 64 * 256 leaves); block
+// scans give the coverage entering the run and the list positions.  s_coff
+// doubles as the difference array.
+template <int kBox, class Hit>
+__device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb, Hit hits,
+                                             unsigned char* s_pass, int* s_cl, int* s_coff,
+                                             const CullTabs& ct, TeamShared& sh) {
+  const int L = m.nleaf;
+  for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
+  __syncthreads();
+  for (int n0 = threadIdx.x; n0 < m.totnode; n0 += kBox * kTeamThreads) {
+    float4 lo[kBox], hi[kBox];
+    int llo[kBox], lhi[kBox];
+#pragma unroll
+    for (int j = 0; j < kBox; j++) {
+      const int n = n0 + j * kTeamThreads;
+      if (n < m.totnode) {
+        lo[j] = __ldcg(&bb[2 * n]);
+        hi[j] = __ldcg(&bb[2 * n + 1]);
+        llo[j] = m.node_leaf_lo[n];
+        lhi[j] = m.node_leaf_hi[n];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kBox; j++) {
+      const int n = n0 + j * kTeamThreads;
+      if (n >= m.totnode) continue;
+      const bool hit = hits(lo[j], hi[j]);
+      s_pass[n] = hit;
+      if (!hit && lhi[j] - llo[j] > 1) {  // internal node (leaves own a range of one)
+        atomicAdd(&s_coff[llo[j]], 1);
+        atomicAdd(&s_coff[lhi[j]], -1);
+      }
+    }
+  }
+  __syncthreads();
+  const int seg = (L + kTeamThreads - 1) / kTeamThreads;
+  const int l0 = min(L, static_cast<int>(threadIdx.x) * seg), l1 = min(L, l0 + seg);
+  int dsum = 0;
+  for (int id = l0; id < l1; id++) dsum += s_coff[id];
+  int dtot;
+  int cov = team_block_scan(dsum, &dtot, sh.scan);
+  unsigned long long okmask = 0ull;
+  unsigned long long cnt = 0ull, nvs = 0ull;
+  for (int id = l0; id < l1; id++) {
+    cov += s_coff[id];
+    if (cov == 0 && s_pass[ct.lnode[id]]) {
+      cnt++;
+      nvs += static_cast<unsigned long long>(ct.lnv[id]);
+      okmask |= 1ull << (id - l0);
+    }
+  }
+  // (vertex count << 24) | leaf count: leaves < 2^24, vertices < 2^31
+  unsigned long long total;
+  const unsigned long long excl = team_block_scan64((nvs << 24) | cnt, &total, sh.scan64);
+  // the scan's barriers separate the reads of s_coff above from the writes below
+  int pos = static_cast<int>(excl & 0xFFFFFFull);
+  int voff = static_cast<int>(excl >> 24);
+  for (int id = l0; id < l1; id++) {
+    if (!((okmask >> (id - l0)) & 1ull)) continue;
+    s_cl[pos] = id;
+    s_coff[pos] = voff;
+    pos++;
+    voff += ct.lnv[id];
+  }
+  if (threadIdx.x == 0) {
+    sh.cnt = static_cast<int>(total & 0xFFFFFFull);
+    sh.total = static_cast<int>(total >> 24);
+    s_coff[sh.cnt] = sh.total;
+  }
+  __syncthreads();
+}
+
+// The sweep of one grab / elastic deform dab over the gathered leaves (every
+// CTA of the team, strided by GT threads); returns the algorithmic bytes.
+__device__ __forceinline__ unsigned long long team_orig_sweep(const DevMesh& m, const DevBrush& b,
+                                                           const DabPasses& dp, const int* s_cl,
+                                                           const int* s_coff, int cnt, int total,
+                                                           int gt, int GT, int* tag_cnt) {
+  // index, original position (+ normal for the front face), mask, automask; position write
+  const unsigned vbytes = (m.type == kFaces ? 4u : 0u) + 12u +
+                          ((b.flag & kBrushFrontFace) ? 12u : 0u) + (m.mask ? 4u : 0u) +
+                          (m.automask ? 4u : 0u) + 12u;
+  const int lane = threadIdx.x & 31;
+  unsigned long long ab = 0;
+  for (int base = gt - lane; base < total; base += GT) {
+    const int i = base + lane;
+    unsigned int moved = 0u;
+    if (i < total) {
+      const int k = smem_find_slot(s_coff, cnt, i);
+      const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+      float4 co = __ldcg(&m.co[v]);
+      moved = orig_vertex(m, b, b.y, dp, v, co);
+      m.co[v] = co;
+      ab += vbytes;
+      if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+    }
+    const unsigned int sum = __reduce_add_sync(0xffffffffu, moved);
+    if (lane == 0 && sum) atomicAdd(&m.work->displaced, (unsigned long long)sum);
+  }
+  return ab;
+}
+
+// The node search of one pass (sphere at the pass location).
+template <int kBox>
+__device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char* s_pass,
+                          int* s_cl, int* s_coff, const CullTabs& ct, TeamShared& sh) {
+  team_cull_by<kBox>(
+      m, pp.original ? m.orig_vb : m.vb,
+      [&](float4 lo, float4 hi) { return box_hits(lo, hi, pp.loc, pp.cull_radius_sq); }, s_pass,
+      s_cl, s_coff, ct, sh);
+}
+
+// The gather of one grab / elastic deform dab (k_cull_dab): orig_vb boxes that
+// meet any pass sphere, or every leaf (all != 0).
+__device__ __forceinline__ void team_cull_union(const DevMesh& m, const DabPasses& dp, float rsq,
+                                             int all, unsigned char* s_pass, int* s_cl,
+                                             int* s_coff, const CullTabs& ct, TeamShared& sh) {
+  team_cull_by<2>(
+      m, m.orig_vb,
+      [&](float4 lo, float4 hi) {
+        bool ok = all != 0;
+        for (int p = 0; p < dp.npass && !ok; p++) ok = box_hits(lo, hi, dp.loc[p], rsq);
+        return ok;
+      },
+      s_pass, s_cl, s_coff, ct, sh);
+}
+
+constexpr int kFlushTab = 128;  // ancestors whose boxes stay on chip
+constexpr unsigned short kNoPos = 0xFFFFu;
+
+constexpr int kFlushTouch = 128;  // touched leaves whose flush data is staged
+
+// Flush tables (CTA 0): new boxes of the first kFlushTab listed ancestors,
+// the new boxes of their children that are touched leaves, and per touched
+// leaf (first kFlushTouch) its slot in kid (or -1) and its chunk range.
+struct FlushSmem {
+  float4 own[2 * kFlushTab];
+  float4 kid[4 * kFlushTab];
+  int kslot[kFlushTouch];
+  int2 kco[kFlushTouch];
+};
+
+// One listed ancestor per thread (fast path): its node, depth, and per child
+// the source of the child's box: 0 = unchanged (a/b registers), 1 = touched
+// leaf (fs.kid), 2 = listed ancestor at list position p0/p1 (fs.own).
+struct FlushState {
+  int node, dep;
+  int k0, k1, p0, p1;
+  float4 a0, a1, b0, b1;
+};
+
+__device__ __forceinline__ bool bit_set(const unsigned int* bits, int i) {
+  return (bits[i >> 5] >> (i & 31)) & 1u;
+}
+
+// Flush, first half (CTA 0 while the other CTAs refit): every ancestor of a
+// touched leaf is listed once (claimed in a bitmap over the nodes, which also
+// marks the touched leaf nodes) and s_idx[node] = its list position; with at
+// most kFlushTab ancestors, each thread takes one and loads the boxes of its
+// children that the update leaves unchanged.  touched: the touched leaves.
+static __device__ void team_flush_mark(const DevMesh& m, int ntouch, const int* touched, const int* s_par,
+                                unsigned int* bits, int* s_list, unsigned short* s_idx,
+                                FlushSmem& fs, TeamShared& sh, FlushState& f) {
+  for (int i = threadIdx.x; i < (m.totnode + 31) / 32; i += kTeamThreads) bits[i] = 0u;
+  if (threadIdx.x == 0) sh.nmark = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < ntouch; k += kTeamThreads) {
+    const int leaf_node = m.leaf_node[touched[k]];
+    atomicOr(&bits[leaf_node >> 5], 1u << (leaf_node & 31));
+    int p = s_par[leaf_node];
+    while (p >= 0) {
+      const unsigned int bit = 1u << (p & 31);
+      if (atomicOr(&bits[p >> 5], bit) & bit) break;  // claimed: so are its ancestors
+      s_list[atomicAdd(&sh.nmark, 1)] = p;
+      p = s_par[p];
+    }
+  }
+  __syncthreads();
+  const int nm = sh.nmark;
+  for (int t = threadIdx.x; t < nm; t += kTeamThreads) s_idx[s_list[t]] = static_cast<unsigned short>(t);
+  __syncthreads();
+  for (int k = threadIdx.x; k < min(ntouch, kFlushTouch); k += kTeamThreads) {
+    const int leaf = touched[k];
+    const int node = m.leaf_node[leaf];
+    const int p = s_par[node];
+    const int pos = p >= 0 ? s_idx[p] : kNoPos;
+    fs.kslot[k] = pos < kFlushTab ? 2 * pos + (node - m.node_child[p]) : -1;
+    fs.kco[k] = make_int2(m.leaf_chunk_off[leaf], m.leaf_chunk_off[leaf + 1]);
+  }
+  f.node = -1;
+  f.dep = -1;
+  if (nm <= kFlushTab && static_cast<int>(threadIdx.x) < nm) {
+    f.node = s_list[threadIdx.x];
+    f.dep = m.node_depth[f.node];
+    const int c = m.node_child[f.node];
+    f.p0 = s_idx[c];
+    f.p1 = s_idx[c + 1];
+    f.k0 = f.p0 != kNoPos ? 2 : (bit_set(bits, c) ? 1 : 0);
+    f.k1 = f.p1 != kNoPos ? 2 : (bit_set(bits, c + 1) ? 1 : 0);
+    if (f.k0 == 0) {
+      f.a0 = __ldcg(&m.vb[2 * c]);
+      f.a1 = __ldcg(&m.vb[2 * c + 1]);
+    }
+    if (f.k1 == 0) {
+      f.b0 = __ldcg(&m.vb[2 * c + 2]);
+      f.b1 = __ldcg(&m.vb[2 * c + 3]);
+    }
+  }
+}
+
+__device__ __forceinline__ void box_union(const float4& a0, const float4& a1, const float4& b0,
+                                          const float4& b1, float4& mn, float4& mx) {
+  mn.x = fmin_ref(fmin_ref(FLT_MAX, a0.x), b0.x);
+  mn.y = fmin_ref(fmin_ref(FLT_MAX, a0.y), b0.y);
+  mn.z = fmin_ref(fmin_ref(FLT_MAX, a0.z), b0.z);
+  mx.x = fmax_ref(fmax_ref(-FLT_MAX, a1.x), b1.x);
+  mx.y = fmax_ref(fmax_ref(-FLT_MAX, a1.y), b1.y);
+  mx.z = fmax_ref(fmax_ref(-FLT_MAX, a1.z), b1.z);
+  mn.w = mx.w = 0.0f;
+}
+
+// Flush, second half (CTA 0, after the refit): the touched leaf boxes from
+// their chunk boxes (one warp per leaf; also handed to the parent's thread in
+// fs.kid), then each listed ancestor becomes the union of its two children
+// (update_node_vb, pbvh.c:2026-2046), deepest level first as pbvh_flush_bb
+// (pbvh.c:3287-3317) orders it.  Resets s_idx to kNoPos.
+static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int* touched,
+                                  const int* s_par, const int* s_list, unsigned short* s_idx,
+                                  FlushSmem& fs, TeamShared& sh, FlushState& f,
+                                  unsigned long long& ab) {
+  const int nm = sh.nmark;
+  const int lane = threadIdx.x & 31;
+  for (int k = threadIdx.x >> 5; k < ntouch; k += kTeamThreads / 32) {
+    int2 co;
+    int slot;
+    if (k < kFlushTouch) {
+      co = fs.kco[k];
+      slot = fs.kslot[k];
+    } else {
+      const int leaf = touched[k];
+      co = make_int2(m.leaf_chunk_off[leaf], m.leaf_chunk_off[leaf + 1]);
+      const int node = m.leaf_node[leaf];
+      const int p = s_par[node];
+      const int pos = p >= 0 ? s_idx[p] : kNoPos;
+      slot = pos < kFlushTab ? 2 * pos + (node - m.node_child[p]) : -1;
+    }
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int id = co.x + lane; id < co.y; id += 32) {
+      const float4 c0 = __ldcg(&m.chunk_box[2 * id]), c1 = __ldcg(&m.chunk_box[2 * id + 1]);
+      mn[0] = fmin_ref(mn[0], c0.x);
+      mn[1] = fmin_ref(mn[1], c0.y);
+      mn[2] = fmin_ref(mn[2], c0.z);
+      mx[0] = fmax_ref(mx[0], c1.x);
+      mx[1] = fmax_ref(mx[1], c1.y);
+      mx[2] = fmax_ref(mx[2], c1.z);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        mn[q] = fmin_ref(mn[q], __shfl_xor_sync(0xffffffffu, mn[q], o));
+        mx[q] = fmax_ref(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], o));
+      }
+    if (lane == 0) {
+      const float4 bmn = make_float4(mn[0], mn[1], mn[2], 0.0f);
+      const float4 bmx = make_float4(mx[0], mx[1], mx[2], 0.0f);
+      const int node = m.leaf_node[touched[k]];
+      m.vb[2 * node] = bmn;
+      m.vb[2 * node + 1] = bmx;
+      if (slot >= 0) {
+        fs.kid[2 * slot] = bmn;
+        fs.kid[2 * slot + 1] = bmx;
+      }
+      ab += 32ull * (co.y - co.x + 1);  // chunk boxes read, leaf box written
+    }
+  }
+  __syncthreads();
+  if (nm <= 32) {
+    // one warp: each lane keeps one ancestor's box in registers and hands it
+    // to its parent's lane by shuffle
+    if (threadIdx.x < 32) {
+      const int t = lane;
+      float own[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+      if (f.node >= 0) ab += 72u;
+      for (int dd = m.max_depth; dd >= 0; dd--) {
+        float c0[6], c1[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+          c0[q] = __shfl_sync(0xffffffffu, own[q], f.p0 & 31);
+          c1[q] = __shfl_sync(0xffffffffu, own[q], f.p1 & 31);
+        }
+        if (f.dep == dd) {
+          if (f.k0 == 2) {
+            f.a0 = make_float4(c0[0], c0[1], c0[2], 0.0f);
+            f.a1 = make_float4(c0[3], c0[4], c0[5], 0.0f);
+          } else if (f.k0 == 1) {
+            f.a0 = fs.kid[4 * t];
+            f.a1 = fs.kid[4 * t + 1];
+          }
+          if (f.k1 == 2) {
+            f.b0 = make_float4(c1[0], c1[1], c1[2], 0.0f);
+            f.b1 = make_float4(c1[3], c1[4], c1[5], 0.0f);
+          } else if (f.k1 == 1) {
+            f.b0 = fs.kid[4 * t + 2];
+            f.b1 = fs.kid[4 * t + 3];
+          }
+          float4 mn, mx;
+          box_union(f.a0, f.a1, f.b0, f.b1, mn, mx);
+          own[0] = mn.x, own[1] = mn.y, own[2] = mn.z;
+          own[3] = mx.x, own[4] = mx.y, own[5] = mx.z;
+          m.vb[2 * f.node] = mn;
+          m.vb[2 * f.node + 1] = mx;
+        }
+      }
+    }
+    __syncthreads();
+  } else if (nm <= kFlushTab) {
+    const int t = threadIdx.x;
+    if (f.node >= 0) ab += 72u;  // two child boxes read, one box written
+    for (int dd = m.max_depth; dd >= 0; dd--) {
+      if (f.dep == dd) {
+        if (f.k0 == 2) {
+          f.a0 = fs.own[2 * f.p0];
+          f.a1 = fs.own[2 * f.p0 + 1];
+        } else if (f.k0 == 1) {
+          f.a0 = fs.kid[4 * t];
+          f.a1 = fs.kid[4 * t + 1];
+        }
+        if (f.k1 == 2) {
+          f.b0 = fs.own[2 * f.p1];
+          f.b1 = fs.own[2 * f.p1 + 1];
+        } else if (f.k1 == 1) {
+          f.b0 = fs.kid[4 * t + 2];
+          f.b1 = fs.kid[4 * t + 3];
+        }
+        float4 mn, mx;
+        box_union(f.a0, f.a1, f.b0, f.b1, mn, mx);
+        fs.own[2 * t] = mn;
+        fs.own[2 * t + 1] = mx;
+        m.vb[2 * f.node] = mn;
+        m.vb[2 * f.node + 1] = mx;
+      }
+      __syncthreads();
+    }
+  } else {
+    // many ancestors: per level, every thread scans the list; child boxes
+    // come from fs.own (first kFlushTab list positions) or global memory
+    for (int dd = m.max_depth; dd >= 0; dd--) {
+      for (int t = threadIdx.x; t < nm; t += kTeamThreads) {
+        const int node = s_list[t];
+        if (m.node_depth[node] != dd) continue;
+        const int c = m.node_child[node];
+        float4 box[2][2];
+        for (int h = 0; h < 2; h++) {
+          const int pc = s_idx[c + h];
+          if (pc < kFlushTab) {
+            box[h][0] = fs.own[2 * pc];
+            box[h][1] = fs.own[2 * pc + 1];
+          } else {
+            box[h][0] = __ldcg(&m.vb[2 * (c + h)]);
+            box[h][1] = __ldcg(&m.vb[2 * (c + h) + 1]);
+          }
+        }
+        float4 mn, mx;
+        box_union(box[0][0], box[0][1], box[1][0], box[1][1], mn, mx);
+        if (t < kFlushTab) {
+          fs.own[2 * t] = mn;
+          fs.own[2 * t + 1] = mx;
+        }
+        m.vb[2 * node] = mn;
+        m.vb[2 * node + 1] = mx;
+        ab += 72u;
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = threadIdx.x; t < nm; t += kTeamThreads) s_idx[s_list[t]] = kNoPos;
+  __syncthreads();
+}
+
+// Compensated area partial of one culled leaf by the CTA (256 lanes), the same
+// structure as k_area.
+static __device__ void team_area_leaf(const DevMesh& m, const PassParams& pp, float rn2, float ra2,
+                               int leaf, Lane* sl, AreaPart* out) {
+  const int t = threadIdx.x;
+  const int nv = leaf_nverts(m, leaf);
+  Lane l;
+#pragma unroll
+  for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
+  l.n_no = l.n_co = 0;
+  // lane t takes elements t, t + 256, ... in order; loads of kAreaBatch of
+  // them are issued together
+  constexpr int kAreaBatch = 2;
+  for (int i0 = t; i0 < nv; i0 += kAreaBatch * kTeamThreads) {
+    int vv[kAreaBatch];
+#pragma unroll
+    for (int j = 0; j < kAreaBatch; j++) {
+      const int i = i0 + j * kTeamThreads;
+      vv[j] = i < nv ? leaf_vert(m, leaf, i) : -1;
+    }
+    float4 co[kAreaBatch], no[kAreaBatch];
+#pragma unroll
+    for (int j = 0; j < kAreaBatch; j++) {
+      if (vv[j] >= 0) {
+        co[j] = __ldcg(&m.co[vv[j]]);
+        no[j] = __ldcg(&m.no[vv[j]]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kAreaBatch; j++) {
+      if (vv[j] < 0) break;
+      const float d2 = dist_sq(co[j], pp.loc);
+      if (d2 <= rn2) {
+        cs_add(l.v[0], no[j].x);
+        cs_add(l.v[1], no[j].y);
+        cs_add(l.v[2], no[j].z);
+        l.n_no++;
+      }
+      if (d2 <= ra2) {
+        cs_add(l.v[3], co[j].x);
+        cs_add(l.v[4], co[j].y);
+        cs_add(l.v[5], co[j].z);
+        l.n_co++;
+      }
+    }
+  }
+  sl[t] = l;
+  __syncthreads();
+  for (int s = kTeamThreads / 2; s >= 32; s >>= 1) {
+    if (t < s) {
+      Lane a = sl[t];
+      lane_merge(a, sl[t + s]);
+      sl[t] = a;
+    }
+    __syncthreads();
+  }
+  if (t < 32) {
+    Lane a = sl[t];
+    for (int s = 16; s >= 1; s >>= 1) {
+      const Lane o = lane_shfl_down(a, s);
+      lane_merge(a, o);
+    }
+    if (t == 0) part_store(out, a);
+  }
+  __syncthreads();
+}
+
+// Final pairwise tree over the leaf partials (i, i+s), s = 1, 2, 4, ... by one
+// CTA in shared memory; writes area normal and centre into sh.area.
+constexpr int kTeamMaxChunks = 64;  // culled leaves per pass <= 64 * 256
+
+static __device__ void team_area_final(const DevMesh& m, const PassParams& pp, int cnt, Lane* sl,
+                                Lane* chunks, TeamShared& sh) {
+  // Partials are staged in shared memory in chunks of kTeamThreads (a power of
+  // two, so each chunk is a complete subtree of the pairwise tree); the chunk
+  // totals then merge with the same pairwise rule, which completes the tree.
+  const int nchunks = (cnt + kTeamThreads - 1) / kTeamThreads;
+  for (int c = 0; c < nchunks; c++) {
+    const int c0 = c * kTeamThreads;
+    const int n = min(kTeamThreads, cnt - c0);
+    if (threadIdx.x < n) sl[threadIdx.x] = part_load(&m.parts[c0 + threadIdx.x]);
+    __syncthreads();
+    for (int s = 1; s < n; s <<= 1) {
+      const int i = threadIdx.x * 2 * s;
+      if (i + s < n) {
+        Lane a = sl[i];
+        lane_merge(a, sl[i + s]);
+        sl[i] = a;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) chunks[c] = sl[0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 1; s < nchunks; s <<= 1)
+      for (int i = 0; i + s < nchunks; i += 2 * s) lane_merge(chunks[i], chunks[i + s]);
+    Lane acc;
+    if (nchunks > 0) {
+      acc = chunks[0];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 6; q++) acc.v[q].s = acc.v[q].e = 0.0f;
+      acc.n_no = acc.n_co = 0;
+    }
+    float nx = acc.v[0].s + acc.v[0].e, ny = acc.v[1].s + acc.v[1].e, nz = acc.v[2].s + acc.v[2].e;
+    normalize3(nx, ny, nz);
+    sh.area[0] = nx;
+    sh.area[1] = ny;
+    sh.area[2] = nz;
+    if (acc.n_co > 0) {
+      const float inv = 1.0f / (float)acc.n_co;
+      sh.area[3] = (acc.v[3].s + acc.v[3].e) * inv;
+      sh.area[4] = (acc.v[4].s + acc.v[4].e) * inv;
+      sh.area[5] = (acc.v[5].s + acc.v[5].e) * inv;
+    } else {
+      sh.area[3] = pp.loc[0];
+      sh.area[4] = pp.loc[1];
+      sh.area[5] = pp.loc[2];
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Team barrier.  A cluster team uses barrier.cluster (cluster.sync():
+// arrive.release, wait.acquire).  The whole-GPU team (every CTA of a
+// cooperative launch, so all of them are resident) counts arrivals in global
+// memory: after a CTA barrier, thread 0 adds one to the counter with release
+// semantics and waits until it reaches the CTA count times the barrier's
+// ordinal, then fences with acquire semantics before the CTA barrier that
+// lets its threads go on.  The wait is bounded by a time limit and an
+// iteration cap; a CTA that gives up records SGPU_ERR_TIMEOUT in *status and
+// sets the counter's abort bit, and every CTA that sees the bit returns false
+// (the kernel then leaves).  extra: arrivals the barrier waits for beyond the
+// CTAs of the launch (0; a host-side test hook makes it 1 so that the wait
+// runs out).
+constexpr unsigned int kBarAbort = 0x80000000u;
+
+__device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <bool kWide>
+struct TeamBarrier {
+  unsigned int C;
+  unsigned int* count;
+  unsigned int target;
+  unsigned long long limit_ns;
+  int* status;
+  int* s_ok;  // shared: the wait's outcome for the CTA
+  unsigned int extra;
+
+  __device__ __forceinline__ bool sync() {
+    if constexpr (!kWide) {
+      if (C > 1) {
+        cg::this_cluster().sync();
+      } else {
+        __syncthreads();
+      }
+      return true;
+    } else {
+      __syncthreads();
+      target += C + extra;
+      if (threadIdx.x == 0) {
+        unsigned int v;
+        asm volatile("atom.release.gpu.global.add.u32 %0, [%1], 1;"
+                     : "=r"(v)
+                     : "l"(count)
+                     : "memory");
+        v += 1u;
+        int ok = 1;
+        unsigned long long t0 = 0ull;
+        for (unsigned int it = 1;; it++) {
+          if (v & kBarAbort) {
+            ok = 0;
+            break;
+          }
+          if (v >= target) break;
+          if ((it & 1023u) == 0u) {
+            const unsigned long long now = global_ns();
+            if (t0 == 0ull) {
+              t0 = now;
+            } else if (now - t0 > limit_ns || it >= (1u << 28)) {
+              atomicCAS(status, 0, SGPU_ERR_TIMEOUT);
+              atomicOr(count, kBarAbort);
+              ok = 0;
+              break;
+            }
+          }
+          v = ld_relaxed_gpu(count);
+        }
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        *s_ok = ok;
+      }
+      __syncthreads();
+      return *s_ok != 0;
+    }
+  }
+};
+
+// Profiling helpers: algorithmic bytes (warp-aggregated, converged code) and
+// per-phase time measured by the team's first thread.
+__device__ __forceinline__ void team_bytes(const TeamArgs& a, int phase, unsigned long long b) {
+  if (!a.prof_bytes) return;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&a.prof_bytes[phase], b);
+}
+
+struct PhaseClock {
+  unsigned long long last;
+  __device__ __forceinline__ void mark(const TeamArgs& a, unsigned rank, int phase) {
+    if (!a.phase_ns || rank != 0 || threadIdx.x != 0) return;
+    const unsigned long long now = global_ns();
+    atomicAdd(&a.phase_ns[phase], now - last);
+    last = now;
+  }
+};
+
+// Two builds of the kernel: one CTA per SM with the full register file (the
+// fastest single strokes), or two CTAs per SM (twice the teams for batches).
+// kOrig: the build that also runs grab, elastic deform and layer dabs (the
+// other build carries none of their code).
+// kWide: the whole-GPU team (cooperative launch, one CTA per SM), which runs
+// the jobs one after another.
+template <int kMinBlocks, bool kOrig, bool kWide>
+__global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamArgs a) {
+  unsigned C, rank;
+  if constexpr (kWide) {
+    C = gridDim.x;
+    rank = blockIdx.x;
+  } else {
+    const cg::cluster_group cluster = cg::this_cluster();
+    C = cluster.num_blocks();
+    rank = cluster.block_rank();
+  }
+  // Item lists are dealt to the team in warp-sized blocks, round-robin over
+  // the CTAs (block b goes to CTA b % C), so that a short list still spreads
+  // its scattered loads over every SM of the cluster.
+  const int lane = threadIdx.x & 31;
+  const int gt = 32 * ((threadIdx.x >> 5) * static_cast<int>(C) + static_cast<int>(rank)) + lane;
+  const int GT = C * kTeamThreads;
+  __shared__ TeamShared sh;
+  // area lanes and flush tables are never live at the same time
+  union Scratch {
+    Lane lanes[kTeamThreads];
+    FlushSmem flush;
+  };
+  static_assert(sizeof(FlushSmem) <= sizeof(Lane) * kTeamThreads, "flush tables exceed the lanes");
+  __shared__ Scratch s_scr;
+  Lane* s_lanes = s_scr.lanes;
+  __shared__ Lane s_chunks[kTeamMaxChunks];
+  extern __shared__ __align__(16) unsigned char dyn[];
+  float4* s_nbc = reinterpret_cast<float4*>(dyn);  // smooth neighbour tables
+  int* s_par = reinterpret_cast<int*>(s_nbc + kNbCache * kTeamThreads);
+  int* s_cl = s_par + a.max_nodes;
+  int* s_coff = s_cl + a.max_leaves + 1;
+  int* s_lnv = s_coff + a.max_leaves + 2;
+  unsigned short* s_idx = reinterpret_cast<unsigned short*>(s_lnv + a.max_leaves);
+  unsigned short* s_lnode = s_idx + ((a.max_nodes + 1) & ~1);
+  // node marks; also the flush's claim bitmap (32-bit words): the ushort
+  // arrays before it have even lengths, so this starts 4-byte aligned
+  unsigned char* s_pass = reinterpret_cast<unsigned char*>(s_lnode + ((a.max_leaves + 1) & ~1));
+  const CullTabs ct{s_lnode, s_lnv};
+  PhaseClock clk;
+  clk.last = a.phase_ns ? global_ns() : 0ull;
+  TeamBarrier<kWide> bar{C, a.bar, 0u, a.wait_ns, a.status, &sh.bar_ok,
+                         static_cast<unsigned int>(a.bar_extra)};
+#define TEAM_SYNC()          \
+  do {                       \
+    if (!bar.sync()) return; \
+  } while (0)
+
+  int next_wide = 0;
+  for (;;) {
+    int jid;
+    if constexpr (kWide) {
+      jid = next_wide++;
+    } else {
+      if (rank == 0 && threadIdx.x == 0) sh.jobid = atomicAdd(a.next_job, 1);
+      TEAM_SYNC();
+      jid = (C > 1) ? *cg::this_cluster().map_shared_rank(&sh.jobid, 0) : sh.jobid;
+      TEAM_SYNC();
+    }
+    if (jid >= a.njobs) return;
+    {
+      const int* src = reinterpret_cast<const int*>(&a.jobs[jid]);
+      int* dst = reinterpret_cast<int*>(&sh.job);
+      for (int i = threadIdx.x; i < static_cast<int>(sizeof(TeamJob) / 4); i += kTeamThreads)
+        dst[i] = src[i];
+    }
+    __syncthreads();
+    {
+      const int* src = reinterpret_cast<const int*>(&a.meshes[sh.job.mesh]);
+      int* dst = reinterpret_cast<int*>(&sh.m);
+      for (int i = threadIdx.x; i < static_cast<int>(sizeof(DevMesh) / 4); i += kTeamThreads)
+        dst[i] = src[i];
+    }
+    __syncthreads();
+    const DevMesh& m = sh.m;
+    DevBrush& b = sh.job.brush;
+    Work* w = m.work;
+    for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) {
+      s_par[i] = m.node_parent[i];
+      s_idx[i] = kNoPos;
+    }
+    for (int k = threadIdx.x; k < m.nleaf; k += kTeamThreads) {
+      s_lnode[k] = static_cast<unsigned short>(m.leaf_node[k]);
+      s_lnv[k] = leaf_nverts(m, k);
+    }
+    // GRIDS work-list stamps: dab d uses epoch grid_epoch0 + d + 1
+    const unsigned int grid_epoch0 = __ldcg(&w->grid_epoch);
+    TEAM_SYNC();
+    if (rank == 0 && threadIdx.x == 0) {
+      for (int k = 0; k < 3; k++) w->hit_count[k] = 0;
+      w->tag_count[0] = w->tag_count[1] = 0;
+      w->touch_count[0] = w->touch_count[1] = 0;
+      if (m.type == kGrids) m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = m.grid_counts[3] = 0;
+    }
+    TEAM_SYNC();
+    // Leaves flagged and vertices tagged before the stroke (by per-call entry
+    // points) join the first dab's update, as they would in the per-call path.
+    if (rank == 0)
+      for (int leaf = threadIdx.x; leaf < m.nleaf; leaf += kTeamThreads) {
+        const int f = __ldcg(&m.leaf_flag[leaf]);
+        if (!(f & (kUpdateNormals | kUpdateBB))) continue;
+        append(m.touch_list, &w->touch_count[0], leaf);
+        if ((f & kUpdateNormals) && m.type == kFaces) {
+          const int off = m.leaf_vert_off[leaf];
+          for (int i = 0; i < m.leaf_uniq[leaf]; i++) {
+            const int v = m.leaf_verts[off + i];
+            if (__ldcg(&m.vtag[v])) m.tag_list[atomicAdd(&w->tag_count[0], 1)] = v;
+          }
+        }
+      }
+    TEAM_SYNC();
+    clk.mark(a, rank, kPhJob);
+    const int default_tool = b.tool;
+    int q = 0;  // smooth sweep counter (hit-list rotation)
+    for (int d = 0; d < sh.job.ndabs; d++) {
+      const int par = d & 1;
+      if (rank == 0 && threadIdx.x == 0) {
+        w->tag_count[par ^ 1] = 0;
+        w->touch_count[par ^ 1] = 0;
+      }
+      const int tool = sh.job.tools ? sh.job.tools[d] : default_tool;
+      __syncthreads();
+      if (threadIdx.x == 0) b.tool = tool;
+      __syncthreads();
+      const float scale = (tool == kToolClayStrips) ? 1.41421356237309504880f : 1.0f;
+      const float r = b.radius * scale;
+      int* tag_cnt = &w->tag_count[par];
+      int* touch_cnt = &w->touch_count[par];
+      if (kOrig && uses_original(tool)) {
+        // grab / elastic deform: one gather over all passes, then each vertex
+        // rebuilt from its stroke-start position (k_cull_dab, k_orig_dab)
+        if (threadIdx.x == 0) {
+          DabPasses& dp = sh.dp;
+          dp.npass = 0;
+          for (int pass = 0; pass < 8; pass++) {
+            if ((pass & ~sh.job.symmetry) != 0) continue;
+            for (int k = 0; k < 3; k++) {
+              const float sgn = (pass & (1 << k)) ? -1.0f : 1.0f;
+              dp.loc[dp.npass][k] = sgn * sh.job.dabs[6 * d + k];
+              dp.delta[dp.npass][k] = sgn * sh.job.dabs[6 * d + 3 + k];
+              dp.view[dp.npass][k] = sgn * sh.job.view[k];
+            }
+            dp.npass++;
+          }
+          // the Kelvinlet force of the dab (BKE_kelvinlet_init_params,
+          // kelvinlet.c:6-21): |grab delta| * strength
+          const float* gd = &sh.job.dabs[6 * d + 3];
+          b.kl_f = sqrtf(gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2]) * b.strength;
+        }
+        __syncthreads();
+        team_cull_union(m, sh.dp, b.radius * b.radius, tool == kToolElasticDeform ? 1 : 0, s_pass,
+                        s_cl, s_coff, ct, sh);
+        const int cnt = sh.cnt, total = sh.total;
+        team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
+        clk.mark(a, rank, kPhCull);
+        if (rank == 0)
+          for (int k = threadIdx.x; k < cnt; k += kTeamThreads) {
+            const int leaf = s_cl[k];
+            const int old = atomicOr(&m.leaf_flag[leaf], kMarkUpdate);
+            if (!(old & kUpdateNormals)) append(m.touch_list, touch_cnt, leaf);
+          }
+        team_bytes(a, kPhBrush, team_orig_sweep(m, b, sh.dp, s_cl, s_coff, cnt, total, gt, GT, tag_cnt));
+        TEAM_SYNC();
+        clk.mark(a, rank, kPhBrush);
+      }
+      for (int pass = 0; pass < 8 && !(kOrig && uses_original(tool)); pass++) {
+        if ((pass & ~sh.job.symmetry) != 0) continue;
+        PassParams pp;
+        for (int k = 0; k < 3; k++) {
+          const float sgn = (pass & (1 << k)) ? -1.0f : 1.0f;
+          pp.loc[k] = sgn * sh.job.dabs[6 * d + k];
+          pp.delta[k] = sgn * sh.job.dabs[6 * d + 3 + k];
+          pp.view[k] = sgn * sh.job.view[k];
+        }
+        pp.cull_radius_sq = r * r;
+        pp.original = sh.job.use_orig || (kOrig && tool == kToolLayer);  // layer: stroke-start boxes
+        pp.iter_strength = 1.0f;
+        pp.iteration = 0;
+        team_cull<kMinBlocks == 1 ? 8 : 2>(m, pp, s_pass, s_cl, s_coff, ct, sh);
+        const int cnt = sh.cnt, total = sh.total;
+        // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
+        team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
+        clk.mark(a, rank, kPhCull);
+        float area_no[3] = {0.0f, 0.0f, 0.0f}, area_co[3] = {0.0f, 0.0f, 0.0f};
+        if (uses_area(tool)) {
+          const float rn = b.radius * b.normal_radius_factor;
+          const float ra = b.radius * b.area_radius_factor;
+          unsigned long long ab = 0;
+          for (int k = rank; k < cnt; k += C) {
+            team_area_leaf(m, pp, rn * rn, ra * ra, s_cl[k], s_lanes, &m.parts[k]);
+            const int nv = leaf_nverts(m, s_cl[k]);
+            if (threadIdx.x < nv)
+              ab += ((m.type == kFaces ? 4ull : 0ull) + 24ull) *
+                    ((nv - threadIdx.x + kTeamThreads - 1) / kTeamThreads);
+          }
+          team_bytes(a, kPhArea, ab);
+          TEAM_SYNC();
+          team_area_final(m, pp, cnt, s_lanes, s_chunks, sh);
+          for (int k = 0; k < 3; k++) {
+            area_no[k] = sh.area[k];
+            area_co[k] = sh.area[3 + k];
+          }
+          clk.mark(a, rank, kPhArea);
+        }
+        BrushFrame f;
+        if (!make_frame(b, pp, area_no, area_co, f)) continue;
+        if (rank == 0)
+          for (int k = threadIdx.x; k < cnt; k += kTeamThreads) {
+            const int leaf = s_cl[k];
+            const int old = atomicOr(&m.leaf_flag[leaf], kMarkUpdate);
+            if (!(old & kUpdateNormals)) append(m.touch_list, touch_cnt, leaf);
+          }
+        if (tool != kToolSmooth) {
+          unsigned long long ab = 0;
+          const unsigned vbytes = (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) +
+                                  (m.automask ? 4u : 0u) +
+                                  ((tool == kToolInflate || (b.flag & kBrushFrontFace)) ? 12u : 0u);
+          for (int base = gt - lane; base < total; base += GT) {
+            const int i = base + lane;
+            bool moved = false;
+            if (i < total) {
+              const int k = smem_find_slot(s_coff, cnt, i);
+              const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+              float4 co = __ldcg(&m.co[v]);
+              ab += vbytes;
+              const bool hit = (kOrig && tool == kToolLayer) ? layer_vertex(m, b, b.y, pp, v, co, moved)
+                                                  : brush_vertex(m, b, b.y, pp, f, v, co, moved);
+              if (hit) {
+                m.co[v] = co;
+                ab += 12u;
+                if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+              }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, moved);
+            if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
+          }
+          team_bytes(a, kPhBrush, ab);
+          TEAM_SYNC();
+          clk.mark(a, rank, kPhBrush);
+        } else {
+          float st = b.strength;
+          if (st < 0.0f) st = 0.0f;
+          if (st > 1.0f) st = 1.0f;
+          const int count = (int)(st * 4.0f);
+          const float last = 4.0f * (st - (float)count * 0.25f);
+          // Jacobi sweeps over slots.  CTA r gives its hits the slots
+          // [r * R, r * R + nh) (R bounds its share of the candidates), so no
+          // slot counter is shared.  The thread that runs a hit's first sweep
+          // keeps it for the later ones; its first hit keeps vertex, value and
+          // ring table on chip.  The last sweep writes the positions.  The two
+          // slot maps alternate by pass, so a pass clears its entries while
+          // the next one fills the other map.
+          int* const smap = m.slot_map[q & 1];
+          q++;
+          int* const slot_v = m.hit_list[0];
+          float4* const val[2] = {m.scratch, m.scratch2};
+          const int R = 32 * ((total + 32 * static_cast<int>(C) - 1) / (32 * static_cast<int>(C)));
+          const int sbase = static_cast<int>(rank) * R;
+          if (threadIdx.x == 0) sh.nh = 0;
+          __syncthreads();
+          // first sweep, stage 1: distance test of this CTA's candidates
+          pp.iter_strength = (count != 0) ? 1.0f : last;
+          pp.iteration = 0;
+          const float rr = b.radius * b.radius;
+          unsigned long long ab = 0;
+          constexpr int kCand = 4;
+          for (int base = gt - lane; base < total; base += kCand * GT) {
+            int vv[kCand];
+            float4 cc[kCand];
+#pragma unroll
+            for (int j = 0; j < kCand; j++) {
+              const int i = base + j * GT + lane;
+              vv[j] = -1;
+              if (i < total) {
+                const int k = smem_find_slot(s_coff, cnt, i);
+                vv[j] = leaf_vert(m, s_cl[k], i - s_coff[k]);
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < kCand; j++)
+              if (vv[j] >= 0) cc[j] = __ldcg(&m.co[vv[j]]);
+#pragma unroll
+            for (int j = 0; j < kCand; j++) {
+              if (vv[j] < 0) continue;
+              ab += 16u;  // vertex id, co
+              if (!(dist_sq(cc[j], pp.loc) <= rr)) continue;
+              cg::coalesced_group g = cg::coalesced_threads();
+              int h = 0;
+              if (g.thread_rank() == 0) h = atomicAdd(&sh.nh, static_cast<int>(g.size()));
+              h = g.shfl(h, 0) + g.thread_rank();
+              slot_v[sbase + h] = vv[j];
+              if (h < kTeamThreads) {
+                sh.hv[h] = vv[j];
+                sh.hco[h] = cc[j];
+              }
+            }
+          }
+          __syncthreads();
+          const int nh = sh.nh;
+          // stage 2: the first sweep of the hits
+          int v0 = -1, n0 = -1;
+          float4 own = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          for (int hb = threadIdx.x - lane; hb < nh; hb += kTeamThreads) {
+            const int h = hb + lane;
+            bool moved = false;
+            if (h < nh) {
+              const int v = h < kTeamThreads ? sh.hv[h] : __ldcg(&slot_v[sbase + h]);
+              const float4 co = h < kTeamThreads ? sh.hco[h] : __ldcg(&m.co[v]);
+              float4 out;
+              int nr = -1;
+              if (h == static_cast<int>(threadIdx.x)) {
+                out = smooth_first(m, b, pp, v, co, s_nbc + threadIdx.x, kTeamThreads, &nr, moved);
+                v0 = v;
+                n0 = nr;
+                own = out;
+              } else {
+                smooth_vertex(m, b, b.y, pp, v, co, out, moved);
+              }
+              val[0][sbase + h] = out;
+              smap[v] = sbase + h;
+              if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+              const int valence = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
+              // mask, ring range and ring (id + co) reads; value, map and slot written
+              ab += (m.mask ? 4ull : 0ull) + (m.type == kFaces ? 8ull : 0ull) + 16ull * valence + 24ull;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, moved);
+            if (lane == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
+          }
+          team_bytes(a, kPhBrush, ab);
+          TEAM_SYNC();
+          clk.mark(a, rank, kPhBrush);
+          if (count == 0) {
+            for (int h = threadIdx.x; h < nh; h += kTeamThreads) {
+              const int v = h == static_cast<int>(threadIdx.x) ? v0 : __ldcg(&slot_v[sbase + h]);
+              m.co[v] = h == static_cast<int>(threadIdx.x) ? own : __ldcg(&val[0][sbase + h]);
+            }
+          }
+          for (int it = 1; it <= count; it++) {
+            pp.iter_strength = (it != count) ? 1.0f : last;
+            pp.iteration = it;
+            const float4* src = val[(it - 1) & 1];
+            float4* dst = val[it & 1];
+            ab = 0;
+            for (int h = threadIdx.x; h < nh; h += kTeamThreads) {
+              float4 out;
+              int v, nring;
+              if (h == static_cast<int>(threadIdx.x) && n0 >= 0) {
+                if (it == 1) smooth_resolve(s_nbc + threadIdx.x, kTeamThreads, n0, smap);
+                out = smooth_slot_cached(m, b, pp, v0, own, n0, s_nbc + threadIdx.x, kTeamThreads, src);
+                v = v0;
+                nring = n0;
+              } else {
+                const bool first = h == static_cast<int>(threadIdx.x);
+                v = first ? v0 : __ldcg(&slot_v[sbase + h]);
+                out = smooth_slot(m, b, pp, v, first ? own : __ldcg(&src[sbase + h]), src, smap);
+                nring = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
+              }
+              if (h == static_cast<int>(threadIdx.x)) own = out;
+              if (it == count) {
+                m.co[v] = out;
+              } else {
+                dst[sbase + h] = out;
+              }
+              // value and mask read, ring values read, value written
+              ab += 16ull + (m.mask ? 4ull : 0ull) + 16ull * nring + 16ull;
+            }
+            team_bytes(a, kPhApply, ab);
+            TEAM_SYNC();
+            clk.mark(a, rank, kPhApply);
+          }
+          if (count == 0) {
+            TEAM_SYNC();
+            clk.mark(a, rank, kPhApply);
+          }
+          // clear this pass's map entries; the map is next filled two smooth
+          // passes later, after at least one more team barrier
+          for (int h = threadIdx.x; h < nh; h += kTeamThreads)
+            smap[h == static_cast<int>(threadIdx.x) ? v0 : __ldcg(&slot_v[sbase + h])] = -1;
+        }
+      }
+      // End of the dab.  FACES: refit of the touched leaves, then the flush
+      // (CTA 0) alongside the normal update of the tagged vertices (the other
+      // CTAs): normals read positions and leaf flags, the flush reads chunk
+      // boxes and writes node boxes.  GRIDS: the normal update moves seam
+      // positions, so it runs first, then refit and flush.
+      const int ntag = __ldcg(tag_cnt);
+      const int ntouch = __ldcg(touch_cnt);
+      unsigned long long ab = 0;
+      FlushState fst;
+      if (m.type == kGrids) {
+        // GRIDS: faces of the touched leaves, the inner normals of their
+        // grids, the face seams and centres, then the base edges and corners
+        // (positions move at the seams, so the refit below follows).
+        const unsigned int epoch = grid_epoch0 + static_cast<unsigned int>(d) + 1u;
+        for (int k = rank; k < ntouch; k += C) {
+          const int leaf = __ldcg(&m.touch_list[k]);
+          const int p0 = m.leaf_prim_off[leaf], p1 = m.leaf_prim_off[leaf + 1];
+          for (int j = p0 + threadIdx.x; j < p1; j += kTeamThreads) grid_claim_face(m, m.leaf_prims[j], epoch);
+        }
+        TEAM_SYNC();
+        const int nf = __ldcg(&m.grid_counts[0]), ng = __ldcg(&m.grid_counts[3]);
+        const long long inner = (long long)ng * m.grid_area;
+        for (long long it = gt; it < inner; it += GT) {
+          grid_inner_item(m, it);
+          ab += 24u;  // co read, normal written
+        }
+        TEAM_SYNC();
+        const long long pairs = (long long)ng * (m.grid_size - 1);
+        for (long long it = gt; it < pairs + nf; it += GT) {
+          grid_face_seam_item(m, it, ng);
+          // co, no and mask read and written per element
+          ab += it < pairs ? 112ull : 56ull * m.face_ngrids[__ldcg(&m.face_list[it - pairs])];
+        }
+        TEAM_SYNC();
+        const int ne = __ldcg(&m.grid_counts[1]), nv = __ldcg(&m.grid_counts[2]);
+        const long long items = (long long)ne * (2 * m.grid_size - 2) + nv;
+        for (long long it = gt; it < items; it += GT) grid_seam_item(m, it, ne);
+        TEAM_SYNC();
+        if (rank == 0 && threadIdx.x == 0)
+          m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = m.grid_counts[3] = 0;
+      }
+      // refit: the chunk boxes of the touched leaves, one warp per chunk
+      // across the team (chunk offsets of the touched leaves in s_coff)
+      {
+        const int seg = (ntouch + kTeamThreads - 1) / kTeamThreads;
+        const int t0 = min(ntouch, static_cast<int>(threadIdx.x) * seg), t1 = min(ntouch, t0 + seg);
+        int nc = 0;
+        for (int k = t0; k < t1; k++) {
+          const int leaf = __ldcg(&m.touch_list[k]);
+          s_cl[k] = leaf;
+          nc += m.leaf_chunk_off[leaf + 1] - m.leaf_chunk_off[leaf];
+        }
+        int nchunk;
+        int off = team_block_scan(nc, &nchunk, sh.scan);
+        for (int k = t0; k < t1; k++) {
+          s_coff[k] = off;
+          off += m.leaf_chunk_off[s_cl[k] + 1] - m.leaf_chunk_off[s_cl[k]];
+        }
+        __syncthreads();
+        // chunks dealt over CTAs 1..C-1 while CTA 0 lists the ancestors to flush
+        const int wpc = kTeamThreads / 32;
+        const int rc = C > 1 ? static_cast<int>(C) - 1 : 1;
+        const int rr = C > 1 ? static_cast<int>(rank) - 1 : 0;
+        const unsigned idb = (m.type == kFaces ? 4u : 0u) + 12u;  // vertex id, position
+        if (rank != 0 || C == 1) {
+          for (int j = (threadIdx.x >> 5) * rc + rr; j < nchunk; j += rc * wpc) {
+            const int k = smem_find_slot(s_coff, ntouch, j);
+            const int leaf = s_cl[k], c = j - s_coff[k];
+            float mn[3], mx[3];
+            chunk_refit_warp(m, leaf, c, mn, mx);
+            if (lane == 0)
+              ab += 32ull + idb * static_cast<unsigned long long>(min(kChunk, leaf_nverts_all(m, leaf) - c * kChunk));
+          }
+        }
+        if (rank == 0)
+          team_flush_mark(m, ntouch, s_cl, s_par, reinterpret_cast<unsigned int*>(s_pass), s_coff, s_idx,
+                          s_scr.flush, sh, fst);
+      }
+      team_bytes(a, kPhUpdate, ab);
+      TEAM_SYNC();
+      clk.mark(a, rank, kPhUpdate);
+      // flush by CTA 0: the listed ancestors bottom-up
+      unsigned long long fb = 0;
+      if (rank == 0) team_flush_levels(m, ntouch, s_cl, s_par, s_coff, s_idx, s_scr.flush, sh, fst, fb);
+      team_bytes(a, kPhFlush, fb);
+      if (m.type == kFaces && (rank != 0 || C == 1)) {
+        // normals over CTAs 1..C-1 (all of the team when it is one CTA)
+        const int nc = C > 1 ? static_cast<int>(C) - 1 : 1;
+        const int cr = C > 1 ? static_cast<int>(rank) - 1 : 0;
+        ab = 0;
+        for (int j = 32 * ((threadIdx.x >> 5) * nc + cr) + lane; j < ntag; j += nc * kTeamThreads) {
+          const int v = __ldcg(&m.tag_list[j]);
+          float4 n;
+          const int used = vertex_normal(m, v, n);
+          m.no[v] = n;
+          m.vtag[v] = 0u;
+          ab += 24ull + 16ull * used;
+        }
+        team_bytes(a, kPhUpdate, ab);
+      }
+      TEAM_SYNC();
+      clk.mark(a, rank, kPhFlush);
+      // the touched leaves' update flags clear once both have read them
+      if (rank == 0)
+        for (int k = threadIdx.x; k < ntouch; k += kTeamThreads)
+          atomicAnd(&m.leaf_flag[__ldcg(&m.touch_list[k])], ~(kUpdateNormals | kUpdateBB));
+    }
+    // end of stroke: BKE_pbvh_update_bounds(UpdateOriginalBB)
+    for (int i = threadIdx.x; i < m.totnode; i += kTeamThreads) s_pass[i] = 0;
+    __syncthreads();
+    for (int leaf = threadIdx.x; leaf < m.nleaf; leaf += kTeamThreads) {
+      if (!(__ldcg(&m.leaf_flag[leaf]) & kUpdateOriginalBB)) continue;
+      int n = m.leaf_node[leaf];
+      s_pass[n] = 1;
+      n = s_par[n];
+      while (n >= 0 && !s_pass[n]) {
+        s_pass[n] = 1;
+        n = s_par[n];
+      }
+    }
+    __syncthreads();
+    for (int n = gt; n < m.totnode; n += GT)
+      if (s_pass[n]) {
+        m.orig_vb[2 * n] = __ldcg(&m.vb[2 * n]);
+        m.orig_vb[2 * n + 1] = __ldcg(&m.vb[2 * n + 1]);
+      }
+    TEAM_SYNC();
+    for (int leaf = gt; leaf < m.nleaf; leaf += GT) atomicAnd(&m.leaf_flag[leaf], ~kUpdateOriginalBB);
+    if (rank == 0 && threadIdx.x == 0 && m.type == kGrids)
+      w->grid_epoch = grid_epoch0 + static_cast<unsigned int>(sh.job.ndabs);
+    TEAM_SYNC();
+    clk.mark(a, rank, kPhJob);
+  }
+}
+#undef TEAM_SYNC
+
+}  // namespace sgpu

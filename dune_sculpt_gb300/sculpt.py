@@ -28,6 +28,8 @@ PBVH_UpdateDrawBuffers, PBVH_UpdateRedraw = 16, 32
 STROKE_EAGER, STROKE_GRAPH, STROKE_TEAM = 0, 1, 2
 BATCH_SEQUENTIAL, BATCH_TEAM = 0, 1
 TEAM_SIZES = (1, 2, 4, 8, 16)
+TEAM_GRID = -1  # SGPU_TEAM_GRID: every SM of the GPU works on one stroke
+INJECT_ALLOC_FAIL, INJECT_WAIT_NS, INJECT_BARRIER_EXTRA = 1, 2, 3
 
 
 class SculptGPUError(RuntimeError):
@@ -90,7 +92,7 @@ EXPORTS = (
     "sgpu_mesh_get_team", "sgpu_autotune_team", "sgpu_batch_stroke", "sgpu_stroke_team_profile",
     "sgpu_raycast", "sgpu_draw_buffers_build", "sgpu_draw_buffers_update",
     "sgpu_draw_buffers_layout", "sgpu_draw_buffers_overlay", "sgpu_draw_buffers_get",
-    "sgpu_draw_buffers_device", "sgpu_draw_buffers_update_timed",
+    "sgpu_draw_buffers_device", "sgpu_draw_buffers_update_timed", "sgpu_debug_inject",
 )
 
 DRAW_STRIDE = 36  # SGPU_DRAW_STRIDE
@@ -168,6 +170,7 @@ def load(path: str | None = None):
     L.sgpu_autotune_team.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp]
     L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
     L.sgpu_mesh_store_original.argtypes = [vp]
+    L.sgpu_debug_inject.argtypes = [i, C.c_int64]
     L.sgpu_draw_buffers_build.argtypes = [vp, C.POINTER(SGPU_DrawSetup)]
     L.sgpu_draw_buffers_update.argtypes = [vp]
     L.sgpu_draw_buffers_update_timed.argtypes = [vp, i, vp]
@@ -177,6 +180,12 @@ def load(path: str | None = None):
     L.sgpu_draw_buffers_device.argtypes = [vp, vp, vp]
     _lib = L
     return L
+
+
+def debug_inject(what: int, value: int):
+    """Host-side failure injection (sgpu_debug_inject): INJECT_ALLOC_FAIL,
+    INJECT_WAIT_NS or INJECT_BARRIER_EXTRA."""
+    _check(load().sgpu_debug_inject(what, value))
 
 
 def batch_stroke(pbvhs, strokes, mode: int = BATCH_TEAM, cluster: int = 0, dab_tools=None):

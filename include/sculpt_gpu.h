@@ -256,7 +256,13 @@ int sgpu_stroke(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, 
                 const int *dab_tools, int mode, SGPU_StrokeStats *stats);
 
 /* Cluster size (CTAs of 256 threads working on one mesh) of the persistent
- * stroke kernel for this mesh: 1, 2, 4, 8 or 16.  Default 8. */
+ * stroke kernel for this mesh: 1, 2, 4, 8 or 16, or SGPU_TEAM_GRID: every
+ * SM of the GPU works on the one stroke (one CTA per SM in a cooperative
+ * launch; the CTAs meet at barriers in global memory whose waits are bounded:
+ * a wait that runs out ends the launch and the call returns
+ * SGPU_ERR_TIMEOUT).  A batch with SGPU_TEAM_GRID runs its strokes one after
+ * another.  Default 8. */
+#define SGPU_TEAM_GRID (-1)
 int sgpu_mesh_set_team(sgpu_mesh *mesh, int cluster_size);
 int sgpu_mesh_get_team(const sgpu_mesh *mesh, int *cluster_size);
 /* Autotuner: times the stroke in SGPU_STROKE_TEAM mode for every cluster size,
@@ -445,6 +451,22 @@ int sgpu_smooth_dab_noalloc(float *co, const float *normals, const float *mask,
                             const float *automask, const int *nb_off, const int *nb_idx,
                             const int *verts, int nverts, const SGPU_Brush *brush,
                             const float location[3], void *stream);
+
+/* ---- failure injection (host side; for tests) ----
+ * SGPU_INJECT_ALLOC_FAIL, value n > 0: the n-th device allocation of mesh
+ *   creation from now on fails as out of memory (the create call returns
+ *   SGPU_ERR_OOM and frees what it had allocated); 0 disarms.
+ * SGPU_INJECT_WAIT_NS, value > 0: the wait limit of the whole-GPU team's
+ *   barriers in nanoseconds; 0 restores the default (2 s).
+ * SGPU_INJECT_BARRIER_EXTRA, value 1: those barriers wait for one arrival
+ *   more than the launch has, so every wait runs out after the limit and the
+ *   stroke returns SGPU_ERR_TIMEOUT; 0 disarms.
+ * No GPU fault is involved: the kernel gives up, records the status and
+ * returns.  Returns SGPU_ERR_INVALID_ARG for an unknown hook. */
+#define SGPU_INJECT_ALLOC_FAIL 1
+#define SGPU_INJECT_WAIT_NS 2
+#define SGPU_INJECT_BARRIER_EXTRA 3
+int sgpu_debug_inject(int what, int64_t value);
 
 /* ---- data access (synchronous) ---- */
 int sgpu_get_verts(sgpu_mesh *mesh, SGPU_MVert *out);          /* FACES */

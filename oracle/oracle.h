@@ -124,6 +124,24 @@ void or_get_vert_tags(const OrMesh *m, unsigned char *out);
 int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
                   const int *dab_tools, int which, int nthreads, int64_t *per_dab_counts);
 
+/* Copies the FP32 state (positions, normals, mask, boxes, stroke-start data)
+ * into the FP64 state, widening each value exactly. */
+void or_sync64(OrMesh *m);
+
+/* The FP32 stroke, with the rounding error of each measured dab (every
+ * stride-th, from dab 0) against FP64, stage by stage from the same input:
+ * the FP64 state is set to the FP32 one (or_sync64) before the brush, before
+ * the normal update and before the bounds refit, each stage runs in both
+ * precisions from the same node flags and vertex tags, and err[5*d .. 5*d+4]
+ * receives max|x32 - x64| / max|x64| of the positions (brush, and the GRIDS
+ * seam averages), max|x32 - x64| of the normals, the norm-wise relative
+ * error of the node boxes, and max|x32 - x64| of the area normal and of the
+ * area centre over the dab's passes (0 without the area reduction); -1 for
+ * dabs not measured.  The FP32 state ends as or_stroke(..., which = 1) leaves
+ * it.  Returns the FP32 vertices displaced. */
+int64_t or_stroke_local_error(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
+                              const int *dab_tools, int stride, int nthreads, double *err);
+
 /* BKE_pbvh_raycast (PBVH_FACES) with the sculpt ray-cast callback of the brush
  * specification.  depth: in = ray length, out = nearest hit depth.  Returns 1
  * on a hit (active vertex, its face and the hit triangle's normal set).

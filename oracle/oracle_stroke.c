@@ -122,6 +122,184 @@ int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
   return total;
 }
 
+/* Copies the FP32 state into the FP64 state (exact widening), so that an FP64
+ * step taken from there measures the rounding error of the same FP32 step. */
+static void widen(double *dst, const float *src, size_t n)
+{
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < (long long)n; i++) {
+    dst[i] = (double)src[i];
+  }
+}
+
+void or_sync64(OrMesh *m)
+{
+  const size_t v3 = 3 * (size_t)m->totvert, n6 = 6 * (size_t)m->totnode;
+  widen(m->sd.co, m->sf.co, v3);
+  widen(m->sd.no, m->sf.no, v3);
+  if (m->sf.mask) {
+    widen(m->sd.mask, m->sf.mask, (size_t)m->totvert);
+  }
+  widen(m->sd.vb, m->sf.vb, n6);
+  widen(m->sd.orig_vb, m->sf.orig_vb, n6);
+  if (m->sf.orig_co) {
+    if (!m->sd.orig_co) {
+      m->sd.orig_co = (double *)malloc(sizeof(double) * v3);
+      m->sd.orig_no = (double *)malloc(sizeof(double) * v3);
+      m->sd.layer_disp = (double *)malloc(sizeof(double) * (size_t)m->totvert);
+    }
+    widen(m->sd.orig_co, m->sf.orig_co, v3);
+    widen(m->sd.orig_no, m->sf.orig_no, v3);
+    widen(m->sd.layer_disp, m->sf.layer_disp, (size_t)m->totvert);
+  }
+}
+
+/* max |f - d| over n values, and max |d| */
+static void max_diff(const float *f, const double *d, size_t n, double *r_diff, double *r_ref)
+{
+  double md = 0.0, mr = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : md, mr)
+  for (long long i = 0; i < (long long)n; i++) {
+    const double e = fabs((double)f[i] - d[i]);
+    const double a = fabs(d[i]);
+    md = e > md ? e : md;
+    mr = a > mr ? a : mr;
+  }
+  *r_diff = md;
+  *r_ref = mr;
+}
+
+/* Node flags and vertex tags (FACES) of the oracle, saved and put back so
+ * that both precisions run a stage from the same flags. */
+typedef struct FlagState {
+  int *flags;
+  unsigned char *tags;
+} FlagState;
+
+static void flags_save(const OrMesh *m, FlagState *f)
+{
+  for (int n = 0; n < m->totnode; n++) {
+    f->flags[n] = m->nodes[n].flag;
+  }
+  if (m->vtag) {
+    memcpy(f->tags, m->vtag, (size_t)m->totvert);
+  }
+}
+
+static void flags_load(OrMesh *m, const FlagState *f)
+{
+  for (int n = 0; n < m->totnode; n++) {
+    m->nodes[n].flag = f->flags[n];
+  }
+  if (m->vtag) {
+    memcpy(m->vtag, f->tags, (size_t)m->totvert);
+  }
+}
+
+static void flags_alloc(const OrMesh *m, FlagState *f)
+{
+  f->flags = (int *)malloc(sizeof(int) * ((size_t)m->totnode + 1));
+  f->tags = (unsigned char *)malloc((size_t)m->totvert + 1);
+}
+
+static void flags_free(FlagState *f)
+{
+  free(f->flags);
+  free(f->tags);
+}
+
+static double rel_diff(const float *f, const double *d, size_t n)
+{
+  double diff, ref;
+  max_diff(f, d, n, &diff, &ref);
+  return ref > 0.0 ? diff / ref : diff;
+}
+
+int64_t or_stroke_local_error(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
+                              const int *tools, int stride, int nthreads, double *err)
+{
+#ifdef _OPENMP
+  if (nthreads > 0) {
+    omp_set_num_threads(nthreads);
+  }
+#else
+  (void)nthreads;
+#endif
+  OrCurve cu;
+  or_curve_build(b->curve_preset, &cu);
+  const size_t V = (size_t)m->totvert, v3 = 3 * V, n6 = 6 * (size_t)m->totnode;
+  int *nodes = (int *)malloc(sizeof(int) * (m->totnode + 1));
+  FlagState f0, fb, fu;
+  flags_alloc(m, &f0);
+  flags_alloc(m, &fb);
+  flags_alloc(m, &fu);
+  if (stroke_needs_start_f(b, ndabs, tools)) {
+    store_original_f(m, &m->sf);
+  }
+  int64_t total = 0;
+  for (int d = 0; d < ndabs; d++) {
+    double *e = err + 5 * (size_t)d;
+    if (stride <= 0 || d % stride != 0) {
+      total += stroke_dab_f(m, &m->sf, b, &cu, dabs, d, tools, nodes);
+      for (int k = 0; k < 5; k++) {
+        e[k] = -1.0;
+      }
+      continue;
+    }
+    /* brush stage from the same input */
+    flags_save(m, &f0);
+    or_sync64(m);
+    float area_f[48];
+    double area_d[48];
+    total += stroke_dab_brush_f(m, &m->sf, b, &cu, dabs, d, tools, nodes, area_f);
+    flags_save(m, &fb);
+    flags_load(m, &f0);
+    stroke_dab_brush_d(m, &m->sd, b, &cu, dabs, d, tools, nodes, area_d);
+    e[0] = rel_diff(m->sf.co, m->sd.co, v3);
+    double ea_no = 0.0, ea_co = 0.0;
+    for (int p = 0; p < 8; p++) {
+      for (int k = 0; k < 3; k++) {
+        const double dn = fabs((double)area_f[6 * p + k] - area_d[6 * p + k]);
+        const double dc = fabs((double)area_f[6 * p + 3 + k] - area_d[6 * p + 3 + k]);
+        ea_no = dn > ea_no ? dn : ea_no;
+        ea_co = dc > ea_co ? dc : ea_co;
+      }
+    }
+    e[3] = ea_no;
+    e[4] = ea_co;
+    /* normal update (GRIDS: with the seam averages of positions and masks)
+     * from the same positions */
+    or_sync64(m);
+    update_normals_f(m, &m->sf);
+    flags_save(m, &fu);
+    flags_load(m, &fb);
+    update_normals_d(m, &m->sd);
+    {
+      double diff, ref;
+      max_diff(m->sf.no, m->sd.no, v3, &diff, &ref);
+      e[1] = diff; /* unit vectors (GRIDS: means of unit vectors) */
+    }
+    const double eco = rel_diff(m->sf.co, m->sd.co, v3);
+    e[0] = eco > e[0] ? eco : e[0];
+    /* bounds refit from the same positions */
+    or_sync64(m);
+    flags_load(m, &fu);
+    update_bounds_f(m, &m->sf, OR_UpdateBB);
+    flags_save(m, &fb);
+    flags_load(m, &fu);
+    update_bounds_d(m, &m->sd, OR_UpdateBB);
+    flags_load(m, &fb);
+    e[2] = rel_diff(m->sf.vb, m->sd.vb, n6);
+    (void)V;
+  }
+  update_bounds_f(m, &m->sf, OR_UpdateOriginalBB);
+  free(nodes);
+  flags_free(&f0);
+  flags_free(&fb);
+  flags_free(&fu);
+  return total;
+}
+
 void or_store_original(OrMesh *m)
 {
   store_original_f(m, &m->sf);

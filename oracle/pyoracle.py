@@ -72,6 +72,9 @@ def lib():
         L.or_get_vert_tags.argtypes = [vp, vp]
         L.or_stroke.restype = C.c_int64
         L.or_stroke.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
+        L.or_sync64.argtypes = [vp]
+        L.or_stroke_local_error.restype = C.c_int64
+        L.or_stroke_local_error.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
         L.or_draw_build.restype = C.c_int64
         L.or_draw_build.argtypes = [vp, C.POINTER(OrDrawSetup), vp, vp, vp, vp]
         L.or_draw_update.argtypes = [vp, C.POINTER(OrDrawSetup), vp, vp, vp]
@@ -355,6 +358,25 @@ class OracleMesh:
         tot = lib().or_stroke(self.h, C.byref(b), _p(d), d.shape[0], _p(tools), which, nthreads,
                               _p(per))
         return int(tot), per
+
+    LOCAL_ERR_FIELDS = ("co", "no", "bb", "area_no", "area_co")
+
+    def stroke_local_error(self, st, dab_tools=None, stride: int = 1, nthreads: int = 0):
+        """The FP32 stroke with each measured dab's FP32-vs-FP64 error from the
+        same input state (or_stroke_local_error).  Returns (vertices displaced,
+        {field: max over the measured dabs})."""
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        err = np.zeros((d.shape[0], 5), dtype=np.float64)
+        tot = lib().or_stroke_local_error(self.h, C.byref(b), _p(d), d.shape[0], _p(tools),
+                                          stride, nthreads, _p(err))
+        measured = err[err[:, 0] >= 0]
+        return int(tot), {k: float(measured[:, i].max()) if measured.size else 0.0
+                          for i, k in enumerate(self.LOCAL_ERR_FIELDS)}
+
+    def sync64(self):
+        lib().or_sync64(self.h)
 
 
 def kelvinlet(kind: int, radius: float, force: float, poisson: float, co, location, dn):

@@ -60,3 +60,16 @@ def test_invalid_arguments_return_codes(lib):
 
 def test_version(lib):
     assert b"sm_103a" in lib.sgpu_version()
+
+
+def test_debug_inject_arguments(lib):
+    """The failure-injection hooks are host-side switches: they take and
+    reject values without touching a device."""
+    assert lib.sgpu_debug_inject(99, 0) == sculpt.ERR_INVALID_ARG
+    assert lib.sgpu_debug_inject(sculpt.INJECT_ALLOC_FAIL, -1) == sculpt.ERR_INVALID_ARG
+    assert lib.sgpu_debug_inject(sculpt.INJECT_BARRIER_EXTRA, 2) == sculpt.ERR_INVALID_ARG
+    for what, value in ((sculpt.INJECT_ALLOC_FAIL, 3), (sculpt.INJECT_WAIT_NS, 1000),
+                        (sculpt.INJECT_BARRIER_EXTRA, 1)):
+        assert lib.sgpu_debug_inject(what, value) == sculpt.OK
+    for what in (sculpt.INJECT_ALLOC_FAIL, sculpt.INJECT_WAIT_NS, sculpt.INJECT_BARRIER_EXTRA):
+        assert lib.sgpu_debug_inject(what, 0) == sculpt.OK

@@ -106,7 +106,7 @@ def test_grids_mixed_stroke(gpu, oracle):
     assert rel_err(gp.positions(), o.co64()) < FP64_TOL_GRIDS
 
 
-@pytest.mark.parametrize("cluster", [1, 8])
+@pytest.mark.parametrize("cluster", [1, 8, -1])
 def test_grids_team_stroke(gpu, oracle, cluster):
     """The persistent stroke kernel on multires grids, mixed tools, X mirror."""
     from dune_sculpt_gb300.sculpt import STROKE_TEAM

@@ -195,3 +195,24 @@ def test_stroke_host_original_brushes(gpu, oracle, tool):
     co = np.ascontiguousarray(vout["co"])
     assert bits_equal(co, o.co()), first_diff(co, o.co())
     _assert_equal(g, o, f"stroke_host tool {tool}")
+
+
+@pytest.mark.parametrize("tool,kind", [(synth.TOOL_GRAB, 0), (synth.TOOL_LAYER, 0),
+                                       (synth.TOOL_ELASTIC_DEFORM, 0),
+                                       (synth.TOOL_ELASTIC_DEFORM, 4)])
+def test_grid_team_original_brushes(gpu, oracle, tool, kind):
+    """The whole-GPU team runs grab, layer and elastic deform strokes itself
+    (elastic deform included: every SM sweeps the mesh)."""
+    from dune_sculpt_gb300.sculpt import TEAM_GRID
+
+    m = small_icosphere(5)
+    g, o = _pair(oracle, m, 600)
+    g.set_team(TEAM_GRID)
+    dabs = synth.arc_dabs(13, 16, 0.04) if tool == synth.TOOL_LAYER else synth.grab_dabs(3, 10, 0.02)
+    st = synth.Stroke(tool, 0.2, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X, dabs, height=0.3,
+                      elastic_deform_type=kind, elastic_deform_volume_preservation=0.3)
+    s = g.stroke(st, mode=STROKE_TEAM)
+    assert s.kernel_launches == 1  # the persistent launch, not a graph replay
+    tot, _ = o.stroke(st, which=1)
+    assert s.verts_displaced == tot and tot > 0
+    _assert_equal(g, o, f"grid team tool {tool}")

@@ -215,11 +215,11 @@ def test_use_original_bb(gpu, oracle):
 # Persistent stroke kernel (one launch per stroke or per batch)
 
 from dune_sculpt_gb300.sculpt import (BATCH_SEQUENTIAL, BATCH_TEAM, STROKE_TEAM,  # noqa: E402
-                                      batch_stroke)
+                                      TEAM_GRID, batch_stroke)
 
 
 @pytest.mark.parametrize("tool", TOOLS)
-@pytest.mark.parametrize("cluster", [1, 4, 16])
+@pytest.mark.parametrize("cluster", [1, 4, 16, TEAM_GRID])
 def test_team_stroke_parity(gpu, oracle, case, tool, cluster):
     name, m, ll = case
     g, o = _pair(gpu, oracle, m, ll)
@@ -261,8 +261,9 @@ def _assert_state_equal_gpu(a, b):
         assert bits_equal(x, y), first_diff(x, y)
 
 
-@pytest.mark.parametrize("mode", [BATCH_SEQUENTIAL, BATCH_TEAM])
-def test_batch_matches_oracle(gpu, oracle, mode):
+@pytest.mark.parametrize("mode,cluster", [(BATCH_SEQUENTIAL, 4), (BATCH_TEAM, 4),
+                                          (BATCH_TEAM, TEAM_GRID)])
+def test_batch_matches_oracle(gpu, oracle, mode, cluster):
     batch = synth.cfg4_batch(nmesh=6, vmin=2000, vmax=20000, ndabs=10)
     gs, os_, strokes = [], [], []
     for k, (m, st, ll) in enumerate(batch):
@@ -274,7 +275,7 @@ def test_batch_matches_oracle(gpu, oracle, mode):
         if k % 3 == 1:
             st.symmetry = synth.SYMM_X
         strokes.append(st)
-    stats, total_ms = batch_stroke(gs, strokes, mode=mode, cluster=4)
+    stats, total_ms = batch_stroke(gs, strokes, mode=mode, cluster=cluster)
     assert total_ms > 0
     for g, o, st, s in zip(gs, os_, strokes, stats):
         tot, _ = o.stroke(st, which=1)
