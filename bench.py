@@ -1,41 +1,54 @@
 #!/usr/bin/env python
 """Benchmark of the sculpt-brush dab path: vertices displaced per second.
 
-Default workload (one GPU): the masked, X-mirrored smooth-brush stroke of 128
-dabs on a noisy level-8 icosphere (655,362 vertices, 1,310,720 looptris,
-PBVH leaf limit 5000 looptris), seeded synthetic input.  A step is that whole
-stroke: per dab and symmetry pass the node search and the brush, then the
-normal update and bounding-box refit, as the reference's stroke does.
+Default workload (one GPU, --workload multires): the multires (PBVH_GRIDS)
+stroke of the fifth configuration, the largest single-GPU one: 50,000 grids of
+17x17 elements (14.45 M) on a seeded noise-displaced torus (R=1, r=0.35), a
+seeded value-noise mask, 256 dabs alternating draw / smooth / inflate, radius
+0.04, strength 0.6; per dab the node search and the brush, then the grid
+normal update with seam stitching and the bounding-box refit, as the
+reference's stroke does.  Seeded synthetic input (no dataset).  A step is that
+whole stroke.  --workload icosphere (masked X-mirrored smooth, 655,362 verts,
+128 dabs), clay (clay strips on a 4,194,304-vertex sphere, X mirror, 256
+dabs) and grid (draw on a 513x513 grid, 64 dabs) select the other
+single-mesh configurations.
 
-  value  : device-resident throughput — Sum(vertices displaced) / Sum(stroke
-           time), stroke time from CUDA events on the mesh stream; the stroke
-           runs as one launch of the persistent stroke kernel (cluster size
-           picked by the autotuner); positions, normals and node boxes are
-           restored from a device snapshot and L2 flushed (256 MiB write, then a
-           256 MiB read of another buffer)
-           before every step, both outside the timed region.
-  e2e    : the same through sgpu_stroke_host with page-locked host buffers:
-           H2D of positions and normals, full box refit, stroke, D2H of
-           positions, all inside the event-timed region.
-  roofline: k_team_stroke (the only kernel of a step): algorithmic bytes per
-           launch (the kernel's own counters, an instrumented run) / mean
-           step time of the timed run, against the measured HBM copy
+  value  : device-resident throughput, Sum(vertices displaced) / Sum(stroke
+           time); the stroke is one launch of the persistent stroke kernel on
+           the autotuned team (the whole GPU or a cluster), CUDA events on the
+           mesh stream; positions, normals, masks and node boxes are restored
+           from a device snapshot and L2 is flushed (256 MiB write, then a
+           256 MiB read of another buffer) before every step, both outside the
+           timed region.
+  e2e    : the same stroke through the host-buffer entry point
+           (sgpu_stroke_host_grids / sgpu_stroke_host) with page-locked
+           buffers: positions and normals in, every leaf box refit, the
+           stroke, positions out, all inside the event-timed region.
+  roofline: k_team_stroke, the only kernel of a step: its algorithmic bytes
+           per launch (the kernel's own counters, an instrumented run) / the
+           mean step time of the timed run, against the measured HBM copy
            bandwidth.
-  plain_graph / plain_eager: the same stroke through the per-call kernels
-           (one kernel per reference call), replayed as a CUDA graph / eager.
-  batch  : the 64-mesh uneven batch, one persistent launch versus 64
-           sequential plain strokes.
-  cpu_baseline: the FP32 CPU restatement (oracle, OpenMP over PBVH nodes) on
-           the host cores, same stroke.
+  max_rel_err: the GPU's positions after the timed strokes against the FP32
+           restatement (bit for bit), and the restatement's error against FP64
+           per dab (each stage from the same input) and over the whole stroke.
+  batch  : the 64-mesh uneven batch (fourth configuration), one persistent
+           launch on the batch autotuner's team versus 64 sequential plain
+           strokes; algorithmic bytes and HBM fraction.
+  batched_clay / batched_multires: K independent seeded strokes on K meshes
+           of the clay / multires workload in one persistent launch (the
+           batched form), with their HBM fraction.
+  cpu_baseline: the FP32 restatement (oracle, OpenMP over PBVH nodes) of the
+           same whole stroke on all host cores.
 
---quick runs three persistent strokes of the workload and exits (the
-command profiled with ncu).  --phases prints the persistent kernel's per-dab
-phase profile on all five workloads.
+--quick runs three persistent strokes of the workload and exits (the command
+profiled with ncu).  --phases prints the persistent kernel's per-dab phase
+profile on the single-mesh workloads.
 
---impl reference times the CPU restatement of the reference path (the
-reference cannot run the path: its brush code and public headers are missing).
-Under torchrun (N>1) each rank runs an independent replica (the path does not
-shard within a mesh); rank 0 prints max-over-ranks timing.
+--impl reference times the CPU restatement of the reference path on the same
+workload and config (the reference cannot run the path: its brush code and
+public headers are missing), the whole stroke per step.  Under torchrun (N>1)
+each rank runs an independent replica (the path does not shard within a
+mesh); rank 0 prints max-over-ranks timing.
 """
 from __future__ import annotations
 
@@ -47,6 +60,7 @@ import subprocess
 import sys
 import tempfile
 import time
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -55,117 +69,121 @@ sys.path.insert(0, ROOT)
 
 METRIC = "vertices displaced/sec"
 UNIT = "verts/s"
+L2_NOTE = "flushed before every step (256 MiB device write, then 256 MiB read)"
 
 
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--cpu-sample-dabs", type=int, default=0,
-                    help="dabs of the stroke in the CPU sample (0 = whole stroke)")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--no-batch", action="store_true", help="skip the 64-mesh batch comparison")
+    ap.add_argument("--workload", choices=["multires", "icosphere", "clay", "grid"],
+                    default="multires")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and checks")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-mesh batch leg")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched clay / multires legs")
+    ap.add_argument("--batched-k", type=int, default=8,
+                    help="strokes (meshes) of the batched clay / multires legs")
+    ap.add_argument("--no-legs", action="store_true", help="skip the ray-cast and draw legs")
     ap.add_argument("--quick", action="store_true",
                     help="three persistent strokes of the workload, no report (for ncu)")
-    ap.add_argument("--cluster", type=int, default=16, help="cluster size for --quick")
+    ap.add_argument("--team", type=int, default=0,
+                    help="team for --quick: cluster size, -1 for the whole GPU, 0 autotuned")
     ap.add_argument("--raycast-only", action="store_true",
-                    help="1024-ray sgpu_raycast batches on the workload mesh and on the "
-                         "multires torus, one JSON line, and exit (the command profiled "
-                         "with ncu for the ray kernels)")
+                    help="1024-ray sgpu_raycast batches on the icosphere and on the multires "
+                         "torus, one JSON line, and exit (the command profiled with ncu for "
+                         "the ray kernels)")
     ap.add_argument("--raycast-mesh", choices=["faces", "grids", "both"], default="both",
                     help="meshes of --raycast-only")
     ap.add_argument("--draw-only", action="store_true",
-                    help="full draw-buffer refreshes on the workload mesh and on the multires "
+                    help="full draw-buffer refreshes on the icosphere and on the multires "
                          "torus, one JSON line, and exit (the command profiled with ncu for "
                          "the draw kernels)")
     ap.add_argument("--draw-mesh", choices=["faces", "grids", "both"], default="both",
                     help="meshes of --draw-only")
     ap.add_argument("--phases", action="store_true",
-                    help="per-phase profile of the persistent stroke on the five workloads "
-                         "and the stroke-start brushes "
-                         "(one JSON line each), no report")
+                    help="per-phase profile of the persistent stroke on the single-mesh "
+                         "workloads (one JSON line each), no report")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="the batched clay / multires legs only, one JSON line")
     return ap.parse_args()
 
 
-def run_quick(args):
-    from dune_sculpt_gb300 import build as libbuild
+@dataclass
+class Workload:
+    name: str
+    kind: str            # "faces" or "grids"
+    mesh: object         # synth.FacesMesh or synth.GridsMesh
+    stroke: object       # synth.Stroke
+    tools: object        # per-dab tools or None
+    leaf_limit: int
+    cfg: dict
 
-    libbuild.build()
-    from dune_sculpt_gb300.sculpt import PBVH, STROKE_TEAM
-
-    m, st, leaf_limit, _ = workload()
-    g = PBVH.build_mesh(m, leaf_limit)
-    g.snapshot()
-    g.set_team(args.cluster)
-    for _ in range(3):
-        g.restore()
-        s = g.stroke(st, mode=STROKE_TEAM)
-    print(f"quick: {s.verts_displaced} vertices displaced, {s.gpu_ms:.3f} ms")
-    return 0
+    @property
+    def nverts(self) -> int:
+        return int(self.mesh.co.shape[0]) if self.kind == "grids" else int(self.mesh.totvert)
 
 
-def run_phases(args):
-    """Per-dab phase times of the persistent stroke kernel on the five workloads:
-    the autotuned cluster, the best of three L2-flushed strokes, then one
-    instrumented stroke (phase timers of the team's first thread)."""
-    from dune_sculpt_gb300 import build as libbuild
+def multires_tools(synth, n):
+    return np.array([(synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE)[d % 3]
+                     for d in range(n)], dtype=np.int32)
 
-    libbuild.build()
+
+def workload(name: str = "multires") -> Workload:
+    """The single-mesh configurations; cfg is the same dict in both arms."""
     from dune_sculpt_gb300 import synth
-    from dune_sculpt_gb300.sculpt import PBVH, STROKE_GRAPH, STROKE_TEAM
 
-    def one(name, g, st, tools=None, graph=False):
-        g.snapshot()
-        best, _ = g.autotune_team(st, dab_tools=tools)
-        times = []
-        for _ in range(3):
-            g.restore()
-            g.flush_l2()
-            times.append(g.stroke(st, mode=STROKE_TEAM, dab_tools=tools).gpu_ms)
-        extra = {}
-        if graph:  # the same stroke replayed from a CUDA graph of the per-call kernels
-            gt = []
-            for _ in range(3):
-                g.restore()
-                g.flush_l2()
-                gt.append(g.stroke(st, mode=STROKE_GRAPH, dab_tools=tools).gpu_ms)
-            extra["graph_ms_per_stroke"] = round(min(gt), 3)
-        g.restore()
-        g.flush_l2()
-        ph, _, stats = g.stroke_team_profile(st, dab_tools=tools)
-        nd = st.dabs.shape[0]
-        print(json.dumps({
-            "workload": name, "cluster": best, "ms_per_stroke": round(min(times), 3),
-            "us_per_dab": round(1000 * min(times) / nd, 2),
-            "verts_displaced": stats.verts_displaced, **extra,
-            "phase_us_per_dab": {k: round(1000 * v["ms"] / nd, 2) for k, v in ph.items()},
-            "phase_alg_MB_per_stroke": {k: round(v["bytes"] / 1e6, 2) for k, v in ph.items()}}),
-            flush=True)
-        g.free()
+    if name == "multires":
+        g, dabs = synth.cfg5_multires()
+        st = synth.Stroke(synth.TOOL_DRAW, 0.04, 0.6, synth.CURVE_SMOOTH, 0, dabs)
+        cfg = {"workload": "multires_torus_50000x17x17_mixed", "grids": g.num_grids,
+               "grid_size": g.grid_size, "elements": int(g.co.shape[0]),
+               "dabs": int(dabs.shape[0]), "tools": "draw/smooth/inflate alternating",
+               "radius": 0.04, "strength": 0.6, "symmetry": "none", "curve": "smooth",
+               "mask": "seeded value noise", "leaf_limit": "34 grids (10000 // 289)",
+               "l2": L2_NOTE}
+        return Workload(name, "grids", g, st, multires_tools(synth, dabs.shape[0]), 0, cfg)
+    if name == "clay":
+        m, st, ll = synth.cfg3_sphere_clay()
+        cfg = {"workload": "uvsphere2048_clay_strips_xmirror", "verts": int(m.totvert),
+               "looptris": int(m.looptris.shape[0]), "dabs": int(st.dabs.shape[0]),
+               "radius": st.radius, "strength": st.strength, "symmetry": "X", "curve": "sharp",
+               "leaf_limit": ll, "l2": L2_NOTE}
+        return Workload(name, "faces", m, st, None, ll, cfg)
+    if name == "grid":
+        m, st, ll = synth.cfg1_grid_draw()
+        cfg = {"workload": "grid513_draw", "verts": int(m.totvert),
+               "looptris": int(m.looptris.shape[0]), "dabs": int(st.dabs.shape[0]),
+               "radius": st.radius, "strength": st.strength, "symmetry": "none",
+               "curve": "smooth", "leaf_limit": ll, "l2": L2_NOTE}
+        return Workload(name, "faces", m, st, None, ll, cfg)
+    m, st, ll = synth.cfg2_icosphere_smooth()
+    cfg = {"workload": "icosphere8_smooth_masked_xmirror", "verts": int(m.totvert),
+           "looptris": int(m.looptris.shape[0]), "dabs": int(st.dabs.shape[0]),
+           "radius": st.radius, "strength": st.strength, "symmetry": "X", "curve": "smooth",
+           "leaf_limit": ll, "mask": "seeded smooth noise", "l2": L2_NOTE}
+    return Workload("icosphere", "faces", m, st, None, ll, cfg)
 
-    m, st, ll = synth.cfg1_grid_draw()
-    one("grid513_draw", PBVH.build_mesh(m, ll), st)
-    m, st, ll = synth.cfg2_icosphere_smooth()
-    one("icosphere8_smooth_masked_xmirror", PBVH.build_mesh(m, ll), st)
-    m, st, ll = synth.cfg3_sphere_clay()
-    one("uvsphere2048_clay_strips_xmirror", PBVH.build_mesh(m, ll), st)
-    g, dabs = synth.cfg5_multires()
-    tools = np.array([(synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE)[d % 3]
-                      for d in range(dabs.shape[0])], dtype=np.int32)
-    st = synth.Stroke(synth.TOOL_DRAW, 0.04, 0.6, synth.CURVE_SMOOTH, 0, dabs)
-    one("multires_torus_50000x17x17_mixed", PBVH.build_grids(g), st, tools)
-    # the stroke-start brushes on the icosphere of the bench workload (128
-    # dabs, X mirror): persistent and graph-replayed
-    m, st, ll = synth.cfg2_icosphere_smooth()
-    grab = synth.grab_dabs(synth.SEED_BASE + 40, st.dabs.shape[0], 0.0005)
-    for name, tool, dabs, kw in (
-            ("grab", synth.TOOL_GRAB, grab, {}),
-            ("layer", synth.TOOL_LAYER, st.dabs, {"height": 0.3})):
-        so = synth.Stroke(tool, st.radius, st.strength, synth.CURVE_SMOOTH, synth.SYMM_X, dabs, **kw)
-        one(f"icosphere8_{name}_xmirror", PBVH.build_mesh(m, ll), so, graph=True)
-    return 0
+
+def build_gpu(W: Workload):
+    from dune_sculpt_gb300.sculpt import PBVH
+
+    if W.kind == "grids":
+        return PBVH.build_grids(W.mesh, W.leaf_limit)
+    return PBVH.build_mesh(W.mesh, W.leaf_limit)
+
+
+def build_oracle(W: Workload):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    o = (pyoracle.OracleMesh.grids(W.mesh, W.leaf_limit) if W.kind == "grids"
+         else pyoracle.OracleMesh.faces(W.mesh, W.leaf_limit))
+    o.recalc_all_normals()
+    return o
 
 
 def dist_env():
@@ -184,16 +202,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def workload():
-    from dune_sculpt_gb300 import synth
-
-    m, st, leaf_limit = synth.cfg2_icosphere_smooth()
-    cfg = {"workload": "icosphere8_smooth_masked_xmirror", "verts": int(m.totvert),
-           "looptris": int(m.looptris.shape[0]), "dabs": int(st.dabs.shape[0]),
-           "radius": st.radius, "strength": st.strength, "symmetry": "X",
-           "curve": "smooth", "leaf_limit": leaf_limit, "mask": "seeded smooth noise",
-           "l2": "flushed before every step (256 MiB device write, then 256 MiB read)"}
-    return m, st, leaf_limit, cfg
+def traffic_for(workload_name: str):
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            return json.load(f).get(workload_name, {}).get("k_team_stroke")
+    return None
 
 
 class ClockSampler:
@@ -256,70 +270,6 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def cpu_baseline(m, st, leaf_limit, sample_dabs: int):
-    """FP32 CPU restatement (oracle) on all host cores: a bounded sample of the
-    same stroke (the first sample_dabs dabs, or the whole stroke)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-
-    pyoracle.build()
-    o = pyoracle.OracleMesh.faces(m, leaf_limit)
-    o.recalc_all_normals()
-    dabs = st.dabs if not sample_dabs else st.dabs[:sample_dabs]
-    threads = pyoracle.max_threads()
-    t0 = time.perf_counter()
-    tot, _ = o.stroke(st, which=1, nthreads=threads, dabs=dabs)
-    dt = time.perf_counter() - t0
-    o.close()
-    return {"value": tot / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{dabs.shape[0]} of {st.dabs.shape[0]} dabs of the same stroke, "
-                      f"{tot} vertices displaced in {dt:.3f} s (FP32 restatement, OpenMP "
-                      f"over PBVH nodes)", "seconds": dt}
-
-
-def run_reference(args):
-    world, rank, _ = dist_env()
-    if rank != 0:
-        return 0
-    m, st, leaf_limit, cfg = workload()
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-
-    pyoracle.build()
-    sample = args.cpu_sample_dabs or 32
-    dabs = st.dabs[:sample]
-    threads = pyoracle.max_threads()
-
-    def fresh():
-        o = pyoracle.OracleMesh.faces(m, leaf_limit)
-        o.recalc_all_normals()
-        return o
-
-    for _ in range(args.warmup):
-        fresh().stroke(st, which=1, nthreads=threads, dabs=dabs)
-    total_v, total_s = 0, 0.0
-    for _ in range(args.steps):
-        o = fresh()  # every step starts from the same mesh state (untimed)
-        t0 = time.perf_counter()
-        tot, _ = o.stroke(st, which=1, nthreads=threads, dabs=dabs)
-        total_s += time.perf_counter() - t0
-        total_v += tot
-        o.close()
-    value = total_v / total_s
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)", "config": cfg,
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"first {sample} of {st.dabs.shape[0]} dabs per step "
-                                       "(FP32 CPU restatement of the reference path: the "
-                                       "reference has no brush code to run)"},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-    return 0
-
 
 def combine_ranks(dist, total_ms, e2e_ms, total_v, e2e_v):
     """Replicas: the slowest rank's times (max) and every rank's vertices
@@ -332,141 +282,6 @@ def combine_ranks(dist, total_ms, e2e_ms, total_v, e2e_v):
     dist.all_reduce(c, op=dist.ReduceOp.SUM)
     return float(t[0]), float(t[1]), int(c[0]), int(c[1])
 
-
-def run_gpu(args):
-    world, rank, local = dist_env()
-    if world > 1:
-        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
-    from dune_sculpt_gb300 import build as libbuild
-
-    libbuild.build()
-    from dune_sculpt_gb300 import synth
-    from dune_sculpt_gb300.sculpt import (BATCH_SEQUENTIAL, BATCH_TEAM, PBVH, STROKE_EAGER,
-                                          STROKE_GRAPH, STROKE_TEAM, PinnedArray, batch_stroke)
-
-    m, st, leaf_limit, cfg = workload()
-    g = PBVH.build_mesh(m, leaf_limit)
-    g.snapshot()
-    cluster, tune_ms = g.autotune_team(st)  # restores the snapshot
-
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    for _ in range(args.warmup):
-        g.restore()
-        g.stroke(st, mode=STROKE_TEAM)
-    barrier()
-    clocks = ClockSampler(local) if rank == 0 else None
-    if clocks:
-        clocks.wait_first()
-    total_ms, total_v, launches = 0.0, 0, 0
-    for _ in range(args.steps):
-        g.restore()
-        g.flush_l2()
-        s = g.stroke(st, mode=STROKE_TEAM)
-        total_ms += s.gpu_ms
-        total_v += s.verts_displaced
-        launches += s.kernel_launches
-    g.sync()
-    barrier()
-    clk = clocks.stop() if clocks else None
-
-    # the same stroke through the per-call kernels: captured graph, and eager
-    def plain(mode, n=2):
-        ms, v = 0.0, 0
-        for _ in range(n):
-            g.restore()
-            g.flush_l2()
-            se = g.stroke(st, mode=mode)
-            ms += se.gpu_ms
-            v += se.verts_displaced
-        return {"value": v / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / n}
-
-    g.restore()
-    g.stroke(st, mode=STROKE_GRAPH)  # graph capture outside the timing
-    plain_graph = plain(STROKE_GRAPH)
-    plain_eager = plain(STROKE_EAGER)
-
-    # e2e through the host-buffer entry point with page-locked buffers
-    V = m.totvert
-    vin = PinnedArray((V,), m.verts.dtype)
-    vin.array[:] = m.verts
-    g.restore()
-    nin = PinnedArray((V, 3), np.float32)
-    nin.array[:] = g.normals()
-    vout = PinnedArray((V,), m.verts.dtype)
-    g.restore()
-    g.stroke_host(st, vin.array, vout.array, nin.array, mode=STROKE_TEAM)
-    e2e_ms, e2e_v = 0.0, 0
-    for _ in range(args.steps):
-        g.restore()
-        g.flush_l2()
-        s2 = g.stroke_host(st, vin.array, vout.array, nin.array, mode=STROKE_TEAM)
-        e2e_ms += s2.gpu_ms
-        e2e_v += s2.verts_displaced
-
-    # phase profile of the persistent kernel (instrumented run, not timed)
-    g.restore()
-    g.flush_l2()
-    phases, prof_ms, _ = g.stroke_team_profile(st)
-    alg_bytes = sum(p["bytes"] for p in phases.values())
-
-    batch = None if args.no_batch else run_batch(args, synth, PBVH, batch_stroke, BATCH_TEAM,
-                                                  BATCH_SEQUENTIAL)
-    g.restore()
-    ray = run_raycast_leg(g, m, leaf_limit, args.no_cpu)
-    g.restore()
-    draw = run_draw_leg(g, m, st, leaf_limit, args.no_cpu, peak=measured_peaks()[0])
-
-    if world > 1:
-        total_ms, e2e_ms, total_v, e2e_v = combine_ranks(dist, total_ms, e2e_ms, total_v, e2e_v)
-    if rank != 0:
-        return 0
-
-    peak, peak_kind = measured_peaks()
-    step_ms = total_ms / args.steps
-    achieved = alg_bytes / (step_ms / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(cfg["workload"], {}).get("k_team_stroke")
-    cpu = None
-    if not args.no_cpu:
-        cpu = cpu_baseline(m, st, leaf_limit, args.cpu_sample_dabs)
-    value = total_v / (total_ms / 1e3)
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded icosphere, Gaussian radial noise, smooth-noise mask)",
-        "config": dict(cfg, parallelism=f"replicas{world}",
-                       mode=f"persistent stroke kernel, cluster of {cluster} CTAs (autotuned)"),
-        "e2e": {"value": e2e_v / (e2e_ms / 1e3), "unit": UNIT,
-                "h2d_bytes_per_step": int(V * 16 + V * 12), "d2h_bytes_per_step": int(V * 16)},
-        "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS hbm_gbs)",
-                     "alg_bytes_per_launch": alg_bytes, "mean_launch_ms": step_ms,
-                     "traffic": traffic},
-        "team_phases_ms": {k: round(v["ms"], 4) for k, v in phases.items()},
-        "team_phases_bytes": {k: v["bytes"] for k, v in phases.items()},
-        "autotune_ms": tune_ms,
-        "plain_graph": plain_graph,
-        "plain_eager": plain_eager,
-        "batch": batch,
-        "raycast": ray,
-        "draw_buffers": draw,
-        "cpu_baseline": ({k: v for k, v in cpu.items() if k != "seconds"} if cpu else None),
-        "clocks": clk,
-    }
-    print(json.dumps(line))
-    return 0
 
 
 def draw_alg_bytes(g, masked: bool) -> int:
@@ -636,47 +451,480 @@ def run_raycast_leg(g, m, leaf_limit, no_cpu):
     return out
 
 
-def run_batch(args, synth, PBVH, batch_stroke, BATCH_TEAM, BATCH_SEQUENTIAL):
-    """The 64-mesh uneven batch: one persistent launch versus 64 sequential
-    plain strokes (each a CUDA graph of per-call kernels)."""
+
+def rel_err(x, ref) -> float:
+    """Norm-wise relative error max|x - ref| / max|ref|."""
+    ref = np.asarray(ref, dtype=np.float64)
+    return float(np.abs(np.asarray(x, dtype=np.float64) - ref).max() /
+                 max(np.abs(ref).max(), 1e-30))
+
+
+def cpu_baseline(W: Workload, gpu_positions=None, fp64_stride: int = 16):
+    """The FP32 restatement (oracle) of the same whole stroke on all host cores,
+    timed; then, as the checker, the GPU's positions against it and the
+    restatement's error against FP64 (per dab, each stage from the same input,
+    every fp64_stride-th dab; and an independent FP64 stroke)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    o = build_oracle(W)
+    threads = pyoracle.max_threads()
+    t0 = time.perf_counter()
+    tot, _ = o.stroke(W.stroke, which=1, nthreads=threads, dab_tools=W.tools)
+    dt = time.perf_counter() - t0
+    out = {"value": tot / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"the whole stroke ({W.stroke.dabs.shape[0]} dabs), {tot} vertices "
+                     f"displaced in {dt:.3f} s (FP32 restatement, OpenMP over PBVH nodes)",
+           "seconds": dt}
+    err = {}
+    if gpu_positions is not None:
+        co = o.co()
+        err["positions_bit_exact_vs_fp32_restatement"] = bool(
+            np.array_equal(np.ascontiguousarray(gpu_positions).view(np.uint32),
+                           np.ascontiguousarray(co).view(np.uint32)))
+        err["vs_fp32_restatement"] = rel_err(gpu_positions, co)
+    o.close()
+    o = build_oracle(W)
+    _, local = o.stroke_local_error(W.stroke, dab_tools=W.tools, stride=fp64_stride,
+                                    nthreads=threads)
+    o.close()
+    err["vs_fp64_per_dab"] = {k: float(f"{v:.3g}") for k, v in local.items()}
+    err["vs_fp64_per_dab_measured_dabs"] = f"every {fp64_stride}th"
+    o = build_oracle(W)
+    o.stroke(W.stroke, which=3, nthreads=threads, dab_tools=W.tools)
+    err["vs_fp64_whole_stroke"] = {"co": float(f"{rel_err(o.co(), o.co64()):.3g}"),
+                                   "no": float(f"{np.abs(o.no() - o.no64()).max():.3g}")}
+    o.close()
+    err["note"] = ("positions: norm-wise relative max|x - ref| / max|ref|; normals, area: "
+                   "absolute; per dab: each stage (brush, normal update, refit) from the same "
+                   "input in both precisions; whole stroke: independent FP32 and FP64 strokes")
+    return out, err
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    W = workload(args.workload)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    threads = pyoracle.max_threads()
+    for _ in range(args.warmup):
+        o = build_oracle(W)
+        o.stroke(W.stroke, which=1, nthreads=threads, dab_tools=W.tools)
+        o.close()
+    total_v, total_s = 0, 0.0
+    for _ in range(args.steps):
+        o = build_oracle(W)  # every step starts from the same mesh state (untimed)
+        t0 = time.perf_counter()
+        tot, _ = o.stroke(W.stroke, which=1, nthreads=threads, dab_tools=W.tools)
+        total_s += time.perf_counter() - t0
+        total_v += tot
+        o.close()
+    value = total_v / total_s
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": W.cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"the whole stroke ({W.stroke.dabs.shape[0]} dabs) per "
+                                       "step (FP32 CPU restatement of the reference path: the "
+                                       "reference has no brush code to run)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def team_label(team: int) -> str:
+    return "whole GPU (one CTA per SM)" if team == -1 else f"cluster of {team} CTAs"
+
+
+def run_gpu(args):
+    world, rank, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    from dune_sculpt_gb300 import build as libbuild
+
+    libbuild.build()
+    from dune_sculpt_gb300 import synth
+    from dune_sculpt_gb300.sculpt import (BATCH_SEQUENTIAL, BATCH_TEAM, PBVH, STROKE_EAGER,
+                                          STROKE_GRAPH, STROKE_TEAM, PinnedArray, autotune_batch,
+                                          batch_stroke)
+
+    W = workload(args.workload)
+    st, tools = W.stroke, W.tools
+    g = build_gpu(W)
+    g.snapshot()
+    team, tune_ms = g.autotune_team(st, dab_tools=tools)  # restores the snapshot
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        g.restore()
+        g.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
+    barrier()
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.wait_first()
+    total_ms, total_v, launches = 0.0, 0, 0
+    for _ in range(args.steps):
+        g.restore()
+        g.flush_l2()
+        s = g.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
+        total_ms += s.gpu_ms
+        total_v += s.verts_displaced
+        launches += s.kernel_launches
+    g.sync()
+    barrier()
+    clk = clocks.stop() if clocks else None
+    final_positions = g.positions()
+
+    # the same stroke through the per-call kernels: captured graph, and eager
+    def plain(mode, n=2):
+        ms, v = 0.0, 0
+        for _ in range(n):
+            g.restore()
+            g.flush_l2()
+            se = g.stroke(st, mode=mode, dab_tools=tools)
+            ms += se.gpu_ms
+            v += se.verts_displaced
+        return {"value": v / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / n}
+
+    g.restore()
+    g.stroke(st, mode=STROKE_GRAPH, dab_tools=tools)  # graph capture outside the timing
+    plain_graph = plain(STROKE_GRAPH)
+    plain_eager = plain(STROKE_EAGER)
+
+    # e2e through the host-buffer entry point with page-locked buffers
+    V = W.nverts
+    g.restore()
+    nin = PinnedArray((V, 3), np.float32)
+    nin.array[:] = g.normals()
+    if W.kind == "grids":
+        cin = PinnedArray((V, 3), np.float32)
+        cin.array[:] = W.mesh.co
+        cout = PinnedArray((V, 3), np.float32)
+
+        def host_stroke():
+            return g.stroke_host_grids(st, cin.array, cout.array, nin.array, dab_tools=tools,
+                                       mode=STROKE_TEAM)
+
+        h2d, d2h = V * 12 + V * 12, V * 12
+    else:
+        cin = PinnedArray((V,), W.mesh.verts.dtype)
+        cin.array[:] = W.mesh.verts
+        cout = PinnedArray((V,), W.mesh.verts.dtype)
+
+        def host_stroke():
+            return g.stroke_host(st, cin.array, cout.array, nin.array, dab_tools=tools,
+                                 mode=STROKE_TEAM)
+
+        h2d, d2h = V * 16 + V * 12, V * 16
+    g.restore()
+    host_stroke()
+    e2e_ms, e2e_v = 0.0, 0
+    for _ in range(args.steps):
+        g.restore()
+        g.flush_l2()
+        s2 = host_stroke()
+        e2e_ms += s2.gpu_ms
+        e2e_v += s2.verts_displaced
+
+    # phase profile of the persistent kernel (instrumented run, not timed)
+    g.restore()
+    g.flush_l2()
+    phases, _, _ = g.stroke_team_profile(st, dab_tools=tools)
+    alg_bytes = sum(p["bytes"] for p in phases.values())
+    g.free()
+
+    peak, peak_kind = measured_peaks()
+    batch = None if args.no_batch else run_batch(synth, PBVH, batch_stroke, autotune_batch,
+                                                  BATCH_TEAM, BATCH_SEQUENTIAL, peak,
+                                                  no_cpu=args.no_cpu)
+    batched = None if args.no_batched else run_batched(args.batched_k, peak, no_cpu=args.no_cpu)
+    ray = draw = None
+    if not args.no_legs:
+        Wi = workload("icosphere")
+        gi = build_gpu(Wi)
+        gi.snapshot()
+        ray = run_raycast_leg(gi, Wi.mesh, Wi.leaf_limit, args.no_cpu)
+        gi.restore()
+        draw = run_draw_leg(gi, Wi.mesh, Wi.stroke, Wi.leaf_limit, args.no_cpu, peak=peak)
+        gi.free()
+
+    if world > 1:
+        total_ms, e2e_ms, total_v, e2e_v = combine_ranks(dist, total_ms, e2e_ms, total_v, e2e_v)
+    if rank != 0:
+        return 0
+
+    step_ms = total_ms / args.steps
+    achieved = alg_bytes / (step_ms / 1e3) / 1e9
+    cpu, err = (None, None)
+    if not args.no_cpu:
+        cpu, err = cpu_baseline(W, final_positions)
+    value = total_v / (total_ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; no dataset)", "config": W.cfg,
+        "parallelism": f"replicas{world}",
+        "mode": f"persistent stroke kernel, {team_label(team)} (autotuned)",
+        "e2e": {"value": e2e_v / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "path": "sgpu_stroke_host_grids" if W.kind == "grids" else "sgpu_stroke_host"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS hbm_gbs)",
+                     "alg_bytes_per_launch": alg_bytes, "mean_launch_ms": step_ms,
+                     "traffic": traffic_for(W.cfg["workload"])},
+        "max_rel_err": err,
+        "team_phases_us_per_dab": {k: round(1e3 * v["ms"] / st.dabs.shape[0], 2)
+                                   for k, v in phases.items()},
+        "team_phases_alg_MB": {k: round(v["bytes"] / 1e6, 3) for k, v in phases.items()},
+        "autotune_ms": {str(k): round(v, 3) for k, v in tune_ms.items()},
+        "plain_graph": plain_graph,
+        "plain_eager": plain_eager,
+        "batch": batch,
+        "batched": batched,
+        "raycast": ray,
+        "draw_buffers": draw,
+        "cpu_baseline": ({k: v for k, v in cpu.items() if k != "seconds"} if cpu else None),
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def stroke_alg_bytes(g, st, tools=None) -> float:
+    """Algorithmic bytes of one persistent stroke of g (instrumented run; the
+    caller restores the mesh before and after)."""
+    phases, _, _ = g.stroke_team_profile(st, dab_tools=tools)
+    return sum(p["bytes"] for p in phases.values())
+
+
+def run_batch(synth, PBVH, batch_stroke, autotune_batch, BATCH_TEAM, BATCH_SEQUENTIAL, peak,
+              no_cpu=False, steps: int = 5):
+    """The 64-mesh uneven batch: one persistent launch on the batch autotuner's
+    team versus 64 sequential plain strokes (each a CUDA graph of per-call
+    kernels); algorithmic bytes from each mesh's instrumented stroke."""
     batch = synth.cfg4_batch()
     gs = [PBVH.build_mesh(mm, ll) for (mm, _, ll) in batch]
     strokes = [s for (_, s, _) in batch]
     for p in gs:
         p.snapshot()
     nverts = sum(mm.totvert for (mm, _, _) in batch)
-    best = None
-    for cl in (4, 8, 16):
+    shape, tune = autotune_batch(gs, strokes)  # restores every mesh
+    alg = 0.0
+    for p, s in zip(gs, strokes):
+        p.restore()
+        alg += stroke_alg_bytes(p, s)
+        p.restore()
+    ms_l, disp = [], 0
+    for _ in range(steps):
         for p in gs:
             p.restore()
-        batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=cl)
-        ms_l = []
-        for _ in range(3):
-            for p in gs:
-                p.restore()
-            gs[0].flush_l2()
-            stats, ms = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=cl)
-            ms_l.append(ms)
+        gs[0].flush_l2()
+        stats, ms = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=0)
+        ms_l.append(ms)
         disp = sum(s.verts_displaced for s in stats)
-        ms = statistics.median(ms_l)
-        if best is None or ms < best["ms_per_step"]:
-            best = {"cluster": cl, "ms_per_step": ms, "value": disp / (ms / 1e3)}
+    ms = statistics.median(ms_l)
     for p in gs:
         p.restore()
     batch_stroke(gs, strokes, mode=BATCH_SEQUENTIAL)  # graph captures
     for p in gs:
         p.restore()
-    t0 = time.perf_counter()
     stats, seq_ms = batch_stroke(gs, strokes, mode=BATCH_SEQUENTIAL)
-    wall = (time.perf_counter() - t0) * 1e3
-    disp = sum(s.verts_displaced for s in stats)
-    return {"workload": "64 meshes (grid/uv-sphere alternating, log-uniform 1e4-5e5 verts, "
-                        f"{nverts} verts total), 32-dab draw/inflate strokes",
-            "persistent": {"value": best["value"], "unit": UNIT, "ms_per_step": best["ms_per_step"],
-                           "cluster": best["cluster"]},
-            "sequential_plain": {"value": disp / (seq_ms / 1e3), "unit": UNIT,
-                                 "ms_per_step": seq_ms, "wall_ms": wall},
-            "speedup": best["value"] / (disp / (seq_ms / 1e3))}
+    seq_disp = sum(s.verts_displaced for s in stats)
+    achieved = alg / (ms / 1e3) / 1e9
+    out = {"workload": "64 meshes (grid/uv-sphere alternating, log-uniform 1e4-5e5 verts, "
+                       f"{nverts} verts total), 32-dab draw/inflate strokes",
+           "persistent": {"value": disp / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+                          "team": {"cluster": shape[0], "ctas_per_sm": shape[1]},
+                          "steps": steps},
+           "sequential_plain": {"value": seq_disp / (seq_ms / 1e3), "unit": UNIT,
+                                "ms_per_step": seq_ms},
+           "speedup": (disp / ms) / (seq_disp / seq_ms),
+           "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "alg_bytes": alg,
+                        "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak},
+           "autotune_ms": {f"{c[0]}x{c[1]}": round(t, 3) for c, t in tune.items()}}
+    for p in gs:
+        p.free()
+    if not no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        pyoracle.build()
+        threads = pyoracle.max_threads()
+        k, tot, dt = 8, 0, 0.0
+        for mm, s, ll in batch[:k]:
+            o = pyoracle.OracleMesh.faces(mm, ll)
+            o.recalc_all_normals()
+            t0 = time.perf_counter()
+            n, _ = o.stroke(s, which=1, nthreads=threads)
+            dt += time.perf_counter() - t0
+            tot += n
+            o.close()
+        out["cpu_baseline"] = {"value": tot / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"the first {k} of the 64 strokes, one after another "
+                                         "(FP32 restatement, OpenMP over PBVH nodes)"}
+    return out
+
+
+def run_batched(K: int, peak, no_cpu=False, steps: int = 3):
+    """The batched form of the clay-strips and multires workloads: K
+    independent seeded strokes on K meshes of that workload (same geometry,
+    separate handles), in one persistent launch on the batch autotuner's team;
+    against the K strokes run one after another on the single-stroke team."""
+    from dune_sculpt_gb300 import synth
+    from dune_sculpt_gb300.sculpt import (BATCH_TEAM, STROKE_TEAM, autotune_batch,
+                                          batch_stroke)
+
+    out = {}
+    for name in ("clay", "multires"):
+        W = workload(name)
+        strokes, tools = [], None
+        for k in range(K):
+            if name == "clay":
+                dabs = synth.arc_dabs(synth.SEED_BASE + 200 + k, W.stroke.dabs.shape[0],
+                                      0.1 * 2 * W.stroke.radius)
+            else:
+                dabs = synth.torus_dabs(synth.SEED_BASE + 200 + k, W.stroke.dabs.shape[0],
+                                        W.stroke.radius)
+            s = synth.Stroke(W.stroke.tool, W.stroke.radius, W.stroke.strength,
+                             W.stroke.curve_preset, W.stroke.symmetry, dabs)
+            strokes.append(s)
+        if W.tools is not None:
+            tools = np.concatenate([W.tools] * K)
+        gs = [build_gpu(W) for _ in range(K)]
+        for p in gs:
+            p.snapshot()
+        shape, tune = autotune_batch(gs, strokes, dab_tools=tools)
+        alg, single_ms, single_v = 0.0, 0.0, 0
+        best_single, _ = gs[0].autotune_team(strokes[0], dab_tools=W.tools)
+        for p, s in zip(gs, strokes):
+            p.set_team(best_single)
+            p.restore()
+            alg += stroke_alg_bytes(p, s, W.tools)
+            p.restore()
+            p.flush_l2()
+            r = p.stroke(s, mode=STROKE_TEAM, dab_tools=W.tools)
+            single_ms += r.gpu_ms
+            single_v += r.verts_displaced
+            p.restore()
+        ms_l, disp = [], 0
+        for _ in range(steps):
+            for p in gs:
+                p.restore()
+            gs[0].flush_l2()
+            stats, ms = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=0, dab_tools=tools)
+            ms_l.append(ms)
+            disp = sum(s.verts_displaced for s in stats)
+        ms = statistics.median(ms_l)
+        achieved = alg / (ms / 1e3) / 1e9
+        out[name] = {"workload": f"{K} independent seeded strokes of the {W.cfg['workload']} "
+                                 "workload on K meshes, one persistent launch",
+                     "strokes": K, "value": disp / (ms / 1e3), "unit": UNIT,
+                     "ms_per_batch": ms,
+                     "team": {"cluster": shape[0], "ctas_per_sm": shape[1]},
+                     "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "alg_bytes": alg,
+                                  "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved / peak},
+                     "one_after_another": {"value": single_v / (single_ms / 1e3), "unit": UNIT,
+                                           "ms": single_ms, "team": best_single},
+                     "speedup_vs_one_after_another": (disp / ms) / (single_v / single_ms),
+                     "autotune_ms": {f"{c[0]}x{c[1]}": round(t, 3) for c, t in tune.items()}}
+        for p in gs:
+            p.free()
+    return out
+
+
+def run_quick(args):
+    from dune_sculpt_gb300 import build as libbuild
+
+    libbuild.build()
+    from dune_sculpt_gb300.sculpt import STROKE_TEAM
+
+    W = workload(args.workload)
+    g = build_gpu(W)
+    g.snapshot()
+    if args.team:
+        g.set_team(args.team)
+    else:
+        g.autotune_team(W.stroke, dab_tools=W.tools)
+    for _ in range(3):
+        g.restore()
+        s = g.stroke(W.stroke, mode=STROKE_TEAM, dab_tools=W.tools)
+    print(f"quick: {s.verts_displaced} vertices displaced, {s.gpu_ms:.3f} ms, team {g.team()}")
+    return 0
+
+
+def run_phases(args):
+    """Per-dab phase times of the persistent stroke kernel on the single-mesh
+    workloads: the autotuned team, the best of three L2-flushed strokes, then
+    one instrumented stroke (phase timers of the team's first thread)."""
+    from dune_sculpt_gb300 import build as libbuild
+
+    libbuild.build()
+    from dune_sculpt_gb300 import synth
+    from dune_sculpt_gb300.sculpt import STROKE_GRAPH, STROKE_TEAM
+
+    def one(name, g, st, tools=None, graph=False):
+        g.snapshot()
+        best, tune = g.autotune_team(st, dab_tools=tools)
+        times = []
+        for _ in range(3):
+            g.restore()
+            g.flush_l2()
+            times.append(g.stroke(st, mode=STROKE_TEAM, dab_tools=tools).gpu_ms)
+        extra = {}
+        if graph:  # the same stroke replayed from a CUDA graph of the per-call kernels
+            gt = []
+            for _ in range(3):
+                g.restore()
+                g.flush_l2()
+                gt.append(g.stroke(st, mode=STROKE_GRAPH, dab_tools=tools).gpu_ms)
+            extra["graph_ms_per_stroke"] = round(min(gt), 3)
+        g.restore()
+        g.flush_l2()
+        ph, _, stats = g.stroke_team_profile(st, dab_tools=tools)
+        nd = st.dabs.shape[0]
+        print(json.dumps({
+            "workload": name, "team": best, "ms_per_stroke": round(min(times), 3),
+            "us_per_dab": round(1000 * min(times) / nd, 2),
+            "verts_displaced": stats.verts_displaced, **extra,
+            "autotune_ms": {str(k): round(v, 3) for k, v in tune.items()},
+            "phase_us_per_dab": {k: round(1000 * v["ms"] / nd, 2) for k, v in ph.items()},
+            "phase_alg_MB_per_stroke": {k: round(v["bytes"] / 1e6, 2) for k, v in ph.items()}}),
+            flush=True)
+        g.free()
+
+    for name in ("grid", "icosphere", "clay", "multires"):
+        W = workload(name)
+        one(W.cfg["workload"], build_gpu(W), W.stroke, W.tools)
+    # the stroke-start brushes on the icosphere (128 dabs, X mirror):
+    # persistent and graph-replayed
+    W = workload("icosphere")
+    st = W.stroke
+    grab = synth.grab_dabs(synth.SEED_BASE + 40, st.dabs.shape[0], 0.0005)
+    for name, tool, dabs, kw in (
+            ("grab", synth.TOOL_GRAB, grab, {}),
+            ("layer", synth.TOOL_LAYER, st.dabs, {"height": 0.3}),
+            ("elastic_deform", synth.TOOL_ELASTIC_DEFORM, grab, {})):
+        so = synth.Stroke(tool, st.radius, st.strength, synth.CURVE_SMOOTH, synth.SYMM_X, dabs, **kw)
+        one(f"icosphere8_{name}_xmirror", build_gpu(W), so, graph=True)
+    return 0
 
 
 def main():
@@ -687,6 +935,12 @@ def main():
         return run_quick(args)
     if args.phases:
         return run_phases(args)
+    if args.batched_only:
+        from dune_sculpt_gb300 import build as libbuild
+
+        libbuild.build()
+        print(json.dumps(run_batched(args.batched_k, measured_peaks()[0], no_cpu=True)))
+        return 0
     if args.draw_only:
         from dune_sculpt_gb300 import build as libbuild
 
@@ -697,10 +951,10 @@ def main():
         peak = measured_peaks()[0]
         out = {}
         if args.draw_mesh in ("faces", "both"):
-            m, st, leaf_limit, _ = workload()
-            g = PBVH.build_mesh(m, leaf_limit)
+            W = workload("icosphere")
+            g = build_gpu(W)
             g.snapshot()
-            out["draw_faces"] = run_draw_leg(g, m, st, leaf_limit, True, peak)
+            out["draw_faces"] = run_draw_leg(g, W.mesh, W.stroke, W.leaf_limit, True, peak)
             g.free()
         if args.draw_mesh in ("grids", "both"):
             out["draw_grids"] = run_draw_grids(synth, PBVH, peak)
@@ -715,10 +969,10 @@ def main():
 
         out = {}
         if args.raycast_mesh in ("faces", "both"):
-            m, _, leaf_limit, _ = workload()
-            g = PBVH.build_mesh(m, leaf_limit)
+            W = workload("icosphere")
+            g = build_gpu(W)
             for _ in range(3):
-                out["raycast_faces"] = run_raycast_leg(g, m, leaf_limit, True)
+                out["raycast_faces"] = run_raycast_leg(g, W.mesh, W.leaf_limit, True)
             g.free()
         if args.raycast_mesh in ("grids", "both"):
             out["raycast_grids"] = run_raycast_grids(synth, PBVH)

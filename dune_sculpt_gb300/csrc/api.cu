@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -21,6 +22,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 using namespace sgpu;
 
@@ -111,6 +115,8 @@ struct sgpu_mesh {
   void* flush_buf = nullptr;
   // persistent stroke kernel: cluster size and device staging of the job
   int team_cluster = 8;
+  int team_build = 0;     // CTAs per SM of the cluster build: 0 auto, 1, 2
+  bool team_set = false;  // set by sgpu_mesh_set_team or the autotuner
   int nchunks = 0;  // refit chunks over all leaves
   DevMesh* t_meshes = nullptr;
   TeamJob* t_jobs = nullptr;
@@ -629,9 +635,55 @@ int run_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, i
 int finish_stroke(sgpu_mesh* mesh, int mode, int launches, SGPU_StrokeStats* stats);
 // wait = false: enqueue only (launch, then the displaced counters into the
 // first mesh's h_disp); the caller synchronizes and reads them.
+// Team of the persistent stroke kernel: cluster size (1..16) or
+// SGPU_TEAM_GRID, and the CTAs per SM of the cluster build (0 auto, 1, 2).
+struct TeamShape {
+  int cluster;
+  int ctas_per_sm;
+};
 int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_Dab* dabs,
-               const int* offs, const int* tools, int cluster, cudaStream_t s,
+               const int* offs, const int* tools, TeamShape shape, cudaStream_t s,
                SGPU_StrokeStats* stats, float* total_ms, bool wait = true);
+
+// Autotuner results, process-wide: a single-mesh stroke is keyed by (mesh
+// type, log2 of its vertex count, the set of tools of the stroke, symmetry
+// passes); a batch by (its mesh count, log2 of its total vertex count, the
+// set of tools).  A mesh whose team was not set explicitly strokes with the
+// cached shape of its key; sgpu_batch_stroke with cluster_size 0 with the
+// cached shape of its batch key.
+struct TuneKey {
+  int batch, type, size_class, passes, nmesh;
+  unsigned tools;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(batch, type, size_class, passes, nmesh, tools) <
+           std::tie(o.batch, o.type, o.size_class, o.passes, o.nmesh, o.tools);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TeamShape> g_tune;
+
+int size_class(long long n) {
+  int c = 0;
+  while (n > 1) {
+    n >>= 1;
+    c++;
+  }
+  return c;
+}
+
+unsigned tools_mask(const SGPU_Brush* b, const int* tools, int ndabs) {
+  unsigned m = 0;
+  for (int d = 0; d < ndabs; d++) m |= 1u << ((tools ? tools[d] : b->sculpt_tool) & 31);
+  if (ndabs == 0) m = 1u << (b->sculpt_tool & 31);
+  return m;
+}
+
+TuneKey stroke_key(const sgpu_mesh* m, const SGPU_Brush* b, const int* tools, int ndabs);
+TuneKey batch_key(sgpu_mesh* const* meshes, int n, const SGPU_Brush* brushes, const int* offs,
+                  const int* tools);
+// The team a single-mesh stroke runs on: the mesh's explicit setting, else
+// the autotuner's cached shape for the stroke's key, else 8 CTAs.
+TeamShape mesh_team(const sgpu_mesh* m, const SGPU_Brush* b, const int* tools, int ndabs);
 // Profiling counters handed to the next persistent launch (nullptr otherwise).
 thread_local unsigned long long* g_team_prof_bytes = nullptr;
 thread_local unsigned long long* g_team_phase_ns = nullptr;
@@ -695,6 +747,70 @@ int do_brush_tool(sgpu_mesh* m, const SGPU_Brush* brush, int tool, const float l
   rc = launch_tool(L, b, pp);
   if (rc) return rc;
   return device_err(m);
+}
+
+// The host-buffer stroke around the upload and download of one mesh type:
+// upload, refit of every leaf box, the stroke (mode as in sgpu_stroke),
+// download, all between two events on the mesh stream.
+template <class Up, class Down>
+int stroke_host_run(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, int ndabs,
+                    const int* dab_tools, int mode, Up upload, Down download, int& launches,
+                    SGPU_StrokeStats* stats) {
+  int rc;
+  if (mode != SGPU_STROKE_EAGER && mode != SGPU_STROKE_GRAPH && mode != SGPU_STROKE_TEAM)
+    return fail(SGPU_ERR_INVALID_ARG, "unknown stroke mode %d", mode);
+  const TeamShape team = mesh_team(mesh, brush, dab_tools, ndabs);
+  if (mode == SGPU_STROKE_TEAM && team.cluster != SGPU_TEAM_GRID &&
+      stroke_has_whole_mesh(brush, dab_tools, ndabs))
+    mode = SGPU_STROKE_GRAPH;
+  if (!mesh->ev_h0) {
+    CK(cudaEventCreate(&mesh->ev_h0), "cudaEventCreate");
+    CK(cudaEventCreate(&mesh->ev_h1), "cudaEventCreate");
+  }
+  DevMesh& d = mesh->dev;
+  CK(cudaEventRecord(mesh->ev_h0, mesh->stream), "event");
+  if ((rc = upload())) return rc;
+  // New positions: every leaf box is refit and flushed before the stroke.
+  CK(launch_mark_all(d, kUpdateBB | kUpdateOriginalBB, mesh->stream), "mark kernel");
+  CK(launch_update_faces(d, 0, kUpdateBB | kUpdateOriginalBB, mesh->stream), "bounds kernel");
+  launches += 2;
+  SGPU_StrokeStats inner;
+  std::memset(&inner, 0, sizeof(inner));
+  if (mode == SGPU_STROKE_TEAM) {
+    const int offs[2] = {0, ndabs};
+    sgpu_mesh* one[1] = {mesh};
+    float total = 0.0f;
+    if ((rc = team_batch(one, 1, brush, dabs, offs, dab_tools, team, mesh->stream, &inner,
+                         &total, false)))
+      return rc;
+    launches += 1;
+  } else {
+    if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, mode, &launches))) return rc;
+  }
+  if ((rc = download())) return rc;
+  CK(cudaEventRecord(mesh->ev_h1, mesh->stream), "event");
+  unsigned long long displaced = 0;
+  if (mode != SGPU_STROKE_TEAM)
+    CK(cudaMemcpyAsync(&displaced, &d.work->displaced, sizeof(displaced), cudaMemcpyDeviceToHost,
+                       mesh->stream),
+       "read counter");
+  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
+  if (mode == SGPU_STROKE_TEAM) {
+    displaced = mesh->h_disp[0];
+    if (const int status = static_cast<int>(mesh->h_disp[1]))
+      return fail(status, "persistent stroke kernel: a team barrier wait ran out (error %d); the "
+                  "stroke is incomplete", status);
+  }
+  if ((rc = device_err(mesh))) return rc;
+  if (stats) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, mesh->ev_h0, mesh->ev_h1), "elapsed");
+    stats->verts_displaced = static_cast<int64_t>(displaced);
+    stats->gpu_ms = ms;
+    stats->kernel_launches = launches;
+    stats->graph_nodes = mode == SGPU_STROKE_GRAPH ? mesh->g_nodes : 0;
+  }
+  return SGPU_OK;
 }
 
 }  // namespace
@@ -1133,6 +1249,36 @@ int sgpu_do_brush(sgpu_mesh* mesh, const SGPU_Brush* brush, const float location
   return do_brush_tool(mesh, brush, brush->sculpt_tool, location, grab_delta, nodes, totnode);
 }
 
+int sgpu_calc_area_normal_and_center(sgpu_mesh* mesh, const SGPU_Brush* brush,
+                                     const float location[3], const int* nodes, int totnode,
+                                     float r_area_no[3], float r_area_co[3]) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  if (!brush || !location || !r_area_no || !r_area_co)
+    return fail(SGPU_ERR_INVALID_ARG, "NULL argument");
+  if (!(brush->radius > 0.0f)) return fail(SGPU_ERR_INVALID_ARG, "radius must be positive");
+  if (nodes && (rc = upload_node_list(mesh, nodes, totnode))) return rc;
+  DevBrush b;
+  if (!make_brush(brush, kToolDraw, &b))
+    return fail(SGPU_ERR_INVALID_ARG, "unknown curve preset %d", brush->curve_preset);
+  PassParams pp{};
+  for (int k = 0; k < 3; k++) pp.loc[k] = location[k];
+  pp.iter_strength = 1.0f;
+  CK(launch_area(mesh->dev, b, pp, mesh->stream), "area kernel");
+  float out[6];
+  static_assert(offsetof(Work, area_co) == offsetof(Work, area_no) + 3 * sizeof(float),
+                "area normal and centre are adjacent");
+  CK(cudaMemcpyAsync(out, mesh->dev.work->area_no, sizeof(out), cudaMemcpyDeviceToHost,
+                     mesh->stream),
+     "read area");
+  if ((rc = device_err(mesh))) return rc;
+  for (int k = 0; k < 3; k++) {
+    r_area_no[k] = out[k];
+    r_area_co[k] = out[3 + k];
+  }
+  return SGPU_OK;
+}
+
 int sgpu_pbvh_update_normals(sgpu_mesh* mesh) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
@@ -1170,15 +1316,15 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   }
   if (brush->symmetry < 0 || brush->symmetry > 7)
     return fail(SGPU_ERR_INVALID_ARG, "symmetry flags out of range");
-  if (mode == SGPU_STROKE_TEAM && mesh->team_cluster != SGPU_TEAM_GRID &&
+  const TeamShape team = mesh_team(mesh, brush, dab_tools, ndabs);
+  if (mode == SGPU_STROKE_TEAM && team.cluster != SGPU_TEAM_GRID &&
       stroke_has_whole_mesh(brush, dab_tools, ndabs))
     mode = SGPU_STROKE_GRAPH;
   if (mode == SGPU_STROKE_TEAM) {
     const int offs[2] = {0, ndabs};
     sgpu_mesh* one[1] = {mesh};
     float total_ms = 0.0f;
-    rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh->team_cluster, mesh->stream,
-                    stats, &total_ms);
+    rc = team_batch(one, 1, brush, dabs, offs, dab_tools, team, mesh->stream, stats, &total_ms);
     return rc;
   }
   CK(cudaEventRecord(mesh->ev0, mesh->stream), "event");
@@ -1204,8 +1350,8 @@ int sgpu_stroke_team_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGP
   sgpu_mesh* one[1] = {mesh};
   float total = 0.0f;
   SGPU_StrokeStats st;
-  rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh->team_cluster, mesh->stream, &st,
-                  &total);
+  rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh_team(mesh, brush, dab_tools, ndabs),
+                  mesh->stream, &st, &total);
   g_team_prof_bytes = nullptr;
   g_team_phase_ns = nullptr;
   unsigned long long host[2 * kTeamPhases] = {};
@@ -1229,6 +1375,8 @@ int sgpu_mesh_set_team(sgpu_mesh* mesh, int cluster_size) {
       cluster_size != 16 && cluster_size != SGPU_TEAM_GRID)
     return fail(SGPU_ERR_INVALID_ARG, "cluster size must be 1, 2, 4, 8, 16 or SGPU_TEAM_GRID");
   mesh->team_cluster = cluster_size;
+  mesh->team_build = 0;
+  mesh->team_set = true;
   return SGPU_OK;
 }
 
@@ -1263,12 +1411,18 @@ int sgpu_autotune_team(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab*
   int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
   if (rc) return rc;
   if ((rc = sgpu_mesh_snapshot(mesh))) return rc;
-  const int sizes[5] = {1, 2, 4, 8, 16};
-  int best = mesh->team_cluster;
+  const int sizes[SGPU_AUTOTUNE_CANDIDATES] = {SGPU_TEAM_GRID, 1, 2, 4, 8, 16};
+  const bool whole = stroke_has_whole_mesh(brush, dab_tools, ndabs);
+  TeamShape best{mesh->team_cluster, 0};
   float best_ms = -1.0f;
-  for (int k = 0; k < 5; k++) {
+  for (int k = 0; k < SGPU_AUTOTUNE_CANDIDATES; k++) {
     float ms = -1.0f;
-    if (team_max_active_clusters(sizes[k], mesh->dev.totnode, mesh->dev.nleaf) > 0) {
+    const TeamShape shape{sizes[k], 1};
+    const bool ok = shape.cluster == SGPU_TEAM_GRID
+                        ? team_wide_ctas(mesh->dev.totnode, mesh->dev.nleaf) > 0
+                        : !whole && team_max_active_clusters(shape.cluster, mesh->dev.totnode,
+                                                             mesh->dev.nleaf) > 0;
+    if (ok) {
       const int offs[2] = {0, ndabs};
       sgpu_mesh* one[1] = {mesh};
       // two trials, keep the second (the first pays one-time setup)
@@ -1276,21 +1430,93 @@ int sgpu_autotune_team(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab*
         if ((rc = sgpu_mesh_restore(mesh))) return rc;
         SGPU_StrokeStats st;
         float total = 0.0f;
-        if ((rc = team_batch(one, 1, brush, dabs, offs, dab_tools, sizes[k], mesh->stream, &st,
+        if ((rc = team_batch(one, 1, brush, dabs, offs, dab_tools, shape, mesh->stream, &st,
                              &total)))
           return rc;
         ms = total;
       }
       if (best_ms < 0.0f || ms < best_ms) {
         best_ms = ms;
-        best = sizes[k];
+        best = shape;
       }
     }
     if (r_ms) r_ms[k] = ms;
   }
   if ((rc = sgpu_mesh_restore(mesh))) return rc;
-  mesh->team_cluster = best;
-  if (r_cluster) *r_cluster = best;
+  mesh->team_cluster = best.cluster;
+  mesh->team_build = best.ctas_per_sm;
+  mesh->team_set = true;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[stroke_key(mesh, brush, dab_tools, ndabs)] = best;
+  }
+  if (r_cluster) *r_cluster = best.cluster;
+  return SGPU_OK;
+}
+
+int sgpu_autotune_batch(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes,
+                        const SGPU_Dab* dabs, const int* dab_offsets, const int* dab_tools,
+                        int* r_cluster, int* r_ctas_per_sm, float* r_ms) {
+  if (!meshes || nmesh <= 0 || !brushes || !dab_offsets)
+    return fail(SGPU_ERR_INVALID_ARG, "NULL or empty batch");
+  for (int i = 0; i < nmesh; i++) {
+    const int nd = dab_offsets[i + 1] - dab_offsets[i];
+    int rc = validate_stroke(meshes[i], &brushes[i], dabs + dab_offsets[i], nd,
+                             dab_tools ? dab_tools + dab_offsets[i] : nullptr);
+    if (rc) return rc;
+  }
+  int rc;
+  for (int i = 0; i < nmesh; i++)
+    if ((rc = sgpu_mesh_snapshot(meshes[i]))) return rc;
+  int max_nodes = 0, max_leaves = 0;
+  for (int i = 0; i < nmesh; i++) {
+    max_nodes = std::max(max_nodes, meshes[i]->dev.totnode);
+    max_leaves = std::max(max_leaves, meshes[i]->dev.nleaf);
+  }
+  const TeamShape cand[SGPU_AUTOTUNE_BATCH_CANDIDATES] = {
+      {16, 1}, {8, 1}, {8, 2}, {4, 1}, {4, 2}, {2, 2}, {SGPU_TEAM_GRID, 1}};
+  TeamShape best{8, 0};
+  float best_ms = -1.0f;
+  auto restore_all = [&]() -> int {
+    for (int i = 0; i < nmesh; i++) {
+      const int r = sgpu_mesh_restore(meshes[i]);
+      if (r) return r;
+    }
+    return SGPU_OK;
+  };
+  for (int k = 0; k < SGPU_AUTOTUNE_BATCH_CANDIDATES; k++) {
+    const TeamShape& c = cand[k];
+    float ms = -1.0f;
+    const bool ok = c.cluster == SGPU_TEAM_GRID
+                        ? team_wide_ctas(max_nodes, max_leaves) > 0
+                        : team_max_active_clusters(c.cluster, max_nodes, max_leaves) > 0;
+    if (ok) {
+      for (int trial = 0; trial < 2; trial++) {
+        if ((rc = restore_all())) return rc;
+        float total = 0.0f;
+        rc = team_batch(meshes, nmesh, brushes, dabs, dab_offsets, dab_tools, c,
+                        meshes[0]->stream, nullptr, &total);
+        if (rc == SGPU_ERR_CUDA && c.cluster != SGPU_TEAM_GRID) {
+          ms = -1.0f;  // this build holds no team of this size on the device
+          break;
+        }
+        if (rc) return rc;
+        ms = total;
+      }
+      if (ms > 0.0f && (best_ms < 0.0f || ms < best_ms)) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+    if (r_ms) r_ms[k] = ms;
+  }
+  if ((rc = restore_all())) return rc;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[batch_key(meshes, nmesh, brushes, dab_offsets, dab_tools)] = best;
+  }
+  if (r_cluster) *r_cluster = best.cluster;
+  if (r_ctas_per_sm) *r_ctas_per_sm = best.ctas_per_sm;
   return SGPU_OK;
 }
 
@@ -1307,9 +1533,15 @@ int sgpu_batch_stroke(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes,
   }
   for (int i = 0; i < nmesh; i++) CK(cudaStreamSynchronize(meshes[i]->stream), "sync");
   if (mode == SGPU_BATCH_TEAM) {
-    const int cl = cluster_size > 0 ? cluster_size : meshes[0]->team_cluster;
+    TeamShape shape{cluster_size, 0};
+    if (cluster_size == 0) {
+      shape = TeamShape{meshes[0]->team_cluster, meshes[0]->team_build};
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      const auto it = g_tune.find(batch_key(meshes, nmesh, brushes, dab_offsets, dab_tools));
+      if (it != g_tune.end()) shape = it->second;
+    }
     float total = 0.0f;
-    int rc = team_batch(meshes, nmesh, brushes, dabs, dab_offsets, dab_tools, cl,
+    int rc = team_batch(meshes, nmesh, brushes, dabs, dab_offsets, dab_tools, shape,
                         meshes[0]->stream, stats, &total);
     if (r_total_ms) *r_total_ms = total;
     return rc;
@@ -1366,74 +1598,73 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
   if (rc) return rc;
   if (mesh->dev.type != kFaces) return fail(SGPU_ERR_INVALID_ARG, "not a FACES mesh");
   if (!verts_in || !verts_out) return fail(SGPU_ERR_INVALID_ARG, "NULL host buffers");
-  if (mode != SGPU_STROKE_EAGER && mode != SGPU_STROKE_GRAPH && mode != SGPU_STROKE_TEAM)
-    return fail(SGPU_ERR_INVALID_ARG, "unknown stroke mode %d", mode);
-  if (mode == SGPU_STROKE_TEAM && mesh->team_cluster != SGPU_TEAM_GRID &&
-      stroke_has_whole_mesh(brush, dab_tools, ndabs))
-    mode = SGPU_STROKE_GRAPH;
-  if (!mesh->ev_h0) {
-    CK(cudaEventCreate(&mesh->ev_h0), "cudaEventCreate");
-    CK(cudaEventCreate(&mesh->ev_h1), "cudaEventCreate");
-  }
   DevMesh& d = mesh->dev;
-  CK(cudaEventRecord(mesh->ev_h0, mesh->stream), "event");
-  // host buffers in the caller's vertex order, converted on the device
-  CK(cudaMemcpyAsync(d.scratch, verts_in, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
-                     mesh->stream),
-     "upload verts");
-  CK(launch_gather_f4(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
-  if (vert_normals_in) {
-    float* flat = reinterpret_cast<float*>(d.scratch2);
-    CK(cudaMemcpyAsync(flat, vert_normals_in, 3 * sizeof(float) * d.totvert, cudaMemcpyHostToDevice,
+  int launches = 0;
+  auto upload = [&]() -> int {
+    // host buffers in the caller's vertex order, converted on the device
+    CK(cudaMemcpyAsync(d.scratch, verts_in, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
                        mesh->stream),
-       "upload normals");
-    CK(launch_xyz_to_f4(d.no, flat, mesh->d_n2o, d.totvert, true, mesh->stream), "gather kernel");
-  }
-  // New positions: every leaf box is refit and flushed before the stroke.
-  CK(launch_mark_all(d, kUpdateBB | kUpdateOriginalBB, mesh->stream), "mark kernel");
-  CK(launch_update_faces(d, 0, kUpdateBB | kUpdateOriginalBB, mesh->stream), "bounds kernel");
-  int launches = 3 + (vert_normals_in ? 1 : 0);  // gathers, mark, bounds
-  SGPU_StrokeStats inner;
-  std::memset(&inner, 0, sizeof(inner));
-  if (mode == SGPU_STROKE_TEAM) {
-    const int offs[2] = {0, ndabs};
-    sgpu_mesh* one[1] = {mesh};
-    float total = 0.0f;
-    if ((rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh->team_cluster, mesh->stream,
-                         &inner, &total, false)))
-      return rc;
-    launches += 1;
-  } else {
-    if ((rc = run_stroke(mesh, brush, dabs, ndabs, dab_tools, mode, &launches))) return rc;
-  }
-  CK(launch_gather_f4(d.scratch, d.co, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
-  launches += 1;
-  CK(cudaMemcpyAsync(verts_out, d.scratch, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
-                     mesh->stream),
-     "download verts");
-  CK(cudaEventRecord(mesh->ev_h1, mesh->stream), "event");
-  unsigned long long displaced = 0;
-  if (mode != SGPU_STROKE_TEAM)
-    CK(cudaMemcpyAsync(&displaced, &d.work->displaced, sizeof(displaced), cudaMemcpyDeviceToHost,
+       "upload verts");
+    CK(launch_gather_f4(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
+    launches++;
+    if (vert_normals_in) {
+      float* flat = reinterpret_cast<float*>(d.scratch2);
+      CK(cudaMemcpyAsync(flat, vert_normals_in, 3 * sizeof(float) * d.totvert,
+                         cudaMemcpyHostToDevice, mesh->stream),
+         "upload normals");
+      CK(launch_xyz_to_f4(d.no, flat, mesh->d_n2o, d.totvert, true, mesh->stream), "gather kernel");
+      launches++;
+    }
+    return SGPU_OK;
+  };
+  auto download = [&]() -> int {
+    CK(launch_gather_f4(d.scratch, d.co, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
+    launches++;
+    CK(cudaMemcpyAsync(verts_out, d.scratch, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
                        mesh->stream),
-       "read counter");
-  CK(cudaStreamSynchronize(mesh->stream), "cudaStreamSynchronize");
-  if (mode == SGPU_STROKE_TEAM) {
-    displaced = mesh->h_disp[0];
-    if (const int status = static_cast<int>(mesh->h_disp[1]))
-      return fail(status, "persistent stroke kernel: a team barrier wait ran out (error %d); the "
-                  "stroke is incomplete", status);
-  }
-  if ((rc = device_err(mesh))) return rc;
-  if (stats) {
-    float ms = 0.0f;
-    CK(cudaEventElapsedTime(&ms, mesh->ev_h0, mesh->ev_h1), "elapsed");
-    stats->verts_displaced = static_cast<int64_t>(displaced);
-    stats->gpu_ms = ms;
-    stats->kernel_launches = launches;
-    stats->graph_nodes = mode == SGPU_STROKE_GRAPH ? mesh->g_nodes : 0;
-  }
-  return SGPU_OK;
+       "download verts");
+    return SGPU_OK;
+  };
+  return stroke_host_run(mesh, brush, dabs, ndabs, dab_tools, mode, upload, download, launches,
+                         stats);
+}
+
+int sgpu_stroke_host_grids(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
+                           int ndabs, const int* dab_tools, const float* grids_co_in,
+                           const float* grids_no_in, float* grids_co_out, int mode,
+                           SGPU_StrokeStats* stats) {
+  int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
+  if (rc) return rc;
+  if (mesh->dev.type != kGrids) return fail(SGPU_ERR_INVALID_ARG, "not a GRIDS mesh");
+  if (!grids_co_in || !grids_co_out) return fail(SGPU_ERR_INVALID_ARG, "NULL host buffers");
+  DevMesh& d = mesh->dev;
+  int launches = 0;
+  float* flat = reinterpret_cast<float*>(d.scratch);
+  auto upload = [&]() -> int {
+    CK(cudaMemcpyAsync(flat, grids_co_in, 3 * sizeof(float) * d.totvert, cudaMemcpyHostToDevice,
+                       mesh->stream),
+       "upload grid positions");
+    CK(launch_xyz_to_f4(d.co, flat, nullptr, d.totvert, false, mesh->stream), "expand kernel");
+    launches++;
+    if (grids_no_in) {
+      CK(cudaMemcpyAsync(flat, grids_no_in, 3 * sizeof(float) * d.totvert,
+                         cudaMemcpyHostToDevice, mesh->stream),
+         "upload grid normals");
+      CK(launch_xyz_to_f4(d.no, flat, nullptr, d.totvert, false, mesh->stream), "expand kernel");
+      launches++;
+    }
+    return SGPU_OK;
+  };
+  auto download = [&]() -> int {
+    CK(launch_f4_to_xyz(flat, d.co, nullptr, d.totvert, mesh->stream), "pack kernel");
+    launches++;
+    CK(cudaMemcpyAsync(grids_co_out, flat, 3 * sizeof(float) * d.totvert, cudaMemcpyDeviceToHost,
+                       mesh->stream),
+       "download grid positions");
+    return SGPU_OK;
+  };
+  return stroke_host_run(mesh, brush, dabs, ndabs, dab_tools, mode, upload, download, launches,
+                         stats);
 }
 
 int sgpu_stroke_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
@@ -1833,9 +2064,33 @@ int ensure_dev(T** p, size_t* cap, size_t n) {
 
 // One persistent launch over the meshes: jobs (whole strokes) are ordered by
 // estimated work, longest first, and taken by cluster teams from a counter.
+TuneKey stroke_key(const sgpu_mesh* m, const SGPU_Brush* b, const int* tools, int ndabs) {
+  return TuneKey{0, m->dev.type, size_class(m->dev.totvert),
+                 1 << __builtin_popcount(b->symmetry & 7), 1, tools_mask(b, tools, ndabs)};
+}
+
+TuneKey batch_key(sgpu_mesh* const* meshes, int n, const SGPU_Brush* brushes, const int* offs,
+                  const int* tools) {
+  long long verts = 0;
+  unsigned mask = 0;
+  for (int i = 0; i < n; i++) {
+    verts += meshes[i]->dev.totvert;
+    mask |= tools_mask(&brushes[i], tools ? tools + offs[i] : nullptr, offs[i + 1] - offs[i]);
+  }
+  return TuneKey{1, meshes[0]->dev.type, size_class(verts), 0, n, mask};
+}
+
+TeamShape mesh_team(const sgpu_mesh* m, const SGPU_Brush* b, const int* tools, int ndabs) {
+  if (m->team_set) return TeamShape{m->team_cluster, m->team_build};
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const auto it = g_tune.find(stroke_key(m, b, tools, ndabs));
+  return it != g_tune.end() ? it->second : TeamShape{m->team_cluster, m->team_build};
+}
+
 int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_Dab* dabs,
-               const int* offs, const int* tools, int cluster, cudaStream_t s,
+               const int* offs, const int* tools, TeamShape shape, cudaStream_t s,
                SGPU_StrokeStats* stats, float* total_ms, bool wait) {
+  const int cluster = shape.cluster;
   sgpu_mesh* m0 = meshes[0];
   // strokes with grab, elastic deform or layer dabs keep the stroke-start
   // positions (stored on the launch stream below)
@@ -1866,6 +2121,8 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
     for (int i = 0; i < n; i++) barriers += 64.0 * (offs[i + 1] - offs[i]) + 8.0;
     if (barriers * (wide_ctas + 1) >= 2147483648.0)
       return fail(SGPU_ERR_UNSUPPORTED, "too many dabs for one whole-GPU launch");
+  } else if (cluster < 1 || cluster > 16 || (cluster & (cluster - 1)) != 0) {
+    return fail(SGPU_ERR_INVALID_ARG, "cluster size %d is not 1, 2, 4, 8 or 16", cluster);
   } else if (team_max_active_clusters(cluster, max_nodes, max_leaves) <= 0) {
     return fail(SGPU_ERR_UNSUPPORTED, "cluster size %d cannot be launched", cluster);
   }
@@ -1945,7 +2202,7 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   if (wide) {
     CK(launch_team_stroke_wide(a, wide_ctas, s), "persistent stroke kernel (whole GPU)");
   } else {
-    CK(launch_team_stroke(a, cluster, s), "persistent stroke kernel");
+    CK(launch_team_stroke(a, cluster, s, shape.ctas_per_sm), "persistent stroke kernel");
   }
   CK(cudaEventRecord(m0->ev1, s), "event");
   // page-locked: n displaced counters, then the status word

@@ -90,16 +90,19 @@ int team_max_active_clusters(int cluster, int max_nodes, int max_leaves) {
   return std::max(active_clusters<1>(cluster, smem), active_clusters<2>(cluster, smem));
 }
 
-cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s) {
+cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s, int ctas_per_sm) {
   const size_t smem = team_smem_bytes(a.max_nodes, a.max_leaves);
-  // the one-CTA-per-SM build when it holds a team for every job
-  const int n1 = active_clusters<1>(cluster, smem);
-  const int n2 = n1 >= a.njobs ? 0 : active_clusters<2>(cluster, smem);
-  const bool wide = n2 > n1;
-  const int nteams = std::max(1, std::min(a.njobs, wide ? n2 : n1));
+  // auto: the one-CTA-per-SM build when it holds a team for every job
+  const int n1 = ctas_per_sm == 2 ? 0 : active_clusters<1>(cluster, smem);
+  const int n2 = ctas_per_sm == 1 || (ctas_per_sm == 0 && n1 >= a.njobs)
+                     ? 0
+                     : active_clusters<2>(cluster, smem);
+  const bool two = n2 > n1;
+  if ((two ? n2 : n1) <= 0) return cudaErrorInvalidConfiguration;
+  const int nteams = std::max(1, std::min(a.njobs, two ? n2 : n1));
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = team_config(cluster, nteams, smem, s, attr);
-  if (wide)
+  if (two)
     return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<2, true, false>, a)
                   : cudaLaunchKernelEx(&cfg, k_team_stroke<2, false, false>, a);
   return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true, false>, a)

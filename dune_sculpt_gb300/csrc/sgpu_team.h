@@ -54,8 +54,10 @@ enum TeamPhase {
 size_t team_smem_bytes(int max_nodes, int max_leaves);
 int team_max_cluster();
 int team_max_active_clusters(int cluster, int max_nodes, int max_leaves);
-// Launches min(njobs, resident teams) teams of the build that holds the most.
-cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s);
+// Launches min(njobs, resident teams) teams.  ctas_per_sm: 1 or 2 picks the
+// build (255 or 128 registers per thread); 0 takes the one-CTA-per-SM build
+// when it holds a team for every job, else the one that holds more teams.
+cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s, int ctas_per_sm);
 // The whole-GPU team: CTAs of one cooperative launch (one per SM), or 0 when
 // the device or the shared-memory size does not allow it.
 int team_wide_ctas(int max_nodes, int max_leaves);

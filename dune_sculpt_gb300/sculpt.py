@@ -27,8 +27,9 @@ PBVH_Leaf, PBVH_UpdateNormals, PBVH_UpdateBB, PBVH_UpdateOriginalBB = 1, 2, 4, 8
 PBVH_UpdateDrawBuffers, PBVH_UpdateRedraw = 16, 32
 STROKE_EAGER, STROKE_GRAPH, STROKE_TEAM = 0, 1, 2
 BATCH_SEQUENTIAL, BATCH_TEAM = 0, 1
-TEAM_SIZES = (1, 2, 4, 8, 16)
 TEAM_GRID = -1  # SGPU_TEAM_GRID: every SM of the GPU works on one stroke
+TEAM_SIZES = (TEAM_GRID, 1, 2, 4, 8, 16)  # sgpu_autotune_team's candidates, in order
+BATCH_TEAM_CANDIDATES = ((16, 1), (8, 1), (8, 2), (4, 1), (4, 2), (2, 2), (TEAM_GRID, 1))
 INJECT_ALLOC_FAIL, INJECT_WAIT_NS, INJECT_BARRIER_EXTRA = 1, 2, 3
 
 
@@ -93,6 +94,7 @@ EXPORTS = (
     "sgpu_raycast", "sgpu_draw_buffers_build", "sgpu_draw_buffers_update",
     "sgpu_draw_buffers_layout", "sgpu_draw_buffers_overlay", "sgpu_draw_buffers_get",
     "sgpu_draw_buffers_device", "sgpu_draw_buffers_update_timed", "sgpu_debug_inject",
+    "sgpu_calc_area_normal_and_center", "sgpu_stroke_host_grids", "sgpu_autotune_batch",
 )
 
 DRAW_STRIDE = 36  # SGPU_DRAW_STRIDE
@@ -169,8 +171,12 @@ def load(path: str | None = None):
     L.sgpu_mesh_get_team.argtypes = [vp, vp]
     L.sgpu_autotune_team.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp]
     L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
+    L.sgpu_autotune_batch.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp]
     L.sgpu_mesh_store_original.argtypes = [vp]
     L.sgpu_debug_inject.argtypes = [i, C.c_int64]
+    L.sgpu_calc_area_normal_and_center.argtypes = [vp, C.POINTER(SGPU_Brush), vp, vp, i, vp, vp]
+    L.sgpu_stroke_host_grids.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp, vp, i,
+                                         C.POINTER(SGPU_StrokeStats)]
     L.sgpu_draw_buffers_build.argtypes = [vp, C.POINTER(SGPU_DrawSetup)]
     L.sgpu_draw_buffers_update.argtypes = [vp]
     L.sgpu_draw_buffers_update_timed.argtypes = [vp, i, vp]
@@ -186,6 +192,28 @@ def debug_inject(what: int, value: int):
     """Host-side failure injection (sgpu_debug_inject): INJECT_ALLOC_FAIL,
     INJECT_WAIT_NS or INJECT_BARRIER_EXTRA."""
     _check(load().sgpu_debug_inject(what, value))
+
+
+def _batch_args(pbvhs, strokes, dab_tools):
+    n = len(pbvhs)
+    handles = (C.c_void_p * n)(*[p.handle for p in pbvhs])
+    brushes = (SGPU_Brush * n)(*[make_brush(s) for s in strokes])
+    dabs = np.ascontiguousarray(np.concatenate([s.dabs for s in strokes]), dtype=np.float32)
+    offs = np.zeros(n + 1, dtype=np.int32)
+    offs[1:] = np.cumsum([s.dabs.shape[0] for s in strokes])
+    tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+    return n, handles, brushes, dabs, offs, tools
+
+
+def autotune_batch(pbvhs, strokes, dab_tools=None):
+    """sgpu_autotune_batch: ((cluster, CTAs per SM) of the fastest team,
+    {candidate: ms})."""
+    n, handles, brushes, dabs, offs, tools = _batch_args(pbvhs, strokes, dab_tools)
+    cl, per_sm = C.c_int(), C.c_int()
+    ms = np.zeros(len(BATCH_TEAM_CANDIDATES), dtype=np.float32)
+    _check(load().sgpu_autotune_batch(handles, n, brushes, _p(dabs), _p(offs), _p(tools),
+                                      C.byref(cl), C.byref(per_sm), _p(ms)))
+    return (cl.value, per_sm.value), {c: float(t) for c, t in zip(BATCH_TEAM_CANDIDATES, ms)}
 
 
 def batch_stroke(pbvhs, strokes, mode: int = BATCH_TEAM, cluster: int = 0, dab_tools=None):
@@ -437,6 +465,18 @@ class PBVH:
         _check(getattr(load(), fn)(self._h, C.byref(b), _p(loc), _p(gd), _p(nd),
                                    0 if nd is None else nd.shape[0]))
 
+    def area_normal_center(self, st, location, nodes=None):
+        """sgpu_calc_area_normal_and_center: (area normal, area centre)."""
+        b = make_brush(st)
+        loc = np.asarray(location, dtype=np.float32)
+        nd = None if nodes is None else np.ascontiguousarray(nodes, dtype=np.int32)
+        no = np.zeros(3, dtype=np.float32)
+        co = np.zeros(3, dtype=np.float32)
+        _check(load().sgpu_calc_area_normal_and_center(
+            self._h, C.byref(b), _p(loc), _p(nd), 0 if nd is None else nd.shape[0], _p(no),
+            _p(co)))
+        return no, co
+
     def do_draw_brush(self, st, location, grab_delta, nodes=None):
         self._brush("sgpu_do_draw_brush", st, location, grab_delta, nodes)
 
@@ -502,6 +542,18 @@ class PBVH:
                                        C.byref(stats)))
         return stats
 
+    def stroke_host_grids(self, st, co_in, co_out, normals_in=None, dabs=None,
+                          dab_tools=None, mode: int = STROKE_TEAM) -> SGPU_StrokeStats:
+        """GRIDS host-buffer stroke (3 floats per element in and out)."""
+        b = make_brush(st)
+        d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
+        tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+        stats = SGPU_StrokeStats()
+        _check(load().sgpu_stroke_host_grids(self._h, C.byref(b), _p(d), d.shape[0], _p(tools),
+                                             _p(co_in), _p(normals_in), _p(co_out), mode,
+                                             C.byref(stats)))
+        return stats
+
     def stroke_team_profile(self, st, dabs=None, dab_tools=None):
         """Persistent stroke with phase timers and algorithmic-byte counters.
         Returns ({phase: {ms, bytes}}, total_ms, stats)."""
@@ -548,7 +600,7 @@ class PBVH:
         d = np.ascontiguousarray(st.dabs if dabs is None else dabs, dtype=np.float32)
         tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
         best = C.c_int()
-        ms = np.zeros(5, dtype=np.float32)
+        ms = np.zeros(len(TEAM_SIZES), dtype=np.float32)
         _check(load().sgpu_autotune_team(self._h, C.byref(b), _p(d), d.shape[0], _p(tools),
                                          C.byref(best), _p(ms)))
         return best.value, {s: float(t) for s, t in zip(TEAM_SIZES, ms)}

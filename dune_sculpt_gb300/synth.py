@@ -68,16 +68,17 @@ def value_noise(seed: int, stream: int, p: np.ndarray, freq: float) -> np.ndarra
     i0 = np.floor(q)
     f = q - i0
     i0 = i0.astype(np.int64)
+    table = hash_u01(seed, stream, np.arange(512, dtype=np.uint64))  # the 8^3 lattice values
+    # per axis: lattice index mod 8 (x & 7 == x % 8 for two's-complement
+    # integers) and weight of the lower and upper corner
+    ii = [[(np.ascontiguousarray(i0[:, a]) + d) & 7 for d in (0, 1)] for a in range(3)]
+    ww = [[1.0 - np.ascontiguousarray(f[:, a]), np.ascontiguousarray(f[:, a])] for a in range(3)]
     out = np.zeros(q.shape[0], dtype=np.float64)
     for dz in (0, 1):
         for dy in (0, 1):
             for dx in (0, 1):
-                ix = (i0[:, 0] + dx) % 8
-                iy = (i0[:, 1] + dy) % 8
-                iz = (i0[:, 2] + dz) % 8
-                lat = hash_u01(seed, stream, (ix * 64 + iy * 8 + iz).astype(np.uint64))
-                w = ((f[:, 0] if dx else 1.0 - f[:, 0]) * (f[:, 1] if dy else 1.0 - f[:, 1])
-                     * (f[:, 2] if dz else 1.0 - f[:, 2]))
+                lat = table[ii[0][dx] * 64 + ii[1][dy] * 8 + ii[2][dz]]
+                w = ww[0][dx] * ww[1][dy] * ww[2][dz]
                 out += w * lat
     return out
 

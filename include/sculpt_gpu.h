@@ -231,6 +231,17 @@ int sgpu_mesh_store_original(sgpu_mesh *mesh);
 int sgpu_do_brush(sgpu_mesh *mesh, const SGPU_Brush *brush, const float location[3],
                   const float grab_delta[3], const int *nodes, int totnode);
 
+/* The area normal and centre that a draw, clay-strips, pinch or crease pass
+ * computes before it moves vertices (SCULPT_calc_area_normal_and_center of
+ * the absent sculpt.c; the compensated tree reduction of the brush
+ * specification): normals of the visited vertices within
+ * radius * normal_radius_factor of location, positions within
+ * radius * area_radius_factor, over the device list of the last search
+ * (nodes == NULL) or the given leaves.  Moves nothing.  Synchronous. */
+int sgpu_calc_area_normal_and_center(sgpu_mesh *mesh, const SGPU_Brush *brush,
+                                     const float location[3], const int *nodes, int totnode,
+                                     float r_area_no[3], float r_area_co[3]);
+
 /* BKE_pbvh_update_normals (FACES: tagged vertices of flagged leaves; GRIDS:
  * inner grid normals of the affected faces plus seam stitching). */
 int sgpu_pbvh_update_normals(sgpu_mesh *mesh);
@@ -261,15 +272,39 @@ int sgpu_stroke(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, 
  * launch; the CTAs meet at barriers in global memory whose waits are bounded:
  * a wait that runs out ends the launch and the call returns
  * SGPU_ERR_TIMEOUT).  A batch with SGPU_TEAM_GRID runs its strokes one after
- * another.  Default 8. */
+ * another.  Default: the autotuner's cached team for the stroke (see
+ * sgpu_autotune_team), else 8. */
 #define SGPU_TEAM_GRID (-1)
 int sgpu_mesh_set_team(sgpu_mesh *mesh, int cluster_size);
 int sgpu_mesh_get_team(const sgpu_mesh *mesh, int *cluster_size);
-/* Autotuner: times the stroke in SGPU_STROKE_TEAM mode for every cluster size,
- * restoring the mesh state between trials, and keeps the fastest for the mesh.
- * r_ms (nullable) receives 5 timings (sizes 1, 2, 4, 8, 16; -1 if unsupported). */
+/* Autotuner of the persistent stroke kernel's team shape.  Times the stroke
+ * in SGPU_STROKE_TEAM mode on every candidate team — the whole GPU, then
+ * clusters of 1, 2, 4, 8 and 16 CTAs (one CTA per SM, the full register
+ * file) — restoring the mesh state between trials (second of two trials), and
+ * keeps the fastest for the mesh.  The choice is also cached process-wide
+ * under (mesh type, log2 of the vertex count, the set of tools in the stroke,
+ * symmetry passes): a mesh whose team was never set (sgpu_mesh_set_team or
+ * this call) strokes on the cached team of its stroke's key.  The block size
+ * is fixed at 256 threads: the area reduction's 256-lane tree is part of the
+ * brush specification.  r_ms (nullable) receives SGPU_AUTOTUNE_CANDIDATES
+ * timings in that order (-1 where a candidate cannot run). */
+#define SGPU_AUTOTUNE_CANDIDATES 6
 int sgpu_autotune_team(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
                        int ndabs, const int *dab_tools, int *r_cluster, float *r_ms);
+
+/* Autotuner of a batch's team shape (the arguments of sgpu_batch_stroke):
+ * times SGPU_BATCH_TEAM on the candidates (cluster, CTAs per SM) = (16, 1),
+ * (8, 1), (8, 2), (4, 1), (4, 2), (2, 2) and the whole GPU (strokes one after
+ * another), restoring every mesh between trials, and caches the fastest under
+ * (mesh count, log2 of the total vertex count, the set of tools), where
+ * sgpu_batch_stroke with cluster_size 0 finds it.  Two CTAs per SM run the
+ * build with 128 registers per thread: twice the teams, slower each.
+ * r_ms (nullable): SGPU_AUTOTUNE_BATCH_CANDIDATES timings, -1 where a
+ * candidate cannot run. */
+#define SGPU_AUTOTUNE_BATCH_CANDIDATES 7
+int sgpu_autotune_batch(sgpu_mesh **meshes, int nmesh, const SGPU_Brush *brushes,
+                        const SGPU_Dab *dabs, const int *dab_offsets, const int *dab_tools,
+                        int *r_cluster, int *r_ctas_per_sm, float *r_ms);
 
 /* Profile of one SGPU_STROKE_TEAM stroke: the persistent kernel's time split
  * by phase (time of the team's first thread from phase start to the barrier
@@ -382,7 +417,8 @@ int sgpu_draw_buffers_device(sgpu_mesh *mesh, void **d_vbo, size_t *bytes);
  *   SGPU_BATCH_SEQUENTIAL: one graph-mode stroke per mesh, one after another.
  *   SGPU_BATCH_TEAM: one persistent launch; cluster teams take meshes from a
  *     work queue, longest estimated stroke first.
- * cluster_size 0 uses the first mesh's setting.  stats (nullable) gets one
+ * cluster_size 0 uses the team sgpu_autotune_batch cached for a batch like
+ * this one, else the first mesh's setting.  stats (nullable) gets one
  * entry per mesh; r_total_ms the CUDA-event time of the whole batch. */
 #define SGPU_BATCH_SEQUENTIAL 0
 #define SGPU_BATCH_TEAM 1
@@ -399,6 +435,14 @@ int sgpu_stroke_host(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *d
                      const int *dab_tools, const SGPU_MVert *verts_in,
                      const float *vert_normals_in, SGPU_MVert *verts_out, int mode,
                      SGPU_StrokeStats *stats);
+
+/* The same for a GRIDS mesh: grids_co_in (and grids_no_in, nullable) hold 3
+ * floats per grid element in the element order of sgpu_mesh_create_grids;
+ * grids_co_out receives the positions after the stroke, same layout. */
+int sgpu_stroke_host_grids(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
+                           int ndabs, const int *dab_tools, const float *grids_co_in,
+                           const float *grids_no_in, float *grids_co_out, int mode,
+                           SGPU_StrokeStats *stats);
 
 /* ---- per-stroke restore (undo) ----
  * snapshot copies positions, normals, mask, node boxes and node flags into

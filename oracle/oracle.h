@@ -128,6 +128,13 @@ int64_t or_stroke(OrMesh *m, const OrBrush *b, const float *dabs, int ndabs,
  * into the FP64 state, widening each value exactly. */
 void or_sync64(OrMesh *m);
 
+/* The area normal and centre of one pass over the given leaves (node
+ * indices) at location, in FP32 (out32: normal, centre) and in FP64 from the
+ * same positions and normals (out64; the FP64 state is set to the FP32 one
+ * first, or_sync64). */
+void or_area_normal_center(OrMesh *m, const OrBrush *b, const float location[3],
+                           const int *nodes, int totnode, float out32[6], double out64[6]);
+
 /* The FP32 stroke, with the rounding error of each measured dab (every
  * stride-th, from dab 0) against FP64, stage by stage from the same input:
  * the FP64 state is set to the FP32 one (or_sync64) before the brush, before

@@ -169,6 +169,23 @@ static void max_diff(const float *f, const double *d, size_t n, double *r_diff, 
   *r_ref = mr;
 }
 
+void or_area_normal_center(OrMesh *m, const OrBrush *b, const float location[3],
+                           const int *nodes, int totnode, float out32[6], double out64[6])
+{
+  or_sync64(m);
+  float nf[3], cf[3];
+  double nd[3], cd[3];
+  const double locd[3] = {location[0], location[1], location[2]};
+  area_calc_f(m, &m->sf, b, location, nodes, totnode, nf, cf);
+  area_calc_d(m, &m->sd, b, locd, nodes, totnode, nd, cd);
+  for (int k = 0; k < 3; k++) {
+    out32[k] = nf[k];
+    out32[3 + k] = cf[k];
+    out64[k] = nd[k];
+    out64[3 + k] = cd[k];
+  }
+}
+
 /* Node flags and vertex tags (FACES) of the oracle, saved and put back so
  * that both precisions run a stage from the same flags. */
 typedef struct FlagState {

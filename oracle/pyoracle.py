@@ -73,6 +73,7 @@ def lib():
         L.or_stroke.restype = C.c_int64
         L.or_stroke.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
         L.or_sync64.argtypes = [vp]
+        L.or_area_normal_center.argtypes = [vp, C.POINTER(OrBrush), vp, vp, i, vp, vp]
         L.or_stroke_local_error.restype = C.c_int64
         L.or_stroke_local_error.argtypes = [vp, C.POINTER(OrBrush), vp, i, vp, i, i, vp]
         L.or_draw_build.restype = C.c_int64
@@ -377,6 +378,18 @@ class OracleMesh:
 
     def sync64(self):
         lib().or_sync64(self.h)
+
+    def area_normal_center(self, st, location, nodes):
+        """Area normal and centre over the leaves nodes at location: (FP32 6
+        floats, FP64 6 doubles from the same state)."""
+        b = make_brush(st)
+        loc = np.asarray(location, dtype=np.float32)
+        nd = np.ascontiguousarray(nodes, dtype=np.int32)
+        o32 = np.zeros(6, dtype=np.float32)
+        o64 = np.zeros(6, dtype=np.float64)
+        lib().or_area_normal_center(self.h, C.byref(b), _p(loc), _p(nd), nd.shape[0], _p(o32),
+                                    _p(o64))
+        return o32, o64
 
 
 def kelvinlet(kind: int, radius: float, force: float, poisson: float, co, location, dn):

@@ -12,12 +12,28 @@ import numpy as np
 import pytest
 
 from dune_sculpt_gb300 import synth
-from dune_sculpt_gb300.sculpt import (BATCH_TEAM, PBVH, STROKE_GRAPH, STROKE_TEAM,
+from dune_sculpt_gb300.sculpt import (BATCH_TEAM, PBVH, STROKE_GRAPH, STROKE_TEAM, TEAM_GRID,
                                       batch_stroke)
 
 from helpers import bits_equal, first_diff, rel_err
 
 pytestmark = pytest.mark.gpu
+
+# Error of the GPU result against FP64 (the GPU equals the FP32 restatement
+# bit for bit, so the restatement's per-stage error from the same input,
+# or_stroke_local_error, is the GPU's): positions and the area normal/centre
+# <= 1e-6, boxes exact, normals <= 4e-6 (the reference's FP32 cross products
+# of near-degenerate triangles and grid quads; measured 1.8e-6 on the
+# multires workload).
+FP64_TOL = 1e-6
+FP64_TOL_NORMALS = 4e-6
+
+
+def _check_local(err, what):
+    assert err["co"] <= FP64_TOL, (what, err)
+    assert err["bb"] == 0.0, (what, err)
+    assert err["area_no"] <= FP64_TOL and err["area_co"] <= FP64_TOL, (what, err)
+    assert err["no"] <= FP64_TOL_NORMALS, (what, err)
 
 
 def _check(gp, o, what):
@@ -28,10 +44,11 @@ def _check(gp, o, what):
 
 
 @pytest.mark.parametrize("cfg", ["grid_draw", "icosphere_smooth"])
-def test_fullsize_faces_vs_oracle_fp64(gpu, oracle, cfg):
+@pytest.mark.parametrize("team", [16, TEAM_GRID])
+def test_fullsize_faces_vs_oracle_fp64(gpu, oracle, cfg, team):
     m, st, ll = (synth.cfg1_grid_draw() if cfg == "grid_draw" else synth.cfg2_icosphere_smooth())
     gp = PBVH.build_mesh(m, ll)
-    gp.set_team(16)
+    gp.set_team(team)
     s = gp.stroke(st, mode=STROKE_TEAM)
     o = oracle.OracleMesh.faces(m, ll)
     o.recalc_all_normals()
@@ -45,19 +62,33 @@ def test_fullsize_clay_strips_sphere(gpu, oracle):
     m, st, ll = synth.cfg3_sphere_clay()
     gp = PBVH.build_mesh(m, ll)
     gp.snapshot()
-    gp.set_team(16)
+    gp.set_team(TEAM_GRID)
     s = gp.stroke(st, mode=STROKE_TEAM)
     o = oracle.OracleMesh.faces(m, ll)
     o.recalc_all_normals()
-    tot, _ = o.stroke(st, which=1)
+    tot, err = o.stroke_local_error(st, stride=4)
     assert s.verts_displaced == tot and tot > 0
     _check(gp, o, "clay strips")
+    _check_local(err, "clay strips")
     # the per-call kernels replayed as a graph give the same state
     team_co = gp.positions()
     gp.restore()
     s2 = gp.stroke(st, mode=STROKE_GRAPH)
     assert s2.verts_displaced == tot
     assert bits_equal(gp.positions(), team_co)
+    # the area normal and centre at every 16th dab location on the GPU against
+    # an FP64 reduction of the same vertex set
+    gp.restore()
+    o = oracle.OracleMesh.faces(m, ll)
+    o.recalc_all_normals()
+    r = np.float32(st.radius) * np.float32(1.41421356237309504880)
+    for d in range(0, st.dabs.shape[0], 16):
+        loc = st.dabs[d, :3]
+        nodes = o.search_sphere(loc, float(np.float32(r * r)))
+        a32, a64 = o.area_normal_center(st, loc, nodes)
+        no, co = gp.area_normal_center(st, loc, nodes)
+        assert bits_equal(np.concatenate([no, co]), a32), d
+        assert np.abs(a32.astype(np.float64) - a64).max() <= FP64_TOL, d
 
 
 def test_fullsize_batch(gpu, oracle):
@@ -69,9 +100,10 @@ def test_fullsize_batch(gpu, oracle):
     for k, ((m, st, ll), g, s) in enumerate(zip(batch, gs, stats)):
         o = oracle.OracleMesh.faces(m, ll)
         o.recalc_all_normals()
-        tot, _ = o.stroke(st, which=1)
+        tot, err = o.stroke_local_error(st)
         assert s.verts_displaced == tot, k
         _check(g, o, f"mesh {k}")
+        _check_local(err, f"mesh {k}")
         o.close()
 
 
@@ -82,14 +114,15 @@ def test_fullsize_multires(gpu, oracle):
     st = synth.Stroke(synth.TOOL_DRAW, 0.04, 0.6, synth.CURVE_SMOOTH, 0, dabs)
     gp = PBVH.build_grids(g)
     assert gp.num_verts == 50000 * 289
-    gp.set_team(16)
+    gp.set_team(TEAM_GRID)
     s = gp.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
     o = oracle.OracleMesh.grids(g)
     o.recalc_all_normals()
-    tot, _ = o.stroke(st, which=1, dab_tools=tools)
+    tot, err = o.stroke_local_error(st, dab_tools=tools, stride=4)
     assert s.verts_displaced == tot and tot > 0
     _check(gp, o, "multires")
     assert bits_equal(gp.mask(), o.mask())
+    _check_local(err, "multires")
 
 
 def test_fullsize_zero_strength_noop(gpu):

@@ -96,3 +96,24 @@ def test_clay_strips_plane_offset_and_factors(gpu, oracle):
                       synth.arc_dabs(31, 12, 0.05), normal_radius_factor=0.3,
                       area_radius_factor=0.8, plane_offset=0.2)
     assert _check(g, o, st, STROKE_TEAM, what="clay offset") > 0
+
+
+def test_area_normal_center_matches_oracle(gpu, oracle):
+    """sgpu_calc_area_normal_and_center: bit-equal to the FP32 restatement and
+    within 1e-6 of an FP64 reduction of the same vertex set, FACES and GRIDS."""
+    from helpers import small_uvsphere
+
+    m = small_uvsphere(128)
+    cases = [(PBVH.build_mesh(m, 800), oracle.OracleMesh.faces(m, 800), synth.arc_dabs(7, 20, 0.05))]
+    gr = synth.torus_grids(16, 6, level=4)
+    cases.append((PBVH.build_grids(gr, 4), oracle.OracleMesh.grids(gr, 4), synth.torus_dabs(9, 20, 0.1)))
+    st = synth.Stroke(synth.TOOL_CLAY_STRIPS, 0.12, 0.8, synth.CURVE_SHARP, 0, None)
+    for g, o, dabs in cases:
+        o.recalc_all_normals()
+        for d in range(dabs.shape[0]):
+            loc = dabs[d, :3]
+            nodes = o.search_sphere(loc, float(np.float32(np.float32(0.12) * np.float32(0.12))))
+            a32, a64 = o.area_normal_center(st, loc, nodes)
+            no, co = g.area_normal_center(st, loc, nodes)
+            assert np.array_equal(np.concatenate([no, co]).view(np.uint32), a32.view(np.uint32)), d
+            assert np.abs(a32.astype(np.float64) - a64).max() <= 1e-6, d

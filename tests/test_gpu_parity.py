@@ -289,11 +289,36 @@ def test_autotune_restores_state(gpu, oracle):
     st = synth.Stroke(synth.TOOL_DRAW, 0.1, 0.5, synth.CURVE_SMOOTH, synth.SYMM_X,
                       synth.arc_dabs(21, 12, 0.03))
     best, times = g.autotune_team(st)
-    assert best in (1, 2, 4, 8, 16)
-    assert times[best] > 0
+    assert best in (TEAM_GRID, 1, 2, 4, 8, 16)
+    assert times[best] > 0 and times[best] == min(t for t in times.values() if t > 0)
     assert g.team() == best
     _assert_state_equal(g, o, "after autotune")
     stats = g.stroke(st, mode=STROKE_TEAM)
     tot, _ = o.stroke(st, which=1)
     assert stats.verts_displaced == tot
     _assert_state_equal(g, o, "autotuned stroke")
+
+
+def test_autotune_batch_and_cached_choice(gpu, oracle):
+    """The batch autotuner restores every mesh, and sgpu_batch_stroke with
+    cluster 0 runs on its cached team with the same result."""
+    from dune_sculpt_gb300.sculpt import autotune_batch
+
+    batch = synth.cfg4_batch(nmesh=5, vmin=2000, vmax=20000, ndabs=8)
+    gs, os_, strokes = [], [], []
+    for m, st, _ in batch:
+        gs.append(PBVH.build_mesh(m, 300))
+        o = oracle.OracleMesh.faces(m, 300)
+        o.recalc_all_normals()
+        os_.append(o)
+        strokes.append(st)
+    (cl, per_sm), times = autotune_batch(gs, strokes)
+    assert times[(cl, per_sm)] > 0
+    assert times[(cl, per_sm)] == min(t for t in times.values() if t > 0)
+    for g, o in zip(gs, os_):
+        _assert_state_equal(g, o, "after batch autotune")
+    stats, _ = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=0)
+    for g, o, st, s in zip(gs, os_, strokes, stats):
+        tot, _ = o.stroke(st, which=1)
+        assert s.verts_displaced == tot
+        _assert_state_equal(g, o, "cached batch team")
