@@ -351,7 +351,16 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->alloc(&d.work, 1))) return rc;
   if ((rc = m->alloc(&d.cull_list, L + 1))) return rc;
   if ((rc = m->alloc(&d.cull_off, L + 2))) return rc;
-  if ((rc = m->alloc(&d.parts, L + 1))) return rc;
+  {
+    int blocks = 1;
+    for (int k = 0; k < L; k++) {
+      const int node = h.leaf_nodes[k];
+      const int nv = h.type == kFaces ? h.uniq[node] : h.totprim[node] * h.grid_area;
+      blocks = std::max(blocks, (nv + kAreaBlock - 1) / kAreaBlock);
+    }
+    d.area_blocks = blocks;
+  }
+  if ((rc = m->alloc(&d.parts, static_cast<size_t>(L) * d.area_blocks + 1))) return rc;
   if ((rc = m->alloc(&d.scratch, nslot))) return rc;
   if ((rc = m->alloc(&d.scratch2, nslot))) return rc;
   for (int k = 0; k < 2; k++) {
@@ -1115,6 +1124,9 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
   if ((rc = m->upload(&d.edge_elems, h.edge_elems))) return bail(rc);
   if ((rc = m->upload(&d.bvert_off, h.bvert_off))) return bail(rc);
   if ((rc = m->upload(&d.bvert_elems, h.bvert_elems))) return bail(rc);
+  if ((rc = m->upload(&d.edge_face, h.edge_face))) return bail(rc);
+  if ((rc = m->upload(&d.bvert_face, h.bvert_face))) return bail(rc);
+  d.max_face_corners = h.max_face_corners;
   if ((rc = m->alloc(&d.face_list, num_faces))) return bail(rc);
   if ((rc = m->alloc(&d.cgrid_list, num_grids))) return bail(rc);
   if ((rc = m->alloc(&d.edge_list, num_base_edges))) return bail(rc);
@@ -2107,7 +2119,11 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
     max_nodes = std::max(max_nodes, meshes[i]->dev.totnode);
     max_leaves = std::max(max_leaves, meshes[i]->dev.nleaf);
   }
-  if (max_leaves > 64 * 256 || team_smem_bytes(max_nodes, max_leaves) > 160 * 1024)
+  int max_parts = 0;
+  for (int i = 0; i < n; i++)
+    max_parts = std::max(max_parts, meshes[i]->dev.nleaf * meshes[i]->dev.area_blocks);
+  if (max_leaves > 64 * 256 || max_parts > 64 * 256 ||
+      team_smem_bytes(max_nodes, max_leaves) > 160 * 1024)
     return fail(SGPU_ERR_UNSUPPORTED, "PBVH too large for the persistent stroke kernel");
   const bool wide = cluster == SGPU_TEAM_GRID;
   int wide_ctas = 0;

@@ -452,6 +452,15 @@ bool build_grids(HostMesh& m, std::string* err) {
       const int g = m.face_start[f] + c;
       m.bvert_elems[vfill[m.face_verts[g]]++] = elem(g, gs - 1, gs - 1);
     }
+  // the face of every edge and base-vertex slot (any element of the slot lies
+  // in a grid of that face), and the most corners of a face
+  m.edge_face.resize(m.edge_off[m.num_base_edges]);
+  for (size_t k = 0; k < m.edge_face.size(); k++)
+    m.edge_face[k] = m.grid_face[m.edge_elems[k * 2 * gs] / area];
+  m.bvert_face.resize(m.bvert_off[m.num_base_verts]);
+  for (size_t k = 0; k < m.bvert_face.size(); k++) m.bvert_face[k] = m.grid_face[m.bvert_elems[k] / area];
+  m.max_face_corners = 0;
+  for (int f = 0; f < m.num_faces; f++) m.max_face_corners = std::max(m.max_face_corners, m.face_ngrids[f]);
   // BKE_pbvh_build_grids, pbvh.c:2516-2561
   std::vector<PrimBox> prims(m.num_grids);
   Box cb;

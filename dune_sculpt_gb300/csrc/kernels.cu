@@ -151,10 +151,12 @@ __global__ void __launch_bounds__(kCullThreads) k_set_list(DevMesh m, const int*
 }
 
 // ---------------------------------------------------------------------------
-// Area normal / centre (spec): per culled leaf, lane t (of 256) sums elements
-// t, t+256, ... with compensated sums; lanes merge pairwise (t, t+s) for
-// s = 128 .. 1; leaf partials then merge pairwise over the culled-list index
-// (i, i+s), s = 1, 2, 4, ...  The last CTA to finish performs that final tree.
+// Area normal / centre (spec): each culled leaf in blocks of kAreaBlock
+// visited vertices (area_blocks per leaf, the empty ones zero); in a block,
+// lane t (of 256) sums its elements t, t+256, ... with compensated sums;
+// lanes merge pairwise (t, t+s) for s = 128 .. 1; the block partials then
+// merge pairwise over (culled-list index, block) in order, (i, i+s),
+// s = 1, 2, 4, ...  The last CTA to finish performs that final tree.
 
 __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassParams pp) {
   __shared__ Lane sl[kThreads];
@@ -165,14 +167,17 @@ __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassPa
   const float rn2 = rn * rn, ra2 = ra * ra;
   const int t = threadIdx.x;
   unsigned long long ab = 0;  // algorithmic bytes (profiling)
-  for (int k = blockIdx.x; k < cnt; k += gridDim.x) {
-    const int leaf = m.cull_list[k];
-    const int nv = leaf_nverts(m, leaf);
+  const int nb = m.area_blocks;
+  const int nparts = cnt * nb;
+  for (int k = blockIdx.x; k < nparts; k += gridDim.x) {
+    const int leaf = m.cull_list[k / nb];
+    const int i0 = (k % nb) * kAreaBlock;
+    const int nv = min(leaf_nverts(m, leaf), i0 + kAreaBlock);
     Lane l;
 #pragma unroll
     for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
     l.n_no = l.n_co = 0;
-    for (int i = t; i < nv; i += kThreads) {
+    for (int i = i0 + t; i < nv; i += kThreads) {
       const int v = leaf_vert(m, leaf, i);
       const float4 co = m.co[v];
       const float d2 = dist_sq(co, pp.loc);
@@ -221,8 +226,8 @@ __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassPa
   __syncthreads();
   if (!am_last) return;
   __threadfence();
-  for (int s = 1; s < cnt; s <<= 1) {
-    for (int i = t * 2 * s; i + s < cnt; i += kThreads * 2 * s) {
+  for (int s = 1; s < nparts; s <<= 1) {
+    for (int i = t * 2 * s; i + s < nparts; i += kThreads * 2 * s) {
       Lane a = part_load(&m.parts[i]);
       lane_merge(a, part_load(&m.parts[i + s]));
       part_store(&m.parts[i], a);
@@ -232,7 +237,7 @@ __global__ void __launch_bounds__(kThreads) k_area(DevMesh m, DevBrush b, PassPa
   }
   if (t == 0) {
     Lane tot;
-    if (cnt > 0) {
+    if (nparts > 0) {
       tot = part_load(&m.parts[0]);
     } else {
 #pragma unroll
@@ -686,7 +691,8 @@ cudaError_t launch_set_list(const DevMesh& m, const int* dev_nodes, int totnode,
 
 cudaError_t launch_area(const DevMesh& m, const DevBrush& b, const PassParams& pp,
                         cudaStream_t s) {
-  int g = m.nleaf < work_grid() ? m.nleaf : work_grid();
+  const int items = m.nleaf * m.area_blocks;
+  int g = items < work_grid() ? items : work_grid();
   if (g < 1) g = 1;
   k_area<<<g, kThreads, 0, s>>>(m, b, pp);
   return cudaGetLastError();

@@ -110,6 +110,9 @@ struct DevMesh {
   const int* edge_elems;
   const int* bvert_off;
   const int* bvert_elems;
+  const int* edge_face;   // face of each edge_elems slot
+  const int* bvert_face;  // face of each bvert_elems slot
+  int max_face_corners;
   int* face_list;
   int* cgrid_list;  // grids of the claimed faces
   int* edge_list;
@@ -122,7 +125,8 @@ struct DevMesh {
   Work* work;
   int* cull_list;  // nleaf
   int* cull_off;   // nleaf+1: prefix of brush-visible vertex counts over cull_list
-  AreaPart* parts;  // nleaf
+  AreaPart* parts;  // nleaf * area_blocks
+  int area_blocks;  // blocks of kAreaBlock visited vertices per leaf in the area reduction
   float4* scratch;   // smooth Jacobi values, totvert
   float4* scratch2;  // second value buffer of the slot sweeps, totvert
   int* slot_map[2];  // vertex -> smooth slot of a pass, or -1; passes alternate
@@ -879,6 +883,21 @@ __device__ __forceinline__ int vertex_normal(const DevMesh& m, int v, float4& ou
 
 __device__ __forceinline__ float fmin_ref(float a, float b) { return (a < b) ? a : b; }
 __device__ __forceinline__ float fmax_ref(float a, float b) { return (a > b) ? a : b; }
+
+// The area reduction visits each culled leaf in blocks of kAreaBlock
+// vertices (256 lanes x 16); every leaf counts DevMesh::area_blocks blocks
+// (the largest ceil(visited vertices / kAreaBlock) over the leaves; blocks
+// past a leaf's end are empty partials).
+constexpr int kAreaBlock = 4096;
+
+// 16-byte asynchronous copy global -> shared (no register holds the data).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned int d = static_cast<unsigned int>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
 
 // Area normal/centre lanes: compensated (s, e) sums of normal xyz and centre
 // xyz plus the two counts; merged pairwise in the order the spec fixes.

@@ -59,6 +59,8 @@ struct HostMesh {
   std::vector<int> grid_face;
   std::vector<int> edge_off, edge_elems;    // per base edge: faces * 2*grid_size elements
   std::vector<int> bvert_off, bvert_elems;  // per base vertex: one corner element per face
+  std::vector<int> edge_face, bvert_face;   // the face of each edge / base-vertex slot
+  int max_face_corners = 0;
   // positions used for the build (float xyz)
   std::vector<float> co;
   // PBVH (reference node numbering)

@@ -551,51 +551,53 @@ static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int
   __syncthreads();
 }
 
-// Compensated area partial of one culled leaf by the CTA (256 lanes), the same
-// structure as k_area.
-static __device__ void team_area_leaf(const DevMesh& m, const PassParams& pp, float rn2, float ra2,
-                               int leaf, Lane* sl, AreaPart* out) {
+// Compensated area partial of one block (at most kAreaBlock visited
+// vertices) of a culled leaf by the CTA: the lane structure of k_area.  The
+// block's positions and normals are staged in shared memory kAreaStage at a
+// time with cp.async (16 bytes each, no register holds them in flight), so a
+// lane's elements arrive together instead of in dependent batches; lane t
+// then adds its elements t, t+256, ... of the stage in order.
+constexpr int kAreaStage = 1024;  // staged vertices per round: 32 KB (positions, normals)
+static_assert(2 * kAreaStage <= kNbCache * kTeamThreads, "the area stage exceeds the smooth tables");
+static __device__ void team_area_block(const DevMesh& m, const PassParams& pp, float rn2,
+                                       float ra2, int leaf, int blk, float4* s_stage, Lane* sl,
+                                       AreaPart* out) {
   const int t = threadIdx.x;
-  const int nv = leaf_nverts(m, leaf);
+  const int i0 = blk * kAreaBlock;
+  const int i1 = min(leaf_nverts(m, leaf), i0 + kAreaBlock);
+  float4* s_co = s_stage;
+  float4* s_no = s_stage + kAreaStage;
   Lane l;
 #pragma unroll
   for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
   l.n_no = l.n_co = 0;
-  // lane t takes elements t, t + 256, ... in order; loads of kAreaBatch of
-  // them are issued together
-  constexpr int kAreaBatch = 2;
-  for (int i0 = t; i0 < nv; i0 += kAreaBatch * kTeamThreads) {
-    int vv[kAreaBatch];
-#pragma unroll
-    for (int j = 0; j < kAreaBatch; j++) {
-      const int i = i0 + j * kTeamThreads;
-      vv[j] = i < nv ? leaf_vert(m, leaf, i) : -1;
+  for (int r0 = i0; r0 < i1; r0 += kAreaStage) {
+    const int r1 = min(i1, r0 + kAreaStage);
+    for (int i = r0 + t; i < r1; i += kTeamThreads) {
+      const int v = leaf_vert(m, leaf, i);
+      cp_async16(&s_co[i - r0], &m.co[v]);
+      cp_async16(&s_no[i - r0], &m.no[v]);
     }
-    float4 co[kAreaBatch], no[kAreaBatch];
-#pragma unroll
-    for (int j = 0; j < kAreaBatch; j++) {
-      if (vv[j] >= 0) {
-        co[j] = __ldcg(&m.co[vv[j]]);
-        no[j] = __ldcg(&m.no[vv[j]]);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < kAreaBatch; j++) {
-      if (vv[j] < 0) break;
-      const float d2 = dist_sq(co[j], pp.loc);
+    cp_async_wait_all();
+    __syncthreads();
+    for (int i = r0 + t; i < r1; i += kTeamThreads) {
+      const float4 co = s_co[i - r0];
+      const float d2 = dist_sq(co, pp.loc);
       if (d2 <= rn2) {
-        cs_add(l.v[0], no[j].x);
-        cs_add(l.v[1], no[j].y);
-        cs_add(l.v[2], no[j].z);
+        const float4 no = s_no[i - r0];
+        cs_add(l.v[0], no.x);
+        cs_add(l.v[1], no.y);
+        cs_add(l.v[2], no.z);
         l.n_no++;
       }
       if (d2 <= ra2) {
-        cs_add(l.v[3], co[j].x);
-        cs_add(l.v[4], co[j].y);
-        cs_add(l.v[5], co[j].z);
+        cs_add(l.v[3], co.x);
+        cs_add(l.v[4], co.y);
+        cs_add(l.v[5], co.z);
         l.n_co++;
       }
     }
+    __syncthreads();  // the stage is free for the next round
   }
   sl[t] = l;
   __syncthreads();
@@ -620,7 +622,7 @@ static __device__ void team_area_leaf(const DevMesh& m, const PassParams& pp, fl
 
 // Final pairwise tree over the leaf partials (i, i+s), s = 1, 2, 4, ... by one
 // CTA in shared memory; writes area normal and centre into sh.area.
-constexpr int kTeamMaxChunks = 64;  // culled leaves per pass <= 64 * 256
+constexpr int kTeamMaxChunks = 64;  // area partials per pass <= 64 * 256
 
 static __device__ void team_area_final(const DevMesh& m, const PassParams& pp, int cnt, Lane* sl,
                                 Lane* chunks, TeamShared& sh) {
@@ -679,6 +681,90 @@ __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+}
+
+// The faces of leaves that a dab marks join the dab's GRIDS normal update
+// (grid_claim_face, once per epoch): CTA r claims for the leaves k = r, r+C,
+// ... of list[0..n).  Called where the leaves are marked, so the claims
+// complete with the phase that marks them.
+__device__ __forceinline__ void team_claim_faces(const DevMesh& m, const int* list, int n,
+                                                 unsigned rank, unsigned C, unsigned int epoch) {
+  for (int k = static_cast<int>(rank); k < n; k += static_cast<int>(C)) {
+    const int leaf = list[k];
+    const int p0 = m.leaf_prim_off[leaf], p1 = m.leaf_prim_off[leaf + 1];
+    for (int j = p0 + threadIdx.x; j < p1; j += kTeamThreads)
+      grid_claim_face_only(m, m.leaf_prims[j], epoch);
+  }
+}
+
+// Grids of one face staged on chip at a time (positions and quad normals,
+// float3): the largest group of at most 4 grids whose tables fit in bytes.
+__host__ __device__ __forceinline__ int face_grid_group(int grid_size, size_t bytes) {
+  const size_t per = 12u * (static_cast<size_t>(grid_size) * grid_size +
+                            static_cast<size_t>(grid_size - 1) * (grid_size - 1));
+  const size_t g = bytes / per;
+  return g >= 4 ? 4 : static_cast<int>(g);
+}
+
+// Inner normals, face-internal seams and the centre of one claimed face by
+// one CTA (subdiv_ccg.c:670-740 and 951-984).  The face's grids are staged
+// in shared memory (positions, then the normal_quad of every quad, computed
+// once: the per-element form evaluates a quad up to four times with the same
+// corners and the same result); each element normal is the mean of its
+// staged quad normals, added in the order of grid_element_normal.  The seam
+// pairs and the centre follow a CTA barrier, as the reference averages after
+// every inner normal (the seams move positions the inner normals read).
+// Faces are independent here: a face's grids hold their own copies of the
+// base-edge elements, which the base-edge pass averages afterwards.
+static __device__ void team_grid_face(const DevMesh& m, int f, float3* s_co, float3* s_q,
+                                      int group) {
+  const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area, qa = g1 * g1;
+  const int s = m.face_start[f], n = m.face_ngrids[f];
+  for (int c0 = 0; c0 < n; c0 += group) {
+    const int nc = min(group, n - c0);
+    for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
+      const int c = i / area, e = i - c * area;
+      s_co[i] = xyz(__ldcg(&m.co[static_cast<size_t>(s + c0 + c) * area + e]));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nc * qa; i += kTeamThreads) {
+      const int c = i / qa, q = i - c * qa, qy = q / g1, qx = q - qy * g1;
+      const float3* p = s_co + c * area;
+      // quad (qx, qy): corners (qx, qy+1), (qx+1, qy+1), (qx+1, qy), (qx, qy)
+      s_q[i] = normal_quad(p[(qy + 1) * gs + qx], p[(qy + 1) * gs + qx + 1], p[qy * gs + qx + 1],
+                           p[qy * gs + qx]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
+      const int c = i / area, e = i - c * area, y = e / gs, x = e - y * gs;
+      const float3* q = s_q + c * qa;
+      float ax = 0.0f, ay = 0.0f, az = 0.0f;
+      int counter = 0;
+      auto add = [&](const float3& v) {
+        ax += v.x, ay += v.y, az += v.z;
+        counter++;
+      };
+      if (x < g1 && y < g1) add(q[y * g1 + x]);
+      if (x >= 1) {
+        if (y < g1) add(q[y * g1 + x - 1]);
+        if (y >= 1) add(q[(y - 1) * g1 + x - 1]);
+      }
+      if (y >= 1 && x < g1) add(q[(y - 1) * g1 + x]);
+      const float inv = 1.0f / (float)counter;
+      m.no[static_cast<size_t>(s + c0 + c) * area + e] = make_float4(ax * inv, ay * inv, az * inv, 0.0f);
+    }
+    __syncthreads();  // the normals are written; the staging tables are free again
+  }
+  const int pairs = n * g1;
+  for (int it = threadIdx.x; it <= pairs; it += kTeamThreads) {
+    if (it < pairs) {
+      const int c = it / g1, i = 1 + (it - c * g1);
+      const int g = s + c, prev = s + (c + n - 1) % n;
+      grid_avg_pair(m, prev * area + i, g * area + i * gs);
+    } else {
+      grid_average_set(m, n, [&](int c) { return (s + c) * area; });
+    }
+  }
 }
 
 // Team barrier.  A cluster team uses barrier.cluster (cluster.sync():
@@ -886,6 +972,9 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         const int f = __ldcg(&m.leaf_flag[leaf]);
         if (!(f & (kUpdateNormals | kUpdateBB))) continue;
         append(m.touch_list, &w->touch_count[0], leaf);
+        if (m.type == kGrids)  // the first dab's normal update takes its faces
+          for (int j = m.leaf_prim_off[leaf]; j < m.leaf_prim_off[leaf + 1]; j++)
+            grid_claim_face_only(m, m.leaf_prims[j], grid_epoch0 + 1u);
         if ((f & kUpdateNormals) && m.type == kFaces) {
           const int off = m.leaf_vert_off[leaf];
           for (int i = 0; i < m.leaf_uniq[leaf]; i++) {
@@ -912,6 +1001,8 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       const float r = b.radius * scale;
       int* tag_cnt = &w->tag_count[par];
       int* touch_cnt = &w->touch_count[par];
+      // GRIDS work-list stamp of this dab
+      const unsigned int epoch = grid_epoch0 + static_cast<unsigned int>(d) + 1u;
       if (kOrig && uses_original(tool)) {
         // grab / elastic deform: one gather over all passes, then each vertex
         // rebuilt from its stroke-start position (k_cull_dab, k_orig_dab)
@@ -945,6 +1036,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
             const int old = atomicOr(&m.leaf_flag[leaf], kMarkUpdate);
             if (!(old & kUpdateNormals)) append(m.touch_list, touch_cnt, leaf);
           }
+        if (m.type == kGrids) team_claim_faces(m, s_cl, cnt, rank, C, epoch);
         team_bytes(a, kPhBrush, team_orig_sweep(m, b, sh.dp, s_cl, s_coff, cnt, total, gt, GT, tag_cnt));
         TEAM_SYNC();
         clk.mark(a, rank, kPhBrush);
@@ -972,16 +1064,18 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           const float rn = b.radius * b.normal_radius_factor;
           const float ra = b.radius * b.area_radius_factor;
           unsigned long long ab = 0;
-          for (int k = rank; k < cnt; k += C) {
-            team_area_leaf(m, pp, rn * rn, ra * ra, s_cl[k], s_lanes, &m.parts[k]);
-            const int nv = leaf_nverts(m, s_cl[k]);
-            if (threadIdx.x < nv)
+          const int nb = m.area_blocks;
+          for (int k = rank; k < cnt * nb; k += C) {
+            const int leaf = s_cl[k / nb], blk = k % nb;
+            team_area_block(m, pp, rn * rn, ra * ra, leaf, blk, s_nbc, s_lanes, &m.parts[k]);
+            const int nv = min(leaf_nverts(m, leaf) - blk * kAreaBlock, kAreaBlock);
+            if (static_cast<int>(threadIdx.x) < nv)
               ab += ((m.type == kFaces ? 4ull : 0ull) + 24ull) *
                     ((nv - threadIdx.x + kTeamThreads - 1) / kTeamThreads);
           }
           team_bytes(a, kPhArea, ab);
           TEAM_SYNC();
-          team_area_final(m, pp, cnt, s_lanes, s_chunks, sh);
+          team_area_final(m, pp, cnt * nb, s_lanes, s_chunks, sh);
           for (int k = 0; k < 3; k++) {
             area_no[k] = sh.area[k];
             area_co[k] = sh.area[3 + k];
@@ -996,6 +1090,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
             const int old = atomicOr(&m.leaf_flag[leaf], kMarkUpdate);
             if (!(old & kUpdateNormals)) append(m.touch_list, touch_cnt, leaf);
           }
+        if (m.type == kGrids) team_claim_faces(m, s_cl, cnt, rank, C, epoch);
         if (tool != kToolSmooth) {
           unsigned long long ab = 0;
           const unsigned vbytes = (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) +
@@ -1174,33 +1269,44 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       unsigned long long ab = 0;
       FlushState fst;
       if (m.type == kGrids) {
-        // GRIDS: faces of the touched leaves, the inner normals of their
-        // grids, the face seams and centres, then the base edges and corners
-        // (positions move at the seams, so the refit below follows).
-        const unsigned int epoch = grid_epoch0 + static_cast<unsigned int>(d) + 1u;
-        for (int k = rank; k < ntouch; k += C) {
-          const int leaf = __ldcg(&m.touch_list[k]);
-          const int p0 = m.leaf_prim_off[leaf], p1 = m.leaf_prim_off[leaf + 1];
-          for (int j = p0 + threadIdx.x; j < p1; j += kTeamThreads) grid_claim_face(m, m.leaf_prims[j], epoch);
+        // GRIDS: the faces of the dab's leaves (claimed where the leaves were
+        // marked): inner normals, face seams and centres, one CTA per face;
+        // then the base edges and corners (positions move at the seams, so
+        // the refit below follows).
+        const int nf = __ldcg(&m.grid_counts[0]);
+        const int group = face_grid_group(m.grid_size, sizeof(float4) * kNbCache * kTeamThreads);
+        if (group > 0) {
+          float3* s_co = reinterpret_cast<float3*>(s_nbc);
+          float3* s_q = s_co + group * m.grid_area;
+          for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C)) {
+            const int f = __ldcg(&m.face_list[fi]);
+            team_grid_face(m, f, s_co, s_q, group);
+            if (threadIdx.x == 0) {
+              const int n = m.face_ngrids[f];
+              // positions read, normals written; the seam pairs and the
+              // centre read and write co, no and mask
+              ab += 24ull * n * m.grid_area + 112ull * n * (m.grid_size - 1) + 56ull * n;
+            }
+          }
+          TEAM_SYNC();
+        } else {
+          // grids too large to stage: one item per element, then the seams
+          const int ng = __ldcg(&m.grid_counts[3]);
+          const long long inner = (long long)ng * m.grid_area;
+          for (long long it = gt; it < inner; it += GT) {
+            grid_inner_item(m, it);
+            ab += 24u;  // co read, normal written
+          }
+          TEAM_SYNC();
+          const long long pairs = (long long)ng * (m.grid_size - 1);
+          for (long long it = gt; it < pairs + nf; it += GT) {
+            grid_face_seam_item(m, it, ng);
+            ab += it < pairs ? 112ull : 56ull * m.face_ngrids[__ldcg(&m.face_list[it - pairs])];
+          }
+          TEAM_SYNC();
         }
-        TEAM_SYNC();
-        const int nf = __ldcg(&m.grid_counts[0]), ng = __ldcg(&m.grid_counts[3]);
-        const long long inner = (long long)ng * m.grid_area;
-        for (long long it = gt; it < inner; it += GT) {
-          grid_inner_item(m, it);
-          ab += 24u;  // co read, normal written
-        }
-        TEAM_SYNC();
-        const long long pairs = (long long)ng * (m.grid_size - 1);
-        for (long long it = gt; it < pairs + nf; it += GT) {
-          grid_face_seam_item(m, it, ng);
-          // co, no and mask read and written per element
-          ab += it < pairs ? 112ull : 56ull * m.face_ngrids[__ldcg(&m.face_list[it - pairs])];
-        }
-        TEAM_SYNC();
-        const int ne = __ldcg(&m.grid_counts[1]), nv = __ldcg(&m.grid_counts[2]);
-        const long long items = (long long)ne * (2 * m.grid_size - 2) + nv;
-        for (long long it = gt; it < items; it += GT) grid_seam_item(m, it, ne);
+        const long long items = (long long)nf * m.max_face_corners * (2 * m.grid_size - 1);
+        for (long long it = gt; it < items; it += GT) grid_owner_seam_item(m, it, epoch);
         TEAM_SYNC();
         if (rank == 0 && threadIdx.x == 0)
           m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = m.grid_counts[3] = 0;
