@@ -139,7 +139,7 @@ struct sgpu_mesh {
   bool ray_configured = false;
   // the captured call (copies in, kernels, copies out) for (rays, original)
   cudaGraphExec_t ray_graph = nullptr;
-  int ray_graph_n = -1, ray_graph_orig = -1;
+  int ray_graph_n = -1, ray_graph_orig = -1, ray_graph_near = -1;
   // stroke-start positions and normals stored (grab, elastic deform)
   bool orig_stored = false;
   // headless draw buffers (sgpu_draw_buffers_build): host layout, device view
@@ -821,6 +821,11 @@ int stroke_host_run(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* da
   }
   return SGPU_OK;
 }
+
+int ray_query(sgpu_mesh* mesh, int nrays, const float* ray_starts, const float* ray_normals,
+              const float* ray_lengths, int original, bool nearest, float* r_depths, int* r_hits,
+              int* r_active_vertices, int* r_active_faces, float* r_face_normals,
+              float* r_dist_sq);
 
 }  // namespace
 
@@ -2313,13 +2318,14 @@ int ensure_ray_buffers(sgpu_mesh* m, int n) {
   return SGPU_OK;
 }
 
-}  // namespace
 
-extern "C" {
-
-int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const float* ray_normals,
-                 const float* ray_lengths, int original, float* r_depths, int* r_hits,
-                 int* r_active_vertices, int* r_active_faces, float* r_face_normals) {
+// One batch of independent ray queries through the cached graph of its shape
+// (rays, original, mode): the ray cast (nearest = false) or the nearest-to-ray
+// query (starting squared distance FLT_MAX; r_dist_sq receives the result).
+int ray_query(sgpu_mesh* mesh, int nrays, const float* ray_starts, const float* ray_normals,
+              const float* ray_lengths, int original, bool nearest, float* r_depths, int* r_hits,
+              int* r_active_vertices, int* r_active_faces, float* r_face_normals,
+              float* r_dist_sq) {
   int rc = check_mesh(mesh);
   if (rc) return rc;
   if (nrays < 0) return fail(SGPU_ERR_INVALID_ARG, "negative ray count");
@@ -2343,7 +2349,8 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
     hin[6 * static_cast<size_t>(nrays) + r] = ray_lengths ? ray_lengths[r] : FLT_MAX;
   }
   cudaStream_t s = mesh->stream;
-  if (!mesh->ray_graph || mesh->ray_graph_n != nrays || mesh->ray_graph_orig != original) {
+  if (!mesh->ray_graph || mesh->ray_graph_n != nrays || mesh->ray_graph_orig != original ||
+      mesh->ray_graph_near != static_cast<int>(nearest)) {
     if (mesh->ray_graph) cudaGraphExecDestroy(mesh->ray_graph);
     mesh->ray_graph = nullptr;
     RayBatch rb = mesh->ray;
@@ -2353,6 +2360,7 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
     rb.rays = din;
     rb.depth_in = din + 6 * static_cast<size_t>(nrays);
     rb.original = original;
+    rb.nearest = nearest ? 1 : 0;
     rb.n2o = mesh->d_n2o;
     // small batches (an interactive cursor ray) in one round: the second
     // round's launches cost more latency than its saved work
@@ -2383,18 +2391,19 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
     if (graph) cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
       mesh->ray_graph = nullptr;
-      return cuda_fail(e, "ray-cast graph");
+      return cuda_fail(e, "ray-query graph");
     }
     mesh->ray_graph_n = nrays;
     mesh->ray_graph_orig = original;
+    mesh->ray_graph_near = static_cast<int>(nearest);
   }
-  CK(cudaGraphLaunch(mesh->ray_graph, s), "ray-cast graph launch");
+  CK(cudaGraphLaunch(mesh->ray_graph, s), "ray-query graph launch");
   CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   const int err = *reinterpret_cast<int*>(mesh->ray_host + lay.err);
   if (err) {
     CK(cudaMemsetAsync(&d.work->err, 0, sizeof(int), s), "reset error word");
     CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    return fail(err, "a ray-cast kernel reported error code %d", err);
+    return fail(err, "a ray-query kernel reported error code %d", err);
   }
   const float* fo = reinterpret_cast<const float*>(mesh->ray_host + lay.out_f);
   const int* io = reinterpret_cast<const int*>(mesh->ray_host + lay.out_i);
@@ -2405,8 +2414,28 @@ int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const floa
     if (r_active_faces) r_active_faces[r] = io[2 * static_cast<size_t>(nrays) + r];
     if (r_face_normals)
       for (int k = 0; k < 3; k++) r_face_normals[3 * r + k] = fo[nrays + 3 * static_cast<size_t>(r) + k];
+    if (r_dist_sq) r_dist_sq[r] = fo[nrays + 3 * static_cast<size_t>(r)];
   }
   return SGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgpu_raycast(sgpu_mesh* mesh, int nrays, const float* ray_starts, const float* ray_normals,
+                 const float* ray_lengths, int original, float* r_depths, int* r_hits,
+                 int* r_active_vertices, int* r_active_faces, float* r_face_normals) {
+  return ray_query(mesh, nrays, ray_starts, ray_normals, ray_lengths, original, false, r_depths,
+                   r_hits, r_active_vertices, r_active_faces, r_face_normals, nullptr);
+}
+
+int sgpu_find_nearest_to_ray(sgpu_mesh* mesh, int nrays, const float* ray_starts,
+                             const float* ray_normals, int original, float* r_depths,
+                             float* r_dist_sq, int* r_hits) {
+  if (nrays > 0 && !r_dist_sq) return fail(SGPU_ERR_INVALID_ARG, "NULL result array");
+  return ray_query(mesh, nrays, ray_starts, ray_normals, nullptr, original, true, r_depths, r_hits,
+                   nullptr, nullptr, nullptr, r_dist_sq);
 }
 
 }  // extern "C"

@@ -34,6 +34,22 @@
 // k_ray_tris flags such a leaf; k_ray_finish replays a flagged leaf quad by
 // quad in order (256 quads at a time, their tests in parallel, the rule
 // sequentially), and every other leaf by its minimum key.
+//
+// The same kernels (kNear) answer BKE_pbvh_find_nearest_to_ray (pbvh.c:
+// 4339-4352) with the sculpt callback of the brush specification: the node
+// test is nearest_to_ray_aabb_dist_sq (pbvh.c:4315-4337: tmin = the squared
+// distance of the box from the ray, dist_squared_ray_to_aabb_v3; the node
+// passes when the depth of that nearest point is positive), a leaf is
+// searched when its tmin is below the running minimum squared distance, and
+// inside it a triangle is taken when its squared distance
+// (dist_squared_ray_to_tri_v3_fast, pbvh.c:3970-3989) is strictly below the
+// current one.  FACES leaves reduce to their minimum key (squared distance in
+// an order-preserving encoding, prim position).  In a GRIDS leaf
+// (ray_face_nearest_quad, pbvh.c:3991-4017) the second triangle of a quad is
+// tested only when the first was taken, which depends on the running value,
+// so every GRIDS leaf is replayed quad by quad; a chunk's quads whose first
+// triangle is not below the value at the chunk's start can never be taken
+// and are skipped.
 #include <cuda_runtime.h>
 
 #include "sgpu_device.cuh"
@@ -144,6 +160,157 @@ __device__ __forceinline__ unsigned long long depth_key(float depth, int pos) {
   return (static_cast<unsigned long long>(bits) << 32) | static_cast<unsigned int>(pos);
 }
 
+// Nearest-to-ray distances (math_geom.cc), the reference's FP32 operations.
+// dist_squared_ray_to_aabb_v3_precalc (:643-655).
+struct RayAabb {
+  float org[3], dir[3], inv[3];
+};
+
+__device__ __forceinline__ void rayaabb_init(RayAabb& r, const float* o, const float* d) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    r.org[i] = o[i];
+    r.dir[i] = d[i];
+    r.inv[i] = (d[i] != 0.0f) ? (1.0f / d[i]) : FLT_MAX;
+  }
+}
+
+__device__ __forceinline__ float dot3(const float* a, const float* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+__device__ __forceinline__ void cross3(float* r, const float* a, const float* b) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// dist_squared_ray_to_seg_v3 (:574-608) with isect_ray_line_v3 (:1997-2021)
+// and interp_v3_v3v3 (math_vector.c:24-31): squared distance of the segment
+// point the line parameter selects (clamped; v0 for a parallel segment) from
+// the ray, and its depth.
+__device__ float ray_seg_dist_sq(const float* o, const float* dir, const float* v0,
+                                 const float* v1, float* r_depth) {
+  const float a[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+  const float t[3] = {v0[0] - o[0], v0[1] - o[1], v0[2] - o[2]};
+  float n[3];
+  cross3(n, a, dir);
+  const float nlen = dot3(n, n);
+  float p[3] = {v0[0], v0[1], v0[2]};
+  if (nlen != 0.0f) {
+    const float c[3] = {n[0] - t[0], n[1] - t[1], n[2] - t[2]};
+    float cray[3];
+    cross3(cray, c, dir);
+    const float lambda = dot3(cray, n) / nlen;
+    if (lambda <= 0.0f) {
+      // v0
+    } else if (lambda >= 1.0f) {
+      p[0] = v1[0], p[1] = v1[1], p[2] = v1[2];
+    } else {
+      const float sl = 1.0f - lambda;
+      p[0] = sl * v0[0] + lambda * v1[0];
+      p[1] = sl * v0[1] + lambda * v1[1];
+      p[2] = sl * v0[2] + lambda * v1[2];
+    }
+  }
+  const float dvec[3] = {p[0] - o[0], p[1] - o[1], p[2] - o[2]};
+  const float depth = dot3(dvec, dir);
+  *r_depth = depth;
+  return dot3(dvec, dvec) - depth * depth;
+}
+
+// dist_squared_ray_to_tri_v3_fast (pbvh.c:3970-3989): the edges (v0, v2),
+// (v1, v0), (v2, v1); the first, then any strictly nearer one.
+__device__ float ray_tri_dist_sq(const float* o, const float* dir, float3 v0, float3 v1, float3 v2,
+                                 float* r_depth) {
+  const float tri[3][3] = {{v0.x, v0.y, v0.z}, {v1.x, v1.y, v1.z}, {v2.x, v2.y, v2.z}};
+  float best = FLT_MAX;
+  for (int i = 0, j = 2; i < 3; j = i++) {
+    float dt = FLT_MAX;
+    const float dd = ray_seg_dist_sq(o, dir, tri[i], tri[j], &dt);
+    if (dd < best || i == 0) {
+      *r_depth = dt;
+      best = dd;
+    }
+  }
+  return best;
+}
+
+// dist_squared_ray_to_aabb_v3 (:657-744) with aabb_get_near_far_from_plane
+// (:610-641): 0 when the ray line meets the box (depth of the far corner),
+// else the squared distance of the box edge nearest the ray.
+__device__ float rayaabb_dist_sq(const RayAabb& r, float4 mn, float4 mx, float* r_depth) {
+  const float bmin[3] = {mn.x, mn.y, mn.z}, bmax[3] = {mx.x, mx.y, mx.z};
+  float lo[3], hi[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const bool neg = r.dir[k] < 0.0f;
+    lo[k] = neg ? bmax[k] : bmin[k];
+    hi[k] = neg ? bmin[k] : bmax[k];
+  }
+  const float tmin[3] = {(lo[0] - r.org[0]) * r.inv[0], (lo[1] - r.org[1]) * r.inv[1],
+                         (lo[2] - r.org[2]) * r.inv[2]};
+  const float tmax[3] = {(hi[0] - r.org[0]) * r.inv[0], (hi[1] - r.org[1]) * r.inv[1],
+                         (hi[2] - r.org[2]) * r.inv[2]};
+  float va[3] = {0.0f, 0.0f, 0.0f}, vb[3] = {0.0f, 0.0f, 0.0f};
+  float rtmin, rtmax;
+  int axis;
+  if ((tmax[0] <= tmax[1]) && (tmax[0] <= tmax[2])) {
+    rtmax = tmax[0];
+    va[0] = vb[0] = hi[0];
+    axis = 3;
+  } else if ((tmax[1] <= tmax[0]) && (tmax[1] <= tmax[2])) {
+    rtmax = tmax[1];
+    va[1] = vb[1] = hi[1];
+    axis = 2;
+  } else {
+    rtmax = tmax[2];
+    va[2] = vb[2] = hi[2];
+    axis = 1;
+  }
+  if ((tmin[0] >= tmin[1]) && (tmin[0] >= tmin[2])) {
+    rtmin = tmin[0];
+    va[0] = vb[0] = lo[0];
+    axis -= 3;
+  } else if ((tmin[1] >= tmin[0]) && (tmin[1] >= tmin[2])) {
+    rtmin = tmin[1];
+    va[1] = vb[1] = lo[1];
+    axis -= 1;
+  } else {
+    rtmin = tmin[2];
+    va[2] = vb[2] = lo[2];
+    axis -= 2;
+  }
+  if (axis < 0) axis += 3;
+  if (rtmin <= rtmax) {
+    const float dvec[3] = {hi[0] - r.org[0], hi[1] - r.org[1], hi[2] - r.org[2]};
+    *r_depth = dot3(dvec, r.dir);
+    return 0.0f;
+  }
+  if (r.dir[axis] >= 0.0f) {
+    va[axis] = lo[axis];
+    vb[axis] = hi[axis];
+  } else {
+    va[axis] = hi[axis];
+    vb[axis] = lo[axis];
+  }
+  return ray_seg_dist_sq(r.org, r.dir, va, vb, r_depth);
+}
+
+// Key of a squared distance (any sign; NaN has none): the float order as an
+// unsigned order, -0 as +0 (they compare equal), then the prim position.
+__device__ __forceinline__ unsigned long long dist_key(float dist, int pos) {
+  unsigned int bits = __float_as_uint(dist);
+  if (bits == 0x80000000u) bits = 0u;
+  bits = (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
+  return (static_cast<unsigned long long>(bits) << 32) | static_cast<unsigned int>(pos);
+}
+__device__ __forceinline__ float key_dist(unsigned long long key) {
+  unsigned int bits = static_cast<unsigned int>(key >> 32);
+  bits = (bits & 0x80000000u) ? (bits & 0x7fffffffu) : ~bits;
+  return __uint_as_float(bits);
+}
+
 __device__ __forceinline__ float len_sq(float3 a, float3 b) {
   const float d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z;
   return d0 * d0 + d1 * d1 + d2 * d2;
@@ -207,6 +374,7 @@ __device__ int ray_block_scan(int v, int* total, int* smem32) {
 
 // Dynamic shared memory: node pass flags (char), node tmin and parents (4 B
 // each), listed leaves' tmin (float).
+template <bool kNear>
 __global__ void __launch_bounds__(kRayThreads) k_ray_leaves(DevMesh m, RayBatch rb) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int scan[32];
@@ -223,14 +391,27 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_leaves(DevMesh m, RayBatch 
     o[k] = rb.rays[6 * ray + k];
     d[k] = rb.rays[6 * ray + 3 + k];
   }
-  RayBox box;
-  raybox_init(box, o, d);
   const float4* bb = rb.original ? m.orig_vb : m.vb;
-  for (int n = threadIdx.x; n < N; n += kRayThreads) {
-    float t = 0.0f;
-    s_pass[n] = raybox_hit(box, __ldcg(&bb[2 * n]), __ldcg(&bb[2 * n + 1]), &t);
-    s_t[n] = t;
-    s_par[n] = m.node_parent[n];
+  if constexpr (kNear) {
+    // nearest_to_ray_aabb_dist_sq: tmin = squared distance, pass when the
+    // nearest point's depth is positive
+    RayAabb ra;
+    rayaabb_init(ra, o, d);
+    for (int n = threadIdx.x; n < N; n += kRayThreads) {
+      float dep = 0.0f;
+      s_t[n] = rayaabb_dist_sq(ra, __ldcg(&bb[2 * n]), __ldcg(&bb[2 * n + 1]), &dep);
+      s_pass[n] = dep > 0.0f;
+      s_par[n] = m.node_parent[n];
+    }
+  } else {
+    RayBox box;
+    raybox_init(box, o, d);
+    for (int n = threadIdx.x; n < N; n += kRayThreads) {
+      float t = 0.0f;
+      s_pass[n] = raybox_hit(box, __ldcg(&bb[2 * n]), __ldcg(&bb[2 * n + 1]), &t);
+      s_t[n] = t;
+      s_par[n] = m.node_parent[n];
+    }
   }
   __syncthreads();
   // pbvh_iter_next_occluded: a leaf is listed when it and all its ancestors
@@ -300,6 +481,7 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_leaves(DevMesh m, RayBatch 
   }
 }
 
+template <bool kNear>
 __global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb, int round) {
   __shared__ unsigned long long s_min[kRayThreads / 32];
   const int L = m.nleaf;
@@ -317,7 +499,17 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_tris(DevMesh m, RayBatch rb
     const int leaf = rb.slot_leaf[item.x];
     const int pos = item.y * kRayChunk + static_cast<int>(threadIdx.x);
     unsigned long long key = kNoKey;
-    if (pos < leaf_units(m, leaf)) {
+    if (kNear && pos < leaf_units(m, leaf)) {
+      if (m.type == kFaces) {
+        const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + pos]];
+        float dt;
+        const float dd = ray_tri_dist_sq(o, d, xyz(__ldcg(&m.co[tv.x])), xyz(__ldcg(&m.co[tv.y])),
+                                         xyz(__ldcg(&m.co[tv.z])), &dt);
+        if (!isnan(dd)) key = dist_key(dd, pos);
+      } else if (pos == 0) {
+        rb.slot_special[item.x] = 1;  // GRIDS: every leaf is replayed in order
+      }
+    } else if (pos < leaf_units(m, leaf)) {
       RayTri rt;
       raytri_init(rt, d);
       if (m.type == kFaces) {
@@ -420,11 +612,41 @@ __device__ void ray_write_result(const DevMesh& m, const RayBatch& rb, int ray, 
   rb.face_normal[3 * ray + 2] = fn[2];
 }
 
+// The nearest query's result: the winning triangle's squared distance and
+// depth recomputed exactly (dist_squared_ray_to_tri_v3_fast; -0 kept); the
+// squared distance goes to face_normal[3 * ray], no active vertex or face.
+__device__ void ray_write_near(const DevMesh& m, const RayBatch& rb, int ray, const float* o,
+                               const float* d, float dist_sq, int win_slot, int win_pos,
+                               int win_tri) {
+  float depth = FLT_MAX;
+  if (win_slot >= 0) {
+    const int leaf = rb.slot_leaf[static_cast<size_t>(ray) * m.nleaf + win_slot];
+    if (m.type == kFaces) {
+      const int4 tv = m.lt_v4[m.leaf_prims[m.leaf_prim_off[leaf] + win_pos]];
+      dist_sq = ray_tri_dist_sq(o, d, xyz(__ldcg(&m.co[tv.x])), xyz(__ldcg(&m.co[tv.y])),
+                                xyz(__ldcg(&m.co[tv.z])), &depth);
+    } else {
+      const GridQuad q = grid_quad(m, leaf, win_pos);
+      dist_sq = win_tri == 0 ? ray_tri_dist_sq(o, d, q.c[0], q.c[1], q.c[2], &depth)
+                             : ray_tri_dist_sq(o, d, q.c[0], q.c[2], q.c[3], &depth);
+    }
+  }
+  rb.depth_out[ray] = depth;
+  rb.hit[ray] = win_slot >= 0;
+  rb.active_vertex[ray] = -1;
+  rb.active_face[ray] = -1;
+  rb.face_normal[3 * ray] = dist_sq;
+  rb.face_normal[3 * ray + 1] = 0.0f;
+  rb.face_normal[3 * ray + 2] = 0.0f;
+}
+
 // One CTA per ray.  Round 0 walks the first first_leaves leaves in entry
 // order, then either settles the ray (its next leaf would not be cast) or
 // saves the state and lists the remaining leaves' work items; round 1 walks
 // those for the unsettled rays.  Dynamic shared memory: per listed leaf its
 // order entry, tmin and key.
+// kNear: s_depth is the running squared distance, keys decode with key_dist.
+template <bool kNear>
 __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch rb, int round) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float s_da[kRayThreads], s_db[kRayThreads];
@@ -491,7 +713,7 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
         if (!(s_tmin[sl] < run_tmin)) continue;
         const unsigned long long key = s_key[sl];
         if (key == kNoKey) continue;
-        const float dmin = __uint_as_float(static_cast<unsigned int>(key >> 32));
+        const float dmin = kNear ? key_dist(key) : __uint_as_float(static_cast<unsigned int>(key >> 32));
         if (dmin < depth) {
           depth = dmin;
           win_slot = sl;
@@ -525,7 +747,7 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
       if (threadIdx.x == 0) {
         const unsigned long long key = s_key[sl];
         if (key != kNoKey) {
-          const float dmin = __uint_as_float(static_cast<unsigned int>(key >> 32));
+          const float dmin = kNear ? key_dist(key) : __uint_as_float(static_cast<unsigned int>(key >> 32));
           if (dmin < s_depth) {
             s_depth = dmin;
             s_win_slot = sl;
@@ -537,9 +759,49 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
       }
       continue;
     }
-    // GRIDS leaf with a folded quad: ray_face_intersection_quad quad by quad
     const int leaf = rb.slot_leaf[base + sl];
     const int units = leaf_units(m, leaf);
+    if constexpr (kNear) {
+      // GRIDS: ray_face_nearest_quad quad by quad; quads whose first triangle
+      // is not below the value at the chunk's start are never taken
+      for (int c0 = 0; c0 < units; c0 += kRayThreads) {
+        const int u = c0 + static_cast<int>(threadIdx.x);
+        float d1 = FLT_MAX, d2 = FLT_MAX, dep = 0.0f;
+        if (u < units) {
+          const GridQuad q = grid_quad(m, leaf, u);
+          d1 = ray_tri_dist_sq(o, d, q.c[0], q.c[1], q.c[2], &dep);
+          d2 = ray_tri_dist_sq(o, d, q.c[0], q.c[2], q.c[3], &dep);
+        }
+        s_da[threadIdx.x] = d1;
+        s_db[threadIdx.x] = d2;
+        const unsigned bal = __ballot_sync(0xffffffffu, u < units && d1 < s_depth);
+        if ((threadIdx.x & 31) == 0) s_mask[threadIdx.x >> 5] = bal;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          float cur = s_depth;
+          for (int w = 0; w < kRayThreads / 32; w++) {
+            for (unsigned b = s_mask[w]; b; b &= b - 1) {
+              const int t = 32 * w + __ffs(static_cast<int>(b)) - 1;
+              if (!(s_da[t] < cur)) continue;
+              cur = s_da[t];
+              s_win_tri = 0;
+              if (s_db[t] < cur) {
+                cur = s_db[t];
+                s_win_tri = 1;
+              }
+              s_win_slot = sl;
+              s_win_pos = c0 + t;
+              s_leaf_hit = 1;
+            }
+          }
+          s_depth = cur;
+        }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0 && s_leaf_hit) s_run_tmin = s_depth;
+      continue;
+    }
+    // GRIDS leaf with a folded quad: ray_face_intersection_quad quad by quad
     for (int c0 = 0; c0 < units; c0 += kRayThreads) {
       const int u = c0 + static_cast<int>(threadIdx.x);
       bool ha = false, hb = false;
@@ -612,7 +874,11 @@ __global__ void __launch_bounds__(kRayThreads) k_ray_finish(DevMesh m, RayBatch 
   }
   if (threadIdx.x != 0) return;
   if (round == 0) rb.st_win[ray] = make_int4(-1, -1, -1, -1);  // settled
-  ray_write_result(m, rb, ray, o, d, rt, s_depth, s_win_slot, s_win_pos, s_win_tri);
+  if constexpr (kNear) {
+    ray_write_near(m, rb, ray, o, d, s_depth, s_win_slot, s_win_pos, s_win_tri);
+  } else {
+    ray_write_result(m, rb, ray, o, d, rt, s_depth, s_win_slot, s_win_pos, s_win_tri);
+  }
 }
 
 }  // namespace
@@ -631,32 +897,46 @@ int ray_items_per_ray(const DevMesh& m) {
   return static_cast<int>(units / kRayChunk) + m.nleaf;
 }
 
-cudaError_t configure_ray_kernels(size_t leaves_smem, size_t finish_smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_ray_leaves, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <bool kNear>
+static cudaError_t configure_ray_mode(size_t leaves_smem, size_t finish_smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_ray_leaves<kNear>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(leaves_smem));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_ray_finish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_ray_finish<kNear>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(finish_smem));
 }
 
-cudaError_t launch_raycast(const DevMesh& m, const RayBatch& rb, int nrays, int tris_grid,
-                           cudaStream_t s) {
+cudaError_t configure_ray_kernels(size_t leaves_smem, size_t finish_smem) {
+  const cudaError_t e = configure_ray_mode<false>(leaves_smem, finish_smem);
+  return e != cudaSuccess ? e : configure_ray_mode<true>(leaves_smem, finish_smem);
+}
+
+template <bool kNear>
+static cudaError_t launch_ray_mode(const DevMesh& m, const RayBatch& rb, int nrays, int tris_grid,
+                                   cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(rb.nitems, 0, sizeof(int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(rb.nitems2, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  k_ray_leaves<<<nrays, kRayThreads, ray_leaves_smem(m), s>>>(m, rb);
+  k_ray_leaves<kNear><<<nrays, kRayThreads, ray_leaves_smem(m), s>>>(m, rb);
   // every leaf in round 0 settles every ray there: no second round
   const int rounds = rb.first_leaves >= m.nleaf ? 1 : 2;
   for (int round = 0; round < rounds && e == cudaSuccess; round++) {
     e = cudaGetLastError();
     if (e != cudaSuccess) break;
-    k_ray_tris<<<tris_grid, kRayThreads, 0, s>>>(m, rb, round);
+    k_ray_tris<kNear><<<tris_grid, kRayThreads, 0, s>>>(m, rb, round);
     e = cudaGetLastError();
     if (e != cudaSuccess) break;
-    k_ray_finish<<<nrays, kRayThreads, ray_finish_smem(m), s>>>(m, rb, round);
+    k_ray_finish<kNear><<<nrays, kRayThreads, ray_finish_smem(m), s>>>(m, rb, round);
   }
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+
+cudaError_t launch_raycast(const DevMesh& m, const RayBatch& rb, int nrays, int tris_grid,
+                           cudaStream_t s) {
+  return rb.nearest ? launch_ray_mode<true>(m, rb, nrays, tris_grid, s)
+                    : launch_ray_mode<false>(m, rb, nrays, tris_grid, s);
 }
 
 }  // namespace sgpu

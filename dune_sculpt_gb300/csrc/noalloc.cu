@@ -45,12 +45,22 @@ int noalloc_fail(int code, const std::string& msg) {
 
 // The device address of the scratch array on the current device, looked up
 // once per device (host code cannot use the symbol's name as an address).
+// A device reset ends the context that held the array, so a cached address
+// that the runtime no longer knows as device memory is looked up again.
 int scratch_for_device(float4** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(SGPU_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(SGPU_ERR_UNSUPPORTED, "device index");
   std::lock_guard<std::mutex> lock(g_mu);
+  if (g_scratch_addr[dev]) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, g_scratch_addr[dev]) != cudaSuccess ||
+        attr.type != cudaMemoryTypeDevice || attr.device != dev) {
+      cudaGetLastError();  // a failed query leaves no sticky error
+      g_scratch_addr[dev] = nullptr;
+    }
+  }
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);

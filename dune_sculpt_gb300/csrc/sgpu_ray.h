@@ -11,6 +11,7 @@ struct RayBatch {
   const float* rays;      // 6 per ray: start xyz, unit direction xyz
   const float* depth_in;  // per ray: ray length (nullable: FLT_MAX)
   int original;           // boxes from orig_vb instead of vb
+  int nearest;            // the nearest-to-ray query (depth_in: starting squared distance)
   const int* n2o;         // device -> caller vertex numbering (nullable: identity)
   // per ray and listed leaf (nleaf slots per ray)
   int* count;

@@ -48,6 +48,8 @@ enum TeamPhase {
   kPhUpdate,
   kPhFlush,
   kPhJob,
+  kPhGridFaces,  // GRIDS: inner normals, face seams and centres
+  kPhGridSeams,  // GRIDS: base edges and corners
   kTeamPhases
 };
 

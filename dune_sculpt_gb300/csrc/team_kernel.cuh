@@ -770,10 +770,11 @@ static __device__ void team_grid_face(const DevMesh& m, int f, float3* s_co, flo
 // Team barrier.  A cluster team uses barrier.cluster (cluster.sync():
 // arrive.release, wait.acquire).  The whole-GPU team (every CTA of a
 // cooperative launch, so all of them are resident) counts arrivals in global
-// memory: after a CTA barrier, thread 0 adds one to the counter with release
-// semantics and waits until it reaches the CTA count times the barrier's
-// ordinal, then fences with acquire semantics before the CTA barrier that
-// lets its threads go on.  The wait is bounded by a time limit and an
+// memory: after a CTA barrier, thread 0 adds one to the counter (acquire and
+// release semantics) and polls it with acquire loads until it reaches the CTA
+// count times the barrier's ordinal, before the CTA barrier that lets its
+// threads go on (the adds form one release sequence, so the load or add that
+// sees the full count synchronizes with every CTA's arrival).  The wait is bounded by a time limit and an
 // iteration cap; a CTA that gives up records SGPU_ERR_TIMEOUT in *status and
 // sets the counter's abort bit, and every CTA that sees the bit returns false
 // (the kernel then leaves).  extra: arrivals the barrier waits for beyond the
@@ -781,9 +782,9 @@ static __device__ void team_grid_face(const DevMesh& m, int f, float3* s_co, flo
 // runs out).
 constexpr unsigned int kBarAbort = 0x80000000u;
 
-__device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
   unsigned int v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
@@ -810,7 +811,7 @@ struct TeamBarrier {
       target += C + extra;
       if (threadIdx.x == 0) {
         unsigned int v;
-        asm volatile("atom.release.gpu.global.add.u32 %0, [%1], 1;"
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
                      : "=r"(v)
                      : "l"(count)
                      : "memory");
@@ -834,9 +835,8 @@ struct TeamBarrier {
               break;
             }
           }
-          v = ld_relaxed_gpu(count);
+          v = ld_acquire_gpu(count);
         }
-        asm volatile("fence.acq_rel.gpu;" ::: "memory");
         *s_ok = ok;
       }
       __syncthreads();
@@ -1288,7 +1288,10 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
               ab += 24ull * n * m.grid_area + 112ull * n * (m.grid_size - 1) + 56ull * n;
             }
           }
+          team_bytes(a, kPhGridFaces, ab);
+          ab = 0;
           TEAM_SYNC();
+          clk.mark(a, rank, kPhGridFaces);
         } else {
           // grids too large to stage: one item per element, then the seams
           const int ng = __ldcg(&m.grid_counts[3]);
@@ -1308,6 +1311,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         const long long items = (long long)nf * m.max_face_corners * (2 * m.grid_size - 1);
         for (long long it = gt; it < items; it += GT) grid_owner_seam_item(m, it, epoch);
         TEAM_SYNC();
+        clk.mark(a, rank, kPhGridSeams);
         if (rank == 0 && threadIdx.x == 0)
           m.grid_counts[0] = m.grid_counts[1] = m.grid_counts[2] = m.grid_counts[3] = 0;
       }

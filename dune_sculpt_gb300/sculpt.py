@@ -68,12 +68,13 @@ class SGPU_KernelProfile(C.Structure):
                 ("alg_bytes", C.c_double)]
 
 
-TEAM_PHASES = ("search", "area", "brush", "smooth_apply", "normals_refit", "flush", "job")
+TEAM_PHASES = ("search", "area", "brush", "smooth_apply", "normals_refit", "flush", "job",
+               "grid_faces", "grid_seams")
 
 
 class SGPU_TeamProfile(C.Structure):
-    _fields_ = [("total_ms", C.c_float), ("phase_ms", C.c_double * 7),
-                ("phase_bytes", C.c_double * 7)]
+    _fields_ = [("total_ms", C.c_float), ("phase_ms", C.c_double * 9),
+                ("phase_bytes", C.c_double * 9)]
 
 
 # Every exported symbol, as declared in include/sculpt_gpu.h.
@@ -95,6 +96,7 @@ EXPORTS = (
     "sgpu_draw_buffers_layout", "sgpu_draw_buffers_overlay", "sgpu_draw_buffers_get",
     "sgpu_draw_buffers_device", "sgpu_draw_buffers_update_timed", "sgpu_debug_inject",
     "sgpu_calc_area_normal_and_center", "sgpu_stroke_host_grids", "sgpu_autotune_batch",
+    "sgpu_find_nearest_to_ray",
 )
 
 DRAW_STRIDE = 36  # SGPU_DRAW_STRIDE
@@ -172,6 +174,7 @@ def load(path: str | None = None):
     L.sgpu_autotune_team.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp]
     L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
     L.sgpu_autotune_batch.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp]
+    L.sgpu_find_nearest_to_ray.argtypes = [vp, i, vp, vp, i, vp, vp, vp]
     L.sgpu_mesh_store_original.argtypes = [vp]
     L.sgpu_debug_inject.argtypes = [i, C.c_int64]
     L.sgpu_calc_area_normal_and_center.argtypes = [vp, C.POINTER(SGPU_Brush), vp, vp, i, vp, vp]
@@ -396,6 +399,20 @@ class PBVH:
         _check(load().sgpu_raycast(self._h, n, _p(o), _p(d), _p(ln), original, _p(dep), _p(hit),
                                    _p(av), _p(af), _p(fn)))
         return hit.astype(bool), dep, av, af, fn
+
+    def nearest_to_ray(self, starts, normals, original: int = 0):
+        """BKE_pbvh_find_nearest_to_ray with the sculpt callback for a batch of
+        rays.  Returns (hit bool[n], depth float32[n], squared distance
+        float32[n])."""
+        o = np.ascontiguousarray(starts, dtype=np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        n = o.shape[0]
+        dep = np.zeros(n, dtype=np.float32)
+        dsq = np.zeros(n, dtype=np.float32)
+        hit = np.zeros(n, dtype=np.int32)
+        _check(load().sgpu_find_nearest_to_ray(self._h, n, _p(o), _p(d), original, _p(dep),
+                                               _p(dsq), _p(hit)))
+        return hit.astype(bool), dep, dsq
 
     # -- headless draw buffers (GPU_pbvh_*_buffers_build / _update)
     def draw_buffers_build(self, face_sets=None, seed: int = 0, color_default: int = 1,

@@ -311,8 +311,10 @@ int sgpu_autotune_batch(sgpu_mesh **meshes, int nmesh, const SGPU_Brush *brushes
  * that ends it) and the algorithmic bytes each phase moved.  Phases: 0 node
  * search, 1 area normal/centre, 2 brush sweep (smooth: candidate test and
  * first sweep), 3 smooth sweeps after the first, 4 normals and leaf refit,
- * 5 ancestor flush, 6 job set-up and end-of-stroke bounds. */
-#define SGPU_TEAM_PHASES 7
+ * 5 ancestor flush, 6 job set-up and end-of-stroke bounds, 7 GRIDS inner
+ * normals with face seams and centres, 8 GRIDS base edges and corners
+ * (phase 4 holds the refit of GRIDS meshes). */
+#define SGPU_TEAM_PHASES 9
 typedef struct SGPU_TeamProfile {
   float total_ms; /* CUDA-event time of the launch */
   double phase_ms[SGPU_TEAM_PHASES];
@@ -342,6 +344,26 @@ int sgpu_stroke_team_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGP
 int sgpu_raycast(sgpu_mesh *mesh, int nrays, const float *ray_starts, const float *ray_normals,
                  const float *ray_lengths, int original, float *r_depths, int *r_hits,
                  int *r_active_vertices, int *r_active_faces, float *r_face_normals);
+
+/* ---- nearest to ray ----
+ * Replaces BKE_pbvh_find_nearest_to_ray (pbvh.c:4339-4352) driven by the
+ * sculpt nearest-to-ray callback (absent with sculpt.c; fixed by the brush
+ * specification like the ray cast's): the location of a dab when the cursor
+ * ray misses the surface.  Leaves are visited in order of their box's squared
+ * distance from the ray (nearest_to_ray_aabb_dist_sq, pbvh.c:4315-4337; a box
+ * whose nearest point lies behind the ray origin is skipped), a leaf is
+ * searched while that distance is below the running minimum, and inside it
+ * the triangle (PBVH_FACES looptri, PBVH_GRIDS quad triangle) of smallest
+ * squared distance from the ray wins (pbvh_faces_node_nearest_to_ray /
+ * pbvh_grids_node_nearest_to_ray, pbvh.c:4354-4460; a quad's second triangle
+ * is tested only when its first one is taken).  Per ray: r_depths the depth
+ * along the ray of the nearest point, r_dist_sq its squared distance, r_hits
+ * 1 when a triangle was taken (the values start at FLT_MAX).  The location
+ * the stroke uses is ray_start + ray_normal * depth.  Shares the ray cast's
+ * buffers and graph cache (a graph per (nrays, original, query)). */
+int sgpu_find_nearest_to_ray(sgpu_mesh *mesh, int nrays, const float *ray_starts,
+                             const float *ray_normals, int original, float *r_depths,
+                             float *r_dist_sq, int *r_hits);
 
 /* ---- headless draw buffers ----
  * Replaces the PBVH draw-buffer path without GL: pbvh_update_draw_buffers
@@ -487,9 +509,15 @@ int sgpu_host_free(void *ptr);
  * The Jacobi scratch is a fixed device array of SGPU_NOALLOC_MAX_VERTS float4
  * (1 MiB) that every GPU loading the library holds until exit; nverts above
  * that returns SGPU_ERR_INVALID_ARG.  The first call on a device looks up the
- * array's device address, so make it before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race.  No cudaMalloc, no
- * cudaFree.  Synchronous on stream (a cudaStream_t; NULL = default stream). */
+ * array's device address (again after a device reset), so make it before any
+ * stream capture: a call with nverts = 0 at set-up does only that, and with
+ * lazy module loading (the CUDA default) it also makes the driver load the
+ * module that holds the array, so that no later call loads it inside a fixed
+ * memory budget (CUDA_MODULE_LOADING=EAGER loads it with the library).  All
+ * calls share the array: calls that overlap on the GPU race.  No cudaMalloc,
+ * no cudaFree.  Every entry of verts and nb_idx must index the caller's co
+ * array (and normals, mask, automask); nothing checks this on the device.
+ * The call waits for its stream (a cudaStream_t; NULL = default stream). */
 #define SGPU_NOALLOC_MAX_VERTS 65536
 int sgpu_smooth_dab_noalloc(float *co, const float *normals, const float *mask,
                             const float *automask, const int *nb_off, const int *nb_idx,

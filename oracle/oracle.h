@@ -157,6 +157,17 @@ int or_raycast(OrMesh *m, const float ray_start[3], const float ray_normal[3], i
                float *depth, int *active_vertex, int *active_face, float face_normal[3],
                int *r_nleaves);
 
+/* BKE_pbvh_find_nearest_to_ray (PBVH_FACES and PBVH_GRIDS) with the sculpt
+ * nearest-to-ray callback of the brush specification: leaves in order of
+ * their box's squared distance to the ray, a leaf searched while that
+ * distance is below the running minimum, the triangle (grid quad) of
+ * smallest squared distance inside (strictly smaller wins).  depth and
+ * dist_sq: in = starting values (FLT_MAX), out = the nearest triangle's
+ * depth along the ray and squared distance.  Returns 1 when some triangle was
+ * taken.  r_nleaves (nullable): leaves listed. */
+int or_nearest_to_ray(OrMesh *m, const float ray_start[3], const float ray_normal[3],
+                      int original, float *depth, float *dist_sq, int *r_nleaves);
+
 /* Test helper: grid quads whose two triangles both meet the ray, the second
  * one closer. */
 int or_grids_special_quads(OrMesh *m, const float ray_start[3], const float ray_normal[3]);

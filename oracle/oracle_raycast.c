@@ -13,6 +13,18 @@
  *   ray_face_intersection_tri / _quad                     pbvh.c:3930-3967
  *   pbvh_faces_node_raycast                               pbvh.c:4042-4108
  *   pbvh_grids_node_raycast                               pbvh.c:4110-4201
+ * and for the nearest-to-ray query:
+ *   dist_squared_ray_to_seg_v3                            math_geom.cc:574-608
+ *   aabb_get_near_far_from_plane                          math_geom.cc:610-641
+ *   dist_squared_ray_to_aabb_v3(_precalc)                 math_geom.cc:643-744
+ *   isect_ray_line_v3                                     math_geom.cc:1997-2021
+ *   interp_v3_v3v3                                        math_vector.c:24-31
+ *   nearest_to_ray_aabb_dist_sq,
+ *   BKE_pbvh_find_nearest_to_ray                          pbvh.c:4315-4352
+ *   dist_squared_ray_to_tri_v3_fast,
+ *   ray_face_nearest_quad / _tri                          pbvh.c:3970-4040
+ *   pbvh_faces_node_nearest_to_ray,
+ *   pbvh_grids_node_nearest_to_ray                        pbvh.c:4354-4460
  * and the sculpt ray-cast callback the reference calls but does not ship
  * (its sculpt.c is absent), fixed by the brush specification: a leaf is ray
  * cast when its entry distance is below the running minimum (FLT_MAX until
@@ -403,4 +415,306 @@ int or_grids_special_quads(OrMesh *m, const float ray_start[3], const float ray_
     }
   }
   return n;
+}
+
+/* ---- nearest to ray ---- */
+
+static float dot3(const float *a, const float *b)
+{
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+static void cross3(float r[3], const float *a, const float *b)
+{
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* isect_ray_line_v3: parameter of the point of the line v0 -> v1 nearest the
+ * ray (0 when the two are parallel, returned as no intersection). */
+static int ray_line(const float *o, const float *dir, const float *v0, const float *v1,
+                    float *r_lambda)
+{
+  const float a[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+  const float t[3] = {v0[0] - o[0], v0[1] - o[1], v0[2] - o[2]};
+  float n[3];
+  cross3(n, a, dir);
+  const float nlen = dot3(n, n);
+  if (nlen == 0.0f) {
+    return 0;
+  }
+  const float c[3] = {n[0] - t[0], n[1] - t[1], n[2] - t[2]};
+  float cray[3];
+  cross3(cray, c, dir);
+  *r_lambda = dot3(cray, n) / nlen;
+  return 1;
+}
+
+/* dist_squared_ray_to_seg_v3: squared distance of the segment point the line
+ * parameter selects (clamped to the ends; v0 for a parallel segment) from the
+ * ray, and its depth along the ray. */
+static float ray_seg_dist_sq(const float *o, const float *dir, const float *v0, const float *v1,
+                             float *r_depth)
+{
+  float lambda, p[3];
+  if (ray_line(o, dir, v0, v1, &lambda)) {
+    if (lambda <= 0.0f) {
+      p[0] = v0[0], p[1] = v0[1], p[2] = v0[2];
+    }
+    else if (lambda >= 1.0f) {
+      p[0] = v1[0], p[1] = v1[1], p[2] = v1[2];
+    }
+    else {
+      const float s = 1.0f - lambda;
+      p[0] = s * v0[0] + lambda * v1[0];
+      p[1] = s * v0[1] + lambda * v1[1];
+      p[2] = s * v0[2] + lambda * v1[2];
+    }
+  }
+  else {
+    p[0] = v0[0], p[1] = v0[1], p[2] = v0[2];
+  }
+  const float dvec[3] = {p[0] - o[0], p[1] - o[1], p[2] - o[2]};
+  const float depth = dot3(dvec, dir);
+  *r_depth = depth;
+  return dot3(dvec, dvec) - depth * depth;
+}
+
+/* dist_squared_ray_to_tri_v3_fast: the nearest of the three edges (in the
+ * order (v0, v2), (v1, v0), (v2, v1); the first edge, then any strictly
+ * nearer one). */
+static float ray_tri_dist_sq(const float *o, const float *dir, const float *v0, const float *v1,
+                             const float *v2, float *r_depth)
+{
+  const float *tri[3] = {v0, v1, v2};
+  float best = FLT_MAX;
+  for (int i = 0, j = 2; i < 3; j = i++) {
+    float dt = FLT_MAX;
+    const float d = ray_seg_dist_sq(o, dir, tri[i], tri[j], &dt);
+    if (d < best || i == 0) {
+      *r_depth = dt;
+      best = d;
+    }
+  }
+  return best;
+}
+
+typedef struct RayAabb {
+  float org[3], dir[3], inv[3];
+} RayAabb;
+
+static void rayaabb_init(RayAabb *r, const float o[3], const float d[3])
+{
+  for (int i = 0; i < 3; i++) {
+    r->org[i] = o[i];
+    r->dir[i] = d[i];
+    r->inv[i] = (d[i] != 0.0f) ? (1.0f / d[i]) : FLT_MAX;
+  }
+}
+
+/* dist_squared_ray_to_aabb_v3: 0 and the depth of the far corner when the
+ * ray line meets the box, else the squared distance to the box edge nearest
+ * the ray and its depth. */
+static float rayaabb_dist_sq(const RayAabb *r, const float *bmin, const float *bmax,
+                             float *r_depth)
+{
+  float lo[3], hi[3];
+  for (int k = 0; k < 3; k++) {
+    /* aabb_get_near_far_from_plane */
+    if (r->dir[k] < 0.0f) {
+      lo[k] = bmax[k];
+      hi[k] = bmin[k];
+    }
+    else {
+      lo[k] = bmin[k];
+      hi[k] = bmax[k];
+    }
+  }
+  const float tmin[3] = {(lo[0] - r->org[0]) * r->inv[0], (lo[1] - r->org[1]) * r->inv[1],
+                         (lo[2] - r->org[2]) * r->inv[2]};
+  const float tmax[3] = {(hi[0] - r->org[0]) * r->inv[0], (hi[1] - r->org[1]) * r->inv[1],
+                         (hi[2] - r->org[2]) * r->inv[2]};
+  float va[3] = {0.0f, 0.0f, 0.0f}, vb[3] = {0.0f, 0.0f, 0.0f};
+  float rtmin, rtmax;
+  int axis;
+  if ((tmax[0] <= tmax[1]) && (tmax[0] <= tmax[2])) {
+    rtmax = tmax[0];
+    va[0] = vb[0] = hi[0];
+    axis = 3;
+  }
+  else if ((tmax[1] <= tmax[0]) && (tmax[1] <= tmax[2])) {
+    rtmax = tmax[1];
+    va[1] = vb[1] = hi[1];
+    axis = 2;
+  }
+  else {
+    rtmax = tmax[2];
+    va[2] = vb[2] = hi[2];
+    axis = 1;
+  }
+  if ((tmin[0] >= tmin[1]) && (tmin[0] >= tmin[2])) {
+    rtmin = tmin[0];
+    va[0] = vb[0] = lo[0];
+    axis -= 3;
+  }
+  else if ((tmin[1] >= tmin[0]) && (tmin[1] >= tmin[2])) {
+    rtmin = tmin[1];
+    va[1] = vb[1] = lo[1];
+    axis -= 1;
+  }
+  else {
+    rtmin = tmin[2];
+    va[2] = vb[2] = lo[2];
+    axis -= 2;
+  }
+  if (axis < 0) {
+    axis += 3;
+  }
+  if (rtmin <= rtmax) {
+    const float dvec[3] = {hi[0] - r->org[0], hi[1] - r->org[1], hi[2] - r->org[2]};
+    *r_depth = dot3(dvec, r->dir);
+    return 0.0f;
+  }
+  if (r->dir[axis] >= 0.0f) {
+    va[axis] = lo[axis];
+    vb[axis] = hi[axis];
+  }
+  else {
+    va[axis] = hi[axis];
+    vb[axis] = lo[axis];
+  }
+  return ray_seg_dist_sq(r->org, r->dir, va, vb, r_depth);
+}
+
+int or_nearest_to_ray(OrMesh *m, const float ray_start[3], const float ray_normal[3],
+                      int original, float *depth, float *dist_sq, int *r_nleaves)
+{
+  if (m->totnode == 0) {
+    if (r_nleaves) {
+      *r_nleaves = 0;
+    }
+    return 0;
+  }
+  const float *boxes = original ? m->sf.orig_vb : m->sf.vb;
+  RayAabb ra;
+  rayaabb_init(&ra, ray_start, ray_normal);
+  /* pbvh_iter_next_occluded with nearest_to_ray_aabb_dist_sq: a node passes
+   * when the depth of its nearest point is positive; its tmin is the squared
+   * distance */
+  int *stack = malloc(sizeof(int) * (size_t)(m->totnode + 1));
+  int *leaf = malloc(sizeof(int) * (size_t)(m->nleaf + 1));
+  float *tmin = malloc(sizeof(float) * (size_t)(m->nleaf + 1));
+  int *left = malloc(sizeof(int) * (size_t)(m->nleaf + 1));
+  int *right = malloc(sizeof(int) * (size_t)(m->nleaf + 1));
+  int ns = 0, nl = 0;
+  stack[ns++] = 0;
+  while (ns) {
+    const int n = stack[--ns];
+    float dep;
+    const float t = rayaabb_dist_sq(&ra, boxes + 6 * n, boxes + 6 * n + 3, &dep);
+    if (!(dep > 0.0f)) {
+      continue;
+    }
+    const OrNode *nd = &m->nodes[n];
+    if (nd->flag & OR_Leaf) {
+      leaf[nl] = n;
+      tmin[nl] = t;
+      left[nl] = right[nl] = -1;
+      if (nl > 0) { /* node_tree_insert */
+        int at = 0;
+        for (;;) {
+          int *next = (t < tmin[at]) ? &left[at] : &right[at];
+          if (*next < 0) {
+            *next = nl;
+            break;
+          }
+          at = *next;
+        }
+      }
+      nl++;
+      continue;
+    }
+    stack[ns++] = nd->children_offset + 1;
+    stack[ns++] = nd->children_offset;
+  }
+  if (r_nleaves) {
+    *r_nleaves = nl;
+  }
+  /* traverse_tree with the callback: a leaf is searched when its tmin is below
+   * the running minimum; a found triangle makes its squared distance the
+   * running minimum */
+  int hit = 0;
+  float run_tmin = FLT_MAX;
+  float dep = *depth, dsq = *dist_sq;
+  int *st = stack;
+  int sp = 0, cur = nl > 0 ? 0 : -1;
+  const int gs = m->grid_size, area = m->grid_area;
+  while (cur >= 0 || sp > 0) {
+    while (cur >= 0) {
+      st[sp++] = cur;
+      cur = left[cur];
+    }
+    cur = st[--sp];
+    if (tmin[cur] < run_tmin) {
+      const OrNode *nd = &m->nodes[leaf[cur]];
+      int node_hit = 0;
+      if (m->type == OR_GRIDS) {
+        /* pbvh_grids_node_nearest_to_ray: quads in (grid, row, column) order;
+         * ray_face_nearest_quad tests the second triangle only when the first
+         * was taken */
+        for (int i = 0; i < nd->totprim; i++) {
+          const int g = m->prim_indices[nd->prim_off + i];
+          const float *base = m->sf.co + 3 * (size_t)g * area;
+          for (int y = 0; y < gs - 1; y++) {
+            for (int x = 0; x < gs - 1; x++) {
+              const float *c0 = base + 3 * (y * gs + x), *c1 = base + 3 * (y * gs + x + 1);
+              const float *c2 = base + 3 * ((y + 1) * gs + x + 1);
+              const float *c3 = base + 3 * ((y + 1) * gs + x);
+              float dt, d = ray_tri_dist_sq(ray_start, ray_normal, c0, c1, c2, &dt);
+              if (d < dsq) {
+                dsq = d;
+                dep = dt;
+                node_hit = 1;
+                d = ray_tri_dist_sq(ray_start, ray_normal, c0, c2, c3, &dt);
+                if (d < dsq) {
+                  dsq = d;
+                  dep = dt;
+                }
+              }
+            }
+          }
+        }
+      }
+      else {
+        /* pbvh_faces_node_nearest_to_ray over the leaf's looptris in prim order */
+        for (int i = 0; i < nd->totprim; i++) {
+          const int t = m->prim_indices[nd->prim_off + i];
+          const int *tv = m->lt_v + 3 * (size_t)t;
+          float dt;
+          const float d = ray_tri_dist_sq(ray_start, ray_normal, m->sf.co + 3 * (size_t)tv[0],
+                                          m->sf.co + 3 * (size_t)tv[1],
+                                          m->sf.co + 3 * (size_t)tv[2], &dt);
+          if (d < dsq) {
+            dsq = d;
+            dep = dt;
+            node_hit = 1;
+          }
+        }
+      }
+      if (node_hit) {
+        hit = 1;
+        run_tmin = dsq;
+      }
+    }
+    cur = right[cur];
+  }
+  *depth = dep;
+  *dist_sq = dsq;
+  free(stack);
+  free(leaf);
+  free(tmin);
+  free(left);
+  free(right);
+  return hit;
 }

@@ -86,6 +86,8 @@ def lib():
         L.or_orig_dab.argtypes = [vp, C.POINTER(OrBrush), vp, vp]
         L.or_raycast.restype = i
         L.or_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp, vp]
+        L.or_nearest_to_ray.restype = i
+        L.or_nearest_to_ray.argtypes = [vp, vp, vp, i, vp, vp, vp]
         L.or_grids_special_quads.restype = i
         L.or_grids_special_quads.argtypes = [vp, vp, vp]
         L.or_curve_table.argtypes = [i, vp, vp]
@@ -345,6 +347,16 @@ class OracleMesh:
         hit = lib().or_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(af), _p(fn),
                                _p(nl))
         return bool(hit), dep[0], int(av[0]), int(af[0]), fn, int(nl[0])
+
+    def nearest_to_ray(self, ray_start, ray_normal, original: int = 0):
+        """(hit, depth, squared distance, leaves listed) of the nearest-to-ray query."""
+        o = np.asarray(ray_start, dtype=np.float32)
+        d = np.asarray(ray_normal, dtype=np.float32)
+        dep = np.array([3.4028234663852886e38], dtype=np.float32)
+        dsq = np.array([3.4028234663852886e38], dtype=np.float32)
+        nl = np.zeros(1, dtype=np.int32)
+        hit = lib().or_nearest_to_ray(self.h, _p(o), _p(d), original, _p(dep), _p(dsq), _p(nl))
+        return bool(hit), dep[0], dsq[0], int(nl[0])
 
     def grids_special_quads(self, ray_start, ray_normal) -> int:
         o = np.asarray(ray_start, dtype=np.float32)

@@ -85,6 +85,9 @@ def lib():
         L.rg_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
         L.rp_raycast.restype = i
         L.rp_raycast.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
+        for name in ("rp_nearest_to_ray", "rg_nearest_to_ray"):
+            getattr(L, name).restype = i
+            getattr(L, name).argtypes = [vp, vp, vp, i, vp, vp]
         L.rp_curve_table.argtypes = [i, vp, vp]
         L.rp_curve_evaluate.argtypes = [i, vp, i, vp]
         L.rp_pbvh.restype = vp
@@ -298,6 +301,16 @@ class RefPBVH:
         hit = lib().rp_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(af), _p(fn))
         return bool(hit), dep[0], int(av[0]), int(af[0]), fn
 
+    def nearest_to_ray(self, ray_start, ray_normal, original: int = 0):
+        """BKE_pbvh_find_nearest_to_ray with the spec'd callback: (hit, depth,
+        squared distance)."""
+        o = np.asarray(ray_start, dtype=np.float32)
+        d = np.asarray(ray_normal, dtype=np.float32)
+        dep = np.array([3.4028234663852886e38], dtype=np.float32)
+        dsq = np.array([3.4028234663852886e38], dtype=np.float32)
+        hit = lib().rp_nearest_to_ray(self.h, _p(o), _p(d), original, _p(dep), _p(dsq))
+        return bool(hit), dep[0], dsq[0]
+
 
 def _refpbvh_draw_setup(self, m, face_sets=None, loop_colors=None, vert_colors=None,
                         use_vert_colors=False, seed: int = 0, color_default: int = 1):
@@ -401,6 +414,15 @@ class RefGrids:
         fn = np.zeros(3, dtype=np.float32)
         hit = lib().rg_raycast(self.h, _p(o), _p(d), original, _p(dep), _p(av), _p(ag), _p(fn))
         return bool(hit), dep[0], int(av[0]), int(ag[0]), fn
+
+    def nearest_to_ray(self, ray_start, ray_normal, original: int = 0):
+        """BKE_pbvh_find_nearest_to_ray on the grids: (hit, depth, squared distance)."""
+        o = np.asarray(ray_start, dtype=np.float32)
+        d = np.asarray(ray_normal, dtype=np.float32)
+        dep = np.array([3.4028234663852886e38], dtype=np.float32)
+        dsq = np.array([3.4028234663852886e38], dtype=np.float32)
+        hit = lib().rg_nearest_to_ray(self.h, _p(o), _p(d), original, _p(dep), _p(dsq))
+        return bool(hit), dep[0], dsq[0]
 
     def draw_setup(self, face_sets=None, grid_flag_mats=None, seed: int = 0,
                    color_default: int = 1):

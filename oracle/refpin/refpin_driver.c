@@ -377,6 +377,49 @@ int rp_raycast(RefPin *r, const float start[3], const float normal[3], int origi
   return d.hit ? 1 : 0;
 }
 
+/* ---- nearest to ray (pbvh.c:4315-4494) ---- */
+typedef struct NearestCb {
+  PBVH *pbvh;
+  const float *start, *normal;
+  float depth, dist_sq;
+  bool hit;
+} NearestCb;
+
+/* The sculpt nearest-to-ray callback of the brush specification (the
+ * reference's sculpt.c, which would hold it, is absent), the same rule as the
+ * ray cast's: a node is searched when its squared distance to the ray is
+ * below the running minimum; a found triangle lowers the minimum to its
+ * squared distance. */
+static void nearest_cb(PBVHNode *node, void *data_v, float *tmin)
+{
+  NearestCb *d = data_v;
+  if (BKE_pbvh_node_get_tmin(node) < *tmin) {
+    if (BKE_pbvh_node_find_nearest_to_ray(d->pbvh, node, NULL, false, d->start, d->normal,
+                                          &d->depth, &d->dist_sq)) {
+      d->hit = true;
+      *tmin = d->dist_sq;
+    }
+  }
+}
+
+/* BKE_pbvh_find_nearest_to_ray with that callback; depth and dist_sq in =
+ * the starting values (FLT_MAX), out = the nearest triangle's. */
+int rp_nearest_to_ray(RefPin *r, const float start[3], const float normal[3], int original,
+                      float *depth, float *dist_sq)
+{
+  NearestCb d;
+  memset(&d, 0, sizeof(d));
+  d.pbvh = r->pbvh;
+  d.start = start;
+  d.normal = normal;
+  d.depth = *depth;
+  d.dist_sq = *dist_sq;
+  BKE_pbvh_find_nearest_to_ray(r->pbvh, nearest_cb, &d, start, normal, original != 0);
+  *depth = d.depth;
+  *dist_sq = d.dist_sq;
+  return d.hit ? 1 : 0;
+}
+
 /* The PBVH of a harness mesh (the draw-buffer functions of refpin_draw.c take it). */
 PBVH *rp_pbvh(RefPin *r)
 {

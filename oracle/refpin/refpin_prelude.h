@@ -156,6 +156,11 @@ float dist_squared_ray_to_seg_v3(const float ray_origin[3], const float ray_dire
                                  float *r_depth);
 float dist_squared_to_ray_v3_normalized(const float ray_origin[3], const float ray_direction[3],
                                         const float co[3]);
+void aabb_get_near_far_from_plane(const float plane_no[3], const float bbmin[3],
+                                  const float bbmax[3], float bb_near[3], float bb_afar[3]);
+bool isect_ray_line_v3(const float ray_origin[3], const float ray_direction[3], const float v0[3],
+                       const float v1[3], float *r_lambda);
+void interp_v3_v3v3(float r[3], const float a[3], const float b[3], const float t);
 void closest_on_tri_to_point_v3(float r[3], const float p[3], const float v1[3],
                                 const float v2[3], const float v3[3]);
 
@@ -642,6 +647,12 @@ bool BKE_pbvh_node_raycast(PBVH *pbvh, PBVHNode *node, float (*origco)[3], bool 
                            float *face_normal);
 void BKE_pbvh_raycast(PBVH *pbvh, BKE_pbvh_HitOccludedCallback cb, void *data,
                       const float ray_start[3], const float ray_normal[3], bool original);
+void BKE_pbvh_find_nearest_to_ray(PBVH *pbvh, BKE_pbvh_SearchNearestCallback cb, void *data,
+                                  const float ray_start[3], const float ray_normal[3],
+                                  bool original);
+bool BKE_pbvh_node_find_nearest_to_ray(PBVH *pbvh, PBVHNode *node, float (*origco)[3],
+                                       bool use_origco, const float ray_start[3],
+                                       const float ray_normal[3], float *depth, float *dist_sq);
 GSet *BKE_pbvh_bmesh_node_unique_verts(PBVHNode *node);
 GSet *BKE_pbvh_bmesh_node_other_verts(PBVHNode *node);
 void BKE_pbvh_node_fully_masked_set(PBVHNode *node, int fully_masked);

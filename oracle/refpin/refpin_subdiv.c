@@ -425,6 +425,43 @@ int rg_raycast(RefGrids *g, const float start[3], const float normal[3], int ori
   return d.hit ? 1 : 0;
 }
 
+/* BKE_pbvh_find_nearest_to_ray on the grids PBVH with the callback of
+ * rp_nearest_to_ray (pbvh_grids_node_nearest_to_ray inside a leaf). */
+typedef struct GridNearestCb {
+  PBVH *pbvh;
+  const float *start, *normal;
+  float depth, dist_sq;
+  bool hit;
+} GridNearestCb;
+
+static void grid_nearest_cb(PBVHNode *node, void *data_v, float *tmin)
+{
+  GridNearestCb *d = data_v;
+  if (BKE_pbvh_node_get_tmin(node) < *tmin) {
+    if (BKE_pbvh_node_find_nearest_to_ray(d->pbvh, node, NULL, false, d->start, d->normal,
+                                          &d->depth, &d->dist_sq)) {
+      d->hit = true;
+      *tmin = d->dist_sq;
+    }
+  }
+}
+
+int rg_nearest_to_ray(RefGrids *g, const float start[3], const float normal[3], int original,
+                      float *depth, float *dist_sq)
+{
+  GridNearestCb d;
+  memset(&d, 0, sizeof(d));
+  d.pbvh = g->pbvh;
+  d.start = start;
+  d.normal = normal;
+  d.depth = *depth;
+  d.dist_sq = *dist_sq;
+  BKE_pbvh_find_nearest_to_ray(g->pbvh, grid_nearest_cb, &d, start, normal, original != 0);
+  *depth = d.depth;
+  *dist_sq = d.dist_sq;
+  return d.hit ? 1 : 0;
+}
+
 PBVH *rg_pbvh(RefGrids *g)
 {
   return g->pbvh;

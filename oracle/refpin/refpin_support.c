@@ -417,26 +417,6 @@ void GPU_pbvh_bmesh_buffers_update_free(GPU_PBVH_Buffers *buffers)
   refpin_unreachable("dyntopo draw buffers");
 }
 
-/* Nearest-to-ray queries are not pinned: dist_squared_ray_to_seg_v3
- * (math_geom.cc:574-580) has an empty body in the reference. */
-void dist_squared_ray_to_aabb_v3_precalc(DistRayAABBPrecalc *neasrest_precalc,
-                                         const float ray_origin[3], const float ray_direction[3])
-{
-  refpin_unreachable("nearest to ray");
-}
-float dist_squared_ray_to_aabb_v3(const DistRayAABBPrecalc *data, const float bb_min[3],
-                                  const float bb_max[3], float r_point[3], float *r_depth)
-{
-  refpin_unreachable("nearest to ray");
-  return 0.0f;
-}
-float dist_squared_ray_to_seg_v3(const float ray_origin[3], const float ray_direction[3],
-                                 const float v0[3], const float v1[3], float r_point[3],
-                                 float *r_depth)
-{
-  refpin_unreachable("nearest to ray");
-  return 0.0f;
-}
 void mid_v3_v3v3(float r[3], const float a[3], const float b[3])
 {
   refpin_unreachable("raycast root projection");

@@ -438,3 +438,86 @@ def test_grids_raycast_matches_reference(oracle, jitter):
     assert hits > 100
     if jitter:
         assert special > 20
+
+
+def _near_rays(rng, n, center, radius):
+    """Rays from a sphere around the mesh towards points scattered up to about
+    the mesh's size from its middle: many pass beside the surface, the case
+    the nearest-to-ray query serves; every seventh one axis-aligned."""
+    out = []
+    for k in range(n):
+        s = rng.normal(size=3)
+        s = (center + s / np.linalg.norm(s) * radius).astype(np.float32)
+        if k % 7 == 0:
+            ax = k % 3
+            d = np.zeros(3, np.float32)
+            d[ax] = -1.0 if s[ax] > center[ax] else 1.0
+        else:
+            t = center + rng.normal(size=3) * 0.45 * radius
+            d = (t - s) / np.linalg.norm(t - s)
+        out.append((s, d.astype(np.float32)))
+    return out
+
+
+def _same_near(a, b):
+    f = lambda x: np.float32(x).view(np.uint32)  # noqa: E731
+    return a[0] == b[0] and f(a[1]) == f(b[1]) and f(a[2]) == f(b[2])
+
+
+@pytest.mark.parametrize("name", ["grid", "icosphere", "uvsphere", "ngon"])
+def test_nearest_to_ray_matches_reference(oracle, name):
+    """BKE_pbvh_find_nearest_to_ray (pbvh.c:4339-4352) with the spec'd sculpt
+    callback, pbvh_faces_node_nearest_to_ray, dist_squared_ray_to_tri_v3_fast
+    and the math_geom.cc ray / segment / box distances: hit flag, depth and
+    squared distance bit for bit, over vb and orig_vb, before and after an
+    edit."""
+    m, o, r = _pair(oracle, name, 5000)
+    co = o.co()
+    center = (co.min(0) + co.max(0)) / 2
+    radius = float(np.linalg.norm(co.max(0) - co.min(0)))
+    rng = np.random.default_rng(23)
+    hits = 0
+    for k, (s, d) in enumerate(_near_rays(rng, 300, center, radius)):
+        a = o.nearest_to_ray(s, d, original=k % 2)
+        b = r.nearest_to_ray(s, d, original=k % 2)
+        assert _same_near(a, b), (k, a, b)
+        hits += a[0]
+    assert hits > 100
+    co2, _ = _edit(o, r, co, center.astype(np.float32), 0.3 * radius, 0.05 * radius)
+    o.update_normals()
+    r.update_normals()
+    o.update_bounds(UPD_BB)
+    r.update_bounds(UPD_BB)
+    for k, (s, d) in enumerate(_near_rays(rng, 100, center, radius)):
+        a = o.nearest_to_ray(s, d, original=k % 2)
+        b = r.nearest_to_ray(s, d, original=k % 2)
+        assert _same_near(a, b), (k, a, b)
+
+
+@pytest.mark.parametrize("jitter", [0.0, 0.02])
+def test_grids_nearest_to_ray_matches_reference(oracle, jitter):
+    """pbvh_grids_node_nearest_to_ray (pbvh.c:4402-4460): grid quads, the
+    second triangle tested only when the first is taken (ray_face_nearest_quad,
+    pbvh.c:3991-4017), on a smooth and a jittered torus."""
+    g = synth.torus_grids(16, 6, 4)
+    rng = np.random.default_rng(31)
+    if jitter:
+        g.co = (g.co + rng.normal(size=g.co.shape) * jitter).astype(np.float32)
+    o = oracle.OracleMesh.grids(g, 0)
+    o.recalc_all_normals()
+    r = pyrefpin.RefGrids(g, np.zeros_like(g.co))
+    for n in np.nonzero(o.nodes()["flag"] & LEAF)[0]:
+        r.node_mark_update(int(n))
+    r.update_normals()
+    r.update_bounds(UPD_BB)
+    hits = 0
+    for k in range(300):
+        s = rng.normal(size=3)
+        s = (2.5 * s / np.linalg.norm(s)).astype(np.float32)
+        t = rng.normal(size=3) * 1.2
+        d = ((t - s) / np.linalg.norm(t - s)).astype(np.float32)
+        a = o.nearest_to_ray(s, d, original=k % 2)
+        b = r.nearest_to_ray(s, d, original=k % 2)
+        assert _same_near(a, b), (k, a, b)
+        hits += a[0]
+    assert hits > 100

@@ -101,20 +101,44 @@ def candidates(pbvh, nodes):
     return np.concatenate(parts).astype(np.int32) if parts else np.zeros(0, np.int32)
 
 
-def test_noalloc_smooth_matches_handle_path(gpu):
+def _noalloc_lib(gpu):
     lib = gpu.load()
     lib.sgpu_smooth_dab_noalloc.argtypes = [C.c_void_p] * 7 + [C.c_int, C.c_void_p,
                                                                 C.c_void_p, C.c_void_p]
+    return lib
+
+
+@pytest.mark.parametrize("strength,frontface", [(0.7, False), (0.25, False), (1.0, False),
+                                                (0.7, True)])
+def test_noalloc_smooth_matches_handle_path(gpu, strength, frontface):
+    """Two calls in a row equal sgpu_do_smooth_brush bit for bit: strength 0.7
+    (two full sweeps and a fractional one), 0.25 (one full sweep and a last
+    one of strength zero), 1.0 (four full sweeps and a last zero one), and the
+    front-face falloff, which reads the normals, with an automask."""
+    lib = _noalloc_lib(gpu)
     rt = _cudart()
     m = small_icosphere(4)
-    g = PBVH.build_mesh(m, 200)
+    automask = None
+    if frontface:
+        automask = (0.25 + 0.75 * synth.value_noise(synth.SEED_BASE + 71, 3,
+                                                    m.verts["co"].astype(np.float64), 3.0))
+        automask = automask.astype(np.float32)
+    g = PBVH.build_mesh(m, 200, automask=automask)
     verts0 = g.verts()
     off, idx = one_ring(m)
     d_co = DevArray(rt, verts0)
     d_mask = DevArray(rt, m.mask)
     d_off = DevArray(rt, off)
     d_idx = DevArray(rt, idx)
-    st = synth.Stroke(synth.TOOL_SMOOTH, 0.18, 0.7, synth.CURVE_SMOOTH, 0, None)
+    d_no = d_am = None
+    if frontface:
+        no4 = np.zeros((m.totvert, 4), np.float32)
+        no4[:, :3] = g.normals()
+        d_no = DevArray(rt, no4)
+        d_am = DevArray(rt, automask)
+    view = (0.3, -0.4, 0.866)
+    st = synth.Stroke(synth.TOOL_SMOOTH, 0.18, strength, synth.CURVE_SMOOTH, 0, None,
+                      flag=(1 << 27) if frontface else 0, view_normal=view)
     brush = make_brush(st)
     co = g.positions()
     try:
@@ -126,8 +150,9 @@ def test_noalloc_smooth_matches_handle_path(gpu):
             assert 0 < cand.size <= 65536
             d_verts = DevArray(rt, cand)
             g.do_smooth_brush(st, center, [1.0, 0.0, 0.0], nodes)
-            rc = lib.sgpu_smooth_dab_noalloc(d_co.ptr, None, d_mask.ptr, None, d_off.ptr,
-                                             d_idx.ptr, d_verts.ptr, cand.size, C.byref(brush),
+            rc = lib.sgpu_smooth_dab_noalloc(d_co.ptr, d_no.ptr if d_no else None, d_mask.ptr,
+                                             d_am.ptr if d_am else None, d_off.ptr, d_idx.ptr,
+                                             d_verts.ptr, cand.size, C.byref(brush),
                                              center.ctypes.data_as(C.c_void_p), None)
             d_verts.free()
             assert rc == 0, lib.sgpu_last_error()
@@ -143,5 +168,37 @@ def test_noalloc_smooth_matches_handle_path(gpu):
                                          np.zeros(3, np.float32).ctypes.data_as(C.c_void_p), None)
         assert rc == 1 and b"65536" in lib.sgpu_last_error()
     finally:
-        for a in (d_co, d_mask, d_off, d_idx):
+        for a in (d_co, d_mask, d_off, d_idx, d_no, d_am):
+            if a is not None:
+                a.free()
+
+
+def test_noalloc_empty_call_and_front_face_without_normals(gpu):
+    """nverts = 0 returns SGPU_OK and leaves the positions alone (it only looks
+    up the scratch address: the warm-up call a caller makes at set-up); the
+    front-face falloff without normals is rejected."""
+    lib = _noalloc_lib(gpu)
+    rt = _cudart()
+    m = small_icosphere(3)
+    verts0 = np.ascontiguousarray(m.verts)
+    off, idx = one_ring(m)
+    d_co = DevArray(rt, verts0)
+    d_off = DevArray(rt, off)
+    d_idx = DevArray(rt, idx)
+    brush = make_brush(synth.Stroke(synth.TOOL_SMOOTH, 0.2, 0.5, synth.CURVE_SMOOTH, 0, None))
+    loc = np.zeros(3, np.float32)
+    try:
+        rc = lib.sgpu_smooth_dab_noalloc(d_co.ptr, None, None, None, d_off.ptr, d_idx.ptr, None,
+                                         0, C.byref(brush), loc.ctypes.data_as(C.c_void_p), None)
+        assert rc == 0, lib.sgpu_last_error()
+        assert bits_equal(d_co.download(verts0)["co"], verts0["co"])
+        ff = make_brush(synth.Stroke(synth.TOOL_SMOOTH, 0.2, 0.5, synth.CURVE_SMOOTH, 0, None,
+                                     flag=1 << 27))
+        rc = lib.sgpu_smooth_dab_noalloc(d_co.ptr, None, None, None, d_off.ptr, d_idx.ptr,
+                                         d_off.ptr, 1, C.byref(ff),
+                                         loc.ctypes.data_as(C.c_void_p), None)
+        assert rc == 1 and b"normals" in lib.sgpu_last_error()
+        assert bits_equal(d_co.download(verts0)["co"], verts0["co"])
+    finally:
+        for a in (d_co, d_off, d_idx):
             a.free()
