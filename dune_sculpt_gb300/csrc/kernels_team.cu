@@ -17,7 +17,7 @@ size_t team_smem_bytes(int max_nodes, int max_leaves) {
   const size_t n = static_cast<size_t>(max_nodes), l = static_cast<size_t>(max_leaves);
   const size_t even_n = (n + 1) & ~static_cast<size_t>(1), even_l = (l + 1) & ~static_cast<size_t>(1);
   const size_t marks = std::max(n, 4 * ((n + 31) / 32));
-  const size_t b = sizeof(float4) * kNbCache * kTeamThreads + sizeof(int) * (n + 3 * l + 3) +
+  const size_t b = kStageBytes + sizeof(int) * (n + 3 * l + 3) +
                    sizeof(unsigned short) * (even_n + even_l) + marks;
   return (b + 15) & ~static_cast<size_t>(15);
 }

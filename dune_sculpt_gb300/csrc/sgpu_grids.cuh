@@ -196,43 +196,4 @@ __device__ __forceinline__ void grid_seam_item(const DevMesh& m, long long it, i
   }
 }
 
-// Base edges and corners of the claimed faces, each averaged once: by the
-// first of its slots whose face is claimed in this epoch.  Item it of
-// nf * max_face_corners * (2*grid_size - 1): claimed face it / per_face,
-// corner (it % per_face) / (2*grid_size - 1), and j = the rest: the edge's
-// boundary index j + 1 for j < 2*grid_size - 2 (subdiv_ccg.c:1010-1048), the
-// corner's base vertex for the last j (:1081-1104).  The same edges and
-// vertices as the claimed edge and vertex lists of grid_claim_face, each item
-// independent of the others.
-__device__ __forceinline__ void grid_owner_seam_item(const DevMesh& m, long long it,
-                                                     unsigned int epoch) {
-  const int g2 = 2 * m.grid_size, per_corner = g2 - 1;
-  const int per_face = m.max_face_corners * per_corner;
-  const int f = __ldcg(&m.face_list[it / per_face]);
-  const int rem = static_cast<int>(it % per_face);
-  const int c = rem / per_corner, j = rem - c * per_corner;
-  if (c >= m.face_ngrids[f]) return;
-  const int s = m.face_start[f];
-  if (j < g2 - 2) {
-    const int e = m.face_edges[s + c];
-    const int f0 = m.edge_off[e], f1 = m.edge_off[e + 1];
-    if (f1 - f0 == 1) return;
-    int owner = -1;
-    for (int k = f0; k < f1 && owner < 0; k++)
-      if (__ldcg(&m.face_mark[m.edge_face[k]]) == epoch) owner = m.edge_face[k];
-    if (owner != f) return;
-    const int i = j + 1;
-    grid_average_set(m, f1 - f0, [&](int k) { return m.edge_elems[(long long)(f0 + k) * g2 + i]; });
-  } else {
-    const int v = m.face_verts[s + c];
-    const int f0 = m.bvert_off[v], f1 = m.bvert_off[v + 1];
-    if (f1 - f0 == 1) return;
-    int owner = -1;
-    for (int k = f0; k < f1 && owner < 0; k++)
-      if (__ldcg(&m.face_mark[m.bvert_face[k]]) == epoch) owner = m.bvert_face[k];
-    if (owner != f) return;
-    grid_average_set(m, f1 - f0, [&](int k) { return m.bvert_elems[f0 + k]; });
-  }
-}
-
 }  // namespace sgpu

@@ -38,6 +38,11 @@ namespace cg = cooperative_groups;
 namespace sgpu {
 
 constexpr int kTeamThreads = 256;
+// Shared staging region at the start of the dynamic shared memory: the smooth
+// neighbour tables, the area stage, or a claimed face's grids (never live at
+// the same time).
+constexpr size_t kStageBytes = 40960;
+static_assert(sizeof(float4) * kNbCache * kTeamThreads <= kStageBytes, "smooth tables");
 
 struct TeamShared {
   DevMesh m;
@@ -558,7 +563,7 @@ static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int
 // lane's elements arrive together instead of in dependent batches; lane t
 // then adds its elements t, t+256, ... of the stage in order.
 constexpr int kAreaStage = 1024;  // staged vertices per round: 32 KB (positions, normals)
-static_assert(2 * kAreaStage <= kNbCache * kTeamThreads, "the area stage exceeds the smooth tables");
+static_assert(2 * kAreaStage * sizeof(float4) <= kStageBytes, "the area stage");
 static __device__ void team_area_block(const DevMesh& m, const PassParams& pp, float rn2,
                                        float ra2, int leaf, int blk, float4* s_stage, Lane* sl,
                                        AreaPart* out) {
@@ -697,74 +702,196 @@ __device__ __forceinline__ void team_claim_faces(const DevMesh& m, const int* li
   }
 }
 
-// Grids of one face staged on chip at a time (positions and quad normals,
-// float3): the largest group of at most 4 grids whose tables fit in bytes.
+// Grids of one face staged on chip at a time: positions (float4), masks and
+// quad normals (float3); the largest group of at most 4 grids whose tables
+// fit in bytes.
+__host__ __device__ __forceinline__ size_t face_group_bytes(int grid_size, int group) {
+  const size_t area = static_cast<size_t>(grid_size) * grid_size;
+  const size_t quads = static_cast<size_t>(grid_size - 1) * (grid_size - 1);
+  return group * (16u * area + 4u * area + 12u * quads);
+}
 __host__ __device__ __forceinline__ int face_grid_group(int grid_size, size_t bytes) {
-  const size_t per = 12u * (static_cast<size_t>(grid_size) * grid_size +
-                            static_cast<size_t>(grid_size - 1) * (grid_size - 1));
-  const size_t g = bytes / per;
-  return g >= 4 ? 4 : static_cast<int>(g);
+  int g = 4;
+  while (g > 0 && face_group_bytes(grid_size, g) > bytes) g--;
+  return g;
+}
+
+// Normal of staged element i (grid i / area of the stage): the mean of the
+// staged normals of the quads around it, added in the order of
+// grid_element_normal (subdiv_ccg.c:707-737).
+__device__ __forceinline__ float3 staged_normal(const float3* s_q, int i, int gs, int area) {
+  const int g1 = gs - 1, c = i / area, e = i - c * area, y = e / gs, x = e - y * gs;
+  const float3* q = s_q + c * g1 * g1;
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  int counter = 0;
+  auto add = [&](const float3& v) {
+    ax += v.x, ay += v.y, az += v.z;
+    counter++;
+  };
+  if (x < g1 && y < g1) add(q[y * g1 + x]);
+  if (x >= 1) {
+    if (y < g1) add(q[y * g1 + x - 1]);
+    if (y >= 1) add(q[(y - 1) * g1 + x - 1]);
+  }
+  if (y >= 1 && x < g1) add(q[(y - 1) * g1 + x]);
+  const float inv = 1.0f / (float)counter;
+  return make_float3(ax * inv, ay * inv, az * inv);
 }
 
 // Inner normals, face-internal seams and the centre of one claimed face by
-// one CTA (subdiv_ccg.c:670-740 and 951-984).  The face's grids are staged
-// in shared memory (positions, then the normal_quad of every quad, computed
-// once: the per-element form evaluates a quad up to four times with the same
-// corners and the same result); each element normal is the mean of its
-// staged quad normals, added in the order of grid_element_normal.  The seam
-// pairs and the centre follow a CTA barrier, as the reference averages after
-// every inner normal (the seams move positions the inner normals read).
-// Faces are independent here: a face's grids hold their own copies of the
-// base-edge elements, which the base-edge pass averages afterwards.
-static __device__ void team_grid_face(const DevMesh& m, int f, float3* s_co, float3* s_q,
-                                      int group) {
+// one CTA (subdiv_ccg.c:670-740 and 951-984).  The face's grids are staged in
+// shared memory with cp.async (positions and masks), the normal_quad of every
+// quad is computed once (the per-element form evaluates a quad up to four
+// times with the same corners and the same result), and each element normal
+// is the mean of its staged quad normals, added in the order of
+// grid_element_normal.  The seam pairs and the centre then average the staged
+// positions and masks and the new normals, as the reference averages after
+// every inner normal; pairs and the centre touch disjoint elements, so each
+// reads the values the inner-normal step left.  Faces are independent here:
+// a face's grids hold their own copies of the base-edge elements, which the
+// base-edge pass averages afterwards.  GRIDS positions carry w = 0.
+static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* stage, int group) {
   const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area, qa = g1 * g1;
   const int s = m.face_start[f], n = m.face_ngrids[f];
+  float4* s_co = reinterpret_cast<float4*>(stage);
+  float* s_mk = reinterpret_cast<float*>(s_co + group * area);
+  float3* s_q = reinterpret_cast<float3*>(s_mk + group * area);  // quad normals
+  const bool whole = n <= group;  // the seams below read the stage
   for (int c0 = 0; c0 < n; c0 += group) {
     const int nc = min(group, n - c0);
     for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
-      const int c = i / area, e = i - c * area;
-      s_co[i] = xyz(__ldcg(&m.co[static_cast<size_t>(s + c0 + c) * area + e]));
+      const size_t e = static_cast<size_t>(s + c0) * area + i;
+      cp_async16(&s_co[i], &m.co[e]);
     }
+    cp_async_wait_all();
+    if (m.mask)
+      for (int i = threadIdx.x; i < nc * area; i += kTeamThreads)
+        s_mk[i] = __ldcg(&m.mask[static_cast<size_t>(s + c0) * area + i]);
     __syncthreads();
     for (int i = threadIdx.x; i < nc * qa; i += kTeamThreads) {
       const int c = i / qa, q = i - c * qa, qy = q / g1, qx = q - qy * g1;
-      const float3* p = s_co + c * area;
+      const float4* p = s_co + c * area;
       // quad (qx, qy): corners (qx, qy+1), (qx+1, qy+1), (qx+1, qy), (qx, qy)
-      s_q[i] = normal_quad(p[(qy + 1) * gs + qx], p[(qy + 1) * gs + qx + 1], p[qy * gs + qx + 1],
-                           p[qy * gs + qx]);
+      s_q[i] = normal_quad(xyz(p[(qy + 1) * gs + qx]), xyz(p[(qy + 1) * gs + qx + 1]),
+                           xyz(p[qy * gs + qx + 1]), xyz(p[qy * gs + qx]));
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
-      const int c = i / area, e = i - c * area, y = e / gs, x = e - y * gs;
-      const float3* q = s_q + c * qa;
-      float ax = 0.0f, ay = 0.0f, az = 0.0f;
-      int counter = 0;
-      auto add = [&](const float3& v) {
-        ax += v.x, ay += v.y, az += v.z;
-        counter++;
-      };
-      if (x < g1 && y < g1) add(q[y * g1 + x]);
-      if (x >= 1) {
-        if (y < g1) add(q[y * g1 + x - 1]);
-        if (y >= 1) add(q[(y - 1) * g1 + x - 1]);
-      }
-      if (y >= 1 && x < g1) add(q[(y - 1) * g1 + x]);
-      const float inv = 1.0f / (float)counter;
-      m.no[static_cast<size_t>(s + c0 + c) * area + e] = make_float4(ax * inv, ay * inv, az * inv, 0.0f);
+      const float3 nv = staged_normal(s_q, i, gs, area);
+      m.no[static_cast<size_t>(s + c0) * area + i] = make_float4(nv.x, nv.y, nv.z, 0.0f);
     }
-    __syncthreads();  // the normals are written; the staging tables are free again
+    __syncthreads();  // a next group restages after this barrier
   }
   const int pairs = n * g1;
-  for (int it = threadIdx.x; it <= pairs; it += kTeamThreads) {
-    if (it < pairs) {
-      const int c = it / g1, i = 1 + (it - c * g1);
-      const int g = s + c, prev = s + (c + n - 1) % n;
-      grid_avg_pair(m, prev * area + i, g * area + i * gs);
-    } else {
-      grid_average_set(m, n, [&](int c) { return (s + c) * area; });
+  if (whole) {
+    // pairs and the centre from the stage
+    auto avg_pair = [&](int ia, int ib) {
+      const float4 ca = s_co[ia], cb = s_co[ib];
+      const float3 na = staged_normal(s_q, ia, gs, area), nb = staged_normal(s_q, ib, gs, area);
+      float4 c;
+      c.x = (ca.x + cb.x) * 0.5f;
+      c.y = (ca.y + cb.y) * 0.5f;
+      c.z = (ca.z + cb.z) * 0.5f;
+      c.w = ca.w;
+      const float4 nn = make_float4((na.x + nb.x) * 0.5f, (na.y + nb.y) * 0.5f,
+                                    (na.z + nb.z) * 0.5f, 0.0f);
+      const size_t ga = static_cast<size_t>(s) * area + ia, gb = static_cast<size_t>(s) * area + ib;
+      m.co[ga] = c;
+      m.co[gb] = c;
+      m.no[ga] = nn;
+      m.no[gb] = nn;
+      if (m.mask) {
+        const float mk = (s_mk[ia] + s_mk[ib]) * 0.5f;
+        m.mask[ga] = mk;
+        m.mask[gb] = mk;
+      }
+    };
+    for (int it = threadIdx.x; it <= pairs; it += kTeamThreads) {
+      if (it < pairs) {
+        const int c = it / g1, i = 1 + (it - c * g1);
+        const int prev = (c + n - 1) % n;
+        avg_pair(prev * area + i, c * area + i * gs);
+      } else {
+        // GridElementAccumulator over element 0 of every grid, in grid order
+        float cx = 0.0f, cy = 0.0f, cz = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f, mk = 0.0f;
+        for (int c = 0; c < n; c++) {
+          const float4 co = s_co[c * area];
+          const float3 no = staged_normal(s_q, c * area, gs, area);
+          cx += co.x, cy += co.y, cz += co.z;
+          nx += no.x, ny += no.y, nz += no.z;
+          if (m.mask) mk += s_mk[c * area];
+        }
+        const float inv = 1.0f / (float)n;
+        cx *= inv, cy *= inv, cz *= inv;
+        nx *= inv, ny *= inv, nz *= inv;
+        mk *= inv;
+        for (int c = 0; c < n; c++) {
+          const size_t e = static_cast<size_t>(s + c) * area;
+          m.co[e] = make_float4(cx, cy, cz, s_co[c * area].w);
+          m.no[e] = make_float4(nx, ny, nz, 0.0f);
+          if (m.mask) m.mask[e] = mk;
+        }
+      }
+    }
+  } else {
+    // more grids than one stage holds: the seams from global memory (the
+    // normals written above are visible to the CTA after the barrier)
+    for (int it = threadIdx.x; it <= pairs; it += kTeamThreads) {
+      if (it < pairs) {
+        const int c = it / g1, i = 1 + (it - c * g1);
+        const int g = s + c, prev = s + (c + n - 1) % n;
+        grid_avg_pair(m, prev * area + i, g * area + i * gs);
+      } else {
+        grid_average_set(m, n, [&](int c) { return (s + c) * area; });
+      }
     }
   }
+}
+
+// Base edges and corners of one claimed face by one CTA: each base edge and
+// base vertex is averaged once, by the first of its faces (slot order) that
+// is claimed in this epoch (subdiv_ccg.c:1010-1048, 1081-1104); the owner
+// decisions of the face's corners are made first, one thread per corner.
+static __device__ void team_grid_face_boundary(const DevMesh& m, int f, unsigned int epoch,
+                                               unsigned char* stage) {
+  const int g2 = 2 * m.grid_size, per_corner = g2 - 1;
+  const int s = m.face_start[f], n = m.face_ngrids[f];
+  int* s_edge = reinterpret_cast<int*>(stage);  // per corner: edge owned (or -1), vertex owned (or -1)
+  int* s_vert = s_edge + n;
+  for (int c = threadIdx.x; c < n; c += kTeamThreads) {
+    const int e = m.face_edges[s + c];
+    int f0 = m.edge_off[e], f1 = m.edge_off[e + 1];
+    int owner = -1;
+    if (f1 - f0 > 1)
+      for (int k = f0; k < f1 && owner < 0; k++)
+        if (__ldcg(&m.face_mark[m.edge_face[k]]) == epoch) owner = m.edge_face[k];
+    s_edge[c] = owner == f ? e : -1;
+    const int v = m.face_verts[s + c];
+    f0 = m.bvert_off[v];
+    f1 = m.bvert_off[v + 1];
+    owner = -1;
+    if (f1 - f0 > 1)
+      for (int k = f0; k < f1 && owner < 0; k++)
+        if (__ldcg(&m.face_mark[m.bvert_face[k]]) == epoch) owner = m.bvert_face[k];
+    s_vert[c] = owner == f ? v : -1;
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < n * per_corner; it += kTeamThreads) {
+    const int c = it / per_corner, j = it - c * per_corner;
+    if (j < g2 - 2) {
+      const int e = s_edge[c];
+      if (e < 0) continue;
+      const int f0 = m.edge_off[e], f1 = m.edge_off[e + 1];
+      const int i = j + 1;
+      grid_average_set(m, f1 - f0, [&](int k) { return m.edge_elems[(long long)(f0 + k) * g2 + i]; });
+    } else {
+      const int v = s_vert[c];
+      if (v < 0) continue;
+      const int f0 = m.bvert_off[v], f1 = m.bvert_off[v + 1];
+      grid_average_set(m, f1 - f0, [&](int k) { return m.bvert_elems[f0 + k]; });
+    }
+  }
+  __syncthreads();  // the corner tables are free again
 }
 
 // Team barrier.  A cluster team uses barrier.cluster (cluster.sync():
@@ -899,7 +1026,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
   __shared__ Lane s_chunks[kTeamMaxChunks];
   extern __shared__ __align__(16) unsigned char dyn[];
   float4* s_nbc = reinterpret_cast<float4*>(dyn);  // smooth neighbour tables
-  int* s_par = reinterpret_cast<int*>(s_nbc + kNbCache * kTeamThreads);
+  int* s_par = reinterpret_cast<int*>(dyn + kStageBytes);
   int* s_cl = s_par + a.max_nodes;
   int* s_coff = s_cl + a.max_leaves + 1;
   int* s_lnv = s_coff + a.max_leaves + 2;
@@ -1274,13 +1401,11 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         // then the base edges and corners (positions move at the seams, so
         // the refit below follows).
         const int nf = __ldcg(&m.grid_counts[0]);
-        const int group = face_grid_group(m.grid_size, sizeof(float4) * kNbCache * kTeamThreads);
+        const int group = face_grid_group(m.grid_size, kStageBytes);
         if (group > 0) {
-          float3* s_co = reinterpret_cast<float3*>(s_nbc);
-          float3* s_q = s_co + group * m.grid_area;
           for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C)) {
             const int f = __ldcg(&m.face_list[fi]);
-            team_grid_face(m, f, s_co, s_q, group);
+            team_grid_face(m, f, dyn, group);
             if (threadIdx.x == 0) {
               const int n = m.face_ngrids[f];
               // positions read, normals written; the seam pairs and the
@@ -1308,8 +1433,8 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           }
           TEAM_SYNC();
         }
-        const long long items = (long long)nf * m.max_face_corners * (2 * m.grid_size - 1);
-        for (long long it = gt; it < items; it += GT) grid_owner_seam_item(m, it, epoch);
+        for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C))
+          team_grid_face_boundary(m, __ldcg(&m.face_list[fi]), epoch, dyn);
         TEAM_SYNC();
         clk.mark(a, rank, kPhGridSeams);
         if (rank == 0 && threadIdx.x == 0)

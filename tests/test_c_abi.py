@@ -41,7 +41,7 @@ def test_c_caller_compiles_and_links():
 @pytest.mark.gpu
 @pytest.mark.parametrize("symmetry", [0, synth.SYMM_X])
 def test_c_caller_matches_oracle(gpu, oracle, symmetry):
-    m = small_icosphere(5)
+    m = small_icosphere(5, masked=False)  # the C caller passes no mask
     ll = 600
     st = synth.Stroke(synth.TOOL_DRAW, 0.15, 0.5, synth.CURVE_SMOOTH, symmetry,
                       synth.arc_dabs(11, 16, 0.04))
