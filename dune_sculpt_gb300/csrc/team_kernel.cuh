@@ -846,6 +846,7 @@ static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* st
       }
     }
   }
+  __syncthreads();  // the stage is read: the CTA's next face may restage it
 }
 
 // Base edges and corners of one claimed face by one CTA: each base edge and
