@@ -108,6 +108,8 @@ def parse_args():
                          "workloads (one JSON line each), no report")
     ap.add_argument("--batched-only", action="store_true",
                     help="the batched clay / multires legs only, one JSON line")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="the 64-mesh batch leg only (no CPU baseline), one JSON line")
     return ap.parse_args()
 
 
@@ -713,6 +715,12 @@ def stroke_alg_bytes(g, st, tools=None) -> float:
     return sum(p["bytes"] for p in phases.values())
 
 
+def _team_kernel(shape) -> str:
+    """The kernel a batch team shape launches."""
+    from dune_sculpt_gb300.sculpt import TEAM_LOCKSTEP
+    return "k_lock_stroke" if shape[0] == TEAM_LOCKSTEP else "k_team_stroke"
+
+
 def run_batch(synth, PBVH, batch_stroke, autotune_batch, BATCH_TEAM, BATCH_SEQUENTIAL, peak,
               no_cpu=False, steps: int = 5):
     """The 64-mesh uneven batch: one persistent launch on the batch autotuner's
@@ -755,7 +763,7 @@ def run_batch(synth, PBVH, batch_stroke, autotune_batch, BATCH_TEAM, BATCH_SEQUE
            "sequential_plain": {"value": seq_disp / (seq_ms / 1e3), "unit": UNIT,
                                 "ms_per_step": seq_ms},
            "speedup": (disp / ms) / (seq_disp / seq_ms),
-           "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "alg_bytes": alg,
+           "roofline": {"bound": "hbm", "kernel": _team_kernel(shape), "alg_bytes": alg,
                         "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak},
            "autotune_ms": {f"{c[0]}x{c[1]}": round(t, 3) for c, t in tune.items()}}
@@ -838,7 +846,7 @@ def run_batched(K: int, peak, no_cpu=False, steps: int = 3):
                      "strokes": K, "value": disp / (ms / 1e3), "unit": UNIT,
                      "ms_per_batch": ms,
                      "team": {"cluster": shape[0], "ctas_per_sm": shape[1]},
-                     "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "alg_bytes": alg,
+                     "roofline": {"bound": "hbm", "kernel": _team_kernel(shape), "alg_bytes": alg,
                                   "achieved": achieved, "peak": peak, "unit": "GB/s",
                                   "frac": achieved / peak},
                      "one_after_another": {"value": single_v / (single_ms / 1e3), "unit": UNIT,
@@ -935,6 +943,17 @@ def main():
         return run_quick(args)
     if args.phases:
         return run_phases(args)
+    if args.batch_only:
+        from dune_sculpt_gb300 import build as libbuild
+
+        libbuild.build()
+        from dune_sculpt_gb300 import synth
+        from dune_sculpt_gb300.sculpt import (BATCH_SEQUENTIAL, BATCH_TEAM, PBVH, autotune_batch,
+                                              batch_stroke)
+
+        print(json.dumps(run_batch(synth, PBVH, batch_stroke, autotune_batch, BATCH_TEAM,
+                                   BATCH_SEQUENTIAL, measured_peaks()[0], no_cpu=True)))
+        return 0
     if args.batched_only:
         from dune_sculpt_gb300 import build as libbuild
 

@@ -62,6 +62,8 @@ constexpr unsigned long long kDefaultWaitNs = 2000000000ull;
 std::atomic<long long> g_inject_alloc{0};
 std::atomic<unsigned long long> g_wait_ns{kDefaultWaitNs};
 std::atomic<int> g_bar_extra{0};
+// Test hook: CTAs per SM of every lockstep launch (0: the team shape's).
+std::atomic<int> g_lock_per_sm{0};
 
 bool injected_alloc_failure() {
   long long n = g_inject_alloc.load();
@@ -123,7 +125,10 @@ struct sgpu_mesh {
   float* t_dabs = nullptr;
   int* t_tools = nullptr;
   int* t_counter = nullptr;
+  LockJob* t_lock = nullptr;     // lockstep launch: per-job state
+  DevBrush* t_lbrush = nullptr;  // and per-job brushes
   size_t t_dab_cap = 0, t_tool_cap = 0, t_mesh_cap = 0, t_job_cap = 0, t_counter_cap = 0;
+  size_t t_lock_cap = 0, t_lbrush_cap = 0;
   // page-locked displaced counters of the last persistent launch
   unsigned long long* h_disp = nullptr;
   size_t h_disp_cap = 0;
@@ -217,8 +222,12 @@ struct sgpu_mesh {
     allocs.clear();
     for (void* p : {static_cast<void*>(t_meshes), static_cast<void*>(t_jobs),
                     static_cast<void*>(t_dabs), static_cast<void*>(t_tools),
-                    static_cast<void*>(t_counter)})
+                    static_cast<void*>(t_counter), static_cast<void*>(t_lock),
+                    static_cast<void*>(t_lbrush)})
       if (p) cudaFree(p);
+    t_lock = nullptr;
+    t_lbrush = nullptr;
+    t_lock_cap = t_lbrush_cap = 0;
     t_meshes = nullptr;
     t_jobs = nullptr;
     t_dabs = nullptr;
@@ -277,6 +286,7 @@ int upload_pbvh(sgpu_mesh* m) {
   const int N = h.totnode, L = static_cast<int>(h.leaf_nodes.size());
   d.totnode = N;
   d.nleaf = L;
+  d.max_leaf_verts = d.max_leaf_chunks = 0;
   d.nlevels = static_cast<int>(h.level_off.size()) - 1;
   std::vector<float4> vb(2 * static_cast<size_t>(N));
   for (int n = 0; n < N; n++) {
@@ -336,6 +346,7 @@ int upload_pbvh(sgpu_mesh* m) {
       const int nall = h.type == kFaces ? h.uniq[node] + h.face_verts_n[node]
                                         : h.totprim[node] * h.grid_area;
       choff[k + 1] = choff[k] + (nall + kChunk - 1) / kChunk;
+      d.max_leaf_chunks = std::max(d.max_leaf_chunks, choff[k + 1] - choff[k]);
     }
     if ((rc = m->upload(&d.leaf_chunk_off, choff))) return rc;
     if ((rc = m->alloc(&d.chunk_box, 2 * static_cast<size_t>(choff[L]) + 2))) return rc;
@@ -347,7 +358,9 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->alloc(&d.hit_list[0], nslot))) return rc;
   if ((rc = m->alloc(&d.hit_list[1], static_cast<size_t>(h.totvert)))) return rc;
   if ((rc = m->alloc(&d.tag_list, static_cast<size_t>(h.totvert)))) return rc;
-  if ((rc = m->alloc(&d.touch_list, L + 1))) return rc;
+  // a leaf flagged before a stroke (update pending) is listed at the stroke
+  // start and may be listed again when the first dab marks it
+  if ((rc = m->alloc(&d.touch_list, 2 * static_cast<size_t>(L) + 2))) return rc;
   if ((rc = m->alloc(&d.work, 1))) return rc;
   if ((rc = m->alloc(&d.cull_list, L + 1))) return rc;
   if ((rc = m->alloc(&d.cull_off, L + 2))) return rc;
@@ -357,6 +370,7 @@ int upload_pbvh(sgpu_mesh* m) {
       const int node = h.leaf_nodes[k];
       const int nv = h.type == kFaces ? h.uniq[node] : h.totprim[node] * h.grid_area;
       blocks = std::max(blocks, (nv + kAreaBlock - 1) / kAreaBlock);
+      d.max_leaf_verts = std::max(d.max_leaf_verts, nv);
     }
     d.area_blocks = blocks;
   }
@@ -1351,24 +1365,29 @@ int sgpu_stroke(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs, 
   return finish_stroke(mesh, mode, launches, stats);
 }
 
-int sgpu_stroke_team_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
-                             int ndabs, const int* dab_tools, SGPU_TeamProfile* out,
-                             SGPU_StrokeStats* stats) {
-  int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
-  if (rc) return rc;
-  if (!out) return fail(SGPU_ERR_INVALID_ARG, "NULL profile");
+// Strokes of one batch run concurrently: a mesh may appear once.
+static int check_distinct(sgpu_mesh* const* meshes, int n) {
+  std::vector<const sgpu_mesh*> v(meshes, meshes + n);
+  std::sort(v.begin(), v.end());
+  for (int i = 0; i < n; i++) {
+    if (!v[i]) return fail(SGPU_ERR_INVALID_ARG, "NULL mesh in the batch");
+    if (i > 0 && v[i] == v[i - 1]) return fail(SGPU_ERR_INVALID_ARG, "a mesh appears twice in the batch");
+  }
+  return SGPU_OK;
+}
+
+// One persistent launch with the phase counters armed; fills out.
+static int profiled_team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes,
+                               const SGPU_Dab* dabs, const int* offs, const int* tools,
+                               TeamShape shape, SGPU_TeamProfile* out, SGPU_StrokeStats* stats) {
   unsigned long long* counters = nullptr;
+  cudaStream_t s = meshes[0]->stream;
   CK(cudaMalloc(&counters, sizeof(unsigned long long) * 2 * kTeamPhases), "cudaMalloc");
-  CK(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2 * kTeamPhases, mesh->stream),
-     "memset");
+  CK(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2 * kTeamPhases, s), "memset");
   g_team_prof_bytes = counters;
   g_team_phase_ns = counters + kTeamPhases;
-  const int offs[2] = {0, ndabs};
-  sgpu_mesh* one[1] = {mesh};
   float total = 0.0f;
-  SGPU_StrokeStats st;
-  rc = team_batch(one, 1, brush, dabs, offs, dab_tools, mesh_team(mesh, brush, dab_tools, ndabs),
-                  mesh->stream, &st, &total);
+  int rc = team_batch(meshes, n, brushes, dabs, offs, tools, shape, s, stats, &total);
   g_team_prof_bytes = nullptr;
   g_team_phase_ns = nullptr;
   unsigned long long host[2 * kTeamPhases] = {};
@@ -1381,8 +1400,48 @@ int sgpu_stroke_team_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGP
     out->phase_bytes[k] = static_cast<double>(host[k]);
     out->phase_ms[k] = static_cast<double>(host[kTeamPhases + k]) * 1e-6;
   }
+  return SGPU_OK;
+}
+
+int sgpu_stroke_team_profile(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* dabs,
+                             int ndabs, const int* dab_tools, SGPU_TeamProfile* out,
+                             SGPU_StrokeStats* stats) {
+  int rc = validate_stroke(mesh, brush, dabs, ndabs, dab_tools);
+  if (rc) return rc;
+  if (!out) return fail(SGPU_ERR_INVALID_ARG, "NULL profile");
+  const int offs[2] = {0, ndabs};
+  sgpu_mesh* one[1] = {mesh};
+  SGPU_StrokeStats st;
+  rc = profiled_team_batch(one, 1, brush, dabs, offs, dab_tools,
+                           mesh_team(mesh, brush, dab_tools, ndabs), out, &st);
+  if (rc) return rc;
   if (stats) *stats = st;
   return SGPU_OK;
+}
+
+int sgpu_batch_team_profile(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes,
+                            const SGPU_Dab* dabs, const int* dab_offsets, const int* dab_tools,
+                            int cluster_size, SGPU_TeamProfile* out, SGPU_StrokeStats* stats) {
+  if (!meshes || nmesh <= 0 || !brushes || !dab_offsets)
+    return fail(SGPU_ERR_INVALID_ARG, "NULL or empty batch");
+  if (!out) return fail(SGPU_ERR_INVALID_ARG, "NULL profile");
+  if (int rc = check_distinct(meshes, nmesh)) return rc;
+  for (int i = 0; i < nmesh; i++) {
+    const int nd = dab_offsets[i + 1] - dab_offsets[i];
+    int rc = validate_stroke(meshes[i], &brushes[i], dabs + dab_offsets[i], nd,
+                             dab_tools ? dab_tools + dab_offsets[i] : nullptr);
+    if (rc) return rc;
+  }
+  for (int i = 0; i < nmesh; i++) CK(cudaStreamSynchronize(meshes[i]->stream), "sync");
+  TeamShape shape{cluster_size, 0};
+  if (cluster_size == 0) {
+    shape = TeamShape{meshes[0]->team_cluster, meshes[0]->team_build};
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const auto it = g_tune.find(batch_key(meshes, nmesh, brushes, dab_offsets, dab_tools));
+    if (it != g_tune.end()) shape = it->second;
+  }
+  return profiled_team_batch(meshes, nmesh, brushes, dabs, dab_offsets, dab_tools, shape, out,
+                             stats);
 }
 
 int sgpu_mesh_set_team(sgpu_mesh* mesh, int cluster_size) {
@@ -1410,6 +1469,10 @@ int sgpu_debug_inject(int what, int64_t value) {
     case SGPU_INJECT_BARRIER_EXTRA:
       if (value < 0 || value > 1) return fail(SGPU_ERR_INVALID_ARG, "barrier extra must be 0 or 1");
       g_bar_extra.store(static_cast<int>(value));
+      return SGPU_OK;
+    case SGPU_DEBUG_LOCKSTEP_PER_SM:
+      if (value < 0 || value > 2) return fail(SGPU_ERR_INVALID_ARG, "CTAs per SM must be 0, 1 or 2");
+      g_lock_per_sm.store(static_cast<int>(value));
       return SGPU_OK;
     default:
       return fail(SGPU_ERR_INVALID_ARG, "unknown injection hook %d", what);
@@ -1476,6 +1539,7 @@ int sgpu_autotune_batch(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes
                         int* r_cluster, int* r_ctas_per_sm, float* r_ms) {
   if (!meshes || nmesh <= 0 || !brushes || !dab_offsets)
     return fail(SGPU_ERR_INVALID_ARG, "NULL or empty batch");
+  if (int rc = check_distinct(meshes, nmesh)) return rc;
   for (int i = 0; i < nmesh; i++) {
     const int nd = dab_offsets[i + 1] - dab_offsets[i];
     int rc = validate_stroke(meshes[i], &brushes[i], dabs + dab_offsets[i], nd,
@@ -1491,7 +1555,8 @@ int sgpu_autotune_batch(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes
     max_leaves = std::max(max_leaves, meshes[i]->dev.nleaf);
   }
   const TeamShape cand[SGPU_AUTOTUNE_BATCH_CANDIDATES] = {
-      {16, 1}, {8, 1}, {8, 2}, {4, 1}, {4, 2}, {2, 2}, {SGPU_TEAM_GRID, 1}};
+      {16, 1}, {8, 1}, {8, 2}, {4, 1}, {4, 2}, {2, 2}, {SGPU_TEAM_GRID, 1}, {SGPU_TEAM_LOCKSTEP, 1},
+      {SGPU_TEAM_LOCKSTEP, 2}};
   TeamShape best{8, 0};
   float best_ms = -1.0f;
   auto restore_all = [&]() -> int {
@@ -1504,17 +1569,21 @@ int sgpu_autotune_batch(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes
   for (int k = 0; k < SGPU_AUTOTUNE_BATCH_CANDIDATES; k++) {
     const TeamShape& c = cand[k];
     float ms = -1.0f;
-    const bool ok = c.cluster == SGPU_TEAM_GRID
-                        ? team_wide_ctas(max_nodes, max_leaves) > 0
-                        : team_max_active_clusters(c.cluster, max_nodes, max_leaves) > 0;
+    const bool ok = c.cluster == SGPU_TEAM_GRID       ? team_wide_ctas(max_nodes, max_leaves) > 0
+                    : c.cluster == SGPU_TEAM_LOCKSTEP ? lock_ctas(max_nodes, max_leaves, c.ctas_per_sm) > 0
+                    : team_max_active_clusters(c.cluster, max_nodes, max_leaves) > 0;
     if (ok) {
       for (int trial = 0; trial < 2; trial++) {
         if ((rc = restore_all())) return rc;
         float total = 0.0f;
         rc = team_batch(meshes, nmesh, brushes, dabs, dab_offsets, dab_tools, c,
                         meshes[0]->stream, nullptr, &total);
-        if (rc == SGPU_ERR_CUDA && c.cluster != SGPU_TEAM_GRID) {
+        if (rc == SGPU_ERR_CUDA && c.cluster > 0) {
           ms = -1.0f;  // this build holds no team of this size on the device
+          break;
+        }
+        if (rc == SGPU_ERR_UNSUPPORTED && c.cluster == SGPU_TEAM_LOCKSTEP) {
+          ms = -1.0f;  // the batch has dabs or grids the lockstep launch does not take
           break;
         }
         if (rc) return rc;
@@ -1542,6 +1611,7 @@ int sgpu_batch_stroke(sgpu_mesh** meshes, int nmesh, const SGPU_Brush* brushes,
                       int mode, int cluster_size, SGPU_StrokeStats* stats, float* r_total_ms) {
   if (!meshes || nmesh <= 0 || !brushes || !dab_offsets)
     return fail(SGPU_ERR_INVALID_ARG, "NULL or empty batch");
+  if (int rc = check_distinct(meshes, nmesh)) return rc;
   for (int i = 0; i < nmesh; i++) {
     const int nd = dab_offsets[i + 1] - dab_offsets[i];
     int rc = validate_stroke(meshes[i], &brushes[i], dabs + dab_offsets[i], nd,
@@ -2131,8 +2201,44 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
       team_smem_bytes(max_nodes, max_leaves) > 160 * 1024)
     return fail(SGPU_ERR_UNSUPPORTED, "PBVH too large for the persistent stroke kernel");
   const bool wide = cluster == SGPU_TEAM_GRID;
-  int wide_ctas = 0;
-  if (wide) {
+  const bool lock = cluster == SGPU_TEAM_LOCKSTEP;
+  int wide_ctas = 0, lock_per_sm = 1;
+  if (lock) {
+    if (n > kLockMaxJobs)
+      return fail(SGPU_ERR_UNSUPPORTED, "the lockstep launch takes at most %d meshes", kLockMaxJobs);
+    for (int i = 0; i < n; i++) {
+      if (h_orig[i])
+        return fail(SGPU_ERR_UNSUPPORTED,
+                    "the lockstep launch runs no grab, elastic deform or layer dabs");
+      const DevMesh& d = meshes[i]->dev;
+      if (d.type == kGrids && !lock_grids_fit(d.grid_size))
+        return fail(SGPU_ERR_UNSUPPORTED, "grids of %d x %d do not fit the lockstep launch's stage",
+                    d.grid_size, d.grid_size);
+    }
+    // every pooled item space fits an int, even with every leaf culled
+    double runs = 0.0, parts = 0.0, chunks = 0.0, verts = 0.0;
+    for (int i = 0; i < n; i++) {
+      const DevMesh& d = meshes[i]->dev;
+      runs += static_cast<double>(d.nleaf) * ((d.max_leaf_verts + 31) / 32);
+      parts += static_cast<double>(d.nleaf) * d.area_blocks;
+      chunks += static_cast<double>(d.nleaf) * d.max_leaf_chunks;
+      verts += static_cast<double>(d.totvert) + d.num_faces;
+    }
+    if (std::max(std::max(runs, parts), std::max(chunks, verts)) >= 2147483647.0)
+      return fail(SGPU_ERR_UNSUPPORTED, "batch too large for one lockstep launch");
+    if (shape.ctas_per_sm != 0 && shape.ctas_per_sm != 1 && shape.ctas_per_sm != 2)
+      return fail(SGPU_ERR_INVALID_ARG, "CTAs per SM must be 1 or 2");
+    lock_per_sm = g_lock_per_sm.load() ? g_lock_per_sm.load() : (shape.ctas_per_sm == 2 ? 2 : 1);
+    wide_ctas = lock_ctas(max_nodes, max_leaves, lock_per_sm);
+    if (wide_ctas <= 0)
+      return fail(SGPU_ERR_UNSUPPORTED, "the lockstep launch cannot run on this device");
+    // barriers: at most 8 passes of at most 8 per dab, 4 more per dab, 1 at
+    // the start
+    int maxd = 0;
+    for (int i = 0; i < n; i++) maxd = std::max(maxd, offs[i + 1] - offs[i]);
+    if ((72.0 * maxd + 8.0) * (wide_ctas + 1) >= 2147483648.0)
+      return fail(SGPU_ERR_UNSUPPORTED, "too many dabs for one lockstep launch");
+  } else if (wide) {
     wide_ctas = team_wide_ctas(max_nodes, max_leaves);
     if (wide_ctas <= 0)
       return fail(SGPU_ERR_UNSUPPORTED, "the whole-GPU team cannot be launched on this device");
@@ -2159,6 +2265,10 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   if ((rc = ensure_dev(&m0->t_jobs, &m0->t_job_cap, static_cast<size_t>(n)))) return rc;
   // [0] job counter, [1] whole-GPU barrier counter, [2] status word
   if ((rc = ensure_dev(&m0->t_counter, &m0->t_counter_cap, 4))) return rc;
+  if (lock) {
+    if ((rc = ensure_dev(&m0->t_lock, &m0->t_lock_cap, static_cast<size_t>(n)))) return rc;
+    if ((rc = ensure_dev(&m0->t_lbrush, &m0->t_lbrush_cap, static_cast<size_t>(n)))) return rc;
+  }
   std::vector<int> order(n);
   std::vector<double> est(n);
   for (int i = 0; i < n; i++) {
@@ -2202,6 +2312,15 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   CK(cudaMemcpyAsync(m0->t_jobs, h_jobs.data(), sizeof(TeamJob) * n, cudaMemcpyHostToDevice, s),
      "upload jobs");
   CK(cudaMemsetAsync(m0->t_counter, 0, 3 * sizeof(int), s), "reset job and barrier counters");
+  if (lock) {
+    static thread_local std::vector<DevBrush> h_lbrush;
+    h_lbrush.resize(n);
+    for (int j = 0; j < n; j++) h_lbrush[j] = h_jobs[j].brush;
+    CK(cudaMemcpyAsync(m0->t_lbrush, h_lbrush.data(), sizeof(DevBrush) * n, cudaMemcpyHostToDevice,
+                       s),
+       "upload brushes");
+    CK(cudaMemsetAsync(m0->t_lock, 0, sizeof(LockJob) * n, s), "reset lockstep state");
+  }
   for (int i = 0; i < n; i++)
     CK(cudaMemsetAsync(&meshes[i]->dev.work->displaced, 0, sizeof(unsigned long long), s),
        "reset counter");
@@ -2220,7 +2339,12 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.status = m0->t_counter + 2;
   a.wait_ns = g_wait_ns.load();
   a.bar_extra = g_bar_extra.load();
-  if (wide) {
+  a.lock = lock ? m0->t_lock : nullptr;
+  a.lbrush = lock ? m0->t_lbrush : nullptr;
+  if (lock) {
+    CK(launch_lock_stroke(a, wide_ctas, lock_per_sm, s),
+       "persistent stroke kernel (lockstep batch)");
+  } else if (wide) {
     CK(launch_team_stroke_wide(a, wide_ctas, s), "persistent stroke kernel (whole GPU)");
   } else {
     CK(launch_team_stroke(a, cluster, s, shape.ctas_per_sm), "persistent stroke kernel");

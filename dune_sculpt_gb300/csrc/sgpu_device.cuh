@@ -127,6 +127,8 @@ struct DevMesh {
   int* cull_off;   // nleaf+1: prefix of brush-visible vertex counts over cull_list
   AreaPart* parts;  // nleaf * area_blocks
   int area_blocks;  // blocks of kAreaBlock visited vertices per leaf in the area reduction
+  int max_leaf_verts;   // largest brush-visible vertex count of a leaf
+  int max_leaf_chunks;  // largest refit chunk count of a leaf
   float4* scratch;   // smooth Jacobi values, totvert
   float4* scratch2;  // second value buffer of the slot sweeps, totvert
   int* slot_map[2];  // vertex -> smooth slot of a pass, or -1; passes alternate

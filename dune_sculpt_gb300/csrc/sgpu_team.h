@@ -20,6 +20,18 @@ struct TeamJob {
   DevBrush brush;     // brush.tool: the default tool
 };
 
+// Per-job state of the lockstep batch launch (k_lock_stroke), in device
+// memory, zeroed by the host before the launch.
+struct LockJob {
+  PassParams pp;       // the job's current symmetry pass (written by its cull CTA)
+  BrushFrame frame;    // brush frame of the pass
+  int cnt, total;      // culled leaves and their brush-visible vertices
+  int go;              // 1: the pass moves vertices (frame valid, leaves marked)
+  unsigned int ticket;  // area items of the pass finished (the last one reduces)
+  int nh[3];           // smooth hits, by the job's smooth pass number mod 3
+  int pad;
+};
+
 struct TeamArgs {
   const DevMesh* meshes;
   const TeamJob* jobs;
@@ -37,6 +49,10 @@ struct TeamArgs {
   // profiling (nullable): algorithmic bytes and nanoseconds per phase
   unsigned long long* prof_bytes;  // kTeamPhases entries
   unsigned long long* phase_ns;    // kTeamPhases entries
+  // lockstep batch launch only: per-job state and per-job brush (the tool of
+  // the current dab is written into it)
+  LockJob* lock;
+  DevBrush* lbrush;
 };
 
 // Phases of a dab in the persistent kernel (profiling).
@@ -66,5 +82,19 @@ int team_wide_ctas(int max_nodes, int max_leaves);
 // Upper bound of team_wide_ctas on any device (sizes the smooth slot arrays).
 constexpr int kTeamMaxWideCtas = 1024;
 cudaError_t launch_team_stroke_wide(const TeamArgs& a, int nctas, cudaStream_t s);
+
+// Lockstep batch launch (kernels_lock.cu): every CTA of one cooperative
+// launch (one per SM) runs every stroke of the batch, dab by dab; each phase
+// pools the work items of all meshes (leaf blocks, claimed faces, touched
+// leaf chunks, tagged vertices) over the whole GPU.  Jobs run no grab,
+// elastic deform or layer dabs; GRIDS faces must fit the on-chip stage.
+constexpr int kLockMaxJobs = 1024;
+size_t lock_smem_bytes(int max_nodes, int max_leaves);
+// CTAs of the launch with per_sm (1 or 2) CTAs on every SM, or 0 when the
+// device cannot hold it.
+int lock_ctas(int max_nodes, int max_leaves, int per_sm);
+cudaError_t launch_lock_stroke(const TeamArgs& a, int nctas, int per_sm, cudaStream_t s);
+// Whether a claimed face's grids of this size fit the on-chip stage.
+bool lock_grids_fit(int grid_size);
 
 }  // namespace sgpu

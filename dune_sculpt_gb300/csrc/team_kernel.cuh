@@ -162,7 +162,8 @@ static __device__ unsigned long long team_block_scan64(unsigned long long v, uns
   return warp_base + x - v;
 }
 
-// Per-job tables of the node search in shared memory.
+// Per-job tables of the node search in shared memory (any type with the same
+// two indexable members serves).
 struct CullTabs {
   const unsigned short* lnode;  // leaf -> node
   const int* lnv;               // leaf -> brush-visible vertex count
@@ -178,10 +179,10 @@ struct CullTabs {
 // leaves (at most 64: the team kernel takes at most 64 * 256 leaves); block
 // scans give the coverage entering the run and the list positions.  s_coff
 // doubles as the difference array.
-template <int kBox, class Hit>
+template <int kBox, class Hit, class Tabs>
 __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb, Hit hits,
                                              unsigned char* s_pass, int* s_cl, int* s_coff,
-                                             const CullTabs& ct, TeamShared& sh) {
+                                             const Tabs& ct, TeamShared& sh) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
   __syncthreads();
@@ -279,9 +280,9 @@ __device__ __forceinline__ unsigned long long team_orig_sweep(const DevMesh& m, 
 }
 
 // The node search of one pass (sphere at the pass location).
-template <int kBox>
+template <int kBox, class Tabs>
 __device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char* s_pass,
-                          int* s_cl, int* s_coff, const CullTabs& ct, TeamShared& sh) {
+                          int* s_cl, int* s_coff, const Tabs& ct, TeamShared& sh) {
   team_cull_by<kBox>(
       m, pp.original ? m.orig_vb : m.vb,
       [&](float4 lo, float4 hi) { return box_hits(lo, hi, pp.loc, pp.cull_radius_sq); }, s_pass,

@@ -28,9 +28,12 @@ PBVH_UpdateDrawBuffers, PBVH_UpdateRedraw = 16, 32
 STROKE_EAGER, STROKE_GRAPH, STROKE_TEAM = 0, 1, 2
 BATCH_SEQUENTIAL, BATCH_TEAM = 0, 1
 TEAM_GRID = -1  # SGPU_TEAM_GRID: every SM of the GPU works on one stroke
+TEAM_LOCKSTEP = -2  # SGPU_TEAM_LOCKSTEP: every SM on every stroke of a batch, phase work pooled
 TEAM_SIZES = (TEAM_GRID, 1, 2, 4, 8, 16)  # sgpu_autotune_team's candidates, in order
-BATCH_TEAM_CANDIDATES = ((16, 1), (8, 1), (8, 2), (4, 1), (4, 2), (2, 2), (TEAM_GRID, 1))
+BATCH_TEAM_CANDIDATES = ((16, 1), (8, 1), (8, 2), (4, 1), (4, 2), (2, 2), (TEAM_GRID, 1),
+                         (TEAM_LOCKSTEP, 1), (TEAM_LOCKSTEP, 2))
 INJECT_ALLOC_FAIL, INJECT_WAIT_NS, INJECT_BARRIER_EXTRA = 1, 2, 3
+DEBUG_LOCKSTEP_PER_SM = 4  # test hook: CTAs per SM of lockstep launches (0: the team shape's)
 
 
 class SculptGPUError(RuntimeError):
@@ -96,7 +99,7 @@ EXPORTS = (
     "sgpu_draw_buffers_layout", "sgpu_draw_buffers_overlay", "sgpu_draw_buffers_get",
     "sgpu_draw_buffers_device", "sgpu_draw_buffers_update_timed", "sgpu_debug_inject",
     "sgpu_calc_area_normal_and_center", "sgpu_stroke_host_grids", "sgpu_autotune_batch",
-    "sgpu_find_nearest_to_ray",
+    "sgpu_find_nearest_to_ray", "sgpu_batch_team_profile",
 )
 
 DRAW_STRIDE = 36  # SGPU_DRAW_STRIDE
@@ -174,6 +177,8 @@ def load(path: str | None = None):
     L.sgpu_autotune_team.argtypes = [vp, C.POINTER(SGPU_Brush), vp, i, vp, vp, vp]
     L.sgpu_batch_stroke.argtypes = [vp, i, vp, vp, vp, vp, i, i, vp, vp]
     L.sgpu_autotune_batch.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp]
+    L.sgpu_batch_team_profile.argtypes = [vp, i, vp, vp, vp, vp, i, C.POINTER(SGPU_TeamProfile),
+                                          vp]
     L.sgpu_find_nearest_to_ray.argtypes = [vp, i, vp, vp, i, vp, vp, vp]
     L.sgpu_mesh_store_original.argtypes = [vp]
     L.sgpu_debug_inject.argtypes = [i, C.c_int64]
@@ -234,6 +239,25 @@ def batch_stroke(pbvhs, strokes, mode: int = BATCH_TEAM, cluster: int = 0, dab_t
     _check(L.sgpu_batch_stroke(handles, n, brushes, _p(dabs), _p(offs), _p(tools), mode,
                                cluster, stats, C.byref(total)))
     return list(stats), total.value
+
+
+def batch_team_profile(pbvhs, strokes, cluster: int = 0, dab_tools=None):
+    """One SGPU_BATCH_TEAM batch with phase timers (those of the launch's first
+    thread).  Returns ({phase: ms}, total_ms, per-mesh stats)."""
+    L = load()
+    n = len(pbvhs)
+    handles = (C.c_void_p * n)(*[p.handle for p in pbvhs])
+    brushes = (SGPU_Brush * n)(*[make_brush(s) for s in strokes])
+    dabs = np.ascontiguousarray(np.concatenate([s.dabs for s in strokes]), dtype=np.float32)
+    offs = np.zeros(n + 1, dtype=np.int32)
+    offs[1:] = np.cumsum([s.dabs.shape[0] for s in strokes])
+    tools = None if dab_tools is None else np.ascontiguousarray(dab_tools, dtype=np.int32)
+    prof = SGPU_TeamProfile()
+    stats = (SGPU_StrokeStats * n)()
+    _check(L.sgpu_batch_team_profile(handles, n, brushes, _p(dabs), _p(offs), _p(tools), cluster,
+                                     C.byref(prof), stats))
+    return ({name: prof.phase_ms[k] for k, name in enumerate(TEAM_PHASES)}, prof.total_ms,
+            list(stats))
 
 
 class PinnedArray:

@@ -275,6 +275,16 @@ int sgpu_stroke(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, 
  * another.  Default: the autotuner's cached team for the stroke (see
  * sgpu_autotune_team), else 8. */
 #define SGPU_TEAM_GRID (-1)
+/* Batches only (sgpu_batch_stroke, sgpu_autotune_batch): every SM works on
+ * every stroke of the batch at once, dab by dab (one cooperative launch).
+ * Each phase of a dab pools the work of all meshes — culled leaves in runs of
+ * 32 vertices, area blocks, smooth hits, claimed GRIDS faces, touched-leaf
+ * refit chunks, tagged vertices — and deals it over the whole GPU, so meshes
+ * of any size mix without one team holding a large mesh alone.  Strokes with
+ * grab, elastic deform or layer dabs, more than 1024 meshes, or GRIDS grids
+ * above 33x33 return SGPU_ERR_UNSUPPORTED.  Results equal each mesh's own
+ * stroke bit for bit. */
+#define SGPU_TEAM_LOCKSTEP (-2)
 int sgpu_mesh_set_team(sgpu_mesh *mesh, int cluster_size);
 int sgpu_mesh_get_team(const sgpu_mesh *mesh, int *cluster_size);
 /* Autotuner of the persistent stroke kernel's team shape.  Times the stroke
@@ -294,14 +304,16 @@ int sgpu_autotune_team(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab 
 
 /* Autotuner of a batch's team shape (the arguments of sgpu_batch_stroke):
  * times SGPU_BATCH_TEAM on the candidates (cluster, CTAs per SM) = (16, 1),
- * (8, 1), (8, 2), (4, 1), (4, 2), (2, 2) and the whole GPU (strokes one after
- * another), restoring every mesh between trials, and caches the fastest under
+ * (8, 1), (8, 2), (4, 1), (4, 2), (2, 2), the whole GPU (strokes one after
+ * another) and SGPU_TEAM_LOCKSTEP with 1 and 2 CTAs per SM (strokes
+ * together; skipped where the batch does not allow it), restoring every mesh
+ * between trials, and caches the fastest under
  * (mesh count, log2 of the total vertex count, the set of tools), where
  * sgpu_batch_stroke with cluster_size 0 finds it.  Two CTAs per SM run the
  * build with 128 registers per thread: twice the teams, slower each.
  * r_ms (nullable): SGPU_AUTOTUNE_BATCH_CANDIDATES timings, -1 where a
  * candidate cannot run. */
-#define SGPU_AUTOTUNE_BATCH_CANDIDATES 7
+#define SGPU_AUTOTUNE_BATCH_CANDIDATES 9
 int sgpu_autotune_batch(sgpu_mesh **meshes, int nmesh, const SGPU_Brush *brushes,
                         const SGPU_Dab *dabs, const int *dab_offsets, const int *dab_tools,
                         int *r_cluster, int *r_ctas_per_sm, float *r_ms);
@@ -323,6 +335,16 @@ typedef struct SGPU_TeamProfile {
 int sgpu_stroke_team_profile(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
                              int ndabs, const int *dab_tools, SGPU_TeamProfile *out,
                              SGPU_StrokeStats *stats);
+/* The same profile for one SGPU_BATCH_TEAM batch (arguments of
+ * sgpu_batch_stroke; cluster_size 0 takes the cached team).  The phase times
+ * are those of the launch's first thread.  Cluster teams: each phase
+ * includes the wait at the barrier that ends it.  SGPU_TEAM_LOCKSTEP: each
+ * phase is the first CTA's own work, phase 6 holds its barrier waits, and
+ * phase 5 the flushes (run by each mesh's home CTA at the next dab start).
+ * stats (nullable): one per mesh. */
+int sgpu_batch_team_profile(sgpu_mesh **meshes, int nmesh, const SGPU_Brush *brushes,
+                            const SGPU_Dab *dabs, const int *dab_offsets, const int *dab_tools,
+                            int cluster_size, SGPU_TeamProfile *out, SGPU_StrokeStats *stats);
 
 /* ---- ray cast ----
  * Replaces BKE_pbvh_raycast (pbvh.c:3916) driven by the sculpt ray-cast
@@ -438,7 +460,10 @@ int sgpu_draw_buffers_device(sgpu_mesh *mesh, void **d_vbo, size_t *bytes);
  * dab_tools (nullable) is indexed like dabs.
  *   SGPU_BATCH_SEQUENTIAL: one graph-mode stroke per mesh, one after another.
  *   SGPU_BATCH_TEAM: one persistent launch; cluster teams take meshes from a
- *     work queue, longest estimated stroke first.
+ *     work queue, longest estimated stroke first; SGPU_TEAM_GRID runs the
+ *     strokes one after another on the whole GPU; SGPU_TEAM_LOCKSTEP runs
+ *     them together on the whole GPU with every phase's work pooled over the
+ *     meshes.  A mesh may appear once per batch.
  * cluster_size 0 uses the team sgpu_autotune_batch cached for a batch like
  * this one, else the first mesh's setting.  stats (nullable) gets one
  * entry per mesh; r_total_ms the CUDA-event time of the whole batch. */
@@ -538,6 +563,10 @@ int sgpu_smooth_dab_noalloc(float *co, const float *normals, const float *mask,
 #define SGPU_INJECT_ALLOC_FAIL 1
 #define SGPU_INJECT_WAIT_NS 2
 #define SGPU_INJECT_BARRIER_EXTRA 3
+/* SGPU_DEBUG_LOCKSTEP_PER_SM, value 1 or 2: every SGPU_TEAM_LOCKSTEP launch
+ * runs that many CTAs per SM (the build the autotuner may also choose); 0
+ * restores the team shape's choice.  A test hook, not a failure. */
+#define SGPU_DEBUG_LOCKSTEP_PER_SM 4
 int sgpu_debug_inject(int what, int64_t value);
 
 /* ---- data access (synchronous) ---- */

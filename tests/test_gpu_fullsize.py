@@ -13,7 +13,7 @@ import pytest
 
 from dune_sculpt_gb300 import synth
 from dune_sculpt_gb300.sculpt import (BATCH_TEAM, PBVH, STROKE_GRAPH, STROKE_TEAM, TEAM_GRID,
-                                      batch_stroke)
+                                      TEAM_LOCKSTEP, batch_stroke)
 
 from helpers import bits_equal, first_diff, rel_err
 
@@ -94,11 +94,12 @@ def test_fullsize_clay_strips_sphere(gpu, oracle):
         assert np.abs(a32.astype(np.float64) - a64).max() <= FP64_TOL, d
 
 
-def test_fullsize_batch(gpu, oracle):
+@pytest.mark.parametrize("team", [8, TEAM_LOCKSTEP])
+def test_fullsize_batch(gpu, oracle, team):
     batch = synth.cfg4_batch()
     gs = [PBVH.build_mesh(m, ll) for (m, _, ll) in batch]
     strokes = [st for (_, st, _) in batch]
-    stats, ms = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=8)
+    stats, ms = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=team)
     assert ms > 0
     for k, ((m, st, ll), g, s) in enumerate(zip(batch, gs, stats)):
         o = oracle.OracleMesh.faces(m, ll)
