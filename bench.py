@@ -90,7 +90,14 @@ def parse_args():
     ap.add_argument("--quick", action="store_true",
                     help="three persistent strokes of the workload, no report (for ncu)")
     ap.add_argument("--team", type=int, default=0,
-                    help="team for --quick: cluster size, -1 for the whole GPU, 0 autotuned")
+                    help="team for --quick: cluster size, -1 for the whole GPU, 0 autotuned; "
+                         "for --quick-batch: cluster size, -1, or -2 for the lockstep launch")
+    ap.add_argument("--quick-dabs", type=int, default=0,
+                    help="--quick strokes only the first N dabs (a shorter launch for a full "
+                         "ncu capture); 0: every dab")
+    ap.add_argument("--quick-batch", action="store_true",
+                    help="three launches of the 64-mesh batch on --team (8 when 0), no report "
+                         "(the command profiled with ncu for the batch kernels)")
     ap.add_argument("--raycast-only", action="store_true",
                     help="1024-ray sgpu_raycast batches on the icosphere and on the multires "
                          "torus, one JSON line, and exit (the command profiled with ncu for "
@@ -110,6 +117,9 @@ def parse_args():
                     help="the batched clay / multires legs only, one JSON line")
     ap.add_argument("--batch-only", action="store_true",
                     help="the 64-mesh batch leg only (no CPU baseline), one JSON line")
+    ap.add_argument("--batch-phases", action="store_true",
+                    help="per-dab phase profile of the batch launches (64-mesh batch, K clay and "
+                         "K multires strokes) on several team shapes, one JSON line each")
     return ap.parse_args()
 
 
@@ -865,16 +875,45 @@ def run_quick(args):
     from dune_sculpt_gb300.sculpt import STROKE_TEAM
 
     W = workload(args.workload)
+    st, tools = W.stroke, W.tools
+    if args.quick_dabs > 0:
+        from dataclasses import replace
+
+        st = replace(st, dabs=st.dabs[:args.quick_dabs])
+        tools = None if tools is None else tools[:args.quick_dabs]
     g = build_gpu(W)
     g.snapshot()
     if args.team:
         g.set_team(args.team)
     else:
-        g.autotune_team(W.stroke, dab_tools=W.tools)
+        g.autotune_team(st, dab_tools=tools)
     for _ in range(3):
         g.restore()
-        s = g.stroke(W.stroke, mode=STROKE_TEAM, dab_tools=W.tools)
+        s = g.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
     print(f"quick: {s.verts_displaced} vertices displaced, {s.gpu_ms:.3f} ms, team {g.team()}")
+    return 0
+
+
+def run_quick_batch(args):
+    """Three launches of the 64-mesh batch on one team shape."""
+    from dune_sculpt_gb300 import build as libbuild
+
+    libbuild.build()
+    from dune_sculpt_gb300 import synth
+    from dune_sculpt_gb300.sculpt import BATCH_TEAM, PBVH, batch_stroke
+
+    batch = synth.cfg4_batch()
+    gs = [PBVH.build_mesh(m, ll) for (m, _, ll) in batch]
+    strokes = [st for (_, st, _) in batch]
+    for p in gs:
+        p.snapshot()
+    team = args.team or 8
+    for _ in range(3):
+        for p in gs:
+            p.restore()
+        stats, ms = batch_stroke(gs, strokes, mode=BATCH_TEAM, cluster=team)
+    print(f"quick batch: {sum(x.verts_displaced for x in stats)} vertices displaced, "
+          f"{ms:.3f} ms, team {team}")
     return 0
 
 
@@ -935,12 +974,86 @@ def run_phases(args):
     return 0
 
 
+def batched_strokes(synth, W, K: int):
+    """K independent seeded strokes of a single-mesh workload (the batched form)."""
+    strokes = []
+    for k in range(K):
+        if W.name == "clay":
+            dabs = synth.arc_dabs(synth.SEED_BASE + 200 + k, W.stroke.dabs.shape[0],
+                                  0.1 * 2 * W.stroke.radius)
+        else:
+            dabs = synth.torus_dabs(synth.SEED_BASE + 200 + k, W.stroke.dabs.shape[0],
+                                    W.stroke.radius)
+        strokes.append(synth.Stroke(W.stroke.tool, W.stroke.radius, W.stroke.strength,
+                                    W.stroke.curve_preset, W.stroke.symmetry, dabs))
+    return strokes
+
+
+def run_batch_phases(args):
+    """Per-dab phase times of the batch launches: the 64-mesh batch and the K
+    clay / multires strokes, each on 8-CTA clusters (two per SM), 16-CTA
+    clusters and the lockstep launch (one and two CTAs per SM); best of three
+    instrumented launches (phase timers of the launch's first thread)."""
+    from dune_sculpt_gb300 import build as libbuild
+
+    libbuild.build()
+    from dune_sculpt_gb300 import synth
+    from dune_sculpt_gb300.sculpt import (DEBUG_LOCKSTEP_PER_SM, PBVH, TEAM_LOCKSTEP,
+                                          SculptGPUError, batch_team_profile, debug_inject)
+
+    def profile(name, gs, strokes, tools, ndabs):
+        for p in gs:
+            p.snapshot()
+        for label, cl, per in (("cluster8", 8, 0), ("cluster16", 16, 0),
+                               ("lockstep_1_per_sm", TEAM_LOCKSTEP, 1),
+                               ("lockstep_2_per_sm", TEAM_LOCKSTEP, 2)):
+            best = None
+            try:
+                for _ in range(3):
+                    for p in gs:
+                        p.restore()
+                    gs[0].flush_l2()
+                    debug_inject(DEBUG_LOCKSTEP_PER_SM, per)
+                    try:
+                        ph, ms, st = batch_team_profile(gs, strokes, cluster=cl, dab_tools=tools)
+                    finally:
+                        debug_inject(DEBUG_LOCKSTEP_PER_SM, 0)
+                    if best is None or ms < best[1]:
+                        best = (ph, ms, st)
+            except SculptGPUError as e:
+                print(json.dumps({"batch": name, "team": label, "unavailable": str(e)}), flush=True)
+                continue
+            ph, ms, st = best
+            print(json.dumps({"batch": name, "team": label, "ms": round(ms, 3),
+                              "verts_displaced": sum(x.verts_displaced for x in st),
+                              "phase_us_per_dab": {k: round(1000 * v / ndabs, 2)
+                                                   for k, v in ph.items()}}), flush=True)
+        for p in gs:
+            p.restore()
+            p.free()
+
+    batch = synth.cfg4_batch()
+    profile("64_meshes_cfg4", [PBVH.build_mesh(m, ll) for (m, _, ll) in batch],
+            [st for (_, st, _) in batch], None, batch[0][1].dabs.shape[0])
+    for name in ("clay", "multires"):
+        W = workload(name)
+        K = args.batched_k
+        tools = np.concatenate([W.tools] * K) if W.tools is not None else None
+        profile(f"{K}x_{W.cfg['workload']}", [build_gpu(W) for _ in range(K)],
+                batched_strokes(synth, W, K), tools, W.stroke.dabs.shape[0])
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.batch_phases:
+        return run_batch_phases(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.quick:
         return run_quick(args)
+    if args.quick_batch:
+        return run_quick_batch(args)
     if args.phases:
         return run_phases(args)
     if args.batch_only:
