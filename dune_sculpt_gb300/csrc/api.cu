@@ -1154,6 +1154,7 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
   if ((rc = m->alloc(&d.edge_mark, num_base_edges))) return bail(rc);
   if ((rc = m->alloc(&d.bvert_mark, num_base_verts))) return bail(rc);
   if ((rc = m->alloc(&d.grid_counts, 4))) return bail(rc);
+  if ((rc = m->alloc(&d.corner_own, 2 * static_cast<size_t>(num_grids)))) return bail(rc);
   if ((rc = upload_pbvh(m))) return bail(rc);
   if (!grids_no) {
     std::vector<int> lflag(d.nleaf);

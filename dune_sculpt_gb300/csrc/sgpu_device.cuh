@@ -121,6 +121,11 @@ struct DevMesh {
   unsigned int* edge_mark;
   unsigned int* bvert_mark;
   int* grid_counts;  // [0] faces, [1] edges, [2] base verts, [3] grids
+  // per grid (corner of its face), written with the face's update in a dab:
+  // [2g] = (first edge_elems slot, faces) of the base edge the corner's face
+  // averages, [2g+1] = (first bvert_elems slot, faces) of its base vertex;
+  // faces = 0 when another claimed face owns it or it has one face
+  int2* corner_own;
   // work
   Work* work;
   int* cull_list;  // nleaf

@@ -739,6 +739,30 @@ __device__ __forceinline__ float3 staged_normal(const float3* s_q, int i, int gs
   return make_float3(ax * inv, ay * inv, az * inv);
 }
 
+// The owner records of face f's corners for the dab of this epoch (threads
+// t_begin, t_begin + t_step, ...): corner c's base edge and base vertex are
+// averaged by the first of their faces (slot order) claimed in the epoch
+// (subdiv_ccg.c:1010-1048, 1081-1104 average each once); the owner's record
+// holds the element slots and face count, the others' a count of 0.  Needs
+// the epoch's claims complete.
+__device__ __forceinline__ void grid_corner_owners(const DevMesh& m, int f, unsigned int epoch,
+                                                   int t_begin, int t_step) {
+  const int s = m.face_start[f], n = m.face_ngrids[f];
+  for (int t = t_begin; t < 2 * n; t += t_step) {
+    const bool edge = t < n;
+    const int c = edge ? t : t - n;
+    const int id = edge ? m.face_edges[s + c] : m.face_verts[s + c];
+    const int* off = edge ? m.edge_off : m.bvert_off;
+    const int* face_of = edge ? m.edge_face : m.bvert_face;
+    const int f0 = off[id], f1 = off[id + 1];
+    int owner = -1;
+    if (f1 - f0 > 1)
+      for (int k = f0; k < f1 && owner < 0; k++)
+        if (__ldcg(&m.face_mark[face_of[k]]) == epoch) owner = face_of[k];
+    m.corner_own[2 * (s + c) + (edge ? 0 : 1)] = make_int2(f0, owner == f ? f1 - f0 : 0);
+  }
+}
+
 // Inner normals, face-internal seams and the centre of one claimed face by
 // one CTA (subdiv_ccg.c:670-740 and 951-984).  The face's grids are staged in
 // shared memory with cp.async (positions and masks), the normal_quad of every
@@ -751,7 +775,10 @@ __device__ __forceinline__ float3 staged_normal(const float3* s_q, int i, int gs
 // reads the values the inner-normal step left.  Faces are independent here:
 // a face's grids hold their own copies of the base-edge elements, which the
 // base-edge pass averages afterwards.  GRIDS positions carry w = 0.
-static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* stage, int group) {
+// The owner records of the face's corners are written while the first
+// stage is in flight (grid_corner_owners).
+static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* stage, int group,
+                                      unsigned int epoch) {
   const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area, qa = g1 * g1;
   const int s = m.face_start[f], n = m.face_ngrids[f];
   float4* s_co = reinterpret_cast<float4*>(stage);
@@ -764,6 +791,7 @@ static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* st
       const size_t e = static_cast<size_t>(s + c0) * area + i;
       cp_async16(&s_co[i], &m.co[e]);
     }
+    if (c0 == 0) grid_corner_owners(m, f, epoch, threadIdx.x, kTeamThreads);
     cp_async_wait_all();
     if (m.mask)
       for (int i = threadIdx.x; i < nc * area; i += kTeamThreads)
@@ -852,48 +880,31 @@ static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* st
 
 // Base edges and corners of one claimed face by one CTA: each base edge and
 // base vertex is averaged once, by the first of its faces (slot order) that
-// is claimed in this epoch (subdiv_ccg.c:1010-1048, 1081-1104); the owner
-// decisions of the face's corners are made first, one thread per corner.
+// is claimed in this epoch (subdiv_ccg.c:1010-1048, 1081-1104).  With
+// records (the face went through team_grid_face this dab) the owner
+// decisions are read from corner_own; without (the unstaged path) they are
+// made here first, one thread per corner record.
 static __device__ void team_grid_face_boundary(const DevMesh& m, int f, unsigned int epoch,
-                                               unsigned char* stage) {
+                                               bool records) {
   const int g2 = 2 * m.grid_size, per_corner = g2 - 1;
   const int s = m.face_start[f], n = m.face_ngrids[f];
-  int* s_edge = reinterpret_cast<int*>(stage);  // per corner: edge owned (or -1), vertex owned (or -1)
-  int* s_vert = s_edge + n;
-  for (int c = threadIdx.x; c < n; c += kTeamThreads) {
-    const int e = m.face_edges[s + c];
-    int f0 = m.edge_off[e], f1 = m.edge_off[e + 1];
-    int owner = -1;
-    if (f1 - f0 > 1)
-      for (int k = f0; k < f1 && owner < 0; k++)
-        if (__ldcg(&m.face_mark[m.edge_face[k]]) == epoch) owner = m.edge_face[k];
-    s_edge[c] = owner == f ? e : -1;
-    const int v = m.face_verts[s + c];
-    f0 = m.bvert_off[v];
-    f1 = m.bvert_off[v + 1];
-    owner = -1;
-    if (f1 - f0 > 1)
-      for (int k = f0; k < f1 && owner < 0; k++)
-        if (__ldcg(&m.face_mark[m.bvert_face[k]]) == epoch) owner = m.bvert_face[k];
-    s_vert[c] = owner == f ? v : -1;
+  if (!records) {
+    grid_corner_owners(m, f, epoch, threadIdx.x, kTeamThreads);
+    __syncthreads();  // the CTA's own records (global memory, CTA barrier)
   }
-  __syncthreads();
   for (int it = threadIdx.x; it < n * per_corner; it += kTeamThreads) {
     const int c = it / per_corner, j = it - c * per_corner;
     if (j < g2 - 2) {
-      const int e = s_edge[c];
-      if (e < 0) continue;
-      const int f0 = m.edge_off[e], f1 = m.edge_off[e + 1];
+      const int2 e = __ldcg(&m.corner_own[2 * (s + c)]);
+      if (e.y == 0) continue;
       const int i = j + 1;
-      grid_average_set(m, f1 - f0, [&](int k) { return m.edge_elems[(long long)(f0 + k) * g2 + i]; });
+      grid_average_set(m, e.y, [&](int k) { return m.edge_elems[(long long)(e.x + k) * g2 + i]; });
     } else {
-      const int v = s_vert[c];
-      if (v < 0) continue;
-      const int f0 = m.bvert_off[v], f1 = m.bvert_off[v + 1];
-      grid_average_set(m, f1 - f0, [&](int k) { return m.bvert_elems[f0 + k]; });
+      const int2 v = __ldcg(&m.corner_own[2 * (s + c) + 1]);
+      if (v.y == 0) continue;
+      grid_average_set(m, v.y, [&](int k) { return m.bvert_elems[v.x + k]; });
     }
   }
-  __syncthreads();  // the corner tables are free again
 }
 
 // Team barrier.  A cluster team uses barrier.cluster (cluster.sync():
@@ -1407,7 +1418,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         if (group > 0) {
           for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C)) {
             const int f = __ldcg(&m.face_list[fi]);
-            team_grid_face(m, f, dyn, group);
+            team_grid_face(m, f, dyn, group, epoch);
             if (threadIdx.x == 0) {
               const int n = m.face_ngrids[f];
               // positions read, normals written; the seam pairs and the
@@ -1436,7 +1447,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           TEAM_SYNC();
         }
         for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C))
-          team_grid_face_boundary(m, __ldcg(&m.face_list[fi]), epoch, dyn);
+          team_grid_face_boundary(m, __ldcg(&m.face_list[fi]), epoch, group > 0);
         TEAM_SYNC();
         clk.mark(a, rank, kPhGridSeams);
         if (rank == 0 && threadIdx.x == 0)

@@ -129,3 +129,23 @@ def test_grids_team_stroke(gpu, oracle, cluster):
     tot, _ = o.stroke(st, which=1, dab_tools=tools)
     assert s.verts_displaced == tot
     _assert_equal(gp, o, f"team{cluster} second")
+
+
+@pytest.mark.parametrize("team", [16, -1])
+def test_grids_persistent_stroke_unstaged_grids(gpu, oracle, team):
+    """Grids of 65x65 do not fit the persistent kernel's shared-memory stage:
+    inner normals and face seams per element, then the base edges and corners
+    with their owner records made in that phase."""
+    from dune_sculpt_gb300.sculpt import STROKE_TEAM
+
+    g = synth.torus_grids(8, 4, level=7, seed=synth.SEED_BASE + 7)
+    assert g.grid_size == 65
+    gp, o = _pair(oracle, g, 2)
+    gp.set_team(team)
+    dabs = synth.torus_dabs(5, 10, 0.2)
+    tools = np.array([TOOLS[d % len(TOOLS)] for d in range(dabs.shape[0])], dtype=np.int32)
+    st = synth.Stroke(synth.TOOL_DRAW, 0.2, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
+    s = gp.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
+    tot, _ = o.stroke(st, which=1, dab_tools=tools)
+    assert s.verts_displaced == tot and tot > 0
+    _assert_equal(gp, o, f"unstaged team {team}")
