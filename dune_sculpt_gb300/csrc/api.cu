@@ -53,6 +53,12 @@ int cuda_fail(cudaError_t e, const char* what) {
     cudaError_t _e = (expr);                        \
     if (_e != cudaSuccess) return cuda_fail(_e, what); \
   } while (0)
+// The same inside a mesh-creation function: frees the partial mesh (bail).
+#define CK_BAIL(expr, what)                                   \
+  do {                                                        \
+    cudaError_t _e = (expr);                                  \
+    if (_e != cudaSuccess) return bail(cuda_fail(_e, what));  \
+  } while (0)
 
 // Host-side test hooks (sgpu_debug_inject).  g_inject_alloc > 0: the mesh
 // allocation that brings it to zero fails as out of memory.  g_wait_ns: the
@@ -1042,9 +1048,9 @@ int sgpu_mesh_create_faces(const SGPU_MVert* verts, int totvert, const SGPU_MPol
     CK(cudaMemsetAsync(d.vtag, 1, sizeof(unsigned int) * totvert, m->stream), "tag all");
     std::vector<int> lflag(d.nleaf);
     for (int k = 0; k < d.nleaf; k++) lflag[k] = h.flag[h.leaf_nodes[k]] | kUpdateNormals;
-    CK(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf, cudaMemcpyHostToDevice,
-                       m->stream),
-       "flag all");
+    CK_BAIL(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf,
+                            cudaMemcpyHostToDevice, m->stream),
+            "flag all");
     CK(launch_update_faces(d, 1, 0, m->stream), "normal kernel");
   }
   CK(cudaStreamSynchronize(m->stream), "cudaStreamSynchronize");
@@ -1155,13 +1161,19 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
   if ((rc = m->alloc(&d.bvert_mark, num_base_verts))) return bail(rc);
   if ((rc = m->alloc(&d.grid_counts, 4))) return bail(rc);
   if ((rc = m->alloc(&d.corner_own, 2 * static_cast<size_t>(num_grids)))) return bail(rc);
+  if ((rc = m->alloc(&d.edge_own, num_base_edges))) return bail(rc);
+  if ((rc = m->alloc(&d.bvert_own, num_base_verts))) return bail(rc);
+  CK_BAIL(cudaMemsetAsync(d.edge_own, 0xFF, sizeof(unsigned long long) * num_base_edges, m->stream),
+          "owner keys");
+  CK_BAIL(cudaMemsetAsync(d.bvert_own, 0xFF, sizeof(unsigned long long) * num_base_verts, m->stream),
+          "owner keys");
   if ((rc = upload_pbvh(m))) return bail(rc);
   if (!grids_no) {
     std::vector<int> lflag(d.nleaf);
     for (int k = 0; k < d.nleaf; k++) lflag[k] = h.flag[h.leaf_nodes[k]] | kUpdateNormals;
-    CK(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf, cudaMemcpyHostToDevice,
-                       m->stream),
-       "flag all");
+    CK_BAIL(cudaMemcpyAsync(d.leaf_flag, lflag.data(), sizeof(int) * d.nleaf,
+                            cudaMemcpyHostToDevice, m->stream),
+            "flag all");
     Launcher L{m};
     if ((rc = launch_update_normals(L, 0))) return bail(rc);
   }

@@ -126,6 +126,12 @@ struct DevMesh {
   // averages, [2g+1] = (first bvert_elems slot, faces) of its base vertex;
   // faces = 0 when another claimed face owns it or it has one face
   int2* corner_own;
+  // per base edge / base vertex: the smallest key ((~epoch) << 32 | face)
+  // over the faces claimed for the persistent kernel's GRIDS update; the
+  // owner in an epoch is the claimed face of least index, which is the first
+  // claimed one in slot order (slots are filled face by face)
+  unsigned long long* edge_own;
+  unsigned long long* bvert_own;
   // work
   Work* work;
   int* cull_list;  // nleaf
@@ -901,6 +907,11 @@ constexpr int kAreaBlock = 4096;
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
   const unsigned int d = static_cast<unsigned int>(__cvta_generic_to_shared(smem_dst));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+// 4-byte asynchronous copy global -> shared (cached in L1).
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+  const unsigned int d = static_cast<unsigned int>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gmem_src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");

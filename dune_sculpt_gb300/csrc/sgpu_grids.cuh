@@ -37,17 +37,40 @@ __device__ __forceinline__ void grid_claim_face(const DevMesh& m, int grid, unsi
   }
 }
 
+// Owner key of a claimed face in an epoch: newer epochs and smaller faces
+// compare smaller.
+__device__ __forceinline__ unsigned long long grid_owner_key(unsigned int epoch, int f) {
+  return (static_cast<unsigned long long>(0xFFFFFFFFu - epoch) << 32) | static_cast<unsigned int>(f);
+}
+
 // The face of a grid joins the update (persistent kernel): the face and its
-// grids are listed; its base edges and corners are not (each is averaged by
-// the first claimed face among its faces, grid_owner_seam_item).
+// grids are listed; its base edges and corners are not — each is averaged
+// once, by the claimed face of least index among its faces, recorded here
+// with a 64-bit minimum per edge and base vertex.
 __device__ __forceinline__ void grid_claim_face_only(const DevMesh& m, int grid, unsigned int epoch) {
   const int f = m.grid_face[grid];
+  // the face's tables are read-only: loaded before the claim's round trip
+  const int n = m.face_ngrids[f], s = m.face_start[f];
   if (!grid_claim(m.face_mark, f, epoch)) return;
-  const int n = m.face_ngrids[f];
   const int fi = atomicAdd(&m.grid_counts[0], 1);
   const int gb = atomicAdd(&m.grid_counts[3], n);
+  const unsigned long long key = grid_owner_key(epoch, f);
+  for (int c0 = 0; c0 < n; c0 += 4) {
+    int e[4], v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (c0 + u < n) {
+        e[u] = m.face_edges[s + c0 + u];
+        v[u] = m.face_verts[s + c0 + u];
+      }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (c0 + u < n) {
+        atomicMin(&m.edge_own[e[u]], key);
+        atomicMin(&m.bvert_own[v[u]], key);
+      }
+  }
   m.face_list[fi] = f;
-  const int s = m.face_start[f];
   for (int c = 0; c < n; c++) m.cgrid_list[gb + c] = s + c;
 }
 

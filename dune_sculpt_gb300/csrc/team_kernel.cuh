@@ -742,24 +742,23 @@ __device__ __forceinline__ float3 staged_normal(const float3* s_q, int i, int gs
 // The owner records of face f's corners for the dab of this epoch (threads
 // t_begin, t_begin + t_step, ...): corner c's base edge and base vertex are
 // averaged by the first of their faces (slot order) claimed in the epoch
-// (subdiv_ccg.c:1010-1048, 1081-1104 average each once); the owner's record
-// holds the element slots and face count, the others' a count of 0.  Needs
-// the epoch's claims complete.
+// (subdiv_ccg.c:1010-1048, 1081-1104 average each once) — the claimed face of
+// least index, whose key the claims left in edge_own / bvert_own; the
+// owner's record holds the element slots and face count, the others' a count
+// of 0.  Needs the epoch's claims complete.
 __device__ __forceinline__ void grid_corner_owners(const DevMesh& m, int f, unsigned int epoch,
                                                    int t_begin, int t_step) {
   const int s = m.face_start[f], n = m.face_ngrids[f];
+  const unsigned long long key = grid_owner_key(epoch, f);
   for (int t = t_begin; t < 2 * n; t += t_step) {
     const bool edge = t < n;
     const int c = edge ? t : t - n;
     const int id = edge ? m.face_edges[s + c] : m.face_verts[s + c];
     const int* off = edge ? m.edge_off : m.bvert_off;
-    const int* face_of = edge ? m.edge_face : m.bvert_face;
+    const unsigned long long own = __ldcg(edge ? &m.edge_own[id] : &m.bvert_own[id]);
     const int f0 = off[id], f1 = off[id + 1];
-    int owner = -1;
-    if (f1 - f0 > 1)
-      for (int k = f0; k < f1 && owner < 0; k++)
-        if (__ldcg(&m.face_mark[face_of[k]]) == epoch) owner = face_of[k];
-    m.corner_own[2 * (s + c) + (edge ? 0 : 1)] = make_int2(f0, owner == f ? f1 - f0 : 0);
+    m.corner_own[2 * (s + c) + (edge ? 0 : 1)] =
+        make_int2(f0, (own == key && f1 - f0 > 1) ? f1 - f0 : 0);
   }
 }
 
@@ -790,12 +789,10 @@ static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* st
     for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
       const size_t e = static_cast<size_t>(s + c0) * area + i;
       cp_async16(&s_co[i], &m.co[e]);
+      if (m.mask) cp_async4(&s_mk[i], &m.mask[e]);
     }
     if (c0 == 0) grid_corner_owners(m, f, epoch, threadIdx.x, kTeamThreads);
     cp_async_wait_all();
-    if (m.mask)
-      for (int i = threadIdx.x; i < nc * area; i += kTeamThreads)
-        s_mk[i] = __ldcg(&m.mask[static_cast<size_t>(s + c0) * area + i]);
     __syncthreads();
     for (int i = threadIdx.x; i < nc * qa; i += kTeamThreads) {
       const int c = i / qa, q = i - c * qa, qy = q / g1, qx = q - qy * g1;
