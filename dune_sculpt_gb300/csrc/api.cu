@@ -1141,6 +1141,14 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
     m->has_mask = true;
   }
   if ((rc = m->upload(&d.grid_face, h.grid_face))) return bail(rc);
+  {
+    std::vector<int4> info(num_grids);
+    for (int gi = 0; gi < num_grids; gi++) {
+      const int f = h.grid_face[gi];
+      info[gi] = make_int4(f, h.face_start[f], h.face_ngrids[f], 0);
+    }
+    if ((rc = m->upload(&d.grid_info, info))) return bail(rc);
+  }
   if ((rc = m->upload(&d.face_start, h.face_start))) return bail(rc);
   if ((rc = m->upload(&d.face_ngrids, h.face_ngrids))) return bail(rc);
   if ((rc = m->upload(&d.face_verts, h.face_verts))) return bail(rc);

@@ -411,7 +411,19 @@ bool build_grids(HostMesh& m, std::string* err) {
     }
   m.grid_face.assign(m.num_grids, -1);
   for (int f = 0; f < m.num_faces; f++)
-    for (int c = 0; c < m.face_ngrids[f]; c++) m.grid_face[m.face_start[f] + c] = f;
+    for (int c = 0; c < m.face_ngrids[f]; c++) {
+      int& owner = m.grid_face[m.face_start[f] + c];
+      if (owner >= 0) {
+        *err = "a grid belongs to two faces";
+        return false;
+      }
+      owner = f;
+    }
+  for (int g = 0; g < m.num_grids; g++)
+    if (m.grid_face[g] < 0) {
+      *err = "a grid belongs to no face";
+      return false;
+    }
   // subdiv_ccg_init_faces_edge_neighborhood, subdiv_ccg.c:397-466
   std::vector<int> edge_verts = std::move(m.edge_elems);  // caller put edge_verts here
   m.edge_off.assign(m.num_base_edges + 1, 0);

@@ -102,6 +102,7 @@ struct DevMesh {
   // GRIDS topology
   int num_faces, num_base_verts, num_base_edges;
   const int* grid_face;
+  const int4* grid_info;  // per grid: (face, face's first grid, face's grid count, 0)
   const int* face_start;
   const int* face_ngrids;
   const int* face_verts;

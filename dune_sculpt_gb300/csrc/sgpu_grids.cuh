@@ -48,9 +48,10 @@ __device__ __forceinline__ unsigned long long grid_owner_key(unsigned int epoch,
 // once, by the claimed face of least index among its faces, recorded here
 // with a 64-bit minimum per edge and base vertex.
 __device__ __forceinline__ void grid_claim_face_only(const DevMesh& m, int grid, unsigned int epoch) {
-  const int f = m.grid_face[grid];
-  // the face's tables are read-only: loaded before the claim's round trip
-  const int n = m.face_ngrids[f], s = m.face_start[f];
+  // the face, its first grid and its size in one load; the corners' edges and
+  // vertices are loaded alongside the claim's round trip
+  const int4 gi = m.grid_info[grid];
+  const int f = gi.x, s = gi.y, n = gi.z;
   if (!grid_claim(m.face_mark, f, epoch)) return;
   const int fi = atomicAdd(&m.grid_counts[0], 1);
   const int gb = atomicAdd(&m.grid_counts[3], n);
