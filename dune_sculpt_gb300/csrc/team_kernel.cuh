@@ -560,32 +560,47 @@ static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int
 // Compensated area partial of one block (at most kAreaBlock visited
 // vertices) of a culled leaf by the CTA: the lane structure of k_area.  The
 // block's positions and normals are staged in shared memory kAreaStage at a
-// time with cp.async (16 bytes each, no register holds them in flight), so a
-// lane's elements arrive together instead of in dependent batches; lane t
-// then adds its elements t, t+256, ... of the stage in order.
-constexpr int kAreaStage = 1024;  // staged vertices per round: 32 KB (positions, normals)
-static_assert(2 * kAreaStage * sizeof(float4) <= kStageBytes, "the area stage");
+// time with cp.async (16 bytes each, no register holds them in flight), in
+// two buffers, so that the copies of the next round are in flight while the
+// current round is summed; lane t adds its elements t, t+256, ... of each
+// round in order, so the sums are those of the one-round form.
+constexpr int kAreaStage = 512;  // staged vertices per round and buffer: 16 KB
+static_assert(4 * kAreaStage * sizeof(float4) <= kStageBytes, "the area stage");
 static __device__ void team_area_block(const DevMesh& m, const PassParams& pp, float rn2,
                                        float ra2, int leaf, int blk, float4* s_stage, Lane* sl,
                                        AreaPart* out) {
   const int t = threadIdx.x;
   const int i0 = blk * kAreaBlock;
   const int i1 = min(leaf_nverts(m, leaf), i0 + kAreaBlock);
-  float4* s_co = s_stage;
-  float4* s_no = s_stage + kAreaStage;
-  Lane l;
-#pragma unroll
-  for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
-  l.n_no = l.n_co = 0;
-  for (int r0 = i0; r0 < i1; r0 += kAreaStage) {
+  auto issue = [&](int r0, int buf) {
+    float4* s_co = s_stage + 2 * buf * kAreaStage;
+    float4* s_no = s_co + kAreaStage;
     const int r1 = min(i1, r0 + kAreaStage);
     for (int i = r0 + t; i < r1; i += kTeamThreads) {
       const int v = leaf_vert(m, leaf, i);
       cp_async16(&s_co[i - r0], &m.co[v]);
       cp_async16(&s_no[i - r0], &m.no[v]);
     }
-    cp_async_wait_all();
+    cp_async_commit();
+  };
+  Lane l;
+#pragma unroll
+  for (int q = 0; q < 6; q++) l.v[q].s = l.v[q].e = 0.0f;
+  l.n_no = l.n_co = 0;
+  if (i0 < i1) issue(i0, 0);
+  int buf = 0;
+  for (int r0 = i0; r0 < i1; r0 += kAreaStage, buf ^= 1) {
+    // the other buffer was summed before the last barrier: refill it
+    if (r0 + kAreaStage < i1) {
+      issue(r0 + kAreaStage, buf ^ 1);
+      cp_async_wait_group1();
+    } else {
+      cp_async_wait_group0();
+    }
     __syncthreads();
+    const float4* s_co = s_stage + 2 * buf * kAreaStage;
+    const float4* s_no = s_co + kAreaStage;
+    const int r1 = min(i1, r0 + kAreaStage);
     for (int i = r0 + t; i < r1; i += kTeamThreads) {
       const float4 co = s_co[i - r0];
       const float d2 = dist_sq(co, pp.loc);
@@ -603,7 +618,7 @@ static __device__ void team_area_block(const DevMesh& m, const PassParams& pp, f
         l.n_co++;
       }
     }
-    __syncthreads();  // the stage is free for the next round
+    __syncthreads();  // this buffer is free for the round after next
   }
   sl[t] = l;
   __syncthreads();
