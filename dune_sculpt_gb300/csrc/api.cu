@@ -342,6 +342,31 @@ int upload_pbvh(sgpu_mesh* m) {
   if ((rc = m->upload(&d.node_leaf_lo, h.leaf_lo))) return rc;
   if ((rc = m->upload(&d.node_leaf_hi, h.leaf_hi))) return rc;
   if ((rc = m->upload(&d.node_depth, h.depth))) return rc;
+  {
+    // two-level node search: nodes of depth <= split, and the descendant
+    // range of each internal node at the split depth; without contiguous
+    // ranges every node goes in the first level
+    std::vector<int> dlo(N, -1), dhi(N, -1), size(N, 1);
+    for (int n = N - 1; n >= 0; n--) {
+      const int c = h.children[n];
+      if (c < 0) continue;
+      size[n] = 1 + size[c] + size[c + 1];
+      dlo[n] = c;
+      dhi[n] = std::max(std::max(c + 2, dhi[c]), dhi[c + 1]);
+    }
+    bool contiguous = true;
+    for (int n = 0; n < N; n++)
+      if (h.children[n] >= 0 && dhi[n] - dlo[n] != size[n] - 1) contiguous = false;
+    const int split = contiguous ? std::min(h.max_depth, 6) : h.max_depth;
+    std::vector<int4> top;
+    for (int n = 0; n < N; n++) {
+      if (h.depth[n] > split) continue;
+      const bool ranged = h.depth[n] == split && h.children[n] >= 0;
+      top.push_back(make_int4(n, ranged ? dlo[n] : -1, ranged ? dhi[n] : -1, 0));
+    }
+    d.cull_ntop = static_cast<int>(top.size());
+    if ((rc = m->upload(&d.cull_top, top))) return rc;
+  }
   d.max_depth = h.max_depth;
   if (h.max_depth >= 256)
     return fail(SGPU_ERR_UNSUPPORTED, "PBVH depth %d above 255", h.max_depth);

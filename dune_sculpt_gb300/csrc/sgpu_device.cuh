@@ -89,6 +89,13 @@ struct DevMesh {
   const int* node_leaf_lo;   // first leaf id under the node
   const int* node_leaf_hi;   // one past the last leaf id under the node
   const int* node_depth;     // root = 0
+  // Two-level node search of the persistent kernels: every node of depth <=
+  // the mesh's split depth, as (node, first descendant, one past the last
+  // descendant) — the range set only for internal nodes at the split depth,
+  // whose descendants occupy one contiguous index range (children are
+  // allocated in pairs before their subtrees), else (-1, -1)
+  const int4* cull_top;
+  int cull_ntop;
   int max_depth;
   // Refit chunks: each leaf's full vertex list (PBVH_ITER_ALL order) in runs
   // of kChunk entries; chunk_box holds each run's box (2 float4), refreshed by

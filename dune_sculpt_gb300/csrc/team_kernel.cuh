@@ -58,6 +58,11 @@ struct TeamShared {
   int nmark;
   int bar_ok;    // outcome of the whole-GPU team barrier's wait
   DabPasses dp;  // passes of a grab / elastic deform dab
+  // node search, second level: descendant ranges of the passing split-depth
+  // nodes (at most 2^6) and their prefix
+  int nrange;
+  int2 crange[64];
+  int croff[65];
 };
 
 // Block-wide exclusive scan (kTeamThreads threads).
@@ -171,11 +176,12 @@ struct CullTabs {
 
 // Node search of one pass into this CTA's shared memory (every CTA of the team
 // computes the same list).  Same result and order as k_cull: a leaf is listed
-// when its box and the boxes of all its ancestors pass.  Every node box is
-// tested (kBox loads in flight per thread); a failing internal node covers
-// the leaf-id range of its subtree (left-first DFS ranks), recorded as +1/-1
-// in a difference array; a running sum over the leaves then says which
-// leaves lie under a failing ancestor.  Each thread owns a run of consecutive
+// when its box and the boxes of all its ancestors pass.  Node boxes are
+// tested in two levels: every node down to the mesh's split depth, then the
+// descendants of the split-depth nodes that passed (kBox loads in flight per
+// thread); a failing internal node covers the leaf-id range of its subtree
+// (left-first DFS ranks), recorded as +1/-1 in a difference array; a running
+// sum over the leaves then says which leaves lie under a failing ancestor.  Each thread owns a run of consecutive
 // leaves (at most 64: the team kernel takes at most 64 * 256 leaves); block
 // scans give the coverage entering the run and the list positions.  s_coff
 // doubles as the difference array.
@@ -185,14 +191,58 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
                                              const Tabs& ct, TeamShared& sh) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
+  if (threadIdx.x == 0) sh.nrange = 0;
   __syncthreads();
-  for (int n0 = threadIdx.x; n0 < m.totnode; n0 += kBox * kTeamThreads) {
+  // A failing internal node marks its leaves' id range in the difference
+  // array; every tested node records its outcome.
+  auto outcome = [&](int n, bool hit, int llo, int lhi) {
+    s_pass[n] = hit;
+    if (!hit && lhi - llo > 1) {  // internal node (leaves own a range of one)
+      atomicAdd(&s_coff[llo], 1);
+      atomicAdd(&s_coff[lhi], -1);
+    }
+  };
+  // First level: every node down to the split depth; a passing internal node
+  // at the split depth lists its descendants' range for the second level.
+  for (int k = threadIdx.x; k < m.cull_ntop; k += kTeamThreads) {
+    const int4 e = m.cull_top[k];
+    const float4 lo = __ldcg(&bb[2 * e.x]), hi = __ldcg(&bb[2 * e.x + 1]);
+    const bool hit = hits(lo, hi);
+    outcome(e.x, hit, m.node_leaf_lo[e.x], m.node_leaf_hi[e.x]);
+    if (hit && e.y >= 0) sh.crange[atomicAdd(&sh.nrange, 1)] = make_int2(e.y, e.z);
+  }
+  __syncthreads();
+  // Second level: the listed ranges, every node tested (kBox loads in flight
+  // per thread).  Nodes under a failing split-depth node are not tested: its
+  // mark covers their leaves, and the leaf pass below reads no outcome there.
+  const int R = sh.nrange;
+  if (threadIdx.x < 32) {
+    int a = 2 * threadIdx.x < R ? sh.crange[2 * threadIdx.x].y - sh.crange[2 * threadIdx.x].x : 0;
+    int b = 2 * threadIdx.x + 1 < R
+                ? sh.crange[2 * threadIdx.x + 1].y - sh.crange[2 * threadIdx.x + 1].x : 0;
+    int x = a + b;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (static_cast<int>(threadIdx.x) >= o) x += y;
+    }
+    sh.croff[2 * threadIdx.x] = x - a - b;
+    sh.croff[2 * threadIdx.x + 1] = x - b;
+    if (threadIdx.x == 31) sh.croff[64] = x;
+  }
+  __syncthreads();
+  const int T2 = sh.croff[64];
+  for (int i0 = threadIdx.x; i0 < T2; i0 += kBox * kTeamThreads) {
     float4 lo[kBox], hi[kBox];
-    int llo[kBox], lhi[kBox];
+    int nn[kBox], llo[kBox], lhi[kBox];
 #pragma unroll
     for (int j = 0; j < kBox; j++) {
-      const int n = n0 + j * kTeamThreads;
-      if (n < m.totnode) {
+      const int i = i0 + j * kTeamThreads;
+      nn[j] = -1;
+      if (i < T2) {
+        const int r = smem_find_slot(sh.croff, R, i);
+        const int n = sh.crange[r].x + (i - sh.croff[r]);
+        nn[j] = n;
         lo[j] = __ldcg(&bb[2 * n]);
         hi[j] = __ldcg(&bb[2 * n + 1]);
         llo[j] = m.node_leaf_lo[n];
@@ -200,16 +250,8 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
       }
     }
 #pragma unroll
-    for (int j = 0; j < kBox; j++) {
-      const int n = n0 + j * kTeamThreads;
-      if (n >= m.totnode) continue;
-      const bool hit = hits(lo[j], hi[j]);
-      s_pass[n] = hit;
-      if (!hit && lhi[j] - llo[j] > 1) {  // internal node (leaves own a range of one)
-        atomicAdd(&s_coff[llo[j]], 1);
-        atomicAdd(&s_coff[lhi[j]], -1);
-      }
-    }
+    for (int j = 0; j < kBox; j++)
+      if (nn[j] >= 0) outcome(nn[j], hits(lo[j], hi[j]), llo[j], lhi[j]);
   }
   __syncthreads();
   const int seg = (L + kTeamThreads - 1) / kTeamThreads;
