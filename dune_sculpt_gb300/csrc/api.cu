@@ -1186,6 +1186,7 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
   if ((rc = m->upload(&d.bvert_face, h.bvert_face))) return bail(rc);
   d.max_face_corners = h.max_face_corners;
   if ((rc = m->alloc(&d.face_list, num_faces))) return bail(rc);
+  if ((rc = m->alloc(&d.face_info, num_faces))) return bail(rc);
   if ((rc = m->alloc(&d.cgrid_list, num_grids))) return bail(rc);
   if ((rc = m->alloc(&d.edge_list, num_base_edges))) return bail(rc);
   if ((rc = m->alloc(&d.bvert_list, num_base_verts))) return bail(rc);

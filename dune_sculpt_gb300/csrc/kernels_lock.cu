@@ -721,7 +721,8 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_lock_stroke(TeamAr
       for (int it = static_cast<int>(rank); it < NF; it += static_cast<int>(C)) {
         const int j = find_job(it);
         const DevMesh& m = mesh_of(j);
-        team_grid_face(m, __ldcg(&m.face_list[it - s_P[j]]), dyn,
+        const int2 fs = __ldcg(&m.face_info[it - s_P[j]]);
+        team_grid_face(m, __ldcg(&m.face_list[it - s_P[j]]), fs.x, fs.y, dyn,
                        face_grid_group(m.grid_size, kStageBytes), s_ep0[j] + d + 1u);
       }
       clk.mark(a, rank, kPhGridFaces);
@@ -729,7 +730,9 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_lock_stroke(TeamAr
       for (int it = static_cast<int>(rank); it < NF; it += static_cast<int>(C)) {
         const int j = find_job(it);
         const DevMesh& m = mesh_of(j);
-        team_grid_face_boundary(m, __ldcg(&m.face_list[it - s_P[j]]), s_ep0[j] + d + 1u, true);
+        const int2 fs = __ldcg(&m.face_info[it - s_P[j]]);
+        team_grid_face_boundary(m, __ldcg(&m.face_list[it - s_P[j]]), fs.x, fs.y, s_ep0[j] + d + 1u,
+                                true);
       }
       clk.mark(a, rank, kPhGridSeams);
       LOCK_SYNC();

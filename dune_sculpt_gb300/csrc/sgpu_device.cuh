@@ -122,6 +122,7 @@ struct DevMesh {
   const int* bvert_face;  // face of each bvert_elems slot
   int max_face_corners;
   int* face_list;
+  int2* face_info;  // per claimed face (face_list order): its first grid and grid count
   int* cgrid_list;  // grids of the claimed faces
   int* edge_list;
   int* bvert_list;

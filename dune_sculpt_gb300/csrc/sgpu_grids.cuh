@@ -72,6 +72,7 @@ __device__ __forceinline__ void grid_claim_face_only(const DevMesh& m, int grid,
       }
   }
   m.face_list[fi] = f;
+  m.face_info[fi] = make_int2(s, n);
   for (int c = 0; c < n; c++) m.cgrid_list[gb + c] = s + c;
 }
 

@@ -803,9 +803,8 @@ __device__ __forceinline__ float3 staged_normal(const float3* s_q, int i, int gs
 // least index, whose key the claims left in edge_own / bvert_own; the
 // owner's record holds the element slots and face count, the others' a count
 // of 0.  Needs the epoch's claims complete.
-__device__ __forceinline__ void grid_corner_owners(const DevMesh& m, int f, unsigned int epoch,
-                                                   int t_begin, int t_step) {
-  const int s = m.face_start[f], n = m.face_ngrids[f];
+__device__ __forceinline__ void grid_corner_owners(const DevMesh& m, int f, int s, int n,
+                                                   unsigned int epoch, int t_begin, int t_step) {
   const unsigned long long key = grid_owner_key(epoch, f);
   for (int t = t_begin; t < 2 * n; t += t_step) {
     const bool edge = t < n;
@@ -833,10 +832,9 @@ __device__ __forceinline__ void grid_corner_owners(const DevMesh& m, int f, unsi
 // base-edge pass averages afterwards.  GRIDS positions carry w = 0.
 // The owner records of the face's corners are written while the first
 // stage is in flight (grid_corner_owners).
-static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* stage, int group,
-                                      unsigned int epoch) {
+static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, unsigned char* stage,
+                                      int group, unsigned int epoch) {
   const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area, qa = g1 * g1;
-  const int s = m.face_start[f], n = m.face_ngrids[f];
   float4* s_co = reinterpret_cast<float4*>(stage);
   float* s_mk = reinterpret_cast<float*>(s_co + group * area);
   float3* s_q = reinterpret_cast<float3*>(s_mk + group * area);  // quad normals
@@ -848,7 +846,7 @@ static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* st
       cp_async16(&s_co[i], &m.co[e]);
       if (m.mask) cp_async4(&s_mk[i], &m.mask[e]);
     }
-    if (c0 == 0) grid_corner_owners(m, f, epoch, threadIdx.x, kTeamThreads);
+    if (c0 == 0) grid_corner_owners(m, f, s, n, epoch, threadIdx.x, kTeamThreads);
     cp_async_wait_all();
     __syncthreads();
     for (int i = threadIdx.x; i < nc * qa; i += kTeamThreads) {
@@ -938,12 +936,11 @@ static __device__ void team_grid_face(const DevMesh& m, int f, unsigned char* st
 // records (the face went through team_grid_face this dab) the owner
 // decisions are read from corner_own; without (the unstaged path) they are
 // made here first, one thread per corner record.
-static __device__ void team_grid_face_boundary(const DevMesh& m, int f, unsigned int epoch,
-                                               bool records) {
+static __device__ void team_grid_face_boundary(const DevMesh& m, int f, int s, int n,
+                                               unsigned int epoch, bool records) {
   const int g2 = 2 * m.grid_size, per_corner = g2 - 1;
-  const int s = m.face_start[f], n = m.face_ngrids[f];
   if (!records) {
-    grid_corner_owners(m, f, epoch, threadIdx.x, kTeamThreads);
+    grid_corner_owners(m, f, s, n, epoch, threadIdx.x, kTeamThreads);
     __syncthreads();  // the CTA's own records (global memory, CTA barrier)
   }
   for (int it = threadIdx.x; it < n * per_corner; it += kTeamThreads) {
@@ -1472,9 +1469,10 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         if (group > 0) {
           for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C)) {
             const int f = __ldcg(&m.face_list[fi]);
-            team_grid_face(m, f, dyn, group, epoch);
+            const int2 fs = __ldcg(&m.face_info[fi]);
+            team_grid_face(m, f, fs.x, fs.y, dyn, group, epoch);
             if (threadIdx.x == 0) {
-              const int n = m.face_ngrids[f];
+              const int n = fs.y;
               // positions read, normals written; the seam pairs and the
               // centre read and write co, no and mask
               ab += 24ull * n * m.grid_area + 112ull * n * (m.grid_size - 1) + 56ull * n;
@@ -1501,7 +1499,10 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           TEAM_SYNC();
         }
         for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C))
-          team_grid_face_boundary(m, __ldcg(&m.face_list[fi]), epoch, group > 0);
+          {
+            const int2 fs = __ldcg(&m.face_info[fi]);
+            team_grid_face_boundary(m, __ldcg(&m.face_list[fi]), fs.x, fs.y, epoch, group > 0);
+          }
         TEAM_SYNC();
         clk.mark(a, rank, kPhGridSeams);
         if (rank == 0 && threadIdx.x == 0)
