@@ -357,14 +357,18 @@ int upload_pbvh(sgpu_mesh* m) {
     bool contiguous = true;
     for (int n = 0; n < N; n++)
       if (h.children[n] >= 0 && dhi[n] - dlo[n] != size[n] - 1) contiguous = false;
+    // up to 4096 nodes (two rounds of batched box loads) the one-level
+    // search over every node is as short: no first-level list then
     const int split = contiguous ? std::min(h.max_depth, 6) : h.max_depth;
+    const bool two_level = contiguous && N > 4096;
     std::vector<int4> top;
     for (int n = 0; n < N; n++) {
       if (h.depth[n] > split) continue;
       const bool ranged = h.depth[n] == split && h.children[n] >= 0;
       top.push_back(make_int4(n, ranged ? dlo[n] : -1, ranged ? dhi[n] : -1, 0));
     }
-    d.cull_ntop = static_cast<int>(top.size());
+    if (!two_level) top.assign(1, make_int4(0, -1, -1, 0));
+    d.cull_ntop = two_level ? static_cast<int>(top.size()) : 0;
     if ((rc = m->upload(&d.cull_top, top))) return rc;
   }
   d.max_depth = h.max_depth;

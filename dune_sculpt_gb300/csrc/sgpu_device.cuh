@@ -95,7 +95,7 @@ struct DevMesh {
   // whose descendants occupy one contiguous index range (children are
   // allocated in pairs before their subtrees), else (-1, -1)
   const int4* cull_top;
-  int cull_ntop;
+  int cull_ntop;  // 0: one level, every node tested directly
   int max_depth;
   // Refit chunks: each leaf's full vertex list (PBVH_ITER_ALL order) in runs
   // of kChunk entries; chunk_box holds each run's box (2 float4), refreshed by

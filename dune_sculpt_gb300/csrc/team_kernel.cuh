@@ -191,7 +191,11 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
                                              const Tabs& ct, TeamShared& sh) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
-  if (threadIdx.x == 0) sh.nrange = 0;
+  // one-level search (cull_ntop 0): the second level's single range is every node
+  if (threadIdx.x == 0) {
+    sh.nrange = m.cull_ntop == 0 ? 1 : 0;
+    sh.crange[0] = make_int2(0, m.totnode);
+  }
   __syncthreads();
   // A failing internal node marks its leaves' id range in the difference
   // array; every tested node records its outcome.
