@@ -2382,6 +2382,8 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   a.next_job = m0->t_counter;
   a.orig = 0;
   for (int i = 0; i < n; i++) a.orig |= h_orig[i];
+  a.two_level = 0;
+  for (int i = 0; i < n; i++) a.two_level |= meshes[i]->dev.cull_ntop > 0 ? 1 : 0;
   a.max_nodes = max_nodes;
   a.max_leaves = max_leaves;
   a.prof_bytes = g_team_prof_bytes;

@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_lock_stroke(TeamAr
         const int tool = s_tool[j];
         const PassParams pp = pass_params(jb, b, d, pass, tool);
         const LockTabs tabs{{m.leaf_node}, {&m}};
-        team_cull<8>(m, pp, s_pass, s_cl, s_coff, tabs, sh);
+        team_cull<8, kMinBlocks == 1>(m, pp, s_pass, s_cl, s_coff, tabs, sh);
         const int cnt = sh.cnt, total = sh.total;
         for (int k = threadIdx.x; k < cnt; k += kTeamThreads) {
           m.cull_list[k] = s_cl[k];

@@ -24,19 +24,26 @@ size_t team_smem_bytes(int max_nodes, int max_leaves) {
 
 int team_max_cluster() { return 16; }
 
-template <int kMinBlocks, bool kOrig>
+template <int kMinBlocks, bool kOrig, bool kTwoLevel>
 cudaError_t configure_team_build(size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_team_stroke<kMinBlocks, kOrig, false>,
+  cudaError_t e = cudaFuncSetAttribute(k_team_stroke<kMinBlocks, kOrig, false, kTwoLevel>,
                                        cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_team_stroke<kMinBlocks, kOrig, false>,
+  return cudaFuncSetAttribute(k_team_stroke<kMinBlocks, kOrig, false, kTwoLevel>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
 }
 
+// The builds of one CTA-per-SM count; the one-CTA-per-SM builds also come
+// with the two-level node search (launches with a large tree take them).
 template <int kMinBlocks>
 cudaError_t configure_team_kernel(size_t smem) {
-  const cudaError_t e = configure_team_build<kMinBlocks, false>(smem);
-  return e != cudaSuccess ? e : configure_team_build<kMinBlocks, true>(smem);
+  cudaError_t e = configure_team_build<kMinBlocks, false, false>(smem);
+  if (e == cudaSuccess) e = configure_team_build<kMinBlocks, true, false>(smem);
+  if constexpr (kMinBlocks == 1) {
+    if (e == cudaSuccess) e = configure_team_build<kMinBlocks, false, true>(smem);
+    if (e == cudaSuccess) e = configure_team_build<kMinBlocks, true, true>(smem);
+  }
+  return e;
 }
 
 static cudaLaunchConfig_t team_config(int cluster, int nteams, size_t smem, cudaStream_t s,
@@ -105,6 +112,9 @@ cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s, i
   if (two)
     return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<2, true, false>, a)
                   : cudaLaunchKernelEx(&cfg, k_team_stroke<2, false, false>, a);
+  if (a.two_level)
+    return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true, false, true>, a)
+                  : cudaLaunchKernelEx(&cfg, k_team_stroke<1, false, false, true>, a);
   return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true, false>, a)
                 : cudaLaunchKernelEx(&cfg, k_team_stroke<1, false, false>, a);
 }

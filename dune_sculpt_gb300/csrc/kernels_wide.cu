@@ -16,7 +16,11 @@ namespace sgpu {
 
 template <bool kOrig>
 static cudaError_t configure_wide(size_t smem) {
-  return cudaFuncSetAttribute(k_team_stroke<1, kOrig, true>,
+  const cudaError_t e = cudaFuncSetAttribute(k_team_stroke<1, kOrig, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_team_stroke<1, kOrig, true, true>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
 }
 
@@ -40,12 +44,17 @@ int team_wide_ctas(int max_nodes, int max_leaves) {
     return 0;
   configured[dev] = want;
   int n0 = 0, n1 = 0;
+  int n2 = 0, n3 = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, k_team_stroke<1, false, true>,
                                                     kTeamThreads, smem) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_team_stroke<1, true, true>,
+                                                    kTeamThreads, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_team_stroke<1, false, true, true>,
+                                                    kTeamThreads, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_team_stroke<1, true, true, true>,
                                                     kTeamThreads, smem) != cudaSuccess)
     return 0;
-  const int n = (std::min(n0, n1) >= 1) ? std::min(sms, kTeamMaxWideCtas) : 0;
+  const int n = (std::min(std::min(n0, n1), std::min(n2, n3)) >= 1) ? std::min(sms, kTeamMaxWideCtas) : 0;
   cache[key] = n;
   return n;
 }
@@ -61,6 +70,9 @@ cudaError_t launch_team_stroke_wide(const TeamArgs& a, int nctas, cudaStream_t s
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (a.two_level)
+    return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true, true, true>, a)
+                  : cudaLaunchKernelEx(&cfg, k_team_stroke<1, false, true, true>, a);
   return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true, true>, a)
                 : cudaLaunchKernelEx(&cfg, k_team_stroke<1, false, true>, a);
 }

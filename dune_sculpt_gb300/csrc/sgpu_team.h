@@ -45,6 +45,7 @@ struct TeamArgs {
   unsigned long long wait_ns;
   int bar_extra;
   int orig;       // some job has grab, elastic deform or layer dabs
+  int two_level;  // some mesh's node search takes two levels (its build runs it)
   int max_nodes, max_leaves;  // shared-memory sizing over the meshes
   // profiling (nullable): algorithmic bytes and nanoseconds per phase
   unsigned long long* prof_bytes;  // kTeamPhases entries

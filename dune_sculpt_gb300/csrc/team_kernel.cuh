@@ -185,14 +185,14 @@ struct CullTabs {
 // leaves (at most 64: the team kernel takes at most 64 * 256 leaves); block
 // scans give the coverage entering the run and the list positions.  s_coff
 // doubles as the difference array.
-template <int kBox, class Hit, class Tabs>
+template <int kBox, bool kTwoLevel, class Hit, class Tabs>
 __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb, Hit hits,
                                              unsigned char* s_pass, int* s_cl, int* s_coff,
                                              const Tabs& ct, TeamShared& sh) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
   // one-level search (cull_ntop 0): the second level's single range is every node
-  if (threadIdx.x == 0) {
+  if (kTwoLevel && threadIdx.x == 0) {
     sh.nrange = m.cull_ntop == 0 ? 1 : 0;
     sh.crange[0] = make_int2(0, m.totnode);
   }
@@ -206,6 +206,29 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
       atomicAdd(&s_coff[lhi], -1);
     }
   };
+  if constexpr (!kTwoLevel) {
+    // the build without the two-level code: every node box tested directly
+    // (the same outcomes; launches whose trees are all small take it)
+    for (int n0 = threadIdx.x; n0 < m.totnode; n0 += kBox * kTeamThreads) {
+      float4 lo[kBox], hi[kBox];
+      int llo[kBox], lhi[kBox];
+#pragma unroll
+      for (int j = 0; j < kBox; j++) {
+        const int n = n0 + j * kTeamThreads;
+        if (n < m.totnode) {
+          lo[j] = __ldcg(&bb[2 * n]);
+          hi[j] = __ldcg(&bb[2 * n + 1]);
+          llo[j] = m.node_leaf_lo[n];
+          lhi[j] = m.node_leaf_hi[n];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kBox; j++) {
+        const int n = n0 + j * kTeamThreads;
+        if (n < m.totnode) outcome(n, hits(lo[j], hi[j]), llo[j], lhi[j]);
+      }
+    }
+  } else {
   // First level: every node down to the split depth; a passing internal node
   // at the split depth lists its descendants' range for the second level.
   for (int k = threadIdx.x; k < m.cull_ntop; k += kTeamThreads) {
@@ -256,6 +279,7 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
 #pragma unroll
     for (int j = 0; j < kBox; j++)
       if (nn[j] >= 0) outcome(nn[j], hits(lo[j], hi[j]), llo[j], lhi[j]);
+  }
   }
   __syncthreads();
   const int seg = (L + kTeamThreads - 1) / kTeamThreads;
@@ -326,10 +350,10 @@ __device__ __forceinline__ unsigned long long team_orig_sweep(const DevMesh& m, 
 }
 
 // The node search of one pass (sphere at the pass location).
-template <int kBox, class Tabs>
+template <int kBox, bool kTwoLevel, class Tabs>
 __device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char* s_pass,
                           int* s_cl, int* s_coff, const Tabs& ct, TeamShared& sh) {
-  team_cull_by<kBox>(
+  team_cull_by<kBox, kTwoLevel>(
       m, pp.original ? m.orig_vb : m.vb,
       [&](float4 lo, float4 hi) { return box_hits(lo, hi, pp.loc, pp.cull_radius_sq); }, s_pass,
       s_cl, s_coff, ct, sh);
@@ -337,10 +361,11 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char*
 
 // The gather of one grab / elastic deform dab (k_cull_dab): orig_vb boxes that
 // meet any pass sphere, or every leaf (all != 0).
+template <bool kTwoLevel>
 __device__ __forceinline__ void team_cull_union(const DevMesh& m, const DabPasses& dp, float rsq,
                                              int all, unsigned char* s_pass, int* s_cl,
                                              int* s_coff, const CullTabs& ct, TeamShared& sh) {
-  team_cull_by<2>(
+  team_cull_by<2, kTwoLevel>(
       m, m.orig_vb,
       [&](float4 lo, float4 hi) {
         bool ok = all != 0;
@@ -1065,7 +1090,7 @@ struct PhaseClock {
 // other build carries none of their code).
 // kWide: the whole-GPU team (cooperative launch, one CTA per SM), which runs
 // the jobs one after another.
-template <int kMinBlocks, bool kOrig, bool kWide>
+template <int kMinBlocks, bool kOrig, bool kWide, bool kTwoLevel = false>
 __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamArgs a) {
   unsigned C, rank;
   if constexpr (kWide) {
@@ -1220,7 +1245,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           b.kl_f = sqrtf(gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2]) * b.strength;
         }
         __syncthreads();
-        team_cull_union(m, sh.dp, b.radius * b.radius, tool == kToolElasticDeform ? 1 : 0, s_pass,
+        team_cull_union<kTwoLevel>(m, sh.dp, b.radius * b.radius, tool == kToolElasticDeform ? 1 : 0, s_pass,
                         s_cl, s_coff, ct, sh);
         const int cnt = sh.cnt, total = sh.total;
         team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
@@ -1249,7 +1274,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         pp.original = sh.job.use_orig || (kOrig && tool == kToolLayer);  // layer: stroke-start boxes
         pp.iter_strength = 1.0f;
         pp.iteration = 0;
-        team_cull<kMinBlocks == 1 ? 8 : 2>(m, pp, s_pass, s_cl, s_coff, ct, sh);
+        team_cull<kMinBlocks == 1 ? 8 : 2, kTwoLevel>(m, pp, s_pass, s_cl, s_coff, ct, sh);
         const int cnt = sh.cnt, total = sh.total;
         // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
         team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
