@@ -25,7 +25,8 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
-CU_SOURCES = ["kernels_team.cu", "kernels_wide.cu", "kernels_lock.cu", "kernels.cu", "kernels_grids.cu", "kernels_ray.cu",
+CU_SOURCES = ["kernels_team.cu", "kernels_wide.cu", "kernels_sym.cu", "kernels_lock.cu", "kernels.cu", "kernels_grids.cu",
+              "kernels_ray.cu",
               "kernels_draw.cu", "noalloc.cu", "api.cu"]
 CXX_SOURCES = ["host_pbvh.cpp", "host_draw.cpp"]
 

@@ -2384,6 +2384,11 @@ int team_batch(sgpu_mesh** meshes, int n, const SGPU_Brush* brushes, const SGPU_
   for (int i = 0; i < n; i++) a.orig |= h_orig[i];
   a.two_level = 0;
   for (int i = 0; i < n; i++) a.two_level |= meshes[i]->dev.cull_ntop > 0 ? 1 : 0;
+  a.sym = 0;
+  for (int i = 0; i < n; i++) {
+    const int sy = brushes[i].symmetry & 7;
+    a.sym |= (sy == 1 || sy == 2 || sy == 4) ? 1 : 0;
+  }
   a.max_nodes = max_nodes;
   a.max_leaves = max_leaves;
   a.prof_bytes = g_team_prof_bytes;

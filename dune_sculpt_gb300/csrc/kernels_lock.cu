@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_lock_stroke(TeamAr
           const int nb = m.area_blocks;
           const float rn = b.radius * b.normal_radius_factor;
           const float ra = b.radius * b.area_radius_factor;
-          team_area_block(m, pp, rn * rn, ra * ra, __ldcg(&m.cull_list[k / nb]), k % nb, s_stage,
+          team_area_block(m, pp.loc, rn * rn, ra * ra, __ldcg(&m.cull_list[k / nb]), k % nb, s_stage,
                           s_scr.lanes, &m.parts[k]);
           if (threadIdx.x == 0) {
             __threadfence();

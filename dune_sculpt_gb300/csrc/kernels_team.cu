@@ -34,7 +34,8 @@ cudaError_t configure_team_build(size_t smem) {
 }
 
 // The builds of one CTA-per-SM count; the one-CTA-per-SM builds also come
-// with the two-level node search (launches with a large tree take them).
+// with the two-level node search (launches with a large tree take them) and
+// with paired symmetry passes (kernels_sym.cu).
 template <int kMinBlocks>
 cudaError_t configure_team_kernel(size_t smem) {
   cudaError_t e = configure_team_build<kMinBlocks, false, false>(smem);
@@ -42,6 +43,7 @@ cudaError_t configure_team_kernel(size_t smem) {
   if constexpr (kMinBlocks == 1) {
     if (e == cudaSuccess) e = configure_team_build<kMinBlocks, false, true>(smem);
     if (e == cudaSuccess) e = configure_team_build<kMinBlocks, true, true>(smem);
+    if (e == cudaSuccess) e = configure_team_sym(smem);
   }
   return e;
 }
@@ -112,6 +114,7 @@ cudaError_t launch_team_stroke(const TeamArgs& a, int cluster, cudaStream_t s, i
   if (two)
     return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<2, true, false>, a)
                   : cudaLaunchKernelEx(&cfg, k_team_stroke<2, false, false>, a);
+  if (a.sym && !a.orig) return launch_team_sym(a, cfg, false);
   if (a.two_level)
     return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true, false, true>, a)
                   : cudaLaunchKernelEx(&cfg, k_team_stroke<1, false, false, true>, a);

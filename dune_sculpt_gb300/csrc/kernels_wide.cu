@@ -40,7 +40,8 @@ int team_wide_ctas(int max_nodes, int max_leaves) {
     return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
   const size_t want = std::max(smem, configured[dev]);
-  if (configure_wide<false>(want) != cudaSuccess || configure_wide<true>(want) != cudaSuccess)
+  if (configure_wide<false>(want) != cudaSuccess || configure_wide<true>(want) != cudaSuccess ||
+      configure_wide_sym(want) != cudaSuccess)
     return 0;
   configured[dev] = want;
   int n0 = 0, n1 = 0;
@@ -54,7 +55,8 @@ int team_wide_ctas(int max_nodes, int max_leaves) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_team_stroke<1, true, true, true>,
                                                     kTeamThreads, smem) != cudaSuccess)
     return 0;
-  const int n = (std::min(std::min(n0, n1), std::min(n2, n3)) >= 1) ? std::min(sms, kTeamMaxWideCtas) : 0;
+  const int n = (std::min(std::min(n0, n1), std::min(n2, n3)) >= 1 && sym_wide_ok(smem))
+                    ? std::min(sms, kTeamMaxWideCtas) : 0;
   cache[key] = n;
   return n;
 }
@@ -70,6 +72,7 @@ cudaError_t launch_team_stroke_wide(const TeamArgs& a, int nctas, cudaStream_t s
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (a.sym && !a.orig) return launch_team_sym(a, cfg, true);
   if (a.two_level)
     return a.orig ? cudaLaunchKernelEx(&cfg, k_team_stroke<1, true, true, true>, a)
                   : cudaLaunchKernelEx(&cfg, k_team_stroke<1, false, true, true>, a);

@@ -46,6 +46,7 @@ struct TeamArgs {
   int bar_extra;
   int orig;       // some job has grab, elastic deform or layer dabs
   int two_level;  // some mesh's node search takes two levels (its build runs it)
+  int sym;        // some stroke mirrors in one axis (the builds that pair passes run it)
   int max_nodes, max_leaves;  // shared-memory sizing over the meshes
   // profiling (nullable): algorithmic bytes and nanoseconds per phase
   unsigned long long* prof_bytes;  // kTeamPhases entries
@@ -83,6 +84,15 @@ int team_wide_ctas(int max_nodes, int max_leaves);
 // Upper bound of team_wide_ctas on any device (sizes the smooth slot arrays).
 constexpr int kTeamMaxWideCtas = 1024;
 cudaError_t launch_team_stroke_wide(const TeamArgs& a, int nctas, cudaStream_t s);
+// The builds that pair the passes of a single-axis symmetry (kernels_sym.cu):
+// one CTA per SM, no stroke-start brushes; cluster and whole-GPU teams with
+// either node search.  configure_* set their shared-memory limit (and the
+// cluster builds' non-portable cluster sizes); sym_wide_ok: each whole-GPU
+// build holds a CTA on an SM with smem bytes.
+cudaError_t configure_team_sym(size_t smem);
+cudaError_t configure_wide_sym(size_t smem);
+bool sym_wide_ok(size_t smem);
+cudaError_t launch_team_sym(const TeamArgs& a, const cudaLaunchConfig_t& cfg, bool wide);
 
 // Lockstep batch launch (kernels_lock.cu): every CTA of one cooperative
 // launch (one per SM) runs every stroke of the batch, dab by dab; each phase

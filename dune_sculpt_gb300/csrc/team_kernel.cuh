@@ -63,6 +63,14 @@ struct TeamShared {
   int nrange;
   int2 crange[64];
   int croff[65];
+  // both passes of a single-axis symmetry searched at once (team_cull_pair):
+  // split = first list entry of the second pass when they run as one (joint;
+  // the list's length otherwise); held = entries of the second pass's list
+  // stored behind the first one's (-1: none), with its vertex total, first
+  // entry and first offset; live1 = the joint second pass has a frame
+  int split, joint, held, held_total, held_base, held_off, live1, pair_ovl;
+  PassParams mpp[2];    // the passes' parameters and frames read by the area
+  BrushFrame mframe[2]; // blocks and the sweep (one pass, or a joint pair)
 };
 
 // Block-wide exclusive scan (kTeamThreads threads).
@@ -185,10 +193,22 @@ struct CullTabs {
 // leaves (at most 64: the team kernel takes at most 64 * 256 leaves); block
 // scans give the coverage entering the run and the list positions.  s_coff
 // doubles as the difference array.
-template <int kBox, bool kTwoLevel, class Hit, class Tabs>
+//
+// kPair: two spheres at once (the two passes of a single-axis symmetry);
+// hits returns a pass mask (bit p: the box meets sphere p), the difference
+// array counts pass 0 in its low 16 bits and pass 1 above (coverage is at
+// most the tree depth), and the lists are written one after the other:
+// pass 0's at [0, sh.split), pass 1's behind it with its vertex offsets
+// continuing from pass 0's total — when both fit the list arrays (cap
+// entries; cap 0: one sphere, bit 1 never set).  Then: lists without a
+// common leaf under a joinable tool make one list of both (sh.joint, sh.cnt
+// and sh.total over both); otherwise sh.cnt and sh.total are pass 0's and
+// sh.held counts pass 1's stored entries (-1 when they did not fit).
+template <int kBox, bool kTwoLevel, bool kPair = false, class Hit, class Tabs>
 __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb, Hit hits,
                                              unsigned char* s_pass, int* s_cl, int* s_coff,
-                                             const Tabs& ct, TeamShared& sh) {
+                                             const Tabs& ct, TeamShared& sh, int cap = 0,
+                                             bool joinable = false) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
   // one-level search (cull_ntop 0): the second level's single range is every node
@@ -196,12 +216,19 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
     sh.nrange = m.cull_ntop == 0 ? 1 : 0;
     sh.crange[0] = make_int2(0, m.totnode);
   }
+  if (kPair && threadIdx.x == 0) sh.pair_ovl = 0;
   __syncthreads();
   // A failing internal node marks its leaves' id range in the difference
   // array; every tested node records its outcome.
-  auto outcome = [&](int n, bool hit, int llo, int lhi) {
-    s_pass[n] = hit;
-    if (!hit && lhi - llo > 1) {  // internal node (leaves own a range of one)
+  auto outcome = [&](int n, unsigned hit, int llo, int lhi) {
+    s_pass[n] = static_cast<unsigned char>(hit);
+    if constexpr (kPair) {
+      const int inc = ((hit & 1u) ? 0 : 1) + ((cap > 0 && !(hit & 2u)) ? 65536 : 0);
+      if (inc != 0 && lhi - llo > 1) {
+        atomicAdd(&s_coff[llo], inc);
+        atomicAdd(&s_coff[lhi], -inc);
+      }
+    } else if (!hit && lhi - llo > 1) {  // internal node (leaves own a range of one)
       atomicAdd(&s_coff[llo], 1);
       atomicAdd(&s_coff[lhi], -1);
     }
@@ -234,7 +261,7 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
   for (int k = threadIdx.x; k < m.cull_ntop; k += kTeamThreads) {
     const int4 e = m.cull_top[k];
     const float4 lo = __ldcg(&bb[2 * e.x]), hi = __ldcg(&bb[2 * e.x + 1]);
-    const bool hit = hits(lo, hi);
+    const unsigned hit = hits(lo, hi);
     outcome(e.x, hit, m.node_leaf_lo[e.x], m.node_leaf_hi[e.x]);
     if (hit && e.y >= 0) sh.crange[atomicAdd(&sh.nrange, 1)] = make_int2(e.y, e.z);
   }
@@ -290,13 +317,75 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
   int cov = team_block_scan(dsum, &dtot, sh.scan);
   unsigned long long okmask = 0ull;
   unsigned long long cnt = 0ull, nvs = 0ull;
-  for (int id = l0; id < l1; id++) {
-    cov += s_coff[id];
-    if (cov == 0 && s_pass[ct.lnode[id]]) {
-      cnt++;
-      nvs += static_cast<unsigned long long>(ct.lnv[id]);
-      okmask |= 1ull << (id - l0);
+  if constexpr (!kPair) {
+    for (int id = l0; id < l1; id++) {
+      cov += s_coff[id];
+      if (cov == 0 && s_pass[ct.lnode[id]]) {
+        cnt++;
+        nvs += static_cast<unsigned long long>(ct.lnv[id]);
+        okmask |= 1ull << (id - l0);
+      }
     }
+  } else {
+    unsigned long long okmask1 = 0ull, cnt1 = 0ull, nvs1 = 0ull;
+    const bool two = cap > 0;
+    for (int id = l0; id < l1; id++) {
+      cov += s_coff[id];
+      const bool in0 = (cov & 0xFFFF) == 0, in1 = two && (cov >> 16) == 0;
+      if (!in0 && !in1) continue;  // under a failing ancestor of every sphere
+      const unsigned pm = s_pass[ct.lnode[id]];
+      if (in0 && (pm & 1u)) {
+        cnt++;
+        nvs += static_cast<unsigned long long>(ct.lnv[id]);
+        okmask |= 1ull << (id - l0);
+      }
+      if (in1 && (pm & 2u)) {
+        cnt1++;
+        nvs1 += static_cast<unsigned long long>(ct.lnv[id]);
+        okmask1 |= 1ull << (id - l0);
+      }
+    }
+    if (okmask & okmask1) sh.pair_ovl = 1;
+    unsigned long long total0, total1 = 0ull, excl1 = 0ull;
+    const unsigned long long excl0 = team_block_scan64((nvs << 24) | cnt, &total0, sh.scan64);
+    if (cap > 0) excl1 = team_block_scan64((nvs1 << 24) | cnt1, &total1, sh.scan64);
+    const int c0 = static_cast<int>(total0 & 0xFFFFFFull), t0 = static_cast<int>(total0 >> 24);
+    const int c1 = static_cast<int>(total1 & 0xFFFFFFull), t1 = static_cast<int>(total1 >> 24);
+    const bool both = cap > 0 && c0 + c1 <= cap;  // (cap 0: one sphere)
+    int pos = static_cast<int>(excl0 & 0xFFFFFFull), voff = static_cast<int>(excl0 >> 24);
+    int pos1 = c0 + static_cast<int>(excl1 & 0xFFFFFFull), voff1 = t0 + static_cast<int>(excl1 >> 24);
+    for (int id = l0; id < l1; id++) {
+      const bool w0 = (okmask >> (id - l0)) & 1ull, w1 = both && ((okmask1 >> (id - l0)) & 1ull);
+      if (!w0 && !w1) continue;
+      const int nv = ct.lnv[id];
+      if (w0) {
+        s_cl[pos] = id;
+        s_coff[pos] = voff;
+        pos++;
+        voff += nv;
+      }
+      if (w1) {
+        s_cl[pos1] = id;
+        s_coff[pos1] = voff1;
+        pos1++;
+        voff1 += nv;
+      }
+    }
+    if (threadIdx.x == 0) {
+      const bool joint = both && joinable && !sh.pair_ovl;
+      sh.joint = joint ? 1 : 0;
+      sh.split = c0;
+      sh.cnt = joint ? c0 + c1 : c0;
+      sh.total = joint ? t0 + t1 : t0;
+      sh.held = (both && !joint) ? c1 : -1;
+      sh.held_total = t1;
+      sh.held_base = c0;
+      sh.held_off = t0;
+      s_coff[c0] = t0;
+      if (both) s_coff[c0 + c1] = t0 + t1;
+    }
+    __syncthreads();
+    return;
   }
   // (vertex count << 24) | leaf count: leaves < 2^24, vertices < 2^31
   unsigned long long total;
@@ -355,8 +444,25 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char*
                           int* s_cl, int* s_coff, const Tabs& ct, TeamShared& sh) {
   team_cull_by<kBox, kTwoLevel>(
       m, pp.original ? m.orig_vb : m.vb,
-      [&](float4 lo, float4 hi) { return box_hits(lo, hi, pp.loc, pp.cull_radius_sq); }, s_pass,
-      s_cl, s_coff, ct, sh);
+      [&](float4 lo, float4 hi) { return box_hits(lo, hi, pp.loc, pp.cull_radius_sq) ? 1u : 0u; },
+      s_pass, s_cl, s_coff, ct, sh);
+}
+
+// The node searches of both passes of a single-axis symmetry in one (the
+// spheres at loc0 and loc1, the same radius and boxes); cap bounds the
+// entries of the two lists together.
+template <int kBox, bool kTwoLevel, class Tabs>
+__device__ void team_cull_pair(const DevMesh& m, const PassParams& pp, const float* loc1, bool pair,
+                               unsigned char* s_pass, int* s_cl, int* s_coff, const Tabs& ct,
+                               TeamShared& sh, int cap, bool joinable) {
+  team_cull_by<kBox, kTwoLevel, true>(
+      m, pp.original ? m.orig_vb : m.vb,
+      [&](float4 lo, float4 hi) {
+        unsigned h = box_hits(lo, hi, pp.loc, pp.cull_radius_sq) ? 1u : 0u;
+        if (pair && box_hits(lo, hi, loc1, pp.cull_radius_sq)) h |= 2u;
+        return h;
+      },
+      s_pass, s_cl, s_coff, ct, sh, pair ? cap : 0, joinable);
 }
 
 // The gather of one grab / elastic deform dab (k_cull_dab): orig_vb boxes that
@@ -370,9 +476,45 @@ __device__ __forceinline__ void team_cull_union(const DevMesh& m, const DabPasse
       [&](float4 lo, float4 hi) {
         bool ok = all != 0;
         for (int p = 0; p < dp.npass && !ok; p++) ok = box_hits(lo, hi, dp.loc[p], rsq);
-        return ok;
+        return ok ? 1u : 0u;
       },
       s_pass, s_cl, s_coff, ct, sh);
+}
+
+// The second pass's list of a pair search, stored behind the first one's
+// (sh.held entries from sh.held_base, offsets from sh.held_off), moved to
+// the front of the list arrays with offsets from 0; sets sh.cnt, sh.total
+// and sh.split to its own.  Rounds of kTeamThreads entries read before they
+// write; later rounds read at or above base + their start.
+__device__ __forceinline__ void team_list_to_front(int* s_cl, int* s_coff, TeamShared& sh) {
+  const int base = sh.held_base, n = sh.held, off = sh.held_off;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sh.cnt = sh.split = n;
+    sh.total = sh.held_total;
+    sh.held = -1;
+  }
+  for (int k0 = 0; k0 <= n; k0 += kTeamThreads) {
+    const int k = k0 + static_cast<int>(threadIdx.x);
+    int leaf = 0, o = 0;
+    if (k <= n) {
+      if (k < n) leaf = s_cl[base + k];
+      o = s_coff[base + k] - off;
+    }
+    __syncthreads();
+    if (k <= n) {
+      if (k < n) s_cl[k] = leaf;
+      s_coff[k] = o;
+    }
+    __syncthreads();
+  }
+}
+
+// Tools whose sweep reads and writes only the vertex itself (and the pass's
+// frame): two passes over disjoint leaves commute and can run as one.
+__device__ __forceinline__ bool pair_tool(int tool) {
+  return tool == kToolDraw || tool == kToolInflate || tool == kToolPinch || tool == kToolCrease ||
+         tool == kToolClayStrips;
 }
 
 constexpr int kFlushTab = 128;  // ancestors whose boxes stay on chip
@@ -637,7 +779,7 @@ static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int
 // round in order, so the sums are those of the one-round form.
 constexpr int kAreaStage = 512;  // staged vertices per round and buffer: 16 KB
 static_assert(4 * kAreaStage * sizeof(float4) <= kStageBytes, "the area stage");
-static __device__ void team_area_block(const DevMesh& m, const PassParams& pp, float rn2,
+static __device__ void team_area_block(const DevMesh& m, const float* c, float rn2,
                                        float ra2, int leaf, int blk, float4* s_stage, Lane* sl,
                                        AreaPart* out) {
   const int t = threadIdx.x;
@@ -674,7 +816,7 @@ static __device__ void team_area_block(const DevMesh& m, const PassParams& pp, f
     const int r1 = min(i1, r0 + kAreaStage);
     for (int i = r0 + t; i < r1; i += kTeamThreads) {
       const float4 co = s_co[i - r0];
-      const float d2 = dist_sq(co, pp.loc);
+      const float d2 = dist_sq(co, c);
       if (d2 <= rn2) {
         const float4 no = s_no[i - r0];
         cs_add(l.v[0], no.x);
@@ -717,7 +859,7 @@ static __device__ void team_area_block(const DevMesh& m, const PassParams& pp, f
 constexpr int kTeamMaxChunks = 64;  // area partials per pass <= 64 * 256
 
 static __device__ void team_area_final(const DevMesh& m, const PassParams& pp, int cnt, Lane* sl,
-                                Lane* chunks, TeamShared& sh) {
+                                Lane* chunks, TeamShared& sh, int first = 0) {
   // Partials are staged in shared memory in chunks of kTeamThreads (a power of
   // two, so each chunk is a complete subtree of the pairwise tree); the chunk
   // totals then merge with the same pairwise rule, which completes the tree.
@@ -725,7 +867,7 @@ static __device__ void team_area_final(const DevMesh& m, const PassParams& pp, i
   for (int c = 0; c < nchunks; c++) {
     const int c0 = c * kTeamThreads;
     const int n = min(kTeamThreads, cnt - c0);
-    if (threadIdx.x < n) sl[threadIdx.x] = part_load(&m.parts[c0 + threadIdx.x]);
+    if (threadIdx.x < n) sl[threadIdx.x] = part_load(&m.parts[first + c0 + threadIdx.x]);
     __syncthreads();
     for (int s = 1; s < n; s <<= 1) {
       const int i = threadIdx.x * 2 * s;
@@ -1090,7 +1232,7 @@ struct PhaseClock {
 // other build carries none of their code).
 // kWide: the whole-GPU team (cooperative launch, one CTA per SM), which runs
 // the jobs one after another.
-template <int kMinBlocks, bool kOrig, bool kWide, bool kTwoLevel = false>
+template <int kMinBlocks, bool kOrig, bool kWide, bool kTwoLevel = false, bool kSym = false>
 __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamArgs a) {
   unsigned C, rank;
   if constexpr (kWide) {
@@ -1261,8 +1403,19 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         TEAM_SYNC();
         clk.mark(a, rank, kPhBrush);
       }
+      // kSym builds, single-axis symmetry: one node search gives both passes'
+      // lists (boxes change only at the end of the dab, so the second pass's
+      // list is the one a search after the first pass would give).  When the
+      // lists share no leaf and the tool reads and writes only the vertex
+      // itself, the two passes commute and run as one (joint): one area phase
+      // with a pairwise tree per pass, one sweep with each vertex under its
+      // own pass's frame.  The pair's state stays in shared memory (sh.split,
+      // sh.joint, sh.held).
       for (int pass = 0; pass < 8 && !(kOrig && uses_original(tool)); pass++) {
         if ((pass & ~sh.job.symmetry) != 0) continue;
+        if constexpr (kSym) {
+          if (pass != 0 && sh.joint) break;  // the second pass ran with the first
+        }
         PassParams pp;
         for (int k = 0; k < 3; k++) {
           const float sgn = (pass & (1 << k)) ? -1.0f : 1.0f;
@@ -1274,10 +1427,41 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         pp.original = sh.job.use_orig || (kOrig && tool == kToolLayer);  // layer: stroke-start boxes
         pp.iter_strength = 1.0f;
         pp.iteration = 0;
-        team_cull<kMinBlocks == 1 ? 8 : 2, kTwoLevel>(m, pp, s_pass, s_cl, s_coff, ct, sh);
+        if constexpr (!kSym) {
+          team_cull<kMinBlocks == 1 ? 8 : 2, kTwoLevel>(m, pp, s_pass, s_cl, s_coff, ct, sh);
+          // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
+          team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * sh.cnt : 0ull);
+        } else {
+          const int sym = sh.job.symmetry;
+          const bool pair = pass == 0 && (sym == 1 || sym == 2 || sym == 4);
+          if (pass != 0 && sh.held >= 0) {
+            if (threadIdx.x == 0) sh.mpp[0] = pp;
+            team_list_to_front(s_cl, s_coff, sh);
+          } else {
+            // (sh.mpp is read after the search's barriers)
+            float loc1[3];
+            for (int k = 0; k < 3; k++) loc1[k] = ((sym >> k) & 1) ? -pp.loc[k] : pp.loc[k];
+            if (threadIdx.x == 0) {
+              sh.mpp[0] = pp;
+              PassParams p1 = pp;
+              for (int k = 0; k < 3; k++) {
+                p1.loc[k] = loc1[k];
+                if ((sym >> k) & 1) {
+                  p1.delta[k] = -pp.delta[k];
+                  p1.view[k] = -pp.view[k];
+                }
+              }
+              sh.mpp[1] = p1;
+            }
+            team_cull_pair<kMinBlocks == 1 ? 8 : 2, kTwoLevel>(m, pp, loc1, pair, s_pass, s_cl, s_coff, ct,
+                                                               sh, a.max_leaves + 1, pair_tool(tool));
+            // node boxes tested once for the pass or pair, 8 B per leaf emitted
+            team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0)
+                                       ? 24ull * m.totnode + 8ull * (sh.held >= 0 ? sh.cnt + sh.held : sh.cnt)
+                                       : 0ull);
+          }
+        }
         const int cnt = sh.cnt, total = sh.total;
-        // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
-        team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
         clk.mark(a, rank, kPhCull);
         float area_no[3] = {0.0f, 0.0f, 0.0f}, area_co[3] = {0.0f, 0.0f, 0.0f};
         if (uses_area(tool)) {
@@ -1287,7 +1471,14 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           const int nb = m.area_blocks;
           for (int k = rank; k < cnt * nb; k += C) {
             const int leaf = s_cl[k / nb], blk = k % nb;
-            team_area_block(m, pp, rn * rn, ra * ra, leaf, blk, s_nbc, s_lanes, &m.parts[k]);
+            if constexpr (!kSym) {
+              team_area_block(m, pp.loc, rn * rn, ra * ra, leaf, blk, s_nbc, s_lanes, &m.parts[k]);
+            } else {
+              const bool second = k / nb >= sh.split;
+              float c[3];
+              for (int q = 0; q < 3; q++) c[q] = second ? sh.mpp[1].loc[q] : pp.loc[q];
+              team_area_block(m, c, rn * rn, ra * ra, leaf, blk, s_nbc, s_lanes, &m.parts[k]);
+            }
             const int nv = min(leaf_nverts(m, leaf) - blk * kAreaBlock, kAreaBlock);
             if (static_cast<int>(threadIdx.x) < nv)
               ab += ((m.type == kFaces ? 4ull : 0ull) + 24ull) *
@@ -1295,45 +1486,99 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           }
           team_bytes(a, kPhArea, ab);
           TEAM_SYNC();
-          team_area_final(m, pp, cnt * nb, s_lanes, s_chunks, sh);
+          if (kSym && sh.joint) {
+            // the second pass's tree over its own partials, and its frame
+            team_area_final(m, sh.mpp[1], (cnt - sh.split) * nb, s_lanes, s_chunks, sh, sh.split * nb);
+            BrushFrame f1;
+            const bool ok1 = make_frame(b, sh.mpp[1], sh.area, sh.area + 3, f1);
+            __syncthreads();  // sh.area read
+            if (threadIdx.x == 0) {
+              sh.live1 = ok1 ? 1 : 0;
+              if (ok1) sh.mframe[1] = f1;
+            }
+          }
+          team_area_final(m, pp, (kSym ? sh.split : cnt) * nb, s_lanes, s_chunks, sh);
           for (int k = 0; k < 3; k++) {
             area_no[k] = sh.area[k];
             area_co[k] = sh.area[3 + k];
           }
           clk.mark(a, rank, kPhArea);
+        } else if (kSym && sh.joint && threadIdx.x == 0) {
+          BrushFrame f1;
+          sh.live1 = make_frame(b, sh.mpp[1], area_no, area_co, f1) ? 1 : 0;
+          sh.mframe[1] = f1;
         }
         BrushFrame f;
-        if (!make_frame(b, pp, area_no, area_co, f)) continue;
+        int lo = 0, hi = cnt;  // the leaves of the passes with a frame
+        bool joint = false;
+        if constexpr (!kSym) {
+          if (!make_frame(b, pp, area_no, area_co, f)) continue;
+        } else {
+          const bool ok0 = make_frame(b, pp, area_no, area_co, f);
+          joint = sh.joint != 0;
+          if (joint) __syncthreads();  // sh.live1
+          // (a pass without a frame marks nothing)
+          const bool ok1 = joint && sh.live1;
+          if (!ok0 && !ok1) continue;
+          if (joint && threadIdx.x == 0) sh.mframe[0] = f;
+          lo = ok0 ? 0 : sh.split;
+          hi = (!joint || ok1) ? cnt : sh.split;
+        }
         if (rank == 0)
-          for (int k = threadIdx.x; k < cnt; k += kTeamThreads) {
+          for (int k = lo + static_cast<int>(threadIdx.x); k < hi; k += kTeamThreads) {
             const int leaf = s_cl[k];
             const int old = atomicOr(&m.leaf_flag[leaf], kMarkUpdate);
             if (!(old & kUpdateNormals)) append(m.touch_list, touch_cnt, leaf);
           }
-        if (m.type == kGrids) team_claim_faces(m, s_cl, cnt, rank, C, epoch);
+        if (m.type == kGrids) team_claim_faces(m, s_cl + lo, hi - lo, rank, C, epoch);
         if (tool != kToolSmooth) {
           unsigned long long ab = 0;
           const unsigned vbytes = (m.type == kFaces ? 4u : 0u) + 12u + (m.mask ? 4u : 0u) +
                                   (m.automask ? 4u : 0u) +
                                   ((tool == kToolInflate || (b.flag & kBrushFrontFace)) ? 12u : 0u);
-          for (int base = gt - lane; base < total; base += GT) {
-            const int i = base + lane;
-            bool moved = false;
-            if (i < total) {
-              const int k = smem_find_slot(s_coff, cnt, i);
-              const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
-              float4 co = __ldcg(&m.co[v]);
-              ab += vbytes;
-              const bool hit = (kOrig && tool == kToolLayer) ? layer_vertex(m, b, b.y, pp, v, co, moved)
-                                                  : brush_vertex(m, b, b.y, pp, f, v, co, moved);
-              if (hit) {
-                m.co[v] = co;
-                ab += 12u;
-                if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+          if (!joint) {
+            for (int base = gt - lane; base < total; base += GT) {
+              const int i = base + lane;
+              bool moved = false;
+              if (i < total) {
+                const int k = smem_find_slot(s_coff, cnt, i);
+                const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+                float4 co = __ldcg(&m.co[v]);
+                ab += vbytes;
+                const bool hit = (kOrig && tool == kToolLayer) ? layer_vertex(m, b, b.y, pp, v, co, moved)
+                                                    : brush_vertex(m, b, b.y, pp, f, v, co, moved);
+                if (hit) {
+                  m.co[v] = co;
+                  ab += 12u;
+                  if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+                }
               }
+              const unsigned bal = __ballot_sync(0xffffffffu, moved);
+              if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, moved);
-            if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
+          } else if constexpr (kSym) {
+            // the joint pair: each vertex under its own pass's parameters and
+            // frame (in shared memory), the passes' vertices [vlo, vhi)
+            const int vlo = s_coff[lo], vhi = s_coff[hi], split = sh.split;
+            __syncthreads();  // the frames in shared memory
+            for (int base = vlo + gt - lane; base < vhi; base += GT) {
+              const int i = base + lane;
+              bool moved = false;
+              if (i < vhi) {
+                const int k = smem_find_slot(s_coff, cnt, i);
+                const int v = leaf_vert(m, s_cl[k], i - s_coff[k]);
+                float4 co = __ldcg(&m.co[v]);
+                ab += vbytes;
+                const int pk = k >= split ? 1 : 0;
+                if (brush_vertex(m, b, b.y, sh.mpp[pk], sh.mframe[pk], v, co, moved)) {
+                  m.co[v] = co;
+                  ab += 12u;
+                  if (m.type == kFaces) tag_vertex(m, v, tag_cnt);
+                }
+              }
+              const unsigned bal = __ballot_sync(0xffffffffu, moved);
+              if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&w->displaced, (unsigned long long)__popc(bal));
+            }
           }
           team_bytes(a, kPhBrush, ab);
           TEAM_SYNC();
