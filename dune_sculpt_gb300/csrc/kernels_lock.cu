@@ -219,10 +219,10 @@ __device__ void lock_flush(const DevMesh& m, int par, int* s_par, unsigned char*
   const int ntouch = __ldcg(&m.work->touch_count[par]);
   FlushState fst;
   unsigned long long fb = 0;
-  team_flush_mark(m, ntouch, m.touch_list, s_par, reinterpret_cast<unsigned int*>(s_pass), s_list,
+  team_flush_mark(m, ntouch, m.touch_list, m.leaf_node, s_par, reinterpret_cast<unsigned int*>(s_pass), s_list,
                   s_idx, fs, sh, fst);
   __syncthreads();
-  team_flush_levels(m, ntouch, m.touch_list, s_par, s_list, s_idx, fs, sh, fst, fb);
+  team_flush_levels(m, ntouch, m.touch_list, m.leaf_node, s_par, s_list, s_idx, fs, sh, fst, fb);
 }
 
 // Refit of chunks c0 .. c0+n-1 (n <= kRuns) of a leaf by one warp: every

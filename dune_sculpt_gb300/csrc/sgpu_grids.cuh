@@ -102,9 +102,42 @@ __device__ __forceinline__ void grid_avg_pair(const DevMesh& m, int a, int b) {
 
 // Averages co, no and mask over els[0..n) (in order) and stores the mean in
 // every one of them (GridElementAccumulator, subdiv_ccg.c:903-949).
+// Up to kAvgBatch copies (base edges: 2, quad-mesh corners: 4): every
+// element index loaded first, then the copies' values (summed in copy
+// order); the mean's positions are written as three scalars, so a copy's
+// fourth component stays as it is without being read again.
+constexpr int kAvgBatch = 4;
 template <class ElemAt>
 __device__ __forceinline__ void grid_average_set(const DevMesh& m, int n, ElemAt el) {
   float cx = 0.0f, cy = 0.0f, cz = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f, mk = 0.0f;
+  if (n <= kAvgBatch) {
+    int e[kAvgBatch];
+#pragma unroll
+    for (int f = 0; f < kAvgBatch; f++) e[f] = f < n ? el(f) : 0;
+#pragma unroll
+    for (int f = 0; f < kAvgBatch; f++)
+      if (f < n) {
+        const float4 co = __ldcg(&m.co[e[f]]), no = __ldcg(&m.no[e[f]]);
+        cx += co.x, cy += co.y, cz += co.z;
+        nx += no.x, ny += no.y, nz += no.z;
+        if (m.mask) mk += __ldcg(&m.mask[e[f]]);
+      }
+    const float inv = 1.0f / (float)n;
+    cx *= inv, cy *= inv, cz *= inv;
+    nx *= inv, ny *= inv, nz *= inv;
+    mk *= inv;
+#pragma unroll
+    for (int f = 0; f < kAvgBatch; f++)
+      if (f < n) {
+        float* c = reinterpret_cast<float*>(&m.co[e[f]]);
+        c[0] = cx;
+        c[1] = cy;
+        c[2] = cz;
+        m.no[e[f]] = make_float4(nx, ny, nz, 0.0f);
+        if (m.mask) m.mask[e[f]] = mk;
+      }
+    return;
+  }
   for (int f = 0; f < n; f++) {
     const int e = el(f);
     const float4 co = __ldcg(&m.co[e]), no = __ldcg(&m.no[e]);

@@ -550,14 +550,16 @@ __device__ __forceinline__ bool bit_set(const unsigned int* bits, int i) {
 // marks the touched leaf nodes) and s_idx[node] = its list position; with at
 // most kFlushTab ancestors, each thread takes one and loads the boxes of its
 // children that the update leaves unchanged.  touched: the touched leaves.
-static __device__ void team_flush_mark(const DevMesh& m, int ntouch, const int* touched, const int* s_par,
+template <class LeafNode>
+static __device__ void team_flush_mark(const DevMesh& m, int ntouch, const int* touched, const LeafNode* lnode,
+                                const int* s_par,
                                 unsigned int* bits, int* s_list, unsigned short* s_idx,
                                 FlushSmem& fs, TeamShared& sh, FlushState& f) {
   for (int i = threadIdx.x; i < (m.totnode + 31) / 32; i += kTeamThreads) bits[i] = 0u;
   if (threadIdx.x == 0) sh.nmark = 0;
   __syncthreads();
   for (int k = threadIdx.x; k < ntouch; k += kTeamThreads) {
-    const int leaf_node = m.leaf_node[touched[k]];
+    const int leaf_node = static_cast<int>(lnode[touched[k]]);
     atomicOr(&bits[leaf_node >> 5], 1u << (leaf_node & 31));
     int p = s_par[leaf_node];
     while (p >= 0) {
@@ -573,7 +575,7 @@ static __device__ void team_flush_mark(const DevMesh& m, int ntouch, const int* 
   __syncthreads();
   for (int k = threadIdx.x; k < min(ntouch, kFlushTouch); k += kTeamThreads) {
     const int leaf = touched[k];
-    const int node = m.leaf_node[leaf];
+    const int node = static_cast<int>(lnode[leaf]);
     const int p = s_par[node];
     const int pos = p >= 0 ? s_idx[p] : kNoPos;
     fs.kslot[k] = pos < kFlushTab ? 2 * pos + (node - m.node_child[p]) : -1;
@@ -616,7 +618,8 @@ __device__ __forceinline__ void box_union(const float4& a0, const float4& a1, co
 // fs.kid), then each listed ancestor becomes the union of its two children
 // (update_node_vb, pbvh.c:2026-2046), deepest level first as pbvh_flush_bb
 // (pbvh.c:3287-3317) orders it.  Resets s_idx to kNoPos.
-static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int* touched,
+template <class LeafNode>
+static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int* touched, const LeafNode* lnode,
                                   const int* s_par, const int* s_list, unsigned short* s_idx,
                                   FlushSmem& fs, TeamShared& sh, FlushState& f,
                                   unsigned long long& ab) {
@@ -631,7 +634,7 @@ static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int
     } else {
       const int leaf = touched[k];
       co = make_int2(m.leaf_chunk_off[leaf], m.leaf_chunk_off[leaf + 1]);
-      const int node = m.leaf_node[leaf];
+      const int node = static_cast<int>(lnode[leaf]);
       const int p = s_par[node];
       const int pos = p >= 0 ? s_idx[p] : kNoPos;
       slot = pos < kFlushTab ? 2 * pos + (node - m.node_child[p]) : -1;
@@ -656,7 +659,7 @@ static __device__ void team_flush_levels(const DevMesh& m, int ntouch, const int
     if (lane == 0) {
       const float4 bmn = make_float4(mn[0], mn[1], mn[2], 0.0f);
       const float4 bmx = make_float4(mx[0], mx[1], mx[2], 0.0f);
-      const int node = m.leaf_node[touched[k]];
+      const int node = static_cast<int>(lnode[touched[k]]);
       m.vb[2 * node] = bmn;
       m.vb[2 * node + 1] = bmx;
       if (slot >= 0) {
@@ -1816,7 +1819,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           }
         }
         if (rank == 0)
-          team_flush_mark(m, ntouch, s_cl, s_par, reinterpret_cast<unsigned int*>(s_pass), s_coff, s_idx,
+          team_flush_mark(m, ntouch, s_cl, s_lnode, s_par, reinterpret_cast<unsigned int*>(s_pass), s_coff, s_idx,
                           s_scr.flush, sh, fst);
       }
       team_bytes(a, kPhUpdate, ab);
@@ -1824,7 +1827,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       clk.mark(a, rank, kPhUpdate);
       // flush by CTA 0: the listed ancestors bottom-up
       unsigned long long fb = 0;
-      if (rank == 0) team_flush_levels(m, ntouch, s_cl, s_par, s_coff, s_idx, s_scr.flush, sh, fst, fb);
+      if (rank == 0) team_flush_levels(m, ntouch, s_cl, s_lnode, s_par, s_coff, s_idx, s_scr.flush, sh, fst, fb);
       team_bytes(a, kPhFlush, fb);
       if (m.type == kFaces && (rank != 0 || C == 1)) {
         // normals over CTAs 1..C-1 (all of the team when it is one CTA)
