@@ -158,6 +158,13 @@ __device__ __forceinline__ void grid_average_set(const DevMesh& m, int n, ElemAt
   }
 }
 
+// 1 / counter for the 1, 2 or 4 quads around a grid element (3 cannot occur
+// in a grid; kept for completeness): the correctly rounded quotients of the
+// division the element normal is defined with, without the division.
+__device__ __forceinline__ float inv_count(int counter) {
+  return counter == 4 ? 0.25f : counter == 2 ? 0.5f : counter == 1 ? 1.0f : 1.0f / 3.0f;
+}
+
 // Normal of element (x, y) of the grid starting at element base: the mean of
 // the normals of the quads around it, added in the order of
 // subdiv_ccg.c:707-737.  Quad (qx, qy) has corners (qx, qy+1), (qx+1, qy+1),
@@ -203,7 +210,7 @@ __device__ __forceinline__ float4 grid_element_normal(const DevMesh& m, int base
     ax += q.x, ay += q.y, az += q.z;
     counter++;
   }
-  const float inv = 1.0f / (float)counter;
+  const float inv = inv_count(counter);
   return make_float4(ax * inv, ay * inv, az * inv, 0.0f);
 }
 

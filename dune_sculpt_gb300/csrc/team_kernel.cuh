@@ -966,8 +966,7 @@ __device__ __forceinline__ float3 staged_normal(const float3* s_q, int i, int gs
     if (y >= 1) add(q[(y - 1) * g1 + x - 1]);
   }
   if (y >= 1 && x < g1) add(q[(y - 1) * g1 + x]);
-  const float inv = 1.0f / (float)counter;
-  return make_float3(ax * inv, ay * inv, az * inv);
+  return make_float3(ax * inv_count(counter), ay * inv_count(counter), az * inv_count(counter));
 }
 
 // The owner records of face f's corners for the dab of this epoch (threads
