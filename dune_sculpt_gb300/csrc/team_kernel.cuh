@@ -951,8 +951,8 @@ __host__ __device__ __forceinline__ int face_grid_group(int grid_size, size_t by
 // Normal of staged element i (grid i / area of the stage): the mean of the
 // staged normals of the quads around it, added in the order of
 // grid_element_normal (subdiv_ccg.c:707-737).
-__device__ __forceinline__ float3 staged_normal(const float3* s_q, int i, int gs, int area) {
-  const int g1 = gs - 1, c = i / area, e = i - c * area, y = e / gs, x = e - y * gs;
+// Element (x, y) of staged grid c.
+__device__ __forceinline__ float3 staged_normal_at(const float3* s_q, int c, int x, int y, int g1) {
   const float3* q = s_q + c * g1 * g1;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   int counter = 0;
@@ -1022,26 +1022,34 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
     if (c0 == 0) grid_corner_owners(m, f, s, n, epoch, threadIdx.x, kTeamThreads);
     cp_async_wait_all();
     __syncthreads();
-    for (int i = threadIdx.x; i < nc * qa; i += kTeamThreads) {
-      const int c = i / qa, q = i - c * qa, qy = q / g1, qx = q - qy * g1;
-      const float4* p = s_co + c * area;
-      // quad (qx, qy): corners (qx, qy+1), (qx+1, qy+1), (qx+1, qy), (qx, qy)
-      s_q[i] = normal_quad(xyz(p[(qy + 1) * gs + qx]), xyz(p[(qy + 1) * gs + qx + 1]),
-                           xyz(p[qy * gs + qx + 1]), xyz(p[qy * gs + qx]));
+    // each thread keeps one quad (element) position and walks the grids
+    for (int q = threadIdx.x; q < qa; q += kTeamThreads) {
+      const int qy = q / g1, qx = q - qy * g1;
+      for (int c = 0; c < nc; c++) {
+        const float4* p = s_co + c * area;
+        // quad (qx, qy): corners (qx, qy+1), (qx+1, qy+1), (qx+1, qy), (qx, qy)
+        s_q[c * qa + q] = normal_quad(xyz(p[(qy + 1) * gs + qx]), xyz(p[(qy + 1) * gs + qx + 1]),
+                                      xyz(p[qy * gs + qx + 1]), xyz(p[qy * gs + qx]));
+      }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
-      const float3 nv = staged_normal(s_q, i, gs, area);
-      m.no[static_cast<size_t>(s + c0) * area + i] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    for (int e = threadIdx.x; e < area; e += kTeamThreads) {
+      const int y = e / gs, x = e - y * gs;
+      for (int c = 0; c < nc; c++) {
+        const float3 nv = staged_normal_at(s_q, c, x, y, g1);
+        m.no[static_cast<size_t>(s + c0 + c) * area + e] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+      }
     }
     __syncthreads();  // a next group restages after this barrier
   }
   const int pairs = n * g1;
   if (whole) {
     // pairs and the centre from the stage
-    auto avg_pair = [&](int ia, int ib) {
+    // element (i, 0) of grid ca and element (0, i) of grid cb
+    auto avg_pair = [&](int ga_, int gb_, int i) {
+      const int ia = ga_ * area + i, ib = gb_ * area + i * gs;
       const float4 ca = s_co[ia], cb = s_co[ib];
-      const float3 na = staged_normal(s_q, ia, gs, area), nb = staged_normal(s_q, ib, gs, area);
+      const float3 na = staged_normal_at(s_q, ga_, i, 0, g1), nb = staged_normal_at(s_q, gb_, 0, i, g1);
       float4 c;
       c.x = (ca.x + cb.x) * 0.5f;
       c.y = (ca.y + cb.y) * 0.5f;
@@ -1063,14 +1071,14 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
     for (int it = threadIdx.x; it <= pairs; it += kTeamThreads) {
       if (it < pairs) {
         const int c = it / g1, i = 1 + (it - c * g1);
-        const int prev = (c + n - 1) % n;
-        avg_pair(prev * area + i, c * area + i * gs);
+        const int prev = c == 0 ? n - 1 : c - 1;
+        avg_pair(prev, c, i);
       } else {
         // GridElementAccumulator over element 0 of every grid, in grid order
         float cx = 0.0f, cy = 0.0f, cz = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f, mk = 0.0f;
         for (int c = 0; c < n; c++) {
           const float4 co = s_co[c * area];
-          const float3 no = staged_normal(s_q, c * area, gs, area);
+          const float3 no = staged_normal_at(s_q, c, 0, 0, g1);
           cx += co.x, cy += co.y, cz += co.z;
           nx += no.x, ny += no.y, nz += no.z;
           if (m.mask) mk += s_mk[c * area];
