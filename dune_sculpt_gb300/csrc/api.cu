@@ -1143,6 +1143,8 @@ int sgpu_mesh_create_grids(int num_grids, int grid_size, const float* grids_co,
   d.totvert = static_cast<int>(elems);
   d.grid_size = grid_size;
   d.grid_area = h.grid_area;
+  div_invariant_params(static_cast<unsigned int>(h.grid_area), &d.area_mul, &d.area_shift);
+  div_invariant_params(static_cast<unsigned int>(grid_size), &d.size_mul, &d.size_shift);
   d.num_faces = num_faces;
   d.num_base_verts = num_base_verts;
   d.num_base_edges = num_base_edges;

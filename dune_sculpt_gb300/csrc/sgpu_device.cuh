@@ -44,6 +44,21 @@ struct AreaPart {
   int n_no, n_co;
 };
 
+// Division by a divisor fixed per mesh (Granlund and Montgomery, "Division
+// by invariant integers using multiplication", PLDI 1994): with
+// s = 31 + ceil(log2 d) and mul = ceil(2^s / d) (below 2^32), n * mul >> s
+// equals n / d for every 0 <= n < 2^31, since mul * d - 2^s < d <= 2^(s - 31)
+// keeps the error term below 1 / d.
+__host__ __device__ __forceinline__ unsigned int div_invariant(unsigned int n, unsigned int mul, int shift) {
+  return static_cast<unsigned int>((static_cast<unsigned long long>(n) * mul) >> shift);
+}
+inline void div_invariant_params(unsigned int d, unsigned int* mul, int* shift) {
+  int l = 0;
+  while ((1ull << l) < d) l++;
+  *shift = 31 + l;
+  *mul = static_cast<unsigned int>(((1ull << *shift) + d - 1) / d);
+}
+
 // Device view of one mesh; passed to kernels by value.
 struct DevMesh {
   int type;
@@ -52,6 +67,9 @@ struct DevMesh {
   int nleaf;
   int totlt;
   int grid_size, grid_area;
+  // n / grid_area and n / grid_size as multiply and shift (div_invariant)
+  unsigned int area_mul, size_mul;
+  int area_shift, size_shift;
   int nlevels;
   float4* co;  // FACES: the MVert bytes (xyz + flag/bweight/pad in w); GRIDS: xyz, 0
   float4* no;
@@ -387,8 +405,9 @@ __device__ __forceinline__ int leaf_nverts(const DevMesh& m, int leaf) {
 __device__ __forceinline__ int leaf_vert(const DevMesh& m, int leaf, int i) {
   // FACES: the unique vertices of a leaf are one range in device order
   if (m.type == kFaces) return m.leaf_ubase[leaf] + i;
-  const int g = m.leaf_prims[m.leaf_prim_off[leaf] + i / m.grid_area];
-  return g * m.grid_area + i % m.grid_area;
+  const int q = static_cast<int>(div_invariant(static_cast<unsigned int>(i), m.area_mul, m.area_shift));
+  const int g = m.leaf_prims[m.leaf_prim_off[leaf] + q];
+  return g * m.grid_area + (i - q * m.grid_area);
 }
 // All vertices of a leaf (PBVH_ITER_ALL) for the bounding-box refit.
 __device__ __forceinline__ int leaf_nverts_all(const DevMesh& m, int leaf) {
@@ -655,7 +674,10 @@ __device__ __forceinline__ float3 ring_average(const DevMesh& m, int v, float4 c
     }
   } else {
     const int gs = m.grid_size, area = m.grid_area;
-    const int g = v / area, r = v % area, x = r % gs, y = r / gs;
+    const int g = static_cast<int>(div_invariant(static_cast<unsigned int>(v), m.area_mul, m.area_shift));
+    const int r = v - g * area;
+    const int y = static_cast<int>(div_invariant(static_cast<unsigned int>(r), m.size_mul, m.size_shift));
+    const int x = r - y * gs;
     const int nx[4] = {x - 1, x + 1, x, x};
     const int ny[4] = {y, y, y - 1, y + 1};
     float3 c[4];
@@ -726,7 +748,10 @@ __device__ __forceinline__ int ring_ids(const DevMesh& m, int v, int* id) {
     for (int j = 0; j < kNbCache; j++) id[j] = j < n ? m.nb_idx[q0 + j] : -1;
   } else {
     const int gs = m.grid_size, area = m.grid_area;
-    const int g = v / area, r = v % area, x = r % gs, y = r / gs;
+    const int g = static_cast<int>(div_invariant(static_cast<unsigned int>(v), m.area_mul, m.area_shift));
+    const int r = v - g * area;
+    const int y = static_cast<int>(div_invariant(static_cast<unsigned int>(r), m.size_mul, m.size_shift));
+    const int x = r - y * gs;
     const int nx[4] = {x - 1, x + 1, x, x};
     const int ny[4] = {y, y, y - 1, y + 1};
 #pragma unroll
