@@ -93,8 +93,12 @@ def parse_args():
                     help="team for --quick: cluster size, -1 for the whole GPU, 0 autotuned; "
                          "for --quick-batch: cluster size, -1, or -2 for the lockstep launch")
     ap.add_argument("--quick-dabs", type=int, default=0,
-                    help="--quick strokes only the first N dabs (a shorter launch for a full "
-                         "ncu capture); 0: every dab")
+                    help="--quick strokes only N dabs (a shorter launch for a full ncu "
+                         "capture); 0: every dab")
+    ap.add_argument("--quick-from", type=int, default=0,
+                    help="first dab of the --quick-dabs slice (the multires stroke's first 23 "
+                         "dabs fall on fully masked elements: they search, update and refit "
+                         "but move nothing)")
     ap.add_argument("--quick-batch", action="store_true",
                     help="three launches of the 64-mesh batch on --team (8 when 0), no report "
                          "(the command profiled with ncu for the batch kernels)")
@@ -879,8 +883,9 @@ def run_quick(args):
     if args.quick_dabs > 0:
         from dataclasses import replace
 
-        st = replace(st, dabs=st.dabs[:args.quick_dabs])
-        tools = None if tools is None else tools[:args.quick_dabs]
+        lo, hi = args.quick_from, args.quick_from + args.quick_dabs
+        st = replace(st, dabs=st.dabs[lo:hi])
+        tools = None if tools is None else tools[lo:hi]
     g = build_gpu(W)
     g.snapshot()
     if args.team:
