@@ -654,6 +654,18 @@ def run_gpu(args):
         s2 = host_stroke()
         e2e_ms += s2.gpu_ms
         e2e_v += s2.verts_displaced
+    d2h_note = "every position through the copy engine"
+    if W.kind == "grids":
+        # the page-locked output takes only the grids the stroke changed from
+        # the device (bitwise against the input); the rest arrives from the
+        # input, copied by host threads while the stroke runs
+        area = W.mesh.grid_size * W.mesh.grid_size
+        changed = np.any((cout.array.view(np.uint32) != cin.array.view(np.uint32)).reshape(-1, 3 * area),
+                         axis=1)
+        d2h = int(changed.sum()) * area * 12
+        d2h_note = (f"the {int(changed.sum())} of {changed.size} grids the stroke changed, written by the "
+                    "device into the page-locked output; the other grids copied from the input by host "
+                    "threads during the stroke (inside the timed call)")
 
     # phase profile of the persistent kernel (instrumented run, not timed)
     g.restore()
@@ -696,7 +708,7 @@ def run_gpu(args):
         "parallelism": f"replicas{world}",
         "mode": f"persistent stroke kernel, {team_label(team)} (autotuned)",
         "e2e": {"value": e2e_v / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h),
+                "d2h_bytes_per_step": int(d2h), "d2h": d2h_note,
                 "path": "sgpu_stroke_host_grids" if W.kind == "grids" else "sgpu_stroke_host"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_team_stroke", "achieved": achieved,

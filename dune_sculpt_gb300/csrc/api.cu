@@ -24,6 +24,7 @@
 #include <chrono>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <tuple>
 
 using namespace sgpu;
@@ -135,6 +136,8 @@ struct sgpu_mesh {
   DevBrush* t_lbrush = nullptr;  // and per-job brushes
   size_t t_dab_cap = 0, t_tool_cap = 0, t_mesh_cap = 0, t_job_cap = 0, t_counter_cap = 0;
   size_t t_lock_cap = 0, t_lbrush_cap = 0;
+  float* t_keep = nullptr;  // host-buffer GRIDS stroke: the positions input, kept
+  size_t t_keep_cap = 0;
   // page-locked displaced counters of the last persistent launch
   unsigned long long* h_disp = nullptr;
   size_t h_disp_cap = 0;
@@ -229,8 +232,10 @@ struct sgpu_mesh {
     for (void* p : {static_cast<void*>(t_meshes), static_cast<void*>(t_jobs),
                     static_cast<void*>(t_dabs), static_cast<void*>(t_tools),
                     static_cast<void*>(t_counter), static_cast<void*>(t_lock),
-                    static_cast<void*>(t_lbrush)})
+                    static_cast<void*>(t_lbrush), static_cast<void*>(t_keep)})
       if (p) cudaFree(p);
+    t_keep = nullptr;
+    t_keep_cap = 0;
     t_lock = nullptr;
     t_lbrush = nullptr;
     t_lock_cap = t_lbrush_cap = 0;
@@ -806,6 +811,48 @@ int do_brush_tool(sgpu_mesh* m, const SGPU_Brush* brush, int tool, const float l
   if (rc) return rc;
   return device_err(m);
 }
+
+template <class T>
+int ensure_dev(T** p, size_t* cap, size_t n);
+
+// The device address of a page-locked host buffer mapped into the device's
+// address space, else null (pageable or unknown memory).
+float* mapped_host_ptr(void* p) {
+  cudaPointerAttributes pa;
+  if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (pa.type != cudaMemoryTypeHost || !pa.devicePointer) return nullptr;
+  return static_cast<float*>(pa.devicePointer);
+}
+
+// A host copy split over a few threads, running while the device works;
+// joined before anything else writes the destination (and on every return).
+struct HostCopy {
+  std::vector<std::thread> threads;
+  void start(void* dst, const void* src, size_t bytes) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t k = std::max<size_t>(1, std::min<size_t>(8, hw > 1 ? hw / 2 : 1));
+    const size_t chunk = ((bytes + k - 1) / k + 4095) & ~static_cast<size_t>(4095);
+    char* d = static_cast<char*>(dst);
+    const char* s = static_cast<const char*>(src);
+    for (size_t off = 0; off < bytes; off += chunk) {
+      const size_t n = std::min(chunk, bytes - off);
+      try {
+        threads.emplace_back([=] { std::memcpy(d + off, s + off, n); });
+      } catch (...) {
+        std::memcpy(d + off, s + off, n);  // no thread to run it: copy here
+      }
+    }
+  }
+  void join() {
+    for (std::thread& t : threads)
+      if (t.joinable()) t.join();
+    threads.clear();
+  }
+  ~HostCopy() { join(); }
+};
 
 // The host-buffer stroke around the upload and download of one mesh type:
 // upload, refit of every leaf box, the stroke (mode as in sgpu_stroke),
@@ -1780,26 +1827,43 @@ int sgpu_stroke_host_grids(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_
   DevMesh& d = mesh->dev;
   int launches = 0;
   float* flat = reinterpret_cast<float*>(d.scratch);
+  const size_t bytes = 3 * sizeof(float) * static_cast<size_t>(d.totvert);
+  // A page-locked, mapped output takes the changed grids straight from the
+  // device; the host threads copy the input into it meanwhile (grids the
+  // stroke leaves bit-identical).  Any other output gets every position back
+  // through the copy engine.
+  float* d_out = mapped_host_ptr(grids_co_out);
+  HostCopy host_copy;
+  if (d_out && (rc = ensure_dev(&mesh->t_keep, &mesh->t_keep_cap, 3 * static_cast<size_t>(d.totvert))))
+    return rc;
+  float* pos_in = d_out ? mesh->t_keep : flat;
   auto upload = [&]() -> int {
-    CK(cudaMemcpyAsync(flat, grids_co_in, 3 * sizeof(float) * d.totvert, cudaMemcpyHostToDevice,
-                       mesh->stream),
+    CK(cudaMemcpyAsync(pos_in, grids_co_in, bytes, cudaMemcpyHostToDevice, mesh->stream),
        "upload grid positions");
-    CK(launch_xyz_to_f4(d.co, flat, nullptr, d.totvert, false, mesh->stream), "expand kernel");
+    CK(launch_xyz_to_f4(d.co, pos_in, nullptr, d.totvert, false, mesh->stream), "expand kernel");
     launches++;
     if (grids_no_in) {
-      CK(cudaMemcpyAsync(flat, grids_no_in, 3 * sizeof(float) * d.totvert,
-                         cudaMemcpyHostToDevice, mesh->stream),
+      CK(cudaMemcpyAsync(flat, grids_no_in, bytes, cudaMemcpyHostToDevice, mesh->stream),
          "upload grid normals");
       CK(launch_xyz_to_f4(d.no, flat, nullptr, d.totvert, false, mesh->stream), "expand kernel");
       launches++;
     }
+    // (after the first event and the queued copies: inside the timed call)
+    if (d_out && grids_co_out != grids_co_in) host_copy.start(grids_co_out, grids_co_in, bytes);
     return SGPU_OK;
   };
   auto download = [&]() -> int {
+    if (d_out) {
+      host_copy.join();  // before the device writes the output
+      CK(launch_grid_writeback(d_out, d.co, mesh->t_keep, d.totvert / d.grid_area, d.grid_area,
+                               mesh->stream),
+         "write-back kernel");
+      launches++;
+      return SGPU_OK;
+    }
     CK(launch_f4_to_xyz(flat, d.co, nullptr, d.totvert, mesh->stream), "pack kernel");
     launches++;
-    CK(cudaMemcpyAsync(grids_co_out, flat, 3 * sizeof(float) * d.totvert, cudaMemcpyDeviceToHost,
-                       mesh->stream),
+    CK(cudaMemcpyAsync(grids_co_out, flat, bytes, cudaMemcpyDeviceToHost, mesh->stream),
        "download grid positions");
     return SGPU_OK;
   };

@@ -785,6 +785,33 @@ __global__ void k_f4_to_xyz(float* out3, const float4* in, const int* idx, int n
   }
 }
 
+// The positions of a GRIDS stroke back into the caller's page-locked output
+// (out3, 3 floats per element, mapped into the device's address space): a
+// grid whose positions equal the stroke's input (in3, the same layout) bit for
+// bit is not written (the host copied the input there); a changed grid is
+// written whole.  One CTA per grid at a time.
+__global__ void k_grid_writeback(float* out3, const float4* co, const float* in3, int ngrids, int area) {
+  for (int g = blockIdx.x; g < ngrids; g += gridDim.x) {
+    const size_t e0 = static_cast<size_t>(g) * area;
+    int diff = 0;
+    for (int i = threadIdx.x; i < area; i += blockDim.x) {
+      const float4 a = co[e0 + i];
+      const float* b = in3 + 3 * (e0 + i);
+      diff |= (__float_as_uint(a.x) != __float_as_uint(b[0])) | (__float_as_uint(a.y) != __float_as_uint(b[1])) |
+              (__float_as_uint(a.z) != __float_as_uint(b[2]));
+    }
+    if (__syncthreads_or(diff)) {
+      for (int i = threadIdx.x; i < area; i += blockDim.x) {
+        const float4 a = co[e0 + i];
+        float* o = out3 + 3 * (e0 + i);
+        o[0] = a.x;
+        o[1] = a.y;
+        o[2] = a.z;
+      }
+    }
+  }
+}
+
 static int gather_grid(int n) {
   const int g = (n + kThreads - 1) / kThreads;
   const int cap = 4 * work_grid();
@@ -806,6 +833,12 @@ cudaError_t launch_xyz_to_f4(float4* out, const float* in3, const int* idx, int 
 }
 cudaError_t launch_f4_to_xyz(float* out3, const float4* in, const int* idx, int n, cudaStream_t s) {
   k_f4_to_xyz<<<gather_grid(n), kThreads, 0, s>>>(out3, in, idx, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_grid_writeback(float* out3, const float4* co, const float* in3, int ngrids, int area,
+                                  cudaStream_t s) {
+  const int cap = 8 * work_grid();
+  k_grid_writeback<<<ngrids < cap ? (ngrids > 0 ? ngrids : 1) : cap, 128, 0, s>>>(out3, co, in3, ngrids, area);
   return cudaGetLastError();
 }
 

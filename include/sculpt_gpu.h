@@ -485,7 +485,12 @@ int sgpu_stroke_host(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *d
 
 /* The same for a GRIDS mesh: grids_co_in (and grids_no_in, nullable) hold 3
  * floats per grid element in the element order of sgpu_mesh_create_grids;
- * grids_co_out receives the positions after the stroke, same layout. */
+ * grids_co_out receives the positions after the stroke, same layout.  When
+ * grids_co_out is page-locked and mapped (sgpu_host_alloc), host threads copy
+ * grids_co_in into it while the stroke runs and the device then writes the
+ * grids whose positions changed (bitwise), instead of copying every position
+ * back; grids_co_out may then be grids_co_in itself, and must not otherwise
+ * overlap it. */
 int sgpu_stroke_host_grids(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs,
                            int ndabs, const int *dab_tools, const float *grids_co_in,
                            const float *grids_no_in, float *grids_co_out, int mode,
