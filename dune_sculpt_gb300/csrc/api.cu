@@ -335,6 +335,33 @@ int upload_pbvh(sgpu_mesh* m) {
       unext += h.uniq[node];
     }
   }
+  // FACES: leaves joined by a mesh edge (a one-ring neighbour owned by
+  // another leaf); the smooth brush's two mirror passes commute when no leaf
+  // of one is joined to a leaf of the other
+  std::vector<int> adj_off(L + 1, 0), adj;
+  if (h.type == kFaces && h.nb_off.size() > 1) {
+    const int V = static_cast<int>(h.nb_off.size()) - 1;
+    std::vector<int> vleaf(V, -1);
+    for (int k = 0; k < L; k++)
+      for (int i = 0; i < uniq[k]; i++) vleaf[ubase[k] + i] = k;
+    std::vector<std::vector<int>> sets(L);
+    for (int v = 0; v < V; v++) {
+      const int lv = vleaf[m->o2n[v]];
+      if (lv < 0) continue;
+      for (int q = h.nb_off[v]; q < h.nb_off[v + 1]; q++) {
+        const int lu = vleaf[m->o2n[h.nb_idx[q]]];
+        if (lu >= 0 && lu != lv) sets[lv].push_back(lu);
+      }
+    }
+    for (int k = 0; k < L; k++) {
+      std::sort(sets[k].begin(), sets[k].end());
+      sets[k].erase(std::unique(sets[k].begin(), sets[k].end()), sets[k].end());
+      adj_off[k + 1] = adj_off[k] + static_cast<int>(sets[k].size());
+      adj.insert(adj.end(), sets[k].begin(), sets[k].end());
+    }
+  }
+  if ((rc = m->upload(&d.leaf_adj_off, adj_off))) return rc;
+  if ((rc = m->upload(&d.leaf_adj, adj))) return rc;
   if ((rc = m->upload(&d.leaf_vert_off, vert_off))) return rc;
   if ((rc = m->upload(&d.leaf_uniq, uniq))) return rc;
   if ((rc = m->upload(&d.leaf_ubase, ubase))) return rc;

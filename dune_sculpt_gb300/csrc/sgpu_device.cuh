@@ -98,6 +98,9 @@ struct DevMesh {
   const int* leaf_vert_off;  // FACES: nleaf+1 offsets into leaf_verts
   const int* leaf_uniq;      // FACES: unique vertex count per leaf
   const int* leaf_ubase;     // FACES: device index of the leaf's first unique vertex
+  // FACES: the leaves joined to each leaf by a mesh edge (CSR; GRIDS: none)
+  const int* leaf_adj_off;
+  const int* leaf_adj;
   const int* leaf_verts;     // FACES: vert_indices per leaf, leaf-id order
   const int* leaf_prim_off;  // nleaf+1
   const int* leaf_prims;     // prim indices, leaf-id order

@@ -201,14 +201,16 @@ struct CullTabs {
 // pass 0's at [0, sh.split), pass 1's behind it with its vertex offsets
 // continuing from pass 0's total — when both fit the list arrays (cap
 // entries; cap 0: one sphere, bit 1 never set).  Then: lists without a
-// common leaf under a joinable tool make one list of both (sh.joint, sh.cnt
-// and sh.total over both); otherwise sh.cnt and sh.total are pass 0's and
-// sh.held counts pass 1's stored entries (-1 when they did not fit).
+// common leaf under a joinable tool (joinable 1; 2: and without a pair of
+// leaves joined by a mesh edge, for the smooth brush's rings) make one list
+// of both (sh.joint, sh.cnt and sh.total over both); otherwise sh.cnt and
+// sh.total are pass 0's and sh.held counts pass 1's stored entries (-1 when
+// they did not fit).
 template <int kBox, bool kTwoLevel, bool kPair = false, class Hit, class Tabs>
 __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb, Hit hits,
                                              unsigned char* s_pass, int* s_cl, int* s_coff,
                                              const Tabs& ct, TeamShared& sh, int cap = 0,
-                                             bool joinable = false) {
+                                             int joinable = 0) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
   // one-level search (cull_ntop 0): the second level's single range is every node
@@ -371,8 +373,31 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
         voff1 += nv;
       }
     }
+    // joinable 2: pass 1's leaves in a bitmap over the leaves (the node marks
+    // are read; their bytes hold it), then pass 0's leaves' neighbours looked up
+    bool joined = false;
+    if (joinable == 2 && both && !sh.pair_ovl) {
+      unsigned int* bits = reinterpret_cast<unsigned int*>(s_pass);
+      __syncthreads();  // the lists are written
+      for (int i = threadIdx.x; i < (L + 31) / 32; i += kTeamThreads) bits[i] = 0u;
+      __syncthreads();
+      for (int k = threadIdx.x; k < c1; k += kTeamThreads) {
+        const int leaf = s_cl[c0 + k];
+        atomicOr(&bits[leaf >> 5], 1u << (leaf & 31));
+      }
+      __syncthreads();
+      int hit = 0;
+      for (int k = threadIdx.x; k < c0 && !hit; k += kTeamThreads) {
+        const int leaf = s_cl[k];
+        for (int j = m.leaf_adj_off[leaf]; j < m.leaf_adj_off[leaf + 1] && !hit; j++) {
+          const int o = m.leaf_adj[j];
+          hit = (bits[o >> 5] >> (o & 31)) & 1u;
+        }
+      }
+      joined = __syncthreads_or(hit) != 0;
+    }
     if (threadIdx.x == 0) {
-      const bool joint = both && joinable && !sh.pair_ovl;
+      const bool joint = both && joinable != 0 && !sh.pair_ovl && !joined;
       sh.joint = joint ? 1 : 0;
       sh.split = c0;
       sh.cnt = joint ? c0 + c1 : c0;
@@ -454,7 +479,7 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char*
 template <int kBox, bool kTwoLevel, class Tabs>
 __device__ void team_cull_pair(const DevMesh& m, const PassParams& pp, const float* loc1, bool pair,
                                unsigned char* s_pass, int* s_cl, int* s_coff, const Tabs& ct,
-                               TeamShared& sh, int cap, bool joinable) {
+                               TeamShared& sh, int cap, int joinable) {
   team_cull_by<kBox, kTwoLevel, true>(
       m, pp.original ? m.orig_vb : m.vb,
       [&](float4 lo, float4 hi) {
@@ -510,11 +535,15 @@ __device__ __forceinline__ void team_list_to_front(int* s_cl, int* s_coff, TeamS
   }
 }
 
-// Tools whose sweep reads and writes only the vertex itself (and the pass's
-// frame): two passes over disjoint leaves commute and can run as one.
-__device__ __forceinline__ bool pair_tool(int tool) {
-  return tool == kToolDraw || tool == kToolInflate || tool == kToolPinch || tool == kToolCrease ||
-         tool == kToolClayStrips;
+// How two passes over disjoint leaves can run as one: 1 for the tools whose
+// sweep reads and writes only the vertex itself (and the pass's frame); 2
+// for smooth, whose hits read their one-ring (the lists must also have no
+// pair of leaves joined by a mesh edge); 0 otherwise.
+__device__ __forceinline__ int pair_tool(int tool) {
+  return (tool == kToolDraw || tool == kToolInflate || tool == kToolPinch || tool == kToolCrease ||
+          tool == kToolClayStrips)
+             ? 1
+             : tool == kToolSmooth ? 2 : 0;
 }
 
 constexpr int kFlushTab = 128;  // ancestors whose boxes stay on chip
@@ -1608,21 +1637,43 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           // the next one fills the other map.
           int* const smap = m.slot_map[q & 1];
           q++;
+          // kSym builds: a hit's slot record holds its pass in the top bit (a
+          // joint pair's hits carry their own pass's parameters, kept in
+          // shared memory with the sweep's strength)
+          auto hit_v = [](int x) { return kSym ? (x & 0x7FFFFFFF) : x; };
+          auto hit_p = [](int x) { return kSym ? static_cast<int>(static_cast<unsigned int>(x) >> 31) : 0; };
+          auto pass_of = [&](int pk) -> const PassParams& {
+            if constexpr (kSym) {
+              return sh.mpp[pk];
+            } else {
+              (void)pk;
+              return pp;
+            }
+          };
+          const int split = kSym ? sh.split : cnt;
           int* const slot_v = m.hit_list[0];
           float4* const val[2] = {m.scratch, m.scratch2};
           const int R = 32 * ((total + 32 * static_cast<int>(C) - 1) / (32 * static_cast<int>(C)));
           const int sbase = static_cast<int>(rank) * R;
-          if (threadIdx.x == 0) sh.nh = 0;
-          __syncthreads();
-          // first sweep, stage 1: distance test of this CTA's candidates
           pp.iter_strength = (count != 0) ? 1.0f : last;
           pp.iteration = 0;
+          if (threadIdx.x == 0) {
+            sh.nh = 0;
+            if constexpr (kSym)
+              for (int k = 0; k < 2; k++) {
+                sh.mpp[k].iter_strength = pp.iter_strength;
+                sh.mpp[k].iteration = 0;
+              }
+          }
+          __syncthreads();
+          // first sweep, stage 1: distance test of this CTA's candidates
           const float rr = b.radius * b.radius;
           unsigned long long ab = 0;
           constexpr int kCand = 4;
           for (int base = gt - lane; base < total; base += kCand * GT) {
             int vv[kCand];
             float4 cc[kCand];
+            unsigned int pm = 0u;  // the candidates of a joint pair's second pass
 #pragma unroll
             for (int j = 0; j < kCand; j++) {
               const int i = base + j * GT + lane;
@@ -1630,6 +1681,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
               if (i < total) {
                 const int k = smem_find_slot(s_coff, cnt, i);
                 vv[j] = leaf_vert(m, s_cl[k], i - s_coff[k]);
+                if (kSym && k >= split) pm |= 1u << j;
               }
             }
 #pragma unroll
@@ -1639,14 +1691,16 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
             for (int j = 0; j < kCand; j++) {
               if (vv[j] < 0) continue;
               ab += 16u;  // vertex id, co
-              if (!(dist_sq(cc[j], pp.loc) <= rr)) continue;
+              const int pk = static_cast<int>((pm >> j) & 1u);
+              if (!(dist_sq(cc[j], pass_of(pk).loc) <= rr)) continue;
               cg::coalesced_group g = cg::coalesced_threads();
               int h = 0;
               if (g.thread_rank() == 0) h = atomicAdd(&sh.nh, static_cast<int>(g.size()));
               h = g.shfl(h, 0) + g.thread_rank();
-              slot_v[sbase + h] = vv[j];
+              const int rec = kSym ? (vv[j] | (pk << 31)) : vv[j];
+              slot_v[sbase + h] = rec;
               if (h < kTeamThreads) {
-                sh.hv[h] = vv[j];
+                sh.hv[h] = rec;
                 sh.hco[h] = cc[j];
               }
             }
@@ -1654,23 +1708,25 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           __syncthreads();
           const int nh = sh.nh;
           // stage 2: the first sweep of the hits
-          int v0 = -1, n0 = -1;
+          int v0 = -1, n0 = -1, p0 = 0;
           float4 own = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
           for (int hb = threadIdx.x - lane; hb < nh; hb += kTeamThreads) {
             const int h = hb + lane;
             bool moved = false;
             if (h < nh) {
-              const int v = h < kTeamThreads ? sh.hv[h] : __ldcg(&slot_v[sbase + h]);
+              const int x = h < kTeamThreads ? sh.hv[h] : __ldcg(&slot_v[sbase + h]);
+              const int v = hit_v(x), pk = hit_p(x);
               const float4 co = h < kTeamThreads ? sh.hco[h] : __ldcg(&m.co[v]);
               float4 out;
               int nr = -1;
               if (h == static_cast<int>(threadIdx.x)) {
-                out = smooth_first(m, b, pp, v, co, s_nbc + threadIdx.x, kTeamThreads, &nr, moved);
+                out = smooth_first(m, b, pass_of(pk), v, co, s_nbc + threadIdx.x, kTeamThreads, &nr, moved);
                 v0 = v;
                 n0 = nr;
+                p0 = pk;
                 own = out;
               } else {
-                smooth_vertex(m, b, b.y, pp, v, co, out, moved);
+                smooth_vertex(m, b, b.y, pass_of(pk), v, co, out, moved);
               }
               val[0][sbase + h] = out;
               smap[v] = sbase + h;
@@ -1687,13 +1743,22 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           clk.mark(a, rank, kPhBrush);
           if (count == 0) {
             for (int h = threadIdx.x; h < nh; h += kTeamThreads) {
-              const int v = h == static_cast<int>(threadIdx.x) ? v0 : __ldcg(&slot_v[sbase + h]);
+              const int v = h == static_cast<int>(threadIdx.x) ? v0 : hit_v(__ldcg(&slot_v[sbase + h]));
               m.co[v] = h == static_cast<int>(threadIdx.x) ? own : __ldcg(&val[0][sbase + h]);
             }
           }
           for (int it = 1; it <= count; it++) {
             pp.iter_strength = (it != count) ? 1.0f : last;
             pp.iteration = it;
+            if constexpr (kSym) {
+              // (the last sweep's reads ended at its team barrier)
+              if (threadIdx.x == 0)
+                for (int k = 0; k < 2; k++) {
+                  sh.mpp[k].iter_strength = pp.iter_strength;
+                  sh.mpp[k].iteration = it;
+                }
+              __syncthreads();
+            }
             const float4* src = val[(it - 1) & 1];
             float4* dst = val[it & 1];
             ab = 0;
@@ -1702,13 +1767,16 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
               int v, nring;
               if (h == static_cast<int>(threadIdx.x) && n0 >= 0) {
                 if (it == 1) smooth_resolve(s_nbc + threadIdx.x, kTeamThreads, n0, smap);
-                out = smooth_slot_cached(m, b, pp, v0, own, n0, s_nbc + threadIdx.x, kTeamThreads, src);
+                out = smooth_slot_cached(m, b, pass_of(p0), v0, own, n0, s_nbc + threadIdx.x, kTeamThreads,
+                                         src);
                 v = v0;
                 nring = n0;
               } else {
                 const bool first = h == static_cast<int>(threadIdx.x);
-                v = first ? v0 : __ldcg(&slot_v[sbase + h]);
-                out = smooth_slot(m, b, pp, v, first ? own : __ldcg(&src[sbase + h]), src, smap);
+                const int x = first ? 0 : __ldcg(&slot_v[sbase + h]);
+                v = first ? v0 : hit_v(x);
+                const int pk = first ? p0 : hit_p(x);
+                out = smooth_slot(m, b, pass_of(pk), v, first ? own : __ldcg(&src[sbase + h]), src, smap);
                 nring = m.type == kFaces ? m.nb_off[v + 1] - m.nb_off[v] : 4;
               }
               if (h == static_cast<int>(threadIdx.x)) own = out;
@@ -1731,7 +1799,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           // clear this pass's map entries; the map is next filled two smooth
           // passes later, after at least one more team barrier
           for (int h = threadIdx.x; h < nh; h += kTeamThreads)
-            smap[h == static_cast<int>(threadIdx.x) ? v0 : __ldcg(&slot_v[sbase + h])] = -1;
+            smap[h == static_cast<int>(threadIdx.x) ? v0 : hit_v(__ldcg(&slot_v[sbase + h]))] = -1;
         }
       }
       // End of the dab.  FACES: refit of the touched leaves, then the flush

@@ -146,3 +146,23 @@ def test_pairs_in_cluster_batch(gpu, oracle, cluster):
         tot, _ = o.stroke(st, which=1)
         assert s.verts_displaced == tot, (k, s.verts_displaced, tot)
         _assert_equal(g, o, f"batch mesh {k}")
+
+
+@pytest.mark.parametrize("team", [16, TEAM_GRID])
+@pytest.mark.parametrize("strength", [0.2, 0.6, 0.95])
+def test_smooth_pairs(gpu, oracle, team, strength):
+    """Smooth with X symmetry: dabs far from the mirror plane pair their
+    passes (no leaf of one pass joined to a leaf of the other by an edge),
+    dabs near it run the passes in turn; strengths give no full sweep, two
+    and three."""
+    m = small_icosphere(4)
+    g, o = _pair(oracle, m, 200)
+    g.set_team(team)
+    far = _arc_near([0.7, 0.4, 0.6], 10, 0.03, seed=13)
+    near = _arc_near([0.03, 0.5, 0.86], 10, 0.03, seed=14)
+    dabs = np.concatenate([far, near, far[::-1]])
+    st = synth.Stroke(synth.TOOL_SMOOTH, 0.12, strength, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
+    s = g.stroke(st, mode=STROKE_TEAM)
+    tot, _ = o.stroke(st, which=1)
+    assert s.verts_displaced == tot and tot > 0
+    _assert_equal(g, o, f"smooth {strength} team {team}")
