@@ -399,8 +399,9 @@ int upload_pbvh(sgpu_mesh* m) {
       const bool ranged = h.depth[n] == split && h.children[n] >= 0;
       top.push_back(make_int4(n, ranged ? dlo[n] : -1, ranged ? dhi[n] : -1, 0));
     }
-    if (!two_level) top.assign(1, make_int4(0, -1, -1, 0));
-    d.cull_ntop = two_level ? static_cast<int>(top.size()) : 0;
+    const bool fits = top.size() <= static_cast<size_t>(kCullTopMax);
+    if (!two_level || !fits) top.assign(1, make_int4(0, -1, -1, 0));
+    d.cull_ntop = two_level && fits ? static_cast<int>(top.size()) : 0;
     if ((rc = m->upload(&d.cull_top, top))) return rc;
   }
   d.max_depth = h.max_depth;

@@ -59,6 +59,9 @@ inline void div_invariant_params(unsigned int d, unsigned int* mul, int* shift) 
   *mul = static_cast<unsigned int>(((1ull << *shift) + d - 1) / d);
 }
 
+// First-level entries of the two-level node search: every node down to depth 6.
+constexpr int kCullTopMax = 127;
+
 // Device view of one mesh; passed to kernels by value.
 struct DevMesh {
   int type;

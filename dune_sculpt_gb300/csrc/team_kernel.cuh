@@ -210,7 +210,7 @@ template <int kBox, bool kTwoLevel, bool kPair = false, class Hit, class Tabs>
 __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb, Hit hits,
                                              unsigned char* s_pass, int* s_cl, int* s_coff,
                                              const Tabs& ct, TeamShared& sh, int cap = 0,
-                                             int joinable = 0) {
+                                             int joinable = 0, const int4* top = nullptr) {
   const int L = m.nleaf;
   for (int i = threadIdx.x; i <= L; i += kTeamThreads) s_coff[i] = 0;
   // one-level search (cull_ntop 0): the second level's single range is every node
@@ -260,8 +260,9 @@ __device__ __forceinline__ void team_cull_by(const DevMesh& m, const float4* bb,
   } else {
   // First level: every node down to the split depth; a passing internal node
   // at the split depth lists its descendants' range for the second level.
+  const int4* tops = top ? top : m.cull_top;  // (a copy on chip, when given)
   for (int k = threadIdx.x; k < m.cull_ntop; k += kTeamThreads) {
-    const int4 e = m.cull_top[k];
+    const int4 e = tops[k];
     const float4 lo = __ldcg(&bb[2 * e.x]), hi = __ldcg(&bb[2 * e.x + 1]);
     const unsigned hit = hits(lo, hi);
     outcome(e.x, hit, m.node_leaf_lo[e.x], m.node_leaf_hi[e.x]);
@@ -466,11 +467,12 @@ __device__ __forceinline__ unsigned long long team_orig_sweep(const DevMesh& m, 
 // The node search of one pass (sphere at the pass location).
 template <int kBox, bool kTwoLevel, class Tabs>
 __device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char* s_pass,
-                          int* s_cl, int* s_coff, const Tabs& ct, TeamShared& sh) {
+                          int* s_cl, int* s_coff, const Tabs& ct, TeamShared& sh,
+                          const int4* top = nullptr) {
   team_cull_by<kBox, kTwoLevel>(
       m, pp.original ? m.orig_vb : m.vb,
       [&](float4 lo, float4 hi) { return box_hits(lo, hi, pp.loc, pp.cull_radius_sq) ? 1u : 0u; },
-      s_pass, s_cl, s_coff, ct, sh);
+      s_pass, s_cl, s_coff, ct, sh, 0, 0, top);
 }
 
 // The node searches of both passes of a single-axis symmetry in one (the
@@ -479,7 +481,7 @@ __device__ void team_cull(const DevMesh& m, const PassParams& pp, unsigned char*
 template <int kBox, bool kTwoLevel, class Tabs>
 __device__ void team_cull_pair(const DevMesh& m, const PassParams& pp, const float* loc1, bool pair,
                                unsigned char* s_pass, int* s_cl, int* s_coff, const Tabs& ct,
-                               TeamShared& sh, int cap, int joinable) {
+                               TeamShared& sh, int cap, int joinable, const int4* top) {
   team_cull_by<kBox, kTwoLevel, true>(
       m, pp.original ? m.orig_vb : m.vb,
       [&](float4 lo, float4 hi) {
@@ -487,7 +489,7 @@ __device__ void team_cull_pair(const DevMesh& m, const PassParams& pp, const flo
         if (pair && box_hits(lo, hi, loc1, pp.cull_radius_sq)) h |= 2u;
         return h;
       },
-      s_pass, s_cl, s_coff, ct, sh, pair ? cap : 0, joinable);
+      s_pass, s_cl, s_coff, ct, sh, pair ? cap : 0, joinable, top);
 }
 
 // The gather of one grab / elastic deform dab (k_cull_dab): orig_vb boxes that
@@ -495,7 +497,8 @@ __device__ void team_cull_pair(const DevMesh& m, const PassParams& pp, const flo
 template <bool kTwoLevel>
 __device__ __forceinline__ void team_cull_union(const DevMesh& m, const DabPasses& dp, float rsq,
                                              int all, unsigned char* s_pass, int* s_cl,
-                                             int* s_coff, const CullTabs& ct, TeamShared& sh) {
+                                             int* s_coff, const CullTabs& ct, TeamShared& sh,
+                                             const int4* top) {
   team_cull_by<2, kTwoLevel>(
       m, m.orig_vb,
       [&](float4 lo, float4 hi) {
@@ -503,7 +506,7 @@ __device__ __forceinline__ void team_cull_union(const DevMesh& m, const DabPasse
         for (int p = 0; p < dp.npass && !ok; p++) ok = box_hits(lo, hi, dp.loc[p], rsq);
         return ok ? 1u : 0u;
       },
-      s_pass, s_cl, s_coff, ct, sh);
+      s_pass, s_cl, s_coff, ct, sh, 0, 0, top);
 }
 
 // The second pass's list of a pair search, stored behind the first one's
@@ -1298,6 +1301,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
   __shared__ Scratch s_scr;
   Lane* s_lanes = s_scr.lanes;
   __shared__ Lane s_chunks[kTeamMaxChunks];
+  __shared__ int4 s_top[kCullTopMax];  // the node search's first level (cull_top)
   extern __shared__ __align__(16) unsigned char dyn[];
   float4* s_nbc = reinterpret_cast<float4*>(dyn);  // smooth neighbour tables
   int* s_par = reinterpret_cast<int*>(dyn + kStageBytes);
@@ -1356,6 +1360,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
       s_lnode[k] = static_cast<unsigned short>(m.leaf_node[k]);
       s_lnv[k] = leaf_nverts(m, k);
     }
+    for (int k = threadIdx.x; k < m.cull_ntop; k += kTeamThreads) s_top[k] = m.cull_top[k];
     // GRIDS work-list stamps: dab d uses epoch grid_epoch0 + d + 1
     const unsigned int grid_epoch0 = __ldcg(&w->grid_epoch);
     TEAM_SYNC();
@@ -1427,7 +1432,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         }
         __syncthreads();
         team_cull_union<kTwoLevel>(m, sh.dp, b.radius * b.radius, tool == kToolElasticDeform ? 1 : 0, s_pass,
-                        s_cl, s_coff, ct, sh);
+                        s_cl, s_coff, ct, sh, s_top);
         const int cnt = sh.cnt, total = sh.total;
         team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * cnt : 0ull);
         clk.mark(a, rank, kPhCull);
@@ -1467,7 +1472,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         pp.iter_strength = 1.0f;
         pp.iteration = 0;
         if constexpr (!kSym) {
-          team_cull<kMinBlocks == 1 ? 8 : 2, kTwoLevel>(m, pp, s_pass, s_cl, s_coff, ct, sh);
+          team_cull<kMinBlocks == 1 ? 8 : 2, kTwoLevel>(m, pp, s_pass, s_cl, s_coff, ct, sh, s_top);
           // 24 B per node box tested, 8 B per leaf emitted (counted once per team)
           team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0) ? 24ull * m.totnode + 8ull * sh.cnt : 0ull);
         } else {
@@ -1493,7 +1498,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
               sh.mpp[1] = p1;
             }
             team_cull_pair<kMinBlocks == 1 ? 8 : 2, kTwoLevel>(m, pp, loc1, pair, s_pass, s_cl, s_coff, ct,
-                                                               sh, a.max_leaves + 1, pair_tool(tool));
+                                                               sh, a.max_leaves + 1, pair_tool(tool), s_top);
             // node boxes tested once for the pass or pair, 8 B per leaf emitted
             team_bytes(a, kPhCull, (rank == 0 && threadIdx.x == 0)
                                        ? 24ull * m.totnode + 8ull * (sh.held >= 0 ? sh.cnt + sh.held : sh.cnt)
