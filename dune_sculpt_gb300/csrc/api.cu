@@ -1815,12 +1815,18 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
   if (!verts_in || !verts_out) return fail(SGPU_ERR_INVALID_ARG, "NULL host buffers");
   DevMesh& d = mesh->dev;
   int launches = 0;
+  const size_t bytes = sizeof(float4) * static_cast<size_t>(d.totvert);
+  // A page-locked, mapped output takes the changed blocks of vertices from
+  // the device; host threads copy the input into it meanwhile (as for GRIDS).
+  float4* d_out = reinterpret_cast<float4*>(mapped_host_ptr(verts_out));
+  HostCopy host_copy;
+  if (d_out && (rc = ensure_dev(&mesh->t_keep, &mesh->t_keep_cap, 4 * static_cast<size_t>(d.totvert))))
+    return rc;
+  float4* verts_dev = d_out ? reinterpret_cast<float4*>(mesh->t_keep) : d.scratch;
   auto upload = [&]() -> int {
     // host buffers in the caller's vertex order, converted on the device
-    CK(cudaMemcpyAsync(d.scratch, verts_in, sizeof(float4) * d.totvert, cudaMemcpyHostToDevice,
-                       mesh->stream),
-       "upload verts");
-    CK(launch_gather_f4(d.co, d.scratch, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
+    CK(cudaMemcpyAsync(verts_dev, verts_in, bytes, cudaMemcpyHostToDevice, mesh->stream), "upload verts");
+    CK(launch_gather_f4(d.co, verts_dev, mesh->d_n2o, d.totvert, mesh->stream), "gather kernel");
     launches++;
     if (vert_normals_in) {
       float* flat = reinterpret_cast<float*>(d.scratch2);
@@ -1830,13 +1836,23 @@ int sgpu_stroke_host(sgpu_mesh* mesh, const SGPU_Brush* brush, const SGPU_Dab* d
       CK(launch_xyz_to_f4(d.no, flat, mesh->d_n2o, d.totvert, true, mesh->stream), "gather kernel");
       launches++;
     }
+    // (after the first event and the queued copies: inside the timed call)
+    if (d_out && static_cast<const void*>(verts_out) != static_cast<const void*>(verts_in))
+      host_copy.start(verts_out, verts_in, bytes);
     return SGPU_OK;
   };
   auto download = [&]() -> int {
+    if (d_out) {
+      host_copy.join();  // before the device writes the output
+      CK(launch_vert_writeback(d_out, d.co, mesh->d_o2n, reinterpret_cast<const float4*>(mesh->t_keep),
+                               d.totvert, mesh->stream),
+         "write-back kernel");
+      launches++;
+      return SGPU_OK;
+    }
     CK(launch_gather_f4(d.scratch, d.co, mesh->d_o2n, d.totvert, mesh->stream), "gather kernel");
     launches++;
-    CK(cudaMemcpyAsync(verts_out, d.scratch, sizeof(float4) * d.totvert, cudaMemcpyDeviceToHost,
-                       mesh->stream),
+    CK(cudaMemcpyAsync(verts_out, d.scratch, bytes, cudaMemcpyDeviceToHost, mesh->stream),
        "download verts");
     return SGPU_OK;
   };

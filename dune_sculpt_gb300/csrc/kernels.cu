@@ -812,6 +812,24 @@ __global__ void k_grid_writeback(float* out3, const float4* co, const float* in3
   }
 }
 
+// The same for a FACES stroke: the caller's vertex order (co[idx[i]] is its
+// vertex i; records of 16 bytes, the MVert layout), blocks of blockDim.x
+// vertices compared bitwise with the input (in) and written whole when changed.
+__global__ void k_vert_writeback(float4* out, const float4* co, const int* idx, const float4* in, int n) {
+  for (int b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
+    const int i = b0 + threadIdx.x;
+    float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    int diff = 0;
+    if (i < n) {
+      a = co[idx[i]];
+      const float4 c = in[i];
+      diff = (__float_as_uint(a.x) != __float_as_uint(c.x)) | (__float_as_uint(a.y) != __float_as_uint(c.y)) |
+             (__float_as_uint(a.z) != __float_as_uint(c.z)) | (__float_as_uint(a.w) != __float_as_uint(c.w));
+    }
+    if (__syncthreads_or(diff) && i < n) out[i] = a;
+  }
+}
+
 static int gather_grid(int n) {
   const int g = (n + kThreads - 1) / kThreads;
   const int cap = 4 * work_grid();
@@ -833,6 +851,11 @@ cudaError_t launch_xyz_to_f4(float4* out, const float* in3, const int* idx, int 
 }
 cudaError_t launch_f4_to_xyz(float* out3, const float4* in, const int* idx, int n, cudaStream_t s) {
   k_f4_to_xyz<<<gather_grid(n), kThreads, 0, s>>>(out3, in, idx, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_vert_writeback(float4* out, const float4* co, const int* idx, const float4* in, int n,
+                                  cudaStream_t s) {
+  k_vert_writeback<<<gather_grid(n), kThreads, 0, s>>>(out, co, idx, in, n);
   return cudaGetLastError();
 }
 cudaError_t launch_grid_writeback(float* out3, const float4* co, const float* in3, int ngrids, int area,

@@ -51,6 +51,10 @@ cudaError_t launch_gather_f1(float* out, const float* in, const int* idx, int n,
 cudaError_t launch_xyz_to_f4(float4* out, const float* in3, const int* idx, int n, bool keep_w,
                              cudaStream_t s);
 cudaError_t launch_f4_to_xyz(float* out3, const float4* in, const int* idx, int n, cudaStream_t s);
+// Changed blocks of vertices (caller order through idx, bitwise against in)
+// into the mapped host output.
+cudaError_t launch_vert_writeback(float4* out, const float4* co, const int* idx, const float4* in, int n,
+                                  cudaStream_t s);
 // Changed grids' positions (bitwise against in3) into the mapped host output.
 cudaError_t launch_grid_writeback(float* out3, const float4* co, const float* in3, int ngrids, int area,
                                   cudaStream_t s);

@@ -477,7 +477,11 @@ int sgpu_batch_stroke(sgpu_mesh **meshes, int nmesh, const SGPU_Brush *brushes,
  * vert_normals_in, nullable) are copied to the device, every leaf box is
  * refit, the stroke runs (mode as in sgpu_stroke), and the positions are
  * copied back to verts_out.  stats->gpu_ms covers the copies and the kernels.
- * FACES meshes. */
+ * FACES meshes.  When verts_out is page-locked and mapped (sgpu_host_alloc),
+ * host threads copy verts_in into it while the stroke runs and the device
+ * then writes the blocks of 256 vertices that changed (bitwise, all 16 bytes
+ * of the record); verts_out may then be verts_in itself, and must not
+ * otherwise overlap it. */
 int sgpu_stroke_host(sgpu_mesh *mesh, const SGPU_Brush *brush, const SGPU_Dab *dabs, int ndabs,
                      const int *dab_tools, const SGPU_MVert *verts_in,
                      const float *vert_normals_in, SGPU_MVert *verts_out, int mode,

@@ -92,3 +92,33 @@ def test_grids_host_stroke_into_page_locked_output(gpu, in_place):
         assert bits_equal(gp.positions(), want)
     for a in {id(x): x for x in (cin, cout, nin)}.values():
         a.free()
+
+
+@pytest.mark.parametrize("in_place", [False, True])
+def test_faces_host_stroke_into_page_locked_output(gpu, in_place):
+    m = small_icosphere(5)
+    g = PBVH.build_mesh(m, 600)
+    g.set_team(TEAM_GRID)
+    g.snapshot()
+    verts0 = g.verts()
+    no0 = g.normals()
+    st = synth.Stroke(synth.TOOL_DRAW, 0.15, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X,
+                      synth.arc_dabs(13, 20, 0.04))
+    s1 = g.stroke(st, mode=STROKE_TEAM)
+    want = g.verts()
+    vin = PinnedArray(verts0.shape, verts0.dtype)
+    vout = vin if in_place else PinnedArray(verts0.shape, verts0.dtype)
+    nin = PinnedArray(no0.shape, np.float32)
+    nin.array[:] = no0
+    for rep in range(2):
+        g.restore()
+        vin.array[:] = verts0
+        if not in_place:
+            vout.array["co"] = np.float32(7.0)  # stale contents the call must replace
+        s2 = g.stroke_host(st, vin.array, vout.array, nin.array, mode=STROKE_TEAM)
+        assert s2.verts_displaced == s1.verts_displaced
+        got, ref = np.ascontiguousarray(vout.array["co"]), np.ascontiguousarray(want["co"])
+        assert bits_equal(got, ref), (rep, first_diff(got, ref))
+        assert vout.array.tobytes() == want.tobytes()
+    for a in {id(x): x for x in (vin, vout, nin)}.values():
+        a.free()
