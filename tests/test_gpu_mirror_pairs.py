@@ -166,3 +166,32 @@ def test_smooth_pairs(gpu, oracle, team, strength):
     tot, _ = o.stroke(st, which=1)
     assert s.verts_displaced == tot and tot > 0
     _assert_equal(g, o, f"smooth {strength} team {team}")
+
+
+@pytest.mark.parametrize("team", [8, TEAM_GRID])
+def test_grids_pairs(gpu, oracle, team):
+    """Multires: a stroke around the torus with X symmetry crosses the mirror
+    plane (passes in turn) and runs far from it (pairs; smooth pairs on
+    disjoint leaves alone, its neighbours being in-grid); draw, smooth and
+    inflate by turns, positions, normals, masks and boxes bit for bit."""
+    gm = synth.torus_grids(16, 6, level=4, seed=synth.SEED_BASE + 4)
+    g = PBVH.build_grids(gm, 4)
+    o = oracle.OracleMesh.grids(gm, 4)
+    o.recalc_all_normals()
+    g.set_team(team)
+    # on the ring (torus_grids: R 1, r 0.35) at tube angle 0.3: u 1.2..1.9
+    # crosses the plane x = 0, u -0.3..0.3 stays far from it
+    ring = 1.0 + 0.35 * np.cos(0.3)
+    u = np.concatenate([np.linspace(1.2, 1.9, 20), np.linspace(-0.3, 0.3, 20)])
+    pts = np.stack([ring * np.cos(u), ring * np.sin(u), np.full(u.size, 0.35 * np.sin(0.3))], 1)
+    dabs = synth._dabs_from_points(pts)
+    mixed = [synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE]
+    tools = np.array([mixed[d % 3] for d in range(dabs.shape[0])], dtype=np.int32)
+    st = synth.Stroke(synth.TOOL_DRAW, 0.12, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
+    ov = _overlaps(o, st, tools)
+    assert any(ov) and not all(ov)
+    s = g.stroke(st, mode=STROKE_TEAM, dab_tools=tools)
+    tot, _ = o.stroke(st, which=1, dab_tools=tools)
+    assert s.verts_displaced == tot
+    _assert_equal(g, o, f"grids team {team}")
+    assert bits_equal(g.mask(), o.mask())
