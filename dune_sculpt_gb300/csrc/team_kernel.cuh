@@ -1036,7 +1036,13 @@ __device__ __forceinline__ void grid_corner_owners(const DevMesh& m, int f, int 
 // a face's grids hold their own copies of the base-edge elements, which the
 // base-edge pass averages afterwards.  GRIDS positions carry w = 0.
 // The owner records of the face's corners are written while the first
-// stage is in flight (grid_corner_owners).
+// stage is in flight (grid_corner_owners); with kSplitOwners and at most
+// kTeamThreads records, one thread per record loads its corner's id before
+// the stage, the owner key and face range after it, and writes the record
+// once the face is done, so that the dependent loads overlap the normals.
+// The cluster builds and the builds that pair mirror passes keep the first
+// form: the split costs them registers.
+template <bool kSplitOwners = true>
 static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, unsigned char* stage,
                                       int group, unsigned int epoch) {
   const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area, qa = g1 * g1;
@@ -1044,6 +1050,13 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
   float* s_mk = reinterpret_cast<float*>(s_co + group * area);
   float3* s_q = reinterpret_cast<float3*>(s_mk + group * area);  // quad normals
   const bool whole = n <= group;  // the seams below read the stage
+  const bool split_owners = kSplitOwners && 2 * n <= kTeamThreads;
+  const int ot = static_cast<int>(threadIdx.x);
+  const bool oedge = ot < n;
+  const int oc = oedge ? ot : ot - n;
+  int oid = -1, of0 = 0, of1 = 0;
+  unsigned long long own = 0ull;
+  if (split_owners && ot < 2 * n) oid = oedge ? m.face_edges[s + oc] : m.face_verts[s + oc];
   for (int c0 = 0; c0 < n; c0 += group) {
     const int nc = min(group, n - c0);
     for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
@@ -1051,9 +1064,15 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
       cp_async16(&s_co[i], &m.co[e]);
       if (m.mask) cp_async4(&s_mk[i], &m.mask[e]);
     }
-    if (c0 == 0) grid_corner_owners(m, f, s, n, epoch, threadIdx.x, kTeamThreads);
+    if (c0 == 0 && !split_owners) grid_corner_owners(m, f, s, n, epoch, threadIdx.x, kTeamThreads);
     cp_async_wait_all();
     __syncthreads();
+    if (c0 == 0 && oid >= 0) {
+      own = __ldcg(oedge ? &m.edge_own[oid] : &m.bvert_own[oid]);
+      const int* off = oedge ? m.edge_off : m.bvert_off;
+      of0 = off[oid];
+      of1 = off[oid + 1];
+    }
     // each thread keeps one quad (element) position and walks the grids
     for (int q = threadIdx.x; q < qa; q += kTeamThreads) {
       const int qy = q / g1, qx = q - qy * g1;
@@ -1140,6 +1159,9 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
       }
     }
   }
+  if (oid >= 0)
+    m.corner_own[2 * (s + oc) + (oedge ? 0 : 1)] =
+        make_int2(of0, (own == grid_owner_key(epoch, f) && of1 - of0 > 1) ? of1 - of0 : 0);
   __syncthreads();  // the stage is read: the CTA's next face may restage it
 }
 
@@ -1827,7 +1849,7 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
           for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C)) {
             const int f = __ldcg(&m.face_list[fi]);
             const int2 fs = __ldcg(&m.face_info[fi]);
-            team_grid_face(m, f, fs.x, fs.y, dyn, group, epoch);
+            team_grid_face<kWide && !kSym>(m, f, fs.x, fs.y, dyn, group, epoch);
             if (threadIdx.x == 0) {
               const int n = fs.y;
               // positions read, normals written; the seam pairs and the
