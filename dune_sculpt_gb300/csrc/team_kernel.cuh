@@ -1042,8 +1042,24 @@ __device__ __forceinline__ void grid_corner_owners(const DevMesh& m, int f, int 
 // once the face is done, so that the dependent loads overlap the normals.
 // The cluster builds and the builds that pair mirror passes keep the first
 // form: the split costs them registers.
-template <bool kSplitOwners = true>
-static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, unsigned char* stage,
+// kPrefetch (with kSplitOwners): when the face's base-edge and corner items
+// (team_grid_face_boundary) fit one per thread and their tables fit the stage
+// after the grids, the records also go to shared memory after the quad
+// normals, each item's thread loads the element indices of its set during the
+// element normals, and the face returns true: the boundary phase of this face
+// on this CTA then reads the indices from boundary_prefetch(...) instead of
+// walking record -> index -> element after the team barrier.
+__host__ __device__ __forceinline__ size_t boundary_prefetch_offset(int grid_size, int group) {
+  return (face_group_bytes(grid_size, group) + 15u) & ~static_cast<size_t>(15);
+}
+// The 2n records (int2, first: 8-byte aligned), then per item the set's size
+// (0: not the owner; -1: larger than kAvgBatch, read the record) and its
+// kAvgBatch element indices.
+__host__ __device__ __forceinline__ size_t boundary_prefetch_bytes(int items, int n) {
+  return 16u * n + static_cast<size_t>(items) * 4u * (1 + kAvgBatch);
+}
+template <bool kSplitOwners = true, bool kPrefetch = false>
+static __device__ bool team_grid_face(const DevMesh& m, int f, int s, int n, unsigned char* stage,
                                       int group, unsigned int epoch) {
   const int gs = m.grid_size, g1 = gs - 1, area = m.grid_area, qa = g1 * g1;
   float4* s_co = reinterpret_cast<float4*>(stage);
@@ -1057,6 +1073,15 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
   int oid = -1, of0 = 0, of1 = 0;
   unsigned long long own = 0ull;
   if (split_owners && ot < 2 * n) oid = oedge ? m.face_edges[s + oc] : m.face_verts[s + oc];
+  const int g2 = 2 * gs, per_corner = g2 - 1, items = n * per_corner;
+  const size_t pre_off = boundary_prefetch_offset(gs, group);
+  const bool pre = kPrefetch && split_owners && whole && items <= kTeamThreads &&
+                   pre_off + boundary_prefetch_bytes(items, n) <= kStageBytes;
+  int2* p_rec = reinterpret_cast<int2*>(stage + pre_off);
+  int* p_cnt = reinterpret_cast<int*>(p_rec + 2 * n);
+  int* p_idx = p_cnt + items;
+  int pidx[kAvgBatch];
+  int pcnt = 0;
   for (int c0 = 0; c0 < n; c0 += group) {
     const int nc = min(group, n - c0);
     for (int i = threadIdx.x; i < nc * area; i += kTeamThreads) {
@@ -1083,13 +1108,30 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
                                       xyz(p[qy * gs + qx + 1]), xyz(p[qy * gs + qx]));
       }
     }
+    if (pre && oid >= 0)
+      p_rec[ot] = make_int2(of0, (own == grid_owner_key(epoch, f) && of1 - of0 > 1) ? of1 - of0 : 0);
     __syncthreads();
+    if (pre && ot < items) {
+      const int c = ot / per_corner, j = ot - c * per_corner;
+      const bool edge = j < g2 - 2;
+      const int2 r = p_rec[edge ? c : n + c];
+      pcnt = r.y > kAvgBatch ? -1 : r.y;
+#pragma unroll
+      for (int k = 0; k < kAvgBatch; k++)
+        if (k < pcnt) pidx[k] = edge ? m.edge_elems[(long long)(r.x + k) * g2 + j + 1] : m.bvert_elems[r.x + k];
+    }
     for (int e = threadIdx.x; e < area; e += kTeamThreads) {
       const int y = e / gs, x = e - y * gs;
       for (int c = 0; c < nc; c++) {
         const float3 nv = staged_normal_at(s_q, c, x, y, g1);
         m.no[static_cast<size_t>(s + c0 + c) * area + e] = make_float4(nv.x, nv.y, nv.z, 0.0f);
       }
+    }
+    if (pre && ot < items) {
+      p_cnt[ot] = pcnt;
+#pragma unroll
+      for (int k = 0; k < kAvgBatch; k++)
+        if (k < pcnt) p_idx[kAvgBatch * ot + k] = pidx[k];
     }
     __syncthreads();  // a next group restages after this barrier
   }
@@ -1163,6 +1205,7 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
     m.corner_own[2 * (s + oc) + (oedge ? 0 : 1)] =
         make_int2(of0, (own == grid_owner_key(epoch, f) && of1 - of0 > 1) ? of1 - of0 : 0);
   __syncthreads();  // the stage is read: the CTA's next face may restage it
+  return pre;
 }
 
 // Base edges and corners of one claimed face by one CTA: each base edge and
@@ -1171,14 +1214,27 @@ static __device__ void team_grid_face(const DevMesh& m, int f, int s, int n, uns
 // records (the face went through team_grid_face this dab) the owner
 // decisions are read from corner_own; without (the unstaged path) they are
 // made here first, one thread per corner record.
+// pre: the tables team_grid_face<true, true> left for this face (null when
+// it left none; records first, then the item tables).
 static __device__ void team_grid_face_boundary(const DevMesh& m, int f, int s, int n,
-                                               unsigned int epoch, bool records) {
+                                               unsigned int epoch, bool records,
+                                               const unsigned char* pre = nullptr) {
   const int g2 = 2 * m.grid_size, per_corner = g2 - 1;
   if (!records) {
     grid_corner_owners(m, f, s, n, epoch, threadIdx.x, kTeamThreads);
     __syncthreads();  // the CTA's own records (global memory, CTA barrier)
   }
   for (int it = threadIdx.x; it < n * per_corner; it += kTeamThreads) {
+    if (pre) {
+      const int* p_cnt = reinterpret_cast<const int*>(pre + 16 * n);
+      const int cnt = p_cnt[it];
+      if (cnt == 0) continue;
+      if (cnt > 0) {
+        const int* idx = p_cnt + n * per_corner + kAvgBatch * it;
+        grid_average_set(m, cnt, [&](int k) { return idx[k]; });
+        continue;
+      }
+    }
     const int c = it / per_corner, j = it - c * per_corner;
     if (j < g2 - 2) {
       const int2 e = __ldcg(&m.corner_own[2 * (s + c)]);
@@ -1845,11 +1901,14 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         // the refit below follows).
         const int nf = __ldcg(&m.grid_counts[0]);
         const int group = face_grid_group(m.grid_size, kStageBytes);
+        int pre_fi = -1;  // the face whose boundary item tables the stage holds
         if (group > 0) {
           for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C)) {
             const int f = __ldcg(&m.face_list[fi]);
             const int2 fs = __ldcg(&m.face_info[fi]);
-            team_grid_face<kWide && !kSym>(m, f, fs.x, fs.y, dyn, group, epoch);
+            pre_fi = team_grid_face<kWide && !kSym, kWide && !kSym>(m, f, fs.x, fs.y, dyn, group, epoch)
+                         ? fi
+                         : -1;
             if (threadIdx.x == 0) {
               const int n = fs.y;
               // positions read, normals written; the seam pairs and the
@@ -1880,7 +1939,9 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_team_stroke(TeamAr
         for (int fi = static_cast<int>(rank); fi < nf; fi += static_cast<int>(C))
           {
             const int2 fs = __ldcg(&m.face_info[fi]);
-            team_grid_face_boundary(m, __ldcg(&m.face_list[fi]), fs.x, fs.y, epoch, group > 0);
+            team_grid_face_boundary(
+                m, __ldcg(&m.face_list[fi]), fs.x, fs.y, epoch, group > 0,
+                fi == pre_fi ? dyn + boundary_prefetch_offset(m.grid_size, group) : nullptr);
           }
         TEAM_SYNC();
         clk.mark(a, rank, kPhGridSeams);
