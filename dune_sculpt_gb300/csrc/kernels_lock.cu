@@ -718,12 +718,16 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_lock_stroke(TeamAr
       const int NF = lock_prefix(J, s_P, sh.scan, [&](int j) {
         return in_dab(j) && mesh_of(j).type == kGrids ? __ldcg(&mesh_of(j).grid_counts[0]) : 0;
       });
+      int pre_it = -1;  // the face whose boundary item tables the stage holds
       for (int it = static_cast<int>(rank); it < NF; it += static_cast<int>(C)) {
         const int j = find_job(it);
         const DevMesh& m = mesh_of(j);
         const int2 fs = __ldcg(&m.face_info[it - s_P[j]]);
-        team_grid_face(m, __ldcg(&m.face_list[it - s_P[j]]), fs.x, fs.y, dyn,
-                       face_grid_group(m.grid_size, kStageBytes), s_ep0[j] + d + 1u);
+        pre_it = team_grid_face<true, true>(m, __ldcg(&m.face_list[it - s_P[j]]), fs.x, fs.y, dyn,
+                                            face_grid_group(m.grid_size, kStageBytes),
+                                            s_ep0[j] + d + 1u)
+                     ? it
+                     : -1;
       }
       clk.mark(a, rank, kPhGridFaces);
       LOCK_SYNC();
@@ -731,8 +735,11 @@ __global__ void __launch_bounds__(kTeamThreads, kMinBlocks) k_lock_stroke(TeamAr
         const int j = find_job(it);
         const DevMesh& m = mesh_of(j);
         const int2 fs = __ldcg(&m.face_info[it - s_P[j]]);
-        team_grid_face_boundary(m, __ldcg(&m.face_list[it - s_P[j]]), fs.x, fs.y, s_ep0[j] + d + 1u,
-                                true);
+        team_grid_face_boundary(
+            m, __ldcg(&m.face_list[it - s_P[j]]), fs.x, fs.y, s_ep0[j] + d + 1u, true,
+            it == pre_it
+                ? dyn + boundary_prefetch_offset(m.grid_size, face_grid_group(m.grid_size, kStageBytes))
+                : nullptr);
       }
       clk.mark(a, rank, kPhGridSeams);
       LOCK_SYNC();
