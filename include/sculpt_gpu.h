@@ -543,8 +543,8 @@ int sgpu_host_free(void *ptr);
  * The Jacobi scratch is a fixed device array of SGPU_NOALLOC_MAX_VERTS float4
  * (1 MiB) that every GPU loading the library holds until exit; nverts above
  * that returns SGPU_ERR_INVALID_ARG.  The first call on a device looks up the
- * array's device address (again after a device reset), so make it before any
- * stream capture: a call with nverts = 0 at set-up does only that, and with
+ * array's device address (again after a device reset): a call with
+ * nverts = 0 at set-up does only that, and with
  * lazy module loading (the CUDA default) it also makes the driver load the
  * module that holds the array, so that no later call loads it inside a fixed
  * memory budget (CUDA_MODULE_LOADING=EAGER loads it with the library).  All
