@@ -353,7 +353,7 @@ class GridsMesh:
 
     @property
     def num_grids(self) -> int:
-        return int(self.face_start.shape[0] * 4)
+        return int(self.face_ngrids.sum())
 
     @property
     def num_faces(self) -> int:
@@ -402,6 +402,68 @@ def torus_grids(nu: int, nv: int, level: int = 5, seed: int = SEED_BASE + 4,
                      face_ngrids=np.full(F, 4, dtype=np.int32), face_verts=face_verts,
                      face_edges=face_edges, edge_verts=edge_verts, num_base_verts=nu * nv,
                      name=f"torus{nu}x{nv}_L{level}")
+
+
+def polygon_grids(co: np.ndarray, polys: list, level: int = 4, seed: int = SEED_BASE + 11,
+                  amp: float = 0.01) -> GridsMesh:
+    """Multires grids over any closed polygon base mesh: one grid per face
+    corner, element (0, 0) at the face centre, (gs-1, 0) at the midpoint of
+    the edge from this corner to the next, (0, gs-1) at the midpoint of the
+    edge from the previous corner, (gs-1, gs-1) at the corner (the layout of
+    torus_grids); positions bilinear over that quad, displaced along the
+    radial direction by seeded noise, with a seeded noise mask."""
+    co = np.asarray(co, dtype=np.float64)
+    gs = (1 << (level - 1)) + 1
+    edges: dict = {}
+    face_start, face_ngrids, face_verts, face_edges = [], [], [], []
+    pos = []
+    t = np.arange(gs, dtype=np.float64) / (gs - 1)
+    uu, ww = np.meshgrid(t, t, indexing="xy")  # [y, x]: u along x, w along y
+    uu = uu.reshape(-1, 1)
+    ww = ww.reshape(-1, 1)
+    g = 0
+    for poly in polys:
+        n = len(poly)
+        face_start.append(g)
+        face_ngrids.append(n)
+        centre = co[list(poly)].mean(axis=0)
+        for c in range(n):
+            a_, b_ = int(poly[c]), int(poly[(c + 1) % n])
+            key = (min(a_, b_), max(a_, b_))
+            if key not in edges:
+                edges[key] = len(edges)
+            face_verts.append(a_)
+            face_edges.append(edges[key])
+            m_next = 0.5 * (co[a_] + co[b_])
+            m_prev = 0.5 * (co[int(poly[c - 1])] + co[a_])
+            pos.append((1 - uu) * (1 - ww) * centre + uu * (1 - ww) * m_next + uu * ww * co[a_]
+                       + (1 - uu) * ww * m_prev)
+            g += 1
+    pos = np.concatenate(pos, axis=0)
+    radial = pos / np.linalg.norm(pos, axis=1, keepdims=True)
+    pos = pos + radial * (amp * (value_noise(seed, 5, pos, 3.0) - 0.5))[:, None]
+    mask = np.clip(1.5 * value_noise(seed, 6, pos, 2.0) - 0.25, 0.0, 1.0)
+    edge_verts = np.zeros((len(edges), 2), dtype=np.int32)
+    for (a_, b_), e in edges.items():
+        edge_verts[e] = (a_, b_)
+    return GridsMesh(grid_size=gs, co=_f32(pos), mask=_f32(mask),
+                     face_start=np.asarray(face_start, dtype=np.int32),
+                     face_ngrids=np.asarray(face_ngrids, dtype=np.int32),
+                     face_verts=np.asarray(face_verts, dtype=np.int32),
+                     face_edges=np.asarray(face_edges, dtype=np.int32), edge_verts=edge_verts,
+                     num_base_verts=int(co.shape[0]), name=f"polygons{len(polys)}_L{level}")
+
+
+def pentagonal_prism() -> tuple[np.ndarray, list]:
+    """Closed prism over a regular pentagon: 2 pentagons and 5 quads, every
+    vertex joining three faces."""
+    ang = 2.0 * np.pi * np.arange(5) / 5.0
+    ring = np.stack([np.cos(ang), np.sin(ang)], 1)
+    co = np.concatenate([np.concatenate([ring, np.full((5, 1), -0.6)], 1),
+                         np.concatenate([ring, np.full((5, 1), 0.6)], 1)], 0)
+    polys = [[4, 3, 2, 1, 0], [5, 6, 7, 8, 9]]
+    polys += [[i, (i + 1) % 5, 5 + (i + 1) % 5, 5 + i] for i in range(5)]
+    return co, polys
 
 
 def torus_dabs(seed: int, n: int, radius: float, R: float = 1.0, r: float = 0.35) -> np.ndarray:

@@ -352,6 +352,65 @@ def test_grids_stroke_replay_in_reference(oracle):
     assert moved > 0
 
 
+def _polygon_base(name):
+    if name == "icosahedron":  # triangles; every base vertex joins five faces
+        co, tris = synth.icosphere(0)
+        return co, [list(t) for t in tris]
+    return synth.pentagonal_prism()  # pentagons and quads; three faces a vertex
+
+
+@pytest.mark.parametrize("base", ["icosahedron", "pentagonal_prism"])
+def test_grids_polygon_base_match_reference(oracle, base):
+    """Multires grids over triangles and pentagons, base vertices joining three
+    or five faces (the tori elsewhere have quads and four): the full normal
+    update with seam stitching, then a mixed X-mirrored stroke with the
+    reference's normal update and refit after every dab, bit for bit."""
+    co, polys = _polygon_base(base)
+    g = synth.polygon_grids(co, polys, 4)
+    # 4 grids of 9x9 a leaf: the oracle counts grids, the reference elements
+    o = oracle.OracleMesh.grids(g, 4)
+    r = pyrefpin.RefGrids(g, np.zeros_like(g.co), 4 * 81)
+    assert o.num_nodes == r.num_nodes > 1
+    o.recalc_all_normals()
+    for n in np.nonzero(o.nodes()["flag"] & LEAF)[0]:
+        r.node_mark_update(int(n))
+    r.update_normals()
+    _assert_same_grids(o, r, "full update")
+    # seam elements computed from two grids' bilinear maps can differ by an
+    # ulp, so the stitching moves them: a second update of every leaf and a
+    # refit in both before the stroke
+    for n in np.nonzero(o.nodes()["flag"] & LEAF)[0]:
+        o.node_mark_update(int(n))
+        r.node_mark_update(int(n))
+    o.update_normals()
+    r.update_normals()
+    _assert_same_grids(o, r, "second update")
+    o.update_bounds(UPD_BB)
+    r.update_bounds(UPD_BB)
+    assert bits_equal(o.bbs()[0], r.bbs()[0])
+    dabs = synth.arc_dabs(synth.SEED_BASE + 11, 12, 0.25, 0.85)
+    tools = (synth.TOOL_DRAW, synth.TOOL_SMOOTH, synth.TOOL_INFLATE)
+    moved = 0
+    for d in range(dabs.shape[0]):
+        st = synth.Stroke(tools[d % 3], 0.3, 0.6, synth.CURVE_SMOOTH, synth.SYMM_X, dabs)
+        rsq = np.float32(0.3) * np.float32(0.3)
+        for p in (0, 1):
+            sgn = np.array([-1 if p & 1 else 1, 1, 1], np.float32)
+            nodes = o.search_sphere(dabs[d, :3] * sgn, rsq, 0)
+            n, _ = o.brush_pass(st, dabs[d, :3] * sgn, dabs[d, 3:] * sgn, nodes)
+            moved += n
+            for nd in nodes:
+                r.node_mark_update(int(nd))
+        r.set(o.co(), o.mask())
+        o.update_normals()
+        r.update_normals()
+        _assert_same_grids(o, r, f"dab {d}")
+        o.update_bounds(UPD_BB)
+        r.update_bounds(UPD_BB)
+        assert bits_equal(o.bbs()[0], r.bbs()[0]), d
+    assert moved > 0
+
+
 def _rays(rng, n, center, radius):
     """Rays from a sphere around the mesh towards points near its middle; every
     seventh one axis-aligned (exercises the 1/0 slabs of the box test)."""
